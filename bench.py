@@ -1,0 +1,347 @@
+#!/usr/bin/env python3
+"""Benchmark: RPY mobility apply, pair-interactions/sec, on GB300.
+
+Workload (the RPY apply microbenchmark): N blobs of radius a = 1 placed
+uniformly in a cube sized for volume fraction 0.05, rejection below
+separation 2.2a; forces and torques i.i.d. N(0,1) per component; the 6-dof
+segment formula (Mss_mult, cuda_functions.cu:246-425) over all N x N pairs,
+self pair included.  One step = one full apply.  Default N = 131072.
+
+  value      pair-interactions/s with inputs resident in HBM (C-ABI call on
+             device arrays: gmi_Mss_mult), FP32C precision by default
+  e2e        the same metric through gmi_Mss_mult with host buffers: the
+             pinned host->device copy of X and F and the device->host copy of
+             V are inside every timed step
+  roofline   compute bound on the FP32 (or FP64) FMA pipe: algorithmic FLOPs
+             (87 per pair) / apply time, against the pipe peak measured on
+             this GPU by gmi_measure_fma_peak
+  cpu_baseline the FP64 CPU oracle (rpy_oracle.c) on a bounded target slice,
+             all host cores
+
+Runs one replica per GPU under torchrun (the apply does not shard here:
+"replicas only"), max-over-ranks time, rank 0 prints one JSON line.
+``--impl reference`` times the reference algorithm's CPU restatement instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FLOP_PER_PAIR_SS = 87  # canonical algorithmic FLOPs per segment-segment pair (FMA = 2)
+METRIC = "RPY pair-interactions/sec"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gmi", "reference"], default="gmi")
+    p.add_argument("--n", type=int, default=131072)
+    p.add_argument("--precision", choices=["fp32c", "fp64"], default="fp32c")
+    p.add_argument("--no-fp64", action="store_true", help="skip the FP64 side measurement")
+    p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU sample")
+    return p.parse_args()
+
+
+# --------------------------------------------------------------------------
+# distributed plumbing (replicas only; the collective is for timing)
+# --------------------------------------------------------------------------
+def dist_setup(args):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# --------------------------------------------------------------------------
+# workload
+# --------------------------------------------------------------------------
+def make_inputs(n: int, seed: int = 2026):
+    from generic_mobility_interface_class_gb300 import seeding
+    x = seeding.random_cube(n, min_sep=2.2, phi=0.05, a=1.0, seed=seed)
+    f = np.random.default_rng(seed + 1).normal(size=(n, 6))
+    return x, f
+
+
+def cpu_sample(x, f, seconds: float):
+    """FP64 CPU oracle on a target slice sized for ~`seconds` of work."""
+    from oracle import rpy
+    n = x.shape[0]
+    probe = min(n, 256)
+    t0 = time.perf_counter()
+    rpy.mss(x, f, targets=(0, probe))
+    dt = max(time.perf_counter() - t0, 1e-6)
+    nt = int(min(n, max(probe, probe * seconds / dt)))
+    t0 = time.perf_counter()
+    rpy.mss(x, f, targets=(0, nt))
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return nt, dt, cores
+
+
+def run_reference(args, world, rank):
+    """Reference arm: the reference algorithm on the host cores (the oracle
+    port of cuda_functions.cu's Mss_mult; the reference's own build cannot
+    run on this host), bounded target slice per step."""
+    if rank != 0:
+        return
+    from oracle import rpy
+    rpy.build(with_reference=False)
+    x, f = make_inputs(args.n)
+    n = x.shape[0]
+    nt, dt, cores = cpu_sample(x, f, max(1.0, min(args.cpu_seconds, 60.0) / max(args.steps, 1)))
+    for _ in range(args.warmup):
+        rpy.mss(x, f, targets=(0, min(nt, 64)))
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        rpy.mss(x, f, targets=(0, nt))
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = nt * n * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"RPY apply microbenchmark, N={n} (cube, phi=0.05, min sep 2.2a, 6-dof Mss)",
+                   "n": n, "sample_targets": nt, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
+                         "sample": f"{nt} targets x {n} sources per step"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gmi(args, world, rank, local):
+    import torch
+    from generic_mobility_interface_class_gb300 import build as gbuild
+    from generic_mobility_interface_class_gb300.mobility import Context
+    from generic_mobility_interface_class_gb300._lib import GMI_FP32C, GMI_FP64
+
+    gbuild.build()
+    dev = local if torch.cuda.device_count() > 1 else 0
+    torch.cuda.set_device(dev)
+    prec = GMI_FP32C if args.precision == "fp32c" else GMI_FP64
+    x, f = make_inputs(args.n, seed=2026 + rank)
+    n = x.shape[0]
+    pairs = float(n) * n
+    stream = torch.cuda.current_stream()
+    ctx = Context(dev, prec, stream)
+    xd = torch.as_tensor(x, device="cuda")
+    fd = torch.as_tensor(f, device="cuda")
+    vd = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+    l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
+
+    ctx.autotune(0, n, n)
+    for _ in range(args.warmup):
+        ctx.mss(xd, fd, out=vd)
+    ctx.synchronize()
+
+    # ---- device-resident timed region -------------------------------------
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = ctx.launches
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clocks:
+        w0 = time.perf_counter()
+        for s in range(args.steps):
+            l2_flush.zero_()
+            ev[s][0].record(stream)
+            ctx.mss(xd, fd, out=vd)
+            ev[s][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+    barrier(world)
+    ctx.synchronize()
+    gpu_launches = ctx.launches - launches0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_dev = max_over_ranks(sum(step_ms) / 1e3, world)
+    value = world * pairs * args.steps / t_dev
+    ms_per_step = 1e3 * t_dev / args.steps
+
+    # ---- end to end through the C ABI with host buffers ----------------------
+    xh = torch.as_tensor(x).pin_memory()
+    fh = torch.as_tensor(f).pin_memory()
+    vh = torch.empty((n, 6), dtype=torch.float64).pin_memory()
+    for _ in range(2):
+        xd.copy_(xh, non_blocking=True)
+        fd.copy_(fh, non_blocking=True)
+        ctx.mss(xd, fd, out=vd)
+        vh.copy_(vd, non_blocking=True)
+    torch.cuda.synchronize()
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        xd.copy_(xh, non_blocking=True)
+        fd.copy_(fh, non_blocking=True)
+        ctx.mss(xd, fd, out=vd)
+        vh.copy_(vd, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
+    e2e_value = world * pairs * args.steps / t_e2e
+
+    # ---- accuracy of this precision against the FP64 path ------------------
+    extra = {}
+    v_main = vd.clone()
+    if not args.no_fp64:
+        ctx.set_precision(GMI_FP64)
+        ctx.mss(xd, fd, out=vd)  # warm
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.mss(xd, fd, out=vd)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t64 = a.elapsed_time(b) / 1e3
+        v64 = vd.clone()
+        ctx.set_precision(prec)
+        d = (v_main - v64)
+        per_t = torch.linalg.norm(d, dim=1) / torch.linalg.norm(v64, dim=1)
+        extra["fp64_path"] = {"value": pairs / t64, "unit": "pairs/s", "ms_per_step": 1e3 * t64}
+        extra["error_vs_fp64"] = {
+            "max_rel_per_target": float(per_t.max()), "rms_rel_per_target": float(torch.sqrt((per_t ** 2).mean())),
+            "global_rel": float(torch.linalg.norm(d) / torch.linalg.norm(v64))}
+        extra["speedup_vs_fp64_path"] = (pairs / (ms_per_step / 1e3)) / (pairs / t64)
+
+    peak = ctx.fma_peak(prec)
+    achieved = FLOP_PER_PAIR_SS * pairs / (ms_per_step / 1e3)
+    roofline = {"bound": "fp32" if prec == GMI_FP32C else "fp64",
+                "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None,
+                "peak_source": "measured FMA-loop probe on this GPU (gmi_measure_fma_peak)",
+                "flops_per_pair": FLOP_PER_PAIR_SS}
+    ctx.close()
+
+    line = None
+    if rank == 0:
+        cpu = None
+        try:
+            from oracle import rpy
+            rpy.build(with_reference=False)
+            nt, dt, cores = cpu_sample(x, f, args.cpu_seconds)
+            cpu = {"value": nt * n / dt, "unit": "pairs/s", "cores": cores, "kind": "port",
+                   "sample": f"FP64 oracle, {nt} targets x {n} sources ({dt:.1f} s), OpenMP over targets"}
+        except Exception as e:  # the baseline is reported, never the measured path
+            cpu = {"value": None, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {e}"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32c" if prec == GMI_FP32C else "f64", "data": "synthetic",
+            "config": {"workload": f"RPY apply microbenchmark, N={n} blobs (cube, phi=0.05, min sep 2.2a, "
+                                   f"f,tau ~ N(0,1), 6-dof Mss formula, all pairs incl. self)",
+                       "n": n, "precision": args.precision, "parallelism": f"replicas x{world}",
+                       "l2": "flushed (256 MB write) between timed steps"},
+            "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(n * 9 * 8),
+                    "d2h_bytes_per_step": int(n * 6 * 8), "path": "gmi_Mss_mult with pinned host X,F -> V"},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clocks.summary(),
+            "gpu_launches": gpu_launches,
+            "wall_s_timed_region": wall,
+        }
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gmi(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

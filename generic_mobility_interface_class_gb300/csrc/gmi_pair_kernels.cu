@@ -1,0 +1,676 @@
+// gmi_pair_kernels.cu -- the O(N^2) RPY pair sums on sm_103a.
+//
+// Data path of one apply (all on the context stream):
+//   1. pack: the reference's AoS FP64 arrays (X[3n], F[3n|6n]) become
+//      12-scalar records per particle.  FP32C records hold the position as a
+//      double-float (hi, lo) pair so differences keep ~FP64 accuracy:
+//        [xh yh zh fx] [xl yl zl fy] [fz tx ty tz]
+//      FP64 records:  [x y z fx fy fz tx ty tz 0 0 0]
+//   2. pair kernel: each CTA owns TPB*TT targets and one contiguous slice
+//      ("split") of the sources.  Source tiles of kTile records are staged
+//      into shared memory by TMA (cp.async.bulk.tensor.2d, one elected
+//      thread, kStages-deep ring of mbarriers); every thread then walks the
+//      tile (broadcast reads, no bank conflicts) for its TT targets.  FP32C
+//      accumulates each tile in plain FP32 and folds the tile sum into a
+//      (hi, lo) two-sum accumulator, so the error does not grow with N.
+//   3. with more than one split, per-split partial sums (FP64) go to scratch
+//      and a reduce kernel adds them in split order into the output (= or +=).
+#include <cstdio>
+#include <vector>
+
+#include "gmi_context.hpp"
+#include "gmi_pairs.cuh"
+#include "gmi_pair_kernels.hpp"
+
+namespace gmi {
+
+constexpr int kRecLen = 12;
+constexpr int kTile = 128;   // sources per TMA box (box rows <= 256)
+constexpr int kStages = 4;   // depth of the shared-memory ring
+
+// ---------------------------------------------------------------------------
+// 1. pack kernels
+// ---------------------------------------------------------------------------
+__global__ void pack_records_f32(const double *__restrict__ x, const double *__restrict__ f, int nf, int n,
+                                 float4 *__restrict__ rec)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double px = x[3 * i], py = x[3 * i + 1], pz = x[3 * i + 2];
+    const float hx = (float)px, hy = (float)py, hz = (float)pz;
+    const float lx = (float)(px - (double)hx), ly = (float)(py - (double)hy), lz = (float)(pz - (double)hz);
+    float f0 = 0.f, f1 = 0.f, f2 = 0.f, t0 = 0.f, t1 = 0.f, t2 = 0.f;
+    if (f != nullptr) {
+        f0 = (float)f[nf * i];
+        f1 = (float)f[nf * i + 1];
+        f2 = (float)f[nf * i + 2];
+        if (nf == 6) {
+            t0 = (float)f[6 * i + 3];
+            t1 = (float)f[6 * i + 4];
+            t2 = (float)f[6 * i + 5];
+        }
+    }
+    float4 *r = rec + 3 * (size_t)i;
+    r[0] = make_float4(hx, hy, hz, f0);
+    r[1] = make_float4(lx, ly, lz, f1);
+    r[2] = make_float4(f2, t0, t1, t2);
+}
+
+__global__ void pack_records_f64(const double *__restrict__ x, const double *__restrict__ f, int nf, int n,
+                                 double2 *__restrict__ rec)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double f0 = 0, f1 = 0, f2 = 0, t0 = 0, t1 = 0, t2 = 0;
+    if (f != nullptr) {
+        f0 = f[nf * i];
+        f1 = f[nf * i + 1];
+        f2 = f[nf * i + 2];
+        if (nf == 6) {
+            t0 = f[6 * i + 3];
+            t1 = f[6 * i + 4];
+            t2 = f[6 * i + 5];
+        }
+    }
+    double2 *r = rec + 6 * (size_t)i;
+    r[0] = make_double2(x[3 * i], x[3 * i + 1]);
+    r[1] = make_double2(x[3 * i + 2], f0);
+    r[2] = make_double2(f1, f2);
+    r[3] = make_double2(t0, t1);
+    r[4] = make_double2(t2, 0.0);
+    r[5] = make_double2(0.0, 0.0);
+}
+
+// ---------------------------------------------------------------------------
+// record access
+// ---------------------------------------------------------------------------
+template <class R> struct Pos {
+    R x, y, z, lx, ly, lz;
+};
+
+// Source record from shared memory: position and the 6 load components.
+__device__ __forceinline__ void load_src(const float *p, Pos<float> &s, float *F)
+{
+    const float4 a = reinterpret_cast<const float4 *>(p)[0];
+    const float4 b = reinterpret_cast<const float4 *>(p)[1];
+    const float4 c = reinterpret_cast<const float4 *>(p)[2];
+    s.x = a.x; s.y = a.y; s.z = a.z; s.lx = b.x; s.ly = b.y; s.lz = b.z;
+    F[0] = a.w; F[1] = b.w; F[2] = c.x; F[3] = c.y; F[4] = c.z; F[5] = c.w;
+}
+__device__ __forceinline__ void load_src(const double *p, Pos<double> &s, double *F)
+{
+    const double2 a = reinterpret_cast<const double2 *>(p)[0];
+    const double2 b = reinterpret_cast<const double2 *>(p)[1];
+    const double2 c = reinterpret_cast<const double2 *>(p)[2];
+    const double2 d = reinterpret_cast<const double2 *>(p)[3];
+    const double2 e = reinterpret_cast<const double2 *>(p)[4];
+    s.x = a.x; s.y = a.y; s.z = b.x; s.lx = s.ly = s.lz = 0.0;
+    F[0] = b.y; F[1] = c.x; F[2] = c.y; F[3] = d.x; F[4] = d.y; F[5] = e.x;
+}
+__device__ __forceinline__ Pos<float> load_tgt(const float *rec, int i)
+{
+    const float4 a = reinterpret_cast<const float4 *>(rec)[3 * (size_t)i];
+    const float4 b = reinterpret_cast<const float4 *>(rec)[3 * (size_t)i + 1];
+    return Pos<float>{a.x, a.y, a.z, b.x, b.y, b.z};
+}
+__device__ __forceinline__ Pos<double> load_tgt(const double *rec, int i)
+{
+    const double2 a = reinterpret_cast<const double2 *>(rec)[6 * (size_t)i];
+    const double2 b = reinterpret_cast<const double2 *>(rec)[6 * (size_t)i + 1];
+    return Pos<double>{a.x, a.y, b.x, 0.0, 0.0, 0.0};
+}
+
+// d = x_i - x_j with the low words folded in (they are zero for FP64).
+template <class R> __device__ __forceinline__ R diff(R hi_i, R hi_j, R lo_i, R lo_j)
+{
+    return (hi_i - hi_j) + (lo_i - lo_j);
+}
+template <> __device__ __forceinline__ double diff<double>(double hi_i, double hi_j, double, double)
+{
+    return hi_i - hi_j;
+}
+
+// Per-target accumulator.  FP32: tile sum + (hi, lo) compensated total.
+template <class R, int NOUT> struct Acc;
+template <int NOUT> struct Acc<double, NOUT> {
+    double t[NOUT];
+    __device__ void zero() {
+#pragma unroll
+        for (int c = 0; c < NOUT; ++c) t[c] = 0.0;
+    }
+    __device__ void fold() {}
+    __device__ double total(int c) const { return t[c]; }
+};
+template <int NOUT> struct Acc<float, NOUT> {
+    float t[NOUT], hi[NOUT], lo[NOUT];
+    __device__ void zero() {
+#pragma unroll
+        for (int c = 0; c < NOUT; ++c) t[c] = hi[c] = lo[c] = 0.f;
+    }
+    // Knuth two-sum of the tile sum into the running total.
+    __device__ void fold() {
+#pragma unroll
+        for (int c = 0; c < NOUT; ++c) {
+            const float s = hi[c] + t[c];
+            const float bp = s - hi[c];
+            const float e = (hi[c] - (s - bp)) + (t[c] - bp);
+            hi[c] = s;
+            lo[c] += e;
+            t[c] = 0.f;
+        }
+    }
+    __device__ double total(int c) const { return (double)hi[c] + (double)lo[c]; }
+};
+
+template <int KIND> struct KindTraits;
+template <> struct KindTraits<kSS> { static constexpr int nout = 6; };
+template <> struct KindTraits<kSSWall> { static constexpr int nout = 6; };
+template <> struct KindTraits<kBB> { static constexpr int nout = 3; };
+template <> struct KindTraits<kSB> { static constexpr int nout = 6; };
+template <> struct KindTraits<kBS> { static constexpr int nout = 3; };
+
+// ---------------------------------------------------------------------------
+// 2. tiled pair kernel
+// ---------------------------------------------------------------------------
+template <class R> struct KernelConsts {
+    EqualK<R> eq;
+    UnequalK<R> uq;
+};
+
+template <class R> __device__ __forceinline__ KernelConsts<R> convert_consts(const PairConsts &c)
+{
+    KernelConsts<R> k;
+    k.eq.two_a = (R)c.eq[0]; k.eq.two_a2 = (R)c.eq[1]; k.eq.f8pm = (R)c.eq[2]; k.eq.f16pm = (R)c.eq[3];
+    k.eq.f6pma = (R)c.eq[4]; k.eq.q32 = (R)c.eq[5]; k.eq.inv_a = (R)c.eq[6]; k.eq.f8pma3 = (R)c.eq[7];
+    k.eq.f16pma3 = (R)c.eq[8]; k.eq.q8 = (R)c.eq[9];
+    k.uq.sum = (R)c.uq[0]; k.uq.dmin = (R)c.uq[1]; k.uq.dmin2 = (R)c.uq[2]; k.uq.far_c = (R)c.uq[3];
+    k.uq.half_sum = (R)c.uq[4]; k.uq.f8pm = (R)c.uq[5]; k.uq.f6pmab = (R)c.uq[6]; k.uq.fmax = (R)c.uq[7];
+    k.uq.c_mid_den = (R)c.uq[8]; k.uq.ab = (R)c.uq[9]; k.uq.as = (R)c.uq[10]; k.uq.ab2 = (R)c.uq[11];
+    k.uq.f8pmas3 = (R)c.uq[12]; k.uq.seg_bigger = (R)c.uq[13];
+    return k;
+}
+
+template <int KIND, class R, int TPB, int TT>
+__global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ CUtensorMap src_map,
+                                                       const PairLaunch args)
+{
+    constexpr int NOUT = KindTraits<KIND>::nout;
+    constexpr int kStageScalars = kTile * kRecLen;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    R *ring = reinterpret_cast<R *>(smem_raw);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + kStages * kStageScalars * sizeof(R));
+
+    const int tid = threadIdx.x;
+    const int j_begin = blockIdx.y * args.chunk;
+    const int j_end = min(j_begin + args.chunk, args.n_src);
+    const int ntiles = j_end > j_begin ? (j_end - j_begin + kTile - 1) / kTile : 0;
+    constexpr unsigned kBoxBytes = kStageScalars * sizeof(R);
+
+    if (tid == 0) {
+        prefetch_tensormap(&src_map);
+#pragma unroll
+        for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int issued = 0;  // tiles requested so far (meaningful on thread 0)
+    if (tid == 0) {
+        for (; issued < kStages && issued < ntiles; ++issued) {
+            mbar_arrive_expect_tx(&bars[issued], kBoxBytes);
+            tma_load_2d(ring + issued * kStageScalars, &src_map, 0, j_begin + issued * kTile, &bars[issued]);
+        }
+    }
+
+    const KernelConsts<R> K = convert_consts<R>(args.k);
+    const R *tgt_rec = reinterpret_cast<const R *>(args.tgt_rec);
+    Pos<R> tp[TT];
+    int ti[TT];
+    Acc<R, NOUT> acc[TT];
+#pragma unroll
+    for (int k = 0; k < TT; ++k) {
+        ti[k] = blockIdx.x * (TPB * TT) + k * TPB + tid;
+        const int gi = args.tgt_start + min(ti[k], args.n_tgt - 1);
+        tp[k] = load_tgt(tgt_rec, gi);
+        acc[k].zero();
+    }
+
+    bool timed_out = false;
+    int t = 0;
+    for (; t < ntiles; ++t) {
+        const int s = t % kStages;
+        const bool ok = mbar_wait_bounded(&bars[s], (t / kStages) & 1);
+        if (__syncthreads_or(!ok)) {
+            timed_out = true;
+            break;
+        }
+        // Every thread has finished tile t-1: its stage can be refilled.
+        if (tid == 0 && t >= 1 && issued < ntiles) {
+            const int sp = (t - 1) % kStages;
+            mbar_arrive_expect_tx(&bars[sp], kBoxBytes);
+            tma_load_2d(ring + sp * kStageScalars, &src_map, 0, j_begin + issued * kTile, &bars[sp]);
+            ++issued;
+        }
+        const R *tile = ring + s * kStageScalars;
+        const int j0 = j_begin + t * kTile;
+        const int jn = min(kTile, j_end - j0);
+#pragma unroll 2
+        for (int jj = 0; jj < jn; ++jj) {
+            Pos<R> sp;
+            R F[6];
+            load_src(tile + jj * kRecLen, sp, F);
+#pragma unroll
+            for (int k = 0; k < TT; ++k) {
+                const R dx = diff<R>(tp[k].x, sp.x, tp[k].lx, sp.lx);
+                const R dy = diff<R>(tp[k].y, sp.y, tp[k].ly, sp.ly);
+                if constexpr (KIND == kSSWall) {
+                    const R zi = tp[k].z + tp[k].lz, zj = sp.z + sp.lz;
+                    const R dz = diff<R>(tp[k].z, sp.z, tp[k].lz, sp.lz);
+                    const R zs = (tp[k].z + sp.z) + (tp[k].lz + sp.lz);
+                    const bool self = (args.tgt_start + ti[k]) == (j0 + jj);
+                    pair_ss_wall<R>(dx, dy, dz, zs, zi, zj, self, F, acc[k].t, acc[k].t + 3);
+                } else {
+                    const R dz = diff<R>(tp[k].z, sp.z, tp[k].lz, sp.lz);
+                    if constexpr (KIND == kSS) pair_ss<R>(dx, dy, dz, F, K.eq, acc[k].t, acc[k].t + 3);
+                    if constexpr (KIND == kBB) pair_bb<R>(dx, dy, dz, F, K.eq, acc[k].t);
+                    if constexpr (KIND == kSB) pair_sb<R>(dx, dy, dz, F, K.uq, acc[k].t, acc[k].t + 3);
+                    if constexpr (KIND == kBS) pair_bs<R>(dx, dy, dz, F, K.uq, acc[k].t);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < TT; ++k) acc[k].fold();
+    }
+
+    if (timed_out) {
+        if (tid == 0) {
+            atomicOr(args.err, kDevErrWaitTimeout);
+            // Let the copies still in flight land (bounded) before the CTA exits.
+            for (int u = t; u < issued; ++u) (void)mbar_wait_bounded(&bars[u % kStages], (u / kStages) & 1);
+        }
+        return;
+    }
+
+#pragma unroll
+    for (int k = 0; k < TT; ++k) {
+        if (ti[k] >= args.n_tgt) continue;
+        if (args.partial != nullptr) {
+            double *p = args.partial + ((size_t)blockIdx.y * args.n_tgt + ti[k]) * NOUT;
+#pragma unroll
+            for (int c = 0; c < NOUT; ++c) p[c] = acc[k].total(c);
+        } else {
+            double *o = args.out + (size_t)ti[k] * NOUT;
+#pragma unroll
+            for (int c = 0; c < NOUT; ++c) o[c] = args.accumulate ? o[c] + acc[k].total(c) : acc[k].total(c);
+        }
+    }
+}
+
+// 3. split reduction: out[i] (=|+=) sum over splits, in split order.
+__global__ void reduce_splits(const double *__restrict__ partial, int splits, int count,
+                              double *__restrict__ out, int accumulate)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    double s = accumulate ? out[e] : 0.0;
+    for (int p = 0; p < splits; ++p) s += partial[(size_t)p * count + e];
+    out[e] = s;
+}
+
+// ---------------------------------------------------------------------------
+// barrier forces: cuda_functions.cu:961-1157.  Positions are screened in
+// FP32; pairs that can be inside the cutoff are re-evaluated in FP64 from
+// the original arrays, so the force arithmetic is the reference's FP64.
+// Targets: segments [0,S) then blobs [S, S+B) (of the requested ranges);
+// sources: all S segments then all B blobs.
+// ---------------------------------------------------------------------------
+constexpr int kBarrierTpb = 128;
+
+__global__ void pack_screen_positions(const double *__restrict__ xs, int S, const double *__restrict__ xb, int B,
+                                      float4 *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S + B) return;
+    const double *p = i < S ? xs + 3 * (size_t)i : xb + 3 * (size_t)(i - S);
+    const float hx = (float)p[0], hy = (float)p[1], hz = (float)p[2];
+    out[2 * (size_t)i] = make_float4(hx, hy, hz, 0.f);
+    out[2 * (size_t)i + 1] =
+        make_float4((float)(p[0] - (double)hx), (float)(p[1] - (double)hy), (float)(p[2] - (double)hz), 0.f);
+}
+
+__global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
+{
+    __shared__ float4 tile[2 * kBarrierTpb];
+    const int N = a.S + a.B;
+    const int local = blockIdx.x * blockDim.x + threadIdx.x;  // over [0, num_segs + num_blobs)
+    const bool is_seg_target = local < a.num_segs;
+    const bool valid = local < a.num_segs + (a.wall ? 0 : a.num_blobs);
+    const int gi = is_seg_target ? a.start_seg + local : a.S + a.start_blob + (local - a.num_segs);
+    double xi = 0, yi = 0, zi = 0;
+    float4 pf = make_float4(0.f, 0.f, 0.f, 0.f), pl = pf;
+    if (valid) {
+        const double *p = is_seg_target ? a.xs + 3 * (size_t)gi : a.xb + 3 * (size_t)(gi - a.S);
+        xi = p[0]; yi = p[1]; zi = p[2];
+        pf = a.screen[2 * (size_t)gi];
+        pl = a.screen[2 * (size_t)gi + 1];
+    }
+    const int fil_i = gi / a.nseg;
+    double g0 = 0, g1 = 0, g2 = 0;
+    const double DL = 2.2 * a.rseg;
+    if (valid && is_seg_target && a.wall && zi < 0.5 * DL) {
+        const double fz = fmin(1.0, 1.0 - (zi - a.rseg) / (0.5 * DL - a.rseg));
+        g2 = a.scale * fz * fz * fz * fz;
+    }
+    // widest cutoff over the source types, with a relative margin for the FP32 screen
+    const double a_tgt = is_seg_target ? a.rseg : a.rblob;
+    for (int j0 = 0; j0 < N; j0 += kBarrierTpb) {
+        const int jl = j0 + threadIdx.x;
+        if (jl < N) {
+            tile[2 * threadIdx.x] = a.screen[2 * (size_t)jl];
+            tile[2 * threadIdx.x + 1] = a.screen[2 * (size_t)jl + 1];
+        }
+        __syncthreads();
+        const int jn = min(kBarrierTpb, N - j0);
+        if (valid) {
+            for (int jj = 0; jj < jn; ++jj) {
+                const int j = j0 + jj;
+                const float4 q = tile[2 * jj], ql = tile[2 * jj + 1];
+                const float dx = (pf.x - q.x) + (pl.x - ql.x);
+                const float dy = (pf.y - q.y) + (pl.y - ql.y);
+                const float dz = (pf.z - q.z) + (pl.z - ql.z);
+                const float d2 = dx * dx + dy * dy + dz * dz;
+                const bool src_seg = j < a.S;
+                const double asum = a_tgt + (src_seg ? a.rseg : a.rblob);
+                const float cut = (float)(1.1 * asum) * 1.001f;
+                if (d2 >= cut * cut) continue;
+                // candidate: exact FP64 evaluation, as the reference
+                bool excluded;
+                if (is_seg_target) {
+                    const int fil_j = j / a.nseg;
+                    const int di = gi - j;
+                    excluded = (fil_i == fil_j) && (di <= 1 && di >= -1);
+                } else {
+                    excluded = (j == gi);
+                }
+                if (excluded) continue;
+                const double *pj = src_seg ? a.xs + 3 * (size_t)j : a.xb + 3 * (size_t)(j - a.S);
+                const double ddx = xi - pj[0], ddy = yi - pj[1], ddz = zi - pj[2];
+                const double dist = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+                if (dist < 1.1 * asum) {
+                    double c = fmin(1.0, 1.0 - (10.0 / asum) * (dist - asum));
+                    c = a.scale * c * c * c * c;
+                    const double idist = 1.0 / dist;
+                    g0 += c * ddx * idist;
+                    g1 += c * ddy * idist;
+                    g2 += c * ddz * idist;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!valid) return;
+    if (is_seg_target) {
+        double *f = a.f_segs + 6 * (size_t)gi;
+        f[0] += g0;
+        f[1] += g1;
+        f[2] += g2;
+    } else {
+        double *f = a.f_blobs_rep + 3 * (size_t)(local - a.num_segs);
+        f[0] = g0;
+        f[1] = g1;
+        f[2] = g2;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+void fill_consts(PairConsts &c, double a_eq, double as, double ab, double mu)
+{
+    const double pi = kPi;
+    c.eq[0] = 2.0 * a_eq;
+    c.eq[1] = 2.0 * a_eq * a_eq;
+    c.eq[2] = 1.0 / (8.0 * pi * mu);
+    c.eq[3] = 1.0 / (16.0 * pi * mu);
+    c.eq[4] = 1.0 / (6.0 * pi * mu * a_eq);
+    c.eq[5] = 3.0 / (32.0 * a_eq);
+    c.eq[6] = 1.0 / a_eq;
+    c.eq[7] = 1.0 / (8.0 * pi * mu * a_eq * a_eq * a_eq);
+    c.eq[8] = 1.0 / (16.0 * pi * mu * a_eq * a_eq * a_eq);
+    c.eq[9] = 3.0 / (8.0 * a_eq);
+    const double dmin = fabs(as - ab);
+    c.uq[0] = as + ab;
+    c.uq[1] = dmin;
+    c.uq[2] = dmin * dmin;
+    c.uq[3] = (as * as + ab * ab) / 3.0;
+    c.uq[4] = 0.5 * (as + ab);
+    c.uq[5] = 1.0 / (8.0 * pi * mu);
+    c.uq[6] = 1.0 / (6.0 * pi * mu * as * ab);
+    c.uq[7] = 1.0 / (6.0 * pi * mu * (as > ab ? as : ab));
+    c.uq[8] = 1.0 / (128.0 * pi * mu * ab * as * as * as);
+    c.uq[9] = ab;
+    c.uq[10] = as;
+    c.uq[11] = ab * ab;
+    c.uq[12] = 1.0 / (8.0 * pi * mu * as * as * as);
+    c.uq[13] = as > ab ? 1.0 : 0.0;
+}
+
+gmi_status pack_records(gmi_context *ctx, const double *x, const double *f, int nf, int n, DeviceBuffer &buf)
+{
+    const bool f64 = ctx->precision == GMI_FP64;
+    const size_t bytes = (size_t)n * kRecLen * (f64 ? sizeof(double) : sizeof(float));
+    gmi_status st = buf.reserve(bytes > 0 ? bytes : 16);
+    if (st != GMI_OK) return st;
+    if (n == 0) return GMI_OK;
+    const int tpb = 256;
+    const int grid = (n + tpb - 1) / tpb;
+    if (f64)
+        pack_records_f64<<<grid, tpb, 0, ctx->stream>>>(x, f, nf, n, static_cast<double2 *>(buf.ptr));
+    else
+        pack_records_f32<<<grid, tpb, 0, ctx->stream>>>(x, f, nf, n, static_cast<float4 *>(buf.ptr));
+    ctx->launches++;
+    GMI_CUDA_TRY(cudaGetLastError());
+    return GMI_OK;
+}
+
+static gmi_status make_record_map(gmi_context *ctx, CUtensorMap *map, const void *base, int n, bool f64)
+{
+    using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    auto encode = reinterpret_cast<EncodeFn>(ctx->encode_tiled);
+    if (encode == nullptr) {
+        set_last_error_msg("cuTensorMapEncodeTiled is unavailable from the driver");
+        return GMI_ERR_CUDA;
+    }
+    const cuuint64_t esize = f64 ? 8 : 4;
+    cuuint64_t dims[2] = {(cuuint64_t)kRecLen, (cuuint64_t)(n > 0 ? n : 1)};
+    cuuint64_t strides[1] = {kRecLen * esize};
+    cuuint32_t box[2] = {(cuuint32_t)kRecLen, (cuuint32_t)kTile};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(map, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                        const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        char msg[128];
+        snprintf(msg, sizeof msg, "cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
+        set_last_error_msg(msg);
+        return GMI_ERR_CUDA;
+    }
+    return GMI_OK;
+}
+
+// Kernel table: (kind, precision, tpb, tt) -> launcher.
+using KernelFn = void (*)(CUtensorMap, PairLaunch);
+
+template <int KIND, class R, int TPB, int TT> struct Inst {
+    static void *fn() { return reinterpret_cast<void *>(&rpy_pair_kernel<KIND, R, TPB, TT>); }
+};
+
+struct ShapeEntry {
+    int tpb, tt;
+};
+static const ShapeEntry kShapes[] = {{128, 1}, {128, 2}, {256, 1}, {256, 2}, {128, 4}};
+constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
+
+template <int KIND, class R> static void *kernel_for_shape(int idx)
+{
+    switch (idx) {
+        case 0: return Inst<KIND, R, 128, 1>::fn();
+        case 1: return Inst<KIND, R, 128, 2>::fn();
+        case 2: return Inst<KIND, R, 256, 1>::fn();
+        case 3: return Inst<KIND, R, 256, 2>::fn();
+        default: return Inst<KIND, R, 128, 4>::fn();
+    }
+}
+
+static void *kernel_ptr(int kind, bool f64, int shape_idx)
+{
+    switch (kind) {
+        case kSS: return f64 ? kernel_for_shape<kSS, double>(shape_idx) : kernel_for_shape<kSS, float>(shape_idx);
+        case kSSWall:
+            return f64 ? kernel_for_shape<kSSWall, double>(shape_idx) : kernel_for_shape<kSSWall, float>(shape_idx);
+        case kBB: return f64 ? kernel_for_shape<kBB, double>(shape_idx) : kernel_for_shape<kBB, float>(shape_idx);
+        case kSB: return f64 ? kernel_for_shape<kSB, double>(shape_idx) : kernel_for_shape<kSB, float>(shape_idx);
+        default: return f64 ? kernel_for_shape<kBS, double>(shape_idx) : kernel_for_shape<kBS, float>(shape_idx);
+    }
+}
+
+static int shape_index(int tpb, int tt)
+{
+    for (int i = 0; i < kNumShapes; ++i)
+        if (kShapes[i].tpb == tpb && kShapes[i].tt == tt) return i;
+    return 1;
+}
+
+static size_t ring_bytes(bool f64) { return (size_t)kStages * kTile * kRecLen * (f64 ? 8 : 4) + kStages * 8; }
+
+static int nout_of(int kind) { return (kind == kBB || kind == kBS) ? 3 : 6; }
+
+// Source splits: enough CTAs for ~2 full waves when the target tiles alone
+// cannot fill the GPU; every split keeps at least two tiles of sources.
+static int choose_splits(const gmi_context *ctx, int n_tgt_ctas, int n_src, int occ)
+{
+    const int slots = ctx->sm_count * (occ > 0 ? occ : 1);
+    const int max_splits = n_src / (2 * kTile) > 1 ? n_src / (2 * kTile) : 1;
+    if (n_tgt_ctas >= 2 * slots) return 1;
+    int s = (2 * slots + n_tgt_ctas - 1) / n_tgt_ctas;
+    return s < max_splits ? s : max_splits;
+}
+
+gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_start, int n_tgt, const void *src_rec,
+                       int n_src, const PairConsts &k, double *out, int accumulate, const PairShape *force_shape)
+{
+    if (n_tgt <= 0) return GMI_OK;
+    const bool f64 = ctx->precision == GMI_FP64;
+    const int nout = nout_of(kind);
+    if (n_src <= 0) {
+        if (!accumulate) GMI_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)n_tgt * nout * sizeof(double), ctx->stream));
+        return GMI_OK;
+    }
+    PairShape shape;
+    if (force_shape) {
+        shape = *force_shape;
+    } else {
+        auto it = ctx->tuned.find(TuneKey{kind, ctx->precision, n_tgt, n_src});
+        if (it != ctx->tuned.end()) shape = it->second;
+    }
+    const int sidx = shape_index(shape.tpb, shape.tt);
+    const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;
+    void *fn = kernel_ptr(kind, f64, sidx);
+    const size_t smem = ring_bytes(f64);
+    GMI_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, tpb, smem));
+    const int n_tgt_ctas = (n_tgt + tpb * tt - 1) / (tpb * tt);
+    int splits = shape.splits > 0 ? shape.splits : choose_splits(ctx, n_tgt_ctas, n_src, occ);
+    int chunk = (n_src + splits - 1) / splits;
+    chunk = (chunk + kTile - 1) / kTile * kTile;
+    splits = (n_src + chunk - 1) / chunk;
+
+    PairLaunch a{};
+    a.tgt_rec = tgt_rec;
+    a.tgt_start = tgt_start;
+    a.n_tgt = n_tgt;
+    a.n_src = n_src;
+    a.chunk = chunk;
+    a.k = k;
+    a.out = out;
+    a.accumulate = accumulate;
+    a.err = ctx->d_err;
+    a.partial = nullptr;
+    if (splits > 1) {
+        gmi_status st = ctx->partial.reserve((size_t)splits * n_tgt * nout * sizeof(double));
+        if (st != GMI_OK) return st;
+        a.partial = static_cast<double *>(ctx->partial.ptr);
+    }
+    CUtensorMap map;
+    gmi_status st = make_record_map(ctx, &map, src_rec, n_src, f64);
+    if (st != GMI_OK) return st;
+    void *params[] = {&map, &a};
+    dim3 grid(n_tgt_ctas, splits);
+    GMI_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(tpb), params, smem, ctx->stream));
+    ctx->launches++;
+    if (splits > 1) {
+        const int count = n_tgt * nout;
+        reduce_splits<<<(count + 255) / 256, 256, 0, ctx->stream>>>(a.partial, splits, count, out, accumulate);
+        ctx->launches++;
+        GMI_CUDA_TRY(cudaGetLastError());
+    }
+    return GMI_OK;
+}
+
+gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &in)
+{
+    BarrierLaunch a = in;
+    const int N = a.S + a.B;
+    const int ntg = a.num_segs + (a.wall ? 0 : a.num_blobs);
+    if (ntg <= 0) return GMI_OK;
+    gmi_status st = ctx->rec_tgt.reserve((size_t)(N > 0 ? N : 1) * 2 * sizeof(float4));
+    if (st != GMI_OK) return st;
+    a.screen = static_cast<float4 *>(ctx->rec_tgt.ptr);
+    pack_screen_positions<<<(N + 255) / 256, 256, 0, ctx->stream>>>(a.xs, a.S, a.xb, a.B, a.screen);
+    barrier_kernel<<<(ntg + kBarrierTpb - 1) / kBarrierTpb, kBarrierTpb, 0, ctx->stream>>>(a);
+    ctx->launches += 2;
+    GMI_CUDA_TRY(cudaGetLastError());
+    return GMI_OK;
+}
+
+// Autotuner: time each candidate shape (with the automatic split choice and
+// with a few explicit split counts) on the records already packed for this
+// problem, keep the fastest.
+gmi_status autotune_pair(gmi_context *ctx, int kind, const void *tgt_rec, int n_tgt, const void *src_rec, int n_src,
+                         const PairConsts &k, double *out)
+{
+    cudaEvent_t e0, e1;
+    GMI_CUDA_TRY(cudaEventCreate(&e0));
+    GMI_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    PairShape best_shape;
+    for (int si = 0; si < kNumShapes; ++si) {
+        for (int sp : {0, 1, 2, 4, 8}) {
+            PairShape s{kShapes[si].tpb, kShapes[si].tt, sp};
+            gmi_status st = launch_pair(ctx, kind, tgt_rec, 0, n_tgt, src_rec, n_src, k, out, 0, &s);
+            if (st != GMI_OK) return st;
+            GMI_CUDA_TRY(cudaEventRecord(e0, ctx->stream));
+            for (int rep = 0; rep < 3; ++rep) {
+                st = launch_pair(ctx, kind, tgt_rec, 0, n_tgt, src_rec, n_src, k, out, 0, &s);
+                if (st != GMI_OK) return st;
+            }
+            GMI_CUDA_TRY(cudaEventRecord(e1, ctx->stream));
+            GMI_CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            GMI_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                best_shape = s;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->tuned[TuneKey{kind, ctx->precision, n_tgt, n_src}] = best_shape;
+    return context_check_device_errors(ctx);
+}
+
+}  // namespace gmi

@@ -1,0 +1,56 @@
+// gmi_pair_kernels.hpp -- host interface of the tiled pair kernels.
+#pragma once
+
+#include "gmi_context.hpp"
+
+namespace gmi {
+
+// Physical constants of one pair kind, precomputed on the host in FP64
+// (converted to the kernel's scalar type on the device).
+struct PairConsts {
+    double eq[10];  // equal radii: see EqualK
+    double uq[14];  // segment/blob radii: see UnequalK
+};
+
+struct PairLaunch {
+    const void *tgt_rec;  // records of the target set
+    int tgt_start, n_tgt; // targets [tgt_start, tgt_start + n_tgt)
+    int n_src, chunk;     // sources, sources per split (multiple of the tile)
+    PairConsts k;
+    double *out;          // direct output when there is one split
+    double *partial;      // [splits][n_tgt][nout] when there are several
+    int accumulate;
+    unsigned *err;
+};
+
+struct BarrierLaunch {
+    double *f_segs;
+    double *f_blobs_rep;
+    const double *xs;
+    const double *xb;
+    float4 *screen;  // FP32 (hi, lo) positions of all S + B particles (filled by the launcher)
+    int S, B;
+    int start_seg, num_segs, start_blob, num_blobs;
+    int nseg;
+    double rseg, rblob, scale;
+    int wall;
+};
+
+void fill_consts(PairConsts &c, double a_eq, double a_seg, double a_blob, double mu);
+
+// Pack AoS FP64 positions (and forces with nf = 3 or 6 components, or none
+// when f == nullptr) into the context's record format for its precision.
+gmi_status pack_records(gmi_context *ctx, const double *x, const double *f, int nf, int n, DeviceBuffer &buf);
+
+// One pair sum: out[nout*(i)] (=|+=) sum_j M(i, j) F_j for targets
+// [tgt_start, tgt_start + n_tgt).  force_shape overrides the tuned shape.
+gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_start, int n_tgt, const void *src_rec,
+                       int n_src, const PairConsts &k, double *out, int accumulate,
+                       const PairShape *force_shape = nullptr);
+
+gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &a);
+
+gmi_status autotune_pair(gmi_context *ctx, int kind, const void *tgt_rec, int n_tgt, const void *src_rec, int n_src,
+                         const PairConsts &k, double *out);
+
+}  // namespace gmi

@@ -1,0 +1,133 @@
+/*
+ * gmi.h -- C ABI of the GB300 mobility library (libgmi.so).
+ *
+ * The library is a drop-in for the GPU half of the reference's
+ * rpy_mobility_solver (rpy_mobility_solver.{hpp,cu}) and for the generic
+ * mobility_solver methods that consume it (mobility_solver.cpp).  Every entry
+ * point takes plain pointers and sizes, returns a gmi_status, and never
+ * exits the process.  Device pointers are marked _d; host pointers _h.
+ *
+ * Precision: GMI_FP64 evaluates the pair sums in FP64 like the reference;
+ * GMI_FP32C evaluates them in FP32 with double-float source positions and
+ * compensated (two-sum) accumulation, and returns FP64 results.
+ */
+#ifndef GMI_H
+#define GMI_H
+
+#if defined(__GNUC__)
+#define GMI_API __attribute__((visibility("default")))
+#else
+#define GMI_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gmi_status {
+    GMI_OK = 0,
+    GMI_ERR_ARG = 1,            /* bad size, null pointer, unsupported option */
+    GMI_ERR_CUDA = 2,           /* a CUDA runtime call failed (see gmi_last_error) */
+    GMI_ERR_DEVICE_TIMEOUT = 3, /* a kernel's bounded wait gave up; results invalid */
+    GMI_ERR_NONFINITE = 4,      /* NaN/Inf met where the reference would diverge */
+    GMI_ERR_NOT_CONVERGED = 5,  /* an iterative solve hit its iteration cap */
+    GMI_ERR_STATE = 6           /* call out of order (e.g. solve before setup) */
+} gmi_status;
+
+typedef enum gmi_precision {
+    GMI_FP64 = 0,  /* reference arithmetic */
+    GMI_FP32C = 1  /* FP32 pair math, compensated accumulation, FP64 I/O */
+} gmi_precision;
+
+/* Message describing the last failure on the calling thread ("" if none). */
+GMI_API const char *gmi_last_error(void);
+/* Library version: major*10000 + minor*100 + patch. */
+GMI_API int gmi_version(void);
+
+/* ------------------------------------------------------------------------
+ * Context: one GPU, one CUDA stream, scratch memory that grows on demand,
+ * the launch-shape cache of the autotuner, and a device error word.
+ * (The reference keeps the equivalent state in rpy_mobility_solver's
+ * members, rpy_mobility_solver.hpp:45-58.)
+ * ---------------------------------------------------------------------- */
+typedef struct gmi_context gmi_context;
+
+GMI_API gmi_status gmi_context_create(int device, gmi_context **out);
+GMI_API gmi_status gmi_context_destroy(gmi_context *ctx);
+/* Use an existing cudaStream_t (passed as void*); NULL selects the context's own stream. */
+GMI_API gmi_status gmi_context_set_stream(gmi_context *ctx, void *cuda_stream);
+GMI_API gmi_status gmi_context_set_precision(gmi_context *ctx, int precision);
+GMI_API int gmi_context_precision(const gmi_context *ctx);
+/* Block until the context's stream drains; reports device-side errors
+ * (bounded-wait timeouts) recorded since the last call.
+ * Replaces rpy_mobility_solver::wait_for_device (rpy_mobility_solver.cu:230-239). */
+GMI_API gmi_status gmi_context_synchronize(gmi_context *ctx);
+/* Number of library kernels launched on this context so far. */
+GMI_API long long gmi_context_launch_count(const gmi_context *ctx);
+
+/* ------------------------------------------------------------------------
+ * Pair sums on device arrays, in the reference's layouts (FP64, AoS):
+ *   X segs [3*S], F segs [6*S] = (f, tau), V segs [6*S] = (v, omega)
+ *   X blobs [3*B], F blobs [3*B], V blobs [3*B]
+ * Targets are [start, start+num) of their set; V is indexed from `start`
+ * (V[0] belongs to target `start`), as in the reference kernels.  All
+ * calls are asynchronous on the context stream.
+ * ---------------------------------------------------------------------- */
+
+/* V = M_ss F: segment <- segment, free space.  Replaces Mss_mult
+ * (cuda_functions.cu:246-425, launched at rpy_mobility_solver.cu:241-255). */
+GMI_API gmi_status gmi_Mss_mult(gmi_context *ctx, double *V_d, const double *F_d, const double *X_d,
+                        int start_seg, int num_segs, int total_segs, double rseg, double mu);
+
+/* V = M_ss F above a no-slip wall at z = 0 (Swan & Brady); a = mu = 1 as in
+ * the reference.  Replaces the INFINITE_PLANE_WALL Mss_mult
+ * (cuda_functions.cu:10-242). */
+GMI_API gmi_status gmi_Mss_mult_wall(gmi_context *ctx, double *V_d, const double *F_d, const double *X_d,
+                             int start_seg, int num_segs, int total_segs);
+
+/* V = M_bb F: blob <- blob.  Replaces Mbb_mult (cuda_functions.cu:429-539,
+ * launched at rpy_mobility_solver.cu:277-291). */
+GMI_API gmi_status gmi_Mbb_mult(gmi_context *ctx, double *V_d, const double *F_d, const double *X_d,
+                        int start_blob, int num_blobs, int total_blobs, double rblob, double mu);
+
+/* V += M_sb F_blobs: segment <- blob (accumulates, as the reference).
+ * Replaces Msb_mult (cuda_functions.cu:541-694, rpy_mobility_solver.cu:259-273). */
+GMI_API gmi_status gmi_Msb_mult(gmi_context *ctx, double *V_d, const double *F_blobs_d, const double *Xs_d,
+                        const double *Xb_d, int start_seg, int num_segs, int total_segs,
+                        int total_blobs, double rseg, double rblob, double mu);
+
+/* V = M_bs F_segs: blob <- segment (overwrites).  Replaces Mbs_mult
+ * (cuda_functions.cu:697-863, rpy_mobility_solver.cu:295-309). */
+GMI_API gmi_status gmi_Mbs_mult(gmi_context *ctx, double *V_d, const double *F_segs_d, const double *Xb_d,
+                        const double *Xs_d, int start_blob, int num_blobs, int total_blobs,
+                        int total_segs, double rseg, double rblob, double mu);
+
+/* Short-range barrier forces.  Segment targets ADD into f_segs[6*i+0..2];
+ * blob targets OVERWRITE f_blobs_repulsion[3*(i-start_blob)..] (skipped when
+ * wall != 0, as with the reference's prescribed wall bodies).  Segments
+ * i, j of one filament (nseg per filament) with |i-j| <= 1 do not repel.
+ * force_scale = REPULSIVE_FORCE_FACTOR * END_FORCE_MAGNITUDE.
+ * Replaces barrier_forces (cuda_functions.cu:961-1157,
+ * rpy_mobility_solver.cu:207-228). */
+GMI_API gmi_status gmi_barrier_forces(gmi_context *ctx, double *f_segs_d, double *f_blobs_repulsion_d,
+                              const double *x_segs_d, const double *x_blobs_d, int start_seg,
+                              int num_segs, int start_blob, int num_blobs, int total_segs,
+                              int total_blobs, int nseg_per_filament, double rseg, double rblob,
+                              double force_scale, int wall);
+
+/* Autotuner: time the candidate launch shapes of one pair kernel for the
+ * given sizes on the context's GPU and keep the fastest for later calls.
+ * kind: 0 = ss, 1 = ss wall, 2 = bb, 3 = sb, 4 = bs. */
+GMI_API gmi_status gmi_autotune(gmi_context *ctx, int kind, int num_targets, int num_sources);
+
+/* Measured FMA-pipe throughput (FLOP/s, FMA = 2) of this GPU for
+ * precision GMI_FP32C (FP32 pipe) or GMI_FP64 (FP64 pipe): the roofline
+ * denominator of the pair kernels, which are bound by that pipe.  No
+ * counterpart in the reference. */
+GMI_API gmi_status gmi_measure_fma_peak(gmi_context *ctx, int precision, double *flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GMI_H */

@@ -1,0 +1,141 @@
+"""GPU parity of the pair sums through the C ABI.
+
+FP64 results must match the reference (golden fixtures from the reference's
+own kernels, and the CPU oracle at larger sizes) to 1e-10 relative; FP32C
+results carry a stated error bound against the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+FP64_TOL = 1e-10      # spec bound for the FP64 path
+FP32C_TOL = 2e-6      # max |v - v64| / max |v64| for the compensated FP32 path
+FREE = [c for c in golden_cases() if not c.startswith("wall")]
+WALL = [c for c in golden_cases() if c.startswith("wall")]
+
+
+def T(a):
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def N(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.fixture(params=[0, 1], ids=["fp64", "fp32c"])
+def prec_ctx(request, gpu_ctx):
+    gpu_ctx.set_precision(request.param)
+    yield gpu_ctx, (FP64_TOL if request.param == 0 else FP32C_TOL)
+    gpu_ctx.set_precision(0)
+
+
+@pytest.mark.parametrize("case", FREE)
+def test_pairs_match_golden(case, prec_ctx):
+    ctx, tol = prec_ctx
+    g = load_golden(case)
+    rs, rb, mu = float(g["rseg"]), float(g["rblob"]), float(g["mu"])
+    xs, xb, fs, fb = T(g["xs"]), T(g["xb"]), T(g["fs"]), T(g["fb"])
+    assert rel_err(N(ctx.mss(xs, fs, rs, mu)), g["v_ss"]) < tol
+    assert rel_err(N(ctx.mbb(xb, fb, rb, mu)), g["v_bb"]) < tol
+    v = T(g["v_in"])
+    ctx.msb(xs, xb, fb, v, rs, rb, mu)
+    assert rel_err(N(v), g["v_sb"]) < tol
+    assert rel_err(N(ctx.mbs(xb, xs, fs, rs, rb, mu)), g["v_bs"]) < tol
+    ctx.synchronize()
+
+
+@pytest.mark.parametrize("case", FREE)
+def test_barrier_matches_golden(case, gpu_ctx):
+    g = load_golden(case)
+    fs = T(g["fs"])
+    fb = gpu_ctx.barrier(T(g["xs"]), T(g["xb"]), fs, int(g["nseg"]), float(g["rseg"]), float(g["rblob"]),
+                         float(g["force_scale"]))
+    gpu_ctx.synchronize()
+    assert rel_err(N(fs), g["fs_barrier"]) < 1e-14
+    assert rel_err(N(fb), g["fb_repulsion"]) < 1e-14
+
+
+@pytest.mark.parametrize("case", WALL)
+def test_wall_matches_golden(case, prec_ctx):
+    ctx, tol = prec_ctx
+    g = load_golden(case)
+    assert rel_err(N(ctx.mss_wall(T(g["xs"]), T(g["fs"]))), g["v_ss"]) < tol
+    fs = T(g["fs"])
+    ctx.barrier(T(g["xs"]), torch.zeros((0, 3), dtype=torch.float64, device="cuda"), fs, int(g["nseg"]),
+                1.0, 1.0, float(g["force_scale"]), wall=True)
+    ctx.synchronize()
+    assert rel_err(N(fs), g["fs_barrier"]) < 1e-14
+
+
+def test_larger_against_oracle(prec_ctx, oracle_built):
+    """Thousands of particles: several TMA tiles, several source splits,
+    ragged last tile; random cube with rejection (config-2 shape)."""
+    from generic_mobility_interface_class_gb300 import seeding
+    ctx, tol = prec_ctx
+    rpy = oracle_built
+    n = 3001
+    x = seeding.random_cube(n, seed=5)
+    f = np.random.default_rng(5).normal(size=(n, 6))
+    want = rpy.mss(x, f)
+    got = N(ctx.mss(T(x), T(f)))
+    assert rel_err(got, want) < tol
+    wantb = rpy.mbb(x, f[:, :3])
+    assert rel_err(N(ctx.mbb(T(x), T(f[:, :3]))), wantb) < tol
+
+
+def test_target_slices_and_accumulate(gpu_ctx, oracle_built):
+    rpy = oracle_built
+    g = load_golden("swimmer_sphere")
+    xs, fs = T(g["xs"]), T(g["fs"])
+    part = N(gpu_ctx.mss(xs, fs, start=7, num=20))
+    assert rel_err(part, g["v_ss"][7:27]) < FP64_TOL
+    # Msb accumulates onto the caller's array for a target slice only
+    v = T(g["v_in"][10:40])
+    gpu_ctx.msb(xs, T(g["xb"]), T(g["fb"]), v, start=10, num=30)
+    assert rel_err(N(v), g["v_sb"][10:40]) < FP64_TOL
+
+
+def test_empty_sources_and_targets(gpu_ctx):
+    z3 = torch.zeros((0, 3), dtype=torch.float64, device="cuda")
+    xs = T(np.array([[0.0, 0.0, 0.0], [3.0, 0.0, 0.0]]))
+    v = T(np.ones((2, 6)))
+    gpu_ctx.msb(xs, z3, z3, v)  # no blobs: V unchanged
+    gpu_ctx.synchronize()
+    np.testing.assert_array_equal(N(v), np.ones((2, 6)))
+    out = gpu_ctx.mbs(z3, xs, T(np.ones((2, 6))))  # no blob targets
+    assert out.shape == (0, 3)
+    vb = gpu_ctx.mbs(T(np.zeros((3, 3))), z3, torch.zeros((0, 6), dtype=torch.float64, device="cuda"))
+    gpu_ctx.synchronize()
+    np.testing.assert_array_equal(N(vb), np.zeros((3, 3)))
+
+
+def test_autotune_keeps_results(gpu_ctx, oracle_built):
+    rpy = oracle_built
+    from generic_mobility_interface_class_gb300 import seeding
+    n = 2048
+    x = seeding.random_cube(n, seed=9)
+    f = np.random.default_rng(9).normal(size=(n, 6))
+    want = rpy.mss(x, f)
+    for prec, tol in ((0, FP64_TOL), (1, FP32C_TOL)):
+        gpu_ctx.set_precision(prec)
+        gpu_ctx.autotune(0, n, n)
+        assert rel_err(N(gpu_ctx.mss(T(x), T(f))), want) < tol
+    gpu_ctx.set_precision(0)
+
+
+def test_fp32c_is_translation_robust(gpu_ctx, oracle_built):
+    """Double-float positions: shifting the whole cloud far from the origin
+    keeps the FP32C error at its bound."""
+    rpy = oracle_built
+    g = load_golden("swimmer_sphere")
+    xs = g["xs"] + np.array([1.0e4, -2.5e4, 3.3e3])
+    want = rpy.mss(xs, g["fs"])
+    gpu_ctx.set_precision(1)
+    got = N(gpu_ctx.mss(T(xs), T(g["fs"])))
+    gpu_ctx.set_precision(0)
+    assert rel_err(got, want) < FP32C_TOL
