@@ -35,7 +35,9 @@ class Context:
         check(self.lib.gmi_context_create(device, ctypes.byref(h)))
         self.handle = h
         s = stream if stream is not None else torch.cuda.current_stream(device)
-        check(self.lib.gmi_context_set_stream(self.handle, ctypes.c_void_p(s.cuda_stream)))
+        # torch's default stream has handle 0; the library needs the explicit
+        # cudaStreamLegacy handle (1) for it, since NULL means "own stream".
+        check(self.lib.gmi_context_set_stream(self.handle, ctypes.c_void_p(s.cuda_stream or 1)))
         self.set_precision(precision)
 
     def set_precision(self, precision: int) -> None:

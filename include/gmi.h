@@ -54,7 +54,10 @@ typedef struct gmi_context gmi_context;
 
 GMI_API gmi_status gmi_context_create(int device, gmi_context **out);
 GMI_API gmi_status gmi_context_destroy(gmi_context *ctx);
-/* Use an existing cudaStream_t (passed as void*); NULL selects the context's own stream. */
+/* Use an existing cudaStream_t (passed as void*); NULL selects the context's
+ * own non-blocking stream.  For the legacy default stream pass
+ * cudaStreamLegacy ((void*)1): work there is ordered with the caller's
+ * default-stream copies. */
 GMI_API gmi_status gmi_context_set_stream(gmi_context *ctx, void *cuda_stream);
 GMI_API gmi_status gmi_context_set_precision(gmi_context *ctx, int precision);
 GMI_API int gmi_context_precision(const gmi_context *ctx);
