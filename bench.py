@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--precision", choices=["fp32c", "fp64"], default="fp32c")
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 side measurement")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU sample")
+    p.add_argument("--no-autotune", action="store_true", help="use the default launch shape (profiling)")
     return p.parse_args()
 
 
@@ -218,7 +219,9 @@ def run_gmi(args, world, rank, local):
     vd = torch.empty((n, 6), dtype=torch.float64, device="cuda")
     l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
 
-    ctx.autotune(0, n, n)
+    if not args.no_autotune:
+        ctx.autotune(0, n, n)
+    tpb, tt, splits, tuned = ctx.tuned_shape(0, n, n)
     for _ in range(args.warmup):
         ctx.mss(xd, fd, out=vd)
     ctx.synchronize()
@@ -318,6 +321,8 @@ def run_gmi(args, world, rank, local):
             "config": {"workload": f"RPY apply microbenchmark, N={n} blobs (cube, phi=0.05, min sep 2.2a, "
                                    f"f,tau ~ N(0,1), 6-dof Mss formula, all pairs incl. self)",
                        "n": n, "precision": args.precision, "parallelism": f"replicas x{world}",
+                       "launch_shape": {"threads_per_cta": tpb, "targets_per_thread": tt,
+                                        "source_splits": splits or "auto", "autotuned": tuned},
                        "l2": "flushed (256 MB write) between timed steps"},
             "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(n * 9 * 8),
                     "d2h_bytes_per_step": int(n * 6 * 8), "path": "gmi_Mss_mult with pinned host X,F -> V"},

@@ -54,7 +54,45 @@ SIGNATURES = {
     "gmi_barrier_forces": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _I], _I),
     "gmi_autotune": ([_P, _I, _I, _I], _I),
     "gmi_measure_fma_peak": ([_P, _I, ctypes.POINTER(_D)], _I),
+    "gmi_tuned_shape": ([_P, _I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
+    "gmi_solver_create": ([_P, ctypes.POINTER(_P)], _I),
+    "gmi_solver_destroy": ([_P], _I),
+    "gmi_solver_host_arrays": ([_P, _P], _I),
+    "gmi_solver_context": ([_P], _P),
+    "gmi_solver_copy_segment_positions_to_device": ([_P], _I),
+    "gmi_solver_copy_segment_forces_to_device": ([_P], _I),
+    "gmi_solver_copy_blob_positions_to_device": ([_P], _I),
+    "gmi_solver_copy_blob_forces_to_device": ([_P], _I),
+    "gmi_solver_copy_interparticle_blob_forces_to_host": ([_P], _I),
+    "gmi_solver_copy_blob_velocities_to_host": ([_P], _I),
+    "gmi_solver_copy_segment_velocities_to_host": ([_P], _I),
+    "gmi_solver_apply_interparticle_forces": ([_P], _I),
+    "gmi_solver_wait_for_device": ([_P], _I),
+    "gmi_solver_evaluate_segment_segment_mobility": ([_P], _I),
+    "gmi_solver_evaluate_segment_blob_mobility": ([_P], _I),
+    "gmi_solver_evaluate_blob_blob_mobility": ([_P], _I),
+    "gmi_solver_evaluate_blob_segment_mobility": ([_P], _I),
+    "gmi_solver_set_blob_references": ([_P, _P], _I),
+    "gmi_solver_make_body_reference_matrices": ([_P, _P, _P, _P, _P], _I),
+    "gmi_solver_set_body_reference_matrices": ([_P, _P, _P], _I),
+    "gmi_solver_compute_velocities": ([_P, _P, _P, _P, ctypes.POINTER(_I)], _I),
+    "gmi_solver_get_v_bodies": ([_P, _P], _I),
+    "gmi_solver_set_v_bodies": ([_P, _P], _I),
 }
+
+
+class SolverConfig(ctypes.Structure):
+    """gmi_solver_config (include/gmi.h)."""
+    _fields_ = [("nswim", _I), ("nfil", _I), ("nseg", _I), ("nblob", _I), ("mu", _D), ("rseg", _D),
+                ("rblob", _D), ("repulsive_force_factor", _D), ("end_force_magnitude", _D), ("wall", _I),
+                ("max_linear_iter", _I), ("linear_tol", _D), ("precision", _I), ("device", _I)]
+
+
+class HostArrays(ctypes.Structure):
+    """gmi_host_arrays (include/gmi.h)."""
+    _fields_ = [(name, ctypes.POINTER(_D)) for name in
+                ("v_segs_host", "v_blobs_host", "x_segs_host", "x_blobs_host", "f_segs_host", "f_blobs_host",
+                 "f_blobs_repulsion_host")]
 
 _lib = None
 

@@ -229,6 +229,20 @@ gmi_status gmi_barrier_forces(gmi_context *ctx, double *f_segs_d, double *f_blob
     return launch_barrier(ctx, a);
 }
 
+gmi_status gmi_tuned_shape(const gmi_context *ctx, int kind, int num_targets, int num_sources, int *threads_per_cta,
+                           int *targets_per_thread, int *source_splits)
+{
+    GMI_ARG_CHECK(ctx && threads_per_cta && targets_per_thread && source_splits, "gmi_tuned_shape: null argument");
+    PairShape s;
+    auto it = ctx->tuned.find(TuneKey{kind, ctx->precision, num_targets, num_sources});
+    const bool found = it != ctx->tuned.end();
+    if (found) s = it->second;
+    *threads_per_cta = s.tpb;
+    *targets_per_thread = s.tt;
+    *source_splits = s.splits;
+    return found ? GMI_OK : GMI_ERR_STATE;
+}
+
 gmi_status gmi_autotune(gmi_context *ctx, int kind, int num_targets, int num_sources)
 {
     GMI_ARG_CHECK(ctx != nullptr, "gmi_autotune: null context");

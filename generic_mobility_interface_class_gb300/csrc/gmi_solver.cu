@@ -1,0 +1,1093 @@
+// gmi_solver.cu -- device-resident mobility solver: the reference's
+// rpy_mobility_solver state and the generic mobility_solver methods
+// (read_positions_and_forces, assemble_rhs, apply_preconditioner,
+// system_matrix_mult, solve_linear_system, compute_velocities,
+// make_body_reference_matrices) with every vector operation on the GPU.
+//
+// Layout in HBM (FP64, the reference's host layouts so host<->device copies
+// are single memcpys):
+//   x_segs[3S] f_segs[6S] v_segs[6S]   x_blobs[3B] f_blobs[3B] v_blobs[3B] f_rep[3B]
+//   bodies: x[3W] q[4W] (scalar first) f[6W] v[6W], R[9W] row-major,
+//           rotated reference matrices ktk_rot[36W], mob_rot[36W] (column-major 6x6)
+//   GMRES system of size n = 3B + 6W, blobs first (swimmer-major), then bodies;
+//   Krylov basis Q[n x (m+1)] column-major, Hessenberg H[(m+1) x (m+1)] column-major.
+// S = nswim*nfil*nseg segments, B = nswim*nblob blobs, W = nswim.
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "gmi_context.hpp"
+#include "gmi_pair_kernels.hpp"
+
+namespace gmi {
+
+constexpr int kRedTpb = 256;      // threads of the reduction kernels
+constexpr int kChunkRows = 1024;  // rows per block in dot-product partials
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum in a fixed order (result valid in thread 0).
+template <int TPB> __device__ __forceinline__ double block_sum(double v, double *smem)
+{
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) smem[wid] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x < 32) {
+        r = threadIdx.x < TPB / 32 ? smem[threadIdx.x] : 0.0;
+        r = warp_sum(r);
+    }
+    __syncthreads();
+    return r;
+}
+
+// Rotation matrix of a unit quaternion (s, v0, v1, v2), row-major, with the
+// reference's order of operations (quaternion.cpp:260-298).
+__device__ __forceinline__ void quat_rot(const double *q, double *R)
+{
+    const double s = q[0], a = q[1], b = q[2], c = q[3];
+    double R00 = 1.0, R11 = 1.0, R22 = 1.0;
+    double t = 2.0 * a * a;
+    R11 -= t; R22 -= t;
+    t = 2.0 * b * b;
+    R00 -= t; R22 -= t;
+    t = 2.0 * c * c;
+    R00 -= t; R11 -= t;
+    t = 2.0 * a * b;
+    double R10 = t, R01 = t;
+    t = 2.0 * a * c;
+    double R20 = t, R02 = t;
+    t = 2.0 * b * c;
+    double R12 = t, R21 = t;
+    t = 2.0 * s * c;
+    R10 += t; R01 -= t;
+    t = 2.0 * s * b;
+    R20 -= t; R02 += t;
+    t = 2.0 * s * a;
+    R21 += t; R12 -= t;
+    R[0] = R00; R[1] = R01; R[2] = R02;
+    R[3] = R10; R[4] = R11; R[5] = R12;
+    R[6] = R20; R[7] = R21; R[8] = R22;
+}
+
+__device__ __forceinline__ void rot_apply(const double *R, const double *v, double *o)
+{
+    o[0] = R[0] * v[0] + R[1] * v[1] + R[2] * v[2];
+    o[1] = R[3] * v[0] + R[4] * v[1] + R[5] * v[2];
+    o[2] = R[6] * v[0] + R[7] * v[1] + R[8] * v[2];
+}
+
+// ---------------------------------------------------------------------------
+// body kernels
+// ---------------------------------------------------------------------------
+// R per swimmer and the 6x6 reference matrices rotated block by block,
+// Q * block * Q^T (mobility_solver.cpp:660-677).
+__global__ void prepare_bodies_kernel(int W, const double *__restrict__ q, const double *__restrict__ ktk_ref,
+                                      const double *__restrict__ mob_ref, double *__restrict__ R,
+                                      double *__restrict__ ktk_rot, double *__restrict__ mob_rot)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= W) return;
+    double Rn[9];
+    quat_rot(q + 4 * n, Rn);
+    for (int k = 0; k < 9; ++k) R[9 * n + k] = Rn[k];
+    const double *src[2] = {ktk_ref, mob_ref};
+    double *dst[2] = {ktk_rot + 36 * n, mob_rot + 36 * n};
+    for (int m = 0; m < 2; ++m) {
+        for (int bi = 0; bi < 2; ++bi)
+            for (int bj = 0; bj < 2; ++bj) {
+                double A[9], T[9];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) A[3 * i + j] = src[m][(3 * bi + i) + 6 * (3 * bj + j)];
+                for (int i = 0; i < 3; ++i)  // T = R A
+                    for (int j = 0; j < 3; ++j)
+                        T[3 * i + j] = Rn[3 * i] * A[j] + Rn[3 * i + 1] * A[3 + j] + Rn[3 * i + 2] * A[6 + j];
+                for (int i = 0; i < 3; ++i)  // T R^T
+                    for (int j = 0; j < 3; ++j)
+                        dst[m][(3 * bi + i) + 6 * (3 * bj + j)] =
+                            T[3 * i] * Rn[3 * j] + T[3 * i + 1] * Rn[3 * j + 1] + T[3 * i + 2] * Rn[3 * j + 2];
+            }
+    }
+}
+
+// x_blob = X + R ref (rigid_body.cpp:334-352).
+__global__ void blob_positions_kernel(int W, int nblob, const double *__restrict__ bx, const double *__restrict__ R,
+                                      const double *__restrict__ refs, double *__restrict__ xb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * nblob) return;
+    const int n = i / nblob, m = i % nblob;
+    double d[3];
+    rot_apply(R + 9 * n, refs + 3 * m, d);
+    xb[3 * i] = bx[3 * n] + d[0];
+    xb[3 * i + 1] = bx[3 * n + 1] + d[1];
+    xb[3 * i + 2] = bx[3 * n + 2] + d[2];
+}
+
+// Per swimmer: sums[6n..] = (sum_m f_m, sum_m (R ref_m) x f_m) over its blobs.
+// This is K^T f (mobility_solver.cpp:690-697, 921-940, 168-188).
+__global__ void __launch_bounds__(kRedTpb) kt_sums_kernel(int nblob, const double *__restrict__ R,
+                                                          const double *__restrict__ refs,
+                                                          const double *__restrict__ f, double *__restrict__ sums)
+{
+    __shared__ double red[32];
+    const int n = blockIdx.x;
+    const double *Rn = R + 9 * n;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int m = threadIdx.x; m < nblob; m += kRedTpb) {
+        const double *fm = f + 3 * ((size_t)n * nblob + m);
+        double d[3];
+        rot_apply(Rn, refs + 3 * m, d);
+        a[0] += fm[0];
+        a[1] += fm[1];
+        a[2] += fm[2];
+        a[3] += d[1] * fm[2] - d[2] * fm[1];
+        a[4] += d[2] * fm[0] - d[0] * fm[2];
+        a[5] += d[0] * fm[1] - d[1] * fm[0];
+    }
+    for (int c = 0; c < 6; ++c) {
+        const double s = block_sum<kRedTpb>(a[c], red);
+        if (threadIdx.x == 0) sums[6 * n + c] = s;
+    }
+}
+
+// body_f += sums (the blob repulsion's force and torque on each body).
+__global__ void add_vec_kernel(int count, const double *__restrict__ a, double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) y[i] += a[i];
+}
+
+// rhs = [-v_blobs ; -body_f] (mobility_solver.cpp:363-419).
+__global__ void assemble_rhs_kernel(int nb3, int nw6, const double *__restrict__ vb, const double *__restrict__ bf,
+                                    double *__restrict__ rhs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nb3) rhs[i] = -vb[i];
+    else if (i < nb3 + nw6) rhs[i] = -bf[i - nb3];
+}
+
+// Preconditioner, body part (mobility_solver.cpp:653-697):
+// out_body = KTKinv_rot * b - mob_rot * in_body with b = -K^T in_blob.
+__global__ void precond_body_kernel(int W, const double *__restrict__ sums, const double *__restrict__ in_body,
+                                    const double *__restrict__ ktk_rot, const double *__restrict__ mob_rot,
+                                    double *__restrict__ out_body)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= W) return;
+    double b[6], u[6];
+    for (int c = 0; c < 6; ++c) {
+        b[c] = -sums[6 * n + c];
+        u[c] = in_body[6 * n + c];
+    }
+    const double *Kt = ktk_rot + 36 * n, *Mb = mob_rot + 36 * n;
+    for (int i = 0; i < 6; ++i) {
+        double x = 0.0, y = 0.0;
+        for (int j = 0; j < 6; ++j) {
+            x += Kt[i + 6 * j] * b[j];
+            y += Mb[i + 6 * j] * u[j];
+        }
+        out_body[6 * n + i] = x - y;
+    }
+}
+
+// Preconditioner, blob part (mobility_solver.cpp:699-719):
+// out_blob = Minv * (in_blob + U + Omega x (R ref)).  The reference scales
+// the whole blob block by Minv inside its loop over swimmers
+// (mobility_solver.cpp:718), so the blobs of swimmer n end up multiplied
+// by Minv (W - n) times; this kernel reproduces that.
+__global__ void precond_blob_kernel(int W, int nblob, const double *__restrict__ in_blob,
+                                    const double *__restrict__ out_body, const double *__restrict__ R,
+                                    const double *__restrict__ refs, double minv, double *__restrict__ out_blob)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * nblob) return;
+    const int n = i / nblob, m = i % nblob;
+    double d[3];
+    rot_apply(R + 9 * n, refs + 3 * m, d);
+    const double *U = out_body + 6 * n;
+    double o0 = in_blob[3 * i] + U[0], o1 = in_blob[3 * i + 1] + U[1], o2 = in_blob[3 * i + 2] + U[2];
+    o0 += U[4] * d[2] - U[5] * d[1];
+    o1 += U[5] * d[0] - U[3] * d[2];
+    o2 += U[3] * d[1] - U[4] * d[0];
+    for (int k = n; k < W; ++k) {
+        o0 *= minv;
+        o1 *= minv;
+        o2 *= minv;
+    }
+    out_blob[3 * i] = o0;
+    out_blob[3 * i + 1] = o1;
+    out_blob[3 * i + 2] = o2;
+}
+
+// System matrix, after the blob-blob apply (mobility_solver.cpp:905-960):
+// out_blob = -(U + Omega x (R ref)) + (M_bb in_blob), out_body = -K^T in_blob.
+__global__ void sysmult_finish_kernel(int W, int nblob, const double *__restrict__ mbb, const double *__restrict__ in_body,
+                                      const double *__restrict__ sums, const double *__restrict__ R,
+                                      const double *__restrict__ refs, double *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nb = W * nblob;
+    if (i < nb) {
+        const int n = i / nblob, m = i % nblob;
+        double d[3];
+        rot_apply(R + 9 * n, refs + 3 * m, d);
+        const double *U = in_body + 6 * n;
+        out[3 * i] = -(U[0] - d[1] * U[5] + d[2] * U[4]) + mbb[3 * i];
+        out[3 * i + 1] = -(U[1] - d[2] * U[3] + d[0] * U[5]) + mbb[3 * i + 1];
+        out[3 * i + 2] = -(U[2] - d[0] * U[4] + d[1] * U[3]) + mbb[3 * i + 2];
+    } else if (i < nb + 6 * W) {
+        out[3 * nb + (i - nb)] = -sums[i - nb];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Krylov kernels
+// ---------------------------------------------------------------------------
+// partial[i * nchunks + c] = sum over rows of chunk c of Q[:, i] . w
+__global__ void __launch_bounds__(kRedTpb) dot_partials_kernel(const double *__restrict__ Q, size_t ld,
+                                                               const double *__restrict__ w, int n, int nchunks,
+                                                               double *__restrict__ partial)
+{
+    __shared__ double red[32];
+    const int c = blockIdx.x, i = blockIdx.y;
+    const double *q = Q + ld * i;
+    double a = 0.0;
+    const int r0 = c * kChunkRows, r1 = min(n, r0 + kChunkRows);
+    for (int r = r0 + threadIdx.x; r < r1; r += kRedTpb) a += q[r] * w[r];
+    const double s = block_sum<kRedTpb>(a, red);
+    if (threadIdx.x == 0) partial[(size_t)i * nchunks + c] = s;
+}
+
+// Classical Gram-Schmidt update: h_i = sum_c partial[i][c]; w -= sum_i h_i Q[:, i];
+// block 0 adds h into the Hessenberg column (pass 0 stores, pass 1 adds).
+__global__ void __launch_bounds__(kRedTpb) cgs_update_kernel(const double *__restrict__ Q, size_t ld, int k,
+                                                             const double *__restrict__ partial, int nchunks,
+                                                             double *__restrict__ w, int n, double *__restrict__ Hcol,
+                                                             int pass)
+{
+    extern __shared__ double h[];
+    for (int i = threadIdx.x; i < k; i += kRedTpb) {
+        double s = 0.0;
+        for (int c = 0; c < nchunks; ++c) s += partial[(size_t)i * nchunks + c];
+        h[i] = s;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0)
+        for (int i = threadIdx.x; i < k; i += kRedTpb) Hcol[i] = pass == 0 ? h[i] : Hcol[i] + h[i];
+    const int r = blockIdx.x * kRedTpb + threadIdx.x;
+    if (r >= n) return;
+    double acc = w[r];
+    for (int i = 0; i < k; ++i) acc -= h[i] * Q[ld * i + r];
+    w[r] = acc;
+}
+
+// q_out = w / ||w|| with ||w|| from the partials; block 0 stores the norm at *hval.
+__global__ void normalize_kernel(const double *__restrict__ w, int n, const double *__restrict__ partial, int nchunks,
+                                 double *__restrict__ q_out, double *__restrict__ hval)
+{
+    __shared__ double nrm;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int c = 0; c < nchunks; ++c) s += partial[c];
+        nrm = sqrt(s);
+        if (blockIdx.x == 0 && hval) *hval = nrm;
+    }
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) q_out[r] = nrm > 0.0 ? w[r] / nrm : 0.0;
+}
+
+// sqrt of the summed partials into out[0] (norms of single vectors).
+__global__ void finish_norm_kernel(const double *__restrict__ partial, int nchunks, double *__restrict__ out)
+{
+    double s = 0.0;
+    for (int c = 0; c < nchunks; ++c) s += partial[c];
+    out[0] = sqrt(s);
+}
+
+// One Givens step of solve_linear_system (mobility_solver.cpp:1189-1231) on
+// column iter-1; writes |beta(iter)| / norm_rhs to *resid.
+__global__ void givens_kernel(double *__restrict__ H, int ldh, double *__restrict__ beta, double *__restrict__ cs,
+                              double *__restrict__ sn, int iter, double norm_rhs, double *__restrict__ resid)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double *col = H + (size_t)ldh * (iter - 1);
+    for (int i = 1; i < iter; ++i) {
+        const double t = cs[i - 1] * col[i - 1] + sn[i - 1] * col[i];
+        col[i] = cs[i - 1] * col[i] - sn[i - 1] * col[i - 1];
+        col[i - 1] = t;
+    }
+    const double hk = col[iter], hd = col[iter - 1];
+    double c, s;
+    if (hk == 0.0) {
+        c = 1.0;
+        s = 0.0;
+    } else if (fabs(hk) > fabs(hd)) {
+        const double t = hd / hk;
+        s = (2.0 * (double)(hk > 0) - 1.0) / sqrt(1.0 + t * t);
+        c = t * s;
+    } else {
+        const double t = hk / hd;
+        c = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + t * t);
+        s = t * c;
+    }
+    cs[iter - 1] = c;
+    sn[iter - 1] = s;
+    col[iter - 1] = c * hd + s * hk;
+    col[iter] = 0.0;
+    beta[iter] = -s * beta[iter - 1];
+    beta[iter - 1] = c * beta[iter - 1];
+    *resid = fabs(beta[iter]) / norm_rhs;
+}
+
+// Back substitution for y (mobility_solver.cpp:1236-1250).
+__global__ void backsolve_kernel(const double *__restrict__ H, int ldh, const double *__restrict__ beta, int iter,
+                                 double *__restrict__ y)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    y[iter - 1] = beta[iter - 1] / H[(size_t)ldh * (iter - 1) + (iter - 1)];
+    for (int i = iter - 2; i >= 0; --i) {
+        double v = beta[i];
+        for (int j = iter - 1; j > i; --j) v -= H[(size_t)ldh * j + i] * y[j];
+        y[i] = v / H[(size_t)ldh * i + i];
+    }
+}
+
+// out = sum_i y_i Q[:, i], in the reference's column order (mobility_solver.cpp:1252-1255).
+__global__ void combine_kernel(const double *__restrict__ Q, size_t ld, const double *__restrict__ y, int k, int n,
+                               double *__restrict__ out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double acc = 0.0;
+    for (int i = 0; i < k; ++i) acc += y[i] * Q[ld * i + r];
+    out[r] = acc;
+}
+
+__global__ void axpby_kernel(int n, double a, const double *__restrict__ x, double b, const double *__restrict__ y,
+                             double *__restrict__ out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) out[r] = a * x[r] + b * y[r];
+}
+
+__global__ void scale_kernel(int n, const double *__restrict__ x, const double *__restrict__ s, double *__restrict__ out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) out[r] = x[r] / s[0];
+}
+
+}  // namespace gmi
+
+// ---------------------------------------------------------------------------
+// solver object
+// ---------------------------------------------------------------------------
+struct gmi_solver {
+    gmi_context *ctx = nullptr;
+    gmi_solver_config cfg{};
+    int S = 0, B = 0, W = 0, n = 0, m = 0;
+    gmi_host_arrays h{};
+    double *h_stage = nullptr;   // pinned staging: body x, q, f, scalars
+    // device state
+    double *x_segs = nullptr, *f_segs = nullptr, *v_segs = nullptr;
+    double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
+    double *body_x = nullptr, *body_q = nullptr, *body_f = nullptr, *v_bodies = nullptr;
+    double *R = nullptr, *ktk_ref = nullptr, *mob_ref = nullptr, *ktk_rot = nullptr, *mob_rot = nullptr;
+    double *refs = nullptr, *sums = nullptr;
+    double *rhs = nullptr, *soln = nullptr, *Q = nullptr, *H = nullptr, *beta = nullptr, *cs = nullptr, *sn = nullptr;
+    double *z = nullptr, *w = nullptr, *tmp = nullptr, *mbb = nullptr, *partial = nullptr, *yv = nullptr;
+    double *scal = nullptr;  // device scalars: [0] norm, [1] resid
+    bool refs_set = false;
+    std::vector<void *> allocs;
+};
+
+namespace gmi {
+
+static inline int grid_for(int n, int tpb = 256) { return (n + tpb - 1) / tpb; }
+
+static gmi_status dalloc(gmi_solver *s, double **p, size_t count)
+{
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(p, count * sizeof(double));
+    if (e != cudaSuccess) {
+        set_last_error(cudaGetErrorString(e), "cudaMalloc", __FILE__, __LINE__);
+        return GMI_ERR_CUDA;
+    }
+    s->allocs.push_back(*p);
+    GMI_CUDA_TRY(cudaMemsetAsync(*p, 0, count * sizeof(double), s->ctx->stream));
+    return GMI_OK;
+}
+
+static gmi_status halloc(double **p, size_t count)
+{
+    if (count == 0) count = 1;
+    GMI_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void **>(p), count * sizeof(double), cudaHostAllocPortable));
+    std::memset(*p, 0, count * sizeof(double));
+    return GMI_OK;
+}
+
+#define GMI_TRY(expr)                  \
+    do {                               \
+        gmi_status gmi_s_ = (expr);    \
+        if (gmi_s_ != GMI_OK) return gmi_s_; \
+    } while (0)
+
+static gmi_status launched(gmi_solver *s, int kernels = 1)
+{
+    s->ctx->launches += kernels;
+    GMI_CUDA_TRY(cudaGetLastError());
+    return GMI_OK;
+}
+
+static gmi_status read_scalar(gmi_solver *s, const double *d_ptr, double *out)
+{
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->h_stage, d_ptr, sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream));
+    GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    *out = s->h_stage[0];
+    return GMI_OK;
+}
+
+static int nchunks_of(int n) { return (n + kChunkRows - 1) / kChunkRows; }
+
+// ||x|| into s->scal[0] (device); no host sync.
+static gmi_status device_norm(gmi_solver *s, const double *x, int n)
+{
+    const int nc = nchunks_of(n);
+    dot_partials_kernel<<<dim3(nc, 1), kRedTpb, 0, s->ctx->stream>>>(x, (size_t)n, x, n, nc, s->partial);
+    finish_norm_kernel<<<1, 1, 0, s->ctx->stream>>>(s->partial, nc, s->scal);
+    return launched(s, 2);
+}
+
+static gmi_status prepare_bodies(gmi_solver *s)
+{
+    if (s->W == 0) return GMI_OK;
+    prepare_bodies_kernel<<<grid_for(s->W, 64), 64, 0, s->ctx->stream>>>(s->W, s->body_q, s->ktk_ref, s->mob_ref,
+                                                                          s->R, s->ktk_rot, s->mob_rot);
+    return launched(s);
+}
+
+// K^T of the blob block of `vec` into s->sums.
+static gmi_status kt_sums(gmi_solver *s, const double *vec)
+{
+    kt_sums_kernel<<<s->W, kRedTpb, 0, s->ctx->stream>>>(s->cfg.nblob, s->R, s->refs, vec, s->sums);
+    return launched(s);
+}
+
+// out = P^-1 in (apply_preconditioner, right preconditioning)
+static gmi_status apply_preconditioner(gmi_solver *s, const double *in, double *out)
+{
+    const int nb = s->B;
+    GMI_TRY(kt_sums(s, in));
+    precond_body_kernel<<<grid_for(s->W, 64), 64, 0, s->ctx->stream>>>(s->W, s->sums, in + 3 * nb, s->ktk_rot,
+                                                                        s->mob_rot, out + 3 * nb);
+    const double minv = 6.0 * kPi * s->cfg.mu * s->cfg.rblob;
+    precond_blob_kernel<<<grid_for(nb), 256, 0, s->ctx->stream>>>(s->W, s->cfg.nblob, in, out + 3 * nb, s->R, s->refs,
+                                                                  minv, out);
+    return launched(s, 2);
+}
+
+// out = A in (system_matrix_mult): [M_bb, -K; -K^T, 0]
+static gmi_status system_matrix_mult(gmi_solver *s, const double *in, double *out)
+{
+    const int nb = s->B;
+    gmi_context *ctx = s->ctx;
+    GMI_TRY(pack_records(ctx, s->x_blobs, in, 3, nb, ctx->rec_src));
+    PairConsts k;
+    fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
+    GMI_TRY(launch_pair(ctx, kBB, ctx->rec_src.ptr, 0, nb, ctx->rec_src.ptr, nb, k, s->mbb, 0));
+    GMI_TRY(kt_sums(s, in));
+    sysmult_finish_kernel<<<grid_for(nb + 6 * s->W), 256, 0, ctx->stream>>>(s->W, s->cfg.nblob, s->mbb, in + 3 * nb,
+                                                                           s->sums, s->R, s->refs, out);
+    return launched(s);
+}
+
+// CGS2 orthogonalisation of w against Q[:, 0..k-1]; H column receives the
+// projections.  Then H(k, col) = ||w|| and Q[:, k] = w / ||w||.
+static gmi_status orthonormalise(gmi_solver *s, double *w, int k, double *Hcol)
+{
+    const int n = s->n, nc = nchunks_of(n);
+    const size_t ld = (size_t)n;
+    for (int pass = 0; pass < 2; ++pass) {
+        dot_partials_kernel<<<dim3(nc, k), kRedTpb, 0, s->ctx->stream>>>(s->Q, ld, w, n, nc, s->partial);
+        cgs_update_kernel<<<grid_for(n, kRedTpb), kRedTpb, k * sizeof(double), s->ctx->stream>>>(
+            s->Q, ld, k, s->partial, nc, w, n, Hcol, pass);
+        GMI_TRY(launched(s, 2));
+    }
+    dot_partials_kernel<<<dim3(nc, 1), kRedTpb, 0, s->ctx->stream>>>(w, ld, w, n, nc, s->partial);
+    normalize_kernel<<<grid_for(n), 256, 0, s->ctx->stream>>>(w, n, s->partial, nc, s->Q + ld * k, Hcol + k);
+    return launched(s, 2);
+}
+
+// solve_linear_system (mobility_solver.cpp:970-1354), right preconditioned,
+// warm started from (f_blobs, v_bodies).  rhs must already be in s->rhs.
+static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
+{
+    const int n = s->n, nb = s->B;
+    const size_t ld = (size_t)n;
+    const double tol = s->cfg.linear_tol;
+    cudaStream_t st = s->ctx->stream;
+    *iters_out = 0;
+    GMI_TRY(device_norm(s, s->rhs, n));
+    double norm_rhs;
+    GMI_TRY(read_scalar(s, s->scal, &norm_rhs));
+    if (!std::isfinite(norm_rhs)) {
+        set_last_error_msg("non-finite right-hand side in the linear solve");
+        return GMI_ERR_NONFINITE;
+    }
+    if (norm_rhs == 0.0) {
+        GMI_CUDA_TRY(cudaMemsetAsync(s->f_blobs, 0, 3 * (size_t)nb * sizeof(double), st));
+        GMI_CUDA_TRY(cudaMemsetAsync(s->v_bodies, 0, 6 * (size_t)s->W * sizeof(double), st));
+        return GMI_OK;
+    }
+    // warm start soln = [f_blobs ; v_bodies]
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->soln, s->f_blobs, 3 * (size_t)nb * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->soln + 3 * nb, s->v_bodies, 6 * (size_t)s->W * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, st));
+    GMI_TRY(system_matrix_mult(s, s->soln, s->tmp));
+    axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->rhs, -1.0, s->tmp, s->w);
+    GMI_TRY(launched(s));
+    GMI_TRY(device_norm(s, s->w, n));
+    double beta0;
+    GMI_TRY(read_scalar(s, s->scal, &beta0));
+    if (fabs(beta0) <= tol * norm_rhs) return GMI_OK;  // warm start already good enough
+    if (fabs(beta0) > norm_rhs) {
+        GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->w, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        beta0 = norm_rhs;
+    }
+    s->h_stage[0] = beta0;
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->beta, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
+    scale_kernel<<<grid_for(n), 256, 0, st>>>(n, s->w, s->scal, s->Q);
+    GMI_TRY(launched(s));
+    const int max_iter = n < s->m ? n : s->m;
+    const int ldh = s->m + 1;
+    for (int iter = 1; iter <= max_iter; ++iter) {
+        GMI_TRY(apply_preconditioner(s, s->Q + ld * (iter - 1), s->z));
+        GMI_TRY(system_matrix_mult(s, s->z, s->w));
+        double *Hcol = s->H + (size_t)ldh * (iter - 1);
+        GMI_TRY(orthonormalise(s, s->w, iter, Hcol));
+        givens_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, s->cs, s->sn, iter, norm_rhs, s->scal + 1);
+        GMI_TRY(launched(s));
+        double resid;
+        GMI_TRY(read_scalar(s, s->scal + 1, &resid));
+        if (!std::isfinite(resid)) {
+            set_last_error_msg("GMRES produced a non-finite residual");
+            return GMI_ERR_NONFINITE;
+        }
+        if (resid <= tol || iter == max_iter) {
+            backsolve_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
+            combine_kernel<<<grid_for(n), 256, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
+            GMI_TRY(launched(s, 2));
+            GMI_TRY(apply_preconditioner(s, s->tmp, s->z));
+            axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->soln, 1.0, s->z, s->soln);
+            GMI_TRY(launched(s));
+            GMI_CUDA_TRY(cudaMemcpyAsync(s->f_blobs, s->soln, 3 * (size_t)nb * sizeof(double),
+                                         cudaMemcpyDeviceToDevice, st));
+            GMI_CUDA_TRY(cudaMemcpyAsync(s->v_bodies, s->soln + 3 * nb, 6 * (size_t)s->W * sizeof(double),
+                                         cudaMemcpyDeviceToDevice, st));
+            *iters_out = iter;
+            return GMI_OK;
+        }
+    }
+    return GMI_OK;
+}
+
+// read_positions_and_forces (mobility_solver.cpp:132-192) minus the host
+// copies: segment arrays already on the device, body state staged.
+static gmi_status positions_and_barrier(gmi_solver *s)
+{
+    gmi_context *ctx = s->ctx;
+    GMI_TRY(prepare_bodies(s));
+    if (s->B > 0) {
+        blob_positions_kernel<<<grid_for(s->B), 256, 0, ctx->stream>>>(s->W, s->cfg.nblob, s->body_x, s->R, s->refs,
+                                                                        s->x_blobs);
+        GMI_TRY(launched(s));
+    }
+    BarrierLaunch a{};
+    a.f_segs = s->f_segs;
+    a.f_blobs_rep = s->f_rep;
+    a.xs = s->x_segs;
+    a.xb = s->x_blobs;
+    a.S = s->S;
+    a.B = s->B;
+    a.start_seg = 0;
+    a.num_segs = s->S;
+    a.start_blob = 0;
+    a.num_blobs = s->B;
+    a.nseg = s->cfg.nseg;
+    a.rseg = s->cfg.rseg;
+    a.rblob = s->cfg.rblob;
+    a.scale = s->cfg.repulsive_force_factor * s->cfg.end_force_magnitude;
+    a.wall = s->cfg.wall;
+    return launch_barrier(ctx, a);
+}
+
+static gmi_status stage_bodies(gmi_solver *s, const double *bx, const double *bq)
+{
+    const int W = s->W;
+    if (W == 0) return GMI_OK;
+    std::memcpy(s->h_stage + 8, bx, 3 * W * sizeof(double));
+    std::memcpy(s->h_stage + 8 + 3 * W, bq, 4 * W * sizeof(double));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->body_x, s->h_stage + 8, 3 * W * sizeof(double), cudaMemcpyHostToDevice,
+                                 s->ctx->stream));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->body_q, s->h_stage + 8 + 3 * W, 4 * W * sizeof(double), cudaMemcpyHostToDevice,
+                                 s->ctx->stream));
+    // the staging area is reused by the next call: make sure these copies have read it
+    GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return GMI_OK;
+}
+
+static gmi_status seg_pair(gmi_solver *s, int kind)
+{
+    gmi_context *ctx = s->ctx;
+    PairConsts k;
+    if (kind == kSS) {
+        GMI_TRY(pack_records(ctx, s->x_segs, s->f_segs, 6, s->S, ctx->rec_src));
+        fill_consts(k, s->cfg.rseg, s->cfg.rseg, s->cfg.rseg, s->cfg.mu);
+        return launch_pair(ctx, s->cfg.wall ? kSSWall : kSS, ctx->rec_src.ptr, 0, s->S, ctx->rec_src.ptr, s->S, k,
+                           s->v_segs, 0);
+    }
+    if (kind == kBS) {
+        GMI_TRY(pack_records(ctx, s->x_blobs, nullptr, 0, s->B, ctx->rec_tgt));
+        GMI_TRY(pack_records(ctx, s->x_segs, s->f_segs, 6, s->S, ctx->rec_src));
+        fill_consts(k, s->cfg.rseg, s->cfg.rseg, s->cfg.rblob, s->cfg.mu);
+        return launch_pair(ctx, kBS, ctx->rec_tgt.ptr, 0, s->B, ctx->rec_src.ptr, s->S, k, s->v_blobs, 0);
+    }
+    if (kind == kSB) {
+        GMI_TRY(pack_records(ctx, s->x_segs, nullptr, 0, s->S, ctx->rec_tgt));
+        GMI_TRY(pack_records(ctx, s->x_blobs, s->f_blobs, 3, s->B, ctx->rec_src));
+        fill_consts(k, s->cfg.rseg, s->cfg.rseg, s->cfg.rblob, s->cfg.mu);
+        return launch_pair(ctx, kSB, ctx->rec_tgt.ptr, 0, s->S, ctx->rec_src.ptr, s->B, k, s->v_segs, 1);
+    }
+    GMI_TRY(pack_records(ctx, s->x_blobs, s->f_blobs, 3, s->B, ctx->rec_src));
+    fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
+    return launch_pair(ctx, kBB, ctx->rec_src.ptr, 0, s->B, ctx->rec_src.ptr, s->B, k, s->v_blobs, 0);
+}
+
+static gmi_status h2d(gmi_solver *s, double *d, const double *h, size_t count)
+{
+    if (count == 0) return GMI_OK;
+    GMI_CUDA_TRY(cudaMemcpyAsync(d, h, count * sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream));
+    return GMI_OK;
+}
+
+static gmi_status d2h(gmi_solver *s, double *h, const double *d, size_t count)
+{
+    if (count == 0) return GMI_OK;
+    GMI_CUDA_TRY(cudaMemcpyAsync(h, d, count * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream));
+    return GMI_OK;
+}
+
+// 6x6 inverse by Gauss-Jordan with partial pivoting (column-major), the
+// reference's matrix::invert (LAPACK dgetrf + dgetri, matrix.cpp:538-571).
+static bool invert6(const double *A, double *Ainv)
+{
+    double M[6][12];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            M[i][j] = A[i + 6 * j];
+            M[i][6 + j] = i == j ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 6; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 6; ++r)
+            if (std::fabs(M[r][c]) > std::fabs(M[p][c])) p = r;
+        if (M[p][c] == 0.0) return false;
+        if (p != c)
+            for (int j = 0; j < 12; ++j) std::swap(M[c][j], M[p][j]);
+        const double d = M[c][c];
+        for (int j = 0; j < 12; ++j) M[c][j] /= d;
+        for (int r = 0; r < 6; ++r)
+            if (r != c) {
+                const double f = M[r][c];
+                if (f != 0.0)
+                    for (int j = 0; j < 12; ++j) M[r][j] -= f * M[c][j];
+            }
+    }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) Ainv[i + 6 * j] = M[i][6 + j];
+    return true;
+}
+
+}  // namespace gmi
+
+using namespace gmi;
+
+#define GMI_ARG_CHECK(cond, msg)     \
+    do {                             \
+        if (!(cond)) {               \
+            set_last_error_msg(msg); \
+            return GMI_ERR_ARG;      \
+        }                            \
+    } while (0)
+
+extern "C" {
+
+gmi_status gmi_solver_destroy(gmi_solver *s)
+{
+    if (s == nullptr) return GMI_OK;
+    if (s->ctx) {
+        cudaSetDevice(s->ctx->device);
+        cudaStreamSynchronize(s->ctx->stream);
+    }
+    for (void *p : s->allocs) cudaFree(p);
+    double *hp[] = {s->h.v_segs_host, s->h.v_blobs_host, s->h.x_segs_host, s->h.x_blobs_host, s->h.f_segs_host,
+                    s->h.f_blobs_host, s->h.f_blobs_repulsion_host, s->h_stage};
+    for (double *p : hp)
+        if (p) cudaFreeHost(p);
+    if (s->ctx) gmi_context_destroy(s->ctx);
+    delete s;
+    return GMI_OK;
+}
+
+gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
+{
+    GMI_ARG_CHECK(cfg && out, "gmi_solver_create: null argument");
+    *out = nullptr;
+    GMI_ARG_CHECK(cfg->nswim >= 1 && cfg->nfil >= 0 && cfg->nseg >= 1 && cfg->nblob >= 0,
+                  "gmi_solver_create: sizes must satisfy nswim >= 1, nfil >= 0, nseg >= 1, nblob >= 0");
+    GMI_ARG_CHECK(cfg->mu > 0 && cfg->rseg > 0 && cfg->rblob > 0, "gmi_solver_create: mu and radii must be positive");
+    GMI_ARG_CHECK(!cfg->wall || (cfg->nblob == 0 && cfg->nswim == 1),
+                  "gmi_solver_create: the wall configuration has one swimmer and no blobs (config.hpp:222-226)");
+    GMI_ARG_CHECK(cfg->wall || cfg->nblob > 0,
+                  "gmi_solver_create: free-swimming bodies need blobs (the linear system is empty otherwise)");
+    GMI_ARG_CHECK(cfg->precision == GMI_FP64 || cfg->precision == GMI_FP32C, "gmi_solver_create: bad precision");
+    gmi_solver *s = new (std::nothrow) gmi_solver();
+    GMI_ARG_CHECK(s != nullptr, "gmi_solver_create: out of host memory");
+    s->cfg = *cfg;
+    if (s->cfg.max_linear_iter <= 0) s->cfg.max_linear_iter = 150;
+    if (s->cfg.linear_tol <= 0) s->cfg.linear_tol = 1e-10;
+    gmi_status st = gmi_context_create(cfg->device, &s->ctx);
+    if (st != GMI_OK) {
+        gmi_solver_destroy(s);
+        return st;
+    }
+    s->ctx->precision = cfg->precision;
+    s->W = cfg->nswim;
+    s->S = cfg->nswim * cfg->nfil * cfg->nseg;
+    s->B = cfg->nswim * cfg->nblob;
+    s->n = cfg->wall ? 0 : 3 * s->B + 6 * s->W;
+    s->m = s->cfg.max_linear_iter;
+    const size_t S = s->S, B = s->B, W = s->W, n = s->n, m = s->m;
+#define TRY_OR_DIE(expr)            \
+    do {                            \
+        st = (expr);                \
+        if (st != GMI_OK) {         \
+            gmi_solver_destroy(s);  \
+            return st;              \
+        }                           \
+    } while (0)
+    TRY_OR_DIE(halloc(&s->h.v_segs_host, 6 * S));
+    TRY_OR_DIE(halloc(&s->h.v_blobs_host, 3 * B));
+    TRY_OR_DIE(halloc(&s->h.x_segs_host, 3 * S));
+    TRY_OR_DIE(halloc(&s->h.x_blobs_host, 3 * B));
+    TRY_OR_DIE(halloc(&s->h.f_segs_host, 6 * S));
+    TRY_OR_DIE(halloc(&s->h.f_blobs_host, 3 * B));
+    TRY_OR_DIE(halloc(&s->h.f_blobs_repulsion_host, 3 * B));
+    TRY_OR_DIE(halloc(&s->h_stage, 16 + 16 * W));
+    TRY_OR_DIE(dalloc(s, &s->x_segs, 3 * S));
+    TRY_OR_DIE(dalloc(s, &s->f_segs, 6 * S));
+    TRY_OR_DIE(dalloc(s, &s->v_segs, 6 * S));
+    TRY_OR_DIE(dalloc(s, &s->x_blobs, 3 * B));
+    TRY_OR_DIE(dalloc(s, &s->f_blobs, 3 * B));
+    TRY_OR_DIE(dalloc(s, &s->v_blobs, 3 * B));
+    TRY_OR_DIE(dalloc(s, &s->f_rep, 3 * B));
+    TRY_OR_DIE(dalloc(s, &s->body_x, 3 * W));
+    TRY_OR_DIE(dalloc(s, &s->body_q, 4 * W));
+    TRY_OR_DIE(dalloc(s, &s->body_f, 6 * W));
+    TRY_OR_DIE(dalloc(s, &s->v_bodies, 6 * W));
+    TRY_OR_DIE(dalloc(s, &s->R, 9 * W));
+    TRY_OR_DIE(dalloc(s, &s->ktk_ref, 36));
+    TRY_OR_DIE(dalloc(s, &s->mob_ref, 36));
+    TRY_OR_DIE(dalloc(s, &s->ktk_rot, 36 * W));
+    TRY_OR_DIE(dalloc(s, &s->mob_rot, 36 * W));
+    TRY_OR_DIE(dalloc(s, &s->refs, 3 * (size_t)cfg->nblob));
+    TRY_OR_DIE(dalloc(s, &s->sums, 6 * W));
+    TRY_OR_DIE(dalloc(s, &s->scal, 8));
+    if (n > 0) {
+        TRY_OR_DIE(dalloc(s, &s->rhs, n));
+        TRY_OR_DIE(dalloc(s, &s->soln, n));
+        TRY_OR_DIE(dalloc(s, &s->Q, n * (m + 1)));
+        TRY_OR_DIE(dalloc(s, &s->H, (m + 1) * (m + 1)));
+        TRY_OR_DIE(dalloc(s, &s->beta, m + 1));
+        TRY_OR_DIE(dalloc(s, &s->cs, m));
+        TRY_OR_DIE(dalloc(s, &s->sn, m));
+        TRY_OR_DIE(dalloc(s, &s->yv, m + 1));
+        TRY_OR_DIE(dalloc(s, &s->z, n));
+        TRY_OR_DIE(dalloc(s, &s->w, n));
+        TRY_OR_DIE(dalloc(s, &s->tmp, n));
+        TRY_OR_DIE(dalloc(s, &s->mbb, 3 * B));
+        TRY_OR_DIE(dalloc(s, &s->partial, (size_t)nchunks_of((int)n) * (m + 1)));
+    }
+    // reference matrices start as identities (mobility_solver.cpp:85-88)
+    double I6[36] = {0};
+    for (int i = 0; i < 6; ++i) I6[i + 6 * i] = 1.0;
+    TRY_OR_DIE(gmi_solver_set_body_reference_matrices(s, I6, I6));
+    st = context_check_device_errors(s->ctx);
+    if (st != GMI_OK) {
+        gmi_solver_destroy(s);
+        return st;
+    }
+#undef TRY_OR_DIE
+    *out = s;
+    return GMI_OK;
+}
+
+gmi_status gmi_solver_host_arrays(gmi_solver *s, gmi_host_arrays *out)
+{
+    GMI_ARG_CHECK(s && out, "gmi_solver_host_arrays: null argument");
+    *out = s->h;
+    return GMI_OK;
+}
+
+gmi_context *gmi_solver_context(gmi_solver *s) { return s ? s->ctx : nullptr; }
+
+#define SOLVER_ENTRY(s)                                          \
+    GMI_ARG_CHECK((s) != nullptr, "null solver");                \
+    GMI_CUDA_TRY(cudaSetDevice((s)->ctx->device))
+
+gmi_status gmi_solver_copy_segment_positions_to_device(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return h2d(s, s->x_segs, s->h.x_segs_host, 3 * (size_t)s->S);
+}
+gmi_status gmi_solver_copy_segment_forces_to_device(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return h2d(s, s->f_segs, s->h.f_segs_host, 6 * (size_t)s->S);
+}
+gmi_status gmi_solver_copy_blob_positions_to_device(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return h2d(s, s->x_blobs, s->h.x_blobs_host, 3 * (size_t)s->B);
+}
+gmi_status gmi_solver_copy_blob_forces_to_device(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return h2d(s, s->f_blobs, s->h.f_blobs_host, 3 * (size_t)s->B);
+}
+gmi_status gmi_solver_copy_interparticle_blob_forces_to_host(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return d2h(s, s->h.f_blobs_repulsion_host, s->f_rep, 3 * (size_t)s->B);
+}
+gmi_status gmi_solver_copy_blob_velocities_to_host(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return d2h(s, s->h.v_blobs_host, s->v_blobs, 3 * (size_t)s->B);
+}
+gmi_status gmi_solver_copy_segment_velocities_to_host(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return d2h(s, s->h.v_segs_host, s->v_segs, 6 * (size_t)s->S);
+}
+gmi_status gmi_solver_apply_interparticle_forces(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    BarrierLaunch a{};
+    a.f_segs = s->f_segs;
+    a.f_blobs_rep = s->f_rep;
+    a.xs = s->x_segs;
+    a.xb = s->x_blobs;
+    a.S = s->S;
+    a.B = s->B;
+    a.num_segs = s->S;
+    a.num_blobs = s->B;
+    a.nseg = s->cfg.nseg;
+    a.rseg = s->cfg.rseg;
+    a.rblob = s->cfg.rblob;
+    a.scale = s->cfg.repulsive_force_factor * s->cfg.end_force_magnitude;
+    a.wall = s->cfg.wall;
+    return launch_barrier(s->ctx, a);
+}
+gmi_status gmi_solver_wait_for_device(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return context_check_device_errors(s->ctx);
+}
+gmi_status gmi_solver_evaluate_segment_segment_mobility(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return seg_pair(s, kSS);
+}
+gmi_status gmi_solver_evaluate_segment_blob_mobility(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return seg_pair(s, kSB);
+}
+gmi_status gmi_solver_evaluate_blob_blob_mobility(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return seg_pair(s, kBB);
+}
+gmi_status gmi_solver_evaluate_blob_segment_mobility(gmi_solver *s)
+{
+    SOLVER_ENTRY(s);
+    return seg_pair(s, kBS);
+}
+
+gmi_status gmi_solver_set_blob_references(gmi_solver *s, const double *refs)
+{
+    SOLVER_ENTRY(s);
+    const int nblob = s->cfg.nblob;
+    GMI_ARG_CHECK(nblob == 0 || refs != nullptr, "gmi_solver_set_blob_references: null references");
+    if (nblob > 0) {
+        GMI_CUDA_TRY(cudaMemcpy(s->refs, refs, 3 * (size_t)nblob * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    s->refs_set = true;
+    return GMI_OK;
+}
+
+gmi_status gmi_solver_set_body_reference_matrices(gmi_solver *s, const double *ktkinv, const double *mob)
+{
+    SOLVER_ENTRY(s);
+    GMI_ARG_CHECK(ktkinv && mob, "gmi_solver_set_body_reference_matrices: null argument");
+    GMI_CUDA_TRY(cudaMemcpy(s->ktk_ref, ktkinv, 36 * sizeof(double), cudaMemcpyHostToDevice));
+    GMI_CUDA_TRY(cudaMemcpy(s->mob_ref, mob, 36 * sizeof(double), cudaMemcpyHostToDevice));
+    return GMI_OK;
+}
+
+gmi_status gmi_solver_get_v_bodies(gmi_solver *s, double *v)
+{
+    SOLVER_ENTRY(s);
+    GMI_ARG_CHECK(v != nullptr, "gmi_solver_get_v_bodies: null output");
+    GMI_CUDA_TRY(cudaMemcpyAsync(v, s->v_bodies, 6 * (size_t)s->W * sizeof(double), cudaMemcpyDeviceToHost,
+                                 s->ctx->stream));
+    return context_check_device_errors(s->ctx);
+}
+
+gmi_status gmi_solver_set_v_bodies(gmi_solver *s, const double *v)
+{
+    SOLVER_ENTRY(s);
+    GMI_ARG_CHECK(v != nullptr, "gmi_solver_set_v_bodies: null input");
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->v_bodies, v, 6 * (size_t)s->W * sizeof(double), cudaMemcpyHostToDevice,
+                                 s->ctx->stream));
+    return context_check_device_errors(s->ctx);
+}
+
+gmi_status gmi_solver_compute_velocities(gmi_solver *s, const double *body_x, const double *body_q, double *body_f,
+                                         int *num_gmres_iterations)
+{
+    SOLVER_ENTRY(s);
+    const int W = s->W, S = s->S, B = s->B;
+    GMI_ARG_CHECK(s->cfg.wall || (body_x && body_q && body_f), "gmi_solver_compute_velocities: null body state");
+    GMI_ARG_CHECK(s->cfg.wall || B == 0 || s->refs_set,
+                  "gmi_solver_compute_velocities: blob references not set (gmi_solver_set_blob_references)");
+    cudaStream_t st = s->ctx->stream;
+    int iters = 0;
+    GMI_TRY(h2d(s, s->x_segs, s->h.x_segs_host, 3 * (size_t)S));
+    GMI_TRY(h2d(s, s->f_segs, s->h.f_segs_host, 6 * (size_t)S));
+    if (s->cfg.wall) {
+        GMI_TRY(positions_and_barrier(s));
+        GMI_TRY(seg_pair(s, kSS));
+        GMI_TRY(d2h(s, s->h.v_segs_host, s->v_segs, 6 * (size_t)S));
+        if (num_gmres_iterations) *num_gmres_iterations = 0;
+        return context_check_device_errors(s->ctx);
+    }
+    GMI_TRY(stage_bodies(s, body_x, body_q));
+    std::memcpy(s->h_stage + 8, body_f, 6 * W * sizeof(double));
+    GMI_TRY(h2d(s, s->body_f, s->h_stage + 8, 6 * (size_t)W));
+    GMI_TRY(positions_and_barrier(s));
+    if (B > 0) {
+        GMI_TRY(kt_sums(s, s->f_rep));
+        add_vec_kernel<<<grid_for(6 * W), 256, 0, st>>>(6 * W, s->sums, s->body_f);
+        GMI_TRY(launched(s));
+    }
+    GMI_TRY(seg_pair(s, kSS));
+    GMI_TRY(seg_pair(s, kBS));
+    assemble_rhs_kernel<<<grid_for(s->n), 256, 0, st>>>(3 * B, 6 * W, s->v_blobs, s->body_f, s->rhs);
+    GMI_TRY(launched(s));
+    GMI_TRY(solve_linear_system(s, &iters));
+    GMI_TRY(seg_pair(s, kSB));
+    GMI_TRY(d2h(s, s->h.v_segs_host, s->v_segs, 6 * (size_t)S));
+    GMI_TRY(d2h(s, s->h.f_blobs_host, s->f_blobs, 3 * (size_t)B));
+    GMI_TRY(d2h(s, s->h.x_blobs_host, s->x_blobs, 3 * (size_t)B));
+    GMI_TRY(d2h(s, s->h.f_blobs_repulsion_host, s->f_rep, 3 * (size_t)B));
+    GMI_TRY(d2h(s, s->h.v_blobs_host, s->v_blobs, 3 * (size_t)B));
+    GMI_TRY(d2h(s, s->h_stage + 8, s->body_f, 6 * (size_t)W));
+    GMI_TRY(context_check_device_errors(s->ctx));
+    std::memcpy(body_f, s->h_stage + 8, 6 * W * sizeof(double));
+    if (num_gmres_iterations) *num_gmres_iterations = iters;
+    return GMI_OK;
+}
+
+gmi_status gmi_solver_make_body_reference_matrices(gmi_solver *s, const double *body_x, const double *body_q,
+                                                   double *ktkinv_out, double *mob_out)
+{
+    SOLVER_ENTRY(s);
+    GMI_ARG_CHECK(!s->cfg.wall, "gmi_solver_make_body_reference_matrices: not used with the wall configuration");
+    GMI_ARG_CHECK(body_x && body_q, "gmi_solver_make_body_reference_matrices: null body state");
+    GMI_ARG_CHECK(s->refs_set, "gmi_solver_make_body_reference_matrices: blob references not set");
+    const int W = s->W, nblob = s->cfg.nblob, B = s->B;
+    // (K^T K) from the references (mobility_solver.cpp:1697-1713), inverted on the host
+    std::vector<double> refs(3 * (size_t)nblob);
+    if (nblob > 0)
+        GMI_CUDA_TRY(cudaMemcpy(refs.data(), s->refs, refs.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    double KTK[36] = {0};
+    KTK[0] = KTK[7] = KTK[14] = (double)nblob;
+    for (int m = 0; m < nblob; ++m) {
+        const double *r = &refs[3 * m];
+        const double rc[9] = {0.0, -r[2], r[1], r[2], 0.0, -r[0], -r[1], r[0], 0.0};  // row-major rcross
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                KTK[i + 6 * (3 + j)] += rc[3 * i + j];
+                KTK[(3 + i) + 6 * j] -= rc[3 * i + j];
+                double rr = 0.0;
+                for (int k = 0; k < 3; ++k) rr += rc[3 * i + k] * rc[3 * k + j];
+                KTK[(3 + i) + 6 * (3 + j)] -= rr;
+            }
+    }
+    double KTKinv[36];
+    if (!invert6(KTK, KTKinv)) {
+        set_last_error_msg("K^T K is singular (are the blob references set?)");
+        return GMI_ERR_NONFINITE;
+    }
+    double mob[36] = {0};
+    for (int i = 0; i < 6; ++i) mob[i + 6 * i] = 1.0;
+    GMI_TRY(gmi_solver_set_body_reference_matrices(s, KTKinv, mob));
+    // all swimmers but the last moved far away (mobility_solver.cpp:1721-1731)
+    std::vector<double> bx(body_x, body_x + 3 * W);
+    const double shift = 1e10 * 2.2 * s->cfg.rseg * s->cfg.nseg;
+    for (int n = 0; n < W - 1; ++n)
+        for (int c = 0; c < 3; ++c) bx[3 * n + c] += shift;
+    GMI_TRY(h2d(s, s->x_segs, s->h.x_segs_host, 3 * (size_t)s->S));
+    GMI_TRY(h2d(s, s->f_segs, s->h.f_segs_host, 6 * (size_t)s->S));
+    GMI_TRY(stage_bodies(s, bx.data(), body_q));
+    GMI_TRY(positions_and_barrier(s));
+    for (int col = 0; col < 6; ++col) {
+        GMI_CUDA_TRY(cudaMemsetAsync(s->rhs, 0, (size_t)s->n * sizeof(double), s->ctx->stream));
+        s->h_stage[0] = -1.0;
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->rhs + (s->n - 1 - col), s->h_stage, sizeof(double), cudaMemcpyHostToDevice,
+                                     s->ctx->stream));
+        GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+        int iters = 0;
+        GMI_TRY(solve_linear_system(s, &iters));
+        double vb[6];
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->h_stage, s->v_bodies + 6 * (W - 1), 6 * sizeof(double),
+                                     cudaMemcpyDeviceToHost, s->ctx->stream));
+        GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
+        std::memcpy(vb, s->h_stage, sizeof vb);
+        for (int i = 0; i < 6; ++i) mob[i + 6 * (5 - col)] = vb[i];
+        // the preconditioner of the next solve sees the updated column
+        GMI_TRY(gmi_solver_set_body_reference_matrices(s, KTKinv, mob));
+        GMI_TRY(prepare_bodies(s));
+    }
+    (void)B;
+    if (ktkinv_out) std::memcpy(ktkinv_out, KTKinv, sizeof KTKinv);
+    if (mob_out) std::memcpy(mob_out, mob, sizeof mob);
+    return context_check_device_errors(s->ctx);
+}
+
+}  // extern "C"

@@ -131,3 +131,10 @@ class Context:
 
     def autotune(self, kind: int, num_targets: int, num_sources: int) -> None:
         check(self.lib.gmi_autotune(self.handle, kind, num_targets, num_sources))
+
+    def tuned_shape(self, kind: int, num_targets: int, num_sources: int):
+        """(threads per CTA, targets per thread, source splits, tuned?)."""
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        st = self.lib.gmi_tuned_shape(self.handle, kind, num_targets, num_sources, ctypes.byref(a),
+                                      ctypes.byref(b), ctypes.byref(c))
+        return a.value, b.value, c.value, st == 0

@@ -122,6 +122,105 @@ GMI_API gmi_status gmi_barrier_forces(gmi_context *ctx, double *f_segs_d, double
  * given sizes on the context's GPU and keep the fastest for later calls.
  * kind: 0 = ss, 1 = ss wall, 2 = bb, 3 = sb, 4 = bs. */
 GMI_API gmi_status gmi_autotune(gmi_context *ctx, int kind, int num_targets, int num_sources);
+/* The launch shape the context will use for this kernel and size:
+ * threads per CTA, targets per thread, source splits (0 = automatic).
+ * Returns GMI_ERR_STATE if the size was never tuned (defaults apply). */
+GMI_API gmi_status gmi_tuned_shape(const gmi_context *ctx, int kind, int num_targets, int num_sources,
+                                   int *threads_per_cta, int *targets_per_thread, int *source_splits);
+
+/* ------------------------------------------------------------------------
+ * Mobility solver: the device-resident replacement of the reference's
+ * rpy_mobility_solver plus the generic mobility_solver methods that drive it
+ * (mobility_solver.hpp:18-102).  One solver couples nswim swimmers, each a
+ * rigid body of nblob blobs with nfil filaments of nseg segments, exactly as
+ * the reference's NSWIM/NFIL/NSEG/NBLOB macros do (config.hpp:95-98).
+ * ---------------------------------------------------------------------- */
+typedef struct gmi_solver gmi_solver;
+
+typedef struct gmi_solver_config {
+    int nswim, nfil, nseg, nblob;       /* NSWIM NFIL NSEG NBLOB */
+    double mu, rseg, rblob;             /* MU RSEG RBLOB */
+    double repulsive_force_factor;      /* REPULSIVE_FORCE_FACTOR */
+    double end_force_magnitude;         /* END_FORCE_MAGNITUDE */
+    int wall;                           /* INFINITE_PLANE_WALL (then nblob = 0) */
+    int max_linear_iter;                /* MAX_LINEAR_SYSTEM_ITER (<= 0: 150) */
+    double linear_tol;                  /* LINEAR_SYSTEM_TOL (<= 0: 1e-10) */
+    int precision;                      /* pair-sum precision, gmi_precision */
+    int device;
+} gmi_solver_config;
+
+/* The solver-owned pinned host arrays the filament and body code reads and
+ * writes in place (mobility_solver.hpp:54-60; allocated with
+ * cudaHostAlloc(..., cudaHostAllocPortable) as rpy_mobility_solver.cu:65-71). */
+typedef struct gmi_host_arrays {
+    double *v_segs_host;            /* [6*S] */
+    double *v_blobs_host;           /* [3*B] */
+    double *x_segs_host;            /* [3*S] */
+    double *x_blobs_host;           /* [3*B] */
+    double *f_segs_host;            /* [6*S] */
+    double *f_blobs_host;           /* [3*B] */
+    double *f_blobs_repulsion_host; /* [3*B] */
+} gmi_host_arrays;
+
+/* allocate_host_memory + allocate_device_memory + mobility_solver::initialise
+ * (rpy_mobility_solver.cu:55-115, mobility_solver.cpp:22-130): zeroes the
+ * blob forces (the first GMRES warm start) and v_bodies. */
+GMI_API gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out);
+/* free_host_memory + free_device_memory (rpy_mobility_solver.cu:14-53). */
+GMI_API gmi_status gmi_solver_destroy(gmi_solver *s);
+GMI_API gmi_status gmi_solver_host_arrays(gmi_solver *s, gmi_host_arrays *out);
+/* The solver's context (pair kernels, stream, precision). */
+GMI_API gmi_context *gmi_solver_context(gmi_solver *s);
+
+/* The 15 per-backend operations of mobility_solver.hpp:25-44, asynchronous
+ * on the solver stream like the reference's cudaMemcpyAsync/launches
+ * (rpy_mobility_solver.cu:119-311). */
+GMI_API gmi_status gmi_solver_copy_segment_positions_to_device(gmi_solver *s);
+GMI_API gmi_status gmi_solver_copy_segment_forces_to_device(gmi_solver *s);
+GMI_API gmi_status gmi_solver_copy_blob_positions_to_device(gmi_solver *s);
+GMI_API gmi_status gmi_solver_copy_blob_forces_to_device(gmi_solver *s);
+GMI_API gmi_status gmi_solver_copy_interparticle_blob_forces_to_host(gmi_solver *s);
+GMI_API gmi_status gmi_solver_copy_blob_velocities_to_host(gmi_solver *s);
+GMI_API gmi_status gmi_solver_copy_segment_velocities_to_host(gmi_solver *s);
+GMI_API gmi_status gmi_solver_apply_interparticle_forces(gmi_solver *s);
+GMI_API gmi_status gmi_solver_wait_for_device(gmi_solver *s);
+GMI_API gmi_status gmi_solver_evaluate_segment_segment_mobility(gmi_solver *s);
+GMI_API gmi_status gmi_solver_evaluate_segment_blob_mobility(gmi_solver *s);
+GMI_API gmi_status gmi_solver_evaluate_blob_blob_mobility(gmi_solver *s);
+GMI_API gmi_status gmi_solver_evaluate_blob_segment_mobility(gmi_solver *s);
+
+/* Blob positions in the body frame, shared by all swimmers (the reference's
+ * rigid_body::blob_references, rigid_body.cpp:184-237), 3*nblob values. */
+GMI_API gmi_status gmi_solver_set_blob_references(gmi_solver *s, const double *blob_references_h);
+
+/* mobility_solver::make_body_reference_matrices (mobility_solver.cpp:1693-1771):
+ * (K^T K)^-1 from the blob references and the 6x6 body mobility of the last
+ * swimmer from six GMRES solves with the other swimmers moved 1e10*DL*NSEG
+ * away.  body_x_h[3*nswim], body_q_h[4*nswim] (scalar part first); the
+ * segment positions/forces are read from the host arrays.  Outputs (may be
+ * NULL): the two 6x6 matrices, column-major like the reference's matrix. */
+GMI_API gmi_status gmi_solver_make_body_reference_matrices(gmi_solver *s, const double *body_x_h,
+                                                           const double *body_q_h, double *ktkinv_h,
+                                                           double *body_mobility_h);
+/* Install reference matrices computed elsewhere (e.g. restored state). */
+GMI_API gmi_status gmi_solver_set_body_reference_matrices(gmi_solver *s, const double *ktkinv_h,
+                                                          const double *body_mobility_h);
+
+/* mobility_solver::compute_velocities (mobility_solver.cpp:1358-1402) with
+ * every step on the device: copies x_segs_host/f_segs_host in, blob
+ * positions from (body_x_h, body_q_h), barrier forces (the blob part is
+ * added into body_f_h[6*nswim] as read_positions_and_forces does,
+ * mobility_solver.cpp:166-188), M_ss, M_bs, the right-hand side, GMRES for
+ * the blob forces and body velocities, M_sb; then v_segs_host,
+ * f_blobs_host, x_blobs_host, f_blobs_repulsion_host and v_blobs_host are
+ * written back and the call returns when they are valid.
+ * num_gmres_iterations may be NULL. */
+GMI_API gmi_status gmi_solver_compute_velocities(gmi_solver *s, const double *body_x_h, const double *body_q_h,
+                                                 double *body_f_h, int *num_gmres_iterations);
+
+/* v_bodies after the last solve: 6*nswim values (U, Omega per swimmer). */
+GMI_API gmi_status gmi_solver_get_v_bodies(gmi_solver *s, double *v_bodies_h);
+GMI_API gmi_status gmi_solver_set_v_bodies(gmi_solver *s, const double *v_bodies_h);
 
 /* Measured FMA-pipe throughput (FLOP/s, FMA = 2) of this GPU for
  * precision GMI_FP32C (FP32 pipe) or GMI_FP64 (FP64 pipe): the roofline

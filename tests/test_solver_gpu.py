@@ -1,0 +1,178 @@
+"""Device-resident mobility solve against the dense FP64 oracle.
+
+The GMRES answer (blob forces, body velocities) and everything around it
+(blob positions, barrier forces and their body force/torque, M_ss, M_bs,
+M_sb) are compared with oracle/mobility_dense.py, which solves the same
+saddle-point system by dense LU.  GMRES stops at a 1e-10 relative residual,
+so the comparison tolerance is 1e-7.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+GMRES_TOL = 1e-7
+
+
+def swimmer_geometry(nswim=1, nfil=4, nseg=10, subdiv=2, R=8.0, seed=3):
+    from generic_mobility_interface_class_gb300 import seeding
+    from oracle import mobility_dense as md
+    rng = np.random.default_rng(seed)
+    refs = R * seeding.icosphere(subdiv)
+    dirs = seeding.icosphere(1)[rng.choice(42, nfil, replace=False)]
+    body_x = np.array([[30.0 * n, 5.0 * n, -2.0 * n] for n in range(nswim)]) + 0.5
+    q = rng.normal(size=(nswim, 4))
+    body_q = q / np.linalg.norm(q, axis=1, keepdims=True)
+    xs = []
+    for n in range(nswim):
+        local = seeding.radial_filaments(dirs, R + 2.1, nseg) + 0.2 * rng.normal(size=(nfil * nseg, 3))
+        xs.append(body_x[n] + local @ md.rot_mat(body_q[n]).T)
+    xs = np.concatenate(xs)
+    fs = rng.normal(size=(nswim * nfil * nseg, 6))
+    body_f = rng.normal(size=(nswim, 6))
+    return refs, body_x, body_q, xs, fs, body_f
+
+
+def make_solver(refs, nswim, nfil, nseg, precision=0, scale=1.5):
+    from generic_mobility_interface_class_gb300.solver import MobilitySolver
+    s = MobilitySolver(nswim=nswim, nfil=nfil, nseg=nseg, nblob=refs.shape[0], repulsive_force_factor=1.0,
+                       end_force_magnitude=scale, precision=precision)
+    s.set_blob_references(refs)
+    return s
+
+
+@pytest.mark.parametrize("nswim", [1, 2])
+def test_compute_velocities_matches_dense(nswim, gmi_lib, oracle_built):
+    from oracle import mobility_dense as md
+    nfil, nseg = 4, 10
+    refs, bx, bq, xs, fs, bf = swimmer_geometry(nswim, nfil, nseg)
+    s = make_solver(refs, nswim, nfil, nseg)
+    s.x_segs_host[:] = xs
+    s.f_segs_host[:] = fs
+    iters, bf_out = s.compute_velocities(bx, bq, bf)
+    want = md.compute_velocities(xs, fs, bx, bq, bf, refs, nseg, force_scale=1.5)
+    assert iters > 0
+    assert rel_err(s.x_blobs_host, want["x_blobs"]) < 1e-14
+    assert rel_err(s.f_blobs_repulsion_host, want["f_rep"]) < 1e-13
+    assert rel_err(bf_out, want["body_f"]) < 1e-13
+    assert rel_err(s.f_blobs_host, want["f_blobs"]) < GMRES_TOL
+    assert rel_err(s.v_bodies(), want["v_bodies"]) < GMRES_TOL
+    assert rel_err(s.v_segs_host, want["v_segs"]) < GMRES_TOL
+    # the host force array is not modified by the barrier (it acts on the device copy)
+    np.testing.assert_array_equal(s.f_segs_host, fs)
+    # a second call warm-starts from the previous solution and needs fewer iterations
+    iters2, _ = s.compute_velocities(bx, bq, bf)
+    assert iters2 < iters
+    assert rel_err(s.v_segs_host, want["v_segs"]) < GMRES_TOL
+    s.close()
+
+
+def test_body_reference_matrices(gmi_lib, oracle_built):
+    from oracle import mobility_dense as md
+    nfil, nseg = 4, 10
+    refs, bx, bq, xs, fs, bf = swimmer_geometry(1, nfil, nseg)
+    s = make_solver(refs, 1, nfil, nseg)
+    s.x_segs_host[:] = xs
+    s.f_segs_host[:] = fs
+    ktk, mob = s.make_body_reference_matrices(bx, bq)
+    assert rel_err(ktk, md.ktk_inverse(refs)) < 1e-12
+    xb = md.blob_positions(bx, bq, refs)
+    want = md.body_mobility_reference(xb, refs, bq[0], 1.0, 1.0)
+    assert rel_err(mob, want) < GMRES_TOL
+    # a sphere of blobs approaches the Stokes sphere mobility 1/(6 pi mu R), 1/(8 pi mu R^3)
+    R_eff = 8.0
+    assert abs(mob[0, 0] * 6 * np.pi * R_eff - 1) < 0.2
+    # the preconditioned solve is faster with the reference matrices in place
+    s.set_v_bodies(np.zeros((1, 6)))
+    iters, _ = s.compute_velocities(bx, bq, bf)
+    s2 = make_solver(refs, 1, nfil, nseg)
+    s2.x_segs_host[:] = xs
+    s2.f_segs_host[:] = fs
+    iters_plain, _ = s2.compute_velocities(bx, bq, bf)
+    assert iters <= iters_plain
+    s.close()
+    s2.close()
+
+
+def test_fp32c_solver_error(gmi_lib, oracle_built):
+    from oracle import mobility_dense as md
+    nfil, nseg = 4, 10
+    refs, bx, bq, xs, fs, bf = swimmer_geometry(1, nfil, nseg)
+    s = make_solver(refs, 1, nfil, nseg, precision=1)
+    s.x_segs_host[:] = xs
+    s.f_segs_host[:] = fs
+    s.compute_velocities(bx, bq, bf)
+    want = md.compute_velocities(xs, fs, bx, bq, bf, refs, nseg, force_scale=1.5)
+    assert rel_err(s.v_segs_host, want["v_segs"]) < 1e-5
+    assert rel_err(s.v_bodies(), want["v_bodies"]) < 1e-5
+    s.close()
+
+
+def test_backend_operations_match_oracle(gmi_lib, oracle_built):
+    """The reference's per-backend calls, one by one, on the solver's pinned arrays."""
+    from oracle import rpy
+    nfil, nseg = 3, 6
+    refs, bx, bq, xs, fs, bf = swimmer_geometry(1, nfil, nseg)
+    from oracle import mobility_dense as md
+    xb = md.blob_positions(bx, bq, refs)
+    s = make_solver(refs, 1, nfil, nseg)
+    rng = np.random.default_rng(1)
+    fb = rng.normal(size=xb.shape)
+    s.x_segs_host[:] = xs
+    s.f_segs_host[:] = fs
+    s.x_blobs_host[:] = xb
+    s.f_blobs_host[:] = fb
+    s.copy_segment_positions_to_device()
+    s.copy_segment_forces_to_device()
+    s.copy_blob_positions_to_device()
+    s.copy_blob_forces_to_device()
+    s.evaluate_segment_segment_mobility()
+    s.evaluate_segment_blob_mobility()
+    s.copy_segment_velocities_to_host()
+    s.evaluate_blob_segment_mobility()
+    s.copy_blob_velocities_to_host()
+    s.wait_for_device()
+    v_segs = rpy.msb(xs, xb, fb, v_in=rpy.mss(xs, fs))
+    assert rel_err(s.v_segs_host, v_segs) < 1e-12
+    assert rel_err(s.v_blobs_host, rpy.mbs(xb, xs, fs)) < 1e-12
+    s.evaluate_blob_blob_mobility()
+    s.copy_blob_velocities_to_host()
+    s.apply_interparticle_forces()
+    s.copy_interparticle_blob_forces_to_host()
+    s.wait_for_device()
+    assert rel_err(s.v_blobs_host, rpy.mbb(xb, fb)) < 1e-12
+    _, frep = rpy.barrier(xs, xb, fs, nseg, 1.0, 1.0, 1.5)
+    assert rel_err(s.f_blobs_repulsion_host, frep) < 1e-13
+    s.close()
+
+
+def test_wall_solver(gmi_lib, oracle_built):
+    from conftest import load_golden
+    from generic_mobility_interface_class_gb300.solver import MobilitySolver
+    g = load_golden("wall_filaments")
+    nfil, nseg = int(g["nfil"]), int(g["nseg"])
+    s = MobilitySolver(nswim=1, nfil=nfil, nseg=nseg, nblob=0, wall=True, repulsive_force_factor=1.0,
+                       end_force_magnitude=float(g["force_scale"]))
+    s.x_segs_host[:] = g["xs"]
+    s.f_segs_host[:] = g["fs"]
+    iters, _ = s.compute_velocities()
+    assert iters == 0
+    from oracle import rpy
+    want = rpy.mss_wall(g["xs"], g["fs_barrier"])
+    assert rel_err(s.v_segs_host, want) < 1e-12
+    s.close()
+
+
+def test_solver_rejects_bad_config(gmi_lib):
+    from generic_mobility_interface_class_gb300._lib import GmiError
+    from generic_mobility_interface_class_gb300.solver import MobilitySolver
+    with pytest.raises(GmiError):
+        MobilitySolver(nswim=1, nfil=1, nseg=2, nblob=10, wall=True)
+    with pytest.raises(GmiError):
+        MobilitySolver(nswim=0, nfil=1, nseg=2, nblob=10)
+    s = MobilitySolver(nswim=1, nfil=1, nseg=2, nblob=10)
+    with pytest.raises(GmiError):
+        s.compute_velocities()  # blob references never set
+    s.close()
