@@ -180,13 +180,13 @@ template <class R> struct KernelConsts {
 template <class R> __device__ __forceinline__ KernelConsts<R> convert_consts(const PairConsts &c)
 {
     KernelConsts<R> k;
-    k.eq.two_a = (R)c.eq[0]; k.eq.two_a2 = (R)c.eq[1]; k.eq.f8pm = (R)c.eq[2]; k.eq.f16pm = (R)c.eq[3];
-    k.eq.f6pma = (R)c.eq[4]; k.eq.q32 = (R)c.eq[5]; k.eq.inv_a = (R)c.eq[6]; k.eq.f8pma3 = (R)c.eq[7];
-    k.eq.f16pma3 = (R)c.eq[8]; k.eq.q8 = (R)c.eq[9];
-    k.uq.sum = (R)c.uq[0]; k.uq.dmin = (R)c.uq[1]; k.uq.dmin2 = (R)c.uq[2]; k.uq.far_c = (R)c.uq[3];
-    k.uq.half_sum = (R)c.uq[4]; k.uq.f8pm = (R)c.uq[5]; k.uq.f6pmab = (R)c.uq[6]; k.uq.fmax = (R)c.uq[7];
-    k.uq.c_mid_den = (R)c.uq[8]; k.uq.ab = (R)c.uq[9]; k.uq.as = (R)c.uq[10]; k.uq.ab2 = (R)c.uq[11];
-    k.uq.f8pmas3 = (R)c.uq[12]; k.uq.seg_bigger = (R)c.uq[13];
+    k.eq.four_a2 = (R)c.eq[0]; k.eq.two_a2 = (R)c.eq[1]; k.eq.f8pm = (R)c.eq[2]; k.eq.f6pma = (R)c.eq[3];
+    k.eq.q32 = (R)c.eq[4]; k.eq.inv_a = (R)c.eq[5]; k.eq.f8pma3 = (R)c.eq[6]; k.eq.f16pma3 = (R)c.eq[7];
+    k.eq.q8 = (R)c.eq[8];
+    k.uq.sum2 = (R)c.uq[0]; k.uq.dmin2 = (R)c.uq[1]; k.uq.far_c = (R)c.uq[2]; k.uq.half_sum = (R)c.uq[3];
+    k.uq.f8pm = (R)c.uq[4]; k.uq.f6pmab = (R)c.uq[5]; k.uq.fmax = (R)c.uq[6]; k.uq.c_mid_den = (R)c.uq[7];
+    k.uq.ab = (R)c.uq[8]; k.uq.as = (R)c.uq[9]; k.uq.ab2 = (R)c.uq[10]; k.uq.inner_c = (R)c.uq[11];
+    k.uq.dmin = (R)c.uq[12];
     return k;
 }
 
@@ -427,31 +427,29 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
 void fill_consts(PairConsts &c, double a_eq, double as, double ab, double mu)
 {
     const double pi = kPi;
-    c.eq[0] = 2.0 * a_eq;
+    c.eq[0] = 4.0 * a_eq * a_eq;
     c.eq[1] = 2.0 * a_eq * a_eq;
     c.eq[2] = 1.0 / (8.0 * pi * mu);
-    c.eq[3] = 1.0 / (16.0 * pi * mu);
-    c.eq[4] = 1.0 / (6.0 * pi * mu * a_eq);
-    c.eq[5] = 3.0 / (32.0 * a_eq);
-    c.eq[6] = 1.0 / a_eq;
-    c.eq[7] = 1.0 / (8.0 * pi * mu * a_eq * a_eq * a_eq);
-    c.eq[8] = 1.0 / (16.0 * pi * mu * a_eq * a_eq * a_eq);
-    c.eq[9] = 3.0 / (8.0 * a_eq);
+    c.eq[3] = 1.0 / (6.0 * pi * mu * a_eq);
+    c.eq[4] = 3.0 / (32.0 * a_eq);
+    c.eq[5] = 1.0 / a_eq;
+    c.eq[6] = 1.0 / (8.0 * pi * mu * a_eq * a_eq * a_eq);
+    c.eq[7] = 1.0 / (16.0 * pi * mu * a_eq * a_eq * a_eq);
+    c.eq[8] = 3.0 / (8.0 * a_eq);
     const double dmin = fabs(as - ab);
-    c.uq[0] = as + ab;
-    c.uq[1] = dmin;
-    c.uq[2] = dmin * dmin;
-    c.uq[3] = (as * as + ab * ab) / 3.0;
-    c.uq[4] = 0.5 * (as + ab);
-    c.uq[5] = 1.0 / (8.0 * pi * mu);
-    c.uq[6] = 1.0 / (6.0 * pi * mu * as * ab);
-    c.uq[7] = 1.0 / (6.0 * pi * mu * (as > ab ? as : ab));
-    c.uq[8] = 1.0 / (128.0 * pi * mu * ab * as * as * as);
-    c.uq[9] = ab;
-    c.uq[10] = as;
-    c.uq[11] = ab * ab;
-    c.uq[12] = 1.0 / (8.0 * pi * mu * as * as * as);
-    c.uq[13] = as > ab ? 1.0 : 0.0;
+    c.uq[0] = (as + ab) * (as + ab);
+    c.uq[1] = dmin * dmin;
+    c.uq[2] = (as * as + ab * ab) / 3.0;
+    c.uq[3] = 0.5 * (as + ab);
+    c.uq[4] = 1.0 / (8.0 * pi * mu);
+    c.uq[5] = 1.0 / (6.0 * pi * mu * as * ab);
+    c.uq[6] = 1.0 / (6.0 * pi * mu * (as > ab ? as : ab));
+    c.uq[7] = 1.0 / (128.0 * pi * mu * ab * as * as * as);
+    c.uq[8] = ab;
+    c.uq[9] = as;
+    c.uq[10] = ab * ab;
+    c.uq[11] = (as > ab ? 1.0 : 0.0) / (8.0 * pi * mu * as * as * as);
+    c.uq[12] = dmin;
 }
 
 gmi_status pack_records(gmi_context *ctx, const double *x, const double *f, int nf, int n, DeviceBuffer &buf)
@@ -510,7 +508,7 @@ template <int KIND, class R, int TPB, int TT> struct Inst {
 struct ShapeEntry {
     int tpb, tt;
 };
-static const ShapeEntry kShapes[] = {{128, 1}, {128, 2}, {256, 1}, {256, 2}, {128, 4}};
+static const ShapeEntry kShapes[] = {{128, 1}, {128, 2}, {256, 1}, {256, 2}, {128, 4}, {64, 1}, {64, 2}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
 template <int KIND, class R> static void *kernel_for_shape(int idx)
@@ -520,7 +518,9 @@ template <int KIND, class R> static void *kernel_for_shape(int idx)
         case 1: return Inst<KIND, R, 128, 2>::fn();
         case 2: return Inst<KIND, R, 256, 1>::fn();
         case 3: return Inst<KIND, R, 256, 2>::fn();
-        default: return Inst<KIND, R, 128, 4>::fn();
+        case 4: return Inst<KIND, R, 128, 4>::fn();
+        case 5: return Inst<KIND, R, 64, 1>::fn();
+        default: return Inst<KIND, R, 64, 2>::fn();
     }
 }
 
@@ -548,11 +548,11 @@ static size_t ring_bytes(bool f64) { return (size_t)kStages * kTile * kRecLen * 
 static int nout_of(int kind) { return (kind == kBB || kind == kBS) ? 3 : 6; }
 
 // Source splits: enough CTAs for ~2 full waves when the target tiles alone
-// cannot fill the GPU; every split keeps at least two tiles of sources.
+// cannot fill the GPU; every split keeps at least one tile of sources.
 static int choose_splits(const gmi_context *ctx, int n_tgt_ctas, int n_src, int occ)
 {
     const int slots = ctx->sm_count * (occ > 0 ? occ : 1);
-    const int max_splits = n_src / (2 * kTile) > 1 ? n_src / (2 * kTile) : 1;
+    const int max_splits = (n_src + kTile - 1) / kTile;
     if (n_tgt_ctas >= 2 * slots) return 1;
     int s = (2 * slots + n_tgt_ctas - 1) / n_tgt_ctas;
     return s < max_splits ? s : max_splits;
@@ -573,7 +573,11 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
         shape = *force_shape;
     } else {
         auto it = ctx->tuned.find(TuneKey{kind, ctx->precision, n_tgt, n_src});
-        if (it != ctx->tuned.end()) shape = it->second;
+        if (it != ctx->tuned.end()) {
+            shape = it->second;
+        } else if ((long long)n_tgt * 2 < (long long)ctx->sm_count * 256) {
+            shape = PairShape{64, 1, 0};  // small target sets: more, smaller CTAs
+        }
     }
     const int sidx = shape_index(shape.tpb, shape.tt);
     const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;

@@ -8,8 +8,8 @@ namespace gmi {
 // Physical constants of one pair kind, precomputed on the host in FP64
 // (converted to the kernel's scalar type on the device).
 struct PairConsts {
-    double eq[10];  // equal radii: see EqualK
-    double uq[14];  // segment/blob radii: see UnequalK
+    double eq[9];   // equal radii: see EqualK
+    double uq[13];  // segment/blob radii: see UnequalK
 };
 
 struct PairLaunch {

@@ -17,53 +17,62 @@ template <> __device__ __forceinline__ double rsq<double>(double x) { return rsq
 
 // Equal-radius constants (segment<-segment with a = a_seg, blob<-blob with a = a_blob).
 template <class R> struct EqualK {
-    R two_a, two_a2, f8pm, f16pm, f6pma, q32, inv_a, f8pma3, f16pma3, q8;
+    R four_a2, two_a2, f8pm, f6pma, q32, inv_a, f8pma3, f16pma3, q8;
 };
 
 // Unequal-radius constants for segment<->blob pairs (radii as, ab).
 template <class R> struct UnequalK {
-    R sum, dmin, dmin2, far_c, half_sum, f8pm, f6pmab, fmax, c_mid_den, ab, as, ab2, f8pmas3, seg_bigger;
+    R sum2, dmin2, far_c, half_sum, f8pm, f6pmab, fmax, c_mid_den, ab, as, ab2, inner_c, dmin;
 };
 
-// translation<-force, rotation<-torque and the two cross couplings, equal radii:
-// cuda_functions.cu:315-398.
+// The pair formulas below are the reference's, rewritten in terms of the
+// separation d = x_i - x_j instead of the unit vector e = d/r: every power
+// of 1/r is folded into the scalar coefficients, so a pair costs one
+// reciprocal square root and its accumulation is a chain of fused
+// multiply-adds.  Near/far is decided on r^2.
+
+// translation<-force, rotation<-torque and the two cross couplings, equal
+// radii: cuda_functions.cu:315-398.
+//   v += At F + Bt d + c3 (T x d),   w += Ar T + Br d + c3 (F x d)
 template <class R>
 __device__ __forceinline__ void pair_ss(R dx, R dy, R dz, const R *F, const EqualK<R> &k, R *v, R *w)
 {
     const R r2 = dx * dx + dy * dy + dz * dz;
     const R ir = rsq<R>(r2);
-    const R r = r2 * ir;
-    const R ex = dx * ir, ey = dy * ir, ez = dz * ir;
-    const R ef = ex * F[0] + ey * F[1] + ez * F[2];
-    const R et = ex * F[3] + ey * F[4] + ez * F[5];
-    R t_id, t_ee, r_id, r_ee, cx;
-    if (r > k.two_a) {
+    const R dF = dx * F[0] + dy * F[1] + dz * F[2];
+    const R dT = dx * F[3] + dy * F[4] + dz * F[5];
+    R At, Bt, Ar, Br, c3;
+    if (r2 > k.four_a2) {
         const R ir2 = ir * ir;
-        const R s = k.two_a2 * ir2;
-        const R ik = ir * k.f8pm;
-        t_id = (R(1) + s * R(1.0 / 3.0)) * ik;
-        t_ee = (R(1) - s) * ik * ef;
-        const R ir3k = ir2 * ir * k.f16pm;
-        r_id = -ir3k;
-        r_ee = R(3) * ir3k * et;
-        cx = ir2 * k.f8pm;
+        const R ir3 = ir2 * ir;
+        const R s = k.two_a2 * ir2;                 // 2a^2/r^2
+        const R ik = ir * k.f8pm;                   // 1/(8 pi mu r)
+        At = ik * (R(1) + s * R(1.0 / 3.0));
+        c3 = ir3 * k.f8pm;
+        const R c3dF = c3 * dF;
+        Bt = c3dF - s * c3dF;                       // (1 - s) dF / (8 pi mu r^3)
+        Ar = R(-0.5) * c3;                          // -1/(16 pi mu r^3)
+        Br = (R(1.5) * c3 * ir2) * dT;              // 3 dT / (16 pi mu r^5)
     } else {
-        const R q = r * k.q32;
-        t_id = (R(1) - R(3) * q) * k.f6pma;
-        t_ee = q * k.f6pma * ef;
+        const R r = r2 * ir;
+        const R ir2 = ir * ir;
+        const R q = r * k.q32;                      // 3r/(32a)
+        At = (R(1) - R(3) * q) * k.f6pma;
+        Bt = q * k.f6pma * ir2 * dF;
         const R ra = r * k.inv_a;
         const R ra3 = ra * ra * ra;
         const R b = R(9.0 / 32.0) * ra;
-        r_id = (R(-3) * b + (R(1) + R(5.0 / 64.0) * ra3)) * k.f8pma3;
-        r_ee = (b - R(3.0 / 64.0) * ra3) * k.f8pma3 * et;
-        cx = r * (R(1) - r * k.q8) * k.f16pma3;
+        Ar = (R(-3) * b + (R(1) + R(5.0 / 64.0) * ra3)) * k.f8pma3;
+        Br = (b - R(3.0 / 64.0) * ra3) * k.f8pma3 * ir2 * dT;
+        c3 = r * (R(1) - r * k.q8) * k.f16pma3 * ir;
     }
-    v[0] += t_id * F[0] + t_ee * ex + cx * (F[4] * ez - F[5] * ey);
-    v[1] += t_id * F[1] + t_ee * ey + cx * (F[5] * ex - F[3] * ez);
-    v[2] += t_id * F[2] + t_ee * ez + cx * (F[3] * ey - F[4] * ex);
-    w[0] += r_id * F[3] + r_ee * ex + cx * (F[1] * ez - F[2] * ey);
-    w[1] += r_id * F[4] + r_ee * ey + cx * (F[2] * ex - F[0] * ez);
-    w[2] += r_id * F[5] + r_ee * ez + cx * (F[0] * ey - F[1] * ex);
+    const R cx = c3 * dx, cy = c3 * dy, cz = c3 * dz;
+    v[0] += At * F[0] + Bt * dx + F[4] * cz - F[5] * cy;
+    v[1] += At * F[1] + Bt * dy + F[5] * cx - F[3] * cz;
+    v[2] += At * F[2] + Bt * dz + F[3] * cy - F[4] * cx;
+    w[0] += Ar * F[3] + Br * dx + F[1] * cz - F[2] * cy;
+    w[1] += Ar * F[4] + Br * dy + F[2] * cx - F[0] * cz;
+    w[2] += Ar * F[5] + Br * dz + F[0] * cy - F[1] * cx;
 }
 
 // translation<-force, equal radii: cuda_functions.cu:465-520.
@@ -72,52 +81,53 @@ __device__ __forceinline__ void pair_bb(R dx, R dy, R dz, const R *F, const Equa
 {
     const R r2 = dx * dx + dy * dy + dz * dz;
     const R ir = rsq<R>(r2);
-    const R r = r2 * ir;
-    const R ex = dx * ir, ey = dy * ir, ez = dz * ir;
-    const R ef = ex * F[0] + ey * F[1] + ez * F[2];
-    R t_id, t_ee;
-    if (r > k.two_a) {
-        const R s = k.two_a2 * ir * ir;
+    const R dF = dx * F[0] + dy * F[1] + dz * F[2];
+    R At, Bt;
+    if (r2 > k.four_a2) {
+        const R ir2 = ir * ir;
+        const R s = k.two_a2 * ir2;
         const R ik = ir * k.f8pm;
-        t_id = (R(1) + s * R(1.0 / 3.0)) * ik;
-        t_ee = (R(1) - s) * ik * ef;
+        At = ik * (R(1) + s * R(1.0 / 3.0));
+        const R c3dF = ik * ir2 * dF;
+        Bt = c3dF - s * c3dF;
     } else {
+        const R r = r2 * ir;
         const R q = r * k.q32;
-        t_id = (R(1) - R(3) * q) * k.f6pma;
-        t_ee = q * k.f6pma * ef;
+        At = (R(1) - R(3) * q) * k.f6pma;
+        Bt = q * k.f6pma * (ir * ir) * dF;
     }
-    v[0] += t_id * F[0] + t_ee * ex;
-    v[1] += t_id * F[1] + t_ee * ey;
-    v[2] += t_id * F[2] + t_ee * ez;
+    v[0] += At * F[0] + Bt * dx;
+    v[1] += At * F[1] + Bt * dy;
+    v[2] += At * F[2] + Bt * dz;
 }
 
-// Unequal-radius coefficients: cuda_functions.cu:608-667 (segment<-blob) and
-// :770-829 (blob<-segment), which share the same expressions in (RSEG, RBLOB).
+// Unequal-radius coefficients, cuda_functions.cu:608-667 (segment<-blob) and
+// :770-829 (blob<-segment), which share the same expressions in (RSEG, RBLOB):
+//   A (of F), Bd (of d, already times d.F), Cd (of the cross product with d).
 template <class R>
-__device__ __forceinline__ void unequal_coeffs(R r, R ir, const UnequalK<R> &k, R &A, R &B, R &C)
+__device__ __forceinline__ void unequal_coeffs(R r2, R ir, R dF, const UnequalK<R> &k, R &A, R &Bd, R &Cd)
 {
-    if (r > k.sum) {
-        const R ir2 = ir * ir;
+    const R ir2 = ir * ir;
+    if (r2 > k.sum2) {
         const R t = ir2 * k.far_c;  // (as^2 + ab^2) / (3 r^2)
         const R ik = ir * k.f8pm;
         A = (t + R(1)) * ik;
-        B = (R(1) - R(3) * t) * ik;
-        C = ir2 * k.f8pm;
-    } else if (r > k.dmin) {
-        const R r_2 = r * r;
-        const R d3 = R(32) * r_2 * r;
-        const R id3 = R(1) / d3;
-        R t = k.dmin2 + R(3) * r_2;
+        Cd = ik * ir2;
+        Bd = (R(1) - R(3) * t) * Cd * dF;
+    } else if (r2 > k.dmin2) {
+        const R r = r2 * ir;
+        const R id3 = R(1.0 / 32.0) * ir2 * ir;  // 1/(32 r^3)
+        const R t = k.dmin2 + R(3) * r2;
         A = (k.half_sum - t * t * id3) * k.f6pmab;
-        const R b = k.dmin2 - r_2;
-        B = R(3) * b * b * id3 * k.f6pmab;
+        const R b = k.dmin2 - r2;
+        Bd = R(3) * b * b * id3 * k.f6pmab * ir2 * dF;
         const R u = k.as - k.ab + r;
         const R p = k.ab2 + R(2) * k.ab * (r + k.as) - R(3) * (k.as - r) * (k.as - r);
-        C = ir * ir * u * u * p * k.c_mid_den;
+        Cd = ir2 * u * u * p * k.c_mid_den * ir;
     } else {
         A = k.fmax;
-        B = R(0);
-        C = k.seg_bigger * r * k.f8pmas3;
+        Bd = R(0);
+        Cd = k.inner_c * (r2 * ir) * ir;
     }
 }
 
@@ -127,17 +137,16 @@ __device__ __forceinline__ void pair_sb(R dx, R dy, R dz, const R *F, const Uneq
 {
     const R r2 = dx * dx + dy * dy + dz * dz;
     const R ir = rsq<R>(r2);
-    const R r = r2 * ir;
-    const R ex = dx * ir, ey = dy * ir, ez = dz * ir;
-    R A, B, C;
-    unequal_coeffs<R>(r, ir, k, A, B, C);
-    const R ef = (ex * F[0] + ey * F[1] + ez * F[2]) * B;
-    v[0] += A * F[0] + ef * ex;
-    v[1] += A * F[1] + ef * ey;
-    v[2] += A * F[2] + ef * ez;
-    w[0] += C * (F[1] * ez - F[2] * ey);
-    w[1] += C * (F[2] * ex - F[0] * ez);
-    w[2] += C * (F[0] * ey - F[1] * ex);
+    const R dF = dx * F[0] + dy * F[1] + dz * F[2];
+    R A, Bd, Cd;
+    unequal_coeffs<R>(r2, ir, dF, k, A, Bd, Cd);
+    const R cx = Cd * dx, cy = Cd * dy, cz = Cd * dz;
+    v[0] += A * F[0] + Bd * dx;
+    v[1] += A * F[1] + Bd * dy;
+    v[2] += A * F[2] + Bd * dz;
+    w[0] += F[1] * cz - F[2] * cy;
+    w[1] += F[2] * cx - F[0] * cz;
+    w[2] += F[0] * cy - F[1] * cx;
 }
 
 // blob <- segment force and torque (6 -> 3): cuda_functions.cu:744-829.
@@ -146,14 +155,13 @@ __device__ __forceinline__ void pair_bs(R dx, R dy, R dz, const R *F, const Uneq
 {
     const R r2 = dx * dx + dy * dy + dz * dz;
     const R ir = rsq<R>(r2);
-    const R r = r2 * ir;
-    const R ex = dx * ir, ey = dy * ir, ez = dz * ir;
-    R A, B, C;
-    unequal_coeffs<R>(r, ir, k, A, B, C);
-    const R ef = (ex * F[0] + ey * F[1] + ez * F[2]) * B;
-    v[0] += A * F[0] + ef * ex + C * (F[4] * ez - F[5] * ey);
-    v[1] += A * F[1] + ef * ey + C * (F[5] * ex - F[3] * ez);
-    v[2] += A * F[2] + ef * ez + C * (F[3] * ey - F[4] * ex);
+    const R dF = dx * F[0] + dy * F[1] + dz * F[2];
+    R A, Bd, Cd;
+    unequal_coeffs<R>(r2, ir, dF, k, A, Bd, Cd);
+    const R cx = Cd * dx, cy = Cd * dy, cz = Cd * dz;
+    v[0] += A * F[0] + Bd * dx + F[4] * cz - F[5] * cy;
+    v[1] += A * F[1] + Bd * dy + F[5] * cx - F[3] * cz;
+    v[2] += A * F[2] + Bd * dz + F[3] * cy - F[4] * cx;
 }
 
 // Segment <- segment above a no-slip wall at z = 0, a = mu = 1 (Swan & Brady):

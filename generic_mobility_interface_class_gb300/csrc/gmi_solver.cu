@@ -407,6 +407,7 @@ struct gmi_solver {
     double *refs = nullptr, *sums = nullptr;
     double *rhs = nullptr, *soln = nullptr, *Q = nullptr, *H = nullptr, *beta = nullptr, *cs = nullptr, *sn = nullptr;
     double *z = nullptr, *w = nullptr, *tmp = nullptr, *mbb = nullptr, *partial = nullptr, *yv = nullptr;
+    double *b64 = nullptr, *xacc = nullptr;  // refinement: FP64 right-hand side, accumulated solution
     double *scal = nullptr;  // device scalars: [0] norm, [1] resid
     bool refs_set = false;
     std::vector<void *> allocs;
@@ -529,8 +530,94 @@ static gmi_status orthonormalise(gmi_solver *s, double *w, int k, double *Hcol)
     return launched(s, 2);
 }
 
-// solve_linear_system (mobility_solver.cpp:970-1354), right preconditioned,
-// warm started from (f_blobs, v_bodies).  rhs must already be in s->rhs.
+// Arnoldi/GMRES core of solve_linear_system (mobility_solver.cpp:1162-1350),
+// right preconditioned, on A x = b with b in s->rhs and the initial guess in
+// s->soln.  Stops when |beta(iter)| <= tol * norm_ref.  reject_warm_start
+// applies the reference's rule that a warm start with a residual above
+// ||b|| is replaced by zero (mobility_solver.cpp:1149-1156).  zero_start
+// skips the initial residual apply (x0 = 0, r0 = b, ||b|| = norm_b).
+static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, double tol, bool reject_warm_start,
+                            bool zero_start, int *iters_out)
+{
+    const int n = s->n;
+    const size_t ld = (size_t)n;
+    cudaStream_t st = s->ctx->stream;
+    *iters_out = 0;
+    double beta0;
+    if (zero_start) {
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->w, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        beta0 = norm_b;
+    } else {
+        GMI_TRY(system_matrix_mult(s, s->soln, s->tmp));
+        axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->rhs, -1.0, s->tmp, s->w);
+        GMI_TRY(launched(s));
+        GMI_TRY(device_norm(s, s->w, n));
+        GMI_TRY(read_scalar(s, s->scal, &beta0));
+        if (fabs(beta0) <= tol * norm_ref) return GMI_OK;  // the initial guess is good enough
+        if (reject_warm_start && fabs(beta0) > norm_b) {
+            GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
+            GMI_CUDA_TRY(cudaMemcpyAsync(s->w, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            beta0 = norm_b;
+        }
+    }
+    s->h_stage[0] = beta0;
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->beta, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
+    scale_kernel<<<grid_for(n), 256, 0, st>>>(n, s->w, s->scal, s->Q);
+    GMI_TRY(launched(s));
+    const int max_iter = n < s->m ? n : s->m;
+    const int ldh = s->m + 1;
+    for (int iter = 1; iter <= max_iter; ++iter) {
+        GMI_TRY(apply_preconditioner(s, s->Q + ld * (iter - 1), s->z));
+        GMI_TRY(system_matrix_mult(s, s->z, s->w));
+        double *Hcol = s->H + (size_t)ldh * (iter - 1);
+        GMI_TRY(orthonormalise(s, s->w, iter, Hcol));
+        givens_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, s->cs, s->sn, iter, norm_ref, s->scal + 1);
+        GMI_TRY(launched(s));
+        double resid;
+        GMI_TRY(read_scalar(s, s->scal + 1, &resid));
+        if (!std::isfinite(resid)) {
+            set_last_error_msg("GMRES produced a non-finite residual");
+            return GMI_ERR_NONFINITE;
+        }
+        if (resid <= tol || iter == max_iter) {
+            backsolve_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
+            combine_kernel<<<grid_for(n), 256, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
+            GMI_TRY(launched(s, 2));
+            GMI_TRY(apply_preconditioner(s, s->tmp, s->z));
+            axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->soln, 1.0, s->z, s->soln);
+            GMI_TRY(launched(s));
+            *iters_out = iter;
+            return GMI_OK;
+        }
+    }
+    return GMI_OK;
+}
+
+static gmi_status store_solution(gmi_solver *s)
+{
+    const int nb = s->B;
+    cudaStream_t st = s->ctx->stream;
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->f_blobs, s->soln, 3 * (size_t)nb * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->v_bodies, s->soln + 3 * nb, 6 * (size_t)s->W * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, st));
+    return GMI_OK;
+}
+
+// solve_linear_system (mobility_solver.cpp:970-1354) warm started from
+// (f_blobs, v_bodies); the right-hand side must be in s->rhs.
+//
+// FP64 context: the reference algorithm as is.
+// FP32C context: mixed-precision iterative refinement.  The residual
+// b - A x is formed with the FP64 operator; each correction solves
+// A d = r by GMRES with the FP32C operator (FP64 Arnoldi, Givens and
+// vectors) to a relative tolerance kInnerTol; x += d.  This converges to
+// the FP64 solution at the requested tolerance, which GMRES on the FP32C
+// operator alone cannot (its answer is off by cond(A) times the operator's
+// rounding).  The iteration count returned is the sum of inner iterations.
+static constexpr double kInnerTol = 1e-4;
+static constexpr int kMaxRefinements = 12;
+
 static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
 {
     const int n = s->n, nb = s->B;
@@ -550,58 +637,52 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         GMI_CUDA_TRY(cudaMemsetAsync(s->v_bodies, 0, 6 * (size_t)s->W * sizeof(double), st));
         return GMI_OK;
     }
-    // warm start soln = [f_blobs ; v_bodies]
     GMI_CUDA_TRY(cudaMemcpyAsync(s->soln, s->f_blobs, 3 * (size_t)nb * sizeof(double), cudaMemcpyDeviceToDevice, st));
     GMI_CUDA_TRY(cudaMemcpyAsync(s->soln + 3 * nb, s->v_bodies, 6 * (size_t)s->W * sizeof(double),
                                  cudaMemcpyDeviceToDevice, st));
-    GMI_TRY(system_matrix_mult(s, s->soln, s->tmp));
-    axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->rhs, -1.0, s->tmp, s->w);
-    GMI_TRY(launched(s));
-    GMI_TRY(device_norm(s, s->w, n));
-    double beta0;
-    GMI_TRY(read_scalar(s, s->scal, &beta0));
-    if (fabs(beta0) <= tol * norm_rhs) return GMI_OK;  // warm start already good enough
-    if (fabs(beta0) > norm_rhs) {
-        GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
-        GMI_CUDA_TRY(cudaMemcpyAsync(s->w, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
-        beta0 = norm_rhs;
+    const int prec = s->ctx->precision;
+    if (prec == GMI_FP64) {
+        int iters = 0;
+        GMI_TRY(gmres_run(s, norm_rhs, norm_rhs, tol, true, false, &iters));
+        *iters_out = iters;
+        return store_solution(s);
     }
-    s->h_stage[0] = beta0;
-    GMI_CUDA_TRY(cudaMemcpyAsync(s->beta, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
-    GMI_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
-    scale_kernel<<<grid_for(n), 256, 0, st>>>(n, s->w, s->scal, s->Q);
-    GMI_TRY(launched(s));
-    const int max_iter = n < s->m ? n : s->m;
-    const int ldh = s->m + 1;
-    for (int iter = 1; iter <= max_iter; ++iter) {
-        GMI_TRY(apply_preconditioner(s, s->Q + ld * (iter - 1), s->z));
-        GMI_TRY(system_matrix_mult(s, s->z, s->w));
-        double *Hcol = s->H + (size_t)ldh * (iter - 1);
-        GMI_TRY(orthonormalise(s, s->w, iter, Hcol));
-        givens_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, s->cs, s->sn, iter, norm_rhs, s->scal + 1);
+    // mixed-precision refinement
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->b64, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    int total = 0;
+    gmi_status status = GMI_OK;
+    for (int outer = 0; outer < kMaxRefinements; ++outer) {
+        s->ctx->precision = GMI_FP64;
+        status = system_matrix_mult(s, s->soln, s->tmp);
+        s->ctx->precision = prec;
+        if (status != GMI_OK) return status;
+        axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->b64, -1.0, s->tmp, s->rhs);
         GMI_TRY(launched(s));
-        double resid;
-        GMI_TRY(read_scalar(s, s->scal + 1, &resid));
-        if (!std::isfinite(resid)) {
-            set_last_error_msg("GMRES produced a non-finite residual");
+        GMI_TRY(device_norm(s, s->rhs, n));
+        double beta;
+        GMI_TRY(read_scalar(s, s->scal, &beta));
+        if (!std::isfinite(beta)) {
+            set_last_error_msg("non-finite residual in the refinement loop");
             return GMI_ERR_NONFINITE;
         }
-        if (resid <= tol || iter == max_iter) {
-            backsolve_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
-            combine_kernel<<<grid_for(n), 256, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
-            GMI_TRY(launched(s, 2));
-            GMI_TRY(apply_preconditioner(s, s->tmp, s->z));
-            axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->soln, 1.0, s->z, s->soln);
-            GMI_TRY(launched(s));
-            GMI_CUDA_TRY(cudaMemcpyAsync(s->f_blobs, s->soln, 3 * (size_t)nb * sizeof(double),
-                                         cudaMemcpyDeviceToDevice, st));
-            GMI_CUDA_TRY(cudaMemcpyAsync(s->v_bodies, s->soln + 3 * nb, 6 * (size_t)s->W * sizeof(double),
-                                         cudaMemcpyDeviceToDevice, st));
-            *iters_out = iter;
-            return GMI_OK;
+        if (beta <= tol * norm_rhs) break;
+        if (outer == 0 && beta > norm_rhs) {  // reject a poor warm start, as the reference does
+            GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
+            GMI_CUDA_TRY(cudaMemcpyAsync(s->rhs, s->b64, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            beta = norm_rhs;
         }
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->xacc, s->soln, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
+        const double inner_tol = tol * norm_rhs / beta > kInnerTol ? tol * norm_rhs / beta : kInnerTol;
+        int iters = 0;
+        GMI_TRY(gmres_run(s, beta, beta, inner_tol, false, true, &iters));
+        total += iters;
+        axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->xacc, 1.0, s->soln, s->soln);
+        GMI_TRY(launched(s));
     }
-    return GMI_OK;
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->rhs, s->b64, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    *iters_out = total;
+    return store_solution(s);
 }
 
 // read_positions_and_forces (mobility_solver.cpp:132-192) minus the host
@@ -828,6 +909,8 @@ gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
         TRY_OR_DIE(dalloc(s, &s->z, n));
         TRY_OR_DIE(dalloc(s, &s->w, n));
         TRY_OR_DIE(dalloc(s, &s->tmp, n));
+        TRY_OR_DIE(dalloc(s, &s->b64, n));
+        TRY_OR_DIE(dalloc(s, &s->xacc, n));
         TRY_OR_DIE(dalloc(s, &s->mbb, 3 * B));
         TRY_OR_DIE(dalloc(s, &s->partial, (size_t)nchunks_of((int)n) * (m + 1)));
     }

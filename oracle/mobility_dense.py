@@ -57,7 +57,8 @@ def mbb_matrix(xb, a, mu):
     return M
 
 
-def saddle_solve(xb, body_q, refs, rhs, a_blob, mu):
+def saddle_matrix(xb, body_q, refs, a_blob, mu):
+    """[M_bb, -K; -K^T, 0] (system_matrix_mult, mobility_solver.cpp:905-962)."""
     Mbb = mbb_matrix(xb, a_blob, mu)
     K = k_matrix(body_q, refs)
     nb, nw = Mbb.shape[0], K.shape[1]
@@ -65,6 +66,12 @@ def saddle_solve(xb, body_q, refs, rhs, a_blob, mu):
     A[:nb, :nb] = Mbb
     A[:nb, nb:] = -K
     A[nb:, :nb] = -K.T
+    return A
+
+
+def saddle_solve(xb, body_q, refs, rhs, a_blob, mu, A=None):
+    A = saddle_matrix(xb, body_q, refs, a_blob, mu) if A is None else A
+    nb = A.shape[0] - 6 * len(np.asarray(body_q).reshape(-1, 4))
     sol = np.linalg.solve(A, rhs)
     return sol[:nb].reshape(-1, 3), sol[nb:].reshape(-1, 6)
 
@@ -85,10 +92,11 @@ def compute_velocities(xs, fs, body_x, body_q, body_f, refs, nseg, rseg=1.0, rbl
     v_segs = rpy.mss(xs, fs2, rseg, mu)
     v_blobs = rpy.mbs(xb, xs, fs2, rseg, rblob, mu)
     rhs = np.concatenate([-v_blobs.ravel(), -bf.ravel()])
-    f_blobs, v_bodies = saddle_solve(xb, body_q, refs, rhs, rblob, mu)
+    A = saddle_matrix(xb, body_q, refs, rblob, mu)
+    f_blobs, v_bodies = saddle_solve(xb, body_q, refs, rhs, rblob, mu, A=A)
     v_segs = rpy.msb(xs, xb, f_blobs, rseg, rblob, mu, v_in=v_segs)
     return dict(v_segs=v_segs, f_blobs=f_blobs, v_bodies=v_bodies, body_f=bf, f_rep=frep, x_blobs=xb,
-                v_blobs_bs=v_blobs)
+                v_blobs_bs=v_blobs, A=A, rhs=rhs)
 
 
 def ktk_inverse(refs):
