@@ -58,3 +58,18 @@ def test_library_missing_is_loud(tmp_path, monkeypatch):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(_lib.GmiLibraryMissing):
         _lib.load()
+
+
+def test_reference_side_adapter_compiles(gmi_lib):
+    """The reference-side binding (adapter/gb300_mobility_solver.cpp) compiles
+    against the reference's own headers (config.hpp, mobility_solver.hpp,
+    swimmer.hpp); skipped where the reference tree is absent."""
+    ref = os.environ.get("GMI_REFERENCE_DIR", "/root/reference")
+    if not os.path.isfile(os.path.join(ref, "mobility_solver.hpp")):
+        pytest.skip("reference tree not present")
+    from generic_mobility_interface_class_gb300 import _lib
+    adapter = os.path.join(_lib.PKG, "adapter")
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I" + ref, "-I" + os.path.join(_lib.ROOT, "include"),
+                        "-I" + adapter, os.path.join(adapter, "gb300_mobility_solver.cpp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
