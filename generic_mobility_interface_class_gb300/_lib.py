@@ -48,6 +48,7 @@ SIGNATURES = {
     "gmi_context_launch_count": ([_P], ctypes.c_longlong),
     "gmi_Mss_mult": ([_P, _P, _P, _P, _I, _I, _I, _D, _D], _I),
     "gmi_Mss_mult_wall": ([_P, _P, _P, _P, _I, _I, _I], _I),
+    "gmi_Mss_mult_noalloc": ([_P, _P, _P, _I, _I, _I, _D, _D, _I, _P], _I),
     "gmi_Mbb_mult": ([_P, _P, _P, _P, _I, _I, _I, _D, _D], _I),
     "gmi_Msb_mult": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _D], _I),
     "gmi_Mbs_mult": ([_P, _P, _P, _P, _P, _I, _I, _I, _I, _D, _D, _D], _I),

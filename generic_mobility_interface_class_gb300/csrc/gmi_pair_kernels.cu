@@ -678,3 +678,108 @@ gmi_status autotune_pair(gmi_context *ctx, int kind, const void *tgt_rec, int n_
 }
 
 }  // namespace gmi
+
+// ---------------------------------------------------------------------------
+// Launchers on caller-provided buffers (no gmi_context): used by the
+// allocation-free entry point in gmi_noalloc.cu.
+// ---------------------------------------------------------------------------
+namespace gmi {
+
+gmi_status pack_records_into(cudaStream_t stream, bool f64, const double *x, const double *f, int nf, int n,
+                             void *dst)
+{
+    if (n == 0) return GMI_OK;
+    const int tpb = 256, grid = (n + tpb - 1) / tpb;
+    if (f64)
+        pack_records_f64<<<grid, tpb, 0, stream>>>(x, f, nf, n, static_cast<double2 *>(dst));
+    else
+        pack_records_f32<<<grid, tpb, 0, stream>>>(x, f, nf, n, static_cast<float4 *>(dst));
+    GMI_CUDA_TRY(cudaGetLastError());
+    return GMI_OK;
+}
+
+size_t record_bytes(bool f64) { return (size_t)kRecLen * (f64 ? sizeof(double) : sizeof(float)); }
+
+// The record tensor map of make_record_map, from an explicit encoder.
+static gmi_status encode_record_map(void *encode_tiled, CUtensorMap *map, const void *base, int n, bool f64)
+{
+    using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    auto encode = reinterpret_cast<EncodeFn>(encode_tiled);
+    if (encode == nullptr) {
+        set_last_error_msg("cuTensorMapEncodeTiled is unavailable from the driver");
+        return GMI_ERR_CUDA;
+    }
+    const cuuint64_t esize = f64 ? 8 : 4;
+    cuuint64_t dims[2] = {(cuuint64_t)kRecLen, (cuuint64_t)(n > 0 ? n : 1)};
+    cuuint64_t strides[1] = {kRecLen * esize};
+    cuuint32_t box[2] = {(cuuint32_t)kRecLen, (cuuint32_t)kTile};
+    cuuint32_t estr[2] = {1, 1};
+    const CUresult r = encode(map, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                              const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_last_error_msg("cuTensorMapEncodeTiled failed");
+        return GMI_ERR_CUDA;
+    }
+    return GMI_OK;
+}
+
+gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, const void *tgt_rec, int tgt_start,
+                            int n_tgt, const void *src_rec, int n_src, const PairConsts &k, double *out,
+                            int accumulate)
+{
+    if (n_tgt <= 0) return GMI_OK;
+    const int nout = nout_of(kind);
+    if (n_src <= 0) {
+        if (!accumulate) GMI_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)n_tgt * nout * sizeof(double), env.stream));
+        return GMI_OK;
+    }
+    const int sidx = shape_index(env.tpb, env.tt);
+    const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;
+    void *fn = kernel_ptr(kind, f64, sidx);
+    const size_t smem = ring_bytes(f64);
+    GMI_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, tpb, smem));
+    const int n_tgt_ctas = (n_tgt + tpb * tt - 1) / (tpb * tt);
+    const int slots = env.sm_count * (occ > 0 ? occ : 1);
+    int splits = 1;
+    if (n_tgt_ctas < 2 * slots) splits = (2 * slots + n_tgt_ctas - 1) / n_tgt_ctas;
+    const int max_by_src = (n_src + kTile - 1) / kTile;
+    if (splits > max_by_src) splits = max_by_src;
+    const size_t per_split = (size_t)n_tgt * nout * sizeof(double);
+    const int max_by_scratch = env.partial_bytes / per_split > 0 ? (int)(env.partial_bytes / per_split) : 1;
+    if (splits > max_by_scratch) splits = max_by_scratch;
+    if (splits < 1) splits = 1;
+    int chunk = (n_src + splits - 1) / splits;
+    chunk = (chunk + kTile - 1) / kTile * kTile;
+    splits = (n_src + chunk - 1) / chunk;
+
+    PairLaunch a{};
+    a.tgt_rec = tgt_rec;
+    a.tgt_start = tgt_start;
+    a.n_tgt = n_tgt;
+    a.n_src = n_src;
+    a.chunk = chunk;
+    a.k = k;
+    a.out = out;
+    a.accumulate = accumulate;
+    a.err = env.err;
+    a.partial = splits > 1 ? env.partial : nullptr;
+    CUtensorMap map;
+    gmi_status st = encode_record_map(env.encode_tiled, &map, src_rec, n_src, f64);
+    if (st != GMI_OK) return st;
+    void *params[] = {&map, &a};
+    GMI_CUDA_TRY(cudaLaunchKernel(fn, dim3(n_tgt_ctas, splits), dim3(tpb), params, smem, env.stream));
+    if (splits > 1) {
+        const int count = n_tgt * nout;
+        reduce_splits<<<(count + 255) / 256, 256, 0, env.stream>>>(a.partial, splits, count, out, accumulate);
+        GMI_CUDA_TRY(cudaGetLastError());
+    }
+    return GMI_OK;
+}
+
+}  // namespace gmi

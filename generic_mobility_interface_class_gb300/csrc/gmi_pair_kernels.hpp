@@ -53,4 +53,22 @@ gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &a);
 gmi_status autotune_pair(gmi_context *ctx, int kind, const void *tgt_rec, int n_tgt, const void *src_rec, int n_src,
                          const PairConsts &k, double *out);
 
+// Everything a pair launch needs, supplied by the caller instead of a context.
+struct ExplicitPairEnv {
+    cudaStream_t stream;
+    double *partial;       // split partial sums
+    size_t partial_bytes;  // capacity of `partial`; bounds the number of splits
+    unsigned *err;         // device error word
+    void *encode_tiled;    // cuTensorMapEncodeTiled
+    int sm_count;
+    int tpb, tt;           // launch shape
+};
+
+size_t record_bytes(bool f64);
+gmi_status pack_records_into(cudaStream_t stream, bool f64, const double *x, const double *f, int nf, int n,
+                             void *dst);
+gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, const void *tgt_rec, int tgt_start,
+                            int n_tgt, const void *src_rec, int n_src, const PairConsts &k, double *out,
+                            int accumulate);
+
 }  // namespace gmi

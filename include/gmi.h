@@ -105,6 +105,22 @@ GMI_API gmi_status gmi_Mbs_mult(gmi_context *ctx, double *V_d, const double *F_s
                         const double *Xs_d, int start_blob, int num_blobs, int total_blobs,
                         int total_segs, double rseg, double rblob, double mu);
 
+/* Allocation-free form of gmi_Mss_mult, for callers that cannot call
+ * cudaMalloc: programs that fix their device-memory budget at start-up and
+ * hand it all to their own allocator, or that cannot accept the device-wide
+ * synchronisation cudaMalloc/cudaFree imply.  It needs no gmi_context:
+ * scratch comes from a 16 MiB array compiled into the library, which every
+ * GPU that loads the library holds until process exit.  Limit:
+ * total_segs <= 32768 (larger problems return GMI_ERR_ARG).  precision is a
+ * gmi_precision; cuda_stream a cudaStream_t (NULL = legacy default stream).
+ * The first call on a device (that device current) looks up the array's
+ * device address; make it before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU race.  Returns when V is complete.
+ * No counterpart in the reference. */
+GMI_API gmi_status gmi_Mss_mult_noalloc(double *V_d, const double *F_d, const double *X_d, int start_seg,
+                                        int num_segs, int total_segs, double rseg, double mu, int precision,
+                                        void *cuda_stream);
+
 /* Short-range barrier forces.  Segment targets ADD into f_segs[6*i+0..2];
  * blob targets OVERWRITE f_blobs_repulsion[3*(i-start_blob)..] (skipped when
  * wall != 0, as with the reference's prescribed wall bodies).  Segments
