@@ -79,6 +79,12 @@ SIGNATURES = {
     "gmi_solver_compute_velocities": ([_P, _P, _P, _P, ctypes.POINTER(_I)], _I),
     "gmi_solver_get_v_bodies": ([_P, _P], _I),
     "gmi_solver_set_v_bodies": ([_P, _P], _I),
+    "gmi_sim_create": ([_P, _P, _P, _P, _P, _P, ctypes.POINTER(_P)], _I),
+    "gmi_sim_destroy": ([_P], _I),
+    "gmi_sim_solver": ([_P], _P),
+    "gmi_sim_prepare": ([_P, _P], _I),
+    "gmi_sim_step": ([_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
+    "gmi_sim_get_state": ([_P, _I, _P], _I),
 }
 
 
@@ -87,6 +93,12 @@ class SolverConfig(ctypes.Structure):
     _fields_ = [("nswim", _I), ("nfil", _I), ("nseg", _I), ("nblob", _I), ("mu", _D), ("rseg", _D),
                 ("rblob", _D), ("repulsive_force_factor", _D), ("end_force_magnitude", _D), ("wall", _I),
                 ("max_linear_iter", _I), ("linear_tol", _D), ("precision", _I), ("device", _I)]
+
+
+class SimConfig(ctypes.Structure):
+    """gmi_sim_config (include/gmi.h)."""
+    _fields_ = [("mobility", SolverConfig), ("kb", _D), ("kt", _D), ("dt", _D), ("num_euler_steps", _I),
+                ("max_broyden_iter", _I), ("tol", _D), ("jacobian_confidence", _D), ("body_radius", _D)]
 
 
 class HostArrays(ctypes.Structure):

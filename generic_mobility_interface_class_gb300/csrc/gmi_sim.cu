@@ -1,0 +1,1504 @@
+// gmi_sim.cu -- the implicit time step of the ciliated-swimmer simulator on
+// the GPU: Broyden's method over the filament Lagrange multipliers, segment
+// Lie-algebra rotations and body state, each iteration evaluating the
+// velocities through the device-resident mobility solver (gmi_solver.cu).
+//
+// Restates, for free-swimming spherical bodies with instability-driven
+// (end-force) filaments and the GMRES linear solve:
+//   cilia_sim_main.cpp:205-343         the step / Broyden loop (host, below)
+//   rigid_body.cpp:247-381              body initial guess, update
+//   segment.cpp:38-90                   segment initial guess, update
+//   filament.cpp:416-463, 825-1018      robot arm, state from body, initial guess
+//   filament.cpp:1096-1220              elastic moments, internal forces
+//   filament.cpp:1222-1539              approximate Jacobian and its inverse
+//   swimmer.cpp:276-325, 329-688 (GMRES branch 466-682)  forces, Schur complement
+//   swimmer.cpp:690-845 (branch 793-837)                  inverse-Jacobian apply
+//   swimmer.cpp:847-871                 state update
+//   mobility_solver.cpp:1404-1689       Broyden residual (compute_errors)
+//   broyden_solver.cpp:26-130           rank-one inverse-Jacobian updates
+// All state is FP64 in HBM; one thread (or one CTA) per filament, one
+// thread per segment where the work is per segment.
+//
+// Layout (F = nswim*nfil filaments, S = F*nseg segments, W swimmers):
+//   segments: x (solver), q[4S] qm1[4S] u[3S] um1[3S] xm1[3S] xm2[3S]
+//   filaments: lambda[3(nseg-1)F] (+m1, m2), tether[3F], clamp[3F] (+m1, m2),
+//              inverse Jacobian [F][6nseg x 6nseg] column-major, jacB [F][6 x 6nseg]
+//   bodies: x, q, f (solver), xm1 xm2 u um1 [3W], qm1 [4W], Q_init [9W] row-major,
+//           schur_inv [36W] column-major
+//   Broyden: C, D [nbroy x max_iter] column-major, error/new_error/update [nbroy]
+//   with nbroy = W * (6*nfil*nseg + 6), the reference's unknown ordering
+//   (per swimmer: per filament [tether, lambdas, clamp, segment u's], then body).
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "gmi_context.hpp"
+#include "gmi_lie.cuh"
+#include "gmi_solver_internal.hpp"
+
+namespace gmi {
+
+struct SimP {
+    int W, NF, NS, NB, F, S, nbroy, per_body, n6, neuler;
+    double DL, DT, KB, KT, MU, RSEG, EFM, TOL, Rbody, conf;
+    // segment state
+    double *x, *f, *v;  // solver arrays: x_segs, f_segs, v_segs
+    double *q, *qm1, *u, *um1, *xm1, *xm2;
+    // filament state
+    double *lam, *lam1, *lam2, *tl, *tl1, *tl2, *cl, *cl1, *cl2, *p1, *p2, *st, *fref;
+    double *invJ, *ecb1, *ecb2, *jacB;
+    // body state
+    double *bx, *bq, *bf, *vb;  // solver arrays: body_x, body_q, body_f, v_bodies
+    double *bxm1, *bxm2, *bu, *bum1, *bqm1, *bQ, *schur;
+    double *mob_ref;
+    int *flags;  // [0] error too large, [1] non-finite error, [2] singular Jacobian
+};
+
+__device__ __forceinline__ Q4 ldq(const double *p) { return Q4{p[0], p[1], p[2], p[3]}; }
+__device__ __forceinline__ void stq(double *p, const Q4 &q) { p[0] = q.s; p[1] = q.x; p[2] = q.y; p[3] = q.z; }
+__device__ __forceinline__ M3 ldm3(const double *p) { M3 m; for (int k = 0; k < 9; ++k) m.a[k] = p[k]; return m; }
+
+// robot_arm (filament.cpp:416-436): positions by midpoint-tangent chaining.
+__device__ void robot_arm(const SimP &P, int fil)
+{
+    const int s0 = fil * P.NS;
+    double t1[3], t2[3];
+    q_tangent(ldq(P.q + 4 * s0), t1);
+    for (int i = 1; i < P.NS; ++i) {
+        const int s = s0 + i;
+        q_tangent(ldq(P.q + 4 * s), t2);
+        for (int c = 0; c < 3; ++c) P.x[3 * s + c] = P.x[3 * (s - 1) + c] + 0.5 * P.DL * (t1[c] + t2[c]);
+        t1[0] = t2[0]; t1[1] = t2[1]; t1[2] = t2[2];
+    }
+}
+
+// segment::update (segment.cpp:68-74): u += du; q = lie_exp(u) qm1
+__device__ void segment_update(const SimP &P, int s, const double *du)
+{
+    for (int c = 0; c < 3; ++c) P.u[3 * s + c] += du[c];
+    stq(P.q + 4 * s, qmul(lie_exp(P.u + 3 * s), ldq(P.qm1 + 4 * s)));
+}
+
+// filament base position: body x + R(body q) ref (swimmer.cpp:252-254, 858-860)
+__device__ void base_position(const SimP &P, int fil, double *base)
+{
+    const int n = fil / P.NF;
+    const M3 R = q_rot_mat(ldq(P.bq + 4 * n));
+    double d[3];
+    m3_vec(R, P.fref + 3 * fil, d);
+    for (int c = 0; c < 3; ++c) base[c] = P.bx[3 * n + c] + d[c];
+}
+
+// accept_state_from_rigid_body (filament.cpp:438-463)
+__device__ void accept_state_from_body(const SimP &P, int fil)
+{
+    const int n = fil / P.NF, s0 = fil * P.NS;
+    double base[3];
+    base_position(P, fil, base);
+    for (int c = 0; c < 3; ++c) P.x[3 * s0 + c] = base[c];
+    const double du[3] = {P.bu[3 * n] - P.u[3 * s0], P.bu[3 * n + 1] - P.u[3 * s0 + 1], P.bu[3 * n + 2] - P.u[3 * s0 + 2]};
+    segment_update(P, s0, du);
+    robot_arm(P, fil);
+}
+
+// rigid_body::initial_guess (rigid_body.cpp:247-290)
+__global__ void body_initial_guess_kernel(SimP P, int nt)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.W) return;
+    double *x = P.bx + 3 * n, *xm1 = P.bxm1 + 3 * n, *xm2 = P.bxm2 + 3 * n, *u = P.bu + 3 * n, *um1 = P.bum1 + 3 * n;
+    double gx[3], gu[3];
+    for (int c = 0; c < 3; ++c) {
+        if (nt <= P.neuler) {
+            gx[c] = 2.0 * x[c] - xm1[c];
+            gu[c] = u[c];
+        } else {
+            gx[c] = 3.0 * (x[c] - xm1[c]) + xm2[c];
+            gu[c] = 2.0 * u[c] - um1[c];
+        }
+    }
+    for (int c = 0; c < 3; ++c) {
+        xm2[c] = xm1[c];
+        xm1[c] = x[c];
+        x[c] = gx[c];
+        um1[c] = u[c];
+        u[c] = gu[c];
+    }
+    const Q4 q = ldq(P.bq + 4 * n);
+    stq(P.bqm1 + 4 * n, q);
+    const Q4 qn = qmul(lie_exp(u), q);
+    stq(P.bq + 4 * n, qn);
+    const M3 R = q_rot_mat(qn);
+    for (int k = 0; k < 9; ++k) P.bQ[9 * n + k] = R.a[k];
+}
+
+__device__ void extrapolate3(double *a, double *a1, double *a2, int count, int nt)
+{
+    for (int k = 0; k < count; ++k) {
+        if (nt == 1) {
+            a1[k] = a[k];
+        } else if (nt == 2) {
+            a2[k] = a1[k];
+            a1[k] = a[k];
+            a[k] = 2.0 * a1[k] - a2[k];
+        } else if (nt > 2) {
+            const double t = 3.0 * (a[k] - a1[k]) + a2[k];
+            a2[k] = a1[k];
+            a1[k] = a[k];
+            a[k] = t;
+        }
+    }
+}
+
+// filament::initial_guess (filament.cpp:825-1018) with segment::initial_guess
+// (segment.cpp:38-66) and the state taken from the body.
+__global__ void filament_initial_guess_kernel(SimP P, int nt)
+{
+    const int fil = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fil >= P.F) return;
+    for (int i = 0; i < P.NS; ++i) {
+        const int s = fil * P.NS + i;
+        for (int c = 0; c < 3; ++c) {
+            P.xm2[3 * s + c] = P.xm1[3 * s + c];
+            P.xm1[3 * s + c] = P.x[3 * s + c];
+        }
+        if (nt <= P.neuler) {
+            for (int c = 0; c < 3; ++c) P.um1[3 * s + c] = P.u[3 * s + c];
+        } else {
+            for (int c = 0; c < 3; ++c) {
+                const double t = 2.0 * P.u[3 * s + c] - P.um1[3 * s + c];
+                P.um1[3 * s + c] = P.u[3 * s + c];
+                P.u[3 * s + c] = t;
+            }
+        }
+        const Q4 q = ldq(P.q + 4 * s);
+        stq(P.qm1 + 4 * s, q);
+        stq(P.q + 4 * s, qmul(lie_exp(P.u + 3 * s), q));
+    }
+    accept_state_from_body(P, fil);
+    const int nl = 3 * (P.NS - 1);
+    extrapolate3(P.lam + nl * fil, P.lam1 + nl * fil, P.lam2 + nl * fil, nl, nt);
+    extrapolate3(P.tl + 3 * fil, P.tl1 + 3 * fil, P.tl2 + 3 * fil, 3, nt);
+    extrapolate3(P.cl + 3 * fil, P.cl1 + 3 * fil, P.cl2 + 3 * fil, 3, nt);
+}
+
+// body_frame_moment (filament.cpp:1096-1110)
+__device__ void body_frame_moment(const SimP &P, int fil, int link, double *M)
+{
+    const int s = fil * P.NS + link;
+    const Q4 qa = ldq(P.q + 4 * s), qb = ldq(P.q + 4 * (s + 1));
+    Q4 mq = qconj(midpoint_quaternion(qa, qb));
+    mq = qscale(qdiv(qmul(mq, qsub(qb, qa)), P.DL), 2.0);
+    const double *st = P.st + 3 * fil;
+    M[0] = P.KT * (mq.x - st[0]);
+    M[1] = P.KB * (mq.y - st[1]);
+    M[2] = P.KB * (mq.z - st[2]);
+}
+
+// filament::internal_forces_and_torques (filament.cpp:1112-1220), instability cilia
+__global__ void filament_forces_kernel(SimP P, int nt)
+{
+    const int fil = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fil >= P.F) return;
+    const int s0 = fil * P.NS;
+    double *f = P.f + 6 * (size_t)s0;
+    for (int k = 0; k < 6 * P.NS; ++k) f[k] = 0.0;
+    const double hdl = 0.5 * P.DL;
+    for (int i = 0; i < P.NS - 1; ++i) {
+        const double *lam = P.lam + 3 * (P.NS - 1) * fil + 3 * i;
+        f[6 * i] -= lam[0];
+        f[6 * i + 1] -= lam[1];
+        f[6 * i + 2] -= lam[2];
+        f[6 * (i + 1)] += lam[0];
+        f[6 * (i + 1) + 1] += lam[1];
+        f[6 * (i + 1) + 2] += lam[2];
+        double t[3];
+        q_tangent(ldq(P.q + 4 * (s0 + i)), t);
+        f[6 * i + 3] -= hdl * (t[1] * lam[2] - t[2] * lam[1]);
+        f[6 * i + 4] -= hdl * (t[2] * lam[0] - t[0] * lam[2]);
+        f[6 * i + 5] -= hdl * (t[0] * lam[1] - t[1] * lam[0]);
+        q_tangent(ldq(P.q + 4 * (s0 + i + 1)), t);
+        f[6 * (i + 1) + 3] -= hdl * (t[1] * lam[2] - t[2] * lam[1]);
+        f[6 * (i + 1) + 4] -= hdl * (t[2] * lam[0] - t[0] * lam[2]);
+        f[6 * (i + 1) + 5] -= hdl * (t[0] * lam[1] - t[1] * lam[0]);
+        const Q4 qmid = midpoint_quaternion(ldq(P.q + 4 * (s0 + i)), ldq(P.q + 4 * (s0 + i + 1)));
+        const M3 R = q_rot_mat(qmid);
+        double Mb[3], M[3];
+        body_frame_moment(P, fil, i, Mb);
+        m3_vec(R, Mb, M);
+        f[6 * i + 3] += M[0];
+        f[6 * i + 4] += M[1];
+        f[6 * i + 5] += M[2];
+        f[6 * (i + 1) + 3] -= M[0];
+        f[6 * (i + 1) + 4] -= M[1];
+        f[6 * (i + 1) + 5] -= M[2];
+    }
+    f[0] += P.tl[3 * fil];
+    f[1] += P.tl[3 * fil + 1];
+    f[2] += P.tl[3 * fil + 2];
+    double t[3];
+    q_tangent(ldq(P.q + 4 * (s0 + P.NS - 1)), t);
+    f[6 * (P.NS - 1)] -= P.EFM * t[0];
+    f[6 * (P.NS - 1) + 1] -= P.EFM * t[1];
+    f[6 * (P.NS - 1) + 2] -= P.EFM * t[2];
+    if (nt == 0) {  // one-off perturbation of segments 4 and 12 (filament.cpp:1181-1196)
+        if (4 < P.NS)
+            for (int c = 0; c < 3; ++c) f[6 * 4 + c] += P.p1[3 * fil + c];
+        if (12 < P.NS)
+            for (int c = 0; c < 3; ++c) f[6 * 12 + c] += P.p2[3 * fil + c];
+    }
+    double ct[3];
+    dexpinv_transpose(ct, P.u + 3 * s0, P.cl + 3 * fil);
+    f[3] += ct[0];
+    f[4] += ct[1];
+    f[5] += ct[2];
+}
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Free-swimming force/torque balance (swimmer.cpp:276-325): body f = -sum of
+// segment forces and torques about the body centre.  One CTA per swimmer.
+__global__ void __launch_bounds__(256) swimmer_force_sum_kernel(SimP P)
+{
+    __shared__ double red[6][8];
+    const int n = blockIdx.x;
+    const int per = P.NF * P.NS;
+    const double *X = P.bx + 3 * n;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = threadIdx.x; k < per; k += 256) {
+        const int s = n * per + k;
+        const double *fs = P.f + 6 * (size_t)s;
+        const double dx = P.x[3 * s] - X[0], dy = P.x[3 * s + 1] - X[1], dz = P.x[3 * s + 2] - X[2];
+        a[0] += fs[0];
+        a[1] += fs[1];
+        a[2] += fs[2];
+        a[3] += fs[3] + dy * fs[2] - dz * fs[1];
+        a[4] += fs[4] + dz * fs[0] - dx * fs[2];
+        a[5] += fs[5] + dx * fs[1] - dy * fs[0];
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int c = 0; c < 6; ++c) {
+        const double v = warp_sum_d(a[c]);
+        if (lane == 0) red[c][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double s = 0.0;
+        for (int w = 0; w < 8; ++w) s += red[threadIdx.x][w];
+        P.bf[6 * n + threadIdx.x] = -s;
+    }
+}
+
+// compute_errors (mobility_solver.cpp:1404-1689), GMRES branch.
+__global__ void compute_errors_kernel(SimP P, int nt, double *err)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const double c1 = -4.0 / 3.0, c2 = 1.0 / 3.0, c3 = -2.0 / 3.0;
+    const bool euler = nt < P.neuler;
+    bool big = false, bad = false;
+    if (g < P.S) {
+        const int per = P.NF * P.NS;
+        const int n = g / per, i = (g / P.NS) % P.NF, j = g % P.NS;
+        const double *v = P.v + 6 * (size_t)g, *om = v + 3;
+        int id = n * P.per_body + 6 * i * P.NS + 3 * j;
+        for (int c = 0; c < 3; ++c) {
+            const double x = P.x[3 * g + c], xm1 = P.xm1[3 * g + c], xm2 = P.xm2[3 * g + c];
+            const double e = euler ? x - xm1 - P.DT * v[c] : x + c1 * xm1 + c2 * xm2 + c3 * P.DT * v[c];
+            err[id + c] = e;
+            big |= fabs(e) > P.DL * P.TOL;
+            bad |= !isfinite(e);
+        }
+        id += 3 * P.NS;
+        double Wv[3];
+        dexpinv(Wv, P.u + 3 * g, om);
+        for (int c = 0; c < 3; ++c) {
+            const double u = P.u[3 * g + c], um1 = P.um1[3 * g + c];
+            const double e = euler ? u - P.DT * Wv[c] : u - c2 * um1 + c3 * P.DT * Wv[c];
+            err[id + c] = e;
+            big |= fabs(e) > P.TOL;
+            bad |= !isfinite(e);
+        }
+    } else if (g < P.S + P.W) {
+        const int n = g - P.S;
+        const int id = n * P.per_body + 6 * P.NF * P.NS;
+        const double *V = P.vb + 6 * n;
+        double w[3];
+        dexpinv(w, P.bu + 3 * n, V + 3);
+        for (int c = 0; c < 3; ++c) {
+            const double x = P.bx[3 * n + c], xm1 = P.bxm1[3 * n + c], xm2 = P.bxm2[3 * n + c];
+            const double e = euler ? x - xm1 - P.DT * V[c] : x + c1 * xm1 + c2 * xm2 + c3 * P.DT * V[c];
+            err[id + c] = e;
+            big |= fabs(e) > P.TOL * P.DL;
+            bad |= !isfinite(e);
+        }
+        for (int c = 0; c < 3; ++c) {
+            const double u = P.bu[3 * n + c], um1 = P.bum1[3 * n + c];
+            const double e = euler ? u - P.DT * w[c] : u - c2 * um1 + c3 * P.DT * w[c];
+            err[id + 3 + c] = e;
+            big |= fabs(e) > P.TOL;
+            bad |= !isfinite(e);
+        }
+    }
+    if (big) atomicOr(P.flags, 1);
+    if (bad) atomicOr(P.flags + 1, 1);
+}
+
+// body_frame_moment_lie_derivative (filament.cpp:8-55): 3x3
+__device__ M3 bfm_lie_derivative(const SimP &P, const Q4 &q1, const Q4 &q2, bool upper)
+{
+    double A[12], L[16];
+    if (upper) {
+        q_psi_mat(q2, A);
+        for (int k = 0; k < 12; ++k) A[k] /= P.DL;
+    } else {
+        q_psi_mat(q1, A);
+        for (int k = 0; k < 12; ++k) A[k] /= -P.DL;
+    }
+    Q4 mq = qconj(midpoint_quaternion(q1, q2));
+    q_left_mult_mat(mq, L);
+    double dM[12];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += L[4 * i + k] * A[3 * k + j];
+            dM[3 * i + j] = s;
+        }
+    mq = qdiv(qsub(q2, q1), P.DL);
+    q_left_mult_mat(mq, L);
+    const double sc = upper ? 0.5 * P.DL : -0.5 * P.DL;
+    for (int k = 0; k < 12; ++k) A[k] *= sc;
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += L[4 * i + k] * A[3 * k + j];
+            dM[3 * i + j] += s;
+        }
+    M3 out;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) out(i, j) = 2.0 * dM[3 * (i + 1) + j];
+    for (int j = 0; j < 3; ++j) {
+        out(0, j) *= P.KT;
+        out(1, j) *= P.KB;
+        out(2, j) *= P.KB;
+    }
+    return out;
+}
+
+__device__ M3 frame_cross(const double K0, const double K1, const double K2, const Q4 &q)
+{
+    double t[3], nn[3], b[3];
+    q_tangent(q, t);
+    q_normal(q, nn);
+    q_binormal(q, b);
+    return m3_add(m3_add(m3_scale(rcross(t), K0), m3_scale(rcross(nn), K1)), m3_scale(rcross(b), K2));
+}
+
+// -tsf (dOmega - 0.5 (OmegaMat + LieMat dOmega) + (rcross(OmegaMat u) + LieMat OmegaMat + LieMat^2 dOmega)/12)
+__device__ M3 diag_block(double tsf, const M3 &dOm, const M3 &Lie, const M3 &Om, const double *u)
+{
+    double Ou[3];
+    m3_vec(Om, u, Ou);
+    const M3 LdO = m3_mul(Lie, dOm);
+    M3 t = m3_sub(dOm, m3_scale(m3_add(Om, LdO), 0.5));
+    const M3 q = m3_add(m3_add(rcross(Ou), m3_mul(Lie, Om)), m3_mul(m3_mul(Lie, Lie), dOm));
+    t = m3_add(t, m3_scale(q, 1.0 / 12.0));
+    return m3_scale(t, -tsf);
+}
+
+// -tsf (dOmega - 0.5 LieMat dOmega + LieMat^2 dOmega / 12)
+__device__ M3 off_block(double tsf, const M3 &dOm, const M3 &Lie)
+{
+    M3 t = m3_sub(dOm, m3_scale(m3_mul(Lie, dOm), 0.5));
+    t = m3_add(t, m3_scale(m3_mul(m3_mul(Lie, Lie), dOm), 1.0 / 12.0));
+    return m3_scale(t, -tsf);
+}
+
+// filament::jacobian_lie_algebra_block (filament.cpp:1222-1404), written into
+// J at rows/cols [3NS, 6NS).
+__device__ void lie_algebra_block(const SimP &P, int fil, int nt, double *J, int ld)
+{
+    const int NS = P.NS, s0 = fil * NS, o = 3 * NS;
+    const double tsf = (nt < P.neuler) ? P.DT : 2.0 * P.DT / 3.0;
+    const double Tfac = 1.0 / (8.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
+    const double *lam = P.lam + 3 * (NS - 1) * fil;
+    const double *f = P.f + 6 * (size_t)s0;
+    auto Q = [&](int k) { return ldq(P.q + 4 * (s0 + k)); };
+    auto Tn = [&](int k, double *t) { q_tangent(Q(k), t); };
+    double Kph[3], Kmh[3], t[3], om[3];
+    // first segment
+    {
+        Tn(0, t);
+        const M3 Cp = m3_mul(m3_scale(rcross(lam), -0.5 * P.DL), rcross(t));
+        const Q4 qph = midpoint_quaternion(Q(0), Q(1));
+        body_frame_moment(P, fil, 0, Kph);
+        M3 LD = bfm_lie_derivative(P, Q(0), Q(1), false);
+        M3 El = m3_scale(frame_cross(Kph[0], Kph[1], Kph[2], Q(0)), 0.5);
+        const M3 R = q_rot_mat(qph);
+        El = m3_add(El, m3_mul(R, LD));
+        M3 dOm = m3_scale(m3_add(El, Cp), Tfac);
+        const M3 Lie = m3_scale(rcross(P.u + 3 * s0), -1.0);
+        for (int c = 0; c < 3; ++c) om[c] = Tfac * f[3 + c];
+        const M3 Om = rcross(om);
+        put_block(J, ld, o, o, diag_block(tsf, dOm, Lie, Om, P.u + 3 * s0));
+        LD = bfm_lie_derivative(P, Q(0), Q(1), true);
+        El = m3_scale(frame_cross(Kph[0], Kph[1], Kph[2], Q(1)), 0.5);
+        El = m3_add(El, m3_mul(R, LD));
+        dOm = m3_scale(El, Tfac);
+        put_block(J, ld, o, o + 3, off_block(tsf, dOm, Lie));
+    }
+    // last segment
+    {
+        const int e = NS - 1;
+        Tn(e, t);
+        const M3 Cp = m3_mul(m3_scale(rcross(lam + 3 * (NS - 2)), -0.5 * P.DL), rcross(t));
+        const Q4 qmh = midpoint_quaternion(Q(e - 1), Q(e));
+        body_frame_moment(P, fil, NS - 2, Kmh);
+        M3 LD = bfm_lie_derivative(P, Q(e - 1), Q(e), true);
+        M3 El = m3_scale(frame_cross(Kmh[0], Kmh[1], Kmh[2], Q(e)), -0.5);
+        const M3 R = q_rot_mat(qmh);
+        El = m3_sub(El, m3_mul(R, LD));
+        M3 dOm = m3_scale(m3_add(El, Cp), Tfac);
+        const M3 Lie = m3_scale(rcross(P.u + 3 * (s0 + e)), -1.0);
+        for (int c = 0; c < 3; ++c) om[c] = Tfac * f[6 * e + 3 + c];
+        const M3 Om = rcross(om);
+        put_block(J, ld, o + 3 * e, o + 3 * e, diag_block(tsf, dOm, Lie, Om, P.u + 3 * (s0 + e)));
+        LD = bfm_lie_derivative(P, Q(e - 1), Q(e), false);
+        El = m3_scale(frame_cross(Kmh[0], Kmh[1], Kmh[2], Q(e - 1)), -0.5);
+        El = m3_sub(El, m3_mul(R, LD));
+        dOm = m3_scale(El, Tfac);
+        put_block(J, ld, o + 3 * e, o + 3 * e - 3, off_block(tsf, dOm, Lie));
+    }
+    for (int k = 1; k < NS - 1; ++k) {
+        Tn(k, t);
+        const M3 Lie = m3_scale(rcross(P.u + 3 * (s0 + k)), -1.0);
+        for (int c = 0; c < 3; ++c) om[c] = Tfac * f[6 * k + 3 + c];
+        const M3 Om = rcross(om);
+        body_frame_moment(P, fil, k, Kph);
+        body_frame_moment(P, fil, k - 1, Kmh);
+        const Q4 qph = midpoint_quaternion(Q(k), Q(k + 1));
+        const Q4 qmh = midpoint_quaternion(Q(k - 1), Q(k));
+        const double lv[3] = {lam[3 * (k - 1)] + lam[3 * k], lam[3 * (k - 1) + 1] + lam[3 * k + 1],
+                              lam[3 * (k - 1) + 2] + lam[3 * k + 2]};
+        const M3 Cp = m3_mul(m3_scale(rcross(lv), -0.5 * P.DL), rcross(t));
+        M3 LD = bfm_lie_derivative(P, Q(k), Q(k + 1), false);
+        M3 El = m3_scale(frame_cross(Kph[0], Kph[1], Kph[2], Q(k)), 0.5);
+        const M3 Rph = q_rot_mat(qph);
+        El = m3_add(El, m3_mul(Rph, LD));
+        M3 LDm = bfm_lie_derivative(P, Q(k - 1), Q(k), true);
+        El = m3_sub(El, m3_scale(frame_cross(Kmh[0], Kmh[1], Kmh[2], Q(k)), 0.5));
+        const M3 Rmh = q_rot_mat(qmh);
+        El = m3_sub(El, m3_mul(Rmh, LDm));
+        M3 dOm = m3_scale(m3_add(Cp, El), Tfac);
+        put_block(J, ld, o + 3 * k, o + 3 * k, diag_block(tsf, dOm, Lie, Om, P.u + 3 * (s0 + k)));
+        LDm = bfm_lie_derivative(P, Q(k - 1), Q(k), false);
+        El = m3_scale(frame_cross(Kmh[0], Kmh[1], Kmh[2], Q(k - 1)), -0.5);
+        El = m3_sub(El, m3_mul(Rmh, LDm));
+        dOm = m3_scale(El, Tfac);
+        put_block(J, ld, o + 3 * k, o + 3 * k - 3, off_block(tsf, dOm, Lie));
+        LD = bfm_lie_derivative(P, Q(k), Q(k + 1), true);
+        El = m3_scale(frame_cross(Kph[0], Kph[1], Kph[2], Q(k + 1)), 0.5);
+        El = m3_add(El, m3_mul(Rph, LD));
+        dOm = m3_scale(El, Tfac);
+        put_block(J, ld, o + 3 * k, o + 3 * k + 3, off_block(tsf, dOm, Lie));
+    }
+    for (int k = 0; k < 3 * NS; ++k) J[(o + k) + (size_t)ld * (o + k)] += 1.0;
+}
+
+// filament::invert_approx_jacobian (filament.cpp:1406-1539) up to the
+// inversion: the approximate Jacobian in invJ, the two clamping blocks saved.
+__global__ void build_jacobian_kernel(SimP P, int nt)
+{
+    const int fil = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fil >= P.F) return;
+    const int NS = P.NS, ld = P.n6, s0 = fil * NS;
+    double *J = P.invJ + (size_t)fil * ld * ld;
+    for (size_t k = 0; k < (size_t)ld * ld; ++k) J[k] = 0.0;
+    const bool euler = nt < P.neuler;
+    double fac = euler ? -P.DT / (6.0 * kPi * P.MU * P.RSEG) : -P.DT / (9.0 * kPi * P.MU * P.RSEG);
+    for (int i = 0; i < 3 * NS; ++i) {
+        J[i + (size_t)ld * i] = fac;
+        if (i < 3 * NS - 3) J[i + (size_t)ld * (i + 3)] = -fac;
+    }
+    double t[3];
+    for (int j = 1; j < NS; ++j) {
+        const int jpos = 3 * (NS + j);
+        q_tangent(ldq(P.q + 4 * (s0 + j)), t);
+        const M3 temp = m3_scale(rcross(t), P.DL);
+        put_block(J, ld, 3 * j, jpos, m3_scale(temp, 0.5));
+        for (int i = j + 1; i < NS; ++i) put_block(J, ld, 3 * i, jpos, temp);
+    }
+    q_tangent(ldq(P.q + 4 * (s0 + NS - 1)), t);
+    {
+        double et[3] = {t[0], t[1], t[2]};
+        const M3 sub = m3_scale(rcross(et), fac * P.EFM);
+        add_block(J, ld, 3 * (NS - 1), 3 * (2 * NS - 1), m3_scale(sub, -1.0));
+    }
+    fac = euler ? P.DL * P.DT / (16.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG)
+                : P.DL * P.DT / (24.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
+    for (int j = 1; j < NS; ++j) {
+        const int jpos = 3 * j;
+        int ipos = 3 * (NS + j - 1);
+        q_tangent(ldq(P.q + 4 * (s0 + j - 1)), t);
+        M3 um = rcross(P.u + 3 * (s0 + j - 1));
+        M3 tm = m3_scale(rcross(t), -1.0);
+        M3 blk = m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
+        put_block(J, ld, ipos, jpos, m3_scale(blk, fac));
+        ipos += 3;
+        q_tangent(ldq(P.q + 4 * (s0 + j)), t);
+        um = rcross(P.u + 3 * (s0 + j));
+        tm = m3_scale(rcross(t), -1.0);
+        blk = m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
+        put_block(J, ld, ipos, jpos, m3_scale(blk, fac));
+    }
+    lie_algebra_block(P, fil, nt, J, ld);
+    fac = euler ? -P.DT / (8.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG)
+                : -P.DT / (12.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
+    const M3 um = rcross(P.u + 3 * s0);
+    M3 blk = m3_add(m3_scale(um, 0.5), m3_scale(m3_mul(um, um), 1.0 / 12.0));
+    M3 blkT = m3_add(m3_scale(um, -0.5), m3_scale(m3_mul(um, um), 1.0 / 12.0));
+    for (int d = 0; d < 3; ++d) {
+        blk(d, d) += 1.0;
+        blkT(d, d) += 1.0;
+    }
+    const M3 e1 = get_block(J, ld, 3 * NS, 3 * NS), e2 = get_block(J, ld, 3 * NS + 3, 3 * NS);
+    for (int k = 0; k < 9; ++k) {
+        P.ecb1[9 * fil + k] = e1.a[k];
+        P.ecb2[9 * fil + k] = e2.a[k];
+    }
+    put_block(J, ld, 3 * NS, 3 * NS, m3_scale(m3_mul(blk, blkT), fac));
+    put_block(J, ld, 3 * NS + 3, 3 * NS, m3_zero());
+}
+
+// In-place inverse of n x n column-major matrices, one CTA each, Gauss-Jordan
+// with partial (row) pivoting and the column swaps undone at the end; the
+// matrix lives in shared memory when it fits.  Stands in for the reference's
+// LAPACK dgetrf + dgetri (matrix.cpp:538-566); a zero pivot sets flags[2].
+constexpr int kGjTpb = 256;
+
+__global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, int use_smem, int *flags)
+{
+    extern __shared__ double sh[];
+    double *Mg = mats + (size_t)blockIdx.x * n * n;
+    double *col = sh;                      // n
+    double *redv = col + n;                // 32
+    int *redi = reinterpret_cast<int *>(redv + 32);  // 32
+    int *perm = redi + 32;                 // n
+    double *A = use_smem ? reinterpret_cast<double *>(perm + ((n + 1) & ~1)) : Mg;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (use_smem)
+        for (int e = tid; e < n * n; e += kGjTpb) A[e] = Mg[e];
+    __syncthreads();
+    __shared__ int singular;
+    if (tid == 0) singular = 0;
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        double best = -1.0;
+        int bi = k;
+        for (int i = k + tid; i < n; i += kGjTpb) {
+            const double a = fabs(A[i + (size_t)n * k]);
+            if (a > best) {
+                best = a;
+                bi = i;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_down_sync(0xffffffffu, best, o);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            redv[wid] = best;
+            redi[wid] = bi;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double b = redv[0];
+            int p = redi[0];
+            for (int w = 1; w < kGjTpb / 32; ++w)
+                if (redv[w] > b || (redv[w] == b && redi[w] < p)) {
+                    b = redv[w];
+                    p = redi[w];
+                }
+            perm[k] = p;
+            if (!(b > 0.0)) singular = 1;
+        }
+        __syncthreads();
+        if (singular) break;
+        const int p = perm[k];
+        if (p != k)
+            for (int j = tid; j < n; j += kGjTpb) {
+                const double t = A[k + (size_t)n * j];
+                A[k + (size_t)n * j] = A[p + (size_t)n * j];
+                A[p + (size_t)n * j] = t;
+            }
+        __syncthreads();
+        const double pivinv = 1.0 / A[k + (size_t)n * k];
+        for (int i = tid; i < n; i += kGjTpb) col[i] = A[i + (size_t)n * k];
+        __syncthreads();
+        for (int j = tid; j < n; j += kGjTpb) A[k + (size_t)n * j] = (j == k) ? pivinv : A[k + (size_t)n * j] * pivinv;
+        __syncthreads();
+        for (int e = tid; e < n * n; e += kGjTpb) {
+            const int i = e % n, j = e / n;
+            if (i == k) continue;
+            A[e] = (j == k) ? -col[i] * pivinv : A[e] - A[k + (size_t)n * j] * col[i];
+        }
+        __syncthreads();
+    }
+    if (singular) {
+        if (tid == 0) atomicOr(flags + 2, 1);
+        return;
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        const int p = perm[k];
+        if (p != k)
+            for (int i = tid; i < n; i += kGjTpb) {
+                const double t = A[i + (size_t)n * k];
+                A[i + (size_t)n * k] = A[i + (size_t)n * p];
+                A[i + (size_t)n * p] = t;
+            }
+        __syncthreads();
+    }
+    if (use_smem)
+        for (int e = tid; e < n * n; e += kGjTpb) Mg[e] = A[e];
+}
+
+// rotated body mobility: Q B Q^T blockwise (swimmer.cpp:522-527)
+__device__ void rotated_mobility(const SimP &P, const M3 &Q, double *bm /*36, column-major*/)
+{
+    const M3 QT = m3_T(Q);
+    for (int bi = 0; bi < 2; ++bi)
+        for (int bj = 0; bj < 2; ++bj) {
+            const M3 b = get_block(P.mob_ref, 6, 3 * bi, 3 * bj);
+            put_block(bm, 6, 3 * bi, 3 * bj, m3_mul(m3_mul(Q, b), QT));
+        }
+}
+
+__device__ M3 mat6_block_mul(const double *bm6, int r0, int c0, const M3 &B)  // bm[r0.., c0..] (3x3) * B
+{
+    return m3_mul(get_block(bm6, 6, r0, c0), B);
+}
+
+// The B block of one filament (swimmer.cpp:553-670), then jacB = B * invJ
+// (swimmer.cpp:671).  One CTA per filament; thread 0 assembles B in shared
+// memory, all threads form the product.
+__global__ void __launch_bounds__(128) filament_B_kernel(SimP P, int nt)
+{
+    extern __shared__ double Bs[];  // 6 x n6, column-major
+    const int fil = blockIdx.x;
+    const int n = fil / P.NF, NS = P.NS, n6 = P.n6, s0 = fil * NS;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 6 * n6; ++k) Bs[k] = 0.0;
+        const double dt_fac = (nt < P.neuler) ? -P.DT : -2.0 * P.DT / 3.0;
+        const double *u = P.bu + 3 * n, *x = P.bx + 3 * n;
+        const M3 Qi = ldm3(P.bQ + 9 * n);
+        const M3 blc = m3_scale(rcross(u), -1.0);
+        const M3 blc2 = m3_scale(m3_mul(blc, blc), 1.0 / 12.0);
+        M3 Dinv = m3_sub(m3_add(m3_eye(), blc2), m3_scale(blc, 0.5));
+        M3 DinvT = m3_add(m3_add(m3_eye(), blc2), m3_scale(blc, 0.5));
+        double fbd[3];
+        m3_vec(Qi, P.fref + 3 * fil, fbd);
+        Bs[0 + 6 * 0] = -1.0;
+        Bs[1 + 6 * 1] = -1.0;
+        Bs[2 + 6 * 2] = -1.0;
+        put_block(Bs, 6, 3, 0, rcross(fbd));
+        put_block(Bs, 6, 3, 3 * NS, m3_scale(DinvT, -1.0));
+        double t[3], te[3];
+        q_tangent(ldq(P.q + 4 * (s0 + NS - 1)), t);
+        for (int c = 0; c < 3; ++c) te[c] = P.EFM * t[c];
+        const M3 Bend = rcross(te);
+        put_block(Bs, 6, 0, 6 * NS - 3, Bend);
+        double diff[3], w[3];
+        for (int c = 0; c < 3; ++c) diff[c] = P.x[3 * (s0 + NS - 1) + c] - x[c];
+        for (int c = 0; c < 3; ++c) w[c] = 0.5 * P.DL * t[c] - diff[c];
+        put_block(Bs, 6, 3, 6 * NS - 3, m3_mul(rcross(w), Bend));
+        for (int m = 1; m < NS - 1; ++m) {
+            double tm[3], dtm[3];
+            q_tangent(ldq(P.q + 4 * (s0 + m)), tm);
+            for (int c = 0; c < 3; ++c) dtm[c] = P.DL * tm[c];
+            put_block(Bs, 6, 3, 3 * (NS + m), m3_mul(Bend, rcross(dtm)));
+        }
+        // B = body_mobility * B
+        double bm[36];
+        rotated_mobility(P, Qi, bm);
+        for (int c = 0; c < n6; ++c) {
+            double colv[6];
+            for (int r = 0; r < 6; ++r) {
+                double s = 0.0;
+                for (int k = 0; k < 6; ++k) s += bm[r + 6 * k] * Bs[k + 6 * c];
+                colv[r] = s;
+            }
+            for (int r = 0; r < 6; ++r) Bs[r + 6 * c] = colv[r];
+        }
+        // sphere corrections (swimmer.cpp:604-658)
+        const double R = P.Rbody;
+        const double R2 = R * R + P.RSEG * P.RSEG;
+        for (int k = 0; k < NS; ++k) {
+            double rh[3];
+            for (int c = 0; c < 3; ++c) rh[c] = P.x[3 * (s0 + k) + c] - x[c];
+            const double r = sqrt(rh[0] * rh[0] + rh[1] * rh[1] + rh[2] * rh[2]);
+            for (int c = 0; c < 3; ++c) rh[c] /= r;
+            M3 rr, I = m3_eye();
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) rr(i, j) = rh[i] * rh[j];
+            const M3 Mtt = m3_scale(m3_add(m3_scale(I, 1.0 + R2 / (3.0 * r * r)), m3_scale(rr, 1.0 - R2 / (r * r))),
+                                    1.0 / (8.0 * kPi * P.MU * r));
+            const M3 Mtr = m3_scale(rcross(rh), 1.0 / (8.0 * kPi * P.MU * r * r));
+            const M3 Mrr = m3_scale(m3_sub(m3_scale(rr, 3.0), I), 1.0 / (16.0 * kPi * P.MU * r * r * r));
+            double tk[3];
+            q_tangent(ldq(P.q + 4 * (s0 + k)), tk);
+            const M3 temp = rcross(tk);
+            const M3 Mtr_t = m3_mul(m3_scale(Mtr, 0.5 * P.DL), temp);
+            const M3 Mrr_t = m3_mul(m3_scale(Mrr, 0.5 * P.DL), temp);
+            if (k == 0) {
+                add_block(Bs, 6, 0, 0, Mtt);
+                add_block(Bs, 6, 3, 0, Mtr);
+                add_block(Bs, 6, 0, 3 * NS, m3_mul(Mtr, DinvT));
+                add_block(Bs, 6, 3, 3 * NS, m3_mul(Mrr, DinvT));
+                add_block(Bs, 6, 0, 3, m3_sub(Mtr_t, Mtt));
+                add_block(Bs, 6, 3, 3, m3_sub(Mrr_t, Mtr));
+            } else if (k == NS - 1) {
+                add_block(Bs, 6, 0, 6 * NS - 3, m3_mul(m3_scale(Mtt, -P.EFM), temp));
+                add_block(Bs, 6, 3, 6 * NS - 3, m3_mul(m3_scale(Mtr, -P.EFM), temp));
+                add_block(Bs, 6, 0, 3 * NS - 3, m3_add(Mtr_t, Mtt));
+                add_block(Bs, 6, 3, 3 * NS - 3, m3_add(Mrr_t, Mtr));
+            } else {
+                add_block(Bs, 6, 0, 3 * k, m3_add(Mtr_t, Mtt));
+                add_block(Bs, 6, 3, 3 * k, m3_add(Mrr_t, Mtr));
+                add_block(Bs, 6, 0, 3 * (k + 1), m3_sub(Mtr_t, Mtt));
+                add_block(Bs, 6, 3, 3 * (k + 1), m3_sub(Mrr_t, Mtr));
+            }
+        }
+        for (int k = 0; k < NS; ++k) {
+            put_block(Bs, 6, 3, 3 * k, m3_mul(Dinv, get_block(Bs, 6, 3, 3 * k)));
+            put_block(Bs, 6, 3, 3 * (k + NS), m3_mul(Dinv, get_block(Bs, 6, 3, 3 * (k + NS))));
+        }
+        for (int k = 0; k < 6 * n6; ++k) Bs[k] *= dt_fac;
+    }
+    __syncthreads();
+    const double *Jinv = P.invJ + (size_t)fil * n6 * n6;
+    double *jB = P.jacB + (size_t)fil * 6 * n6;
+    for (int c = threadIdx.x; c < n6; c += blockDim.x) {
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        for (int k = 0; k < n6; ++k) {
+            const double jv = Jinv[k + (size_t)n6 * c];
+            for (int r = 0; r < 6; ++r) acc[r] += Bs[r + 6 * k] * jv;
+        }
+        for (int r = 0; r < 6; ++r) jB[r + 6 * c] = acc[r];
+    }
+}
+
+// 6x6 inverse (Gauss-Jordan, partial pivoting), column-major in place.
+__device__ bool invert6_dev(double *A)
+{
+    double M[6][12];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            M[i][j] = A[i + 6 * j];
+            M[i][6 + j] = i == j ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 6; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 6; ++r)
+            if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
+        if (M[p][c] == 0.0) return false;
+        if (p != c)
+            for (int j = 0; j < 12; ++j) {
+                const double t = M[c][j];
+                M[c][j] = M[p][j];
+                M[p][j] = t;
+            }
+        const double d = M[c][c];
+        for (int j = 0; j < 12; ++j) M[c][j] /= d;
+        for (int r = 0; r < 6; ++r)
+            if (r != c) {
+                const double f = M[r][c];
+                if (f != 0.0)
+                    for (int j = 0; j < 12; ++j) M[r][j] -= f * M[c][j];
+            }
+    }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) A[i + 6 * j] = M[i][6 + j];
+    return true;
+}
+
+// A_f * (U, Omega) for the swimmer.cpp:800-812 block A of filament fil.
+__device__ void A_apply(const SimP &P, int fil, const double *ub, int row, double *out3)
+{
+    const int NS = P.NS, n = fil / P.NF;
+    const M3 Qi = ldm3(P.bQ + 9 * n);
+    if (row < 3 * NS) {
+        double fbd[3], dd[3];
+        m3_vec(Qi, P.fref + 3 * fil, fbd);
+        const double dn = sqrt(fbd[0] * fbd[0] + fbd[1] * fbd[1] + fbd[2] * fbd[2]);
+        for (int c = 0; c < 3; ++c) dd[c] = (0.5 * P.DL + dn) * fbd[c] / dn;
+        const M3 D = rcross(dd);
+        double t[3];
+        m3_vec(D, ub + 3, t);
+        for (int c = 0; c < 3; ++c) out3[c] = ub[c] + t[c];
+    } else if (row == 3 * NS) {
+        m3_vec(ldm3(P.ecb1 + 9 * fil), ub + 3, out3);
+    } else if (row == 3 * NS + 3) {
+        m3_vec(ldm3(P.ecb2 + 9 * fil), ub + 3, out3);
+    } else {
+        out3[0] = out3[1] = out3[2] = 0.0;
+    }
+}
+
+// The Schur complement of the body equations (swimmer.cpp:466-682), one
+// thread per swimmer, inverted in place.
+__global__ void swimmer_schur_kernel(SimP P, int nt)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.W) return;
+    const int NS = P.NS, n6 = P.n6;
+    const double dt_fac = (nt < P.neuler) ? -P.DT : -2.0 * P.DT / 3.0;
+    const double *u = P.bu + 3 * n;
+    const M3 Qi = ldm3(P.bQ + 9 * n);
+    const M3 blc = m3_scale(rcross(u), -1.0);
+    const M3 cbo = m3_scale(blc, -1.0 / dt_fac);
+    double S6[36];
+    for (int k = 0; k < 36; ++k) S6[k] = 0.0;
+    for (int d = 0; d < 6; ++d) S6[d + 6 * d] = 1.0;
+    add_block(S6, 6, 3, 3, m3_scale(m3_sub(m3_scale(m3_mul(blc, cbo), 1.0 / 12.0), m3_scale(cbo, 0.5)), dt_fac));
+    M3 old = m3_zero();
+    for (int i = 0; i < P.NF; ++i) {
+        const int fil = n * P.NF + i;
+        double fbd[3];
+        m3_vec(Qi, P.fref + 3 * fil, fbd);
+        old = m3_sub(old, m3_mul(rcross(P.tl + 3 * fil), rcross(fbd)));
+        const double *cl = P.cl + 3 * fil;
+        const double ucl[3] = {u[1] * cl[2] - u[2] * cl[1], u[2] * cl[0] - u[0] * cl[2], u[0] * cl[1] - u[1] * cl[0]};
+        old = m3_add(old, m3_sub(m3_scale(rcross(cl), 0.5),
+                                 m3_scale(m3_add(rcross(ucl), m3_mul(blc, rcross(cl))), 1.0 / 12.0)));
+        double t[3], te[3], dd[3];
+        q_tangent(ldq(P.q + 4 * (fil * NS + NS - 1)), t);
+        for (int c = 0; c < 3; ++c) te[c] = P.EFM * t[c];
+        const double dn = sqrt(fbd[0] * fbd[0] + fbd[1] * fbd[1] + fbd[2] * fbd[2]);
+        for (int c = 0; c < 3; ++c) dd[c] = (0.5 * P.DL + dn) * fbd[c] / dn;
+        old = m3_add(old, m3_mul(rcross(te), rcross(dd)));
+    }
+    double bm[36];
+    rotated_mobility(P, Qi, bm);
+    old = m3_mul(get_block(bm, 6, 3, 3), old);
+    const M3 add = m3_add(m3_sub(old, m3_scale(m3_mul(blc, old), 0.5)), m3_scale(m3_mul(m3_mul(blc, blc), old), 1.0 / 12.0));
+    add_block(S6, 6, 3, 3, m3_scale(add, dt_fac));
+    // schur -= jacB_f * A_f
+    for (int i = 0; i < P.NF; ++i) {
+        const int fil = n * P.NF + i;
+        const double *jB = P.jacB + (size_t)fil * 6 * n6;
+        for (int c = 0; c < 6; ++c) {
+            double ub[6] = {0, 0, 0, 0, 0, 0};
+            ub[c] = 1.0;
+            double colv[6] = {0, 0, 0, 0, 0, 0};
+            for (int row = 0; row < n6; row += 3) {
+                double a3[3];
+                A_apply(P, fil, ub, row, a3);
+                for (int r = 0; r < 6; ++r)
+                    colv[r] += jB[r + 6 * row] * a3[0] + jB[r + 6 * (row + 1)] * a3[1] + jB[r + 6 * (row + 2)] * a3[2];
+            }
+            for (int r = 0; r < 6; ++r) S6[r + 6 * c] -= colv[r];
+        }
+    }
+    if (!invert6_dev(S6)) atomicOr(P.flags + 2, 1);
+    for (int k = 0; k < 36; ++k) P.schur[36 * n + k] = S6[k];
+}
+
+// jacobian_inv_mult (swimmer.cpp:793-837), three stages.
+// (1) per filament: part[6 fil..] = jacB_f * in_f
+__global__ void __launch_bounds__(128) jim_partial_kernel(SimP P, const double *in, double *part)
+{
+    __shared__ double red[6][4];
+    const int fil = blockIdx.x, n = fil / P.NF, i = fil % P.NF;
+    const double *x = in + (size_t)n * P.per_body + (size_t)6 * P.NS * i;
+    const double *jB = P.jacB + (size_t)fil * 6 * P.n6;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = threadIdx.x; c < P.n6; c += 128)
+        for (int r = 0; r < 6; ++r) a[r] += jB[r + 6 * c] * x[c];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int r = 0; r < 6; ++r) {
+        const double v = warp_sum_d(a[r]);
+        if (lane == 0) red[r][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) part[6 * fil + threadIdx.x] = red[threadIdx.x][0] + red[threadIdx.x][1] +
+                                                       red[threadIdx.x][2] + red[threadIdx.x][3];
+}
+
+// (2) per swimmer: out_body = schur_inv * (in_body - sum_f part_f)
+__global__ void jim_body_kernel(SimP P, const double *in, const double *part, double *out)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.W) return;
+    const size_t b = (size_t)n * P.per_body + 6 * P.NF * P.NS;
+    double b2[6];
+    for (int r = 0; r < 6; ++r) b2[r] = in[b + r];
+    for (int i = 0; i < P.NF; ++i)
+        for (int r = 0; r < 6; ++r) b2[r] -= part[6 * (n * P.NF + i) + r];
+    const double *Si = P.schur + 36 * n;
+    for (int r = 0; r < 6; ++r) {
+        double s = 0.0;
+        for (int k = 0; k < 6; ++k) s += Si[r + 6 * k] * b2[k];
+        out[b + r] = s;
+    }
+}
+
+// (3) per filament: out_f = invJ_f * (in_f - A_f out_body)
+__global__ void __launch_bounds__(128) jim_fil_kernel(SimP P, const double *in, double *out)
+{
+    extern __shared__ double rhs[];
+    const int fil = blockIdx.x, n = fil / P.NF, i = fil % P.NF, n6 = P.n6;
+    const size_t base = (size_t)n * P.per_body + (size_t)6 * P.NS * i;
+    const double *ub = out + (size_t)n * P.per_body + 6 * P.NF * P.NS;
+    for (int row = threadIdx.x * 3; row < n6; row += 3 * 128) {
+        double a3[3];
+        A_apply(P, fil, ub, row, a3);
+        for (int c = 0; c < 3; ++c) rhs[row + c] = in[base + row + c] - a3[c];
+    }
+    __syncthreads();
+    const double *Ji = P.invJ + (size_t)fil * n6 * n6;
+    for (int r = threadIdx.x; r < n6; r += 128) {
+        double s = 0.0;
+        for (int k = 0; k < n6; ++k) s += Ji[r + (size_t)n6 * k] * rhs[k];
+        out[base + r] = s;
+    }
+}
+
+// rigid_body::update (rigid_body.cpp:354-381) for the body part of the update.
+__global__ void body_update_kernel(SimP P, const double *upd)
+{
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= P.W) return;
+    const double *b = upd + (size_t)n * P.per_body + 6 * P.NF * P.NS;
+    for (int c = 0; c < 3; ++c) {
+        P.bx[3 * n + c] += b[c];
+        P.bu[3 * n + c] += b[3 + c];
+    }
+    stq(P.bq + 4 * n, qmul(lie_exp(P.bu + 3 * n), ldq(P.bqm1 + 4 * n)));
+}
+
+// swimmer::update's per-filament part (swimmer.cpp:858-868) with
+// filament::update (filament.cpp:1541-1575).
+__global__ void filament_update_kernel(SimP P, const double *upd)
+{
+    const int fil = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fil >= P.F) return;
+    const int n = fil / P.NF, i = fil % P.NF, NS = P.NS;
+    accept_state_from_body(P, fil);
+    const double *du = upd + (size_t)n * P.per_body + (size_t)6 * NS * i;
+    for (int c = 0; c < 3; ++c) P.tl[3 * fil + c] += du[c];
+    double *lam = P.lam + 3 * (NS - 1) * fil;
+    for (int k = 1; k < NS; ++k) {
+        for (int c = 0; c < 3; ++c) lam[3 * (k - 1) + c] += du[3 * k + c];
+        segment_update(P, fil * NS + k, du + 3 * (NS + k));
+    }
+    for (int c = 0; c < 3; ++c) P.cl[3 * fil + c] += du[3 * NS + c];
+    robot_arm(P, fil);
+}
+
+// ---- Broyden vector kernels ----------------------------------------------
+constexpr int kVecTpb = 256;
+constexpr int kVecChunk = 2048;
+
+// part[i * nch + c] = sum over chunk c of M[:, i] . v   (i < k)
+__global__ void __launch_bounds__(kVecTpb) coldot_partial_kernel(const double *M, size_t ld, int k, const double *v,
+                                                                  int n, int nch, double *part)
+{
+    __shared__ double red[8];
+    const int c = blockIdx.x, i = blockIdx.y;
+    double a = 0.0;
+    const int r1 = min(n, (c + 1) * kVecChunk);
+    for (int r = c * kVecChunk + threadIdx.x; r < r1; r += kVecTpb) a += M[ld * i + r] * v[r];
+    a = warp_sum_d(a);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < kVecTpb / 32; ++w) s += red[w];
+        part[(size_t)i * nch + c] = s;
+    }
+}
+
+__global__ void coldot_finish_kernel(const double *part, int k, int nch, double *dots)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= k) return;
+    double s = 0.0;
+    for (int c = 0; c < nch; ++c) s += part[(size_t)i * nch + c];
+    dots[i] = s;
+}
+
+// out[r] = a * x[r] - sum_{i<k} dots[i] C[r, i]   (in order of i)
+__global__ void broyden_combine_kernel(int n, double a, const double *x, const double *C, size_t ld, const double *dots,
+                                       int k, double *out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    double v = a * x[r];
+    for (int i = 0; i < k; ++i) v -= dots[i] * C[ld * i + r];
+    out[r] = v;
+}
+
+__global__ void vec_sub_kernel(int n, const double *a, const double *b, double *out)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) out[r] = a[r] - b[r];
+}
+
+__global__ void vec_div2_kernel(int n, double *a, double *b, const double *nrm2)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const double d = sqrt(nrm2[0]);
+    if (r < n) {
+        a[r] /= d;
+        b[r] /= d;
+    }
+}
+
+}  // namespace gmi
+
+// ---------------------------------------------------------------------------
+// simulation object and host control flow
+// ---------------------------------------------------------------------------
+struct gmi_sim {
+    gmi_sim_config cfg{};
+    gmi_solver *solver = nullptr;
+    gmi::SimP P{};
+    int maxb = 100;
+    double *C = nullptr, *D = nullptr, *err = nullptr, *nerr = nullptr, *upd = nullptr, *tmp = nullptr;
+    double *dots = nullptr, *part = nullptr, *jpart = nullptr, *scal = nullptr;
+    int *h_flags = nullptr;
+    std::vector<void *> allocs;
+    bool prepared = false;
+    int broyden_iter = 0;
+};
+
+namespace gmi {
+
+static inline int gridN(int n, int tpb = 128) { return (n + tpb - 1) / tpb; }
+
+#define GMI_TRY(expr)                        \
+    do {                                     \
+        gmi_status gmi_s_ = (expr);          \
+        if (gmi_s_ != GMI_OK) return gmi_s_; \
+    } while (0)
+
+static gmi_status sim_alloc(gmi_sim *m, double **p, size_t count)
+{
+    if (count == 0) count = 1;
+    GMI_CUDA_TRY(cudaMalloc(p, count * sizeof(double)));
+    m->allocs.push_back(*p);
+    GMI_CUDA_TRY(cudaMemset(*p, 0, count * sizeof(double)));
+    return GMI_OK;
+}
+
+static gmi_status sim_launched(gmi_sim *m, int k = 1)
+{
+    m->solver->ctx->launches += k;
+    GMI_CUDA_TRY(cudaGetLastError());
+    return GMI_OK;
+}
+
+static cudaStream_t sst(gmi_sim *m) { return m->solver->ctx->stream; }
+
+static gmi_status read_flags(gmi_sim *m)
+{
+    GMI_CUDA_TRY(cudaMemcpyAsync(m->h_flags, m->P.flags, 3 * sizeof(int), cudaMemcpyDeviceToHost, sst(m)));
+    GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
+    return GMI_OK;
+}
+
+static gmi_status forces_and_torques(gmi_sim *m, int nt)
+{
+    filament_forces_kernel<<<gridN(m->P.F, 64), 64, 0, sst(m)>>>(m->P, nt);
+    swimmer_force_sum_kernel<<<m->P.W, 256, 0, sst(m)>>>(m->P);
+    return sim_launched(m, 2);
+}
+
+// compute_velocities + compute_errors; sets *too_large, *nonfinite
+static gmi_status velocities_and_errors(gmi_sim *m, int nt, double *err_out, bool *too_large, bool *nonfinite,
+                                        int *gmres_iters)
+{
+    GMI_TRY(solver_compute_velocities_device(m->solver, gmres_iters));
+    GMI_CUDA_TRY(cudaMemsetAsync(m->P.flags, 0, 3 * sizeof(int), sst(m)));
+    compute_errors_kernel<<<gridN(m->P.S + m->P.W), 128, 0, sst(m)>>>(m->P, nt, err_out);
+    GMI_TRY(sim_launched(m));
+    GMI_TRY(read_flags(m));
+    *too_large = m->h_flags[0] != 0;
+    *nonfinite = m->h_flags[1] != 0;
+    return GMI_OK;
+}
+
+static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
+{
+    const SimP &P = m->P;
+    build_jacobian_kernel<<<gridN(P.F, 32), 32, 0, sst(m)>>>(P, nt);
+    const size_t mat = (size_t)P.n6 * P.n6 * sizeof(double);
+    const size_t base = (size_t)P.n6 * sizeof(double) + 32 * sizeof(double) + 32 * sizeof(int) +
+                        (size_t)((P.n6 + 1) & ~1) * sizeof(int);
+    int use_smem = 0;
+    size_t smem = base;
+    int dev_max = 0;
+    GMI_CUDA_TRY(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->solver->ctx->device));
+    if (base + mat + 256 <= (size_t)dev_max) {
+        use_smem = 1;
+        smem = base + mat;
+    }
+    GMI_CUDA_TRY(cudaFuncSetAttribute(gj_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    gj_invert_kernel<<<P.F, kGjTpb, smem, sst(m)>>>(P.invJ, P.n6, use_smem, P.flags);
+    filament_B_kernel<<<P.F, 128, 6 * P.n6 * sizeof(double), sst(m)>>>(P, nt);
+    swimmer_schur_kernel<<<gridN(P.W, 32), 32, 0, sst(m)>>>(P, nt);
+    GMI_TRY(sim_launched(m, 4));
+    GMI_TRY(read_flags(m));
+    if (m->h_flags[2]) {
+        set_last_error_msg("the approximate Jacobian is singular (matrix.cpp:549-554 stops the reference here)");
+        return GMI_ERR_NONFINITE;
+    }
+    return GMI_OK;
+}
+
+static gmi_status jacobian_inv_mult(gmi_sim *m, const double *in, double *out)
+{
+    const SimP &P = m->P;
+    jim_partial_kernel<<<P.F, 128, 0, sst(m)>>>(P, in, m->jpart);
+    jim_body_kernel<<<gridN(P.W, 32), 32, 0, sst(m)>>>(P, in, m->jpart, out);
+    jim_fil_kernel<<<P.F, 128, P.n6 * sizeof(double), sst(m)>>>(P, in, out);
+    return sim_launched(m, 3);
+}
+
+// dots[i] = v . D[:, i], i < k
+static gmi_status dots_with_D(gmi_sim *m, const double *v, int k)
+{
+    if (k == 0) return GMI_OK;
+    const int n = m->P.nbroy, nch = (n + kVecChunk - 1) / kVecChunk;
+    coldot_partial_kernel<<<dim3(nch, k), kVecTpb, 0, sst(m)>>>(m->D, (size_t)n, k, v, n, nch, m->part);
+    coldot_finish_kernel<<<gridN(k, 64), 64, 0, sst(m)>>>(m->part, k, nch, m->dots);
+    return sim_launched(m, 2);
+}
+
+// broyden_solver::find_update (broyden_solver.cpp:26-68)
+static gmi_status find_update(gmi_sim *m)
+{
+    const int n = m->P.nbroy, it = m->broyden_iter;
+    GMI_TRY(jacobian_inv_mult(m, m->err, m->tmp));
+    GMI_TRY(dots_with_D(m, m->err, it));
+    broyden_combine_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, -m->P.conf, m->tmp, m->C, (size_t)n, m->dots, it,
+                                                              m->upd);
+    return sim_launched(m);
+}
+
+// broyden_solver::end_of_iter (broyden_solver.cpp:70-130)
+static gmi_status end_of_iter(gmi_sim *m, bool too_large)
+{
+    const int n = m->P.nbroy, it = m->broyden_iter;
+    if (too_large && it < m->maxb - 1) {
+        double *Ccol = m->C + (size_t)n * it, *Dcol = m->D + (size_t)n * it;
+        GMI_TRY(jacobian_inv_mult(m, m->nerr, m->tmp));
+        GMI_TRY(dots_with_D(m, m->nerr, it));
+        broyden_combine_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, -m->P.conf, m->tmp, m->C, (size_t)n, m->dots,
+                                                                  it, Ccol);
+        vec_sub_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, m->nerr, m->err, Dcol);
+        GMI_TRY(sim_launched(m, 2));
+        const int nch = (n + kVecChunk - 1) / kVecChunk;
+        coldot_partial_kernel<<<dim3(nch, 1), kVecTpb, 0, sst(m)>>>(Dcol, (size_t)n, 1, Dcol, n, nch, m->part);
+        coldot_finish_kernel<<<1, 64, 0, sst(m)>>>(m->part, 1, nch, m->scal);
+        vec_div2_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, Ccol, Dcol, m->scal);
+        GMI_TRY(sim_launched(m, 3));
+        std::swap(m->err, m->nerr);
+    }
+    m->broyden_iter++;
+    return GMI_OK;
+}
+
+// swimmer::update (swimmer.cpp:847-871)
+static gmi_status swimmer_update(gmi_sim *m)
+{
+    body_update_kernel<<<gridN(m->P.W, 32), 32, 0, sst(m)>>>(m->P, m->upd);
+    filament_update_kernel<<<gridN(m->P.F, 64), 64, 0, sst(m)>>>(m->P, m->upd);
+    return sim_launched(m, 2);
+}
+
+}  // namespace gmi
+
+using namespace gmi;
+
+#define SIM_ARG_CHECK(cond, msg)     \
+    do {                             \
+        if (!(cond)) {               \
+            set_last_error_msg(msg); \
+            return GMI_ERR_ARG;      \
+        }                            \
+    } while (0)
+
+extern "C" {
+
+gmi_status gmi_sim_destroy(gmi_sim *m)
+{
+    if (m == nullptr) return GMI_OK;
+    if (m->solver) {
+        cudaSetDevice(m->solver->ctx->device);
+        cudaStreamSynchronize(m->solver->ctx->stream);
+    }
+    for (void *p : m->allocs) cudaFree(p);
+    if (m->h_flags) cudaFreeHost(m->h_flags);
+    if (m->solver) gmi_solver_destroy(m->solver);
+    delete m;
+    return GMI_OK;
+}
+
+gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, const double *fil_refs,
+                          const double *body_x0, const double *perturb1, const double *perturb2, gmi_sim **out)
+{
+    SIM_ARG_CHECK(cfg && out && fil_refs && body_x0, "gmi_sim_create: null argument");
+    *out = nullptr;
+    const gmi_solver_config &mc = cfg->mobility;
+    SIM_ARG_CHECK(!mc.wall, "gmi_sim_create: the time step covers free-swimming bodies (no wall configuration)");
+    SIM_ARG_CHECK(mc.nfil >= 1 && mc.nseg >= 2 && mc.nblob >= 1 && mc.nswim >= 1, "gmi_sim_create: bad sizes");
+    SIM_ARG_CHECK(blob_refs != nullptr, "gmi_sim_create: null blob references");
+    SIM_ARG_CHECK(cfg->dt > 0 && cfg->kb > 0 && cfg->kt > 0 && cfg->body_radius > 0,
+                  "gmi_sim_create: dt, kb, kt and body_radius must be positive");
+    gmi_sim *m = new (std::nothrow) gmi_sim();
+    SIM_ARG_CHECK(m != nullptr, "gmi_sim_create: out of host memory");
+    m->cfg = *cfg;
+    gmi_status st = gmi_solver_create(&mc, &m->solver);
+    if (st != GMI_OK) {
+        gmi_sim_destroy(m);
+        return st;
+    }
+    gmi_solver *s = m->solver;
+    m->maxb = cfg->max_broyden_iter > 0 ? cfg->max_broyden_iter : 100;
+    SimP &P = m->P;
+    P.W = mc.nswim;
+    P.NF = mc.nfil;
+    P.NS = mc.nseg;
+    P.NB = mc.nblob;
+    P.F = P.W * P.NF;
+    P.S = P.F * P.NS;
+    P.per_body = 6 * P.NF * P.NS + 6;
+    P.nbroy = P.W * P.per_body;
+    P.n6 = 6 * P.NS;
+    P.neuler = cfg->num_euler_steps > 0 ? cfg->num_euler_steps : 1;
+    P.DL = 2.2 * mc.rseg;
+    P.DT = cfg->dt;
+    P.KB = cfg->kb;
+    P.KT = cfg->kt;
+    P.MU = mc.mu;
+    P.RSEG = mc.rseg;
+    P.EFM = mc.end_force_magnitude;
+    P.TOL = cfg->tol > 0 ? cfg->tol : 1e-4;
+    P.Rbody = cfg->body_radius;
+    P.conf = cfg->jacobian_confidence > 0 ? cfg->jacobian_confidence : 0.1;
+    P.x = s->x_segs;
+    P.f = s->f_segs;
+    P.v = s->v_segs;
+    P.bx = s->body_x;
+    P.bq = s->body_q;
+    P.bf = s->body_f;
+    P.vb = s->v_bodies;
+    const size_t S = P.S, F = P.F, W = P.W, n6 = P.n6, nb = P.nbroy;
+#define SIM_ALLOC(ptr, count)                  \
+    do {                                       \
+        st = sim_alloc(m, &(ptr), (count));    \
+        if (st != GMI_OK) {                    \
+            gmi_sim_destroy(m);                \
+            return st;                         \
+        }                                      \
+    } while (0)
+    SIM_ALLOC(P.q, 4 * S);
+    SIM_ALLOC(P.qm1, 4 * S);
+    SIM_ALLOC(P.u, 3 * S);
+    SIM_ALLOC(P.um1, 3 * S);
+    SIM_ALLOC(P.xm1, 3 * S);
+    SIM_ALLOC(P.xm2, 3 * S);
+    SIM_ALLOC(P.lam, 3 * (P.NS - 1) * F);
+    SIM_ALLOC(P.lam1, 3 * (P.NS - 1) * F);
+    SIM_ALLOC(P.lam2, 3 * (P.NS - 1) * F);
+    SIM_ALLOC(P.tl, 3 * F);
+    SIM_ALLOC(P.tl1, 3 * F);
+    SIM_ALLOC(P.tl2, 3 * F);
+    SIM_ALLOC(P.cl, 3 * F);
+    SIM_ALLOC(P.cl1, 3 * F);
+    SIM_ALLOC(P.cl2, 3 * F);
+    SIM_ALLOC(P.p1, 3 * F);
+    SIM_ALLOC(P.p2, 3 * F);
+    SIM_ALLOC(P.st, 3 * F);
+    SIM_ALLOC(P.fref, 3 * F);
+    SIM_ALLOC(P.invJ, F * n6 * n6);
+    SIM_ALLOC(P.ecb1, 9 * F);
+    SIM_ALLOC(P.ecb2, 9 * F);
+    SIM_ALLOC(P.jacB, F * 6 * n6);
+    SIM_ALLOC(P.bxm1, 3 * W);
+    SIM_ALLOC(P.bxm2, 3 * W);
+    SIM_ALLOC(P.bu, 3 * W);
+    SIM_ALLOC(P.bum1, 3 * W);
+    SIM_ALLOC(P.bqm1, 4 * W);
+    SIM_ALLOC(P.bQ, 9 * W);
+    SIM_ALLOC(P.schur, 36 * W);
+    SIM_ALLOC(P.mob_ref, 36);
+    SIM_ALLOC(m->C, nb * m->maxb);
+    SIM_ALLOC(m->D, nb * m->maxb);
+    SIM_ALLOC(m->err, nb);
+    SIM_ALLOC(m->nerr, nb);
+    SIM_ALLOC(m->upd, nb);
+    SIM_ALLOC(m->tmp, nb);
+    SIM_ALLOC(m->dots, m->maxb + 1);
+    SIM_ALLOC(m->part, (size_t)((nb + kVecChunk - 1) / kVecChunk) * (m->maxb + 1));
+    SIM_ALLOC(m->jpart, 6 * F);
+    SIM_ALLOC(m->scal, 4);
+    {
+        double *fl = nullptr;
+        SIM_ALLOC(fl, 4);
+        P.flags = reinterpret_cast<int *>(fl);
+    }
+#undef SIM_ALLOC
+    if (cudaMallocHost(&m->h_flags, 4 * sizeof(int)) != cudaSuccess) {
+        set_last_error_msg("gmi_sim_create: pinned allocation failed");
+        gmi_sim_destroy(m);
+        return GMI_ERR_CUDA;
+    }
+    // initial state: swimmer::initial_setup for spheres (swimmer.cpp:169-230),
+    // rigid_body::initial_setup (rigid_body.cpp:184-213), filament::initial_setup
+    // (filament.cpp:60-81, 265-323), built on the host then copied.
+    const int NS = P.NS;
+    std::vector<double> hx(3 * S), hq(4 * S), hbx(3 * W), hbq(4 * W, 0.0), hfref(3 * F), hp1(3 * F, 0.0),
+        hp2(3 * F, 0.0);
+    for (size_t n = 0; n < W; ++n) {
+        for (int c = 0; c < 3; ++c) hbx[3 * n + c] = body_x0[3 * n + c];
+        hbq[4 * n] = 1.0;
+    }
+    for (size_t fil = 0; fil < F; ++fil) {
+        const size_t n = fil / P.NF, i = fil % P.NF;
+        const double *dref = fil_refs + 3 * i;
+        for (int c = 0; c < 3; ++c) hfref[3 * fil + c] = dref[c];
+        if (perturb1)
+            for (int c = 0; c < 3; ++c) hp1[3 * fil + c] = perturb1[3 * fil + c];
+        if (perturb2)
+            for (int c = 0; c < 3; ++c) hp2[3 * fil + c] = perturb2[3 * fil + c];
+        const double nrm = std::sqrt(dref[0] * dref[0] + dref[1] * dref[1] + dref[2] * dref[2]);
+        const double dir[3] = {dref[0] / nrm, dref[1] / nrm, dref[2] / nrm};
+        Q4 qt{dir[0], 0.0, -dir[2], dir[1]};
+        qsqrt_in_place(qt);
+        double pos[3] = {hbx[3 * n] + dref[0], hbx[3 * n + 1] + dref[1], hbx[3 * n + 2] + dref[2]};
+        for (int k = 0; k < NS; ++k) {
+            const size_t sidx = fil * NS + k;
+            for (int c = 0; c < 3; ++c) hx[3 * sidx + c] = pos[c];
+            hq[4 * sidx] = qt.s;
+            hq[4 * sidx + 1] = qt.x;
+            hq[4 * sidx + 2] = qt.y;
+            hq[4 * sidx + 3] = qt.z;
+            for (int c = 0; c < 3; ++c) pos[c] += P.DL * dir[c];
+        }
+    }
+    auto up = [&](double *d, const std::vector<double> &h) -> gmi_status {
+        GMI_CUDA_TRY(cudaMemcpy(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        return GMI_OK;
+    };
+    if ((st = up(P.x, hx)) != GMI_OK || (st = up(P.xm1, hx)) != GMI_OK || (st = up(P.xm2, hx)) != GMI_OK ||
+        (st = up(P.q, hq)) != GMI_OK || (st = up(P.qm1, hq)) != GMI_OK || (st = up(P.bx, hbx)) != GMI_OK ||
+        (st = up(P.bxm1, hbx)) != GMI_OK || (st = up(P.bxm2, hbx)) != GMI_OK || (st = up(P.bq, hbq)) != GMI_OK ||
+        (st = up(P.bqm1, hbq)) != GMI_OK || (st = up(P.fref, hfref)) != GMI_OK || (st = up(P.p1, hp1)) != GMI_OK ||
+        (st = up(P.p2, hp2)) != GMI_OK) {
+        gmi_sim_destroy(m);
+        return st;
+    }
+    st = gmi_solver_set_blob_references(s, blob_refs);
+    if (st != GMI_OK) {
+        gmi_sim_destroy(m);
+        return st;
+    }
+    *out = m;
+    return GMI_OK;
+}
+
+gmi_solver *gmi_sim_solver(gmi_sim *m) { return m ? m->solver : nullptr; }
+
+// mobility_solver::make_body_reference_matrices on the initial state
+// (cilia_sim_main.cpp:159-165)
+gmi_status gmi_sim_prepare(gmi_sim *m, double *body_mobility_out)
+{
+    SIM_ARG_CHECK(m != nullptr, "gmi_sim_prepare: null simulation");
+    GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
+    double mob[36];
+    GMI_TRY(solver_make_body_reference_matrices_device(m->solver, nullptr, mob));
+    GMI_CUDA_TRY(cudaMemcpy(m->P.mob_ref, mob, sizeof mob, cudaMemcpyHostToDevice));
+    if (body_mobility_out) std::memcpy(body_mobility_out, mob, sizeof mob);
+    m->prepared = true;
+    return GMI_OK;
+}
+
+// One time step, cilia_sim_main.cpp:207-343 (GMRES branch).
+gmi_status gmi_sim_step(gmi_sim *m, int nt, int *broyden_iters, int *gmres_iters_total)
+{
+    SIM_ARG_CHECK(m != nullptr && nt >= 0, "gmi_sim_step: bad argument");
+    SIM_ARG_CHECK(m->prepared, "gmi_sim_step: call gmi_sim_prepare first");
+    GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
+    const SimP &P = m->P;
+    body_initial_guess_kernel<<<gridN(P.W, 32), 32, 0, sst(m)>>>(P, nt);
+    filament_initial_guess_kernel<<<gridN(P.F, 64), 64, 0, sst(m)>>>(P, nt);
+    GMI_TRY(sim_launched(m, 2));
+    GMI_TRY(forces_and_torques(m, nt));
+    int gi = 0, gtot = 0;
+    bool too_large = false, nonfinite = false;
+    GMI_TRY(velocities_and_errors(m, nt, m->err, &too_large, &nonfinite, &gi));
+    gtot += gi;
+    if (too_large) GMI_TRY(prepare_jacobian_inv(m, nt));
+    m->broyden_iter = 0;
+    while (too_large && m->broyden_iter < m->maxb) {
+        GMI_TRY(find_update(m));
+        GMI_TRY(swimmer_update(m));
+        GMI_TRY(forces_and_torques(m, nt));
+        GMI_TRY(velocities_and_errors(m, nt, m->nerr, &too_large, &nonfinite, &gi));
+        gtot += gi;
+        if (nonfinite) {
+            set_last_error_msg("Broyden's method diverged (non-finite residual)");
+            return GMI_ERR_NONFINITE;
+        }
+        GMI_TRY(end_of_iter(m, too_large));
+    }
+    if (broyden_iters) *broyden_iters = m->broyden_iter;
+    if (gmres_iters_total) *gmres_iters_total = gtot;
+    GMI_TRY(context_check_device_errors(m->solver->ctx));
+    if (too_large) {
+        set_last_error_msg("Broyden's method did not converge within max_broyden_iter iterations");
+        return GMI_ERR_NOT_CONVERGED;
+    }
+    return GMI_OK;
+}
+
+gmi_status gmi_sim_get_state(gmi_sim *m, int field, double *out_h)
+{
+    SIM_ARG_CHECK(m && out_h, "gmi_sim_get_state: null argument");
+    const SimP &P = m->P;
+    const double *src = nullptr;
+    size_t count = 0;
+    switch (field) {
+        case GMI_STATE_SEG_X: src = P.x; count = 3 * (size_t)P.S; break;
+        case GMI_STATE_SEG_Q: src = P.q; count = 4 * (size_t)P.S; break;
+        case GMI_STATE_SEG_U: src = P.u; count = 3 * (size_t)P.S; break;
+        case GMI_STATE_SEG_V: src = P.v; count = 6 * (size_t)P.S; break;
+        case GMI_STATE_SEG_F: src = P.f; count = 6 * (size_t)P.S; break;
+        case GMI_STATE_BODY_X: src = P.bx; count = 3 * (size_t)P.W; break;
+        case GMI_STATE_BODY_Q: src = P.bq; count = 4 * (size_t)P.W; break;
+        case GMI_STATE_BODY_U: src = P.bu; count = 3 * (size_t)P.W; break;
+        case GMI_STATE_BODY_V: src = P.vb; count = 6 * (size_t)P.W; break;
+        case GMI_STATE_LAMBDA: src = P.lam; count = 3 * (size_t)(P.NS - 1) * P.F; break;
+        case GMI_STATE_TETHER: src = P.tl; count = 3 * (size_t)P.F; break;
+        case GMI_STATE_CLAMP: src = P.cl; count = 3 * (size_t)P.F; break;
+        case GMI_STATE_BLOB_F: src = m->solver->f_blobs; count = 3 * (size_t)m->solver->B; break;
+        default: SIM_ARG_CHECK(false, "gmi_sim_get_state: unknown field");
+    }
+    GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
+    GMI_CUDA_TRY(cudaMemcpyAsync(out_h, src, count * sizeof(double), cudaMemcpyDeviceToHost, sst(m)));
+    GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
+    return GMI_OK;
+}
+
+}  // extern "C"

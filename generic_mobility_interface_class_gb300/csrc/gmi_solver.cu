@@ -19,6 +19,7 @@
 
 #include "gmi_context.hpp"
 #include "gmi_pair_kernels.hpp"
+#include "gmi_solver_internal.hpp"
 
 namespace gmi {
 
@@ -389,29 +390,6 @@ __global__ void scale_kernel(int n, const double *__restrict__ x, const double *
 }
 
 }  // namespace gmi
-
-// ---------------------------------------------------------------------------
-// solver object
-// ---------------------------------------------------------------------------
-struct gmi_solver {
-    gmi_context *ctx = nullptr;
-    gmi_solver_config cfg{};
-    int S = 0, B = 0, W = 0, n = 0, m = 0;
-    gmi_host_arrays h{};
-    double *h_stage = nullptr;   // pinned staging: body x, q, f, scalars
-    // device state
-    double *x_segs = nullptr, *f_segs = nullptr, *v_segs = nullptr;
-    double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
-    double *body_x = nullptr, *body_q = nullptr, *body_f = nullptr, *v_bodies = nullptr;
-    double *R = nullptr, *ktk_ref = nullptr, *mob_ref = nullptr, *ktk_rot = nullptr, *mob_rot = nullptr;
-    double *refs = nullptr, *sums = nullptr;
-    double *rhs = nullptr, *soln = nullptr, *Q = nullptr, *H = nullptr, *beta = nullptr, *cs = nullptr, *sn = nullptr;
-    double *z = nullptr, *w = nullptr, *tmp = nullptr, *mbb = nullptr, *partial = nullptr, *yv = nullptr;
-    double *b64 = nullptr, *xacc = nullptr;  // refinement: FP64 right-hand side, accumulated solution
-    double *scal = nullptr;  // device scalars: [0] norm, [1] resid
-    bool refs_set = false;
-    std::vector<void *> allocs;
-};
 
 namespace gmi {
 
@@ -804,6 +782,33 @@ static bool invert6(const double *A, double *Ainv)
 
 }  // namespace gmi
 
+namespace gmi {
+
+gmi_status solver_compute_velocities_device(gmi_solver *s, int *iters)
+{
+    const int W = s->W, B = s->B;
+    cudaStream_t st = s->ctx->stream;
+    *iters = 0;
+    if (s->cfg.wall) {
+        GMI_TRY(positions_and_barrier(s));
+        return seg_pair(s, kSS);
+    }
+    GMI_TRY(positions_and_barrier(s));
+    if (B > 0) {
+        GMI_TRY(kt_sums(s, s->f_rep));
+        add_vec_kernel<<<grid_for(6 * W), 256, 0, st>>>(6 * W, s->sums, s->body_f);
+        GMI_TRY(launched(s));
+    }
+    GMI_TRY(seg_pair(s, kSS));
+    GMI_TRY(seg_pair(s, kBS));
+    assemble_rhs_kernel<<<grid_for(s->n), 256, 0, st>>>(3 * B, 6 * W, s->v_blobs, s->body_f, s->rhs);
+    GMI_TRY(launched(s));
+    GMI_TRY(solve_linear_system(s, iters));
+    return seg_pair(s, kSB);
+}
+
+}  // namespace gmi
+
 using namespace gmi;
 
 #define GMI_ARG_CHECK(cond, msg)     \
@@ -1068,40 +1073,25 @@ gmi_status gmi_solver_compute_velocities(gmi_solver *s, const double *body_x, co
     GMI_ARG_CHECK(s->cfg.wall || (body_x && body_q && body_f), "gmi_solver_compute_velocities: null body state");
     GMI_ARG_CHECK(s->cfg.wall || B == 0 || s->refs_set,
                   "gmi_solver_compute_velocities: blob references not set (gmi_solver_set_blob_references)");
-    cudaStream_t st = s->ctx->stream;
     int iters = 0;
     GMI_TRY(h2d(s, s->x_segs, s->h.x_segs_host, 3 * (size_t)S));
     GMI_TRY(h2d(s, s->f_segs, s->h.f_segs_host, 6 * (size_t)S));
-    if (s->cfg.wall) {
-        GMI_TRY(positions_and_barrier(s));
-        GMI_TRY(seg_pair(s, kSS));
-        GMI_TRY(d2h(s, s->h.v_segs_host, s->v_segs, 6 * (size_t)S));
-        if (num_gmres_iterations) *num_gmres_iterations = 0;
-        return context_check_device_errors(s->ctx);
+    if (!s->cfg.wall) {
+        GMI_TRY(stage_bodies(s, body_x, body_q));
+        std::memcpy(s->h_stage + 8, body_f, 6 * W * sizeof(double));
+        GMI_TRY(h2d(s, s->body_f, s->h_stage + 8, 6 * (size_t)W));
     }
-    GMI_TRY(stage_bodies(s, body_x, body_q));
-    std::memcpy(s->h_stage + 8, body_f, 6 * W * sizeof(double));
-    GMI_TRY(h2d(s, s->body_f, s->h_stage + 8, 6 * (size_t)W));
-    GMI_TRY(positions_and_barrier(s));
-    if (B > 0) {
-        GMI_TRY(kt_sums(s, s->f_rep));
-        add_vec_kernel<<<grid_for(6 * W), 256, 0, st>>>(6 * W, s->sums, s->body_f);
-        GMI_TRY(launched(s));
-    }
-    GMI_TRY(seg_pair(s, kSS));
-    GMI_TRY(seg_pair(s, kBS));
-    assemble_rhs_kernel<<<grid_for(s->n), 256, 0, st>>>(3 * B, 6 * W, s->v_blobs, s->body_f, s->rhs);
-    GMI_TRY(launched(s));
-    GMI_TRY(solve_linear_system(s, &iters));
-    GMI_TRY(seg_pair(s, kSB));
+    GMI_TRY(solver_compute_velocities_device(s, &iters));
     GMI_TRY(d2h(s, s->h.v_segs_host, s->v_segs, 6 * (size_t)S));
-    GMI_TRY(d2h(s, s->h.f_blobs_host, s->f_blobs, 3 * (size_t)B));
-    GMI_TRY(d2h(s, s->h.x_blobs_host, s->x_blobs, 3 * (size_t)B));
-    GMI_TRY(d2h(s, s->h.f_blobs_repulsion_host, s->f_rep, 3 * (size_t)B));
-    GMI_TRY(d2h(s, s->h.v_blobs_host, s->v_blobs, 3 * (size_t)B));
-    GMI_TRY(d2h(s, s->h_stage + 8, s->body_f, 6 * (size_t)W));
+    if (!s->cfg.wall) {
+        GMI_TRY(d2h(s, s->h.f_blobs_host, s->f_blobs, 3 * (size_t)B));
+        GMI_TRY(d2h(s, s->h.x_blobs_host, s->x_blobs, 3 * (size_t)B));
+        GMI_TRY(d2h(s, s->h.f_blobs_repulsion_host, s->f_rep, 3 * (size_t)B));
+        GMI_TRY(d2h(s, s->h.v_blobs_host, s->v_blobs, 3 * (size_t)B));
+        GMI_TRY(d2h(s, s->h_stage + 8, s->body_f, 6 * (size_t)W));
+    }
     GMI_TRY(context_check_device_errors(s->ctx));
-    std::memcpy(body_f, s->h_stage + 8, 6 * W * sizeof(double));
+    if (!s->cfg.wall) std::memcpy(body_f, s->h_stage + 8, 6 * W * sizeof(double));
     if (num_gmres_iterations) *num_gmres_iterations = iters;
     return GMI_OK;
 }
@@ -1113,7 +1103,19 @@ gmi_status gmi_solver_make_body_reference_matrices(gmi_solver *s, const double *
     GMI_ARG_CHECK(!s->cfg.wall, "gmi_solver_make_body_reference_matrices: not used with the wall configuration");
     GMI_ARG_CHECK(body_x && body_q, "gmi_solver_make_body_reference_matrices: null body state");
     GMI_ARG_CHECK(s->refs_set, "gmi_solver_make_body_reference_matrices: blob references not set");
-    const int W = s->W, nblob = s->cfg.nblob, B = s->B;
+    GMI_TRY(h2d(s, s->x_segs, s->h.x_segs_host, 3 * (size_t)s->S));
+    GMI_TRY(h2d(s, s->f_segs, s->h.f_segs_host, 6 * (size_t)s->S));
+    GMI_TRY(stage_bodies(s, body_x, body_q));
+    return solver_make_body_reference_matrices_device(s, ktkinv_out, mob_out);
+}
+
+}  // extern "C"
+
+namespace gmi {
+
+gmi_status solver_make_body_reference_matrices_device(gmi_solver *s, double *ktkinv_out, double *mob_out)
+{
+    const int W = s->W, nblob = s->cfg.nblob;
     // (K^T K) from the references (mobility_solver.cpp:1697-1713), inverted on the host
     std::vector<double> refs(3 * (size_t)nblob);
     if (nblob > 0)
@@ -1122,7 +1124,8 @@ gmi_status gmi_solver_make_body_reference_matrices(gmi_solver *s, const double *
     KTK[0] = KTK[7] = KTK[14] = (double)nblob;
     for (int m = 0; m < nblob; ++m) {
         const double *r = &refs[3 * m];
-        const double rc[9] = {0.0, -r[2], r[1], r[2], 0.0, -r[0], -r[1], r[0], 0.0};  // row-major rcross
+        // the reference's rcross(r) (matrix.cpp:665-679), row-major: rcross(r) b = b x r
+        const double rc[9] = {0.0, r[2], -r[1], -r[2], 0.0, r[0], r[1], -r[0], 0.0};
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) {
                 KTK[i + 6 * (3 + j)] += rc[3 * i + j];
@@ -1140,14 +1143,14 @@ gmi_status gmi_solver_make_body_reference_matrices(gmi_solver *s, const double *
     double mob[36] = {0};
     for (int i = 0; i < 6; ++i) mob[i + 6 * i] = 1.0;
     GMI_TRY(gmi_solver_set_body_reference_matrices(s, KTKinv, mob));
-    // all swimmers but the last moved far away (mobility_solver.cpp:1721-1731)
-    std::vector<double> bx(body_x, body_x + 3 * W);
+    // all swimmers but the last moved far away (mobility_solver.cpp:1721-1731), restored after
+    std::vector<double> bx0(3 * (size_t)W), bx;
+    GMI_CUDA_TRY(cudaMemcpy(bx0.data(), s->body_x, bx0.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    bx = bx0;
     const double shift = 1e10 * 2.2 * s->cfg.rseg * s->cfg.nseg;
     for (int n = 0; n < W - 1; ++n)
         for (int c = 0; c < 3; ++c) bx[3 * n + c] += shift;
-    GMI_TRY(h2d(s, s->x_segs, s->h.x_segs_host, 3 * (size_t)s->S));
-    GMI_TRY(h2d(s, s->f_segs, s->h.f_segs_host, 6 * (size_t)s->S));
-    GMI_TRY(stage_bodies(s, bx.data(), body_q));
+    GMI_CUDA_TRY(cudaMemcpy(s->body_x, bx.data(), bx.size() * sizeof(double), cudaMemcpyHostToDevice));
     GMI_TRY(positions_and_barrier(s));
     for (int col = 0; col < 6; ++col) {
         GMI_CUDA_TRY(cudaMemsetAsync(s->rhs, 0, (size_t)s->n * sizeof(double), s->ctx->stream));
@@ -1157,20 +1160,19 @@ gmi_status gmi_solver_make_body_reference_matrices(gmi_solver *s, const double *
         GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
         int iters = 0;
         GMI_TRY(solve_linear_system(s, &iters));
-        double vb[6];
         GMI_CUDA_TRY(cudaMemcpyAsync(s->h_stage, s->v_bodies + 6 * (W - 1), 6 * sizeof(double),
                                      cudaMemcpyDeviceToHost, s->ctx->stream));
         GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
-        std::memcpy(vb, s->h_stage, sizeof vb);
-        for (int i = 0; i < 6; ++i) mob[i + 6 * (5 - col)] = vb[i];
+        for (int i = 0; i < 6; ++i) mob[i + 6 * (5 - col)] = s->h_stage[i];
         // the preconditioner of the next solve sees the updated column
         GMI_TRY(gmi_solver_set_body_reference_matrices(s, KTKinv, mob));
         GMI_TRY(prepare_bodies(s));
     }
-    (void)B;
+    GMI_CUDA_TRY(cudaMemcpy(s->body_x, bx0.data(), bx0.size() * sizeof(double), cudaMemcpyHostToDevice));
     if (ktkinv_out) std::memcpy(ktkinv_out, KTKinv, sizeof KTKinv);
     if (mob_out) std::memcpy(mob_out, mob, sizeof mob);
     return context_check_device_errors(s->ctx);
 }
 
-}  // extern "C"
+}  // namespace gmi
+

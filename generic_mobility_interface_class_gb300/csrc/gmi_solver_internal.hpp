@@ -1,0 +1,43 @@
+// gmi_solver_internal.hpp -- the mobility solver object, shared by the
+// C-ABI solver entry points (gmi_solver.cu) and the implicit time step
+// (gmi_sim.cu), which drives the solver on device-resident state.
+#pragma once
+
+#include <vector>
+
+#include "gmi_context.hpp"
+
+struct gmi_solver {
+    gmi_context *ctx = nullptr;
+    gmi_solver_config cfg{};
+    int S = 0, B = 0, W = 0, n = 0, m = 0;
+    gmi_host_arrays h{};
+    double *h_stage = nullptr;   // pinned staging: body x, q, f, scalars
+    // device state
+    double *x_segs = nullptr, *f_segs = nullptr, *v_segs = nullptr;
+    double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
+    double *body_x = nullptr, *body_q = nullptr, *body_f = nullptr, *v_bodies = nullptr;
+    double *R = nullptr, *ktk_ref = nullptr, *mob_ref = nullptr, *ktk_rot = nullptr, *mob_rot = nullptr;
+    double *refs = nullptr, *sums = nullptr;
+    double *rhs = nullptr, *soln = nullptr, *Q = nullptr, *H = nullptr, *beta = nullptr, *cs = nullptr, *sn = nullptr;
+    double *z = nullptr, *w = nullptr, *tmp = nullptr, *mbb = nullptr, *partial = nullptr, *yv = nullptr;
+    double *b64 = nullptr, *xacc = nullptr;  // refinement: FP64 right-hand side, accumulated solution
+    double *scal = nullptr;  // device scalars: [0] norm, [1] resid
+    bool refs_set = false;
+    std::vector<void *> allocs;
+};
+
+
+namespace gmi {
+
+// mobility_solver::compute_velocities on inputs already on the device
+// (x_segs, f_segs, body_x, body_q, body_f): blob positions, barrier forces
+// (their blob part added into body_f), M_ss, M_bs, the right-hand side, the
+// linear solve, M_sb.  Leaves v_segs, f_blobs, v_bodies on the device.
+gmi_status solver_compute_velocities_device(gmi_solver *s, int *iters);
+
+// make_body_reference_matrices on the device-resident x_segs/f_segs and
+// body state; the outputs (may be null) are column-major 6x6.
+gmi_status solver_make_body_reference_matrices_device(gmi_solver *s, double *ktkinv_out, double *mob_out);
+
+}  // namespace gmi

@@ -1,0 +1,94 @@
+"""Python wrapper of the device time step (gmi_sim_*): the reference's main
+loop (cilia_sim_main.cpp:205-343) for free-swimming spherical swimmers."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import GMI_FP64, SimConfig, SolverConfig, check
+
+STATE = dict(seg_x=(0, 3), seg_q=(1, 4), seg_u=(2, 3), seg_v=(3, 6), seg_f=(4, 6), body_x=(5, 3), body_q=(6, 4),
+             body_u=(7, 3), body_v=(8, 6), lam=(9, 3), tether=(10, 3), clamp=(11, 3), blob_f=(12, 3))
+
+
+def _c(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Simulation:
+    def __init__(self, *, nswim=1, nfil, nseg, nblob, blob_refs, fil_refs, body_x0=None, perturbation1=None,
+                 perturbation2=None, mu=1.0, rseg=1.0, rblob=1.0, kb, kt, dt, end_force_magnitude,
+                 repulsive_force_factor=2.0, body_radius, tol=1e-4, max_broyden_iter=100, jacobian_confidence=0.1,
+                 num_euler_steps=1, linear_tol=1e-10, max_linear_iter=150, precision=GMI_FP64, device=0):
+        self.lib = _lib.load()
+        mob = SolverConfig(nswim, nfil, nseg, nblob, mu, rseg, rblob, repulsive_force_factor, end_force_magnitude, 0,
+                           max_linear_iter, linear_tol, precision, device)
+        cfg = SimConfig(mob, kb, kt, dt, num_euler_steps, max_broyden_iter, tol, jacobian_confidence, body_radius)
+        F = nswim * nfil
+        self.nswim, self.nfil, self.nseg, self.nblob = nswim, nfil, nseg, nblob
+        self.F, self.S = F, F * nseg
+        body_x0 = np.zeros((nswim, 3)) if body_x0 is None else body_x0
+
+        def per_fil(p):
+            if p is None:
+                return np.zeros((F, 3))
+            p = np.asarray(p, dtype=np.float64)
+            return np.tile(p.reshape(1, 3), (F, 1)) if p.size == 3 else p.reshape(F, 3)
+
+        arrays = [_c(blob_refs), _c(fil_refs), _c(body_x0), _c(per_fil(perturbation1)), _c(per_fil(perturbation2))]
+        h = ctypes.c_void_p()
+        check(self.lib.gmi_sim_create(ctypes.byref(cfg), *[p for _, p in arrays], ctypes.byref(h)))
+        self.handle = h
+        self.nt = 0
+
+    def prepare(self):
+        mob = np.zeros(36)
+        check(self.lib.gmi_sim_prepare(self.handle, mob.ctypes.data_as(ctypes.c_void_p)))
+        return mob.reshape(6, 6, order="F")
+
+    def step(self, nt=None):
+        nt = self.nt if nt is None else nt
+        b, g = ctypes.c_int(), ctypes.c_int()
+        check(self.lib.gmi_sim_step(self.handle, nt, ctypes.byref(b), ctypes.byref(g)))
+        self.nt = nt + 1
+        return b.value, g.value
+
+    def state(self, name):
+        field, cols = STATE[name]
+        rows = {"body_x": self.nswim, "body_q": self.nswim, "body_u": self.nswim, "body_v": self.nswim,
+                "lam": (self.nseg - 1) * self.F, "tether": self.F, "clamp": self.F,
+                "blob_f": self.nswim * self.nblob}.get(name, self.S)
+        out = np.zeros((rows, cols))
+        check(self.lib.gmi_sim_get_state(self.handle, field, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    @property
+    def launches(self):
+        solver = self.lib.gmi_sim_solver(self.handle)
+        return int(self.lib.gmi_context_launch_count(self.lib.gmi_solver_context(solver)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.gmi_sim_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @classmethod
+    def from_golden(cls, g, **kw):
+        args = dict(nfil=int(g["nfil"]), nseg=int(g["nseg"]), nblob=int(g["nblob"]), blob_refs=g["blob_refs"],
+                    fil_refs=g["fil_refs"], perturbation1=g["perturbation1"], perturbation2=g["perturbation2"],
+                    mu=float(g["mu"]), rseg=float(g["rseg"]), rblob=float(g["rblob"]), kb=float(g["kb"]),
+                    kt=float(g["kt"]), dt=float(g["dt"]), end_force_magnitude=float(g["end_force_magnitude"]),
+                    repulsive_force_factor=float(g["repulsive_force_factor"]), body_radius=float(g["body_radius"]),
+                    tol=float(g["tol"]), linear_tol=float(g["linear_tol"]),
+                    max_linear_iter=int(g["max_linear_iter"]))
+        args.update(kw)
+        return cls(**args)

@@ -238,6 +238,64 @@ GMI_API gmi_status gmi_solver_compute_velocities(gmi_solver *s, const double *bo
 GMI_API gmi_status gmi_solver_get_v_bodies(gmi_solver *s, double *v_bodies_h);
 GMI_API gmi_status gmi_solver_set_v_bodies(gmi_solver *s, const double *v_bodies_h);
 
+/* ------------------------------------------------------------------------
+ * Implicit time step on the device: the reference's main loop
+ * (cilia_sim_main.cpp:205-343) with Broyden's method (broyden_solver.cpp),
+ * the swimmer/filament/segment/body state updates and forces (swimmer.cpp,
+ * filament.cpp, segment.cpp, rigid_body.cpp), the approximate inverse
+ * Jacobian (filament.cpp:1222-1539, swimmer.cpp:329-845) and the residual
+ * (mobility_solver.cpp:1404-1689), for free-swimming spherical bodies with
+ * end-force-driven filaments (CILIA_TYPE 0) and the GMRES linear solve.
+ * ---------------------------------------------------------------------- */
+typedef struct gmi_sim gmi_sim;
+
+typedef struct gmi_sim_config {
+    gmi_solver_config mobility;   /* sizes, radii, viscosity, barrier scale, GMRES, precision, device */
+    double kb, kt;                /* KB, KT */
+    double dt;                    /* DT */
+    int num_euler_steps;          /* NUM_EULER_STEPS (<= 0: 1) */
+    int max_broyden_iter;         /* MAX_BROYDEN_ITER (<= 0: 100) */
+    double tol;                   /* TOL (<= 0: 1e-4) */
+    double jacobian_confidence;   /* JACOBIAN_CONFIDENCE_FACTOR (<= 0: 0.1) */
+    double body_radius;           /* R_OVER_L*DL*NSEG: sphere radius in the approximate Jacobian (swimmer.cpp:607) */
+} gmi_sim_config;
+
+/* State fields readable with gmi_sim_get_state (FP64, reference layouts). */
+typedef enum gmi_state_field {
+    GMI_STATE_SEG_X = 0,  /* [3*S] segment positions */
+    GMI_STATE_SEG_Q = 1,  /* [4*S] segment quaternions (scalar first) */
+    GMI_STATE_SEG_U = 2,  /* [3*S] segment Lie-algebra updates */
+    GMI_STATE_SEG_V = 3,  /* [6*S] segment velocities of the last solve */
+    GMI_STATE_SEG_F = 4,  /* [6*S] segment forces/torques of the last solve (before barrier) */
+    GMI_STATE_BODY_X = 5, /* [3*W] */
+    GMI_STATE_BODY_Q = 6, /* [4*W] */
+    GMI_STATE_BODY_U = 7, /* [3*W] */
+    GMI_STATE_BODY_V = 8, /* [6*W] body velocities of the last solve */
+    GMI_STATE_LAMBDA = 9, /* [3*(nseg-1)*F] inextensibility multipliers */
+    GMI_STATE_TETHER = 10, /* [3*F] */
+    GMI_STATE_CLAMP = 11,  /* [3*F] */
+    GMI_STATE_BLOB_F = 12  /* [3*B] blob forces of the last solve */
+} gmi_state_field;
+
+/* swimmer::initial_setup for free-swimming spheres (swimmer.cpp:169-230,
+ * rigid_body.cpp:184-213, filament.cpp:60-81, 265-323): blob_refs[3*nblob]
+ * (body frame, scaled), fil_refs[3*nfil] (filament base relative to the body
+ * centre, scaled; the filament stands along it), body_x0[3*nswim];
+ * perturb1/perturb2[3*F] (or NULL) are added to segments 4 and 12 at step 0
+ * (filament.cpp:1181-1196). */
+GMI_API gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, const double *fil_refs,
+                                  const double *body_x0, const double *perturb1, const double *perturb2,
+                                  gmi_sim **out);
+GMI_API gmi_status gmi_sim_destroy(gmi_sim *sim);
+GMI_API gmi_solver *gmi_sim_solver(gmi_sim *sim);
+/* make_body_reference_matrices on the initial state (cilia_sim_main.cpp:159-165);
+ * body_mobility_out (36, column-major) may be NULL. */
+GMI_API gmi_status gmi_sim_prepare(gmi_sim *sim, double *body_mobility_out);
+/* Time step nt (0-based): Broyden until the residual meets tol.  Returns
+ * GMI_ERR_NOT_CONVERGED / GMI_ERR_NONFINITE where the reference stops. */
+GMI_API gmi_status gmi_sim_step(gmi_sim *sim, int nt, int *broyden_iters, int *gmres_iters_total);
+GMI_API gmi_status gmi_sim_get_state(gmi_sim *sim, int field, double *out_h);
+
 /* Measured FMA-pipe throughput (FLOP/s, FMA = 2) of this GPU for
  * precision GMI_FP32C (FP32 pipe) or GMI_FP64 (FP64 pipe): the roofline
  * denominator of the pair kernels, which are bound by that pipe.  No

@@ -1,0 +1,140 @@
+"""Build and run the reference's own simulator on the CPU.  TEST INFRASTRUCTURE ONLY.
+
+The reference's unmodified host sources (cilia_sim_main.cpp, mobility_solver.cpp,
+broyden_solver.cpp, swimmer.cpp, filament.cpp, rigid_body.cpp, segment.cpp,
+quaternion.cpp, matrix.cpp) and its kernels (cuda_functions.cu, compiled as C++
+through ../ref_cpu_shim.h) are compiled from where they lie in the reference
+tree.  Each case gets a config.hpp derived from the reference's own config.hpp
+by replacing the values of named #define lines; it is written to the build
+directory under oracle/_ref and force-included, so its include guard keeps the
+reference's copy out.  ref_solver_shim.h makes the run reproducible and
+full-precision and swaps the CUDA rpy_mobility_solver for a CPU one.
+
+    python oracle/ref_solver/build_ref_solver.py <case> [--run]
+
+Outputs (oracle/_ref/solver_<case>/run): the reference's .dat and .backup files,
+written every step with 17 significant digits, and stdout with the Broyden
+iteration counts.
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE = os.path.dirname(HERE)
+ROOT = os.path.dirname(ORACLE)
+REF = os.environ.get("GMI_REFERENCE_DIR", "/root/reference")
+SCIPY_LIBS = "/usr/local/lib/python3.12/dist-packages/scipy.libs"
+
+REF_CPP = ["cilia_sim_main.cpp", "matrix.cpp", "quaternion.cpp", "segment.cpp", "filament.cpp", "broyden_solver.cpp",
+           "rigid_body.cpp", "swimmer.cpp", "mobility_solver.cpp"]
+
+# Values common to every case: free-swimming instability-driven cilia on a
+# spherical body with the RPY mobility and GMRES, written every step.
+COMMON = dict(CILIA_TYPE="0", BODY_OR_SURFACE_TYPE="2", MOBILITY_TYPE="1", SOLVER_TYPE="1",
+              INITIAL_CONDITIONS_TYPE="0", THREADS_PER_BLOCK="1", SAVES_PER_PERIOD="STEPS_PER_PERIOD",
+              NSWIM="1", MU="1.0", RSEG="1.0")
+
+CASES = {
+    # small swimmer: 4 filaments x 20 segments on 162 blobs
+    "small_swimmer": dict(NFIL="4", NSEG="20", NBLOB="162", R_OVER_L="0.25", RBLOB="1.0", KB="1800.0",
+                          KT="1800.0", TOTAL_TIME_STEPS="12", nblob_subdiv=2, fil_subdiv=1, seed=5),
+    # BASELINE config 1 geometry: sphere of radius 10a, 642 blobs (icosphere 3),
+    # 16 filaments x 20 segments at random icosphere vertices, dt = 1/300,
+    # GMRES tol 1e-8, Broyden tol 1e-4, KB = KT = 1, driven by the reference's
+    # end force (CILIA_TYPE 0)
+    "config1": dict(NFIL="16", NSEG="20", NBLOB="642", R_OVER_L="(10.0/44.0)", RBLOB="1.0", KB="1.0", KT="1.0",
+                    DT="(1.0/300.0)", LINEAR_SYSTEM_TOL="1e-8", TOTAL_TIME_STEPS="100", nblob_subdiv=3,
+                    fil_subdiv=3, seed=2026),
+}
+
+
+def config_text(overrides: dict) -> str:
+    text = open(os.path.join(REF, "config.hpp")).read()
+    for key, val in overrides.items():
+        pat = re.compile(r"(#define[ \t]+" + re.escape(key) + r"[ \t]+)([^\n]*)")
+        text, n = pat.subn(lambda m: m.group(1) + val, text)
+        if n == 0:
+            raise KeyError(f"config.hpp has no #define {key}")
+    return text
+
+
+def build(case: str) -> str:
+    spec = dict(COMMON)
+    spec.update({k: v for k, v in CASES[case].items() if k.isupper()})
+    out = os.path.join(ORACLE, "_ref", f"solver_{case}")
+    os.makedirs(out, exist_ok=True)
+    with open(os.path.join(out, "config.hpp"), "w") as fh:
+        fh.write(config_text(spec))
+    exe = os.path.join(out, "cilia_cpu")
+    inc = ["-I" + out, "-I" + HERE, "-I" + ORACLE, "-I" + REF]
+    base = ["g++", "-O2", "-fopenmp", "-ffp-contract=off", "-std=c++17", "-w", *inc,
+            "-include", os.path.join(out, "config.hpp")]
+    jobs = []
+    for f in REF_CPP:
+        jobs.append(base + ["-include", os.path.join(HERE, "ref_solver_shim.h"), "-c", os.path.join(REF, f),
+                            "-o", os.path.join(out, f + ".o")])
+    jobs.append(base + ["-c", os.path.join(HERE, "cpu_rpy_mobility_solver.cpp"),
+                        "-o", os.path.join(out, "cpu_rpy_mobility_solver.o")])
+    jobs.append(base + ["-c", os.path.join(HERE, "seeding_stub.cpp"), "-o", os.path.join(out, "seeding_stub.o")])
+    jobs.append(base + ["-include", os.path.join(ORACLE, "ref_cpu_shim.h"), "-x", "c++", "-c",
+                        os.path.join(REF, "cuda_functions.cu"), "-o", os.path.join(out, "cuda_functions.o")])
+    jobs.append(["gcc", "-O2", "-c", os.path.join(HERE, "lapack_shim.c"), "-o", os.path.join(out, "lapack_shim.o")])
+
+    def run(cmd):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(" ".join(cmd) + "\n" + r.stderr)
+
+    with ThreadPoolExecutor(8) as ex:
+        list(ex.map(run, jobs))
+    objs = [os.path.join(out, f) for f in os.listdir(out) if f.endswith(".o")]
+    blas = [f for f in os.listdir(SCIPY_LIBS) if f.startswith("libscipy_openblas")][0]
+    run(["g++", "-fopenmp", *objs, "-o", exe, os.path.join(SCIPY_LIBS, blas), "-Wl,-rpath," + SCIPY_LIBS])
+    return exe
+
+
+def seeds(case: str):
+    """Unit-sphere seeds: blobs on an icosphere, filaments at random icosphere vertices."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    from generic_mobility_interface_class_gb300 import seeding
+    spec = CASES[case]
+    nblob, nfil = int(spec["NBLOB"]), int(spec["NFIL"])
+    blobs = seeding.icosphere(spec["nblob_subdiv"])[:nblob]
+    verts = seeding.icosphere(spec["fil_subdiv"])
+    rng = np.random.default_rng(spec["seed"])
+    fils = verts[rng.choice(len(verts), nfil, replace=False)]
+    return blobs, fils
+
+
+def run_case(case: str, exe: str | None = None) -> str:
+    import numpy as np
+    exe = exe or build(case)
+    rundir = os.path.join(os.path.dirname(exe), "run")
+    os.makedirs(rundir, exist_ok=True)
+    for f in os.listdir(rundir):
+        os.remove(os.path.join(rundir, f))
+    blobs, fils = seeds(case)
+    spec = CASES[case]
+    assert spec["NBLOB"] != spec["NFIL"]
+    np.savetxt(os.path.join(rundir, f"sphere{spec['NBLOB']}.seed"), blobs.ravel()[None, :], fmt="%.17g")
+    np.savetxt(os.path.join(rundir, f"sphere{spec['NFIL']}.seed"), fils.ravel()[None, :], fmt="%.17g")
+    r = subprocess.run([exe], cwd=rundir, capture_output=True, text=True)
+    with open(os.path.join(rundir, "stdout.txt"), "w") as fh:
+        fh.write(r.stdout)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr + r.stdout[-2000:])
+    return rundir
+
+
+if __name__ == "__main__":
+    case = sys.argv[1]
+    exe = build(case)
+    print(exe)
+    if "--run" in sys.argv:
+        print(run_case(case, exe))

@@ -1,0 +1,91 @@
+"""Golden trajectories from the reference's own simulator run on the CPU.
+
+Builds cilia_sim_main.cpp and the rest of the reference (unmodified, from
+the reference tree) with oracle/ref_solver/build_ref_solver.py, runs a case,
+and stores its inputs (blob and filament references, the initial force
+perturbations) and its per-step output (segment quaternions, body state,
+segment and body velocities, Broyden iteration counts, final backup) in
+sim_<case>.npz.  The fixtures are committed; the tests never need the tree.
+
+    python tests/golden/make_golden_sim.py small_swimmer
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.ref_solver import build_ref_solver as brs  # noqa: E402
+
+
+def parse_dat(path, skip_cols=1):
+    rows = [np.array(ln.split()[skip_cols:], dtype=np.float64) for ln in open(path) if ln.strip()]
+    return np.stack(rows)
+
+
+def main(case):
+    rundir = brs.run_case(case)
+    spec = dict(brs.COMMON)
+    spec.update({k: v for k, v in brs.CASES[case].items() if k.isupper()})
+    cfg = open(os.path.join(os.path.dirname(rundir), "config.hpp")).read()
+
+    def macro(name):
+        m = re.search(r"#define[ \t]+" + name + r"[ \t]+([^\n/]*)", cfg)
+        return m.group(1).strip()
+
+    nseg, nfil, nblob = int(spec["NSEG"]), int(spec["NFIL"]), int(spec["NBLOB"])
+    DL = 2.2 * float(spec["RSEG"])
+    kb = float(spec["KB"])
+    dimless = float(macro("DIMENSIONLESS_FORCE"))
+    efm = dimless * kb / (DL * DL * nseg * nseg)
+    steps_per_period = float(macro("STEPS_PER_PERIOD"))
+    dt = eval(spec.get("DT", f"(36.3833/{steps_per_period})"))
+    r_over_l = eval(spec["R_OVER_L"])
+    # perturbations: the reference's generator, compiled here
+    exe = os.path.join(os.path.dirname(rundir), "perturbation")
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", os.path.join(ROOT, "oracle", "ref_solver", "perturbation.cpp"),
+                    "-o", exe], check=True)
+    p = np.array([ln.split() for ln in subprocess.run([exe, repr(efm)], capture_output=True, text=True,
+                                                       check=True).stdout.split("\n") if ln.strip()], dtype=float)
+    # The reference writes its reference-position files at the default stream
+    # precision (6 digits); rebuild the exact values the way it does: unit
+    # seeds times Rsphere (rigid_body.cpp:200, 231) and times
+    # R_OVER_L*L + 1.05*(0.5*DL + RBLOB) for the filament bases (swimmer.cpp:172, 199).
+    blobs, fils = brs.seeds(case)
+    L = DL * nseg
+    blob_refs = blobs * (r_over_l * DL * nseg)
+    fil_refs = fils * (r_over_l * L + 1.05 * (0.5 * DL + float(spec["RBLOB"])))
+    chk_b = parse_dat(os.path.join(rundir, "test_blob_references.dat"), 0).reshape(-1, 3)
+    chk_f = parse_dat(os.path.join(rundir, "test_fil_references.dat"), 0).reshape(-1, 3)
+    assert np.allclose(chk_b, blob_refs, rtol=1e-5, atol=1e-5) and np.allclose(chk_f, fil_refs, rtol=1e-5, atol=1e-5)
+    out = subprocess.run(["cat", os.path.join(rundir, "stdout.txt")], capture_output=True, text=True).stdout
+    broyden = [int(m) for m in re.findall(r"Completed step \d+/\d+ in (\d+) Broyden iterations", out)]
+    data = dict(
+        nfil=nfil, nseg=nseg, nblob=nblob, kb=kb, kt=float(spec["KT"]), dt=dt, end_force_magnitude=efm,
+        repulsive_force_factor=float(macro("REPULSIVE_FORCE_FACTOR")), rseg=float(spec["RSEG"]),
+        rblob=float(spec["RBLOB"]), mu=float(spec["MU"]), body_radius=r_over_l * DL * nseg,
+        tol=float(macro("TOL")), linear_tol=float(macro("LINEAR_SYSTEM_TOL")),
+        max_linear_iter=int(macro("MAX_LINEAR_SYSTEM_ITER")),
+        blob_refs=blob_refs, fil_refs=fil_refs,
+        perturbation1=p[0], perturbation2=p[1],
+        seg_q=parse_dat(os.path.join(rundir, "test_seg_states.dat")),
+        body_state=parse_dat(os.path.join(rundir, "test_body_states.dat")),
+        seg_v=parse_dat(os.path.join(rundir, "test_seg_vels.dat")),
+        body_v=parse_dat(os.path.join(rundir, "test_body_vels.dat")),
+        blob_f=parse_dat(os.path.join(rundir, "test_blob_forces.dat")),
+        broyden_iters=np.array(broyden),
+        backup=parse_dat(os.path.join(rundir, "test.backup")),
+    )
+    np.savez_compressed(os.path.join(HERE, f"sim_{case}.npz"), **data)
+    print(case, {k: np.shape(v) for k, v in data.items() if np.ndim(v)})
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "small_swimmer")

@@ -107,6 +107,20 @@ def test_body_reference_matrices(gmi_lib, oracle_built):
     s2.close()
 
 
+def test_ktk_inverse_asymmetric_references(gmi_lib, oracle_built):
+    """(K^T K)^-1 with blob references whose centroid is off the origin, so
+    the off-diagonal blocks (sum of cross-product matrices) do not vanish."""
+    from oracle import mobility_dense as md
+    rng = np.random.default_rng(8)
+    refs = 6.0 * rng.normal(size=(40, 3)) + np.array([2.0, -1.0, 3.0])
+    s = make_solver(refs, 1, 1, 4)
+    s.x_segs_host[:] = 50.0 + rng.normal(size=(4, 3))
+    s.f_segs_host[:] = 0.0
+    ktk, _ = s.make_body_reference_matrices(np.zeros((1, 3)), np.array([[1.0, 0, 0, 0]]))
+    assert rel_err(ktk, md.ktk_inverse(refs)) < 1e-10
+    s.close()
+
+
 def test_fp32c_solver_error(gmi_lib, oracle_built):
     from oracle import mobility_dense as md
     nfil, nseg = 4, 10
