@@ -200,6 +200,7 @@ __global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ C
     R *ring = reinterpret_cast<R *>(smem_raw);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + kStages * kStageScalars * sizeof(R));
 
+    if (args.skip != nullptr && *args.skip != 0) return;
     const int tid = threadIdx.x;
     const int j_begin = blockIdx.y * args.chunk;
     const int j_end = min(j_begin + args.chunk, args.n_src);
@@ -307,8 +308,9 @@ __global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ C
 
 // 3. split reduction: out[i] (=|+=) sum over splits, in split order.
 __global__ void reduce_splits(const double *__restrict__ partial, int splits, int count,
-                              double *__restrict__ out, int accumulate)
+                              double *__restrict__ out, int accumulate, const int *skip)
 {
+    if (skip != nullptr && *skip != 0) return;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= count) return;
     double s = accumulate ? out[e] : 0.0;
@@ -617,7 +619,8 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
     ctx->launches++;
     if (splits > 1) {
         const int count = n_tgt * nout;
-        reduce_splits<<<(count + 255) / 256, 256, 0, ctx->stream>>>(a.partial, splits, count, out, accumulate);
+        reduce_splits<<<(count + 255) / 256, 256, 0, ctx->stream>>>(a.partial, splits, count, out, accumulate,
+                                                                    nullptr);
         ctx->launches++;
         GMI_CUDA_TRY(cudaGetLastError());
     }
@@ -769,6 +772,7 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     a.accumulate = accumulate;
     a.err = env.err;
     a.partial = splits > 1 ? env.partial : nullptr;
+    a.skip = env.skip;
     CUtensorMap map;
     gmi_status st = encode_record_map(env.encode_tiled, &map, src_rec, n_src, f64);
     if (st != GMI_OK) return st;
@@ -776,7 +780,8 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     GMI_CUDA_TRY(cudaLaunchKernel(fn, dim3(n_tgt_ctas, splits), dim3(tpb), params, smem, env.stream));
     if (splits > 1) {
         const int count = n_tgt * nout;
-        reduce_splits<<<(count + 255) / 256, 256, 0, env.stream>>>(a.partial, splits, count, out, accumulate);
+        reduce_splits<<<(count + 255) / 256, 256, 0, env.stream>>>(a.partial, splits, count, out, accumulate,
+                                                                   env.skip);
         GMI_CUDA_TRY(cudaGetLastError());
     }
     return GMI_OK;

@@ -21,6 +21,7 @@ struct PairLaunch {
     double *partial;      // [splits][n_tgt][nout] when there are several
     int accumulate;
     unsigned *err;
+    const int *skip;      // if non-null and *skip != 0 the launch does nothing (converged GMRES)
 };
 
 struct BarrierLaunch {
@@ -62,6 +63,7 @@ struct ExplicitPairEnv {
     void *encode_tiled;    // cuTensorMapEncodeTiled
     int sm_count;
     int tpb, tt;           // launch shape
+    const int *skip;       // optional device flag: non-zero turns the launch into a no-op
 };
 
 size_t record_bytes(bool f64);

@@ -389,6 +389,221 @@ __global__ void scale_kernel(int n, const double *__restrict__ x, const double *
     if (r < n) out[r] = x[r] / s[0];
 }
 
+
+// ---------------------------------------------------------------------------
+// Device-controlled Arnoldi step.  The iteration count and the convergence
+// flag live in a GmresCtl block on the device, so one step needs no host
+// round trip and can be replayed from a CUDA graph; after convergence every
+// kernel of a replayed step returns at once.  A kernel taking `use_col`
+// reads its input at base + ld*(k-1) (the last Krylov vector), else at base.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ const double *gk_in(const double *base, size_t ld, int use_col, const GmresCtl *c)
+{
+    return use_col ? base + ld * (size_t)(c->k - 1) : base;
+}
+
+__global__ void __launch_bounds__(kRedTpb) gk_kt_sums_kernel(int nblob, const double *__restrict__ R,
+                                                             const double *__restrict__ refs, const double *base,
+                                                             size_t ld, int use_col, const GmresCtl *ctl,
+                                                             double *__restrict__ sums)
+{
+    if (ctl->done) return;
+    __shared__ double red[32];
+    const double *f = gk_in(base, ld, use_col, ctl);
+    const int n = blockIdx.x;
+    const double *Rn = R + 9 * n;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int m = threadIdx.x; m < nblob; m += kRedTpb) {
+        const double *fm = f + 3 * ((size_t)n * nblob + m);
+        double d[3];
+        rot_apply(Rn, refs + 3 * m, d);
+        a[0] += fm[0];
+        a[1] += fm[1];
+        a[2] += fm[2];
+        a[3] += d[1] * fm[2] - d[2] * fm[1];
+        a[4] += d[2] * fm[0] - d[0] * fm[2];
+        a[5] += d[0] * fm[1] - d[1] * fm[0];
+    }
+    for (int c = 0; c < 6; ++c) {
+        const double v = block_sum<kRedTpb>(a[c], red);
+        if (threadIdx.x == 0) sums[6 * n + c] = v;
+    }
+}
+
+__global__ void gk_precond_body_kernel(int W, const double *__restrict__ sums, const double *base, size_t ld,
+                                       int use_col, int nb3, const double *__restrict__ ktk_rot,
+                                       const double *__restrict__ mob_rot, double *__restrict__ out_body,
+                                       const GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= W) return;
+    const double *in_body = gk_in(base, ld, use_col, ctl) + nb3;
+    double b[6], u[6];
+    for (int c = 0; c < 6; ++c) {
+        b[c] = -sums[6 * n + c];
+        u[c] = in_body[6 * n + c];
+    }
+    const double *Kt = ktk_rot + 36 * n, *Mb = mob_rot + 36 * n;
+    for (int i = 0; i < 6; ++i) {
+        double x = 0.0, y = 0.0;
+        for (int j = 0; j < 6; ++j) {
+            x += Kt[i + 6 * j] * b[j];
+            y += Mb[i + 6 * j] * u[j];
+        }
+        out_body[6 * n + i] = x - y;
+    }
+}
+
+__global__ void gk_precond_blob_kernel(int W, int nblob, const double *base, size_t ld, int use_col,
+                                       const double *__restrict__ out_body, const double *__restrict__ R,
+                                       const double *__restrict__ refs, double minv, double *__restrict__ out_blob,
+                                       const GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= W * nblob) return;
+    const double *in_blob = gk_in(base, ld, use_col, ctl);
+    const int n = i / nblob, m = i % nblob;
+    double d[3];
+    rot_apply(R + 9 * n, refs + 3 * m, d);
+    const double *U = out_body + 6 * n;
+    double o0 = in_blob[3 * i] + U[0], o1 = in_blob[3 * i + 1] + U[1], o2 = in_blob[3 * i + 2] + U[2];
+    o0 += U[4] * d[2] - U[5] * d[1];
+    o1 += U[5] * d[0] - U[3] * d[2];
+    o2 += U[3] * d[1] - U[4] * d[0];
+    for (int k = n; k < W; ++k) {
+        o0 *= minv;
+        o1 *= minv;
+        o2 *= minv;
+    }
+    out_blob[3 * i] = o0;
+    out_blob[3 * i + 1] = o1;
+    out_blob[3 * i + 2] = o2;
+}
+
+__global__ void gk_sysmult_finish_kernel(int W, int nblob, const double *__restrict__ mbb,
+                                         const double *__restrict__ in_body, const double *__restrict__ sums,
+                                         const double *__restrict__ R, const double *__restrict__ refs,
+                                         double *__restrict__ out, const GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nb = W * nblob;
+    if (i < nb) {
+        const int n = i / nblob, m = i % nblob;
+        double d[3];
+        rot_apply(R + 9 * n, refs + 3 * m, d);
+        const double *U = in_body + 6 * n;
+        out[3 * i] = -(U[0] - d[1] * U[5] + d[2] * U[4]) + mbb[3 * i];
+        out[3 * i + 1] = -(U[1] - d[2] * U[3] + d[0] * U[5]) + mbb[3 * i + 1];
+        out[3 * i + 2] = -(U[2] - d[0] * U[4] + d[1] * U[3]) + mbb[3 * i + 2];
+    } else if (i < nb + 6 * W) {
+        out[3 * nb + (i - nb)] = -sums[i - nb];
+    }
+}
+
+// partial[i * nchunks + c] for i < k (grid.y spans the largest k); or the
+// norm of w when k_override > 0.
+__global__ void __launch_bounds__(kRedTpb) gk_dot_partials_kernel(const double *__restrict__ Q, size_t ld,
+                                                                  const double *__restrict__ w, int n, int nchunks,
+                                                                  double *__restrict__ partial, const GmresCtl *ctl,
+                                                                  int k_override)
+{
+    if (ctl->done) return;
+    const int k = k_override > 0 ? k_override : ctl->k;
+    const int c = blockIdx.x, i = blockIdx.y;
+    if (i >= k) return;
+    __shared__ double red[32];
+    const double *q = Q + ld * i;
+    double a = 0.0;
+    const int r0 = c * kChunkRows, r1 = min(n, r0 + kChunkRows);
+    for (int r = r0 + threadIdx.x; r < r1; r += kRedTpb) a += q[r] * w[r];
+    const double v = block_sum<kRedTpb>(a, red);
+    if (threadIdx.x == 0) partial[(size_t)i * nchunks + c] = v;
+}
+
+__global__ void __launch_bounds__(kRedTpb) gk_cgs_update_kernel(const double *__restrict__ Q, size_t ld,
+                                                                const double *__restrict__ partial, int nchunks,
+                                                                double *__restrict__ w, int n, double *__restrict__ H,
+                                                                int ldh, const GmresCtl *ctl, int pass)
+{
+    if (ctl->done) return;
+    extern __shared__ double h[];
+    const int k = ctl->k;
+    double *Hcol = H + (size_t)ldh * (k - 1);
+    for (int i = threadIdx.x; i < k; i += kRedTpb) {
+        double s = 0.0;
+        for (int c = 0; c < nchunks; ++c) s += partial[(size_t)i * nchunks + c];
+        h[i] = s;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0)
+        for (int i = threadIdx.x; i < k; i += kRedTpb) Hcol[i] = pass == 0 ? h[i] : Hcol[i] + h[i];
+    const int r = blockIdx.x * kRedTpb + threadIdx.x;
+    if (r >= n) return;
+    double acc = w[r];
+    for (int i = 0; i < k; ++i) acc -= h[i] * Q[ld * i + r];
+    w[r] = acc;
+}
+
+__global__ void gk_normalize_kernel(const double *__restrict__ w, int n, const double *__restrict__ partial,
+                                    int nchunks, double *__restrict__ Q, size_t ld, double *__restrict__ H, int ldh,
+                                    const GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    __shared__ double nrm;
+    const int k = ctl->k;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int c = 0; c < nchunks; ++c) s += partial[c];
+        nrm = sqrt(s);
+        if (blockIdx.x == 0) H[(size_t)ldh * (k - 1) + k] = nrm;
+    }
+    __syncthreads();
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) Q[ld * k + r] = nrm > 0.0 ? w[r] / nrm : 0.0;
+}
+
+__global__ void gk_givens_kernel(double *__restrict__ H, int ldh, double *__restrict__ beta, double *__restrict__ cs,
+                                 double *__restrict__ sn, GmresCtl *ctl)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0 || ctl->done) return;
+    const int iter = ctl->k;
+    double *col = H + (size_t)ldh * (iter - 1);
+    for (int i = 1; i < iter; ++i) {
+        const double t = cs[i - 1] * col[i - 1] + sn[i - 1] * col[i];
+        col[i] = cs[i - 1] * col[i] - sn[i - 1] * col[i - 1];
+        col[i - 1] = t;
+    }
+    const double hk = col[iter], hd = col[iter - 1];
+    double c, s;
+    if (hk == 0.0) {
+        c = 1.0;
+        s = 0.0;
+    } else if (fabs(hk) > fabs(hd)) {
+        const double t = hd / hk;
+        s = (2.0 * (double)(hk > 0) - 1.0) / sqrt(1.0 + t * t);
+        c = t * s;
+    } else {
+        const double t = hk / hd;
+        c = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + t * t);
+        s = t * c;
+    }
+    cs[iter - 1] = c;
+    sn[iter - 1] = s;
+    col[iter - 1] = c * hd + s * hk;
+    col[iter] = 0.0;
+    beta[iter] = -s * beta[iter - 1];
+    beta[iter - 1] = c * beta[iter - 1];
+    const double resid = fabs(beta[iter]) / ctl->norm_ref;
+    ctl->resid = resid;
+    if (!(resid > ctl->tol) || iter >= ctl->max_iter)  // converged, at the cap, or NaN
+        ctl->done = 1;
+    else
+        ctl->k = iter + 1;
+}
+
 }  // namespace gmi
 
 namespace gmi {
@@ -508,6 +723,81 @@ static gmi_status orthonormalise(gmi_solver *s, double *w, int k, double *Hcol)
     return launched(s, 2);
 }
 
+// One device-controlled Arnoldi step (apply_preconditioner, system_matrix_mult,
+// CGS2, normalisation, Givens) enqueued on the solver stream; captured once
+// per precision into s->graph[pidx].
+static gmi_status enqueue_arnoldi_step(gmi_solver *s)
+{
+    gmi_context *ctx = s->ctx;
+    cudaStream_t st = ctx->stream;
+    const int nb = s->B, n = s->n, W = s->W, nblob = s->cfg.nblob, ldh = s->m + 1, nc = nchunks_of(n);
+    const size_t ld = (size_t)n;
+    const bool f64 = ctx->precision == GMI_FP64;
+    const double minv = 6.0 * kPi * s->cfg.mu * s->cfg.rblob;
+    gk_kt_sums_kernel<<<W, kRedTpb, 0, st>>>(nblob, s->R, s->refs, s->Q, ld, 1, s->ctl, s->sums);
+    gk_precond_body_kernel<<<grid_for(W, 64), 64, 0, st>>>(W, s->sums, s->Q, ld, 1, 3 * nb, s->ktk_rot, s->mob_rot,
+                                                          s->z + 3 * nb, s->ctl);
+    gk_precond_blob_kernel<<<grid_for(nb), 256, 0, st>>>(W, nblob, s->Q, ld, 1, s->z + 3 * nb, s->R, s->refs, minv,
+                                                         s->z, s->ctl);
+    GMI_CUDA_TRY(cudaGetLastError());
+    GMI_TRY(pack_records_into(st, f64, s->x_blobs, s->z, 3, nb, s->gm_rec));
+    ExplicitPairEnv env{};
+    env.stream = st;
+    env.partial = s->gm_partial;
+    env.partial_bytes = s->gm_partial_bytes;
+    env.err = ctx->d_err;
+    env.encode_tiled = ctx->encode_tiled;
+    env.sm_count = ctx->sm_count;
+    const bool small = (long long)nb * 2 < (long long)ctx->sm_count * 256;
+    env.tpb = small ? 64 : 128;
+    env.tt = small ? 1 : 2;
+    env.skip = &s->ctl->done;
+    PairConsts k;
+    fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
+    GMI_TRY(launch_pair_into(env, kBB, f64, s->gm_rec, 0, nb, s->gm_rec, nb, k, s->mbb, 0));
+    gk_kt_sums_kernel<<<W, kRedTpb, 0, st>>>(nblob, s->R, s->refs, s->z, ld, 0, s->ctl, s->sums);
+    gk_sysmult_finish_kernel<<<grid_for(nb + 6 * W), 256, 0, st>>>(W, nblob, s->mbb, s->z + 3 * nb, s->sums, s->R,
+                                                                   s->refs, s->w, s->ctl);
+    for (int pass = 0; pass < 2; ++pass) {
+        gk_dot_partials_kernel<<<dim3(nc, s->m), kRedTpb, 0, st>>>(s->Q, ld, s->w, n, nc, s->partial, s->ctl, 0);
+        gk_cgs_update_kernel<<<grid_for(n, kRedTpb), kRedTpb, (size_t)s->m * sizeof(double), st>>>(
+            s->Q, ld, s->partial, nc, s->w, n, s->H, ldh, s->ctl, pass);
+    }
+    gk_dot_partials_kernel<<<dim3(nc, 1), kRedTpb, 0, st>>>(s->w, ld, s->w, n, nc, s->partial, s->ctl, 1);
+    gk_normalize_kernel<<<grid_for(n), 256, 0, st>>>(s->w, n, s->partial, nc, s->Q, ld, s->H, ldh, s->ctl);
+    gk_givens_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, s->cs, s->sn, s->ctl);
+    GMI_CUDA_TRY(cudaGetLastError());
+    return GMI_OK;
+}
+
+static gmi_status ensure_arnoldi_graph(gmi_solver *s, int pidx, size_t *nodes)
+{
+    cudaStream_t st = s->ctx->stream;
+    if (st == nullptr || st == cudaStreamLegacy || st == cudaStreamPerThread) {
+        set_last_error_msg("graph capture needs a non-default stream");
+        return GMI_ERR_STATE;
+    }
+    if (s->graph[pidx] == nullptr) {
+        GMI_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+        const gmi_status est = enqueue_arnoldi_step(s);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (est != GMI_OK) {
+            if (g) cudaGraphDestroy(g);
+            return est;
+        }
+        GMI_CUDA_TRY(ce);
+        const cudaError_t ie = cudaGraphInstantiate(&s->graph[pidx], g, 0);
+        size_t cnt = 0;
+        cudaGraphGetNodes(g, nullptr, &cnt);
+        cudaGraphDestroy(g);
+        GMI_CUDA_TRY(ie);
+        s->graph_nodes[pidx] = cnt;
+    }
+    *nodes = s->graph_nodes[pidx];
+    return GMI_OK;
+}
+
 // Arnoldi/GMRES core of solve_linear_system (mobility_solver.cpp:1162-1350),
 // right preconditioned, on A x = b with b in s->rhs and the initial guess in
 // s->soln.  Stops when |beta(iter)| <= tol * norm_ref.  reject_warm_start
@@ -545,6 +835,46 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
     GMI_TRY(launched(s));
     const int max_iter = n < s->m ? n : s->m;
     const int ldh = s->m + 1;
+    const int pidx = s->ctx->precision == GMI_FP64 ? 0 : 1;
+    size_t nodes = 0;
+    if (s->use_graphs && ensure_arnoldi_graph(s, pidx, &nodes) != GMI_OK) s->use_graphs = false;
+    if (s->use_graphs) {
+        GmresCtl c{};
+        c.k = 1;
+        c.done = 0;
+        c.max_iter = max_iter;
+        c.tol = tol;
+        c.norm_ref = norm_ref;
+        *s->h_ctl = c;
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->ctl, s->h_ctl, sizeof c, cudaMemcpyHostToDevice, st));
+        int batch = 4, replayed = 0;
+        for (;;) {
+            for (int b = 0; b < batch; ++b) GMI_CUDA_TRY(cudaGraphLaunch(s->graph[pidx], st));
+            replayed += batch;
+            s->ctx->launches += (long long)batch * (long long)nodes;
+            GMI_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->ctl, sizeof c, cudaMemcpyDeviceToHost, st));
+            GMI_CUDA_TRY(cudaStreamSynchronize(st));
+            if (s->h_ctl->done) break;
+            if (replayed > max_iter + 64) {
+                set_last_error_msg("GMRES control block never signalled completion");
+                return GMI_ERR_STATE;
+            }
+            batch = batch * 2 < 32 ? batch * 2 : 32;
+        }
+        if (!std::isfinite(s->h_ctl->resid)) {
+            set_last_error_msg("GMRES produced a non-finite residual");
+            return GMI_ERR_NONFINITE;
+        }
+        const int iter = s->h_ctl->k;
+        backsolve_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
+        combine_kernel<<<grid_for(n), 256, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
+        GMI_TRY(launched(s, 2));
+        GMI_TRY(apply_preconditioner(s, s->tmp, s->z));
+        axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->soln, 1.0, s->z, s->soln);
+        GMI_TRY(launched(s));
+        *iters_out = iter;
+        return GMI_OK;
+    }
     for (int iter = 1; iter <= max_iter; ++iter) {
         GMI_TRY(apply_preconditioner(s, s->Q + ld * (iter - 1), s->z));
         GMI_TRY(system_matrix_mult(s, s->z, s->w));
@@ -828,6 +1158,9 @@ gmi_status gmi_solver_destroy(gmi_solver *s)
         cudaSetDevice(s->ctx->device);
         cudaStreamSynchronize(s->ctx->stream);
     }
+    for (int g = 0; g < 2; ++g)
+        if (s->graph[g]) cudaGraphExecDestroy(s->graph[g]);
+    if (s->h_ctl) cudaFreeHost(s->h_ctl);
     for (void *p : s->allocs) cudaFree(p);
     double *hp[] = {s->h.v_segs_host, s->h.v_blobs_host, s->h.x_segs_host, s->h.x_blobs_host, s->h.f_segs_host,
                     s->h.f_blobs_host, s->h.f_blobs_repulsion_host, s->h_stage};
@@ -918,6 +1251,21 @@ gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
         TRY_OR_DIE(dalloc(s, &s->xacc, n));
         TRY_OR_DIE(dalloc(s, &s->mbb, 3 * B));
         TRY_OR_DIE(dalloc(s, &s->partial, (size_t)nchunks_of((int)n) * (m + 1)));
+        double *ctl_mem = nullptr, *rec_mem = nullptr, *part_mem = nullptr;
+        TRY_OR_DIE(dalloc(s, &ctl_mem, 8));
+        s->ctl = reinterpret_cast<GmresCtl *>(ctl_mem);
+        TRY_OR_DIE(dalloc(s, &rec_mem, 12 * B));
+        s->gm_rec = rec_mem;
+        const size_t max_splits = (B + 127) / 128 + 1;
+        TRY_OR_DIE(dalloc(s, &part_mem, max_splits * 3 * B));
+        s->gm_partial = part_mem;
+        s->gm_partial_bytes = max_splits * 3 * B * sizeof(double);
+        if (cudaMallocHost(&s->h_ctl, sizeof(GmresCtl)) != cudaSuccess) {
+            s->h_ctl = nullptr;
+            set_last_error_msg("gmi_solver_create: pinned allocation failed");
+            gmi_solver_destroy(s);
+            return GMI_ERR_CUDA;
+        }
     }
     // reference matrices start as identities (mobility_solver.cpp:85-88)
     double I6[36] = {0};

@@ -25,8 +25,28 @@ struct gmi_solver {
     double *scal = nullptr;  // device scalars: [0] norm, [1] resid
     bool refs_set = false;
     std::vector<void *> allocs;
+    // device-controlled Arnoldi iterations replayed from a CUDA graph
+    struct GmresCtl *ctl = nullptr;   // device control block
+    struct GmresCtl *h_ctl = nullptr; // pinned mirror
+    void *gm_rec = nullptr;           // blob records of the GMRES operator (own buffer: fixed address)
+    double *gm_partial = nullptr;     // split partial sums of the GMRES operator
+    size_t gm_partial_bytes = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one Arnoldi step, per precision
+    size_t graph_nodes[2] = {0, 0};
+    bool use_graphs = true;
 };
 
+
+// Iteration state of a GMRES solve that the device advances by itself.
+struct GmresCtl {
+    int k;         // current Arnoldi iteration (1-based)
+    int done;      // set by the Givens step when converged or at max_iter
+    int max_iter;
+    int pad;
+    double tol;    // relative residual target
+    double norm_ref;
+    double resid;  // |beta(k)| / norm_ref after the last Givens step
+};
 
 namespace gmi {
 

@@ -8,8 +8,8 @@ both multiplier-extrapolation stages).  Every step is compared: Broyden
 iteration count, segment quaternions, body position and orientation, segment
 and body velocities.  Differences come from GMRES (CGS2 vs MGS Arnoldi,
 tolerance 1e-10), the approximate-Jacobian inverse (Gauss-Jordan vs LAPACK)
-and summation order, so the tolerance is on the order of the GMRES residual
-times the Broyden amplification.
+and summation order, so state agrees to ~1e-12 and velocities to the GMRES tolerance (~1e-9)
+when the Broyden iteration counts agree, which they must, step by step.
 """
 import numpy as np
 import pytest
@@ -18,7 +18,8 @@ from conftest import load_golden, rel_err
 
 pytestmark = pytest.mark.gpu
 
-TRAJ_TOL = 1e-7
+TRAJ_TOL = 1e-10
+VEL_TOL = 1e-7
 
 
 def test_trajectory_matches_reference(gmi_lib):
@@ -35,6 +36,6 @@ def test_trajectory_matches_reference(gmi_lib):
         bx, bq = sim.state("body_x").ravel(), sim.state("body_q").ravel()
         assert np.max(np.abs(bx - g["body_state"][nt][:3])) < TRAJ_TOL * 10, nt
         assert np.max(np.abs(bq - g["body_state"][nt][3:])) < TRAJ_TOL, nt
-        assert rel_err(sim.state("seg_v").ravel(), g["seg_v"][nt]) < 1e-6, nt
-        assert rel_err(sim.state("body_v").ravel(), g["body_v"][nt]) < 1e-6, nt
+        assert rel_err(sim.state("seg_v").ravel(), g["seg_v"][nt]) < VEL_TOL, nt
+        assert rel_err(sim.state("body_v").ravel(), g["body_v"][nt]) < VEL_TOL, nt
     sim.close()
