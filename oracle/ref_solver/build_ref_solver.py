@@ -44,12 +44,14 @@ CASES = {
     "small_swimmer": dict(NFIL="4", NSEG="20", NBLOB="162", R_OVER_L="0.25", RBLOB="1.0", KB="1800.0",
                           KT="1800.0", TOTAL_TIME_STEPS="12", nblob_subdiv=2, fil_subdiv=1, seed=5),
     # BASELINE config 1 geometry: sphere of radius 10a, 642 blobs (icosphere 3),
-    # 16 filaments x 20 segments at random icosphere vertices, dt = 1/300,
-    # GMRES tol 1e-8, Broyden tol 1e-4, KB = KT = 1, driven by the reference's
-    # end force (CILIA_TYPE 0)
-    "config1": dict(NFIL="16", NSEG="20", NBLOB="642", R_OVER_L="(10.0/44.0)", RBLOB="1.0", KB="1.0", KT="1.0",
-                    DT="(1.0/300.0)", LINEAR_SYSTEM_TOL="1e-8", TOTAL_TIME_STEPS="100", nblob_subdiv=3,
-                    fil_subdiv=3, seed=2026),
+    # 16 filaments x 20 segments at random icosphere vertices, GMRES tol 1e-8,
+    # Broyden tol 1e-4, 100 steps.  The prescribed preferred-curvature beat of
+    # that config is not a reference feature; the filaments are driven by the
+    # reference's end force at its default stiffness and time step (with
+    # KB = KT = 1 and dt = 1/300 the extrapolated guess already meets the
+    # tolerance and Broyden never iterates).
+    "config1": dict(NFIL="16", NSEG="20", NBLOB="642", R_OVER_L="(10.0/44.0)", RBLOB="1.0",
+                    LINEAR_SYSTEM_TOL="1e-8", TOTAL_TIME_STEPS="100", nblob_subdiv=3, fil_subdiv=3, seed=2026),
 }
 
 

@@ -42,7 +42,7 @@ def main(case):
 
     nseg, nfil, nblob = int(spec["NSEG"]), int(spec["NFIL"]), int(spec["NBLOB"])
     DL = 2.2 * float(spec["RSEG"])
-    kb = float(spec["KB"])
+    kb = float(macro("KB"))
     dimless = float(macro("DIMENSIONLESS_FORCE"))
     efm = dimless * kb / (DL * DL * nseg * nseg)
     steps_per_period = float(macro("STEPS_PER_PERIOD"))
@@ -68,7 +68,7 @@ def main(case):
     out = subprocess.run(["cat", os.path.join(rundir, "stdout.txt")], capture_output=True, text=True).stdout
     broyden = [int(m) for m in re.findall(r"Completed step \d+/\d+ in (\d+) Broyden iterations", out)]
     data = dict(
-        nfil=nfil, nseg=nseg, nblob=nblob, kb=kb, kt=float(spec["KT"]), dt=dt, end_force_magnitude=efm,
+        nfil=nfil, nseg=nseg, nblob=nblob, kb=kb, kt=float(macro("KT")), dt=dt, end_force_magnitude=efm,
         repulsive_force_factor=float(macro("REPULSIVE_FORCE_FACTOR")), rseg=float(spec["RSEG"]),
         rblob=float(spec["RBLOB"]), mu=float(spec["MU"]), body_radius=r_over_l * DL * nseg,
         tol=float(macro("TOL")), linear_tol=float(macro("LINEAR_SYSTEM_TOL")),
@@ -83,6 +83,11 @@ def main(case):
         broyden_iters=np.array(broyden),
         backup=parse_dat(os.path.join(rundir, "test.backup")),
     )
+    nsteps = data["seg_q"].shape[0]
+    keep = np.arange(nsteps) if nsteps <= 20 else np.unique(np.r_[np.arange(0, nsteps, 10), nsteps - 1])
+    for key in ("seg_q", "body_state", "seg_v", "body_v", "blob_f"):
+        data[key] = data[key][keep]
+    data["steps"] = keep
     np.savez_compressed(os.path.join(HERE, f"sim_{case}.npz"), **data)
     print(case, {k: np.shape(v) for k, v in data.items() if np.ndim(v)})
 

@@ -22,20 +22,44 @@ TRAJ_TOL = 1e-10
 VEL_TOL = 1e-7
 
 
-def test_trajectory_matches_reference(gmi_lib):
+def run_against_golden(case, state_tol, vel_tol, precision=0):
     from generic_mobility_interface_class_gb300.sim import Simulation
-    g = load_golden("small_swimmer", prefix="sim_")
-    sim = Simulation.from_golden(g)
+    g = load_golden(case, prefix="sim_")
+    sim = Simulation.from_golden(g, precision=precision)
     sim.prepare()
-    nsteps = g["seg_q"].shape[0]
-    for nt in range(nsteps):
-        biters, giters = sim.step(nt)
-        assert biters == int(g["broyden_iters"][nt]), (nt, biters, int(g["broyden_iters"][nt]))
-        q = sim.state("seg_q").ravel()
-        assert rel_err(q, g["seg_q"][nt]) < TRAJ_TOL, nt
-        bx, bq = sim.state("body_x").ravel(), sim.state("body_q").ravel()
-        assert np.max(np.abs(bx - g["body_state"][nt][:3])) < TRAJ_TOL * 10, nt
-        assert np.max(np.abs(bq - g["body_state"][nt][3:])) < TRAJ_TOL, nt
-        assert rel_err(sim.state("seg_v").ravel(), g["seg_v"][nt]) < VEL_TOL, nt
-        assert rel_err(sim.state("body_v").ravel(), g["body_v"][nt]) < VEL_TOL, nt
+    kept = {int(s): k for k, s in enumerate(g["steps"])}
+    worst = {"q": 0.0, "body": 0.0, "v": 0.0}
+    for nt in range(int(g["steps"][-1]) + 1):
+        biters, _ = sim.step(nt)
+        if precision == 0:
+            assert biters == int(g["broyden_iters"][nt]), (nt, biters, int(g["broyden_iters"][nt]))
+        if nt not in kept:
+            continue
+        k = kept[nt]
+        worst["q"] = max(worst["q"], rel_err(sim.state("seg_q").ravel(), g["seg_q"][k]))
+        bs = np.concatenate([sim.state("body_x").ravel(), sim.state("body_q").ravel()])
+        worst["body"] = max(worst["body"], float(np.max(np.abs(bs - g["body_state"][k]))))
+        worst["v"] = max(worst["v"], rel_err(sim.state("seg_v").ravel(), g["seg_v"][k]),
+                         rel_err(sim.state("body_v").ravel(), g["body_v"][k]))
+        assert worst["q"] < state_tol and worst["body"] < state_tol * 10 and worst["v"] < vel_tol, (nt, worst)
     sim.close()
+    return worst
+
+
+def test_trajectory_matches_reference(gmi_lib):
+    """12 steps of a 4-filament swimmer, every step compared."""
+    run_against_golden("small_swimmer", TRAJ_TOL, VEL_TOL)
+
+
+def test_config1_100_steps_match_reference(gmi_lib):
+    """BASELINE config-1 geometry (642 blobs, 16 x 20 segments), 100 steps:
+    identical Broyden iteration counts at every step and the state at every
+    10th step against the reference's own run."""
+    run_against_golden("config1", 1e-9, 1e-6)
+
+
+def test_config1_mixed_precision_trajectory(gmi_lib):
+    """The FP32C pair sums with FP64 solves follow the FP64 trajectory:
+    swimmer velocities within 1e-5 of the reference after 100 steps."""
+    worst = run_against_golden("config1", 1e-5, 1e-5, precision=1)
+    assert worst["v"] < 1e-5
