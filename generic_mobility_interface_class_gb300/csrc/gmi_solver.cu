@@ -12,6 +12,7 @@
 //   GMRES system of size n = 3B + 6W, blobs first (swimmer-major), then bodies;
 //   Krylov basis Q[n x (m+1)] column-major, Hessenberg H[(m+1) x (m+1)] column-major.
 // S = nswim*nfil*nseg segments, B = nswim*nblob blobs, W = nswim.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -604,6 +605,247 @@ __global__ void gk_givens_kernel(double *__restrict__ H, int ldh, double *__rest
         ctl->k = iter + 1;
 }
 
+
+// ---------------------------------------------------------------------------
+// Fused form of the device-controlled Arnoldi step: the same arithmetic as
+// the gk_* kernels above in seven dependent launches instead of sixteen.
+//   F1 (CTA per swimmer)  z = P^-1 q_{k-1}; records of z for the blob-blob
+//                          apply; body rows of w = -K^T z
+//   pair kernel (+ split reduction) on the records -> mbb
+//   F3 (row chunks)       blob rows of w = M_bb z - K z_body; first CGS pass
+//                          partial dots Q^T w                   -> P1
+//   F4 (row chunks)       h1 = sum P1; w -= Q h1; second pass dots -> P2
+//   F5 (row chunks)       h2 = sum P2; H += h2; w -= Q h2; ||w||^2 partials -> P1
+//   F6 (row chunks)       q_k = w / ||w||; H(k, k-1) = ||w||
+//   Givens step           (gk_givens_kernel)
+// Each row-chunk kernel owns kFRows rows; its dots use one warp-shuffle
+// reduction per column and a single block barrier.
+// ---------------------------------------------------------------------------
+constexpr int kFTpb = 256;
+constexpr int kFPer = 1;                 // rows per thread
+constexpr int kFRows = kFTpb * kFPer;    // rows per block
+constexpr int kFMaxK = 160;              // >= max_iter + 1
+
+__device__ __forceinline__ void pack_record(void *rec, int i, const double *x, const double *f, int f64)
+{
+    if (f64) {
+        double2 *r = static_cast<double2 *>(rec) + 6 * (size_t)i;
+        r[0] = make_double2(x[0], x[1]);
+        r[1] = make_double2(x[2], f[0]);
+        r[2] = make_double2(f[1], f[2]);
+        r[3] = make_double2(0.0, 0.0);
+        r[4] = make_double2(0.0, 0.0);
+        r[5] = make_double2(0.0, 0.0);
+    } else {
+        const float hx = (float)x[0], hy = (float)x[1], hz = (float)x[2];
+        float4 *r = static_cast<float4 *>(rec) + 3 * (size_t)i;
+        r[0] = make_float4(hx, hy, hz, (float)f[0]);
+        r[1] = make_float4((float)(x[0] - (double)hx), (float)(x[1] - (double)hy), (float)(x[2] - (double)hz),
+                           (float)f[1]);
+        r[2] = make_float4((float)f[2], 0.f, 0.f, 0.f);
+    }
+}
+
+// F1: one CTA per swimmer.
+__global__ void __launch_bounds__(kRedTpb) f1_precond_kernel(int W, int nblob, const double *__restrict__ Q, size_t ld,
+                                                             const double *__restrict__ R, const double *__restrict__ refs,
+                                                             const double *__restrict__ ktk_rot,
+                                                             const double *__restrict__ mob_rot, double minv,
+                                                             const double *__restrict__ xb, double *__restrict__ z,
+                                                             double *__restrict__ w, void *rec, int f64,
+                                                             const GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    __shared__ double red[32];
+    __shared__ double U[6];
+    const int n = blockIdx.x, nb = W * nblob;
+    const double *in = Q + ld * (size_t)(ctl->k - 1);
+    const double *Rn = R + 9 * n;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int m = threadIdx.x; m < nblob; m += kRedTpb) {
+        const double *fm = in + 3 * ((size_t)n * nblob + m);
+        double d[3];
+        rot_apply(Rn, refs + 3 * m, d);
+        a[0] += fm[0];
+        a[1] += fm[1];
+        a[2] += fm[2];
+        a[3] += d[1] * fm[2] - d[2] * fm[1];
+        a[4] += d[2] * fm[0] - d[0] * fm[2];
+        a[5] += d[0] * fm[1] - d[1] * fm[0];
+    }
+    double sums[6];
+    for (int c = 0; c < 6; ++c) sums[c] = block_sum<kRedTpb>(a[c], red);
+    if (threadIdx.x == 0) {
+        const double *in_body = in + 3 * nb + 6 * n;
+        const double *Kt = ktk_rot + 36 * n, *Mb = mob_rot + 36 * n;
+        for (int i = 0; i < 6; ++i) {
+            double x = 0.0, y = 0.0;
+            for (int j = 0; j < 6; ++j) {
+                x += Kt[i + 6 * j] * (-sums[j]);
+                y += Mb[i + 6 * j] * in_body[j];
+            }
+            U[i] = x - y;
+            z[3 * nb + 6 * n + i] = x - y;
+        }
+    }
+    __syncthreads();
+    double b[6] = {0, 0, 0, 0, 0, 0};
+    for (int m = threadIdx.x; m < nblob; m += kRedTpb) {
+        const int i = n * nblob + m;
+        double d[3];
+        rot_apply(Rn, refs + 3 * m, d);
+        double o[3] = {in[3 * i] + U[0], in[3 * i + 1] + U[1], in[3 * i + 2] + U[2]};
+        o[0] += U[4] * d[2] - U[5] * d[1];
+        o[1] += U[5] * d[0] - U[3] * d[2];
+        o[2] += U[3] * d[1] - U[4] * d[0];
+        for (int k = n; k < W; ++k) {
+            o[0] *= minv;
+            o[1] *= minv;
+            o[2] *= minv;
+        }
+        z[3 * i] = o[0];
+        z[3 * i + 1] = o[1];
+        z[3 * i + 2] = o[2];
+        pack_record(rec, i, xb + 3 * (size_t)i, o, f64);
+        b[0] += o[0];
+        b[1] += o[1];
+        b[2] += o[2];
+        b[3] += d[1] * o[2] - d[2] * o[1];
+        b[4] += d[2] * o[0] - d[0] * o[2];
+        b[5] += d[0] * o[1] - d[1] * o[0];
+    }
+    for (int c = 0; c < 6; ++c) {
+        const double v = block_sum<kRedTpb>(b[c], red);
+        if (threadIdx.x == 0) w[3 * nb + 6 * n + c] = -v;
+    }
+}
+
+// Partial dots of this block's rows (wr[] of every thread) against Q[:, 0..k):
+// the rows go to shared memory, then each warp reduces whole columns.
+__device__ __forceinline__ void f_block_dots(const double *__restrict__ Q, size_t ld, int n, int row0, int k,
+                                             const double *wr, double *ws, double *__restrict__ out, int nchunks)
+{
+#pragma unroll
+    for (int j = 0; j < kFPer; ++j) ws[threadIdx.x + j * kFTpb] = wr[j];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int rows = min(kFRows, n - row0);
+    for (int i = wid; i < k; i += kFTpb / 32) {
+        const double *q = Q + ld * i + row0;
+        double a = 0.0;
+        for (int rr = lane; rr < rows; rr += 32) a += q[rr] * ws[rr];
+        a = warp_sum(a);
+        if (lane == 0) out[(size_t)i * nchunks + blockIdx.x] = a;
+    }
+}
+
+// F3: blob rows of w, first-pass dots.
+__global__ void __launch_bounds__(kFTpb) f3_finish_dots_kernel(int W, int nblob, const double *__restrict__ mbb,
+                                                               const double *__restrict__ z,
+                                                               const double *__restrict__ R,
+                                                               const double *__restrict__ refs, double *__restrict__ w,
+                                                               const double *__restrict__ Q, size_t ld, int n,
+                                                               int nchunks, double *__restrict__ P1,
+                                                               const GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    __shared__ double ws[kFRows];
+    const int k = ctl->k, row0 = blockIdx.x * kFRows, nb3 = 3 * W * nblob;
+    double wr[kFPer];
+#pragma unroll
+    for (int j = 0; j < kFPer; ++j) {
+        const int r = row0 + threadIdx.x + j * kFTpb;
+        double v = 0.0;
+        if (r < nb3) {
+            const int i = r / 3, c = r % 3, sw = i / nblob, m = i % nblob;
+            double d[3];
+            rot_apply(R + 9 * sw, refs + 3 * m, d);
+            const double *U = z + nb3 + 6 * sw;
+            double kz;
+            if (c == 0) kz = U[0] - d[1] * U[5] + d[2] * U[4];
+            else if (c == 1) kz = U[1] - d[2] * U[3] + d[0] * U[5];
+            else kz = U[2] - d[0] * U[4] + d[1] * U[3];
+            v = -kz + mbb[r];
+            w[r] = v;
+        } else if (r < n) {
+            v = w[r];
+        }
+        wr[j] = v;
+    }
+    f_block_dots(Q, ld, n, row0, k, wr, ws, P1, nchunks);
+}
+
+// F4 / F5: h = sum of the partials; H column gets h (pass 0: store, pass 1:
+// add); w -= Q h; then either the next pass's dots (Pout, pass 0) or the
+// partial squared norm of w (Pout[block], pass 1).
+__global__ void __launch_bounds__(kFTpb) f45_update_kernel(const double *__restrict__ Q, size_t ld, int n,
+                                                           int nchunks, const double *__restrict__ Pin,
+                                                           double *__restrict__ Pout, double *__restrict__ w,
+                                                           double *__restrict__ H, int ldh, const GmresCtl *ctl,
+                                                           int pass)
+{
+    if (ctl->done) return;
+    __shared__ double ws[kFRows];
+    __shared__ double h[kFMaxK];
+    const int k = ctl->k, row0 = blockIdx.x * kFRows;
+    for (int i = threadIdx.x; i < k; i += kFTpb) {
+        double t = 0.0;
+        for (int c = 0; c < nchunks; ++c) t += Pin[(size_t)i * nchunks + c];
+        h[i] = t;
+    }
+    __syncthreads();
+    if (blockIdx.x == 0) {
+        double *Hcol = H + (size_t)ldh * (k - 1);
+        for (int i = threadIdx.x; i < k; i += kFTpb) Hcol[i] = pass == 0 ? h[i] : Hcol[i] + h[i];
+    }
+    double wr[kFPer];
+#pragma unroll
+    for (int j = 0; j < kFPer; ++j) {
+        const int r = row0 + threadIdx.x + j * kFTpb;
+        double v = 0.0;
+        if (r < n) {
+            v = w[r];
+            for (int i = 0; i < k; ++i) v -= h[i] * Q[ld * i + r];
+            w[r] = v;
+        }
+        wr[j] = v;
+    }
+    if (pass == 0) {
+        f_block_dots(Q, ld, n, row0, k, wr, ws, Pout, nchunks);
+    } else {
+        double a = 0.0;
+#pragma unroll
+        for (int j = 0; j < kFPer; ++j) a += wr[j] * wr[j];
+        __shared__ double red[32];
+        const double t = block_sum<kFTpb>(a, red);
+        if (threadIdx.x == 0) Pout[blockIdx.x] = t;
+    }
+}
+
+// F6: q_k = w / ||w||, H(k, k-1) = ||w||.
+__global__ void __launch_bounds__(kFTpb) f6_normalize_kernel(const double *__restrict__ w, int n, int nchunks,
+                                                             const double *__restrict__ P, double *__restrict__ Q,
+                                                             size_t ld, double *__restrict__ H, int ldh,
+                                                             const GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    __shared__ double nrm;
+    const int k = ctl->k;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int c = 0; c < nchunks; ++c) t += P[c];
+        nrm = sqrt(t);
+        if (blockIdx.x == 0) H[(size_t)ldh * (k - 1) + k] = nrm;
+    }
+    __syncthreads();
+    const int row0 = blockIdx.x * kFRows;
+#pragma unroll
+    for (int j = 0; j < kFPer; ++j) {
+        const int r = row0 + threadIdx.x + j * kFTpb;
+        if (r < n) Q[ld * k + r] = nrm > 0.0 ? w[r] / nrm : 0.0;
+    }
+}
+
 }  // namespace gmi
 
 namespace gmi {
@@ -730,17 +972,20 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s)
 {
     gmi_context *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
-    const int nb = s->B, n = s->n, W = s->W, nblob = s->cfg.nblob, ldh = s->m + 1, nc = nchunks_of(n);
+    const int nb = s->B, n = s->n, W = s->W, nblob = s->cfg.nblob, ldh = s->m + 1;
+    const int nc = (n + kFRows - 1) / kFRows;
     const size_t ld = (size_t)n;
     const bool f64 = ctx->precision == GMI_FP64;
     const double minv = 6.0 * kPi * s->cfg.mu * s->cfg.rblob;
-    gk_kt_sums_kernel<<<W, kRedTpb, 0, st>>>(nblob, s->R, s->refs, s->Q, ld, 1, s->ctl, s->sums);
-    gk_precond_body_kernel<<<grid_for(W, 64), 64, 0, st>>>(W, s->sums, s->Q, ld, 1, 3 * nb, s->ktk_rot, s->mob_rot,
-                                                          s->z + 3 * nb, s->ctl);
-    gk_precond_blob_kernel<<<grid_for(nb), 256, 0, st>>>(W, nblob, s->Q, ld, 1, s->z + 3 * nb, s->R, s->refs, minv,
-                                                         s->z, s->ctl);
+    if (2 * (size_t)nc * (s->m + 1) > s->partial_count || s->m + 1 > kFMaxK) {
+        set_last_error("partial-sum buffer smaller than the Arnoldi step needs", "enqueue_arnoldi_step", __FILE__,
+                       __LINE__);
+        return GMI_ERR_STATE;
+    }
+    double *P1 = s->partial, *P2 = s->partial + (size_t)nc * (s->m + 1);
+    f1_precond_kernel<<<W, kRedTpb, 0, st>>>(W, nblob, s->Q, ld, s->R, s->refs, s->ktk_rot, s->mob_rot, minv,
+                                             s->x_blobs, s->z, s->w, s->gm_rec, f64 ? 1 : 0, s->ctl);
     GMI_CUDA_TRY(cudaGetLastError());
-    GMI_TRY(pack_records_into(st, f64, s->x_blobs, s->z, 3, nb, s->gm_rec));
     ExplicitPairEnv env{};
     env.stream = st;
     env.partial = s->gm_partial;
@@ -755,16 +1000,11 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s)
     PairConsts k;
     fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
     GMI_TRY(launch_pair_into(env, kBB, f64, s->gm_rec, 0, nb, s->gm_rec, nb, k, s->mbb, 0));
-    gk_kt_sums_kernel<<<W, kRedTpb, 0, st>>>(nblob, s->R, s->refs, s->z, ld, 0, s->ctl, s->sums);
-    gk_sysmult_finish_kernel<<<grid_for(nb + 6 * W), 256, 0, st>>>(W, nblob, s->mbb, s->z + 3 * nb, s->sums, s->R,
-                                                                   s->refs, s->w, s->ctl);
-    for (int pass = 0; pass < 2; ++pass) {
-        gk_dot_partials_kernel<<<dim3(nc, s->m), kRedTpb, 0, st>>>(s->Q, ld, s->w, n, nc, s->partial, s->ctl, 0);
-        gk_cgs_update_kernel<<<grid_for(n, kRedTpb), kRedTpb, (size_t)s->m * sizeof(double), st>>>(
-            s->Q, ld, s->partial, nc, s->w, n, s->H, ldh, s->ctl, pass);
-    }
-    gk_dot_partials_kernel<<<dim3(nc, 1), kRedTpb, 0, st>>>(s->w, ld, s->w, n, nc, s->partial, s->ctl, 1);
-    gk_normalize_kernel<<<grid_for(n), 256, 0, st>>>(s->w, n, s->partial, nc, s->Q, ld, s->H, ldh, s->ctl);
+    f3_finish_dots_kernel<<<nc, kFTpb, 0, st>>>(W, nblob, s->mbb, s->z, s->R, s->refs, s->w, s->Q, ld, n, nc, P1,
+                                                s->ctl);
+    f45_update_kernel<<<nc, kFTpb, 0, st>>>(s->Q, ld, n, nc, P1, P2, s->w, s->H, ldh, s->ctl, 0);
+    f45_update_kernel<<<nc, kFTpb, 0, st>>>(s->Q, ld, n, nc, P2, P1, s->w, s->H, ldh, s->ctl, 1);
+    f6_normalize_kernel<<<nc, kFTpb, 0, st>>>(s->w, n, nc, P1, s->Q, ld, s->H, ldh, s->ctl);
     gk_givens_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, s->cs, s->sn, s->ctl);
     GMI_CUDA_TRY(cudaGetLastError());
     return GMI_OK;
@@ -1187,6 +1427,11 @@ gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
     GMI_ARG_CHECK(s != nullptr, "gmi_solver_create: out of host memory");
     s->cfg = *cfg;
     if (s->cfg.max_linear_iter <= 0) s->cfg.max_linear_iter = 150;
+    if (s->cfg.max_linear_iter > kFMaxK - 1) {
+        set_last_error_msg("gmi_solver_create: max_linear_iter above the supported 159");
+        delete s;
+        return GMI_ERR_ARG;
+    }
     if (s->cfg.linear_tol <= 0) s->cfg.linear_tol = 1e-10;
     gmi_status st = gmi_context_create(cfg->device, &s->ctx);
     if (st != GMI_OK) {
@@ -1250,7 +1495,11 @@ gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
         TRY_OR_DIE(dalloc(s, &s->b64, n));
         TRY_OR_DIE(dalloc(s, &s->xacc, n));
         TRY_OR_DIE(dalloc(s, &s->mbb, 3 * B));
-        TRY_OR_DIE(dalloc(s, &s->partial, (size_t)nchunks_of((int)n) * (m + 1)));
+        // Two partial arrays of (m + 1) columns, each long enough for either
+        // row chunking (kChunkRows for the host loop, kFRows for the graph).
+        const size_t pch = std::max<size_t>((size_t)nchunks_of((int)n) + n / 1024 + 1, (n + kFRows - 1) / kFRows);
+        s->partial_count = 2 * pch * (m + 1);
+        TRY_OR_DIE(dalloc(s, &s->partial, s->partial_count));
         double *ctl_mem = nullptr, *rec_mem = nullptr, *part_mem = nullptr;
         TRY_OR_DIE(dalloc(s, &ctl_mem, 8));
         s->ctl = reinterpret_cast<GmresCtl *>(ctl_mem);

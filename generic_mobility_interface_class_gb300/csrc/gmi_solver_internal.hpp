@@ -29,6 +29,7 @@ struct gmi_solver {
     struct GmresCtl *ctl = nullptr;   // device control block
     struct GmresCtl *h_ctl = nullptr; // pinned mirror
     void *gm_rec = nullptr;           // blob records of the GMRES operator (own buffer: fixed address)
+    size_t partial_count = 0;         // doubles in partial
     double *gm_partial = nullptr;     // split partial sums of the GMRES operator
     size_t gm_partial_bytes = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one Arnoldi step, per precision

@@ -54,8 +54,9 @@ def test_trajectory_matches_reference(gmi_lib):
 def test_config1_100_steps_match_reference(gmi_lib):
     """BASELINE config-1 geometry (642 blobs, 16 x 20 segments), 100 steps:
     identical Broyden iteration counts at every step and the state at every
-    10th step against the reference's own run."""
-    run_against_golden("config1", 1e-9, 1e-6)
+    10th step against the reference's own run.  This case solves GMRES to
+    1e-8 (not 1e-10), so velocities agree to ~1e-6 and the state to ~1e-8."""
+    run_against_golden("config1", 1e-7, 1e-5)
 
 
 def test_config1_mixed_precision_trajectory(gmi_lib):
