@@ -324,8 +324,17 @@ __global__ void reduce_splits(const double *__restrict__ partial, int splits, in
 // the original arrays, so the force arithmetic is the reference's FP64.
 // Targets: segments [0,S) then blobs [S, S+B) (of the requested ranges);
 // sources: all S segments then all B blobs.
+//
+// The FP64 path (sqrt, divide) is slow on this GPU and rare per lane, so the
+// lanes of a warp do not each run it for their own candidates: every warp
+// queues its candidates (lane, j) in shared memory in screening order,
+// evaluates them 32 at a time, one per lane, and each lane then adds its own
+// entries in queue order, which is ascending j: the reference's summation
+// order per target.
 // ---------------------------------------------------------------------------
-constexpr int kBarrierTpb = 128;
+constexpr int kBarrierTpb = 64;
+constexpr int kBarrierWarps = kBarrierTpb / 32;
+constexpr int kBarrierQ = 64;  // queue entries per warp (flushed at >= 32)
 
 __global__ void pack_screen_positions(const double *__restrict__ xs, int S, const double *__restrict__ xb, int B,
                                       float4 *__restrict__ out)
@@ -339,9 +348,63 @@ __global__ void pack_screen_positions(const double *__restrict__ xs, int S, cons
         make_float4((float)(p[0] - (double)hx), (float)(p[1] - (double)hy), (float)(p[2] - (double)hz), 0.f);
 }
 
+struct BarrierQueue {
+    int j[kBarrierQ];
+    int lane[kBarrierQ];
+    double v[3][kBarrierQ];
+};
+
+// Evaluate the warp's queued candidates in FP64 and add them, in queue order,
+// to the owning lanes' accumulators.
+__device__ __forceinline__ void barrier_flush(const BarrierLaunch &a, BarrierQueue &q, int count, double xi,
+                                              double yi, double zi, double a_tgt, double &g0, double &g1, double &g2)
+{
+    const int lane = threadIdx.x & 31;
+    for (int base = 0; base < count; base += 32) {
+        const int e = base + lane;
+        const int src = e < count ? q.lane[e] : lane;
+        const double tx = __shfl_sync(0xffffffffu, xi, src);
+        const double ty = __shfl_sync(0xffffffffu, yi, src);
+        const double tz = __shfl_sync(0xffffffffu, zi, src);
+        const double ta = __shfl_sync(0xffffffffu, a_tgt, src);
+        if (e < count) {
+            const int j = q.j[e];
+            const bool src_seg = j < a.S;
+            const double asum = ta + (src_seg ? a.rseg : a.rblob);
+            const double *pj = src_seg ? a.xs + 3 * (size_t)j : a.xb + 3 * (size_t)(j - a.S);
+            const double ddx = tx - pj[0], ddy = ty - pj[1], ddz = tz - pj[2];
+            const double dist = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+            double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+            if (dist < 1.1 * asum) {
+                double c = fmin(1.0, 1.0 - (10.0 / asum) * (dist - asum));
+                c = a.scale * c * c * c * c;
+                const double idist = 1.0 / dist;
+                v0 = c * ddx * idist;
+                v1 = c * ddy * idist;
+                v2 = c * ddz * idist;
+            }
+            q.v[0][e] = v0;
+            q.v[1][e] = v1;
+            q.v[2][e] = v2;
+        }
+    }
+    __syncwarp();
+    for (int e = 0; e < count; ++e) {
+        if (q.lane[e] == lane) {
+            g0 += q.v[0][e];
+            g1 += q.v[1][e];
+            g2 += q.v[2][e];
+        }
+    }
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
 {
     __shared__ float4 tile[2 * kBarrierTpb];
+    __shared__ BarrierQueue queues[kBarrierWarps];
+    BarrierQueue &q = queues[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
     const int N = a.S + a.B;
     const int local = blockIdx.x * blockDim.x + threadIdx.x;  // over [0, num_segs + num_blobs)
     const bool is_seg_target = local < a.num_segs;
@@ -362,8 +425,11 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
         const double fz = fmin(1.0, 1.0 - (zi - a.rseg) / (0.5 * DL - a.rseg));
         g2 = a.scale * fz * fz * fz * fz;
     }
-    // widest cutoff over the source types, with a relative margin for the FP32 screen
     const double a_tgt = is_seg_target ? a.rseg : a.rblob;
+    // FP32 screen cutoffs against segment and blob sources, with a relative margin
+    const float cut_s = (float)(1.1 * (a_tgt + a.rseg)) * 1.001f;
+    const float cut_b = (float)(1.1 * (a_tgt + a.rblob)) * 1.001f;
+    int count = 0;  // warp-uniform
     for (int j0 = 0; j0 < N; j0 += kBarrierTpb) {
         const int jl = j0 + threadIdx.x;
         if (jl < N) {
@@ -372,43 +438,41 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
         }
         __syncthreads();
         const int jn = min(kBarrierTpb, N - j0);
-        if (valid) {
-            for (int jj = 0; jj < jn; ++jj) {
-                const int j = j0 + jj;
-                const float4 q = tile[2 * jj], ql = tile[2 * jj + 1];
-                const float dx = (pf.x - q.x) + (pl.x - ql.x);
-                const float dy = (pf.y - q.y) + (pl.y - ql.y);
-                const float dz = (pf.z - q.z) + (pl.z - ql.z);
-                const float d2 = dx * dx + dy * dy + dz * dz;
-                const bool src_seg = j < a.S;
-                const double asum = a_tgt + (src_seg ? a.rseg : a.rblob);
-                const float cut = (float)(1.1 * asum) * 1.001f;
-                if (d2 >= cut * cut) continue;
-                // candidate: exact FP64 evaluation, as the reference
-                bool excluded;
+        for (int jj = 0; jj < jn; ++jj) {
+            const int j = j0 + jj;
+            const float4 s = tile[2 * jj], sl = tile[2 * jj + 1];
+            const float dx = (pf.x - s.x) + (pl.x - sl.x);
+            const float dy = (pf.y - s.y) + (pl.y - sl.y);
+            const float dz = (pf.z - s.z) + (pl.z - sl.z);
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float cut = j < a.S ? cut_s : cut_b;
+            bool cand = valid && d2 < cut * cut;
+            if (cand) {
                 if (is_seg_target) {
-                    const int fil_j = j / a.nseg;
                     const int di = gi - j;
-                    excluded = (fil_i == fil_j) && (di <= 1 && di >= -1);
+                    cand = !((fil_i == j / a.nseg) && (di <= 1 && di >= -1));
                 } else {
-                    excluded = (j == gi);
+                    cand = (j != gi);
                 }
-                if (excluded) continue;
-                const double *pj = src_seg ? a.xs + 3 * (size_t)j : a.xb + 3 * (size_t)(j - a.S);
-                const double ddx = xi - pj[0], ddy = yi - pj[1], ddz = zi - pj[2];
-                const double dist = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
-                if (dist < 1.1 * asum) {
-                    double c = fmin(1.0, 1.0 - (10.0 / asum) * (dist - asum));
-                    c = a.scale * c * c * c * c;
-                    const double idist = 1.0 / dist;
-                    g0 += c * ddx * idist;
-                    g1 += c * ddy * idist;
-                    g2 += c * ddz * idist;
+            }
+            const unsigned mask = __ballot_sync(0xffffffffu, cand);
+            if (mask) {
+                if (cand) {
+                    const int pos = count + __popc(mask & ((1u << lane) - 1u));
+                    q.j[pos] = j;
+                    q.lane[pos] = lane;
+                }
+                count += __popc(mask);
+                __syncwarp();
+                if (count >= 32) {
+                    barrier_flush(a, q, count, xi, yi, zi, a_tgt, g0, g1, g2);
+                    count = 0;
                 }
             }
         }
         __syncthreads();
     }
+    if (count > 0) barrier_flush(a, q, count, xi, yi, zi, a_tgt, g0, g1, g2);
     if (!valid) return;
     if (is_seg_target) {
         double *f = a.f_segs + 6 * (size_t)gi;

@@ -353,19 +353,6 @@ __global__ void givens_kernel(double *__restrict__ H, int ldh, double *__restric
     *resid = fabs(beta[iter]) / norm_rhs;
 }
 
-// Back substitution for y (mobility_solver.cpp:1236-1250).
-__global__ void backsolve_kernel(const double *__restrict__ H, int ldh, const double *__restrict__ beta, int iter,
-                                 double *__restrict__ y)
-{
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    y[iter - 1] = beta[iter - 1] / H[(size_t)ldh * (iter - 1) + (iter - 1)];
-    for (int i = iter - 2; i >= 0; --i) {
-        double v = beta[i];
-        for (int j = iter - 1; j > i; --j) v -= H[(size_t)ldh * j + i] * y[j];
-        y[i] = v / H[(size_t)ldh * i + i];
-    }
-}
-
 // out = sum_i y_i Q[:, i], in the reference's column order (mobility_solver.cpp:1252-1255).
 __global__ void combine_kernel(const double *__restrict__ Q, size_t ld, const double *__restrict__ y, int k, int n,
                                double *__restrict__ out)
@@ -392,239 +379,35 @@ __global__ void scale_kernel(int n, const double *__restrict__ x, const double *
 
 
 // ---------------------------------------------------------------------------
-// Device-controlled Arnoldi step.  The iteration count and the convergence
-// flag live in a GmresCtl block on the device, so one step needs no host
-// round trip and can be replayed from a CUDA graph; after convergence every
-// kernel of a replayed step returns at once.  A kernel taking `use_col`
-// reads its input at base + ld*(k-1) (the last Krylov vector), else at base.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ const double *gk_in(const double *base, size_t ld, int use_col, const GmresCtl *c)
-{
-    return use_col ? base + ld * (size_t)(c->k - 1) : base;
-}
-
-__global__ void __launch_bounds__(kRedTpb) gk_kt_sums_kernel(int nblob, const double *__restrict__ R,
-                                                             const double *__restrict__ refs, const double *base,
-                                                             size_t ld, int use_col, const GmresCtl *ctl,
-                                                             double *__restrict__ sums)
-{
-    if (ctl->done) return;
-    __shared__ double red[32];
-    const double *f = gk_in(base, ld, use_col, ctl);
-    const int n = blockIdx.x;
-    const double *Rn = R + 9 * n;
-    double a[6] = {0, 0, 0, 0, 0, 0};
-    for (int m = threadIdx.x; m < nblob; m += kRedTpb) {
-        const double *fm = f + 3 * ((size_t)n * nblob + m);
-        double d[3];
-        rot_apply(Rn, refs + 3 * m, d);
-        a[0] += fm[0];
-        a[1] += fm[1];
-        a[2] += fm[2];
-        a[3] += d[1] * fm[2] - d[2] * fm[1];
-        a[4] += d[2] * fm[0] - d[0] * fm[2];
-        a[5] += d[0] * fm[1] - d[1] * fm[0];
-    }
-    for (int c = 0; c < 6; ++c) {
-        const double v = block_sum<kRedTpb>(a[c], red);
-        if (threadIdx.x == 0) sums[6 * n + c] = v;
-    }
-}
-
-__global__ void gk_precond_body_kernel(int W, const double *__restrict__ sums, const double *base, size_t ld,
-                                       int use_col, int nb3, const double *__restrict__ ktk_rot,
-                                       const double *__restrict__ mob_rot, double *__restrict__ out_body,
-                                       const GmresCtl *ctl)
-{
-    if (ctl->done) return;
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= W) return;
-    const double *in_body = gk_in(base, ld, use_col, ctl) + nb3;
-    double b[6], u[6];
-    for (int c = 0; c < 6; ++c) {
-        b[c] = -sums[6 * n + c];
-        u[c] = in_body[6 * n + c];
-    }
-    const double *Kt = ktk_rot + 36 * n, *Mb = mob_rot + 36 * n;
-    for (int i = 0; i < 6; ++i) {
-        double x = 0.0, y = 0.0;
-        for (int j = 0; j < 6; ++j) {
-            x += Kt[i + 6 * j] * b[j];
-            y += Mb[i + 6 * j] * u[j];
-        }
-        out_body[6 * n + i] = x - y;
-    }
-}
-
-__global__ void gk_precond_blob_kernel(int W, int nblob, const double *base, size_t ld, int use_col,
-                                       const double *__restrict__ out_body, const double *__restrict__ R,
-                                       const double *__restrict__ refs, double minv, double *__restrict__ out_blob,
-                                       const GmresCtl *ctl)
-{
-    if (ctl->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= W * nblob) return;
-    const double *in_blob = gk_in(base, ld, use_col, ctl);
-    const int n = i / nblob, m = i % nblob;
-    double d[3];
-    rot_apply(R + 9 * n, refs + 3 * m, d);
-    const double *U = out_body + 6 * n;
-    double o0 = in_blob[3 * i] + U[0], o1 = in_blob[3 * i + 1] + U[1], o2 = in_blob[3 * i + 2] + U[2];
-    o0 += U[4] * d[2] - U[5] * d[1];
-    o1 += U[5] * d[0] - U[3] * d[2];
-    o2 += U[3] * d[1] - U[4] * d[0];
-    for (int k = n; k < W; ++k) {
-        o0 *= minv;
-        o1 *= minv;
-        o2 *= minv;
-    }
-    out_blob[3 * i] = o0;
-    out_blob[3 * i + 1] = o1;
-    out_blob[3 * i + 2] = o2;
-}
-
-__global__ void gk_sysmult_finish_kernel(int W, int nblob, const double *__restrict__ mbb,
-                                         const double *__restrict__ in_body, const double *__restrict__ sums,
-                                         const double *__restrict__ R, const double *__restrict__ refs,
-                                         double *__restrict__ out, const GmresCtl *ctl)
-{
-    if (ctl->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nb = W * nblob;
-    if (i < nb) {
-        const int n = i / nblob, m = i % nblob;
-        double d[3];
-        rot_apply(R + 9 * n, refs + 3 * m, d);
-        const double *U = in_body + 6 * n;
-        out[3 * i] = -(U[0] - d[1] * U[5] + d[2] * U[4]) + mbb[3 * i];
-        out[3 * i + 1] = -(U[1] - d[2] * U[3] + d[0] * U[5]) + mbb[3 * i + 1];
-        out[3 * i + 2] = -(U[2] - d[0] * U[4] + d[1] * U[3]) + mbb[3 * i + 2];
-    } else if (i < nb + 6 * W) {
-        out[3 * nb + (i - nb)] = -sums[i - nb];
-    }
-}
-
-// partial[i * nchunks + c] for i < k (grid.y spans the largest k); or the
-// norm of w when k_override > 0.
-__global__ void __launch_bounds__(kRedTpb) gk_dot_partials_kernel(const double *__restrict__ Q, size_t ld,
-                                                                  const double *__restrict__ w, int n, int nchunks,
-                                                                  double *__restrict__ partial, const GmresCtl *ctl,
-                                                                  int k_override)
-{
-    if (ctl->done) return;
-    const int k = k_override > 0 ? k_override : ctl->k;
-    const int c = blockIdx.x, i = blockIdx.y;
-    if (i >= k) return;
-    __shared__ double red[32];
-    const double *q = Q + ld * i;
-    double a = 0.0;
-    const int r0 = c * kChunkRows, r1 = min(n, r0 + kChunkRows);
-    for (int r = r0 + threadIdx.x; r < r1; r += kRedTpb) a += q[r] * w[r];
-    const double v = block_sum<kRedTpb>(a, red);
-    if (threadIdx.x == 0) partial[(size_t)i * nchunks + c] = v;
-}
-
-__global__ void __launch_bounds__(kRedTpb) gk_cgs_update_kernel(const double *__restrict__ Q, size_t ld,
-                                                                const double *__restrict__ partial, int nchunks,
-                                                                double *__restrict__ w, int n, double *__restrict__ H,
-                                                                int ldh, const GmresCtl *ctl, int pass)
-{
-    if (ctl->done) return;
-    extern __shared__ double h[];
-    const int k = ctl->k;
-    double *Hcol = H + (size_t)ldh * (k - 1);
-    for (int i = threadIdx.x; i < k; i += kRedTpb) {
-        double s = 0.0;
-        for (int c = 0; c < nchunks; ++c) s += partial[(size_t)i * nchunks + c];
-        h[i] = s;
-    }
-    __syncthreads();
-    if (blockIdx.x == 0)
-        for (int i = threadIdx.x; i < k; i += kRedTpb) Hcol[i] = pass == 0 ? h[i] : Hcol[i] + h[i];
-    const int r = blockIdx.x * kRedTpb + threadIdx.x;
-    if (r >= n) return;
-    double acc = w[r];
-    for (int i = 0; i < k; ++i) acc -= h[i] * Q[ld * i + r];
-    w[r] = acc;
-}
-
-__global__ void gk_normalize_kernel(const double *__restrict__ w, int n, const double *__restrict__ partial,
-                                    int nchunks, double *__restrict__ Q, size_t ld, double *__restrict__ H, int ldh,
-                                    const GmresCtl *ctl)
-{
-    if (ctl->done) return;
-    __shared__ double nrm;
-    const int k = ctl->k;
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (int c = 0; c < nchunks; ++c) s += partial[c];
-        nrm = sqrt(s);
-        if (blockIdx.x == 0) H[(size_t)ldh * (k - 1) + k] = nrm;
-    }
-    __syncthreads();
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < n) Q[ld * k + r] = nrm > 0.0 ? w[r] / nrm : 0.0;
-}
-
-__global__ void gk_givens_kernel(double *__restrict__ H, int ldh, double *__restrict__ beta, double *__restrict__ cs,
-                                 double *__restrict__ sn, GmresCtl *ctl)
-{
-    if (threadIdx.x != 0 || blockIdx.x != 0 || ctl->done) return;
-    const int iter = ctl->k;
-    double *col = H + (size_t)ldh * (iter - 1);
-    for (int i = 1; i < iter; ++i) {
-        const double t = cs[i - 1] * col[i - 1] + sn[i - 1] * col[i];
-        col[i] = cs[i - 1] * col[i] - sn[i - 1] * col[i - 1];
-        col[i - 1] = t;
-    }
-    const double hk = col[iter], hd = col[iter - 1];
-    double c, s;
-    if (hk == 0.0) {
-        c = 1.0;
-        s = 0.0;
-    } else if (fabs(hk) > fabs(hd)) {
-        const double t = hd / hk;
-        s = (2.0 * (double)(hk > 0) - 1.0) / sqrt(1.0 + t * t);
-        c = t * s;
-    } else {
-        const double t = hk / hd;
-        c = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + t * t);
-        s = t * c;
-    }
-    cs[iter - 1] = c;
-    sn[iter - 1] = s;
-    col[iter - 1] = c * hd + s * hk;
-    col[iter] = 0.0;
-    beta[iter] = -s * beta[iter - 1];
-    beta[iter - 1] = c * beta[iter - 1];
-    const double resid = fabs(beta[iter]) / ctl->norm_ref;
-    ctl->resid = resid;
-    if (!(resid > ctl->tol) || iter >= ctl->max_iter)  // converged, at the cap, or NaN
-        ctl->done = 1;
-    else
-        ctl->k = iter + 1;
-}
-
-
-// ---------------------------------------------------------------------------
-// Fused form of the device-controlled Arnoldi step: the same arithmetic as
-// the gk_* kernels above in seven dependent launches instead of sixteen.
-//   F1 (CTA per swimmer)  z = P^-1 q_{k-1}; records of z for the blob-blob
-//                          apply; body rows of w = -K^T z
+// Device-controlled Arnoldi step (apply_preconditioner, system_matrix_mult,
+// CGS2 orthogonalisation, Givens: mobility_solver.cpp:1162-1230).  The
+// iteration count and the convergence flag live in a GmresCtl block on the
+// device, so a step needs no host round trip and is replayed from a CUDA
+// graph; once converged, every kernel of a replayed step returns at once.
+//
+// FP64 throughput per SM is low on this GPU, so every kernel spreads its
+// rows over many CTAs and avoids FP64 shuffle trees.  Sums across CTAs (body
+// moments, CGS projections, the norm) are finished by the last CTA to arrive
+// (an atomic ticket; nobody waits), in a fixed order, so results are
+// deterministic.  Projections use two levels: the last CTA of each group of
+// kSGroup CTAs sums the group, the last group finisher sums the groups.
+//   S1 (CTA per 128 blobs)  q_{k-1} = w / ||w|| into Q; body moments;
+//                            last CTA: body rows of q and z_body = U
+//   S2 (CTA per 128 blobs)  z_blob; records of z; last CTA: w_body = -K^T z
 //   pair kernel (+ split reduction) on the records -> mbb
-//   F3 (row chunks)       blob rows of w = M_bb z - K z_body; first CGS pass
-//                          partial dots Q^T w                   -> P1
-//   F4 (row chunks)       h1 = sum P1; w -= Q h1; second pass dots -> P2
-//   F5 (row chunks)       h2 = sum P2; H += h2; w -= Q h2; ||w||^2 partials -> P1
-//   F6 (row chunks)       q_k = w / ||w||; H(k, k-1) = ||w||
-//   Givens step           (gk_givens_kernel)
-// Each row-chunk kernel owns kFRows rows; its dots use one warp-shuffle
-// reduction per column and a single block barrier.
+//   S3 (CTA per kSRows rows) w_blob = M_bb z - K z_body; Q^T w; last: h, H col
+//   S4 (CTA per kSRows rows) w -= Q h; Q^T w; last: h, H col +=
+//   S5 (CTA per kSRows rows) w -= Q h; ||w||^2; last: H(k, k-1), Givens, ctl
 // ---------------------------------------------------------------------------
-constexpr int kFTpb = 256;
-constexpr int kFPer = 1;                 // rows per thread
-constexpr int kFRows = kFTpb * kFPer;    // rows per block
-constexpr int kFMaxK = 160;              // >= max_iter + 1
+constexpr int kSBlobs = 128;  // blobs (threads) per CTA in S1, S2
+constexpr int kSRows = 32;    // rows per CTA in S3-S5
+constexpr int kSTpb = 128;    // threads per CTA in S3-S5
+constexpr int kSGroup = 16;   // CTAs per first-level group of the projection sums
+constexpr int kFMaxK = 160;   // >= max_iter + 1
+// layout of the step's scalar workspace (doubles)
+constexpr int kHOff = 0;             // h[kFMaxK]: the last projections
+constexpr int kNormOff = kFMaxK;     // ||w|| of the last step (or beta0 before the first)
+constexpr int kStepScalars = kFMaxK + 8;
 
 __device__ __forceinline__ void pack_record(void *rec, int i, const double *x, const double *f, int f64)
 {
@@ -646,54 +429,116 @@ __device__ __forceinline__ void pack_record(void *rec, int i, const double *x, c
     }
 }
 
-// F1: one CTA per swimmer.
-__global__ void __launch_bounds__(kRedTpb) f1_precond_kernel(int W, int nblob, const double *__restrict__ Q, size_t ld,
-                                                             const double *__restrict__ R, const double *__restrict__ refs,
-                                                             const double *__restrict__ ktk_rot,
-                                                             const double *__restrict__ mob_rot, double minv,
-                                                             const double *__restrict__ xb, double *__restrict__ z,
-                                                             double *__restrict__ w, void *rec, int f64,
-                                                             const GmresCtl *ctl)
+// True in every thread of the CTA that arrives last (of `total`) at *ticket;
+// that CTA re-arms the ticket for the next launch.  Partials written before
+// the call are visible to the last CTA through L2 (__ldcg).
+__device__ __forceinline__ bool last_cta(int *ticket, int total)
+{
+    __shared__ int is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int t = atomicAdd(ticket, 1);
+        is_last = (t == total - 1);
+        if (is_last) *ticket = 0;
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+
+// Block sum of 6 per-thread values, in a fixed order; thread 0 writes them to out[0..6).
+template <int TPB> __device__ __forceinline__ void block_sum6(const double *v, double *out)
+{
+    __shared__ double red[6][TPB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const double t = warp_sum(v[c]);
+        if (lane == 0) red[c][wid] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double t = 0.0;
+        for (int w = 0; w < TPB / 32; ++w) t += red[threadIdx.x][w];
+        out[threadIdx.x] = t;
+    }
+}
+
+// Sum over the gx per-CTA 6-vectors of each swimmer (part[(n*gx + x)*6 + c]).
+__device__ __forceinline__ void swimmer_sums(const double *part, int n, int gx, double *sums)
+{
+    for (int c = 0; c < 6; ++c) sums[c] = 0.0;
+    for (int x = 0; x < gx; ++x)
+        for (int c = 0; c < 6; ++c) sums[c] += __ldcg(part + ((size_t)n * gx + x) * 6 + c);
+}
+
+// S1: grid (ceil(nblob/kSBlobs), W).
+__global__ void __launch_bounds__(kSBlobs) s1_normalise_moments_kernel(
+    int W, int nblob, double *__restrict__ Q, size_t ld, const double *__restrict__ w,
+    const double *__restrict__ R, const double *__restrict__ refs, const double *__restrict__ ktk_rot,
+    const double *__restrict__ mob_rot, double *__restrict__ z, double *__restrict__ part,
+    const double *__restrict__ scal, int *ticket, const GmresCtl *ctl)
 {
     if (ctl->done) return;
-    __shared__ double red[32];
-    __shared__ double U[6];
-    const int n = blockIdx.x, nb = W * nblob;
-    const double *in = Q + ld * (size_t)(ctl->k - 1);
-    const double *Rn = R + 9 * n;
+    const int n = blockIdx.y, m = blockIdx.x * kSBlobs + threadIdx.x, nb = W * nblob;
+    double *q = Q + ld * (size_t)(ctl->k - 1);
+    const double nrm = scal[kNormOff];
     double a[6] = {0, 0, 0, 0, 0, 0};
-    for (int m = threadIdx.x; m < nblob; m += kRedTpb) {
-        const double *fm = in + 3 * ((size_t)n * nblob + m);
+    if (m < nblob) {
+        const size_t i = (size_t)n * nblob + m;
+        double f[3];
+        for (int c = 0; c < 3; ++c) {
+            f[c] = w[3 * i + c] / nrm;
+            q[3 * i + c] = f[c];
+        }
         double d[3];
-        rot_apply(Rn, refs + 3 * m, d);
-        a[0] += fm[0];
-        a[1] += fm[1];
-        a[2] += fm[2];
-        a[3] += d[1] * fm[2] - d[2] * fm[1];
-        a[4] += d[2] * fm[0] - d[0] * fm[2];
-        a[5] += d[0] * fm[1] - d[1] * fm[0];
+        rot_apply(R + 9 * n, refs + 3 * m, d);
+        a[0] = f[0];
+        a[1] = f[1];
+        a[2] = f[2];
+        a[3] = d[1] * f[2] - d[2] * f[1];
+        a[4] = d[2] * f[0] - d[0] * f[2];
+        a[5] = d[0] * f[1] - d[1] * f[0];
     }
-    double sums[6];
-    for (int c = 0; c < 6; ++c) sums[c] = block_sum<kRedTpb>(a[c], red);
-    if (threadIdx.x == 0) {
-        const double *in_body = in + 3 * nb + 6 * n;
-        const double *Kt = ktk_rot + 36 * n, *Mb = mob_rot + 36 * n;
+    block_sum6<kSBlobs>(a, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
+    if (!last_cta(ticket, gridDim.x * gridDim.y)) return;
+    for (int s = threadIdx.x; s < W; s += kSBlobs) {
+        double sums[6], qb[6];
+        swimmer_sums(part, s, gridDim.x, sums);
+        for (int c = 0; c < 6; ++c) {
+            qb[c] = w[3 * nb + 6 * s + c] / nrm;
+            q[3 * nb + 6 * s + c] = qb[c];
+        }
+        const double *Kt = ktk_rot + 36 * s, *Mb = mob_rot + 36 * s;
         for (int i = 0; i < 6; ++i) {
             double x = 0.0, y = 0.0;
             for (int j = 0; j < 6; ++j) {
                 x += Kt[i + 6 * j] * (-sums[j]);
-                y += Mb[i + 6 * j] * in_body[j];
+                y += Mb[i + 6 * j] * qb[j];
             }
-            U[i] = x - y;
-            z[3 * nb + 6 * n + i] = x - y;
+            z[3 * nb + 6 * s + i] = x - y;
         }
     }
-    __syncthreads();
+}
+
+// S2: grid (ceil(nblob/kSBlobs), W).  The blob block of the preconditioner
+// is applied W - n times for swimmer n, as the reference's loop does
+// (mobility_solver.cpp:651-721).
+__global__ void __launch_bounds__(kSBlobs) s2_precond_blobs_kernel(
+    int W, int nblob, const double *__restrict__ Q, size_t ld, const double *__restrict__ R,
+    const double *__restrict__ refs, double minv, const double *__restrict__ xb, double *__restrict__ z,
+    double *__restrict__ w, void *rec, int f64, double *__restrict__ part, int *ticket, const GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    const int n = blockIdx.y, m = blockIdx.x * kSBlobs + threadIdx.x, nb = W * nblob;
+    const double *in = Q + ld * (size_t)(ctl->k - 1);
+    const double *U = z + 3 * nb + 6 * n;
     double b[6] = {0, 0, 0, 0, 0, 0};
-    for (int m = threadIdx.x; m < nblob; m += kRedTpb) {
-        const int i = n * nblob + m;
+    if (m < nblob) {
+        const size_t i = (size_t)n * nblob + m;
         double d[3];
-        rot_apply(Rn, refs + 3 * m, d);
+        rot_apply(R + 9 * n, refs + 3 * m, d);
         double o[3] = {in[3 * i] + U[0], in[3 * i + 1] + U[1], in[3 * i + 2] + U[2]};
         o[0] += U[4] * d[2] - U[5] * d[1];
         o[1] += U[5] * d[0] - U[3] * d[2];
@@ -706,55 +551,71 @@ __global__ void __launch_bounds__(kRedTpb) f1_precond_kernel(int W, int nblob, c
         z[3 * i] = o[0];
         z[3 * i + 1] = o[1];
         z[3 * i + 2] = o[2];
-        pack_record(rec, i, xb + 3 * (size_t)i, o, f64);
-        b[0] += o[0];
-        b[1] += o[1];
-        b[2] += o[2];
-        b[3] += d[1] * o[2] - d[2] * o[1];
-        b[4] += d[2] * o[0] - d[0] * o[2];
-        b[5] += d[0] * o[1] - d[1] * o[0];
+        pack_record(rec, (int)i, xb + 3 * i, o, f64);
+        b[0] = o[0];
+        b[1] = o[1];
+        b[2] = o[2];
+        b[3] = d[1] * o[2] - d[2] * o[1];
+        b[4] = d[2] * o[0] - d[0] * o[2];
+        b[5] = d[0] * o[1] - d[1] * o[0];
     }
-    for (int c = 0; c < 6; ++c) {
-        const double v = block_sum<kRedTpb>(b[c], red);
-        if (threadIdx.x == 0) w[3 * nb + 6 * n + c] = -v;
+    block_sum6<kSBlobs>(b, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
+    if (!last_cta(ticket, gridDim.x * gridDim.y)) return;
+    for (int s = threadIdx.x; s < W; s += kSBlobs) {
+        double sums[6];
+        swimmer_sums(part, s, gridDim.x, sums);
+        for (int c = 0; c < 6; ++c) w[3 * nb + 6 * s + c] = -sums[c];
     }
 }
 
-// Partial dots of this block's rows (wr[] of every thread) against Q[:, 0..k):
-// the rows go to shared memory, then each warp reduces whole columns.
-__device__ __forceinline__ void f_block_dots(const double *__restrict__ Q, size_t ld, int n, int row0, int k,
-                                             const double *wr, double *ws, double *__restrict__ out, int nchunks)
+// Projections of this CTA's rows (ws, kSRows of them) on Q[:, 0..k): one
+// column per thread, summed over the rows in order.  P[i*nblk + blk].
+__device__ __forceinline__ void cta_projections(const double *__restrict__ Q, size_t ld, int row0, int rows, int k,
+                                                const double *ws, double *__restrict__ P, int nblk)
 {
-#pragma unroll
-    for (int j = 0; j < kFPer; ++j) ws[threadIdx.x + j * kFTpb] = wr[j];
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int rows = min(kFRows, n - row0);
-    for (int i = wid; i < k; i += kFTpb / 32) {
+    for (int i = threadIdx.x; i < k; i += kSTpb) {
         const double *q = Q + ld * i + row0;
         double a = 0.0;
-        for (int rr = lane; rr < rows; rr += 32) a += q[rr] * ws[rr];
-        a = warp_sum(a);
-        if (lane == 0) out[(size_t)i * nchunks + blockIdx.x] = a;
+        for (int r = 0; r < rows; ++r) a += q[r] * ws[r];
+        P[(size_t)i * nblk + blockIdx.x] = a;
     }
 }
 
-// F3: blob rows of w, first-pass dots.
-__global__ void __launch_bounds__(kFTpb) f3_finish_dots_kernel(int W, int nblob, const double *__restrict__ mbb,
-                                                               const double *__restrict__ z,
-                                                               const double *__restrict__ R,
-                                                               const double *__restrict__ refs, double *__restrict__ w,
-                                                               const double *__restrict__ Q, size_t ld, int n,
-                                                               int nchunks, double *__restrict__ P1,
-                                                               const GmresCtl *ctl)
+// Two-level sum of the per-CTA projections into h[0..k); true in the CTA
+// that finished it.  tickets[0] is the top level, tickets[1 + g] group g's.
+__device__ __forceinline__ bool finish_projections(const double *P, int k, int nblk, double *G, int *tickets,
+                                                   double *h)
+{
+    const int ngroups = (nblk + kSGroup - 1) / kSGroup, g = blockIdx.x / kSGroup;
+    const int first = g * kSGroup, gsize = min(kSGroup, nblk - first);
+    if (!last_cta(tickets + 1 + g, gsize)) return false;
+    for (int i = threadIdx.x; i < k; i += kSTpb) {
+        double t = 0.0;
+        for (int b = 0; b < gsize; ++b) t += __ldcg(P + (size_t)i * nblk + first + b);
+        G[(size_t)i * ngroups + g] = t;
+    }
+    if (!last_cta(tickets, ngroups)) return false;
+    for (int i = threadIdx.x; i < k; i += kSTpb) {
+        double t = 0.0;
+        for (int b = 0; b < ngroups; ++b) t += __ldcg(G + (size_t)i * ngroups + b);
+        h[i] = t;
+    }
+    return true;
+}
+
+// S3: blob rows of w, first CGS pass.
+__global__ void __launch_bounds__(kSTpb) s3_finish_project_kernel(
+    int W, int nblob, const double *__restrict__ mbb, const double *__restrict__ z, const double *__restrict__ R,
+    const double *__restrict__ refs, double *__restrict__ w, const double *__restrict__ Q, size_t ld, int n,
+    double *__restrict__ P, double *__restrict__ G, int *tickets, double *__restrict__ scal,
+    double *__restrict__ H, int ldh, const GmresCtl *ctl)
 {
     if (ctl->done) return;
-    __shared__ double ws[kFRows];
-    const int k = ctl->k, row0 = blockIdx.x * kFRows, nb3 = 3 * W * nblob;
-    double wr[kFPer];
-#pragma unroll
-    for (int j = 0; j < kFPer; ++j) {
-        const int r = row0 + threadIdx.x + j * kFTpb;
+    __shared__ double ws[kSRows];
+    const int k = ctl->k, row0 = blockIdx.x * kSRows, nb3 = 3 * W * nblob;
+    const int rows = min(kSRows, n - row0);
+    if (threadIdx.x < kSRows) {
+        const int r = row0 + threadIdx.x;
         double v = 0.0;
         if (r < nb3) {
             const int i = r / 3, c = r % 3, sw = i / nblob, m = i % nblob;
@@ -770,79 +631,126 @@ __global__ void __launch_bounds__(kFTpb) f3_finish_dots_kernel(int W, int nblob,
         } else if (r < n) {
             v = w[r];
         }
-        wr[j] = v;
-    }
-    f_block_dots(Q, ld, n, row0, k, wr, ws, P1, nchunks);
-}
-
-// F4 / F5: h = sum of the partials; H column gets h (pass 0: store, pass 1:
-// add); w -= Q h; then either the next pass's dots (Pout, pass 0) or the
-// partial squared norm of w (Pout[block], pass 1).
-__global__ void __launch_bounds__(kFTpb) f45_update_kernel(const double *__restrict__ Q, size_t ld, int n,
-                                                           int nchunks, const double *__restrict__ Pin,
-                                                           double *__restrict__ Pout, double *__restrict__ w,
-                                                           double *__restrict__ H, int ldh, const GmresCtl *ctl,
-                                                           int pass)
-{
-    if (ctl->done) return;
-    __shared__ double ws[kFRows];
-    __shared__ double h[kFMaxK];
-    const int k = ctl->k, row0 = blockIdx.x * kFRows;
-    for (int i = threadIdx.x; i < k; i += kFTpb) {
-        double t = 0.0;
-        for (int c = 0; c < nchunks; ++c) t += Pin[(size_t)i * nchunks + c];
-        h[i] = t;
+        ws[threadIdx.x] = v;
     }
     __syncthreads();
-    if (blockIdx.x == 0) {
-        double *Hcol = H + (size_t)ldh * (k - 1);
-        for (int i = threadIdx.x; i < k; i += kFTpb) Hcol[i] = pass == 0 ? h[i] : Hcol[i] + h[i];
-    }
-    double wr[kFPer];
-#pragma unroll
-    for (int j = 0; j < kFPer; ++j) {
-        const int r = row0 + threadIdx.x + j * kFTpb;
+    cta_projections(Q, ld, row0, rows, k, ws, P, gridDim.x);
+    double *h = scal + kHOff;
+    if (!finish_projections(P, k, gridDim.x, G, tickets, h)) return;
+    double *Hcol = H + (size_t)ldh * (k - 1);
+    for (int i = threadIdx.x; i < k; i += kSTpb) Hcol[i] = h[i];
+}
+
+// w -= Q h on this CTA's rows (rows go to ws).
+__device__ __forceinline__ void cta_update(const double *__restrict__ Q, size_t ld, int row0, int rows, int k,
+                                           const double *__restrict__ h, double *__restrict__ w, double *ws)
+{
+    __shared__ double hs[kFMaxK];
+    for (int i = threadIdx.x; i < k; i += kSTpb) hs[i] = h[i];
+    __syncthreads();
+    if (threadIdx.x < kSRows) {
         double v = 0.0;
-        if (r < n) {
+        if (threadIdx.x < rows) {
+            const int r = row0 + threadIdx.x;
             v = w[r];
-            for (int i = 0; i < k; ++i) v -= h[i] * Q[ld * i + r];
+            for (int i = 0; i < k; ++i) v -= hs[i] * Q[ld * i + r];
             w[r] = v;
         }
-        wr[j] = v;
-    }
-    if (pass == 0) {
-        f_block_dots(Q, ld, n, row0, k, wr, ws, Pout, nchunks);
-    } else {
-        double a = 0.0;
-#pragma unroll
-        for (int j = 0; j < kFPer; ++j) a += wr[j] * wr[j];
-        __shared__ double red[32];
-        const double t = block_sum<kFTpb>(a, red);
-        if (threadIdx.x == 0) Pout[blockIdx.x] = t;
-    }
-}
-
-// F6: q_k = w / ||w||, H(k, k-1) = ||w||.
-__global__ void __launch_bounds__(kFTpb) f6_normalize_kernel(const double *__restrict__ w, int n, int nchunks,
-                                                             const double *__restrict__ P, double *__restrict__ Q,
-                                                             size_t ld, double *__restrict__ H, int ldh,
-                                                             const GmresCtl *ctl)
-{
-    if (ctl->done) return;
-    __shared__ double nrm;
-    const int k = ctl->k;
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int c = 0; c < nchunks; ++c) t += P[c];
-        nrm = sqrt(t);
-        if (blockIdx.x == 0) H[(size_t)ldh * (k - 1) + k] = nrm;
+        ws[threadIdx.x] = v;
     }
     __syncthreads();
-    const int row0 = blockIdx.x * kFRows;
-#pragma unroll
-    for (int j = 0; j < kFPer; ++j) {
-        const int r = row0 + threadIdx.x + j * kFTpb;
-        if (r < n) Q[ld * k + r] = nrm > 0.0 ? w[r] / nrm : 0.0;
+}
+
+// S4: second CGS pass.
+__global__ void __launch_bounds__(kSTpb) s4_update_project_kernel(const double *__restrict__ Q, size_t ld, int n,
+                                                                  double *__restrict__ w, double *__restrict__ P,
+                                                                  double *__restrict__ G, int *tickets,
+                                                                  double *__restrict__ scal, double *__restrict__ H,
+                                                                  int ldh, const GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    __shared__ double ws[kSRows];
+    const int k = ctl->k, row0 = blockIdx.x * kSRows, rows = min(kSRows, n - row0);
+    double *h = scal + kHOff;
+    cta_update(Q, ld, row0, rows, k, h, w, ws);
+    cta_projections(Q, ld, row0, rows, k, ws, P, gridDim.x);
+    // h is overwritten only after every CTA has read it (all arrived)
+    if (!finish_projections(P, k, gridDim.x, G, tickets, h)) return;
+    double *Hcol = H + (size_t)ldh * (k - 1);
+    for (int i = threadIdx.x; i < k; i += kSTpb) Hcol[i] += h[i];
+}
+
+// S5: w -= Q h; ||w||; H(k, k-1) = ||w||; Givens rotation; iteration control.
+__global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
+    const double *__restrict__ Q, size_t ld, int n, double *__restrict__ w, double *__restrict__ P, int *ticket,
+    double *__restrict__ scal, double *__restrict__ H, int ldh, double *__restrict__ beta, double *__restrict__ cs,
+    double *__restrict__ sn, GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    __shared__ double ws[kSRows];
+    const int k = ctl->k, row0 = blockIdx.x * kSRows, rows = min(kSRows, n - row0);
+    cta_update(Q, ld, row0, rows, k, scal + kHOff, w, ws);
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        for (int r = 0; r < rows; ++r) a += ws[r] * ws[r];
+        P[blockIdx.x] = a;
+    }
+    if (!last_cta(ticket, gridDim.x)) return;
+    if (threadIdx.x != 0) return;
+    double t = 0.0;
+    for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(P + b);
+    const double nrm = sqrt(t);
+    scal[kNormOff] = nrm;
+    const int iter = k;
+    double *col = H + (size_t)ldh * (iter - 1);
+    col[iter] = nrm;
+    for (int i = 1; i < iter; ++i) {
+        const double u = cs[i - 1] * col[i - 1] + sn[i - 1] * col[i];
+        col[i] = cs[i - 1] * col[i] - sn[i - 1] * col[i - 1];
+        col[i - 1] = u;
+    }
+    const double hk = col[iter], hd = col[iter - 1];
+    double c, s;
+    if (hk == 0.0) {
+        c = 1.0;
+        s = 0.0;
+    } else if (fabs(hk) > fabs(hd)) {
+        const double u = hd / hk;
+        s = (2.0 * (double)(hk > 0) - 1.0) / sqrt(1.0 + u * u);
+        c = u * s;
+    } else {
+        const double u = hk / hd;
+        c = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + u * u);
+        s = u * c;
+    }
+    cs[iter - 1] = c;
+    sn[iter - 1] = s;
+    col[iter - 1] = c * hd + s * hk;
+    col[iter] = 0.0;
+    beta[iter] = -s * beta[iter - 1];
+    beta[iter - 1] = c * beta[iter - 1];
+    const double resid = fabs(beta[iter]) / ctl->norm_ref;
+    ctl->resid = resid;
+    if (!(resid > ctl->tol) || iter >= ctl->max_iter)  // converged, at the cap, or NaN
+        ctl->done = 1;
+    else
+        ctl->k = iter + 1;
+}
+
+// Back substitution y = H(0:iter, 0:iter)^-1 beta(0:iter)
+// (mobility_solver.cpp:1236-1250) by one warp: column by column, the lanes
+// update the remaining right-hand side, each row in the reference's order.
+__global__ void backsolve_warp_kernel(const double *__restrict__ H, int ldh, const double *__restrict__ beta,
+                                      int iter, double *__restrict__ y)
+{
+    __shared__ double b[kFMaxK];
+    for (int i = threadIdx.x; i < iter; i += 32) b[i] = beta[i];
+    __syncwarp();
+    for (int j = iter - 1; j >= 0; --j) {
+        const double yj = b[j] / H[j + (size_t)ldh * j];
+        for (int i = threadIdx.x; i < j; i += 32) b[i] -= H[i + (size_t)ldh * j] * yj;
+        if (threadIdx.x == 0) y[j] = yj;
+        __syncwarp();
     }
 }
 
@@ -965,26 +873,48 @@ static gmi_status orthonormalise(gmi_solver *s, double *w, int k, double *Hcol)
     return launched(s, 2);
 }
 
-// One device-controlled Arnoldi step (apply_preconditioner, system_matrix_mult,
-// CGS2, normalisation, Givens) enqueued on the solver stream; captured once
-// per precision into s->graph[pidx].
+// Sizes of the Arnoldi step's workspace inside s->partial and s->st_tickets.
+struct StepLayout {
+    int gx, nblk, ngroups;
+    size_t doubles, tickets;
+};
+
+static StepLayout step_layout(int n, int nblob, int W)
+{
+    StepLayout L;
+    L.gx = (nblob + kSBlobs - 1) / kSBlobs;
+    L.nblk = (n + kSRows - 1) / kSRows;
+    L.ngroups = (L.nblk + kSGroup - 1) / kSGroup;
+    L.doubles = (size_t)kFMaxK * (L.nblk + L.ngroups) + (size_t)W * L.gx * 6;
+    L.tickets = 5 + 2 * (size_t)L.ngroups;
+    return L;
+}
+
+// One device-controlled Arnoldi step (S1, S2, the blob-blob pair apply, S3,
+// S4, S5) enqueued on the solver stream; captured once per precision into
+// s->graph[pidx].
 static gmi_status enqueue_arnoldi_step(gmi_solver *s)
 {
     gmi_context *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
     const int nb = s->B, n = s->n, W = s->W, nblob = s->cfg.nblob, ldh = s->m + 1;
-    const int nc = (n + kFRows - 1) / kFRows;
     const size_t ld = (size_t)n;
     const bool f64 = ctx->precision == GMI_FP64;
     const double minv = 6.0 * kPi * s->cfg.mu * s->cfg.rblob;
-    if (2 * (size_t)nc * (s->m + 1) > s->partial_count || s->m + 1 > kFMaxK) {
-        set_last_error("partial-sum buffer smaller than the Arnoldi step needs", "enqueue_arnoldi_step", __FILE__,
+    const StepLayout L = step_layout(n, nblob, W);
+    if (L.doubles > s->partial_count || L.tickets > s->st_ticket_count || s->m + 1 > kFMaxK || L.gx == 0 || W == 0) {
+        set_last_error("Arnoldi step workspace smaller than the step needs", "enqueue_arnoldi_step", __FILE__,
                        __LINE__);
         return GMI_ERR_STATE;
     }
-    double *P1 = s->partial, *P2 = s->partial + (size_t)nc * (s->m + 1);
-    f1_precond_kernel<<<W, kRedTpb, 0, st>>>(W, nblob, s->Q, ld, s->R, s->refs, s->ktk_rot, s->mob_rot, minv,
-                                             s->x_blobs, s->z, s->w, s->gm_rec, f64 ? 1 : 0, s->ctl);
+    double *P = s->partial, *G = P + (size_t)kFMaxK * L.nblk, *part = G + (size_t)kFMaxK * L.ngroups;
+    int *tk = s->st_tickets;
+    int *tk3 = tk + 2, *tk4 = tk3 + 1 + L.ngroups, *tk5 = tk4 + 1 + L.ngroups;
+    const dim3 bgrid(L.gx, W);
+    s1_normalise_moments_kernel<<<bgrid, kSBlobs, 0, st>>>(W, nblob, s->Q, ld, s->w, s->R, s->refs, s->ktk_rot,
+                                                          s->mob_rot, s->z, part, s->st_scal, tk, s->ctl);
+    s2_precond_blobs_kernel<<<bgrid, kSBlobs, 0, st>>>(W, nblob, s->Q, ld, s->R, s->refs, minv, s->x_blobs, s->z,
+                                                      s->w, s->gm_rec, f64 ? 1 : 0, part, tk + 1, s->ctl);
     GMI_CUDA_TRY(cudaGetLastError());
     ExplicitPairEnv env{};
     env.stream = st;
@@ -1000,12 +930,11 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s)
     PairConsts k;
     fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
     GMI_TRY(launch_pair_into(env, kBB, f64, s->gm_rec, 0, nb, s->gm_rec, nb, k, s->mbb, 0));
-    f3_finish_dots_kernel<<<nc, kFTpb, 0, st>>>(W, nblob, s->mbb, s->z, s->R, s->refs, s->w, s->Q, ld, n, nc, P1,
-                                                s->ctl);
-    f45_update_kernel<<<nc, kFTpb, 0, st>>>(s->Q, ld, n, nc, P1, P2, s->w, s->H, ldh, s->ctl, 0);
-    f45_update_kernel<<<nc, kFTpb, 0, st>>>(s->Q, ld, n, nc, P2, P1, s->w, s->H, ldh, s->ctl, 1);
-    f6_normalize_kernel<<<nc, kFTpb, 0, st>>>(s->w, n, nc, P1, s->Q, ld, s->H, ldh, s->ctl);
-    gk_givens_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, s->cs, s->sn, s->ctl);
+    s3_finish_project_kernel<<<L.nblk, kSTpb, 0, st>>>(W, nblob, s->mbb, s->z, s->R, s->refs, s->w, s->Q, ld, n, P,
+                                                       G, tk3, s->st_scal, s->H, ldh, s->ctl);
+    s4_update_project_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, G, tk4, s->st_scal, s->H, ldh, s->ctl);
+    s5_update_norm_givens_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, tk5, s->st_scal, s->H, ldh,
+                                                           s->beta, s->cs, s->sn, s->ctl);
     GMI_CUDA_TRY(cudaGetLastError());
     return GMI_OK;
 }
@@ -1070,15 +999,14 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
     }
     s->h_stage[0] = beta0;
     GMI_CUDA_TRY(cudaMemcpyAsync(s->beta, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
-    GMI_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
-    scale_kernel<<<grid_for(n), 256, 0, st>>>(n, s->w, s->scal, s->Q);
-    GMI_TRY(launched(s));
     const int max_iter = n < s->m ? n : s->m;
     const int ldh = s->m + 1;
     const int pidx = s->ctx->precision == GMI_FP64 ? 0 : 1;
     size_t nodes = 0;
     if (s->use_graphs && ensure_arnoldi_graph(s, pidx, &nodes) != GMI_OK) s->use_graphs = false;
     if (s->use_graphs) {
+        // the first step normalises w = r0 by beta0 into Q[:, 0]
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->st_scal + kNormOff, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
         GmresCtl c{};
         c.k = 1;
         c.done = 0;
@@ -1106,8 +1034,8 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
             return GMI_ERR_NONFINITE;
         }
         const int iter = s->h_ctl->k;
-        backsolve_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
-        combine_kernel<<<grid_for(n), 256, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
+        backsolve_warp_kernel<<<1, 32, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
+        combine_kernel<<<grid_for(n, 64), 64, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
         GMI_TRY(launched(s, 2));
         GMI_TRY(apply_preconditioner(s, s->tmp, s->z));
         axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->soln, 1.0, s->z, s->soln);
@@ -1115,6 +1043,9 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
         *iters_out = iter;
         return GMI_OK;
     }
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
+    scale_kernel<<<grid_for(n), 256, 0, st>>>(n, s->w, s->scal, s->Q);
+    GMI_TRY(launched(s));
     for (int iter = 1; iter <= max_iter; ++iter) {
         GMI_TRY(apply_preconditioner(s, s->Q + ld * (iter - 1), s->z));
         GMI_TRY(system_matrix_mult(s, s->z, s->w));
@@ -1129,8 +1060,8 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
             return GMI_ERR_NONFINITE;
         }
         if (resid <= tol || iter == max_iter) {
-            backsolve_kernel<<<1, 1, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
-            combine_kernel<<<grid_for(n), 256, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
+            backsolve_warp_kernel<<<1, 32, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
+            combine_kernel<<<grid_for(n, 64), 64, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
             GMI_TRY(launched(s, 2));
             GMI_TRY(apply_preconditioner(s, s->tmp, s->z));
             axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->soln, 1.0, s->z, s->soln);
@@ -1495,11 +1426,16 @@ gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
         TRY_OR_DIE(dalloc(s, &s->b64, n));
         TRY_OR_DIE(dalloc(s, &s->xacc, n));
         TRY_OR_DIE(dalloc(s, &s->mbb, 3 * B));
-        // Two partial arrays of (m + 1) columns, each long enough for either
-        // row chunking (kChunkRows for the host loop, kFRows for the graph).
-        const size_t pch = std::max<size_t>((size_t)nchunks_of((int)n) + n / 1024 + 1, (n + kFRows - 1) / kFRows);
-        s->partial_count = 2 * pch * (m + 1);
+        // partial serves the host loop's dot partials (two arrays of m + 1
+        // columns over kChunkRows chunks) and the graph step's workspace.
+        const StepLayout L = step_layout((int)n, cfg->nblob, (int)W);
+        s->partial_count = std::max<size_t>(2 * ((size_t)nchunks_of((int)n) + n / 1024 + 1) * (m + 1), L.doubles);
         TRY_OR_DIE(dalloc(s, &s->partial, s->partial_count));
+        TRY_OR_DIE(dalloc(s, &s->st_scal, kStepScalars));
+        double *tk_mem = nullptr;
+        s->st_ticket_count = L.tickets;
+        TRY_OR_DIE(dalloc(s, &tk_mem, (L.tickets + 1) / 2));
+        s->st_tickets = reinterpret_cast<int *>(tk_mem);
         double *ctl_mem = nullptr, *rec_mem = nullptr, *part_mem = nullptr;
         TRY_OR_DIE(dalloc(s, &ctl_mem, 8));
         s->ctl = reinterpret_cast<GmresCtl *>(ctl_mem);

@@ -30,6 +30,9 @@ struct gmi_solver {
     struct GmresCtl *h_ctl = nullptr; // pinned mirror
     void *gm_rec = nullptr;           // blob records of the GMRES operator (own buffer: fixed address)
     size_t partial_count = 0;         // doubles in partial
+    double *st_scal = nullptr;        // Arnoldi step scalars: projections h, ||w||
+    int *st_tickets = nullptr;        // Arnoldi step arrival tickets (zero between launches)
+    size_t st_ticket_count = 0;
     double *gm_partial = nullptr;     // split partial sums of the GMRES operator
     size_t gm_partial_bytes = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one Arnoldi step, per precision
