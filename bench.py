@@ -17,6 +17,11 @@ self pair included.  One step = one full apply.  Default N = 131072.
              this GPU by gmi_measure_fma_peak
   cpu_baseline the FP64 CPU oracle (rpy_oracle.c) on a bounded target slice,
              all host cores
+  time_steps time-steps/sec of the whole implicit time step (gmi_sim_step:
+             Broyden, GMRES, every pair sum) on seeded free swimmers
+             (1 sphere of 642 blobs with 16 x 20 segments; 1 sphere of 4096
+             blobs with 640 x 20 segments), plain FP64 against FP32C pair
+             sums with FP64 solves, with the velocity error between the two
 
 Runs one replica per GPU under torchrun (the apply does not shard here:
 "replicas only"), max-over-ranks time, rank 0 prints one JSON line.
@@ -53,6 +58,10 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 side measurement")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU sample")
     p.add_argument("--no-autotune", action="store_true", help="use the default launch shape (profiling)")
+    p.add_argument("--ts-workloads", default="config1,config3",
+                   help="time-step workloads (comma separated; empty to skip)")
+    p.add_argument("--ts-steps", default="config1:100,config3:10", help="timed steps per workload")
+    p.add_argument("--ts-warmup", type=int, default=5, help="untimed steps before the timed ones")
     return p.parse_args()
 
 
@@ -199,6 +208,57 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_time_steps(args, dev):
+    """time-steps/sec of the device time step (gmi_sim_step) on the seeded
+    swimmer workloads, plain FP64 against FP32C pair sums with FP64 solves,
+    from the same initial state: Broyden tolerance 1e-4, GMRES 1e-8."""
+    import torch
+    from generic_mobility_interface_class_gb300 import workloads
+    from generic_mobility_interface_class_gb300.sim import Simulation
+    from generic_mobility_interface_class_gb300._lib import GMI_FP32C, GMI_FP64
+    steps_for = dict(kv.split(":") for kv in args.ts_steps.split(",") if kv)
+    out = {}
+    for name in [w for w in args.ts_workloads.split(",") if w]:
+        desc, make = workloads.WORKLOADS[name]
+        kw = make()
+        nsteps = int(steps_for.get(name, 10))
+        runs, final = {}, {}
+        for label, prec in (("fp64", GMI_FP64), ("fp32c", GMI_FP32C)):
+            sim = Simulation(**kw, precision=prec, device=dev)
+            sim.prepare()
+            for nt in range(args.ts_warmup):
+                sim.step(nt)
+            torch.cuda.synchronize()
+            l0 = sim.launches
+            broyden, gmres = [], []
+            with ClockSampler(dev) as clocks:
+                t0 = time.perf_counter()
+                for nt in range(args.ts_warmup, args.ts_warmup + nsteps):
+                    b, g = sim.step(nt)
+                    broyden.append(b)
+                    gmres.append(g)
+                torch.cuda.synchronize()
+                wall = time.perf_counter() - t0
+            runs[label] = {"steps_per_s": nsteps / wall, "ms_per_step": 1e3 * wall / nsteps,
+                           "broyden_iters_per_step": sum(broyden) / nsteps, "gmres_iters_per_step": sum(gmres) / nsteps,
+                           "broyden_iters": broyden, "gpu_launches": sim.launches - l0, "clocks": clocks.summary()}
+            final[label] = {f: sim.state(f).ravel() for f in ("body_v", "seg_v", "seg_q", "body_x")}
+            sim.close()
+
+        def rel(f):
+            a, b = final["fp64"][f], final["fp32c"][f]
+            return float(np.linalg.norm(b - a) / max(np.linalg.norm(a), 1e-300))
+
+        out[name] = {"workload": desc, "timed_steps": nsteps, "warmup_steps": args.ts_warmup,
+                     "broyden_tol": kw["tol"], "gmres_tol": kw["linear_tol"], **runs,
+                     "speedup_fp32c_vs_fp64": runs["fp32c"]["steps_per_s"] / runs["fp64"]["steps_per_s"],
+                     "error_fp32c_vs_fp64_after_run": {"swimmer_velocity_rel": rel("body_v"),
+                                                       "segment_velocity_rel": rel("seg_v"),
+                                                       "segment_quaternion_rel": rel("seg_q"),
+                                                       "body_position_rel": rel("body_x")}}
+    return out
+
+
 def run_gmi(args, world, rank, local):
     import torch
     from generic_mobility_interface_class_gb300 import build as gbuild
@@ -301,6 +361,7 @@ def run_gmi(args, world, rank, local):
                 "peak_source": "measured FMA-loop probe on this GPU (gmi_measure_fma_peak)",
                 "flops_per_pair": FLOP_PER_PAIR_SS}
     ctx.close()
+    time_steps = run_time_steps(args, dev) if args.ts_workloads else {}
 
     line = None
     if rank == 0:
@@ -331,6 +392,7 @@ def run_gmi(args, world, rank, local):
             "clocks": clocks.summary(),
             "gpu_launches": gpu_launches,
             "wall_s_timed_region": wall,
+            "time_steps": time_steps,
         }
         line.update(extra)
         print(json.dumps(line), flush=True)

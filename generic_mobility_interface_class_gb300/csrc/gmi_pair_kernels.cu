@@ -15,6 +15,7 @@
 //      (hi, lo) two-sum accumulator, so the error does not grow with N.
 //   3. with more than one split, per-split partial sums (FP64) go to scratch
 //      and a reduce kernel adds them in split order into the output (= or +=).
+#include <algorithm>
 #include <cstdio>
 #include <vector>
 
@@ -330,7 +331,8 @@ __global__ void reduce_splits(const double *__restrict__ partial, int splits, in
 // queues its candidates (lane, j) in shared memory in screening order,
 // evaluates them 32 at a time, one per lane, and each lane then adds its own
 // entries in queue order, which is ascending j: the reference's summation
-// order per target.
+// order per target.  Sources are split over blockIdx.y (for occupancy); each
+// split sums in j order and the splits are added in order by barrier_reduce.
 // ---------------------------------------------------------------------------
 constexpr int kBarrierTpb = 64;
 constexpr int kBarrierWarps = kBarrierTpb / 32;
@@ -421,7 +423,8 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
     const int fil_i = gi / a.nseg;
     double g0 = 0, g1 = 0, g2 = 0;
     const double DL = 2.2 * a.rseg;
-    if (valid && is_seg_target && a.wall && zi < 0.5 * DL) {
+    const int j_begin = blockIdx.y * a.chunk, j_end = min(N, j_begin + a.chunk);
+    if (blockIdx.y == 0 && valid && is_seg_target && a.wall && zi < 0.5 * DL) {
         const double fz = fmin(1.0, 1.0 - (zi - a.rseg) / (0.5 * DL - a.rseg));
         g2 = a.scale * fz * fz * fz * fz;
     }
@@ -430,14 +433,14 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
     const float cut_s = (float)(1.1 * (a_tgt + a.rseg)) * 1.001f;
     const float cut_b = (float)(1.1 * (a_tgt + a.rblob)) * 1.001f;
     int count = 0;  // warp-uniform
-    for (int j0 = 0; j0 < N; j0 += kBarrierTpb) {
+    for (int j0 = j_begin; j0 < j_end; j0 += kBarrierTpb) {
         const int jl = j0 + threadIdx.x;
-        if (jl < N) {
+        if (jl < j_end) {
             tile[2 * threadIdx.x] = a.screen[2 * (size_t)jl];
             tile[2 * threadIdx.x + 1] = a.screen[2 * (size_t)jl + 1];
         }
         __syncthreads();
-        const int jn = min(kBarrierTpb, N - j0);
+        const int jn = min(kBarrierTpb, j_end - j0);
         for (int jj = 0; jj < jn; ++jj) {
             const int j = j0 + jj;
             const float4 s = tile[2 * jj], sl = tile[2 * jj + 1];
@@ -474,6 +477,14 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
     }
     if (count > 0) barrier_flush(a, q, count, xi, yi, zi, a_tgt, g0, g1, g2);
     if (!valid) return;
+    if (a.partial != nullptr) {
+        const int ntg = a.num_segs + (a.wall ? 0 : a.num_blobs);
+        double *p = a.partial + ((size_t)blockIdx.y * ntg + local) * 3;
+        p[0] = g0;
+        p[1] = g1;
+        p[2] = g2;
+        return;
+    }
     if (is_seg_target) {
         double *f = a.f_segs + 6 * (size_t)gi;
         f[0] += g0;
@@ -485,6 +496,22 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
         f[1] = g1;
         f[2] = g2;
     }
+}
+
+// Barrier split sums, in split order: segment targets add into f_segs,
+// blob targets overwrite their repulsion force.
+__global__ void barrier_reduce(BarrierLaunch a, int splits)
+{
+    const int ntg = a.num_segs + (a.wall ? 0 : a.num_blobs);
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 3 * ntg) return;
+    const int local = e / 3, c = e % 3;
+    double g = 0.0;
+    for (int p = 0; p < splits; ++p) g += a.partial[((size_t)p * ntg + local) * 3 + c];
+    if (local < a.num_segs)
+        a.f_segs[6 * (size_t)(a.start_seg + local) + c] += g;
+    else
+        a.f_blobs_rep[3 * (size_t)(local - a.num_segs) + c] = g;
 }
 
 // ---------------------------------------------------------------------------
@@ -700,9 +727,25 @@ gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &in)
     gmi_status st = ctx->rec_tgt.reserve((size_t)(N > 0 ? N : 1) * 2 * sizeof(float4));
     if (st != GMI_OK) return st;
     a.screen = static_cast<float4 *>(ctx->rec_tgt.ptr);
+    // source splits: enough CTAs for ~8 per SM, at least 256 sources each
+    const int tgt_ctas = (ntg + kBarrierTpb - 1) / kBarrierTpb;
+    int splits = (8 * ctx->sm_count + tgt_ctas - 1) / tgt_ctas;
+    splits = std::max(1, std::min(splits, N / 256));
+    a.chunk = (N + splits - 1) / splits;
+    splits = (N + a.chunk - 1) / a.chunk;
+    a.partial = nullptr;
+    if (splits > 1) {
+        st = ctx->partial.reserve((size_t)splits * ntg * 3 * sizeof(double));
+        if (st != GMI_OK) return st;
+        a.partial = static_cast<double *>(ctx->partial.ptr);
+    }
     pack_screen_positions<<<(N + 255) / 256, 256, 0, ctx->stream>>>(a.xs, a.S, a.xb, a.B, a.screen);
-    barrier_kernel<<<(ntg + kBarrierTpb - 1) / kBarrierTpb, kBarrierTpb, 0, ctx->stream>>>(a);
+    barrier_kernel<<<dim3(tgt_ctas, splits), kBarrierTpb, 0, ctx->stream>>>(a);
     ctx->launches += 2;
+    if (splits > 1) {
+        barrier_reduce<<<(3 * ntg + 255) / 256, 256, 0, ctx->stream>>>(a, splits);
+        ctx->launches++;
+    }
     GMI_CUDA_TRY(cudaGetLastError());
     return GMI_OK;
 }

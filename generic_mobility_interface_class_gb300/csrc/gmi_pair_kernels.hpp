@@ -35,6 +35,8 @@ struct BarrierLaunch {
     int nseg;
     double rseg, rblob, scale;
     int wall;
+    int chunk;            // sources per split (filled by the launcher)
+    double *partial;      // [splits][targets][3] when there are several splits (filled by the launcher)
 };
 
 void fill_consts(PairConsts &c, double a_eq, double a_seg, double a_blob, double mu);

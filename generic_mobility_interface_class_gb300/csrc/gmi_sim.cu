@@ -853,13 +853,68 @@ __device__ void A_apply(const SimP &P, int fil, const double *ub, int row, doubl
     }
 }
 
-// The Schur complement of the body equations (swimmer.cpp:466-682), one
-// thread per swimmer, inverted in place.
-__global__ void swimmer_schur_kernel(SimP P, int nt)
+// Per-filament parts of the swimmer's 6x6 Schur complement
+// (swimmer.cpp:466-682, GMRES branch), one CTA per filament: thread c < 6
+// forms column c of jacB_f * A_f (A_f applied to the unit body velocity e_c,
+// row block by row block, in row order); thread 6 forms the filament's 3x3
+// term of the body rotation block.  part[45 fil + 6c + r] and part[45 fil + 36 + 3i + j].
+__global__ void __launch_bounds__(32) schur_filament_kernel(SimP P, double *part)
 {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= P.W) return;
-    const int NS = P.NS, n6 = P.n6;
+    const int fil = blockIdx.x, n = fil / P.NF, NS = P.NS, n6 = P.n6, c = threadIdx.x;
+    double *out = part + 45 * (size_t)fil;
+    const M3 Qi = ldm3(P.bQ + 9 * n);
+    double fbd[3], dd[3];
+    m3_vec(Qi, P.fref + 3 * fil, fbd);
+    const double dn = sqrt(fbd[0] * fbd[0] + fbd[1] * fbd[1] + fbd[2] * fbd[2]);
+    for (int k = 0; k < 3; ++k) dd[k] = (0.5 * P.DL + dn) * fbd[k] / dn;
+    if (c < 6) {
+        // the rows of A_f e_c (A_apply): [I | rcross(dd)] on the position rows,
+        // the end-clamp blocks on rows 3NS and 3NS+3, zero elsewhere
+        double ub[6] = {0, 0, 0, 0, 0, 0};
+        ub[c] = 1.0;
+        double at[3], a1[3], a2[3], t[3];
+        m3_vec(rcross(dd), ub + 3, t);
+        for (int k = 0; k < 3; ++k) at[k] = ub[k] + t[k];
+        m3_vec(ldm3(P.ecb1 + 9 * fil), ub + 3, a1);
+        m3_vec(ldm3(P.ecb2 + 9 * fil), ub + 3, a2);
+        const double *jB = P.jacB + (size_t)fil * 6 * n6;
+        double colv[6] = {0, 0, 0, 0, 0, 0};
+        for (int row = 0; row < n6; row += 3) {
+            const double *a3 = row < 3 * NS ? at : row == 3 * NS ? a1 : row == 3 * NS + 3 ? a2 : nullptr;
+            if (a3 == nullptr) continue;
+            for (int r = 0; r < 6; ++r)
+                colv[r] += jB[r + 6 * row] * a3[0] + jB[r + 6 * (row + 1)] * a3[1] + jB[r + 6 * (row + 2)] * a3[2];
+        }
+        for (int r = 0; r < 6; ++r) out[6 * c + r] = colv[r];
+    } else if (c == 6) {
+        const double *u = P.bu + 3 * n;
+        const M3 blc = m3_scale(rcross(u), -1.0);
+        M3 o = m3_sub(m3_zero(), m3_mul(rcross(P.tl + 3 * fil), rcross(fbd)));
+        const double *cl = P.cl + 3 * fil;
+        const double ucl[3] = {u[1] * cl[2] - u[2] * cl[1], u[2] * cl[0] - u[0] * cl[2], u[0] * cl[1] - u[1] * cl[0]};
+        o = m3_add(o, m3_sub(m3_scale(rcross(cl), 0.5),
+                             m3_scale(m3_add(rcross(ucl), m3_mul(blc, rcross(cl))), 1.0 / 12.0)));
+        double tg[3], te[3];
+        q_tangent(ldq(P.q + 4 * (fil * NS + NS - 1)), tg);
+        for (int k = 0; k < 3; ++k) te[k] = P.EFM * tg[k];
+        o = m3_add(o, m3_mul(rcross(te), rcross(dd)));
+        for (int k = 0; k < 9; ++k) out[36 + k] = o.a[k];
+    }
+}
+
+// The swimmer's Schur complement from the per-filament parts (summed in
+// filament order), inverted in place.  One CTA per swimmer.
+__global__ void __launch_bounds__(64) swimmer_schur_kernel(SimP P, int nt, const double *part)
+{
+    __shared__ double sums[45];
+    const int n = blockIdx.x;
+    if (threadIdx.x < 45) {
+        double t = 0.0;
+        for (int i = 0; i < P.NF; ++i) t += part[45 * (size_t)(n * P.NF + i) + threadIdx.x];
+        sums[threadIdx.x] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
     const double dt_fac = (nt < P.neuler) ? -P.DT : -2.0 * P.DT / 3.0;
     const double *u = P.bu + 3 * n;
     const M3 Qi = ldm3(P.bQ + 9 * n);
@@ -869,45 +924,14 @@ __global__ void swimmer_schur_kernel(SimP P, int nt)
     for (int k = 0; k < 36; ++k) S6[k] = 0.0;
     for (int d = 0; d < 6; ++d) S6[d + 6 * d] = 1.0;
     add_block(S6, 6, 3, 3, m3_scale(m3_sub(m3_scale(m3_mul(blc, cbo), 1.0 / 12.0), m3_scale(cbo, 0.5)), dt_fac));
-    M3 old = m3_zero();
-    for (int i = 0; i < P.NF; ++i) {
-        const int fil = n * P.NF + i;
-        double fbd[3];
-        m3_vec(Qi, P.fref + 3 * fil, fbd);
-        old = m3_sub(old, m3_mul(rcross(P.tl + 3 * fil), rcross(fbd)));
-        const double *cl = P.cl + 3 * fil;
-        const double ucl[3] = {u[1] * cl[2] - u[2] * cl[1], u[2] * cl[0] - u[0] * cl[2], u[0] * cl[1] - u[1] * cl[0]};
-        old = m3_add(old, m3_sub(m3_scale(rcross(cl), 0.5),
-                                 m3_scale(m3_add(rcross(ucl), m3_mul(blc, rcross(cl))), 1.0 / 12.0)));
-        double t[3], te[3], dd[3];
-        q_tangent(ldq(P.q + 4 * (fil * NS + NS - 1)), t);
-        for (int c = 0; c < 3; ++c) te[c] = P.EFM * t[c];
-        const double dn = sqrt(fbd[0] * fbd[0] + fbd[1] * fbd[1] + fbd[2] * fbd[2]);
-        for (int c = 0; c < 3; ++c) dd[c] = (0.5 * P.DL + dn) * fbd[c] / dn;
-        old = m3_add(old, m3_mul(rcross(te), rcross(dd)));
-    }
+    M3 old;
+    for (int k = 0; k < 9; ++k) old.a[k] = sums[36 + k];
     double bm[36];
     rotated_mobility(P, Qi, bm);
     old = m3_mul(get_block(bm, 6, 3, 3), old);
     const M3 add = m3_add(m3_sub(old, m3_scale(m3_mul(blc, old), 0.5)), m3_scale(m3_mul(m3_mul(blc, blc), old), 1.0 / 12.0));
     add_block(S6, 6, 3, 3, m3_scale(add, dt_fac));
-    // schur -= jacB_f * A_f
-    for (int i = 0; i < P.NF; ++i) {
-        const int fil = n * P.NF + i;
-        const double *jB = P.jacB + (size_t)fil * 6 * n6;
-        for (int c = 0; c < 6; ++c) {
-            double ub[6] = {0, 0, 0, 0, 0, 0};
-            ub[c] = 1.0;
-            double colv[6] = {0, 0, 0, 0, 0, 0};
-            for (int row = 0; row < n6; row += 3) {
-                double a3[3];
-                A_apply(P, fil, ub, row, a3);
-                for (int r = 0; r < 6; ++r)
-                    colv[r] += jB[r + 6 * row] * a3[0] + jB[r + 6 * (row + 1)] * a3[1] + jB[r + 6 * (row + 2)] * a3[2];
-            }
-            for (int r = 0; r < 6; ++r) S6[r + 6 * c] -= colv[r];
-        }
-    }
+    for (int k = 0; k < 36; ++k) S6[k] -= sums[k];
     if (!invert6_dev(S6)) atomicOr(P.flags + 2, 1);
     for (int k = 0; k < 36; ++k) P.schur[36 * n + k] = S6[k];
 }
@@ -933,18 +957,23 @@ __global__ void __launch_bounds__(128) jim_partial_kernel(SimP P, const double *
                                                        red[threadIdx.x][2] + red[threadIdx.x][3];
 }
 
-// (2) per swimmer: out_body = schur_inv * (in_body - sum_f part_f)
-__global__ void jim_body_kernel(SimP P, const double *in, const double *part, double *out)
+// (2) per swimmer: out_body = schur_inv * (in_body - sum_f part_f); one CTA
+// per swimmer, thread r subtracts the filaments' parts of row r in order.
+__global__ void __launch_bounds__(32) jim_body_kernel(SimP P, const double *in, const double *part, double *out)
 {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= P.W) return;
+    __shared__ double b2[6];
+    const int n = blockIdx.x;
     const size_t b = (size_t)n * P.per_body + 6 * P.NF * P.NS;
-    double b2[6];
-    for (int r = 0; r < 6; ++r) b2[r] = in[b + r];
-    for (int i = 0; i < P.NF; ++i)
-        for (int r = 0; r < 6; ++r) b2[r] -= part[6 * (n * P.NF + i) + r];
-    const double *Si = P.schur + 36 * n;
-    for (int r = 0; r < 6; ++r) {
+    if (threadIdx.x < 6) {
+        const int r = threadIdx.x;
+        double v = in[b + r];
+        for (int i = 0; i < P.NF; ++i) v -= part[6 * (n * P.NF + i) + r];
+        b2[r] = v;
+    }
+    __syncwarp();
+    if (threadIdx.x < 6) {
+        const int r = threadIdx.x;
+        const double *Si = P.schur + 36 * n;
         double s = 0.0;
         for (int k = 0; k < 6; ++k) s += Si[r + 6 * k] * b2[k];
         out[b + r] = s;
@@ -1075,6 +1104,7 @@ struct gmi_sim {
     int maxb = 100;
     double *C = nullptr, *D = nullptr, *err = nullptr, *nerr = nullptr, *upd = nullptr, *tmp = nullptr;
     double *dots = nullptr, *part = nullptr, *jpart = nullptr, *scal = nullptr;
+    double *spart = nullptr;  // per-filament parts of the Schur complement (45 each)
     int *h_flags = nullptr;
     std::vector<void *> allocs;
     bool prepared = false;
@@ -1155,8 +1185,9 @@ static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
     GMI_CUDA_TRY(cudaFuncSetAttribute(gj_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     gj_invert_kernel<<<P.F, kGjTpb, smem, sst(m)>>>(P.invJ, P.n6, use_smem, P.flags);
     filament_B_kernel<<<P.F, 128, 6 * P.n6 * sizeof(double), sst(m)>>>(P, nt);
-    swimmer_schur_kernel<<<gridN(P.W, 32), 32, 0, sst(m)>>>(P, nt);
-    GMI_TRY(sim_launched(m, 4));
+    schur_filament_kernel<<<P.F, 32, 0, sst(m)>>>(P, m->spart);
+    swimmer_schur_kernel<<<P.W, 64, 0, sst(m)>>>(P, nt, m->spart);
+    GMI_TRY(sim_launched(m, 5));
     GMI_TRY(read_flags(m));
     if (m->h_flags[2]) {
         set_last_error_msg("the approximate Jacobian is singular (matrix.cpp:549-554 stops the reference here)");
@@ -1169,7 +1200,7 @@ static gmi_status jacobian_inv_mult(gmi_sim *m, const double *in, double *out)
 {
     const SimP &P = m->P;
     jim_partial_kernel<<<P.F, 128, 0, sst(m)>>>(P, in, m->jpart);
-    jim_body_kernel<<<gridN(P.W, 32), 32, 0, sst(m)>>>(P, in, m->jpart, out);
+    jim_body_kernel<<<P.W, 32, 0, sst(m)>>>(P, in, m->jpart, out);
     jim_fil_kernel<<<P.F, 128, P.n6 * sizeof(double), sst(m)>>>(P, in, out);
     return sim_launched(m, 3);
 }
@@ -1352,6 +1383,7 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
     SIM_ALLOC(m->dots, m->maxb + 1);
     SIM_ALLOC(m->part, (size_t)((nb + kVecChunk - 1) / kVecChunk) * (m->maxb + 1));
     SIM_ALLOC(m->jpart, 6 * F);
+    SIM_ALLOC(m->spart, 45 * F);
     SIM_ALLOC(m->scal, 4);
     {
         double *fl = nullptr;

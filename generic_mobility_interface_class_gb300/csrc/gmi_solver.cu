@@ -465,12 +465,19 @@ template <int TPB> __device__ __forceinline__ void block_sum6(const double *v, d
     }
 }
 
-// Sum over the gx per-CTA 6-vectors of each swimmer (part[(n*gx + x)*6 + c]).
-__device__ __forceinline__ void swimmer_sums(const double *part, int n, int gx, double *sums)
+// Sum over the gx per-CTA 6-vectors of each swimmer (part[(n*gx + x)*6 + c])
+// into sh[6n + c], in x order; one thread per (swimmer, component), loads
+// unrolled so they are in flight together.
+__device__ __forceinline__ void swimmer_sums(const double *part, int W, int gx, double *sh)
 {
-    for (int c = 0; c < 6; ++c) sums[c] = 0.0;
-    for (int x = 0; x < gx; ++x)
-        for (int c = 0; c < 6; ++c) sums[c] += __ldcg(part + ((size_t)n * gx + x) * 6 + c);
+    for (int e = threadIdx.x; e < 6 * W; e += blockDim.x) {
+        const double *p = part + (size_t)(e / 6) * gx * 6 + (e % 6);
+        double t = 0.0;
+#pragma unroll 8
+        for (int x = 0; x < gx; ++x) t += __ldcg(p + 6 * (size_t)x);
+        sh[e] = t;
+    }
+    __syncthreads();
 }
 
 // S1: grid (ceil(nblob/kSBlobs), W).
@@ -503,9 +510,11 @@ __global__ void __launch_bounds__(kSBlobs) s1_normalise_moments_kernel(
     }
     block_sum6<kSBlobs>(a, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
     if (!last_cta(ticket, gridDim.x * gridDim.y)) return;
+    extern __shared__ double sh[];  // 6 W
+    swimmer_sums(part, W, gridDim.x, sh);
     for (int s = threadIdx.x; s < W; s += kSBlobs) {
-        double sums[6], qb[6];
-        swimmer_sums(part, s, gridDim.x, sums);
+        const double *sums = sh + 6 * s;
+        double qb[6];
         for (int c = 0; c < 6; ++c) {
             qb[c] = w[3 * nb + 6 * s + c] / nrm;
             q[3 * nb + 6 * s + c] = qb[c];
@@ -561,11 +570,9 @@ __global__ void __launch_bounds__(kSBlobs) s2_precond_blobs_kernel(
     }
     block_sum6<kSBlobs>(b, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
     if (!last_cta(ticket, gridDim.x * gridDim.y)) return;
-    for (int s = threadIdx.x; s < W; s += kSBlobs) {
-        double sums[6];
-        swimmer_sums(part, s, gridDim.x, sums);
-        for (int c = 0; c < 6; ++c) w[3 * nb + 6 * s + c] = -sums[c];
-    }
+    extern __shared__ double sh[];  // 6 W
+    swimmer_sums(part, W, gridDim.x, sh);
+    for (int e = threadIdx.x; e < 6 * W; e += kSBlobs) w[3 * nb + e] = -sh[e];
 }
 
 // Projections of this CTA's rows (ws, kSRows of them) on Q[:, 0..k): one
@@ -590,14 +597,19 @@ __device__ __forceinline__ bool finish_projections(const double *P, int k, int n
     const int first = g * kSGroup, gsize = min(kSGroup, nblk - first);
     if (!last_cta(tickets + 1 + g, gsize)) return false;
     for (int i = threadIdx.x; i < k; i += kSTpb) {
+        const double *p = P + (size_t)i * nblk + first;
         double t = 0.0;
-        for (int b = 0; b < gsize; ++b) t += __ldcg(P + (size_t)i * nblk + first + b);
+#pragma unroll
+        for (int b = 0; b < kSGroup; ++b)
+            if (b < gsize) t += __ldcg(p + b);
         G[(size_t)i * ngroups + g] = t;
     }
     if (!last_cta(tickets, ngroups)) return false;
     for (int i = threadIdx.x; i < k; i += kSTpb) {
+        const double *p = G + (size_t)i * ngroups;
         double t = 0.0;
-        for (int b = 0; b < ngroups; ++b) t += __ldcg(G + (size_t)i * ngroups + b);
+#pragma unroll 8
+        for (int b = 0; b < ngroups; ++b) t += __ldcg(p + b);
         h[i] = t;
     }
     return true;
@@ -696,17 +708,34 @@ __global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
         P[blockIdx.x] = a;
     }
     if (!last_cta(ticket, gridDim.x)) return;
-    if (threadIdx.x != 0) return;
+    // ||w||^2 in a fixed two-level order; the H column and the rotations to
+    // shared memory, so the sequential Givens sweep reads no global memory
+    __shared__ double red[kSTpb];
+    __shared__ double col[kFMaxK + 1], csh[kFMaxK], snh[kFMaxK];
     double t = 0.0;
-    for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(P + b);
-    const double nrm = sqrt(t);
-    scal[kNormOff] = nrm;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += kSTpb) t += __ldcg(P + b);
+    red[threadIdx.x] = t;
     const int iter = k;
-    double *col = H + (size_t)ldh * (iter - 1);
+    double *gcol = H + (size_t)ldh * (iter - 1);
+    for (int i = threadIdx.x; i < iter; i += kSTpb) {
+        col[i] = gcol[i];
+        if (i < iter - 1) {
+            csh[i] = cs[i];
+            snh[i] = sn[i];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    double r = 0.0;
+    for (int b = threadIdx.x; b < kSTpb; b += 32) r += red[b];
+    r = warp_sum(r);
+    if (threadIdx.x != 0) return;
+    const double nrm = sqrt(r);
+    scal[kNormOff] = nrm;
     col[iter] = nrm;
     for (int i = 1; i < iter; ++i) {
-        const double u = cs[i - 1] * col[i - 1] + sn[i - 1] * col[i];
-        col[i] = cs[i - 1] * col[i] - sn[i - 1] * col[i - 1];
+        const double u = csh[i - 1] * col[i - 1] + snh[i - 1] * col[i];
+        col[i] = csh[i - 1] * col[i] - snh[i - 1] * col[i - 1];
         col[i - 1] = u;
     }
     const double hk = col[iter], hd = col[iter - 1];
@@ -727,14 +756,29 @@ __global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
     sn[iter - 1] = s;
     col[iter - 1] = c * hd + s * hk;
     col[iter] = 0.0;
+    for (int i = 0; i <= iter; ++i) gcol[i] = col[i];
     beta[iter] = -s * beta[iter - 1];
     beta[iter - 1] = c * beta[iter - 1];
     const double resid = fabs(beta[iter]) / ctl->norm_ref;
     ctl->resid = resid;
-    if (!(resid > ctl->tol) || iter >= ctl->max_iter)  // converged, at the cap, or NaN
+    const int replays = ++ctl->replays;
+    // converged, at the cap, or NaN; the replay count bounds the loop even if k stalled
+    const bool done = !(resid > ctl->tol) || iter >= ctl->max_iter || replays > ctl->max_iter;
+    if (done)
         ctl->done = 1;
     else
         ctl->k = iter + 1;
+}
+
+// Last node of the device-side loop's body: one thread decides whether the
+// loop runs again.  It runs once per pass whatever the step kernels did, and
+// its own pass count ends the loop after max_iter + 1 passes in any case.
+__global__ void arnoldi_loop_guard_kernel(GmresCtl *ctl, cudaGraphConditionalHandle loop)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int passes = ++ctl->guard;
+    const bool again = ctl->done == 0 && passes <= ctl->max_iter + 1;
+    cudaGraphSetConditional(loop, again ? 1u : 0u);
 }
 
 // Back substitution y = H(0:iter, 0:iter)^-1 beta(0:iter)
@@ -743,14 +787,35 @@ __global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
 __global__ void backsolve_warp_kernel(const double *__restrict__ H, int ldh, const double *__restrict__ beta,
                                       int iter, double *__restrict__ y)
 {
+    constexpr int kPer = (kFMaxK + 31) / 32;
     __shared__ double b[kFMaxK];
     for (int i = threadIdx.x; i < iter; i += 32) b[i] = beta[i];
     __syncwarp();
-    for (int j = iter - 1; j >= 0; --j) {
-        const double yj = b[j] / H[j + (size_t)ldh * j];
-        for (int i = threadIdx.x; i < j; i += 32) b[i] -= H[i + (size_t)ldh * j] * yj;
+    // column j of H in registers (row i = lane + 32 q), the next one in flight
+    double cur[kPer], nxt[kPer];
+    const int j0 = iter - 1;
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+        const int i = threadIdx.x + 32 * q;
+        cur[q] = i <= j0 ? H[i + (size_t)ldh * j0] : 0.0;
+    }
+    for (int j = j0; j >= 0; --j) {
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int i = threadIdx.x + 32 * q;
+            nxt[q] = (j > 0 && i <= j - 1) ? H[i + (size_t)ldh * (j - 1)] : 0.0;
+        }
+        const double diag = __shfl_sync(0xffffffffu, cur[j / 32], j % 32);
+        const double yj = b[j] / diag;
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int i = threadIdx.x + 32 * q;
+            if (i < j) b[i] -= cur[q] * yj;
+        }
         if (threadIdx.x == 0) y[j] = yj;
         __syncwarp();
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) cur[q] = nxt[q];
     }
 }
 
@@ -893,7 +958,7 @@ static StepLayout step_layout(int n, int nblob, int W)
 // One device-controlled Arnoldi step (S1, S2, the blob-blob pair apply, S3,
 // S4, S5) enqueued on the solver stream; captured once per precision into
 // s->graph[pidx].
-static gmi_status enqueue_arnoldi_step(gmi_solver *s)
+static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle loop, bool use_loop)
 {
     gmi_context *ctx = s->ctx;
     cudaStream_t st = ctx->stream;
@@ -911,9 +976,10 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s)
     int *tk = s->st_tickets;
     int *tk3 = tk + 2, *tk4 = tk3 + 1 + L.ngroups, *tk5 = tk4 + 1 + L.ngroups;
     const dim3 bgrid(L.gx, W);
-    s1_normalise_moments_kernel<<<bgrid, kSBlobs, 0, st>>>(W, nblob, s->Q, ld, s->w, s->R, s->refs, s->ktk_rot,
+    const size_t wsm = 6 * (size_t)W * sizeof(double);
+    s1_normalise_moments_kernel<<<bgrid, kSBlobs, wsm, st>>>(W, nblob, s->Q, ld, s->w, s->R, s->refs, s->ktk_rot,
                                                           s->mob_rot, s->z, part, s->st_scal, tk, s->ctl);
-    s2_precond_blobs_kernel<<<bgrid, kSBlobs, 0, st>>>(W, nblob, s->Q, ld, s->R, s->refs, minv, s->x_blobs, s->z,
+    s2_precond_blobs_kernel<<<bgrid, kSBlobs, wsm, st>>>(W, nblob, s->Q, ld, s->R, s->refs, minv, s->x_blobs, s->z,
                                                       s->w, s->gm_rec, f64 ? 1 : 0, part, tk + 1, s->ctl);
     GMI_CUDA_TRY(cudaGetLastError());
     ExplicitPairEnv env{};
@@ -935,10 +1001,37 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s)
     s4_update_project_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, G, tk4, s->st_scal, s->H, ldh, s->ctl);
     s5_update_norm_givens_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, tk5, s->st_scal, s->H, ldh,
                                                            s->beta, s->cs, s->sn, s->ctl);
+    if (use_loop) arnoldi_loop_guard_kernel<<<1, 32, 0, st>>>(s->ctl, loop);
     GMI_CUDA_TRY(cudaGetLastError());
     return GMI_OK;
 }
 
+// Capture the Arnoldi step into body (a conditional node's body graph, or a
+// fresh graph when body is null).
+static gmi_status capture_step(gmi_solver *s, cudaGraph_t body, cudaGraphConditionalHandle loop, bool use_loop,
+                               cudaGraph_t *out)
+{
+    cudaStream_t st = s->ctx->stream;
+    if (body)
+        GMI_CUDA_TRY(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    else
+        GMI_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    const gmi_status est = enqueue_arnoldi_step(s, loop, use_loop);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (est != GMI_OK) {
+        if (g && !body) cudaGraphDestroy(g);
+        return est;
+    }
+    GMI_CUDA_TRY(ce);
+    *out = g;
+    return GMI_OK;
+}
+
+// The whole Arnoldi loop as one graph: a WHILE conditional node whose body is
+// one step; the norm kernel of the step clears the condition when the solve
+// is done.  Falls back to a graph of one step, replayed in batches from the
+// host, where conditional nodes are unavailable.
 static gmi_status ensure_arnoldi_graph(gmi_solver *s, int pidx, size_t *nodes)
 {
     cudaStream_t st = s->ctx->stream;
@@ -947,21 +1040,44 @@ static gmi_status ensure_arnoldi_graph(gmi_solver *s, int pidx, size_t *nodes)
         return GMI_ERR_STATE;
     }
     if (s->graph[pidx] == nullptr) {
-        GMI_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
-        const gmi_status est = enqueue_arnoldi_step(s);
         cudaGraph_t g = nullptr;
-        const cudaError_t ce = cudaStreamEndCapture(st, &g);
-        if (est != GMI_OK) {
-            if (g) cudaGraphDestroy(g);
-            return est;
+        bool loops = false;
+        size_t body_nodes = 0;
+        if (cudaGraphCreate(&g, 0) == cudaSuccess) {
+            cudaGraphConditionalHandle h{};
+            cudaGraphNodeParams cp{};
+            cp.type = cudaGraphNodeTypeConditional;
+            cudaGraphNode_t node;
+            bool ok = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+            if (ok) {
+                cp.conditional.handle = h;
+                cp.conditional.type = cudaGraphCondTypeWhile;
+                cp.conditional.size = 1;
+                ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
+            }
+            if (ok) {
+                cudaGraph_t body = cp.conditional.phGraph_out[0], captured = nullptr;
+                const gmi_status cst = capture_step(s, body, h, true, &captured);
+                if (cst != GMI_OK) {
+                    cudaGraphDestroy(g);
+                    return cst;
+                }
+                cudaGraphGetNodes(body, nullptr, &body_nodes);
+                loops = true;
+            } else {
+                cudaGraphDestroy(g);
+                g = nullptr;
+                cudaGetLastError();
+            }
         }
-        GMI_CUDA_TRY(ce);
+        if (!loops) GMI_TRY(capture_step(s, nullptr, cudaGraphConditionalHandle{}, false, &g));
         const cudaError_t ie = cudaGraphInstantiate(&s->graph[pidx], g, 0);
-        size_t cnt = 0;
-        cudaGraphGetNodes(g, nullptr, &cnt);
+        size_t cnt = body_nodes;  // launches per Arnoldi step
+        if (!loops) cudaGraphGetNodes(g, nullptr, &cnt);
         cudaGraphDestroy(g);
         GMI_CUDA_TRY(ie);
         s->graph_nodes[pidx] = cnt;
+        s->graph_loops[pidx] = loops;
     }
     *nodes = s->graph_nodes[pidx];
     return GMI_OK;
@@ -1011,12 +1127,24 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
         c.k = 1;
         c.done = 0;
         c.max_iter = max_iter;
+        c.replays = 0;
+        c.guard = 0;
         c.tol = tol;
         c.norm_ref = norm_ref;
         *s->h_ctl = c;
         GMI_CUDA_TRY(cudaMemcpyAsync(s->ctl, s->h_ctl, sizeof c, cudaMemcpyHostToDevice, st));
         int batch = 4, replayed = 0;
-        for (;;) {
+        if (s->graph_loops[pidx]) {
+            GMI_CUDA_TRY(cudaGraphLaunch(s->graph[pidx], st));
+            GMI_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->ctl, sizeof c, cudaMemcpyDeviceToHost, st));
+            GMI_CUDA_TRY(cudaStreamSynchronize(st));
+            s->ctx->launches += (long long)s->h_ctl->guard * (long long)nodes;
+            if (!s->h_ctl->done) {
+                set_last_error_msg("GMRES loop ended without completion");
+                return GMI_ERR_STATE;
+            }
+        }
+        for (; !s->graph_loops[pidx];) {
             for (int b = 0; b < batch; ++b) GMI_CUDA_TRY(cudaGraphLaunch(s->graph[pidx], st));
             replayed += batch;
             s->ctx->launches += (long long)batch * (long long)nodes;

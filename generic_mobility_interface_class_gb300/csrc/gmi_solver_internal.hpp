@@ -35,8 +35,9 @@ struct gmi_solver {
     size_t st_ticket_count = 0;
     double *gm_partial = nullptr;     // split partial sums of the GMRES operator
     size_t gm_partial_bytes = 0;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // one Arnoldi step, per precision
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};  // per precision: the Arnoldi loop (or one step)
     size_t graph_nodes[2] = {0, 0};
+    bool graph_loops[2] = {false, false};           // graph holds the whole device-side loop
     bool use_graphs = true;
 };
 
@@ -46,6 +47,8 @@ struct GmresCtl {
     int k;         // current Arnoldi iteration (1-based)
     int done;      // set by the Givens step when converged or at max_iter
     int max_iter;
+    int replays;   // Arnoldi steps completed by the norm kernel in this solve
+    int guard;     // passes of the device-side loop (counted by its guard kernel)
     int pad;
     double tol;    // relative residual target
     double norm_ref;
