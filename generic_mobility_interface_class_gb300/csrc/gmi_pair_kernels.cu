@@ -727,10 +727,10 @@ gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &in)
     gmi_status st = ctx->rec_tgt.reserve((size_t)(N > 0 ? N : 1) * 2 * sizeof(float4));
     if (st != GMI_OK) return st;
     a.screen = static_cast<float4 *>(ctx->rec_tgt.ptr);
-    // source splits: enough CTAs for ~8 per SM, at least 256 sources each
+    // source splits: enough CTAs for ~8 per SM, at least 64 sources each
     const int tgt_ctas = (ntg + kBarrierTpb - 1) / kBarrierTpb;
     int splits = (8 * ctx->sm_count + tgt_ctas - 1) / tgt_ctas;
-    splits = std::max(1, std::min(splits, N / 256));
+    splits = std::max(1, std::min(splits, N / 64));
     a.chunk = (N + splits - 1) / splits;
     splits = (N + a.chunk - 1) / a.chunk;
     a.partial = nullptr;
