@@ -191,6 +191,26 @@ template <class R> __device__ __forceinline__ KernelConsts<R> convert_consts(con
     return k;
 }
 
+// One source's contribution to one target's accumulator (self: the target
+// and the source are the same particle; only the wall formula needs it).
+template <int KIND, class R>
+__device__ __forceinline__ void pair_apply(const Pos<R> &t, const Pos<R> &sp, const R *F, const KernelConsts<R> &K,
+                                           bool self, R *acc)
+{
+    const R dx = diff<R>(t.x, sp.x, t.lx, sp.lx);
+    const R dy = diff<R>(t.y, sp.y, t.ly, sp.ly);
+    const R dz = diff<R>(t.z, sp.z, t.lz, sp.lz);
+    if constexpr (KIND == kSSWall) {
+        const R zi = t.z + t.lz, zj = sp.z + sp.lz;
+        const R zs = (t.z + sp.z) + (t.lz + sp.lz);
+        pair_ss_wall<R>(dx, dy, dz, zs, zi, zj, self, F, acc, acc + 3);
+    }
+    if constexpr (KIND == kSS) pair_ss<R>(dx, dy, dz, F, K.eq, acc, acc + 3);
+    if constexpr (KIND == kBB) pair_bb<R>(dx, dy, dz, F, K.eq, acc);
+    if constexpr (KIND == kSB) pair_sb<R>(dx, dy, dz, F, K.uq, acc, acc + 3);
+    if constexpr (KIND == kBS) pair_bs<R>(dx, dy, dz, F, K.uq, acc);
+}
+
 template <int KIND, class R, int TPB, int TT>
 __global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ CUtensorMap src_map,
                                                        const PairLaunch args)
@@ -261,23 +281,8 @@ __global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ C
             R F[6];
             load_src(tile + jj * kRecLen, sp, F);
 #pragma unroll
-            for (int k = 0; k < TT; ++k) {
-                const R dx = diff<R>(tp[k].x, sp.x, tp[k].lx, sp.lx);
-                const R dy = diff<R>(tp[k].y, sp.y, tp[k].ly, sp.ly);
-                if constexpr (KIND == kSSWall) {
-                    const R zi = tp[k].z + tp[k].lz, zj = sp.z + sp.lz;
-                    const R dz = diff<R>(tp[k].z, sp.z, tp[k].lz, sp.lz);
-                    const R zs = (tp[k].z + sp.z) + (tp[k].lz + sp.lz);
-                    const bool self = (args.tgt_start + ti[k]) == (j0 + jj);
-                    pair_ss_wall<R>(dx, dy, dz, zs, zi, zj, self, F, acc[k].t, acc[k].t + 3);
-                } else {
-                    const R dz = diff<R>(tp[k].z, sp.z, tp[k].lz, sp.lz);
-                    if constexpr (KIND == kSS) pair_ss<R>(dx, dy, dz, F, K.eq, acc[k].t, acc[k].t + 3);
-                    if constexpr (KIND == kBB) pair_bb<R>(dx, dy, dz, F, K.eq, acc[k].t);
-                    if constexpr (KIND == kSB) pair_sb<R>(dx, dy, dz, F, K.uq, acc[k].t, acc[k].t + 3);
-                    if constexpr (KIND == kBS) pair_bs<R>(dx, dy, dz, F, K.uq, acc[k].t);
-                }
-            }
+            for (int k = 0; k < TT; ++k)
+                pair_apply<KIND, R>(tp[k], sp, F, K, (args.tgt_start + ti[k]) == (j0 + jj), acc[k].t);
         }
 #pragma unroll
         for (int k = 0; k < TT; ++k) acc[k].fold();
@@ -317,6 +322,70 @@ __global__ void reduce_splits(const double *__restrict__ partial, int splits, in
     double s = accumulate ? out[e] : 0.0;
     for (int p = 0; p < splits; ++p) s += partial[(size_t)p * count + e];
     out[e] = s;
+}
+
+// ---------------------------------------------------------------------------
+// 2b. small problems (up to a few thousand sources): one warp per TPW
+// targets, its 32 lanes stride over the sources with direct vector loads
+// (records stay in L1/L2), each lane sums its share (FP32C folds its tile
+// sum every kWarpFold sources), and the warp adds the lane sums in FP64.
+// At these sizes the tiled kernel cannot field enough threads to fill the
+// GPU; this one runs N/TPW warps with no split reduction.
+// ---------------------------------------------------------------------------
+constexpr int kWarpCta = 128;  // threads per CTA of the warp kernel
+constexpr int kWarpFold = 32;
+
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int KIND, class R, int TPW>
+__global__ void __launch_bounds__(kWarpCta) rpy_pair_warp_kernel(const PairLaunch args, const R *__restrict__ src)
+{
+    constexpr int NOUT = KindTraits<KIND>::nout;
+    if (args.skip != nullptr && *args.skip != 0) return;
+    const int lane = threadIdx.x & 31;
+    const int t0 = ((blockIdx.x * kWarpCta + threadIdx.x) >> 5) * TPW;
+    if (t0 >= args.n_tgt) return;  // whole warp
+    const KernelConsts<R> K = convert_consts<R>(args.k);
+    const R *tgt_rec = reinterpret_cast<const R *>(args.tgt_rec);
+    Pos<R> tp[TPW];
+    int gi[TPW];
+    Acc<R, NOUT> acc[TPW];
+#pragma unroll
+    for (int k = 0; k < TPW; ++k) {
+        gi[k] = args.tgt_start + min(t0 + k, args.n_tgt - 1);
+        tp[k] = load_tgt(tgt_rec, gi[k]);
+        acc[k].zero();
+    }
+    int cnt = 0;
+    for (int j = lane; j < args.n_src; j += 32) {
+        Pos<R> sp;
+        R F[6];
+        load_src(src + (size_t)j * kRecLen, sp, F);
+#pragma unroll
+        for (int k = 0; k < TPW; ++k) pair_apply<KIND, R>(tp[k], sp, F, K, gi[k] == j, acc[k].t);
+        if (++cnt == kWarpFold) {
+#pragma unroll
+            for (int k = 0; k < TPW; ++k) acc[k].fold();
+            cnt = 0;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < TPW; ++k) {
+        acc[k].fold();
+        double v[NOUT];
+#pragma unroll
+        for (int c = 0; c < NOUT; ++c) v[c] = warp_sum_d(acc[k].total(c));
+        if (lane == 0 && t0 + k < args.n_tgt) {
+            double *o = args.out + (size_t)(t0 + k) * NOUT;
+#pragma unroll
+            for (int c = 0; c < NOUT; ++c) o[c] = args.accumulate ? o[c] + v[c] : v[c];
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -429,9 +498,10 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
         g2 = a.scale * fz * fz * fz * fz;
     }
     const double a_tgt = is_seg_target ? a.rseg : a.rblob;
-    // FP32 screen cutoffs against segment and blob sources, with a relative margin
-    const float cut_s = (float)(1.1 * (a_tgt + a.rseg)) * 1.001f;
-    const float cut_b = (float)(1.1 * (a_tgt + a.rblob)) * 1.001f;
+    // squared FP32 screen cutoffs against segment and blob sources (host
+    // precomputed: no FP64 arithmetic in the loop)
+    const float c2_s = is_seg_target ? a.cut2_ss : a.cut2_sb;
+    const float c2_b = is_seg_target ? a.cut2_sb : a.cut2_bb;
     int count = 0;  // warp-uniform
     for (int j0 = j_begin; j0 < j_end; j0 += kBarrierTpb) {
         const int jl = j0 + threadIdx.x;
@@ -448,8 +518,7 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
             const float dy = (pf.y - s.y) + (pl.y - sl.y);
             const float dz = (pf.z - s.z) + (pl.z - sl.z);
             const float d2 = dx * dx + dy * dy + dz * dz;
-            const float cut = j < a.S ? cut_s : cut_b;
-            bool cand = valid && d2 < cut * cut;
+            bool cand = valid && d2 < (j < a.S ? c2_s : c2_b);
             if (cand) {
                 if (is_seg_target) {
                     const int di = gi - j;
@@ -629,6 +698,42 @@ static void *kernel_ptr(int kind, bool f64, int shape_idx)
     }
 }
 
+constexpr int kWarpShapeTpb = kPairWarpShapeTpb;
+constexpr int kWarpMaxSources = kPairWarpMaxSources;
+
+template <int KIND> static void *warp_kernel_for(bool f64, int tpw)
+{
+    if (f64) return tpw >= 2 ? reinterpret_cast<void *>(&rpy_pair_warp_kernel<KIND, double, 2>)
+                              : reinterpret_cast<void *>(&rpy_pair_warp_kernel<KIND, double, 1>);
+    return tpw >= 2 ? reinterpret_cast<void *>(&rpy_pair_warp_kernel<KIND, float, 2>)
+                    : reinterpret_cast<void *>(&rpy_pair_warp_kernel<KIND, float, 1>);
+}
+
+static void *warp_kernel_ptr(int kind, bool f64, int tpw)
+{
+    switch (kind) {
+        case kSS: return warp_kernel_for<kSS>(f64, tpw);
+        case kSSWall: return warp_kernel_for<kSSWall>(f64, tpw);
+        case kBB: return warp_kernel_for<kBB>(f64, tpw);
+        case kSB: return warp_kernel_for<kSB>(f64, tpw);
+        default: return warp_kernel_for<kBS>(f64, tpw);
+    }
+}
+
+static gmi_status launch_warp(cudaStream_t stream, int kind, bool f64, int tpw, const PairLaunch &a,
+                              const void *src_rec)
+{
+    tpw = tpw >= 2 ? 2 : 1;
+    void *fn = warp_kernel_ptr(kind, f64, tpw);
+    const long long warps = ((long long)a.n_tgt + tpw - 1) / tpw;
+    const int ctas = (int)((warps * 32 + kWarpCta - 1) / kWarpCta);
+    PairLaunch la = a;
+    la.partial = nullptr;
+    void *params[] = {&la, const_cast<void **>(&src_rec)};
+    GMI_CUDA_TRY(cudaLaunchKernel(fn, dim3(ctas), dim3(kWarpCta), params, 0, stream));
+    return GMI_OK;
+}
+
 static int shape_index(int tpb, int tt)
 {
     for (int i = 0; i < kNumShapes; ++i)
@@ -668,9 +773,25 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
         auto it = ctx->tuned.find(TuneKey{kind, ctx->precision, n_tgt, n_src});
         if (it != ctx->tuned.end()) {
             shape = it->second;
+        } else if (n_src <= kWarpMaxSources) {
+            shape = PairShape{kWarpShapeTpb, 2, 0};  // few sources: warp per two targets
         } else if ((long long)n_tgt * 2 < (long long)ctx->sm_count * 256) {
             shape = PairShape{64, 1, 0};  // small target sets: more, smaller CTAs
         }
+    }
+    if (shape.tpb == kWarpShapeTpb) {
+        PairLaunch a{};
+        a.tgt_rec = tgt_rec;
+        a.tgt_start = tgt_start;
+        a.n_tgt = n_tgt;
+        a.n_src = n_src;
+        a.k = k;
+        a.out = out;
+        a.accumulate = accumulate;
+        a.err = ctx->d_err;
+        const gmi_status ws = launch_warp(ctx->stream, kind, f64, shape.tt, a, src_rec);
+        if (ws == GMI_OK) ctx->launches++;
+        return ws;
     }
     const int sidx = shape_index(shape.tpb, shape.tt);
     const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;
@@ -727,6 +848,15 @@ gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &in)
     gmi_status st = ctx->rec_tgt.reserve((size_t)(N > 0 ? N : 1) * 2 * sizeof(float4));
     if (st != GMI_OK) return st;
     a.screen = static_cast<float4 *>(ctx->rec_tgt.ptr);
+    // screen cutoffs 1.1 (a_i + a_j) with a relative margin of 1e-3 for the
+    // FP32 separation; pairs inside are re-evaluated in FP64
+    auto cut2 = [](double asum) {
+        const float c = (float)(1.1 * asum) * 1.001f;
+        return c * c;
+    };
+    a.cut2_ss = cut2(2.0 * a.rseg);
+    a.cut2_sb = cut2(a.rseg + a.rblob);
+    a.cut2_bb = cut2(2.0 * a.rblob);
     // source splits: enough CTAs for ~8 per SM, at least 64 sources each
     const int tgt_ctas = (ntg + kBarrierTpb - 1) / kBarrierTpb;
     int splits = (8 * ctx->sm_count + tgt_ctas - 1) / tgt_ctas;
@@ -761,9 +891,12 @@ gmi_status autotune_pair(gmi_context *ctx, int kind, const void *tgt_rec, int n_
     GMI_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
     PairShape best_shape;
-    for (int si = 0; si < kNumShapes; ++si) {
+    for (int si = 0; si < kNumShapes + 2; ++si) {
+        const bool warp = si >= kNumShapes;
         for (int sp : {0, 1, 2, 4, 8}) {
-            PairShape s{kShapes[si].tpb, kShapes[si].tt, sp};
+            if (warp && sp != 0) continue;
+            PairShape s = warp ? PairShape{kWarpShapeTpb, si - kNumShapes + 1, 0}
+                               : PairShape{kShapes[si].tpb, kShapes[si].tt, sp};
             gmi_status st = launch_pair(ctx, kind, tgt_rec, 0, n_tgt, src_rec, n_src, k, out, 0, &s);
             if (st != GMI_OK) return st;
             GMI_CUDA_TRY(cudaEventRecord(e0, ctx->stream));
@@ -846,6 +979,19 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     if (n_src <= 0) {
         if (!accumulate) GMI_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)n_tgt * nout * sizeof(double), env.stream));
         return GMI_OK;
+    }
+    if (env.tpb == kWarpShapeTpb) {
+        PairLaunch a{};
+        a.tgt_rec = tgt_rec;
+        a.tgt_start = tgt_start;
+        a.n_tgt = n_tgt;
+        a.n_src = n_src;
+        a.k = k;
+        a.out = out;
+        a.accumulate = accumulate;
+        a.err = env.err;
+        a.skip = env.skip;
+        return launch_warp(env.stream, kind, f64, env.tt, a, src_rec);
     }
     const int sidx = shape_index(env.tpb, env.tt);
     const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;

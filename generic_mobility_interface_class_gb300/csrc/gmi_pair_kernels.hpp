@@ -35,9 +35,16 @@ struct BarrierLaunch {
     int nseg;
     double rseg, rblob, scale;
     int wall;
+    float cut2_ss, cut2_sb, cut2_bb;  // squared FP32 screen cutoffs (filled by the launcher)
     int chunk;            // sources per split (filled by the launcher)
     double *partial;      // [splits][targets][3] when there are several splits (filled by the launcher)
 };
+
+// Launch shape with tpb == kPairWarpShapeTpb: the warp-per-target kernel for
+// small source sets (tt = targets per warp, 1 or 2).  Chosen by default for
+// up to kPairWarpMaxSources sources.
+constexpr int kPairWarpShapeTpb = 32;
+constexpr int kPairWarpMaxSources = 2048;
 
 void fill_consts(PairConsts &c, double a_eq, double a_seg, double a_blob, double mu);
 

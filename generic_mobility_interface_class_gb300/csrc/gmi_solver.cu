@@ -14,6 +14,7 @@
 // S = nswim*nfil*nseg segments, B = nswim*nblob blobs, W = nswim.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -391,15 +392,15 @@ __global__ void scale_kernel(int n, const double *__restrict__ x, const double *
 // (an atomic ticket; nobody waits), in a fixed order, so results are
 // deterministic.  Projections use two levels: the last CTA of each group of
 // kSGroup CTAs sums the group, the last group finisher sums the groups.
-//   S1 (CTA per 128 blobs)  q_{k-1} = w / ||w|| into Q; body moments;
+//   S1 (CTA per 64 blobs)   q_{k-1} = w / ||w|| into Q; body moments;
 //                            last CTA: body rows of q and z_body = U
-//   S2 (CTA per 128 blobs)  z_blob; records of z; last CTA: w_body = -K^T z
+//   S2 (CTA per 64 blobs)   z_blob; records of z; last CTA: w_body = -K^T z
 //   pair kernel (+ split reduction) on the records -> mbb
 //   S3 (CTA per kSRows rows) w_blob = M_bb z - K z_body; Q^T w; last: h, H col
 //   S4 (CTA per kSRows rows) w -= Q h; Q^T w; last: h, H col +=
 //   S5 (CTA per kSRows rows) w -= Q h; ||w||^2; last: H(k, k-1), Givens, ctl
 // ---------------------------------------------------------------------------
-constexpr int kSBlobs = 128;  // blobs (threads) per CTA in S1, S2
+constexpr int kSBlobs = 64;   // blobs (threads) per CTA in S1, S2
 constexpr int kSRows = 32;    // rows per CTA in S3-S5
 constexpr int kSTpb = 128;    // threads per CTA in S3-S5
 constexpr int kSGroup = 16;   // CTAs per first-level group of the projection sums
@@ -490,13 +491,13 @@ __global__ void __launch_bounds__(kSBlobs) s1_normalise_moments_kernel(
     if (ctl->done) return;
     const int n = blockIdx.y, m = blockIdx.x * kSBlobs + threadIdx.x, nb = W * nblob;
     double *q = Q + ld * (size_t)(ctl->k - 1);
-    const double nrm = scal[kNormOff];
+    const double nrm = scal[kNormOff], inrm = 1.0 / nrm;
     double a[6] = {0, 0, 0, 0, 0, 0};
     if (m < nblob) {
         const size_t i = (size_t)n * nblob + m;
         double f[3];
         for (int c = 0; c < 3; ++c) {
-            f[c] = w[3 * i + c] / nrm;
+            f[c] = w[3 * i + c] * inrm;
             q[3 * i + c] = f[c];
         }
         double d[3];
@@ -516,7 +517,7 @@ __global__ void __launch_bounds__(kSBlobs) s1_normalise_moments_kernel(
         const double *sums = sh + 6 * s;
         double qb[6];
         for (int c = 0; c < 6; ++c) {
-            qb[c] = w[3 * nb + 6 * s + c] / nrm;
+            qb[c] = w[3 * nb + 6 * s + c] * inrm;
             q[3 * nb + 6 * s + c] = qb[c];
         }
         const double *Kt = ktk_rot + 36 * s, *Mb = mob_rot + 36 * s;
@@ -989,9 +990,14 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     env.err = ctx->d_err;
     env.encode_tiled = ctx->encode_tiled;
     env.sm_count = ctx->sm_count;
-    const bool small = (long long)nb * 2 < (long long)ctx->sm_count * 256;
-    env.tpb = small ? 64 : 128;
-    env.tt = small ? 1 : 2;
+    if (nb <= kPairWarpMaxSources) {
+        env.tpb = kPairWarpShapeTpb;  // warp per two target blobs
+        env.tt = 2;
+    } else {
+        const bool small = (long long)nb * 2 < (long long)ctx->sm_count * 256;
+        env.tpb = small ? 64 : 128;
+        env.tt = small ? 1 : 2;
+    }
     env.skip = &s->ctl->done;
     PairConsts k;
     fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
@@ -1043,7 +1049,11 @@ static gmi_status ensure_arnoldi_graph(gmi_solver *s, int pidx, size_t *nodes)
         cudaGraph_t g = nullptr;
         bool loops = false;
         size_t body_nodes = 0;
-        if (cudaGraphCreate(&g, 0) == cudaSuccess) {
+        // GMI_GMRES_DEVICE_LOOP=0 selects the host-replayed step graph (whose
+        // kernels profilers can attribute one by one)
+        const char *env = std::getenv("GMI_GMRES_DEVICE_LOOP");
+        const bool want_loop = !(env && env[0] == '0');
+        if (want_loop && cudaGraphCreate(&g, 0) == cudaSuccess) {
             cudaGraphConditionalHandle h{};
             cudaGraphNodeParams cp{};
             cp.type = cudaGraphNodeTypeConditional;
@@ -1254,17 +1264,26 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         *iters_out = iters;
         return store_solution(s);
     }
-    // mixed-precision refinement
+    // Mixed-precision refinement.  The residual of the warm start is formed
+    // with the FP64 operator; after each correction delta (solved to 1e-4,
+    // so |A delta| ~ |r|) it is updated as r -= A delta with the FP32C
+    // operator, whose error (~3e-7 |A delta|) stays far below the tolerance.
     GMI_CUDA_TRY(cudaMemcpyAsync(s->b64, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
     int total = 0;
     gmi_status status = GMI_OK;
+    s->ctx->precision = GMI_FP64;
+    status = system_matrix_mult(s, s->soln, s->tmp);
+    s->ctx->precision = prec;
+    if (status != GMI_OK) return status;
+    axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->b64, -1.0, s->tmp, s->rhs);
+    GMI_TRY(launched(s));
     for (int outer = 0; outer < kMaxRefinements; ++outer) {
-        s->ctx->precision = GMI_FP64;
-        status = system_matrix_mult(s, s->soln, s->tmp);
-        s->ctx->precision = prec;
-        if (status != GMI_OK) return status;
-        axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->b64, -1.0, s->tmp, s->rhs);
-        GMI_TRY(launched(s));
+        if (outer > 0) {
+            // r -= A delta (delta in s->z, the last correction)
+            GMI_TRY(system_matrix_mult(s, s->z, s->tmp));
+            axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->rhs, -1.0, s->tmp, s->rhs);
+            GMI_TRY(launched(s));
+        }
         GMI_TRY(device_norm(s, s->rhs, n));
         double beta;
         GMI_TRY(read_scalar(s, s->scal, &beta));
@@ -1284,6 +1303,8 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         int iters = 0;
         GMI_TRY(gmres_run(s, beta, beta, inner_tol, false, true, &iters));
         total += iters;
+        // keep the correction for the residual update, then accumulate it
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->z, s->soln, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
         axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->xacc, 1.0, s->soln, s->soln);
         GMI_TRY(launched(s));
     }

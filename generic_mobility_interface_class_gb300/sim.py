@@ -83,7 +83,9 @@ class Simulation:
 
     @classmethod
     def from_golden(cls, g, **kw):
-        args = dict(nfil=int(g["nfil"]), nseg=int(g["nseg"]), nblob=int(g["nblob"]), blob_refs=g["blob_refs"],
+        args = dict(nswim=int(g["nswim"]) if "nswim" in g else 1,
+                    body_x0=g["body_x0"] if "body_x0" in g else None,
+                    nfil=int(g["nfil"]), nseg=int(g["nseg"]), nblob=int(g["nblob"]), blob_refs=g["blob_refs"],
                     fil_refs=g["fil_refs"], perturbation1=g["perturbation1"], perturbation2=g["perturbation2"],
                     mu=float(g["mu"]), rseg=float(g["rseg"]), rblob=float(g["rblob"]), kb=float(g["kb"]),
                     kt=float(g["kt"]), dt=float(g["dt"]), end_force_magnitude=float(g["end_force_magnitude"]),

@@ -43,6 +43,10 @@ CASES = {
     # small swimmer: 4 filaments x 20 segments on 162 blobs
     "small_swimmer": dict(NFIL="4", NSEG="20", NBLOB="162", R_OVER_L="0.25", RBLOB="1.0", KB="1800.0",
                           KT="1800.0", TOTAL_TIME_STEPS="12", nblob_subdiv=2, fil_subdiv=1, seed=5),
+    # two identical swimmers (the reference places swimmer n at x = 3 n (R + L),
+    # rigid_body.cpp SPHEROID_BODIES branch): the multi-swimmer paths
+    "two_swimmers": dict(NSWIM="2", NFIL="4", NSEG="20", NBLOB="162", R_OVER_L="0.25", RBLOB="1.0", KB="1800.0",
+                         KT="1800.0", TOTAL_TIME_STEPS="8", nblob_subdiv=2, fil_subdiv=1, seed=7),
     # BASELINE config 1 geometry: sphere of radius 10a, 642 blobs (icosphere 3),
     # 16 filaments x 20 segments at random icosphere vertices, GMRES tol 1e-8,
     # Broyden tol 1e-4, 100 steps.  The prescribed preferred-curvature beat of

@@ -41,6 +41,7 @@ def main(case):
         return m.group(1).strip()
 
     nseg, nfil, nblob = int(spec["NSEG"]), int(spec["NFIL"]), int(spec["NBLOB"])
+    nswim = int(spec["NSWIM"])
     DL = 2.2 * float(spec["RSEG"])
     kb = float(macro("KB"))
     dimless = float(macro("DIMENSIONLESS_FORCE"))
@@ -67,8 +68,11 @@ def main(case):
     assert np.allclose(chk_b, blob_refs, rtol=1e-5, atol=1e-5) and np.allclose(chk_f, fil_refs, rtol=1e-5, atol=1e-5)
     out = subprocess.run(["cat", os.path.join(rundir, "stdout.txt")], capture_output=True, text=True).stdout
     broyden = [int(m) for m in re.findall(r"Completed step \d+/\d+ in (\d+) Broyden iterations", out)]
+    # swimmer n starts at x = n * 3 (R + L) (rigid_body.cpp, SPHEROID_BODIES)
+    body_x0 = np.zeros((nswim, 3))
+    body_x0[:, 0] = np.arange(nswim) * 3.0 * (r_over_l * DL * nseg + L)
     data = dict(
-        nfil=nfil, nseg=nseg, nblob=nblob, kb=kb, kt=float(macro("KT")), dt=dt, end_force_magnitude=efm,
+        nswim=nswim, body_x0=body_x0, nfil=nfil, nseg=nseg, nblob=nblob, kb=kb, kt=float(macro("KT")), dt=dt, end_force_magnitude=efm,
         repulsive_force_factor=float(macro("REPULSIVE_FORCE_FACTOR")), rseg=float(spec["RSEG"]),
         rblob=float(spec["RBLOB"]), mu=float(spec["MU"]), body_radius=r_over_l * DL * nseg,
         tol=float(macro("TOL")), linear_tol=float(macro("LINEAR_SYSTEM_TOL")),

@@ -73,8 +73,8 @@ def test_wall_matches_golden(case, prec_ctx):
 
 
 def test_larger_against_oracle(prec_ctx, oracle_built):
-    """Thousands of particles: several TMA tiles, several source splits,
-    ragged last tile; random cube with rejection (config-2 shape)."""
+    """Thousands of particles (the warp-per-target kernel, at most 4096
+    sources); random cube with rejection (config-2 shape)."""
     from generic_mobility_interface_class_gb300 import seeding
     ctx, tol = prec_ctx
     rpy = oracle_built
@@ -86,6 +86,30 @@ def test_larger_against_oracle(prec_ctx, oracle_built):
     assert rel_err(got, want) < tol
     wantb = rpy.mbb(x, f[:, :3])
     assert rel_err(N(ctx.mbb(T(x), T(f[:, :3]))), wantb) < tol
+
+
+def test_tiled_kernel_against_oracle(prec_ctx, oracle_built):
+    """More than 4096 sources (the TMA-tiled kernel): several tiles, several
+    source splits, a ragged last tile; every pair kind, including the
+    unequal-radius segment/blob couplings."""
+    from generic_mobility_interface_class_gb300 import seeding
+    ctx, tol = prec_ctx
+    rpy = oracle_built
+    n = 5003
+    x = seeding.random_cube(n, seed=11)
+    f = np.random.default_rng(11).normal(size=(n, 6))
+    assert rel_err(N(ctx.mss(T(x), T(f))), rpy.mss(x, f)) < tol
+    assert rel_err(N(ctx.mbb(T(x), T(f[:, :3]))), rpy.mbb(x, f[:, :3])) < tol
+    # 700 segments against 5003 blobs (radii 1 and 1.4, all three branches
+    # occur in a dense cloud) and 700 blobs against 5003 segments
+    xs = x[:700] + 0.37
+    v_in = np.random.default_rng(12).normal(size=(700, 6))
+    v = T(v_in)
+    ctx.msb(T(xs), T(x), T(f[:, :3]), v, a_seg=1.0, a_blob=1.4)
+    want = rpy.msb(xs, x, f[:, :3], a_seg=1.0, a_blob=1.4, v_in=v_in)
+    assert rel_err(N(v), want) < tol
+    got = N(ctx.mbs(T(xs), T(x), T(f), a_seg=1.0, a_blob=1.4))
+    assert rel_err(got, rpy.mbs(xs, x, f, a_seg=1.0, a_blob=1.4)) < tol
 
 
 def test_target_slices_and_accumulate(gpu_ctx, oracle_built):
