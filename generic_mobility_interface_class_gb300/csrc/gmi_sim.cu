@@ -41,6 +41,7 @@ namespace gmi {
 
 struct SimP {
     int W, NF, NS, NB, F, S, nbroy, per_body, n6, neuler;
+    int wall;  // filaments on an infinite no-slip wall: no body unknowns (INFINITE_PLANE_WALL)
     double DL, DT, KB, KT, MU, RSEG, EFM, TOL, Rbody, conf;
     // segment state
     double *x, *f, *v;  // solver arrays: x_segs, f_segs, v_segs
@@ -988,8 +989,8 @@ __global__ void __launch_bounds__(128) jim_fil_kernel(SimP P, const double *in, 
     const size_t base = (size_t)n * P.per_body + (size_t)6 * P.NS * i;
     const double *ub = out + (size_t)n * P.per_body + 6 * P.NF * P.NS;
     for (int row = threadIdx.x * 3; row < n6; row += 3 * 128) {
-        double a3[3];
-        A_apply(P, fil, ub, row, a3);
+        double a3[3] = {0.0, 0.0, 0.0};
+        if (!P.wall) A_apply(P, fil, ub, row, a3);  // the wall branch is invJ_f in_f (swimmer.cpp:696-702)
         for (int c = 0; c < 3; ++c) rhs[row + c] = in[base + row + c] - a3[c];
     }
     __syncthreads();
@@ -1149,6 +1150,7 @@ static gmi_status read_flags(gmi_sim *m)
 static gmi_status forces_and_torques(gmi_sim *m, int nt)
 {
     filament_forces_kernel<<<gridN(m->P.F, 64), 64, 0, sst(m)>>>(m->P, nt);
+    if (m->P.wall) return sim_launched(m);
     swimmer_force_sum_kernel<<<m->P.W, 256, 0, sst(m)>>>(m->P);
     return sim_launched(m, 2);
 }
@@ -1159,7 +1161,8 @@ static gmi_status velocities_and_errors(gmi_sim *m, int nt, double *err_out, boo
 {
     GMI_TRY(solver_compute_velocities_device(m->solver, gmres_iters));
     GMI_CUDA_TRY(cudaMemsetAsync(m->P.flags, 0, 3 * sizeof(int), sst(m)));
-    compute_errors_kernel<<<gridN(m->P.S + m->P.W), 128, 0, sst(m)>>>(m->P, nt, err_out);
+    const int rows = m->P.S + (m->P.wall ? 0 : m->P.W);  // the wall has no body equations
+    compute_errors_kernel<<<gridN(rows), 128, 0, sst(m)>>>(m->P, nt, err_out);
     GMI_TRY(sim_launched(m));
     GMI_TRY(read_flags(m));
     *too_large = m->h_flags[0] != 0;
@@ -1184,10 +1187,12 @@ static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
     }
     GMI_CUDA_TRY(cudaFuncSetAttribute(gj_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     gj_invert_kernel<<<P.F, kGjTpb, smem, sst(m)>>>(P.invJ, P.n6, use_smem, P.flags);
-    filament_B_kernel<<<P.F, 128, 6 * P.n6 * sizeof(double), sst(m)>>>(P, nt);
-    schur_filament_kernel<<<P.F, 32, 0, sst(m)>>>(P, m->spart);
-    swimmer_schur_kernel<<<P.W, 64, 0, sst(m)>>>(P, nt, m->spart);
-    GMI_TRY(sim_launched(m, 5));
+    if (!P.wall) {  // the body coupling (swimmer.cpp:466-682); none on the wall
+        filament_B_kernel<<<P.F, 128, 6 * P.n6 * sizeof(double), sst(m)>>>(P, nt);
+        schur_filament_kernel<<<P.F, 32, 0, sst(m)>>>(P, m->spart);
+        swimmer_schur_kernel<<<P.W, 64, 0, sst(m)>>>(P, nt, m->spart);
+    }
+    GMI_TRY(sim_launched(m, P.wall ? 2 : 5));
     GMI_TRY(read_flags(m));
     if (m->h_flags[2]) {
         set_last_error_msg("the approximate Jacobian is singular (matrix.cpp:549-554 stops the reference here)");
@@ -1199,6 +1204,10 @@ static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
 static gmi_status jacobian_inv_mult(gmi_sim *m, const double *in, double *out)
 {
     const SimP &P = m->P;
+    if (P.wall) {
+        jim_fil_kernel<<<P.F, 128, P.n6 * sizeof(double), sst(m)>>>(P, in, out);
+        return sim_launched(m);
+    }
     jim_partial_kernel<<<P.F, 128, 0, sst(m)>>>(P, in, m->jpart);
     jim_body_kernel<<<P.W, 32, 0, sst(m)>>>(P, in, m->jpart, out);
     jim_fil_kernel<<<P.F, 128, P.n6 * sizeof(double), sst(m)>>>(P, in, out);
@@ -1252,9 +1261,9 @@ static gmi_status end_of_iter(gmi_sim *m, bool too_large)
 // swimmer::update (swimmer.cpp:847-871)
 static gmi_status swimmer_update(gmi_sim *m)
 {
-    body_update_kernel<<<gridN(m->P.W, 32), 32, 0, sst(m)>>>(m->P, m->upd);
+    if (!m->P.wall) body_update_kernel<<<gridN(m->P.W, 32), 32, 0, sst(m)>>>(m->P, m->upd);
     filament_update_kernel<<<gridN(m->P.F, 64), 64, 0, sst(m)>>>(m->P, m->upd);
-    return sim_launched(m, 2);
+    return sim_launched(m, m->P.wall ? 1 : 2);
 }
 
 }  // namespace gmi
@@ -1288,14 +1297,22 @@ gmi_status gmi_sim_destroy(gmi_sim *m)
 gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, const double *fil_refs,
                           const double *body_x0, const double *perturb1, const double *perturb2, gmi_sim **out)
 {
-    SIM_ARG_CHECK(cfg && out && fil_refs && body_x0, "gmi_sim_create: null argument");
+    SIM_ARG_CHECK(cfg && out && fil_refs, "gmi_sim_create: null argument");
     *out = nullptr;
     const gmi_solver_config &mc = cfg->mobility;
-    SIM_ARG_CHECK(!mc.wall, "gmi_sim_create: the time step covers free-swimming bodies (no wall configuration)");
-    SIM_ARG_CHECK(mc.nfil >= 1 && mc.nseg >= 2 && mc.nblob >= 1 && mc.nswim >= 1, "gmi_sim_create: bad sizes");
-    SIM_ARG_CHECK(blob_refs != nullptr, "gmi_sim_create: null blob references");
-    SIM_ARG_CHECK(cfg->dt > 0 && cfg->kb > 0 && cfg->kt > 0 && cfg->body_radius > 0,
-                  "gmi_sim_create: dt, kb, kt and body_radius must be positive");
+    const bool wall = mc.wall != 0;
+    if (wall) {
+        // filaments standing on the wall z = 0 (config.hpp:276-287): one
+        // "swimmer", no blobs, the body fixed at the origin
+        SIM_ARG_CHECK(mc.nswim == 1 && mc.nblob == 0 && mc.nfil >= 1 && mc.nseg >= 2,
+                      "gmi_sim_create: the wall configuration has nswim = 1, nblob = 0");
+    } else {
+        SIM_ARG_CHECK(body_x0 != nullptr, "gmi_sim_create: null body positions");
+        SIM_ARG_CHECK(mc.nfil >= 1 && mc.nseg >= 2 && mc.nblob >= 1 && mc.nswim >= 1, "gmi_sim_create: bad sizes");
+        SIM_ARG_CHECK(blob_refs != nullptr, "gmi_sim_create: null blob references");
+        SIM_ARG_CHECK(cfg->body_radius > 0, "gmi_sim_create: body_radius must be positive");
+    }
+    SIM_ARG_CHECK(cfg->dt > 0 && cfg->kb > 0 && cfg->kt > 0, "gmi_sim_create: dt, kb and kt must be positive");
     gmi_sim *m = new (std::nothrow) gmi_sim();
     SIM_ARG_CHECK(m != nullptr, "gmi_sim_create: out of host memory");
     m->cfg = *cfg;
@@ -1313,7 +1330,8 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
     P.NB = mc.nblob;
     P.F = P.W * P.NF;
     P.S = P.F * P.NS;
-    P.per_body = 6 * P.NF * P.NS + 6;
+    P.wall = wall ? 1 : 0;
+    P.per_body = 6 * P.NF * P.NS + (wall ? 0 : 6);
     P.nbroy = P.W * P.per_body;
     P.n6 = 6 * P.NS;
     P.neuler = cfg->num_euler_steps > 0 ? cfg->num_euler_steps : 1;
@@ -1403,7 +1421,7 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
     std::vector<double> hx(3 * S), hq(4 * S), hbx(3 * W), hbq(4 * W, 0.0), hfref(3 * F), hp1(3 * F, 0.0),
         hp2(3 * F, 0.0);
     for (size_t n = 0; n < W; ++n) {
-        for (int c = 0; c < 3; ++c) hbx[3 * n + c] = body_x0[3 * n + c];
+        for (int c = 0; c < 3; ++c) hbx[3 * n + c] = wall || !body_x0 ? 0.0 : body_x0[3 * n + c];
         hbq[4 * n] = 1.0;
     }
     for (size_t fil = 0; fil < F; ++fil) {
@@ -1414,8 +1432,9 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
             for (int c = 0; c < 3; ++c) hp1[3 * fil + c] = perturb1[3 * fil + c];
         if (perturb2)
             for (int c = 0; c < 3; ++c) hp2[3 * fil + c] = perturb2[3 * fil + c];
+        // radial on a sphere; along +z on the wall (swimmer.cpp:82)
         const double nrm = std::sqrt(dref[0] * dref[0] + dref[1] * dref[1] + dref[2] * dref[2]);
-        const double dir[3] = {dref[0] / nrm, dref[1] / nrm, dref[2] / nrm};
+        const double dir[3] = {wall ? 0.0 : dref[0] / nrm, wall ? 0.0 : dref[1] / nrm, wall ? 1.0 : dref[2] / nrm};
         Q4 qt{dir[0], 0.0, -dir[2], dir[1]};
         qsqrt_in_place(qt);
         double pos[3] = {hbx[3 * n] + dref[0], hbx[3 * n + 1] + dref[1], hbx[3 * n + 2] + dref[2]};
@@ -1441,10 +1460,12 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
         gmi_sim_destroy(m);
         return st;
     }
-    st = gmi_solver_set_blob_references(s, blob_refs);
-    if (st != GMI_OK) {
-        gmi_sim_destroy(m);
-        return st;
+    if (!wall) {
+        st = gmi_solver_set_blob_references(s, blob_refs);
+        if (st != GMI_OK) {
+            gmi_sim_destroy(m);
+            return st;
+        }
     }
     *out = m;
     return GMI_OK;
@@ -1458,7 +1479,12 @@ gmi_status gmi_sim_prepare(gmi_sim *m, double *body_mobility_out)
 {
     SIM_ARG_CHECK(m != nullptr, "gmi_sim_prepare: null simulation");
     GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
-    double mob[36];
+    double mob[36] = {0};
+    if (m->P.wall) {  // prescribed (zero) body velocity: no reference matrices
+        if (body_mobility_out) std::memcpy(body_mobility_out, mob, sizeof mob);
+        m->prepared = true;
+        return GMI_OK;
+    }
     GMI_TRY(solver_make_body_reference_matrices_device(m->solver, nullptr, mob));
     GMI_CUDA_TRY(cudaMemcpy(m->P.mob_ref, mob, sizeof mob, cudaMemcpyHostToDevice));
     if (body_mobility_out) std::memcpy(body_mobility_out, mob, sizeof mob);
@@ -1473,9 +1499,9 @@ gmi_status gmi_sim_step(gmi_sim *m, int nt, int *broyden_iters, int *gmres_iters
     SIM_ARG_CHECK(m->prepared, "gmi_sim_step: call gmi_sim_prepare first");
     GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
     const SimP &P = m->P;
-    body_initial_guess_kernel<<<gridN(P.W, 32), 32, 0, sst(m)>>>(P, nt);
+    if (!P.wall) body_initial_guess_kernel<<<gridN(P.W, 32), 32, 0, sst(m)>>>(P, nt);
     filament_initial_guess_kernel<<<gridN(P.F, 64), 64, 0, sst(m)>>>(P, nt);
-    GMI_TRY(sim_launched(m, 2));
+    GMI_TRY(sim_launched(m, P.wall ? 1 : 2));
     GMI_TRY(forces_and_torques(m, nt));
     int gi = 0, gtot = 0;
     bool too_large = false, nonfinite = false;

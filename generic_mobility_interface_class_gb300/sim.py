@@ -22,10 +22,11 @@ class Simulation:
     def __init__(self, *, nswim=1, nfil, nseg, nblob, blob_refs, fil_refs, body_x0=None, perturbation1=None,
                  perturbation2=None, mu=1.0, rseg=1.0, rblob=1.0, kb, kt, dt, end_force_magnitude,
                  repulsive_force_factor=2.0, body_radius, tol=1e-4, max_broyden_iter=100, jacobian_confidence=0.1,
-                 num_euler_steps=1, linear_tol=1e-10, max_linear_iter=150, precision=GMI_FP64, device=0):
+                 num_euler_steps=1, linear_tol=1e-10, max_linear_iter=150, precision=GMI_FP64, device=0,
+                 wall=False):
         self.lib = _lib.load()
-        mob = SolverConfig(nswim, nfil, nseg, nblob, mu, rseg, rblob, repulsive_force_factor, end_force_magnitude, 0,
-                           max_linear_iter, linear_tol, precision, device)
+        mob = SolverConfig(nswim, nfil, nseg, nblob, mu, rseg, rblob, repulsive_force_factor, end_force_magnitude,
+                           int(wall), max_linear_iter, linear_tol, precision, device)
         cfg = SimConfig(mob, kb, kt, dt, num_euler_steps, max_broyden_iter, tol, jacobian_confidence, body_radius)
         F = nswim * nfil
         self.nswim, self.nfil, self.nseg, self.nblob = nswim, nfil, nseg, nblob
@@ -38,6 +39,7 @@ class Simulation:
             p = np.asarray(p, dtype=np.float64)
             return np.tile(p.reshape(1, 3), (F, 1)) if p.size == 3 else p.reshape(F, 3)
 
+        blob_refs = np.zeros((0, 3)) if blob_refs is None else blob_refs
         arrays = [_c(blob_refs), _c(fil_refs), _c(body_x0), _c(per_fil(perturbation1)), _c(per_fil(perturbation2))]
         h = ctypes.c_void_p()
         check(self.lib.gmi_sim_create(ctypes.byref(cfg), *[p for _, p in arrays], ctypes.byref(h)))
@@ -83,7 +85,8 @@ class Simulation:
 
     @classmethod
     def from_golden(cls, g, **kw):
-        args = dict(nswim=int(g["nswim"]) if "nswim" in g else 1,
+        args = dict(wall=bool(g["wall"]) if "wall" in g else False,
+                    nswim=int(g["nswim"]) if "nswim" in g else 1,
                     body_x0=g["body_x0"] if "body_x0" in g else None,
                     nfil=int(g["nfil"]), nseg=int(g["nseg"]), nblob=int(g["nblob"]), blob_refs=g["blob_refs"],
                     fil_refs=g["fil_refs"], perturbation1=g["perturbation1"], perturbation2=g["perturbation2"],

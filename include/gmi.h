@@ -282,7 +282,11 @@ typedef enum gmi_state_field {
  * (body frame, scaled), fil_refs[3*nfil] (filament base relative to the body
  * centre, scaled; the filament stands along it), body_x0[3*nswim];
  * perturb1/perturb2[3*F] (or NULL) are added to segments 4 and 12 at step 0
- * (filament.cpp:1181-1196). */
+ * (filament.cpp:1181-1196).
+ * With cfg->mobility.wall set: filaments on the infinite no-slip wall z = 0
+ * (INFINITE_PLANE_WALL, swimmer.cpp:68-110): nswim = 1, nblob = 0,
+ * blob_refs and body_x0 may be NULL, fil_refs are the base points and every
+ * filament stands along +z; no body unknowns, no linear solve. */
 GMI_API gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, const double *fil_refs,
                                   const double *body_x0, const double *perturb1, const double *perturb2,
                                   gmi_sim **out);

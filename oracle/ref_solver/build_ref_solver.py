@@ -47,6 +47,11 @@ CASES = {
     # rigid_body.cpp SPHEROID_BODIES branch): the multi-swimmer paths
     "two_swimmers": dict(NSWIM="2", NFIL="4", NSEG="20", NBLOB="162", R_OVER_L="0.25", RBLOB="1.0", KB="1800.0",
                          KT="1800.0", TOTAL_TIME_STEPS="8", nblob_subdiv=2, fil_subdiv=1, seed=7),
+    # filaments on an infinite no-slip wall (INFINITE_PLANE_WALL): a 3 x 3
+    # rectangular grid of 20-segment filaments, Swan-Brady wall mobility, no
+    # rigid body and no linear solve
+    "wall_filaments": dict(BODY_OR_SURFACE_TYPE="0", NFIL="9", NSEG="20", NBLOB="0", R_OVER_L="0.25",
+                           RBLOB="1.0", TOTAL_TIME_STEPS="10", seed=3),
     # BASELINE config 1 geometry: sphere of radius 10a, 642 blobs (icosphere 3),
     # 16 filaments x 20 segments at random icosphere vertices, GMRES tol 1e-8,
     # Broyden tol 1e-4, 100 steps.  The prescribed preferred-curvature beat of
@@ -104,6 +109,29 @@ def build(case: str) -> str:
     return exe
 
 
+def is_wall(case: str) -> bool:
+    return CASES[case].get("BODY_OR_SURFACE_TYPE", COMMON["BODY_OR_SURFACE_TYPE"]) == "0"
+
+
+def wall_filament_bases(nfil: int, nseg: int, dl: float = 2.2):
+    """The reference's rectangular grid of filament bases on the wall
+    (swimmer.cpp:68-110, RECTANGULAR_SEEDING): step 1.4 L, height DL / 2."""
+    import math
+    import numpy as np
+    L = dl * nseg
+    gx = int(math.sqrt(float(nfil)))
+    gy = max(1, int(math.ceil(nfil / float(gx))))
+    step = 1.4 * L
+    im, jm = 0.5 * (gx - 1.0), 0.5 * (gy - 1.0)
+    out = np.zeros((nfil, 3))
+    for i in range(gx):
+        for j in range(gy):
+            f = j + i * gy
+            if f < nfil:
+                out[f] = [(i - im) * step, (j - jm) * step, 0.5 * dl]
+    return out
+
+
 def seeds(case: str):
     """Unit-sphere seeds: blobs on an icosphere, filaments at random icosphere vertices."""
     import numpy as np
@@ -125,11 +153,12 @@ def run_case(case: str, exe: str | None = None) -> str:
     os.makedirs(rundir, exist_ok=True)
     for f in os.listdir(rundir):
         os.remove(os.path.join(rundir, f))
-    blobs, fils = seeds(case)
     spec = CASES[case]
-    assert spec["NBLOB"] != spec["NFIL"]
-    np.savetxt(os.path.join(rundir, f"sphere{spec['NBLOB']}.seed"), blobs.ravel()[None, :], fmt="%.17g")
-    np.savetxt(os.path.join(rundir, f"sphere{spec['NFIL']}.seed"), fils.ravel()[None, :], fmt="%.17g")
+    if not is_wall(case):  # spheres read their seeds; the wall seeds a grid itself
+        blobs, fils = seeds(case)
+        assert spec["NBLOB"] != spec["NFIL"]
+        np.savetxt(os.path.join(rundir, f"sphere{spec['NBLOB']}.seed"), blobs.ravel()[None, :], fmt="%.17g")
+        np.savetxt(os.path.join(rundir, f"sphere{spec['NFIL']}.seed"), fils.ravel()[None, :], fmt="%.17g")
     r = subprocess.run([exe], cwd=rundir, capture_output=True, text=True)
     with open(os.path.join(rundir, "stdout.txt"), "w") as fh:
         fh.write(r.stdout)

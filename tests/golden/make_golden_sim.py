@@ -59,20 +59,35 @@ def main(case):
     # precision (6 digits); rebuild the exact values the way it does: unit
     # seeds times Rsphere (rigid_body.cpp:200, 231) and times
     # R_OVER_L*L + 1.05*(0.5*DL + RBLOB) for the filament bases (swimmer.cpp:172, 199).
-    blobs, fils = brs.seeds(case)
-    L = DL * nseg
-    blob_refs = blobs * (r_over_l * DL * nseg)
-    fil_refs = fils * (r_over_l * L + 1.05 * (0.5 * DL + float(spec["RBLOB"])))
-    chk_b = parse_dat(os.path.join(rundir, "test_blob_references.dat"), 0).reshape(-1, 3)
-    chk_f = parse_dat(os.path.join(rundir, "test_fil_references.dat"), 0).reshape(-1, 3)
-    assert np.allclose(chk_b, blob_refs, rtol=1e-5, atol=1e-5) and np.allclose(chk_f, fil_refs, rtol=1e-5, atol=1e-5)
     out = subprocess.run(["cat", os.path.join(rundir, "stdout.txt")], capture_output=True, text=True).stdout
     broyden = [int(m) for m in re.findall(r"Completed step \d+/\d+ in (\d+) Broyden iterations", out)]
+    L = DL * nseg
+    wall = brs.is_wall(case)
+    if wall:
+        # filaments on the wall: the reference's rectangular grid, no body
+        nswim, nblob = 1, 0
+        blob_refs = np.zeros((0, 3))
+        fil_refs = brs.wall_filament_bases(nfil, nseg, DL)
+    else:
+        blobs, fils = brs.seeds(case)
+        blob_refs = blobs * (r_over_l * DL * nseg)
+        fil_refs = fils * (r_over_l * L + 1.05 * (0.5 * DL + float(spec["RBLOB"])))
+        chk_b = parse_dat(os.path.join(rundir, "test_blob_references.dat"), 0).reshape(-1, 3)
+        assert np.allclose(chk_b, blob_refs, rtol=1e-5, atol=1e-5)
+    chk_f = parse_dat(os.path.join(rundir, "test_fil_references.dat"), 0).reshape(-1, 3)
+    assert np.allclose(chk_f, fil_refs, rtol=1e-5, atol=1e-5)
+
     # swimmer n starts at x = n * 3 (R + L) (rigid_body.cpp, SPHEROID_BODIES)
     body_x0 = np.zeros((nswim, 3))
     body_x0[:, 0] = np.arange(nswim) * 3.0 * (r_over_l * DL * nseg + L)
+    def dat(name, ncols):
+        path = os.path.join(rundir, name)
+        if os.path.exists(path):
+            return parse_dat(path)
+        return np.zeros((len(broyden), ncols))  # not written for the wall (mobility_solver.cpp:1786-1879)
+
     data = dict(
-        nswim=nswim, body_x0=body_x0, nfil=nfil, nseg=nseg, nblob=nblob, kb=kb, kt=float(macro("KT")), dt=dt, end_force_magnitude=efm,
+        wall=int(wall), nswim=nswim, body_x0=body_x0, nfil=nfil, nseg=nseg, nblob=nblob, kb=kb, kt=float(macro("KT")), dt=dt, end_force_magnitude=efm,
         repulsive_force_factor=float(macro("REPULSIVE_FORCE_FACTOR")), rseg=float(spec["RSEG"]),
         rblob=float(spec["RBLOB"]), mu=float(spec["MU"]), body_radius=r_over_l * DL * nseg,
         tol=float(macro("TOL")), linear_tol=float(macro("LINEAR_SYSTEM_TOL")),
@@ -80,10 +95,10 @@ def main(case):
         blob_refs=blob_refs, fil_refs=fil_refs,
         perturbation1=p[0], perturbation2=p[1],
         seg_q=parse_dat(os.path.join(rundir, "test_seg_states.dat")),
-        body_state=parse_dat(os.path.join(rundir, "test_body_states.dat")),
+        body_state=dat("test_body_states.dat", 7 * nswim),
         seg_v=parse_dat(os.path.join(rundir, "test_seg_vels.dat")),
-        body_v=parse_dat(os.path.join(rundir, "test_body_vels.dat")),
-        blob_f=parse_dat(os.path.join(rundir, "test_blob_forces.dat")),
+        body_v=dat("test_body_vels.dat", 6 * nswim),
+        blob_f=dat("test_blob_forces.dat", 3 * nblob * nswim),
         broyden_iters=np.array(broyden),
         backup=parse_dat(os.path.join(rundir, "test.backup")),
     )

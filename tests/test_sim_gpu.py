@@ -5,7 +5,8 @@ cilia_sim_main.cpp and solver classes compiled for the CPU
 (tests/golden/make_golden_sim.py): small_swimmer, one free-swimming sphere of
 162 blobs with 4 end-force-driven filaments of 20 segments, 12 steps (Euler,
 then BDF2 with both multiplier-extrapolation stages); two_swimmers, two such
-swimmers, 8 steps; config1, 642 blobs and 16 x 20 segments, 100 steps (every
+swimmers, 8 steps; wall_filaments, nine filaments on an infinite no-slip wall
+(INFINITE_PLANE_WALL), 10 steps; config1, 642 blobs and 16 x 20 segments, 100 steps (every
 10th stored).  Every stored step is compared: Broyden
 iteration count, segment quaternions, body position and orientation, segment
 and body velocities.  Differences come from GMRES (CGS2 vs MGS Arnoldi,
@@ -31,6 +32,7 @@ def run_against_golden(case, state_tol, vel_tol, precision=0, doubling_steps=Non
     at the GMRES tolerance grow while the filaments' instability develops."""
     from generic_mobility_interface_class_gb300.sim import Simulation
     g = load_golden(case, prefix="sim_")
+    wall = bool(g["wall"]) if "wall" in g else False
     sim = Simulation.from_golden(g, precision=precision)
     sim.prepare()
     kept = {int(s): k for k, s in enumerate(g["steps"])}
@@ -44,9 +46,10 @@ def run_against_golden(case, state_tol, vel_tol, precision=0, doubling_steps=Non
         k = kept[nt]
         grow = 2.0 ** (nt / doubling_steps) if doubling_steps else 1.0
         err = {"q": rel_err(sim.state("seg_q").ravel(), g["seg_q"][k])}
-        bs = np.concatenate([sim.state("body_x").ravel(), sim.state("body_q").ravel()])
+        # the reference writes each swimmer's body state as x (3) then q (4)
+        bs = np.hstack([sim.state("body_x"), sim.state("body_q")]).ravel()
         err["body"] = float(np.max(np.abs(bs - g["body_state"][k])))
-        err["body_v"] = rel_err(sim.state("body_v").ravel(), g["body_v"][k])
+        err["body_v"] = 0.0 if wall else rel_err(sim.state("body_v").ravel(), g["body_v"][k])
         err["v"] = max(rel_err(sim.state("seg_v").ravel(), g["seg_v"][k]), err["body_v"])
         for key in worst:
             worst[key] = max(worst[key], err[key])
@@ -66,6 +69,12 @@ def test_two_swimmers_match_reference(gmi_lib):
     the reference places them), 8 steps: the per-swimmer offsets of every
     kernel of the time step, and the preconditioner's Minv^(W - n) scaling."""
     run_against_golden("two_swimmers", TRAJ_TOL, VEL_TOL)
+
+
+def test_wall_filaments_match_reference(gmi_lib):
+    """Nine filaments on the infinite no-slip wall (Swan-Brady mobility,
+    wall barrier, no rigid body, no linear solve), 10 steps."""
+    run_against_golden("wall_filaments", TRAJ_TOL, VEL_TOL)
 
 
 def test_config1_100_steps_match_reference(gmi_lib):
