@@ -467,15 +467,27 @@ template <int TPB> __device__ __forceinline__ void block_sum6(const double *v, d
 }
 
 // Sum over the gx per-CTA 6-vectors of each swimmer (part[(n*gx + x)*6 + c])
-// into sh[6n + c], in x order; one thread per (swimmer, component), loads
-// unrolled so they are in flight together.
+// into sh[6n + c], in x order.  The CTA first copies the partials into
+// shared memory (stage, kStageMax doubles) with coalesced loads, so the
+// sequential sums read no global memory; one thread per (swimmer, component).
+constexpr int kStageMax = 4096;
 __device__ __forceinline__ void swimmer_sums(const double *part, int W, int gx, double *sh)
 {
+    __shared__ double stage[kStageMax];
+    const int total = 6 * W * gx;
+    const bool staged = total <= kStageMax;
+    if (staged)
+        for (int e = threadIdx.x; e < total; e += blockDim.x) stage[e] = __ldcg(part + e);
+    __syncthreads();
     for (int e = threadIdx.x; e < 6 * W; e += blockDim.x) {
-        const double *p = part + (size_t)(e / 6) * gx * 6 + (e % 6);
+        const int off = (e / 6) * gx * 6 + (e % 6);
         double t = 0.0;
+        if (staged) {
+            for (int x = 0; x < gx; ++x) t += stage[off + 6 * x];
+        } else {
 #pragma unroll 8
-        for (int x = 0; x < gx; ++x) t += __ldcg(p + 6 * (size_t)x);
+            for (int x = 0; x < gx; ++x) t += __ldcg(part + off + 6 * (size_t)x);
+        }
         sh[e] = t;
     }
     __syncthreads();

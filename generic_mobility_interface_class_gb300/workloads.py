@@ -102,3 +102,40 @@ WORKLOADS = {
     "config1": ("1 swimmer, R=10a, 642 icosphere blobs, 16 x 20 segments (962 particles)", config1),
     "config3": ("1 swimmer, R=40a, 4096 Fibonacci blobs, 640 x 20 segments (16,896 particles)", config3),
 }
+
+
+def main(argv=None) -> None:
+    """Run a seeded workload through the device time step and print, per
+    step, the Broyden and GMRES iteration counts and the wall time:
+
+        python -m generic_mobility_interface_class_gb300.workloads config3 --precision fp32c --steps 3
+    """
+    import argparse
+    import time
+
+    from . import build
+    from ._lib import GMI_FP32C, GMI_FP64
+    from .sim import Simulation
+
+    p = argparse.ArgumentParser(prog="python -m generic_mobility_interface_class_gb300.workloads")
+    p.add_argument("workload", choices=sorted(WORKLOADS))
+    p.add_argument("--precision", choices=["fp64", "fp32c"], default="fp32c")
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--device", type=int, default=0)
+    args = p.parse_args(argv)
+    build.build()
+    desc, make = WORKLOADS[args.workload]
+    sim = Simulation(**make(), precision=GMI_FP32C if args.precision == "fp32c" else GMI_FP64, device=args.device)
+    t0 = time.perf_counter()
+    sim.prepare()
+    print(f"{args.workload} ({desc}), {args.precision}: prepare {1e3 * (time.perf_counter() - t0):.1f} ms", flush=True)
+    for nt in range(args.steps):
+        t0 = time.perf_counter()
+        b, g = sim.step(nt)
+        print(f"step {nt}: {b} Broyden iterations, {g} GMRES iterations, {1e3 * (time.perf_counter() - t0):.1f} ms",
+              flush=True)
+    sim.close()
+
+
+if __name__ == "__main__":
+    main()
