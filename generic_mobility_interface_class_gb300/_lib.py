@@ -85,6 +85,9 @@ SIGNATURES = {
     "gmi_sim_prepare": ([_P, _P], _I),
     "gmi_sim_step": ([_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
     "gmi_sim_get_state": ([_P, _I, _P], _I),
+    "gmi_sim_backup_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "gmi_sim_export_backup": ([_P, _P], _I),
+    "gmi_sim_import_backup": ([_P, _P], _I),
 }
 
 

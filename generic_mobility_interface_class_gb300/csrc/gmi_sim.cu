@@ -1106,6 +1106,7 @@ struct gmi_sim {
     double *C = nullptr, *D = nullptr, *err = nullptr, *nerr = nullptr, *upd = nullptr, *tmp = nullptr;
     double *dots = nullptr, *part = nullptr, *jpart = nullptr, *scal = nullptr;
     double *spart = nullptr;  // per-filament parts of the Schur complement (45 each)
+    double *f_internal = nullptr;  // segment forces before the barrier (the reference's f_segs_host)
     int *h_flags = nullptr;
     std::vector<void *> allocs;
     bool prepared = false;
@@ -1150,6 +1151,10 @@ static gmi_status read_flags(gmi_sim *m)
 static gmi_status forces_and_torques(gmi_sim *m, int nt)
 {
     filament_forces_kernel<<<gridN(m->P.F, 64), 64, 0, sst(m)>>>(m->P, nt);
+    // the host copy of the segment forces never receives the barrier forces
+    // (mobility_solver.cpp:132-192); keep it for the writers
+    GMI_CUDA_TRY(cudaMemcpyAsync(m->f_internal, m->P.f, 6 * (size_t)m->P.S * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, sst(m)));
     if (m->P.wall) return sim_launched(m);
     swimmer_force_sum_kernel<<<m->P.W, 256, 0, sst(m)>>>(m->P);
     return sim_launched(m, 2);
@@ -1278,6 +1283,68 @@ using namespace gmi;
         }                            \
     } while (0)
 
+namespace {
+
+struct BackupHost {
+    std::vector<double> q, x, xm1, xm2, u, um1, tl, tl1, tl2, cl, cl1, cl2, lam, lam1, lam2;
+    std::vector<double> bq, bx, bxm1, bxm2, bu, bum1;
+};
+
+size_t per_fil_count(const SimP &P) { return 9 + 28 * (size_t)P.NS; }
+size_t per_swimmer_count(const SimP &P) { return 19 + (size_t)P.NF * per_fil_count(P); }
+
+// pairs (device array, host vector) of everything the backup holds
+template <class F> gmi_status for_each_field(const SimP &P, BackupHost &h, F &&fn)
+{
+    const size_t S = P.S, F_ = P.F, W = P.W, nl = 3 * (size_t)(P.NS - 1) * F_;
+    struct Field {
+        double *d;
+        std::vector<double> *h;
+        size_t n;
+    } f[] = {{P.q, &h.q, 4 * S},       {P.x, &h.x, 3 * S},       {P.xm1, &h.xm1, 3 * S},  {P.xm2, &h.xm2, 3 * S},
+             {P.u, &h.u, 3 * S},       {P.um1, &h.um1, 3 * S},   {P.tl, &h.tl, 3 * F_},   {P.tl1, &h.tl1, 3 * F_},
+             {P.tl2, &h.tl2, 3 * F_},  {P.cl, &h.cl, 3 * F_},    {P.cl1, &h.cl1, 3 * F_}, {P.cl2, &h.cl2, 3 * F_},
+             {P.lam, &h.lam, nl},      {P.lam1, &h.lam1, nl},    {P.lam2, &h.lam2, nl},   {P.bq, &h.bq, 4 * W},
+             {P.bx, &h.bx, 3 * W},     {P.bxm1, &h.bxm1, 3 * W}, {P.bxm2, &h.bxm2, 3 * W}, {P.bu, &h.bu, 3 * W},
+             {P.bum1, &h.bum1, 3 * W}};
+    for (auto &e : f) {
+        gmi_status st = fn(e.d, *e.h, e.n);
+        if (st != GMI_OK) return st;
+    }
+    return GMI_OK;
+}
+
+// Walk the backup order; op(value_in_backup, host_slot) for every entry.
+template <class Op> void walk_backup(const SimP &P, BackupHost &h, Op &&op)
+{
+    const int NS = P.NS;
+    for (int n = 0; n < P.W; ++n) {
+        for (int i = 0; i < P.NF; ++i) {
+            const int fil = n * P.NF + i;
+            for (int k = 0; k < NS; ++k) {
+                const size_t sg = (size_t)fil * NS + k;
+                for (int c = 0; c < 4; ++c) op(h.q[4 * sg + c]);
+                for (int c = 0; c < 3; ++c) op(h.x[3 * sg + c]);
+                for (int c = 0; c < 3; ++c) op(h.xm1[3 * sg + c]);
+                for (int c = 0; c < 3; ++c) op(h.xm2[3 * sg + c]);
+                for (int c = 0; c < 3; ++c) op(h.u[3 * sg + c]);
+                for (int c = 0; c < 3; ++c) op(h.um1[3 * sg + c]);
+            }
+            for (auto *v : {&h.tl, &h.tl1, &h.tl2, &h.cl, &h.cl1, &h.cl2})
+                for (int c = 0; c < 3; ++c) op((*v)[3 * (size_t)fil + c]);
+            const size_t l0 = 3 * (size_t)(NS - 1) * fil;
+            for (int k = 0; k < NS - 1; ++k)
+                for (auto *v : {&h.lam, &h.lam1, &h.lam2})
+                    for (int c = 0; c < 3; ++c) op((*v)[l0 + 3 * k + c]);
+        }
+        for (int c = 0; c < 4; ++c) op(h.bq[4 * (size_t)n + c]);
+        for (auto *v : {&h.bx, &h.bxm1, &h.bxm2, &h.bu, &h.bum1})
+            for (int c = 0; c < 3; ++c) op((*v)[3 * (size_t)n + c]);
+    }
+}
+
+}  // namespace
+
 extern "C" {
 
 gmi_status gmi_sim_destroy(gmi_sim *m)
@@ -1402,6 +1469,7 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
     SIM_ALLOC(m->part, (size_t)((nb + kVecChunk - 1) / kVecChunk) * (m->maxb + 1));
     SIM_ALLOC(m->jpart, 6 * F);
     SIM_ALLOC(m->spart, 45 * F);
+    SIM_ALLOC(m->f_internal, 6 * S);
     SIM_ALLOC(m->scal, 4);
     {
         double *fl = nullptr;
@@ -1551,11 +1619,71 @@ gmi_status gmi_sim_get_state(gmi_sim *m, int field, double *out_h)
         case GMI_STATE_TETHER: src = P.tl; count = 3 * (size_t)P.F; break;
         case GMI_STATE_CLAMP: src = P.cl; count = 3 * (size_t)P.F; break;
         case GMI_STATE_BLOB_F: src = m->solver->f_blobs; count = 3 * (size_t)m->solver->B; break;
+        case GMI_STATE_SEG_F_INTERNAL: src = m->f_internal; count = 6 * (size_t)P.S; break;
         default: SIM_ARG_CHECK(false, "gmi_sim_get_state: unknown field");
     }
     GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
     GMI_CUDA_TRY(cudaMemcpyAsync(out_h, src, count * sizeof(double), cudaMemcpyDeviceToHost, sst(m)));
     GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
+    return GMI_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Checkpoints in the reference's .backup layout (cilia_sim_main.cpp:370-381):
+// per swimmer, each filament (filament.cpp:1595-1650: per segment q, x, xm1,
+// xm2, u, um1; tether and clamp multipliers with their two previous values;
+// the inextensibility multipliers with theirs), then the body
+// (rigid_body.cpp:408-432: q, x, xm1, xm2, u, um1).
+// ---------------------------------------------------------------------------
+
+gmi_status gmi_sim_backup_count(const gmi_sim *m, long long *count)
+{
+    SIM_ARG_CHECK(m && count, "gmi_sim_backup_count: null argument");
+    *count = (long long)m->P.W * (long long)per_swimmer_count(m->P);
+    return GMI_OK;
+}
+
+gmi_status gmi_sim_export_backup(gmi_sim *m, double *out_h)
+{
+    SIM_ARG_CHECK(m && out_h, "gmi_sim_export_backup: null argument");
+    GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
+    GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
+    BackupHost h;
+    GMI_TRY(for_each_field(m->P, h, [](double *d, std::vector<double> &v, size_t n) -> gmi_status {
+        v.resize(n);
+        GMI_CUDA_TRY(cudaMemcpy(v.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost));
+        return GMI_OK;
+    }));
+    size_t p = 0;
+    walk_backup(m->P, h, [&](double &v) { out_h[p++] = v; });
+    return GMI_OK;
+}
+
+gmi_status gmi_sim_import_backup(gmi_sim *m, const double *in_h)
+{
+    SIM_ARG_CHECK(m && in_h, "gmi_sim_import_backup: null argument");
+    GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
+    GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
+    BackupHost h;
+    GMI_TRY(for_each_field(m->P, h, [](double *, std::vector<double> &v, size_t n) -> gmi_status {
+        v.assign(n, 0.0);
+        return GMI_OK;
+    }));
+    size_t p = 0;
+    walk_backup(m->P, h, [&](double &v) { v = in_h[p++]; });
+    GMI_TRY(for_each_field(m->P, h, [](double *d, std::vector<double> &v, size_t n) -> gmi_status {
+        GMI_CUDA_TRY(cudaMemcpy(d, v.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        return GMI_OK;
+    }));
+    // q^{n-1} = q for segments and bodies (filament.cpp initial_setup and
+    // rigid_body.cpp:71-100 read the backup this way); a fresh linear solver
+    // starts from zero blob forces and body velocities
+    GMI_CUDA_TRY(cudaMemcpy(m->P.qm1, m->P.q, 4 * (size_t)m->P.S * sizeof(double), cudaMemcpyDeviceToDevice));
+    GMI_CUDA_TRY(cudaMemcpy(m->P.bqm1, m->P.bq, 4 * (size_t)m->P.W * sizeof(double), cudaMemcpyDeviceToDevice));
+    GMI_CUDA_TRY(cudaMemset(m->solver->f_blobs, 0, 3 * (size_t)m->solver->B * sizeof(double)));
+    GMI_CUDA_TRY(cudaMemset(m->solver->v_bodies, 0, 6 * (size_t)m->P.W * sizeof(double)));
+    m->prepared = false;  // the body reference matrices follow the restored state
     return GMI_OK;
 }
 

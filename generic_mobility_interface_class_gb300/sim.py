@@ -6,11 +6,12 @@ import ctypes
 
 import numpy as np
 
-from . import _lib
+from . import _lib, formats
 from ._lib import GMI_FP64, SimConfig, SolverConfig, check
 
 STATE = dict(seg_x=(0, 3), seg_q=(1, 4), seg_u=(2, 3), seg_v=(3, 6), seg_f=(4, 6), body_x=(5, 3), body_q=(6, 4),
-             body_u=(7, 3), body_v=(8, 6), lam=(9, 3), tether=(10, 3), clamp=(11, 3), blob_f=(12, 3))
+             body_u=(7, 3), body_v=(8, 6), lam=(9, 3), tether=(10, 3), clamp=(11, 3), blob_f=(12, 3),
+             seg_f_internal=(13, 6))
 
 
 def _c(a):
@@ -30,6 +31,7 @@ class Simulation:
         cfg = SimConfig(mob, kb, kt, dt, num_euler_steps, max_broyden_iter, tol, jacobian_confidence, body_radius)
         F = nswim * nfil
         self.nswim, self.nfil, self.nseg, self.nblob = nswim, nfil, nseg, nblob
+        self.wall = bool(wall)
         self.F, self.S = F, F * nseg
         body_x0 = np.zeros((nswim, 3)) if body_x0 is None else body_x0
 
@@ -66,6 +68,42 @@ class Simulation:
         out = np.zeros((rows, cols))
         check(self.lib.gmi_sim_get_state(self.handle, field, out.ctypes.data_as(ctypes.c_void_p)))
         return out
+
+    # -- checkpoints and time series in the reference's formats ------------
+    def export_backup(self) -> np.ndarray:
+        n = ctypes.c_longlong()
+        check(self.lib.gmi_sim_backup_count(self.handle, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        check(self.lib.gmi_sim_export_backup(self.handle, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def import_backup(self, values) -> None:
+        """Restore a backup; call prepare() again before stepping (the body
+        reference matrices follow the restored state)."""
+        n = ctypes.c_longlong()
+        check(self.lib.gmi_sim_backup_count(self.handle, ctypes.byref(n)))
+        v, p = _c(values)
+        if v.size != n.value:
+            raise ValueError(f"backup holds {v.size} values, this simulation needs {n.value}")
+        check(self.lib.gmi_sim_import_backup(self.handle, p))
+
+    def write_backup(self, path, nt_completed, digits=formats.DIGITS):
+        formats.write_backup(path, nt_completed, self.export_backup(), digits)
+
+    def read_backup(self, path) -> int:
+        """Restore the state of a .backup file; returns its completed-step
+        count, the step to continue from."""
+        nt, values = formats.read_backup(path)
+        self.import_backup(values)
+        self.nt = nt
+        return nt
+
+    def write_step_data(self, prefix, nt, digits=formats.DIGITS):
+        """Append step nt to the reference's .dat files under prefix."""
+        formats.write_step_data(prefix, nt, self.state("seg_q"), self.state("body_x"), self.state("body_q"),
+                                self.state("seg_v"), self.state("seg_f_internal"),
+                                None if self.wall else self.state("body_v"),
+                                None if self.wall else self.state("blob_f"), digits)
 
     @property
     def launches(self):

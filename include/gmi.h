@@ -274,7 +274,9 @@ typedef enum gmi_state_field {
     GMI_STATE_LAMBDA = 9, /* [3*(nseg-1)*F] inextensibility multipliers */
     GMI_STATE_TETHER = 10, /* [3*F] */
     GMI_STATE_CLAMP = 11,  /* [3*F] */
-    GMI_STATE_BLOB_F = 12  /* [3*B] blob forces of the last solve */
+    GMI_STATE_BLOB_F = 12, /* [3*B] blob forces of the last solve */
+    GMI_STATE_SEG_F_INTERNAL = 13 /* [6*S] segment forces without the barrier
+                                     (the reference's f_segs_host) */
 } gmi_state_field;
 
 /* swimmer::initial_setup for free-swimming spheres (swimmer.cpp:169-230,
@@ -299,6 +301,19 @@ GMI_API gmi_status gmi_sim_prepare(gmi_sim *sim, double *body_mobility_out);
  * GMI_ERR_NOT_CONVERGED / GMI_ERR_NONFINITE where the reference stops. */
 GMI_API gmi_status gmi_sim_step(gmi_sim *sim, int nt, int *broyden_iters, int *gmres_iters_total);
 GMI_API gmi_status gmi_sim_get_state(gmi_sim *sim, int field, double *out_h);
+
+/* Checkpoints in the reference's .backup layout (replaces the state part of
+ * cilia_sim_main.cpp:370-381 and :29-77; filament.cpp:1595-1650;
+ * rigid_body.cpp:408-432): per swimmer, NFIL filaments of 9 + 28*NSEG values
+ * (per segment q, x, xm1, xm2, u, um1; tether and clamp multipliers and their
+ * two previous values; the inextensibility multipliers and theirs), then the
+ * body (q, x, xm1, xm2, u, um1: 19 values).  The step number that the file
+ * starts with is the caller's.  Import sets q^{n-1} = q, zeroes the linear
+ * solver's warm start, and requires gmi_sim_prepare again, as the reference's
+ * restart does. */
+GMI_API gmi_status gmi_sim_backup_count(const gmi_sim *sim, long long *count);
+GMI_API gmi_status gmi_sim_export_backup(gmi_sim *sim, double *out_h);
+GMI_API gmi_status gmi_sim_import_backup(gmi_sim *sim, const double *in_h);
 
 /* Measured FMA-pipe throughput (FLOP/s, FMA = 2) of this GPU for
  * precision GMI_FP32C (FP32 pipe) or GMI_FP64 (FP64 pipe): the roofline

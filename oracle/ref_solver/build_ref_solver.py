@@ -74,10 +74,11 @@ def config_text(overrides: dict) -> str:
     return text
 
 
-def build(case: str) -> str:
+def build(case: str, overrides: dict | None = None, tag: str = "") -> str:
     spec = dict(COMMON)
     spec.update({k: v for k, v in CASES[case].items() if k.isupper()})
-    out = os.path.join(ORACLE, "_ref", f"solver_{case}")
+    spec.update(overrides or {})
+    out = os.path.join(ORACLE, "_ref", f"solver_{case}{tag}")
     os.makedirs(out, exist_ok=True)
     with open(os.path.join(out, "config.hpp"), "w") as fh:
         fh.write(config_text(spec))
@@ -165,6 +166,29 @@ def run_case(case: str, exe: str | None = None) -> str:
     if r.returncode != 0:
         raise RuntimeError(r.stderr + r.stdout[-2000:])
     return rundir
+
+
+def run_restart(case: str, extra_steps: int) -> tuple[str, str]:
+    """Run the case, then the reference restarting from its final backup
+    (INITIAL_CONDITIONS_TYPE 1, cilia_sim_main.cpp:29-77) for extra_steps
+    more steps.  Returns (first run dir, restart run dir)."""
+    import shutil
+    first = run_case(case)
+    total = int(CASES[case]["TOTAL_TIME_STEPS"]) + extra_steps
+    exe = build(case, {"INITIAL_CONDITIONS_TYPE": "1", "TOTAL_TIME_STEPS": str(total)}, tag="_restart")
+    rundir = os.path.join(os.path.dirname(exe), "run")
+    os.makedirs(rundir, exist_ok=True)
+    for f in os.listdir(rundir):
+        os.remove(os.path.join(rundir, f))
+    for f in os.listdir(first):
+        if f.endswith(".seed") or f.endswith(".backup"):
+            shutil.copy(os.path.join(first, f), rundir)
+    r = subprocess.run([exe], cwd=rundir, capture_output=True, text=True)
+    with open(os.path.join(rundir, "stdout.txt"), "w") as fh:
+        fh.write(r.stdout)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr + r.stdout[-2000:])
+    return first, rundir
 
 
 if __name__ == "__main__":

@@ -8,6 +8,11 @@ segment and body velocities, Broyden iteration counts, final backup) in
 sim_<case>.npz.  The fixtures are committed; the tests never need the tree.
 
     python tests/golden/make_golden_sim.py small_swimmer
+    python tests/golden/make_golden_sim.py small_swimmer --restart 4
+
+With --restart N the reference is run again from the first run's final
+.backup for N more steps (its INITIAL_CONDITIONS_TYPE 1 path), and the
+restart's inputs and steps go to sim_<case>_restart.npz.
 """
 from __future__ import annotations
 
@@ -30,8 +35,11 @@ def parse_dat(path, skip_cols=1):
     return np.stack(rows)
 
 
-def main(case):
-    rundir = brs.run_case(case)
+def main(case, restart_steps=0):
+    if restart_steps:
+        first, rundir = brs.run_restart(case, restart_steps)
+    else:
+        rundir = brs.run_case(case)
     spec = dict(brs.COMMON)
     spec.update({k: v for k, v in brs.CASES[case].items() if k.isupper()})
     cfg = open(os.path.join(os.path.dirname(rundir), "config.hpp")).read()
@@ -107,9 +115,22 @@ def main(case):
     for key in ("seg_q", "body_state", "seg_v", "body_v", "blob_f"):
         data[key] = data[key][keep]
     data["steps"] = keep
-    np.savez_compressed(os.path.join(HERE, f"sim_{case}.npz"), **data)
+    name = f"sim_{case}"
+    if restart_steps:
+        # the restart began from the first run's final backup: the steps here
+        # are nt_start .. nt_start + restart_steps - 1
+        with open(os.path.join(first, "test.backup")) as fh:
+            tok = fh.read().split()
+        data["nt_start"] = int(tok[0])
+        data["backup_in"] = np.array(tok[1:], dtype=np.float64)
+        data["steps"] = keep + int(tok[0])
+        name += "_restart"
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **data)
     print(case, {k: np.shape(v) for k, v in data.items() if np.ndim(v)})
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "small_swimmer")
+    # python tests/golden/make_golden_sim.py <case> [--restart N]
+    args = sys.argv[1:]
+    n_restart = int(args[args.index("--restart") + 1]) if "--restart" in args else 0
+    main(args[0] if args and not args[0].startswith("--") else "small_swimmer", n_restart)
