@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ C
         const R *tile = ring + s * kStageScalars;
         const int j0 = j_begin + t * kTile;
         const int jn = min(kTile, j_end - j0);
-#pragma unroll 2
+#pragma unroll 4
         for (int jj = 0; jj < jn; ++jj) {
             Pos<R> sp;
             R F[6];

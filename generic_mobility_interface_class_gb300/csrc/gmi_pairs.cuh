@@ -12,7 +12,15 @@
 namespace gmi {
 
 template <class R> __device__ __forceinline__ R rsq(R x);
-template <> __device__ __forceinline__ float rsq<float>(float x) { return rsqrtf(fmaxf(x, 1e-30f)); }
+// FP32: the hardware approximate reciprocal square root (PTX rsqrt.approx,
+// relative error below 2^-22.9), flushing denormals; the clamp keeps the
+// argument normal (the self pair has r^2 = 0).
+template <> __device__ __forceinline__ float rsq<float>(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(fmaxf(x, 1e-30f)));
+    return y;
+}
 template <> __device__ __forceinline__ double rsq<double>(double x) { return rsqrt(fmax(x, 1e-300)); }
 
 // Equal-radius constants (segment<-segment with a = a_seg, blob<-blob with a = a_blob).
@@ -34,6 +42,26 @@ template <class R> struct UnequalK {
 // translation<-force, rotation<-torque and the two cross couplings, equal
 // radii: cuda_functions.cu:315-398.
 //   v += At F + Bt d + c3 (T x d),   w += Ar T + Br d + c3 (F x d)
+// Near-field (overlapping, r <= 2a) coefficients of pair_ss, out of line:
+// the branch is taken only by the self pair and overlapping particles, and a
+// real branch keeps its arithmetic off the issue slots of every other pair.
+template <class R>
+__device__ __noinline__ void ss_near_coeffs(R r2, R ir, R dF, R dT, const EqualK<R> &k, R &At, R &Bt, R &Ar, R &Br,
+                                            R &c3)
+{
+    const R r = r2 * ir;
+    const R ir2 = ir * ir;
+    const R q = r * k.q32;                      // 3r/(32a)
+    At = (R(1) - R(3) * q) * k.f6pma;
+    Bt = q * k.f6pma * ir2 * dF;
+    const R ra = r * k.inv_a;
+    const R ra3 = ra * ra * ra;
+    const R b = R(9.0 / 32.0) * ra;
+    Ar = (R(-3) * b + (R(1) + R(5.0 / 64.0) * ra3)) * k.f8pma3;
+    Br = (b - R(3.0 / 64.0) * ra3) * k.f8pma3 * ir2 * dT;
+    c3 = r * (R(1) - r * k.q8) * k.f16pma3 * ir;
+}
+
 template <class R>
 __device__ __forceinline__ void pair_ss(R dx, R dy, R dz, const R *F, const EqualK<R> &k, R *v, R *w)
 {
@@ -54,17 +82,7 @@ __device__ __forceinline__ void pair_ss(R dx, R dy, R dz, const R *F, const Equa
         Ar = R(-0.5) * c3;                          // -1/(16 pi mu r^3)
         Br = (R(1.5) * c3 * ir2) * dT;              // 3 dT / (16 pi mu r^5)
     } else {
-        const R r = r2 * ir;
-        const R ir2 = ir * ir;
-        const R q = r * k.q32;                      // 3r/(32a)
-        At = (R(1) - R(3) * q) * k.f6pma;
-        Bt = q * k.f6pma * ir2 * dF;
-        const R ra = r * k.inv_a;
-        const R ra3 = ra * ra * ra;
-        const R b = R(9.0 / 32.0) * ra;
-        Ar = (R(-3) * b + (R(1) + R(5.0 / 64.0) * ra3)) * k.f8pma3;
-        Br = (b - R(3.0 / 64.0) * ra3) * k.f8pma3 * ir2 * dT;
-        c3 = r * (R(1) - r * k.q8) * k.f16pma3 * ir;
+        ss_near_coeffs<R>(r2, ir, dF, dT, k, At, Bt, Ar, Br, c3);
     }
     const R cx = c3 * dx, cy = c3 * dy, cz = c3 * dz;
     v[0] += At * F[0] + Bt * dx + F[4] * cz - F[5] * cy;
