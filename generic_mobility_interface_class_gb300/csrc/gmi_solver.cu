@@ -21,6 +21,7 @@
 
 #include "gmi_context.hpp"
 #include "gmi_pair_kernels.hpp"
+#include "gmi_solver_device.cuh"
 #include "gmi_solver_internal.hpp"
 
 namespace gmi {
@@ -31,13 +32,6 @@ constexpr int kChunkRows = 1024;  // rows per block in dot-product partials
 // ---------------------------------------------------------------------------
 // small helpers
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double warp_sum(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    return v;
-}
-
 // Block-wide sum in a fixed order (result valid in thread 0).
 template <int TPB> __device__ __forceinline__ double block_sum(double v, double *smem)
 {
@@ -81,13 +75,6 @@ __device__ __forceinline__ void quat_rot(const double *q, double *R)
     R[0] = R00; R[1] = R01; R[2] = R02;
     R[3] = R10; R[4] = R11; R[5] = R12;
     R[6] = R20; R[7] = R21; R[8] = R22;
-}
-
-__device__ __forceinline__ void rot_apply(const double *R, const double *v, double *o)
-{
-    o[0] = R[0] * v[0] + R[1] * v[1] + R[2] * v[2];
-    o[1] = R[3] * v[0] + R[4] * v[1] + R[5] * v[2];
-    o[2] = R[6] * v[0] + R[7] * v[1] + R[8] * v[2];
 }
 
 // ---------------------------------------------------------------------------
@@ -409,26 +396,6 @@ constexpr int kFMaxK = 160;   // >= max_iter + 1
 constexpr int kHOff = 0;             // h[kFMaxK]: the last projections
 constexpr int kNormOff = kFMaxK;     // ||w|| of the last step (or beta0 before the first)
 constexpr int kStepScalars = kFMaxK + 8;
-
-__device__ __forceinline__ void pack_record(void *rec, int i, const double *x, const double *f, int f64)
-{
-    if (f64) {
-        double2 *r = static_cast<double2 *>(rec) + 6 * (size_t)i;
-        r[0] = make_double2(x[0], x[1]);
-        r[1] = make_double2(x[2], f[0]);
-        r[2] = make_double2(f[1], f[2]);
-        r[3] = make_double2(0.0, 0.0);
-        r[4] = make_double2(0.0, 0.0);
-        r[5] = make_double2(0.0, 0.0);
-    } else {
-        const float hx = (float)x[0], hy = (float)x[1], hz = (float)x[2];
-        float4 *r = static_cast<float4 *>(rec) + 3 * (size_t)i;
-        r[0] = make_float4(hx, hy, hz, (float)f[0]);
-        r[1] = make_float4((float)(x[0] - (double)hx), (float)(x[1] - (double)hy), (float)(x[2] - (double)hz),
-                           (float)f[1]);
-        r[2] = make_float4((float)f[2], 0.f, 0.f, 0.f);
-    }
-}
 
 // True in every thread of the CTA that arrives last (of `total`) at *ticket;
 // that CTA re-arms the ticket for the next launch.  Partials written before
