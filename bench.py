@@ -53,7 +53,8 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gmi", "reference"], default="gmi")
-    p.add_argument("--n", type=int, default=131072)
+    p.add_argument("--n", "--particles", dest="n", type=int, default=131072,
+                   help="particles of the apply benchmark (--particles under torchrun, whose parser takes --n*)")
     p.add_argument("--precision", choices=["fp32c", "fp64"], default="fp32c")
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 side measurement")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU sample")
