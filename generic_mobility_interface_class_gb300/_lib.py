@@ -77,6 +77,7 @@ SIGNATURES = {
     "gmi_solver_make_body_reference_matrices": ([_P, _P, _P, _P, _P], _I),
     "gmi_solver_set_body_reference_matrices": ([_P, _P, _P], _I),
     "gmi_solver_compute_velocities": ([_P, _P, _P, _P, ctypes.POINTER(_I)], _I),
+    "gmi_solver_compute_velocities_prescribed": ([_P, _P, _P, _P, _P, ctypes.POINTER(_I)], _I),
     "gmi_solver_get_v_bodies": ([_P, _P], _I),
     "gmi_solver_set_v_bodies": ([_P, _P], _I),
     "gmi_sim_create": ([_P, _P, _P, _P, _P, _P, ctypes.POINTER(_P)], _I),

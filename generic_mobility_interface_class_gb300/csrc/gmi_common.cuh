@@ -32,6 +32,13 @@ constexpr unsigned long long kWaitDeadlineNs = 2000000000ull;
         }                                                         \
     } while (0)
 
+// Return the status of a gmi call that failed.
+#define GMI_TRY(expr)                        \
+    do {                                     \
+        gmi_status gmi_s_ = (expr);          \
+        if (gmi_s_ != GMI_OK) return gmi_s_; \
+    } while (0)
+
 void set_last_error(const char *what, const char *expr, const char *file, int line);
 void set_last_error_msg(const char *msg);
 

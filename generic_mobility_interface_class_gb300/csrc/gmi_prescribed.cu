@@ -1,0 +1,408 @@
+// gmi_prescribed.cu -- mobility_solver::compute_velocities for cilia whose
+// shapes are prescribed (CILIA_TYPE 3, mobility_solver.cpp:1362-1369), free
+// bodies, phases advancing at the speed the caller gives:
+//
+//   unknowns  x = [f_seg (3 per segment) | f_blob (3 per blob) | U (6 per body)]
+//   operator  (system_matrix_mult, mobility_solver.cpp:733-905)
+//             seg:  M_ss f_seg + M_sb f_blob - (U + Omega x d_seg)      (translation rows)
+//             blob: M_bs f_seg + M_bb f_blob - (U + Omega x d_blob)
+//             body: -sum (f, d x f) over the body's segments and blobs
+//   rhs       (assemble_rhs, :211-310) segment rows phase_speed * vel_dir, the rest 0
+//   precond.  (apply_preconditioner, :427-649) M ~ I / (6 pi mu a) per particle and
+//             the body block through (K^T M^-1 K)^-1 (swimmer::make_precon_mat,
+//             swimmer.cpp:929-1037)
+// All four pair sums run inside every GMRES iteration.  Segments carry no
+// torques in this system (their forces are the unknowns).
+#include <cstring>
+#include <new>
+
+#include "gmi_context.hpp"
+#include "gmi_gmres.hpp"
+#include "gmi_lie.cuh"
+#include "gmi_pair_kernels.hpp"
+#include "gmi_solver_device.cuh"
+#include "gmi_solver_internal.hpp"
+
+
+struct PrescribedWork {
+    gmi::KrylovSpace K;
+    int np = 0;
+    double *vel_dir = nullptr, *phase = nullptr, *P6 = nullptr, *rhs = nullptr, *soln = nullptr, *f6 = nullptr;
+    int *flag = nullptr;
+};
+
+namespace gmi {
+
+namespace {
+
+constexpr int kTpb = 256;
+
+struct PSizes {
+    int S, B, W, nseg_sw, nblob;  // nseg_sw: segments per swimmer
+};
+
+__device__ __forceinline__ void seg_arm(const PSizes &z, const double *xs, const double *bx, int m, int &sw,
+                                        double *d)
+{
+    sw = m / z.nseg_sw;
+    for (int c = 0; c < 3; ++c) d[c] = xs[3 * (size_t)m + c] - bx[3 * sw + c];
+}
+__device__ __forceinline__ void blob_arm(const PSizes &z, const double *R, const double *refs, int i, int &sw,
+                                         double *d)
+{
+    sw = i / z.nblob;
+    rot_apply(R + 9 * sw, refs + 3 * (i % z.nblob), d);
+}
+
+// CTA sum of N per-thread values in a fixed order; result valid in red[0..N) after the call
+template <int N> __device__ void cta_sum(double *v, double (*red)[kTpb / 32])
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int e = 0; e < N; ++e) {
+        const double t = warp_sum(v[e]);
+        if (lane == 0) red[e][wid] = t;
+    }
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double t = 0.0;
+        for (int q = 0; q < kTpb / 32; ++q) t += red[threadIdx.x][q];
+        red[threadIdx.x][0] = t;
+    }
+    __syncthreads();
+}
+
+// In-place inverse of a column-major 6x6 (Gauss-Jordan, partial pivoting);
+// false if singular.
+__device__ bool invert6(double *A)
+{
+    double M[6][12];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+            M[i][j] = A[i + 6 * j];
+            M[i][6 + j] = i == j ? 1.0 : 0.0;
+        }
+    for (int c = 0; c < 6; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 6; ++r)
+            if (fabs(M[r][c]) > fabs(M[p][c])) p = r;
+        if (M[p][c] == 0.0) return false;
+        if (p != c)
+            for (int j = 0; j < 12; ++j) {
+                const double t = M[c][j];
+                M[c][j] = M[p][j];
+                M[p][j] = t;
+            }
+        const double inv = 1.0 / M[c][c];
+        for (int j = 0; j < 12; ++j) M[c][j] *= inv;
+        for (int r = 0; r < 6; ++r) {
+            if (r == c) continue;
+            const double f = M[r][c];
+            if (f != 0.0)
+                for (int j = 0; j < 12; ++j) M[r][j] -= f * M[c][j];
+        }
+    }
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) A[i + 6 * j] = M[i][6 + j];
+    return true;
+}
+
+// (K^T M^-1 K)^-1 per swimmer, column-major (swimmer.cpp:929-1037 without
+// the phase terms): [[e I, sum m rc(d)], [-sum m rc(d), -sum m rc(d)^2]]^-1,
+// e = sum of the mobility factors, rc the reference's rcross.
+__global__ void __launch_bounds__(kTpb) pk_precon_mats(PSizes z, const double *__restrict__ xs,
+                                                       const double *__restrict__ bx, const double *__restrict__ R,
+                                                       const double *__restrict__ refs, double seg_mob,
+                                                       double blob_mob, double *__restrict__ P6, int *flag)
+{
+    __shared__ double red[18][kTpb / 32];
+    const int n = blockIdx.x;
+    double acc[18];
+    for (int e = 0; e < 18; ++e) acc[e] = 0.0;
+    for (int e = threadIdx.x; e < z.nseg_sw + z.nblob; e += kTpb) {
+        double d[3], mob;
+        int sw;
+        if (e < z.nseg_sw) {
+            seg_arm(z, xs, bx, n * z.nseg_sw + e, sw, d);
+            mob = seg_mob;
+        } else {
+            blob_arm(z, R, refs, n * z.nblob + (e - z.nseg_sw), sw, d);
+            mob = blob_mob;
+        }
+        const M3 rc = rcross(d), rc2 = m3_mul(rc, rc);
+        for (int k = 0; k < 9; ++k) {
+            acc[k] += mob * rc.a[k];
+            acc[9 + k] += mob * rc2.a[k];
+        }
+    }
+    cta_sum<18>(acc, red);
+    if (threadIdx.x != 0) return;
+    double A[36];
+    const double eye = (double)z.nseg_sw * seg_mob + (double)z.nblob * blob_mob;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const double tr = red[3 * i + j][0], br = red[9 + 3 * i + j][0];
+            A[i + 6 * j] = i == j ? eye : 0.0;
+            A[i + 6 * (3 + j)] = tr;
+            A[(3 + i) + 6 * j] = -tr;
+            A[(3 + i) + 6 * (3 + j)] = -br;
+        }
+    if (!invert6(A)) atomicOr(flag, 1);
+    for (int k = 0; k < 36; ++k) P6[36 * n + k] = A[k];
+}
+
+// f6 = (f, 0) per segment from the 3-per-segment unknowns
+__global__ void pk_expand(int S, const double *__restrict__ in, double *__restrict__ f6)
+{
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= S) return;
+    for (int c = 0; c < 3; ++c) {
+        f6[6 * (size_t)m + c] = in[3 * (size_t)m + c];
+        f6[6 * (size_t)m + 3 + c] = 0.0;
+    }
+}
+
+// particle rows: out = base - s (U + Omega x d), base = v (operator) or a (in + U + Omega x d) (preconditioner)
+template <bool PRECOND>
+__global__ void pk_rows(PSizes z, const double *__restrict__ in, const double *__restrict__ vsegs,
+                        const double *__restrict__ vblobs, const double *__restrict__ xs, const double *__restrict__ bx,
+                        const double *__restrict__ R, const double *__restrict__ refs, double seg_mob, double blob_mob,
+                        const double *__restrict__ Uall, double *__restrict__ out)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= z.S + z.B) return;
+    double d[3];
+    int sw;
+    const bool seg = p < z.S;
+    if (seg)
+        seg_arm(z, xs, bx, p, sw, d);
+    else
+        blob_arm(z, R, refs, p - z.S, sw, d);
+    const double *U = Uall + 6 * sw;
+    const double k[3] = {U[0] + U[4] * d[2] - U[5] * d[1], U[1] + U[5] * d[0] - U[3] * d[2],
+                         U[2] + U[3] * d[1] - U[4] * d[0]};
+    const size_t r = 3 * (size_t)p;
+    for (int c = 0; c < 3; ++c) {
+        if (PRECOND) {
+            const double mob = seg ? seg_mob : blob_mob;
+            out[r + c] = mob * in[r + c] + mob * k[c];
+        } else {
+            const double v = seg ? vsegs[6 * (size_t)p + c] : vblobs[3 * (size_t)(p - z.S) + c];
+            out[r + c] = v - k[c];
+        }
+    }
+}
+
+// body rows, one CTA per swimmer: t = sum over its segments and blobs of
+// (s f, d x s f) with s = mob (preconditioner) or 1 (operator); operator
+// out_body = -t; preconditioner out_body = P6 (-in_body - t)
+template <bool PRECOND>
+__global__ void __launch_bounds__(kTpb) pk_body(PSizes z, const double *__restrict__ in, const double *__restrict__ xs,
+                                                const double *__restrict__ bx, const double *__restrict__ R,
+                                                const double *__restrict__ refs, double seg_mob, double blob_mob,
+                                                const double *__restrict__ P6, double *__restrict__ out)
+{
+    __shared__ double red[6][kTpb / 32];
+    const int n = blockIdx.x;
+    const size_t uoff = 3 * (size_t)(z.S + z.B);
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int e = threadIdx.x; e < z.nseg_sw + z.nblob; e += kTpb) {
+        double d[3];
+        int sw, p;
+        if (e < z.nseg_sw) {
+            p = n * z.nseg_sw + e;
+            seg_arm(z, xs, bx, p, sw, d);
+        } else {
+            p = z.S + n * z.nblob + (e - z.nseg_sw);
+            blob_arm(z, R, refs, p - z.S, sw, d);
+        }
+        const double sc = PRECOND ? (e < z.nseg_sw ? seg_mob : blob_mob) : 1.0;
+        const double f[3] = {sc * in[3 * (size_t)p], sc * in[3 * (size_t)p + 1], sc * in[3 * (size_t)p + 2]};
+        acc[0] += f[0];
+        acc[1] += f[1];
+        acc[2] += f[2];
+        acc[3] += d[1] * f[2] - d[2] * f[1];
+        acc[4] += d[2] * f[0] - d[0] * f[2];
+        acc[5] += d[0] * f[1] - d[1] * f[0];
+    }
+    cta_sum<6>(acc, red);
+    if (threadIdx.x != 0) return;
+    if (!PRECOND) {
+        for (int j = 0; j < 6; ++j) out[uoff + 6 * n + j] = -red[j][0];
+        return;
+    }
+    double b[6];
+    for (int j = 0; j < 6; ++j) b[j] = -in[uoff + 6 * n + j] - red[j][0];
+    const double *A = P6 + 36 * n;
+    for (int i = 0; i < 6; ++i) {
+        double t = 0.0;
+        for (int j = 0; j < 6; ++j) t += A[i + 6 * j] * b[j];
+        out[uoff + 6 * n + i] = t;
+    }
+}
+
+// segment rows of the right-hand side: phase_speed * vel_dir; zero elsewhere
+__global__ void pk_rhs(int np, int S3, int nseg3, const double *__restrict__ vel_dir,
+                       const double *__restrict__ phase, double *__restrict__ rhs)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= np) return;
+    rhs[r] = r < S3 ? phase[r / nseg3] * vel_dir[r] : 0.0;
+}
+
+// solution -> f_segs (forces, zero torques), f_blobs, v_bodies
+__global__ void pk_store(PSizes z, const double *__restrict__ x, double *__restrict__ f6, double *__restrict__ fb,
+                         double *__restrict__ vb)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < z.S) {
+        for (int c = 0; c < 3; ++c) {
+            f6[6 * (size_t)p + c] = x[3 * (size_t)p + c];
+            f6[6 * (size_t)p + 3 + c] = 0.0;
+        }
+    } else if (p < z.S + z.B) {
+        for (int c = 0; c < 3; ++c) fb[3 * (size_t)(p - z.S) + c] = x[3 * (size_t)p + c];
+    } else if (p < z.S + z.B + z.W) {
+        const int n = p - z.S - z.B;
+        for (int j = 0; j < 6; ++j) vb[6 * n + j] = x[3 * (size_t)(z.S + z.B) + 6 * n + j];
+    }
+}
+
+inline int blocks(int n) { return (n + kTpb - 1) / kTpb; }
+
+gmi_status dalloc0(double **p, size_t n, cudaStream_t st)
+{
+    GMI_CUDA_TRY(cudaMalloc(p, (n ? n : 1) * sizeof(double)));
+    GMI_CUDA_TRY(cudaMemsetAsync(*p, 0, (n ? n : 1) * sizeof(double), st));
+    return GMI_OK;
+}
+
+gmi_status ensure_work(gmi_solver *s)
+{
+    if (s->prescribed) return GMI_OK;
+    PrescribedWork *pw = new (std::nothrow) PrescribedWork();
+    if (!pw) {
+        set_last_error_msg("prescribed cilia: out of host memory");
+        return GMI_ERR_ARG;
+    }
+    s->prescribed = pw;
+    cudaStream_t st = s->ctx->stream;
+    const size_t S = s->S, B = s->B, W = s->W, F = (size_t)s->W * s->cfg.nfil;
+    pw->np = (int)(3 * S + 3 * B + 6 * W);
+    GMI_TRY(krylov_alloc(pw->K, pw->np, s->m, st));
+    GMI_TRY(dalloc0(&pw->vel_dir, 3 * S, st));
+    GMI_TRY(dalloc0(&pw->phase, F, st));
+    GMI_TRY(dalloc0(&pw->P6, 36 * W, st));
+    GMI_TRY(dalloc0(&pw->rhs, pw->np, st));
+    GMI_TRY(dalloc0(&pw->soln, pw->np, st));
+    GMI_TRY(dalloc0(&pw->f6, 6 * S, st));
+    double *fl = nullptr;
+    GMI_TRY(dalloc0(&fl, 1, st));
+    pw->flag = reinterpret_cast<int *>(fl);
+    return GMI_OK;
+}
+
+}  // namespace
+
+void prescribed_release(gmi_solver *s)
+{
+    PrescribedWork *pw = s->prescribed;
+    if (!pw) return;
+    krylov_free(pw->K);
+    for (double *p : {pw->vel_dir, pw->phase, pw->P6, pw->rhs, pw->soln, pw->f6})
+        if (p) cudaFree(p);
+    if (pw->flag) cudaFree(pw->flag);
+    delete pw;
+    s->prescribed = nullptr;
+}
+
+}  // namespace gmi
+
+using namespace gmi;
+
+extern "C" gmi_status gmi_solver_compute_velocities_prescribed(gmi_solver *s, const double *body_x,
+                                                               const double *body_q, const double *vel_dir,
+                                                               const double *phase_speed, int *gmres_iters)
+{
+    if (!s || !body_x || !body_q || !vel_dir || !phase_speed) {
+        set_last_error_msg("gmi_solver_compute_velocities_prescribed: null argument");
+        return GMI_ERR_ARG;
+    }
+    if (s->cfg.wall || s->B == 0 || !s->refs_set) {
+        set_last_error_msg("gmi_solver_compute_velocities_prescribed: free-swimming bodies with blob references");
+        return GMI_ERR_ARG;
+    }
+    gmi_context *ctx = s->ctx;
+    GMI_CUDA_TRY(cudaSetDevice(ctx->device));
+    GMI_TRY(ensure_work(s));
+    PrescribedWork *pw = s->prescribed;
+    cudaStream_t st = ctx->stream;
+    const int S = s->S, B = s->B, W = s->W, F = W * s->cfg.nfil, nseg = s->cfg.nseg;
+    const PSizes z{S, B, W, s->cfg.nfil * nseg, s->cfg.nblob};
+    const double seg_mob = 6.0 * kPi * s->cfg.mu * s->cfg.rseg, blob_mob = 6.0 * kPi * s->cfg.mu * s->cfg.rblob;
+    // segment positions from the caller's host array, shapes, phase speeds, bodies
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->x_segs, s->h.x_segs_host, 3 * (size_t)S * sizeof(double), cudaMemcpyHostToDevice,
+                                 st));
+    GMI_CUDA_TRY(cudaMemcpyAsync(pw->vel_dir, vel_dir, 3 * (size_t)S * sizeof(double), cudaMemcpyHostToDevice, st));
+    GMI_CUDA_TRY(cudaMemcpyAsync(pw->phase, phase_speed, (size_t)F * sizeof(double), cudaMemcpyHostToDevice, st));
+    GMI_TRY(solver_place_blobs(s, body_x, body_q));
+    GMI_CUDA_TRY(cudaMemsetAsync(pw->flag, 0, sizeof(int), st));
+    pk_precon_mats<<<W, kTpb, 0, st>>>(z, s->x_segs, s->body_x, s->R, s->refs, seg_mob, blob_mob, pw->P6, pw->flag);
+    pk_rhs<<<blocks(pw->np), kTpb, 0, st>>>(pw->np, 3 * S, 3 * nseg, pw->vel_dir, pw->phase, pw->rhs);
+    ctx->launches += 2;
+    GMI_CUDA_TRY(cudaGetLastError());
+
+    PairConsts kss, ksb, kbb;
+    fill_consts(kss, s->cfg.rseg, s->cfg.rseg, s->cfg.rseg, s->cfg.mu);
+    fill_consts(ksb, s->cfg.rseg, s->cfg.rseg, s->cfg.rblob, s->cfg.mu);
+    fill_consts(kbb, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
+    const size_t uoff = 3 * (size_t)(S + B);
+    DeviceApply matvec = [&](const double *in, double *out) -> gmi_status {
+        pk_expand<<<blocks(S), kTpb, 0, st>>>(S, in, pw->f6);
+        ctx->launches++;
+        // segments with their forces; M_ss onto segments, M_bs onto blobs
+        GMI_TRY(pack_records(ctx, s->x_segs, pw->f6, 6, S, ctx->rec_src));
+        GMI_TRY(launch_pair(ctx, kSS, ctx->rec_src.ptr, 0, S, ctx->rec_src.ptr, S, kss, s->v_segs, 0));
+        GMI_TRY(pack_records(ctx, s->x_blobs, nullptr, 0, B, ctx->rec_tgt));
+        GMI_TRY(launch_pair(ctx, kBS, ctx->rec_tgt.ptr, 0, B, ctx->rec_src.ptr, S, ksb, s->v_blobs, 0));
+        // blobs with their forces; M_bb onto blobs, M_sb onto segments
+        GMI_TRY(pack_records(ctx, s->x_blobs, in + 3 * (size_t)S, 3, B, ctx->rec_src));
+        GMI_TRY(launch_pair(ctx, kBB, ctx->rec_src.ptr, 0, B, ctx->rec_src.ptr, B, kbb, s->v_blobs, 1));
+        GMI_TRY(pack_records(ctx, s->x_segs, nullptr, 0, S, ctx->rec_tgt));
+        GMI_TRY(launch_pair(ctx, kSB, ctx->rec_tgt.ptr, 0, S, ctx->rec_src.ptr, B, ksb, s->v_segs, 1));
+        pk_rows<false><<<blocks(S + B), kTpb, 0, st>>>(z, in, s->v_segs, s->v_blobs, s->x_segs, s->body_x, s->R,
+                                                       s->refs, seg_mob, blob_mob, in + uoff, out);
+        pk_body<false><<<W, kTpb, 0, st>>>(z, in, s->x_segs, s->body_x, s->R, s->refs, seg_mob, blob_mob, pw->P6,
+                                           out);
+        ctx->launches += 2;
+        GMI_CUDA_TRY(cudaGetLastError());
+        return GMI_OK;
+    };
+    DeviceApply precond = [&](const double *in, double *out) -> gmi_status {
+        pk_body<true><<<W, kTpb, 0, st>>>(z, in, s->x_segs, s->body_x, s->R, s->refs, seg_mob, blob_mob, pw->P6,
+                                          out);
+        pk_rows<true><<<blocks(S + B), kTpb, 0, st>>>(z, in, nullptr, nullptr, s->x_segs, s->body_x, s->R, s->refs,
+                                                      seg_mob, blob_mob, out + uoff, out);
+        ctx->launches += 2;
+        GMI_CUDA_TRY(cudaGetLastError());
+        return GMI_OK;
+    };
+    int iters = 0;
+    GMI_TRY(krylov_gmres(ctx, pw->K, precond, matvec, pw->rhs, pw->soln, s->cfg.linear_tol, &iters));
+    pk_store<<<blocks(S + B + W), kTpb, 0, st>>>(z, pw->soln, s->f_segs, s->f_blobs, s->v_bodies);
+    ctx->launches++;
+    GMI_CUDA_TRY(cudaGetLastError());
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->h.f_segs_host, s->f_segs, 6 * (size_t)S * sizeof(double), cudaMemcpyDeviceToHost,
+                                 st));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->h.f_blobs_host, s->f_blobs, 3 * (size_t)B * sizeof(double),
+                                 cudaMemcpyDeviceToHost, st));
+    int flag = 0;
+    GMI_CUDA_TRY(cudaMemcpyAsync(&flag, pw->flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GMI_CUDA_TRY(cudaStreamSynchronize(st));
+    GMI_TRY(context_check_device_errors(ctx));
+    if (flag) {
+        set_last_error_msg("gmi_solver_compute_velocities_prescribed: singular body preconditioner matrix");
+        return GMI_ERR_NONFINITE;
+    }
+    if (gmres_iters) *gmres_iters = iters;
+    return GMI_OK;
+}

@@ -1117,11 +1117,6 @@ namespace gmi {
 
 static inline int gridN(int n, int tpb = 128) { return (n + tpb - 1) / tpb; }
 
-#define GMI_TRY(expr)                        \
-    do {                                     \
-        gmi_status gmi_s_ = (expr);          \
-        if (gmi_s_ != GMI_OK) return gmi_s_; \
-    } while (0)
 
 static gmi_status sim_alloc(gmi_sim *m, double **p, size_t count)
 {

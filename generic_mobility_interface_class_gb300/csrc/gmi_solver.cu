@@ -826,11 +826,6 @@ static gmi_status halloc(double **p, size_t count)
     return GMI_OK;
 }
 
-#define GMI_TRY(expr)                  \
-    do {                               \
-        gmi_status gmi_s_ = (expr);    \
-        if (gmi_s_ != GMI_OK) return gmi_s_; \
-    } while (0)
 
 static gmi_status launched(gmi_solver *s, int kernels = 1)
 {
@@ -1337,6 +1332,19 @@ static gmi_status stage_bodies(gmi_solver *s, const double *bx, const double *bq
     return GMI_OK;
 }
 
+gmi_status solver_place_blobs(gmi_solver *s, const double *body_x, const double *body_q)
+{
+    GMI_TRY(stage_bodies(s, body_x, body_q));
+    GMI_TRY(prepare_bodies(s));
+    if (s->B > 0) {
+        blob_positions_kernel<<<grid_for(s->B), 256, 0, s->ctx->stream>>>(s->W, s->cfg.nblob, s->body_x, s->R,
+                                                                           s->refs, s->x_blobs);
+        GMI_TRY(launched(s));
+    }
+    return GMI_OK;
+}
+
+
 static gmi_status seg_pair(gmi_solver *s, int kind)
 {
     gmi_context *ctx = s->ctx;
@@ -1459,6 +1467,7 @@ gmi_status gmi_solver_destroy(gmi_solver *s)
     }
     for (int g = 0; g < 2; ++g)
         if (s->graph[g]) cudaGraphExecDestroy(s->graph[g]);
+    prescribed_release(s);
     if (s->h_ctl) cudaFreeHost(s->h_ctl);
     for (void *p : s->allocs) cudaFree(p);
     double *hp[] = {s->h.v_segs_host, s->h.v_blobs_host, s->h.x_segs_host, s->h.x_blobs_host, s->h.f_segs_host,

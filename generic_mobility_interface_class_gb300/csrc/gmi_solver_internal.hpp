@@ -7,6 +7,8 @@
 
 #include "gmi_context.hpp"
 
+struct PrescribedWork;  // workspace of the prescribed-shape cilia solve (gmi_prescribed.cu)
+
 struct gmi_solver {
     gmi_context *ctx = nullptr;
     gmi_solver_config cfg{};
@@ -39,6 +41,7 @@ struct gmi_solver {
     size_t graph_nodes[2] = {0, 0};
     bool graph_loops[2] = {false, false};           // graph holds the whole device-side loop
     bool use_graphs = true;
+    PrescribedWork *prescribed = nullptr;  // allocated by the first prescribed-cilia solve
 };
 
 
@@ -62,6 +65,13 @@ namespace gmi {
 // (their blob part added into body_f), M_ss, M_bs, the right-hand side, the
 // linear solve, M_sb.  Leaves v_segs, f_blobs, v_bodies on the device.
 gmi_status solver_compute_velocities_device(gmi_solver *s, int *iters);
+
+// Body state from the host (x[3W], q[4W]), rotation matrices and blob
+// positions on the device.
+gmi_status solver_place_blobs(gmi_solver *s, const double *body_x, const double *body_q);
+
+// Frees the prescribed-cilia workspace (gmi_solver_destroy).
+void prescribed_release(gmi_solver *s);
 
 // make_body_reference_matrices on the device-resident x_segs/f_segs and
 // body state; the outputs (may be null) are column-major 6x6.

@@ -120,6 +120,21 @@ class MobilitySolver:
         check(self.lib.gmi_solver_compute_velocities(self.handle, _cptr(bx), _cptr(bq), _cptr(bf), ctypes.byref(it)))
         return it.value, bf
 
+    def compute_velocities_prescribed(self, vel_dir, phase_speed, body_x=None, body_q=None):
+        """Prescribed-shape cilia: returns the number of GMRES iterations; the
+        segment forces land in f_segs_host[:, :3], the blob forces in
+        f_blobs_host, the body velocities in v_bodies().  Segment positions are
+        read from x_segs_host; vel_dir is (S, 3), phase_speed (W*nfil,)."""
+        W = self.W
+        bx = np.ascontiguousarray(np.zeros((W, 3)) if body_x is None else body_x, dtype=np.float64)
+        bq = np.ascontiguousarray(np.tile([1.0, 0, 0, 0], (W, 1)) if body_q is None else body_q, dtype=np.float64)
+        vd = np.ascontiguousarray(vel_dir, dtype=np.float64)
+        ph = np.ascontiguousarray(phase_speed, dtype=np.float64)
+        it = ctypes.c_int()
+        check(self.lib.gmi_solver_compute_velocities_prescribed(self.handle, _cptr(bx), _cptr(bq), _cptr(vd), _cptr(ph),
+                                                                ctypes.byref(it)))
+        return it.value
+
     def v_bodies(self):
         out = np.zeros((self.W, 6))
         check(self.lib.gmi_solver_get_v_bodies(self.handle, _cptr(out)))

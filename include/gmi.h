@@ -234,6 +234,21 @@ GMI_API gmi_status gmi_solver_set_body_reference_matrices(gmi_solver *s, const d
 GMI_API gmi_status gmi_solver_compute_velocities(gmi_solver *s, const double *body_x_h, const double *body_q_h,
                                                  double *body_f_h, int *num_gmres_iterations);
 
+/* mobility_solver::compute_velocities for prescribed-shape cilia (CILIA_TYPE 3;
+ * mobility_solver.cpp:1362-1369 with assemble_rhs :211-310, the preconditioner
+ * :427-649, system_matrix_mult :733-905 and swimmer::make_precon_mat,
+ * swimmer.cpp:929-1037), free bodies, phases at the caller's speeds: solves
+ * for the segment forces, blob forces and body velocities that move the
+ * segments (x_segs_host, filled by the caller) at phase_speed[F] times
+ * vel_dir[3*S] (the filaments' shape-velocity directions) while the bodies
+ * swim force- and torque-free.  Results: f_segs_host (forces; torques 0),
+ * f_blobs_host, and the body velocities (gmi_solver_get_v_bodies).  Each
+ * solve warm-starts from the previous one; no barrier forces (as the
+ * reference). */
+GMI_API gmi_status gmi_solver_compute_velocities_prescribed(gmi_solver *s, const double *body_x_h,
+                                                            const double *body_q_h, const double *vel_dir_h,
+                                                            const double *phase_speed_h, int *gmres_iters);
+
 /* v_bodies after the last solve: 6*nswim values (U, Omega per swimmer). */
 GMI_API gmi_status gmi_solver_get_v_bodies(gmi_solver *s, double *v_bodies_h);
 GMI_API gmi_status gmi_solver_set_v_bodies(gmi_solver *s, const double *v_bodies_h);

@@ -50,6 +50,10 @@ CASES = {
     # filaments on an infinite no-slip wall (INFINITE_PLANE_WALL): a 3 x 3
     # rectangular grid of 20-segment filaments, Swan-Brady wall mobility, no
     # rigid body and no linear solve
+    # prescribed-shape cilia (CILIA_TYPE 3, the coral-larvae beat fit, phases
+    # advancing at constant speed): the solver's prescribed-motion system
+    "prescribed": dict(CILIA_TYPE="3", NFIL="4", NSEG="20", NBLOB="162", R_OVER_L="0.25", RBLOB="1.0",
+                       TOTAL_TIME_STEPS="3", DYNAMIC_PHASE_EVOLUTION="false", nblob_subdiv=2, fil_subdiv=1, seed=5),
     "wall_filaments": dict(BODY_OR_SURFACE_TYPE="0", NFIL="9", NSEG="20", NBLOB="0", R_OVER_L="0.25",
                            RBLOB="1.0", TOTAL_TIME_STEPS="10", seed=3),
     # BASELINE config 1 geometry: sphere of radius 10a, 642 blobs (icosphere 3),
@@ -74,7 +78,7 @@ def config_text(overrides: dict) -> str:
     return text
 
 
-def build(case: str, overrides: dict | None = None, tag: str = "") -> str:
+def build(case: str, overrides: dict | None = None, tag: str = "", driver: str | None = None) -> str:
     spec = dict(COMMON)
     spec.update({k: v for k, v in CASES[case].items() if k.isupper()})
     spec.update(overrides or {})
@@ -88,6 +92,12 @@ def build(case: str, overrides: dict | None = None, tag: str = "") -> str:
             "-include", os.path.join(out, "config.hpp")]
     jobs = []
     for f in REF_CPP:
+        if driver and f == "cilia_sim_main.cpp":
+            # a test driver takes the place of the reference's main
+            f_src = os.path.join(HERE, driver)
+            jobs.append(base + ["-include", os.path.join(HERE, "ref_solver_shim.h"), "-I" + REF, "-c", f_src,
+                                "-o", os.path.join(out, driver + ".o")])
+            continue
         jobs.append(base + ["-include", os.path.join(HERE, "ref_solver_shim.h"), "-c", os.path.join(REF, f),
                             "-o", os.path.join(out, f + ".o")])
     jobs.append(base + ["-c", os.path.join(HERE, "cpu_rpy_mobility_solver.cpp"),
@@ -166,6 +176,25 @@ def run_case(case: str, exe: str | None = None) -> str:
     if r.returncode != 0:
         raise RuntimeError(r.stderr + r.stdout[-2000:])
     return rundir
+
+
+def run_prescribed_dump(case: str) -> str:
+    """Build the case with prescribed_dump.cpp as its driver, run it, and
+    return the path of its dump (see prescribed_dump.cpp)."""
+    exe = build(case, tag="_dump", driver="prescribed_dump.cpp")
+    rundir = os.path.join(os.path.dirname(exe), "run")
+    os.makedirs(rundir, exist_ok=True)
+    for f in os.listdir(rundir):
+        os.remove(os.path.join(rundir, f))
+    blobs, fils = seeds(case)
+    spec = CASES[case]
+    import numpy as np
+    np.savetxt(os.path.join(rundir, f"sphere{spec['NBLOB']}.seed"), blobs.ravel()[None, :], fmt="%.17g")
+    np.savetxt(os.path.join(rundir, f"sphere{spec['NFIL']}.seed"), fils.ravel()[None, :], fmt="%.17g")
+    r = subprocess.run([exe], cwd=rundir, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr + r.stdout[-2000:])
+    return os.path.join(rundir, "prescribed_dump.txt")
 
 
 def run_restart(case: str, extra_steps: int) -> tuple[str, str]:

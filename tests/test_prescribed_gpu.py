@@ -1,0 +1,56 @@
+"""Prescribed-shape cilia: the linear solves of mobility_solver::compute_velocities
+(CILIA_TYPE 3) against the reference's own, step by step.
+
+tests/golden/prescribed.npz comes from the reference's unmodified sources
+built for CILIA_TYPE 3 (its coral-larvae beat fit, phases at constant speed,
+one sphere of 162 blobs with 4 x 20-segment cilia) and driven by
+oracle/ref_solver/prescribed_dump.cpp, which records what the mobility solver
+received and returned at every step (tests/golden/make_golden_prescribed.py).
+Each solve here gets the same segment positions, shape-velocity directions,
+phase speeds and body state, warm-starts from the previous solve as the
+reference does, and must return the same segment forces, blob forces and
+body velocities to the GMRES tolerance (1e-10).
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+SOLVE_TOL = 1e-7  # GMRES stops at a relative residual of 1e-10 on both sides
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32c"])
+def test_prescribed_solves_match_reference(gmi_lib, precision):
+    from generic_mobility_interface_class_gb300.solver import MobilitySolver
+    g = load_golden("prescribed", prefix="")
+    nfil, nseg, nblob = int(g["nfil"]), int(g["nseg"]), int(g["nblob"])
+    s = MobilitySolver(nswim=1, nfil=nfil, nseg=nseg, nblob=nblob, mu=float(g["mu"]), rseg=float(g["rseg"]),
+                       rblob=float(g["rblob"]), linear_tol=float(g["linear_tol"]),
+                       max_linear_iter=int(g["max_linear_iter"]), precision=precision)
+    s.set_blob_references(g["blob_refs"])
+    S = nfil * nseg
+    tol = SOLVE_TOL if precision == 0 else 1e-4
+    for k in range(len(g["gmres_iters"])):
+        s.x_segs_host[:] = g["x_segs"][k].reshape(S, 3)
+        it = s.compute_velocities_prescribed(g["vel_dir"][k].reshape(S, 3), g["phase_speed"][k],
+                                             g["body_x"][k].reshape(1, 3), g["body_q"][k].reshape(1, 4))
+        fs = np.array(s.f_segs_host[:, :3])
+        want_fs = g["f_segs"][k].reshape(S, 6)[:, :3]
+        assert rel_err(fs, want_fs) < tol, (k, rel_err(fs, want_fs))
+        assert np.all(np.array(s.f_segs_host[:, 3:]) == 0.0)
+        assert rel_err(np.array(s.f_blobs_host), g["f_blobs"][k].reshape(nblob, 3)) < tol, k
+        assert rel_err(s.v_bodies().ravel(), g["v_bodies"][k]) < tol, k
+        if precision == 0:
+            assert abs(it - int(g["gmres_iters"][k])) <= 3, (k, it, int(g["gmres_iters"][k]))
+    s.close()
+
+
+def test_prescribed_rejects_the_wall(gmi_lib):
+    from generic_mobility_interface_class_gb300._lib import GmiError
+    from generic_mobility_interface_class_gb300.solver import MobilitySolver
+    s = MobilitySolver(nswim=1, nfil=1, nseg=4, nblob=0, wall=True)
+    with pytest.raises(GmiError):
+        s.compute_velocities_prescribed(np.zeros((4, 3)), np.ones(1))
+    s.close()
