@@ -283,6 +283,7 @@ def run_gmi(args, world, rank, local):
     if not args.no_autotune:
         ctx.autotune(0, n, n)
     tpb, tt, splits, tuned = ctx.tuned_shape(0, n, n)
+    per_step = ctx.tuned_sources_per_step(0, n, n)
     for _ in range(args.warmup):
         ctx.mss(xd, fd, out=vd)
     ctx.synchronize()
@@ -384,7 +385,8 @@ def run_gmi(args, world, rank, local):
                                    f"f,tau ~ N(0,1), 6-dof Mss formula, all pairs incl. self)",
                        "n": n, "precision": args.precision, "parallelism": f"replicas x{world}",
                        "launch_shape": {"threads_per_cta": tpb, "targets_per_thread": tt,
-                                        "source_splits": splits or "auto", "autotuned": tuned},
+                                        "source_splits": splits or "auto", "sources_per_step": per_step,
+                                        "autotuned": tuned},
                        "l2": "flushed (256 MB write) between timed steps"},
             "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(n * 9 * 8),
                     "d2h_bytes_per_step": int(n * 6 * 8), "path": "gmi_Mss_mult with pinned host X,F -> V"},

@@ -56,6 +56,8 @@ SIGNATURES = {
     "gmi_autotune": ([_P, _I, _I, _I], _I),
     "gmi_measure_fma_peak": ([_P, _I, ctypes.POINTER(_D)], _I),
     "gmi_tuned_shape": ([_P, _I, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
+    "gmi_tuned_sources_per_step": ([_P, _I, _I, _I, ctypes.POINTER(_I)], _I),
+    "gmi_set_shape": ([_P, _I, _I, _I, _I, _I, _I, _I], _I),
     "gmi_solver_create": ([_P, ctypes.POINTER(_P)], _I),
     "gmi_solver_destroy": ([_P], _I),
     "gmi_solver_host_arrays": ([_P, _P], _I),

@@ -243,6 +243,32 @@ gmi_status gmi_tuned_shape(const gmi_context *ctx, int kind, int num_targets, in
     return found ? GMI_OK : GMI_ERR_STATE;
 }
 
+gmi_status gmi_tuned_sources_per_step(const gmi_context *ctx, int kind, int num_targets, int num_sources,
+                                      int *sources_per_step)
+{
+    GMI_ARG_CHECK(ctx && sources_per_step, "gmi_tuned_sources_per_step: null argument");
+    PairShape s;
+    auto it = ctx->tuned.find(TuneKey{kind, ctx->precision, num_targets, num_sources});
+    const bool found = it != ctx->tuned.end();
+    if (found) s = it->second;
+    *sources_per_step = pair_shape_is_packed(s, kind, ctx->precision == GMI_FP64) ? 2 : 1;
+    return found ? GMI_OK : GMI_ERR_STATE;
+}
+
+gmi_status gmi_set_shape(gmi_context *ctx, int kind, int num_targets, int num_sources, int threads_per_cta,
+                         int targets_per_thread, int source_splits, int sources_per_step)
+{
+    GMI_ARG_CHECK(ctx != nullptr, "gmi_set_shape: null context");
+    GMI_ARG_CHECK(kind >= 0 && kind <= 4, "gmi_set_shape: kind must be 0..4");
+    GMI_ARG_CHECK(source_splits >= 0, "gmi_set_shape: source_splits must be >= 0");
+    GMI_ARG_CHECK(sources_per_step == 1 || sources_per_step == 2, "gmi_set_shape: sources_per_step must be 1 or 2");
+    const bool f64 = ctx->precision == GMI_FP64;
+    PairShape s{threads_per_cta, targets_per_thread, source_splits, sources_per_step == 2 ? 1 : 0};
+    GMI_ARG_CHECK(pair_shape_exists(s, kind, f64), "gmi_set_shape: no kernel for this shape, kind and precision");
+    ctx->tuned[TuneKey{kind, ctx->precision, num_targets, num_sources}] = s;
+    return GMI_OK;
+}
+
 gmi_status gmi_autotune(gmi_context *ctx, int kind, int num_targets, int num_sources)
 {
     GMI_ARG_CHECK(ctx != nullptr, "gmi_autotune: null context");

@@ -26,6 +26,7 @@ struct PairShape {
     int tpb = 128;     // threads per CTA
     int tt = 2;        // targets per thread
     int splits = 0;    // source splits; 0 = choose from the SM count
+    int packed = -1;   // two sources per thread step (FP32, no wall): 1 yes, 0 no, -1 where available
 };
 
 enum PairKind : int { kSS = 0, kSSWall = 1, kBB = 2, kSB = 3, kBS = 4 };

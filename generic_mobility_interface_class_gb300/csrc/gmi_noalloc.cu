@@ -131,7 +131,7 @@ extern "C" gmi_status gmi_Mss_mult_noalloc(double *V_d, const double *F_d, const
     env.sm_count = d->sm_count;
     const bool small = (long long)num_segs * 2 < (long long)d->sm_count * 256;
     env.tpb = small ? 64 : 128;
-    env.tt = small ? 1 : 2;
+    env.tt = (small || !f64) ? 1 : 2;  // FP32: the packed kernel, one target per thread
     st = launch_pair_into(env, kSS, f64, records, start_seg, num_segs, records, total_segs, k, V_d, 0);
     if (st != GMI_OK) return st;
     // V is complete when this returns; report a bounded-wait timeout, if any

@@ -17,10 +17,12 @@
 //      and a reduce kernel adds them in split order into the output (= or +=).
 #include <algorithm>
 #include <cstdio>
+#include <type_traits>
 #include <vector>
 
 #include "gmi_context.hpp"
 #include "gmi_pairs.cuh"
+#include "gmi_pairs2.cuh"
 #include "gmi_pair_kernels.hpp"
 
 namespace gmi {
@@ -308,6 +310,188 @@ __global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ C
             double *o = args.out + (size_t)ti[k] * NOUT;
 #pragma unroll
             for (int c = 0; c < NOUT; ++c) o[c] = args.accumulate ? o[c] + acc[k].total(c) : acc[k].total(c);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2'. packed FP32 variant (kinds SS, BB, SB, BS): each thread takes two
+// sources per step, one per lane of the packed f32x2 instructions.  After a
+// tile lands, the CTA rewrites it into a pair-interleaved buffer (every
+// record component as {source 2p, source 2p+1}, positions negated so that
+// differences are additions); the TMA stage is free again right after that
+// pass, so a 2-deep ring suffices, and the interleaved buffer is double
+// buffered so that one barrier per tile orders everything:
+//   wait(stage) -> interleave into ibuf[t&1] -> barrier -> refill stage
+//   -> compute on ibuf[t&1]
+// (a thread interleaves tile t+1 into ibuf[(t+1)&1] only after the barrier
+// of tile t, which every thread reaches after finishing tile t-1).
+// Accumulation: per target, plus and minus parts per lane (gmi_pairs2.cuh),
+// added up at the end of each tile and folded into the (hi, lo) total.
+// ---------------------------------------------------------------------------
+constexpr int kStagesP = 2;
+constexpr int kTilePairs = kTile / 2;
+
+template <int KIND>
+__device__ __forceinline__ void pair2_apply(float2 dx, float2 dy, float2 dz, const float2 *F,
+                                            const KernelConsts<float> &K, float2 *p, float2 *m)
+{
+    if constexpr (KIND == kSS) pair2_ss(dx, dy, dz, F, K.eq, p, m);
+    if constexpr (KIND == kBB) pair2_bb(dx, dy, dz, F, K.eq, p);
+    if constexpr (KIND == kSB) pair2_sb(dx, dy, dz, F, K.uq, p, m);
+    if constexpr (KIND == kBS) pair2_bs(dx, dy, dz, F, K.uq, p, m);
+}
+
+template <int KIND, int TPB, int TT>
+__global__ void __launch_bounds__(TPB) rpy_pair2_kernel(const __grid_constant__ CUtensorMap src_map,
+                                                        const PairLaunch args)
+{
+    constexpr int NOUT = KindTraits<KIND>::nout;
+    constexpr int kStageScalars = kTile * kRecLen;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float *ring = reinterpret_cast<float *>(smem_raw);
+    float4 *ibuf = reinterpret_cast<float4 *>(smem_raw + kStagesP * kStageScalars * sizeof(float));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + (kStagesP + 2) * kStageScalars * sizeof(float));
+
+    if (args.skip != nullptr && *args.skip != 0) return;
+    const int tid = threadIdx.x;
+    const int j_begin = blockIdx.y * args.chunk;
+    const int j_end = min(j_begin + args.chunk, args.n_src);
+    const int ntiles = j_end > j_begin ? (j_end - j_begin + kTile - 1) / kTile : 0;
+    constexpr unsigned kBoxBytes = kStageScalars * sizeof(float);
+
+    if (tid == 0) {
+        prefetch_tensormap(&src_map);
+#pragma unroll
+        for (int s = 0; s < kStagesP; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int issued = 0;  // tiles requested so far (meaningful on thread 0)
+    if (tid == 0) {
+        for (; issued < kStagesP && issued < ntiles; ++issued) {
+            mbar_arrive_expect_tx(&bars[issued], kBoxBytes);
+            tma_load_2d(ring + issued * kStageScalars, &src_map, 0, j_begin + issued * kTile, &bars[issued]);
+        }
+    }
+
+    const KernelConsts<float> K = convert_consts<float>(args.k);
+    // loads enter the packed formulas times 1/(8 pi mu) (gmi_pairs2.cuh)
+    const float load_scale = (KIND == kSB || KIND == kBS) ? K.uq.f8pm : K.eq.f8pm;
+    const float *tgt_rec = reinterpret_cast<const float *>(args.tgt_rec);
+    float2 th[TT][3], tl[TT][3];  // target position (hi, lo), both lanes
+    int ti[TT];
+    float2 p[TT][NOUT], m[TT][NOUT];
+    float hi[TT][NOUT], lo[TT][NOUT];
+#pragma unroll
+    for (int k = 0; k < TT; ++k) {
+        ti[k] = blockIdx.x * (TPB * TT) + k * TPB + tid;
+        const Pos<float> tp = load_tgt(tgt_rec, args.tgt_start + min(ti[k], args.n_tgt - 1));
+        th[k][0] = bc2(tp.x); th[k][1] = bc2(tp.y); th[k][2] = bc2(tp.z);
+        tl[k][0] = bc2(tp.lx); tl[k][1] = bc2(tp.ly); tl[k][2] = bc2(tp.lz);
+#pragma unroll
+        for (int c = 0; c < NOUT; ++c) {
+            p[k][c] = m[k][c] = make_float2(0.f, 0.f);
+            hi[k][c] = lo[k][c] = 0.f;
+        }
+    }
+
+    bool timed_out = false;
+    int t = 0;
+    for (; t < ntiles; ++t) {
+        const int s = t % kStagesP;
+        const bool ok = mbar_wait_bounded(&bars[s], (t / kStagesP) & 1);
+        const int j0 = j_begin + t * kTile;
+        const int jn = min(kTile, j_end - j0);
+        const int npair = (jn + 1) >> 1;
+        float4 *ib = ibuf + (t & 1) * (kTilePairs * 6);
+        if (ok) {
+            // interleave: item (pair pp, quarter q) turns float4 q of records
+            // 2pp and 2pp+1 into two float4 of {a, b} lanes; a missing odd
+            // source (jn odd) is all zeros and contributes nothing
+            const float4 *st = reinterpret_cast<const float4 *>(ring + s * kStageScalars);
+            for (int it = tid; it < 3 * npair; it += TPB) {
+                const int pp = it / 3, q = it - 3 * pp;
+                float4 a = st[6 * pp + q];
+                float4 b = 2 * pp + 1 < jn ? st[6 * pp + 3 + q] : make_float4(0.f, 0.f, 0.f, 0.f);
+                if (q < 2) {  // .xyz are positions (hi for q = 0, lo for q = 1), .w a load
+                    a.x = -a.x; a.y = -a.y; a.z = -a.z;
+                    b.x = -b.x; b.y = -b.y; b.z = -b.z;
+                    a.w *= load_scale; b.w *= load_scale;
+                } else {
+                    a.x *= load_scale; a.y *= load_scale; a.z *= load_scale; a.w *= load_scale;
+                    b.x *= load_scale; b.y *= load_scale; b.z *= load_scale; b.w *= load_scale;
+                }
+                ib[6 * pp + 2 * q] = make_float4(a.x, b.x, a.y, b.y);
+                ib[6 * pp + 2 * q + 1] = make_float4(a.z, b.z, a.w, b.w);
+            }
+        }
+        if (__syncthreads_or(!ok)) {
+            timed_out = true;
+            break;
+        }
+        // every thread has interleaved tile t: its stage can be refilled
+        if (tid == 0 && issued < ntiles) {
+            mbar_arrive_expect_tx(&bars[s], kBoxBytes);
+            tma_load_2d(ring + s * kStageScalars, &src_map, 0, j_begin + issued * kTile, &bars[s]);
+            ++issued;
+        }
+#pragma unroll 2
+        for (int pp = 0; pp < npair; ++pp) {
+            // record order: [xh yh zh f0][xl yl zl f1][f2 f3 f4 f5], lanes paired
+            const float4 q0 = ib[6 * pp], q1 = ib[6 * pp + 1], q2 = ib[6 * pp + 2];
+            const float4 q3 = ib[6 * pp + 3], q4 = ib[6 * pp + 4], q5 = ib[6 * pp + 5];
+            const float2 nxh = make_float2(q0.x, q0.y), nyh = make_float2(q0.z, q0.w);
+            const float2 nzh = make_float2(q1.x, q1.y);
+            const float2 nxl = make_float2(q2.x, q2.y), nyl = make_float2(q2.z, q2.w);
+            const float2 nzl = make_float2(q3.x, q3.y);
+            const float2 F[6] = {make_float2(q1.z, q1.w), make_float2(q3.z, q3.w), make_float2(q4.x, q4.y),
+                                 make_float2(q4.z, q4.w), make_float2(q5.x, q5.y), make_float2(q5.z, q5.w)};
+#pragma unroll
+            for (int k = 0; k < TT; ++k) {
+                const float2 dx = add2(add2(th[k][0], nxh), add2(tl[k][0], nxl));
+                const float2 dy = add2(add2(th[k][1], nyh), add2(tl[k][1], nyl));
+                const float2 dz = add2(add2(th[k][2], nzh), add2(tl[k][2], nzl));
+                pair2_apply<KIND>(dx, dy, dz, F, K, p[k], m[k]);
+            }
+        }
+        // tile sum of both lanes, plus minus minus, folded by two-sum
+#pragma unroll
+        for (int k = 0; k < TT; ++k) {
+#pragma unroll
+            for (int c = 0; c < NOUT; ++c) {
+                const float v = (p[k][c].x + p[k][c].y) - (m[k][c].x + m[k][c].y);
+                const float sum = hi[k][c] + v;
+                const float bp = sum - hi[k][c];
+                lo[k][c] += (hi[k][c] - (sum - bp)) + (v - bp);
+                hi[k][c] = sum;
+                p[k][c] = m[k][c] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+
+    if (timed_out) {
+        if (tid == 0) {
+            atomicOr(args.err, kDevErrWaitTimeout);
+            for (int u = t; u < issued; ++u) (void)mbar_wait_bounded(&bars[u % kStagesP], (u / kStagesP) & 1);
+        }
+        return;
+    }
+
+#pragma unroll
+    for (int k = 0; k < TT; ++k) {
+        if (ti[k] >= args.n_tgt) continue;
+        if (args.partial != nullptr) {
+            double *o = args.partial + ((size_t)blockIdx.y * args.n_tgt + ti[k]) * NOUT;
+#pragma unroll
+            for (int c = 0; c < NOUT; ++c) o[c] = (double)hi[k][c] + (double)lo[k][c];
+        } else {
+            double *o = args.out + (size_t)ti[k] * NOUT;
+#pragma unroll
+            for (int c = 0; c < NOUT; ++c) {
+                const double v = (double)hi[k][c] + (double)lo[k][c];
+                o[c] = args.accumulate ? o[c] + v : v;
+            }
         }
     }
 }
@@ -660,17 +844,29 @@ static gmi_status make_record_map(gmi_context *ctx, CUtensorMap *map, const void
     return GMI_OK;
 }
 
-// Kernel table: (kind, precision, tpb, tt) -> launcher.
+// Kernel table: (kind, precision, tpb, tt, packed) -> kernel.  Packed
+// entries exist for FP32 and the kinds without a wall.
 using KernelFn = void (*)(CUtensorMap, PairLaunch);
 
 template <int KIND, class R, int TPB, int TT> struct Inst {
     static void *fn() { return reinterpret_cast<void *>(&rpy_pair_kernel<KIND, R, TPB, TT>); }
 };
+template <int KIND, class R, int TPB, int TT> struct Inst2 {
+    static void *fn()
+    {
+        if constexpr (std::is_same<R, float>::value && KIND != kSSWall)
+            return reinterpret_cast<void *>(&rpy_pair2_kernel<KIND, TPB, TT>);
+        else
+            return nullptr;
+    }
+};
 
 struct ShapeEntry {
-    int tpb, tt;
+    int tpb, tt, packed;
 };
-static const ShapeEntry kShapes[] = {{128, 1}, {128, 2}, {256, 1}, {256, 2}, {128, 4}, {64, 1}, {64, 2}};
+static const ShapeEntry kShapes[] = {{128, 1, 0}, {128, 2, 0}, {256, 1, 0}, {256, 2, 0}, {128, 4, 0},
+                                     {64, 1, 0},  {64, 2, 0},  {64, 1, 1},  {64, 2, 1},  {128, 1, 1},
+                                     {128, 2, 1}, {256, 1, 1}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
 template <int KIND, class R> static void *kernel_for_shape(int idx)
@@ -682,7 +878,12 @@ template <int KIND, class R> static void *kernel_for_shape(int idx)
         case 3: return Inst<KIND, R, 256, 2>::fn();
         case 4: return Inst<KIND, R, 128, 4>::fn();
         case 5: return Inst<KIND, R, 64, 1>::fn();
-        default: return Inst<KIND, R, 64, 2>::fn();
+        case 6: return Inst<KIND, R, 64, 2>::fn();
+        case 7: return Inst2<KIND, R, 64, 1>::fn();
+        case 8: return Inst2<KIND, R, 64, 2>::fn();
+        case 9: return Inst2<KIND, R, 128, 1>::fn();
+        case 10: return Inst2<KIND, R, 128, 2>::fn();
+        default: return Inst2<KIND, R, 256, 1>::fn();
     }
 }
 
@@ -697,6 +898,8 @@ static void *kernel_ptr(int kind, bool f64, int shape_idx)
         default: return f64 ? kernel_for_shape<kBS, double>(shape_idx) : kernel_for_shape<kBS, float>(shape_idx);
     }
 }
+
+static bool packed_available(int kind, bool f64) { return !f64 && kind != kSSWall; }
 
 constexpr int kWarpShapeTpb = kPairWarpShapeTpb;
 constexpr int kWarpMaxSources = kPairWarpMaxSources;
@@ -734,14 +937,40 @@ static gmi_status launch_warp(cudaStream_t stream, int kind, bool f64, int tpw, 
     return GMI_OK;
 }
 
-static int shape_index(int tpb, int tt)
+// Index of the table entry for (tpb, tt); packed < 0 picks the packed
+// variant where it exists.  Falls back to the scalar (tpb, tt) entry, then to
+// 128 x 2.
+static int shape_index(int tpb, int tt, int packed, int kind, bool f64)
 {
+    const int want = packed < 0 ? (packed_available(kind, f64) ? 1 : 0) : (packed_available(kind, f64) ? packed : 0);
     for (int i = 0; i < kNumShapes; ++i)
-        if (kShapes[i].tpb == tpb && kShapes[i].tt == tt) return i;
+        if (kShapes[i].tpb == tpb && kShapes[i].tt == tt && kShapes[i].packed == want) return i;
+    for (int i = 0; i < kNumShapes; ++i)
+        if (kShapes[i].tpb == tpb && kShapes[i].tt == tt && kShapes[i].packed == 0) return i;
     return 1;
 }
 
-static size_t ring_bytes(bool f64) { return (size_t)kStages * kTile * kRecLen * (f64 ? 8 : 4) + kStages * 8; }
+bool pair_shape_exists(const PairShape &s, int kind, bool f64)
+{
+    if (s.tpb == kWarpShapeTpb) return (s.tt == 1 || s.tt == 2) && s.packed != 1;
+    for (int i = 0; i < kNumShapes; ++i)
+        if (kShapes[i].tpb == s.tpb && kShapes[i].tt == s.tt &&
+            (s.packed < 0 || kShapes[i].packed == s.packed) && (!kShapes[i].packed || packed_available(kind, f64)))
+            return true;
+    return false;
+}
+
+bool pair_shape_is_packed(const PairShape &s, int kind, bool f64)
+{
+    if (s.tpb == kWarpShapeTpb) return false;
+    return kShapes[shape_index(s.tpb, s.tt, s.packed, kind, f64)].packed != 0;
+}
+
+static size_t ring_bytes(bool f64, bool packed)
+{
+    if (packed) return (size_t)(kStagesP + 2) * kTile * kRecLen * sizeof(float) + kStagesP * 8;
+    return (size_t)kStages * kTile * kRecLen * (f64 ? 8 : 4) + kStages * 8;
+}
 
 static int nout_of(int kind) { return (kind == kBB || kind == kBS) ? 3 : 6; }
 
@@ -777,6 +1006,8 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
             shape = PairShape{kWarpShapeTpb, 2, 0};  // few sources: warp per two targets
         } else if ((long long)n_tgt * 2 < (long long)ctx->sm_count * 256) {
             shape = PairShape{64, 1, 0};  // small target sets: more, smaller CTAs
+        } else if (packed_available(kind, f64)) {
+            shape = PairShape{128, 1, 0};
         }
     }
     if (shape.tpb == kWarpShapeTpb) {
@@ -793,10 +1024,10 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
         if (ws == GMI_OK) ctx->launches++;
         return ws;
     }
-    const int sidx = shape_index(shape.tpb, shape.tt);
+    const int sidx = shape_index(shape.tpb, shape.tt, shape.packed, kind, f64);
     const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;
     void *fn = kernel_ptr(kind, f64, sidx);
-    const size_t smem = ring_bytes(f64);
+    const size_t smem = ring_bytes(f64, kShapes[sidx].packed != 0);
     GMI_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, tpb, smem));
@@ -891,12 +1122,15 @@ gmi_status autotune_pair(gmi_context *ctx, int kind, const void *tgt_rec, int n_
     GMI_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
     PairShape best_shape;
+    const bool f64 = ctx->precision == GMI_FP64;
     for (int si = 0; si < kNumShapes + 2; ++si) {
         const bool warp = si >= kNumShapes;
-        for (int sp : {0, 1, 2, 4, 8}) {
+        if (!warp && kShapes[si].packed && !packed_available(kind, f64)) continue;
+        if (warp && n_src > 4 * kWarpMaxSources) continue;  // the warp kernel is for small source sets
+        for (int sp : {0, 1, 2, 4, 8, 16, 32}) {
             if (warp && sp != 0) continue;
             PairShape s = warp ? PairShape{kWarpShapeTpb, si - kNumShapes + 1, 0}
-                               : PairShape{kShapes[si].tpb, kShapes[si].tt, sp};
+                               : PairShape{kShapes[si].tpb, kShapes[si].tt, sp, kShapes[si].packed};
             gmi_status st = launch_pair(ctx, kind, tgt_rec, 0, n_tgt, src_rec, n_src, k, out, 0, &s);
             if (st != GMI_OK) return st;
             GMI_CUDA_TRY(cudaEventRecord(e0, ctx->stream));
@@ -993,10 +1227,10 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
         a.skip = env.skip;
         return launch_warp(env.stream, kind, f64, env.tt, a, src_rec);
     }
-    const int sidx = shape_index(env.tpb, env.tt);
+    const int sidx = shape_index(env.tpb, env.tt, env.scalar_only ? 0 : -1, kind, f64);
     const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;
     void *fn = kernel_ptr(kind, f64, sidx);
-    const size_t smem = ring_bytes(f64);
+    const size_t smem = ring_bytes(f64, kShapes[sidx].packed != 0);
     GMI_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, tpb, smem));

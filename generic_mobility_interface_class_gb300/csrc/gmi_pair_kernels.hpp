@@ -60,6 +60,11 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
 
 gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &a);
 
+// Whether a kernel exists for this shape, kind and precision, and whether the
+// shape resolves to the packed (two sources per step) kernel.
+bool pair_shape_exists(const PairShape &s, int kind, bool f64);
+bool pair_shape_is_packed(const PairShape &s, int kind, bool f64);
+
 gmi_status autotune_pair(gmi_context *ctx, int kind, const void *tgt_rec, int n_tgt, const void *src_rec, int n_src,
                          const PairConsts &k, double *out);
 
@@ -72,6 +77,7 @@ struct ExplicitPairEnv {
     void *encode_tiled;    // cuTensorMapEncodeTiled
     int sm_count;
     int tpb, tt;           // launch shape
+    int scalar_only;       // non-zero: one source per thread step even where the packed kernel exists
     const int *skip;       // optional device flag: non-zero turns the launch into a no-op
 };
 

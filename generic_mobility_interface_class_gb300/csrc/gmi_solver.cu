@@ -970,7 +970,7 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     } else {
         const bool small = (long long)nb * 2 < (long long)ctx->sm_count * 256;
         env.tpb = small ? 64 : 128;
-        env.tt = small ? 1 : 2;
+        env.tt = (small || !f64) ? 1 : 2;  // FP32: the packed kernel, one target per thread
     }
     env.skip = &s->ctl->done;
     PairConsts k;

@@ -138,3 +138,16 @@ class Context:
         st = self.lib.gmi_tuned_shape(self.handle, kind, num_targets, num_sources, ctypes.byref(a),
                                       ctypes.byref(b), ctypes.byref(c))
         return a.value, b.value, c.value, st == 0
+
+    def tuned_sources_per_step(self, kind: int, num_targets: int, num_sources: int) -> int:
+        """2 when that size runs the packed FP32 kernel (two sources per
+        f32x2 step), else 1."""
+        a = ctypes.c_int()
+        self.lib.gmi_tuned_sources_per_step(self.handle, kind, num_targets, num_sources, ctypes.byref(a))
+        return a.value
+
+    def set_shape(self, kind: int, num_targets: int, num_sources: int, threads_per_cta: int,
+                  targets_per_thread: int, source_splits: int = 0, sources_per_step: int = 2) -> None:
+        """Pin the launch shape used for this kernel and size."""
+        check(self.lib.gmi_set_shape(self.handle, kind, num_targets, num_sources, threads_per_cta,
+                                     targets_per_thread, source_splits, sources_per_step))

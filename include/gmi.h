@@ -143,6 +143,19 @@ GMI_API gmi_status gmi_autotune(gmi_context *ctx, int kind, int num_targets, int
  * Returns GMI_ERR_STATE if the size was never tuned (defaults apply). */
 GMI_API gmi_status gmi_tuned_shape(const gmi_context *ctx, int kind, int num_targets, int num_sources,
                                    int *threads_per_cta, int *targets_per_thread, int *source_splits);
+/* Sources one thread takes per step in that shape: 2 for the packed FP32
+ * kernel (two sources per f32x2 instruction), 1 otherwise.  Same return
+ * convention as gmi_tuned_shape. */
+GMI_API gmi_status gmi_tuned_sources_per_step(const gmi_context *ctx, int kind, int num_targets, int num_sources,
+                                              int *sources_per_step);
+/* Pin the launch shape of one pair kernel and size (what gmi_autotune would
+ * store).  threads_per_cta / targets_per_thread: a tiled shape (64, 128 or
+ * 256 threads; 1, 2 or 4 targets as the kernel table has them) or 32 for the
+ * warp-per-target kernel (1 or 2 targets per warp); source_splits 0 =
+ * automatic; sources_per_step 2 (packed) needs FP32 and kind != 1.
+ * GMI_ERR_ARG for a shape that has no kernel. */
+GMI_API gmi_status gmi_set_shape(gmi_context *ctx, int kind, int num_targets, int num_sources, int threads_per_cta,
+                                 int targets_per_thread, int source_splits, int sources_per_step);
 
 /* ------------------------------------------------------------------------
  * Mobility solver: the device-resident replacement of the reference's

@@ -112,6 +112,66 @@ def test_tiled_kernel_against_oracle(prec_ctx, oracle_built):
     assert rel_err(got, rpy.mbs(xs, x, f, a_seg=1.0, a_blob=1.4)) < tol
 
 
+TILED_SHAPES = [(128, 1), (128, 2), (256, 1), (256, 2), (128, 4), (64, 1), (64, 2)]
+PACKED_SHAPES = [(64, 1), (64, 2), (128, 1), (128, 2), (256, 1)]
+
+
+@pytest.fixture
+def own_ctx(gmi_lib):
+    """A context of its own: pinned shapes and precision stay in this test."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from generic_mobility_interface_class_gb300.mobility import Context
+    ctx = Context(0)
+    yield ctx
+    ctx.close()
+
+
+@pytest.mark.parametrize("splits", [0, 3])
+@pytest.mark.parametrize("per_step,tpb,tt", [(1, *s) for s in TILED_SHAPES] + [(2, *s) for s in PACKED_SHAPES])
+def test_every_tiled_shape_against_oracle(own_ctx, oracle_built, per_step, tpb, tt, splits):
+    """Every entry of the tiled-kernel table, scalar (one source per thread
+    step) and packed (two sources per f32x2 step), pinned with set_shape, on
+    an odd source count (a ragged last tile whose last source has no
+    partner) and with forced source splits: all four free-space kinds
+    against the FP64 oracle at the FP32C bound."""
+    from generic_mobility_interface_class_gb300 import seeding
+    rpy = oracle_built
+    ctx = own_ctx
+    ctx.set_precision(1)
+    n, ns = 1031, 301
+    x = seeding.random_cube(n, seed=23)
+    f = np.random.default_rng(23).normal(size=(n, 6))
+    xs = x[:ns] + 0.37
+    for kind, nt, nsrc in [(0, n, n), (2, n, n), (3, ns, n), (4, ns, n)]:
+        ctx.set_shape(kind, nt, nsrc, tpb, tt, splits, per_step)
+        assert ctx.tuned_sources_per_step(kind, nt, nsrc) == per_step
+    assert rel_err(N(ctx.mss(T(x), T(f))), rpy.mss(x, f)) < FP32C_TOL
+    assert rel_err(N(ctx.mbb(T(x), T(f[:, :3]))), rpy.mbb(x, f[:, :3])) < FP32C_TOL
+    v_in = np.random.default_rng(24).normal(size=(ns, 6))
+    v = T(v_in)
+    ctx.msb(T(xs), T(x), T(f[:, :3]), v, a_seg=1.0, a_blob=1.4)
+    assert rel_err(N(v), rpy.msb(xs, x, f[:, :3], a_seg=1.0, a_blob=1.4, v_in=v_in)) < FP32C_TOL
+    got = N(ctx.mbs(T(xs), T(x), T(f), a_seg=1.0, a_blob=1.4))
+    assert rel_err(got, rpy.mbs(xs, x, f, a_seg=1.0, a_blob=1.4)) < FP32C_TOL
+
+
+def test_set_shape_rejects_missing_kernels(own_ctx):
+    """No packed kernel in FP64 or for the wall kind; no 64 x 4 entry."""
+    from generic_mobility_interface_class_gb300._lib import GmiError
+    ctx = own_ctx
+    ctx.set_precision(0)
+    with pytest.raises(GmiError):
+        ctx.set_shape(0, 100, 100, 128, 2, 0, 2)
+    ctx.set_precision(1)
+    with pytest.raises(GmiError):
+        ctx.set_shape(1, 100, 100, 128, 2, 0, 2)
+    with pytest.raises(GmiError):
+        ctx.set_shape(0, 100, 100, 64, 4, 0, 1)
+    ctx.set_shape(0, 100, 100, 32, 2, 0, 1)
+    assert ctx.tuned_shape(0, 100, 100)[:2] == (32, 2)
+
+
 def test_target_slices_and_accumulate(gpu_ctx, oracle_built):
     rpy = oracle_built
     g = load_golden("swimmer_sphere")
