@@ -1,0 +1,563 @@
+// gmi_gmres_cluster.cu -- the FP32C GMRES solve of a small free-swimmer
+// saddle-point system (mobility_solver.cpp:970-1354, the CILIA_TYPE != 3
+// branches of apply_preconditioner :651-721 and system_matrix_mult
+// :905-962) run to completion by ONE thread-block cluster.
+//
+// At small sizes (a few hundred to two thousand blobs) the graph-replayed
+// Arnoldi step is bound by latency: six dependent kernels whose cross-CTA
+// sums go through L2 (fence, atomic ticket, reload).  Here the whole Arnoldi
+// loop is one launch of C CTAs (16 where the GPU allows non-portable
+// clusters, else 8).  Each CTA owns a contiguous slice of the blobs and their
+// rows (the last CTA also owns the 6W body rows).  Every cross-CTA sum is a
+// cluster barrier followed by one DSMEM load per lane (lane r reads CTA r)
+// and a fixed shuffle tree, so all CTAs hold bit-identical copies of h,
+// ||w|| and the Givens state and take the same stop decision.
+//
+// Per Arnoldi iteration k (phases of the multi-kernel step S1..S5):
+//   A  q = w / ||w|| into Q[:, k-1]; body moments of q  -> barrier 1
+//      z_body from the summed moments (every CTA)
+//   B  blob block of the preconditioner; the CTA's blob loads (z, FP32,
+//      pair-interleaved) into its shared memory; moments of z  -> barrier 2
+//      copy the other CTAs' loads; w_body = -K^T z (last CTA)
+//   C  blob-blob RPY sum over all blobs, packed FP32 (gmi_pairs2.cuh), from
+//      shared memory; meanwhile one reserved warp finishes the Givens step
+//      of iteration k-1, whose stop flag is read right after this phase
+//      (iteration k then ends unused: it has written only scratch and
+//      Q[:, k-1], a column past the solution)
+//      w_blob = M_bb z - K z_body
+//   D  first classical Gram-Schmidt projections  -> barrier 3, h
+//   E  w -= Q h; second projections  -> barrier 4, h2
+//   F  w -= Q h2; ||w||^2  -> barrier 5; ||w||
+// All arithmetic except the pair sum is FP64, as in the multi-kernel step.
+#include <cooperative_groups.h>
+
+#include <cmath>
+#include <cstdlib>
+
+#include "gmi_context.hpp"
+#include "gmi_gmres_cluster.hpp"
+#include "gmi_pair_kernels.hpp"
+#include "gmi_pairs2.cuh"
+#include "gmi_solver_device.cuh"
+#include "gmi_solver_internal.hpp"
+
+namespace cg = cooperative_groups;
+
+namespace gmi {
+
+constexpr int kCgTpb = 512;
+constexpr int kCgWarps = kCgTpb / 32;
+constexpr int kCgPairThreads = kCgTpb - 32;  // the last warp runs the Givens step during phase C
+constexpr int kCgMaxK = 160;                 // H rows and Givens state (>= max_iter + 1)
+constexpr int kCgMaxBlobs = 2048;
+constexpr int kCgMaxSwimmers = 16;
+constexpr int kCgFold = 16;                  // source pairs summed in FP32 before an FP64 add
+
+struct ClusterGmresArgs {
+    int W, nblob, nb, n, ldh, max_iter, bpc;
+    size_t ld;
+    double *Q, *H, *beta, *cs, *sn;
+    const double *w0;                 // r0, all n rows
+    const double *R, *refs, *ktk_rot, *mob_rot, *xb;
+    double minv, beta0, tol, norm_ref;
+    GmresCtl *ctl;
+    EqualK<float> kbb;
+};
+
+// Shared-memory layout (offsets in bytes), fixed by nb, W and bpc.
+struct CgLayout {
+    size_t ipos, iload, wl, ql, av, dl, kt, mb, mom1, mom2, sums, zb, hp1, hp2, h, h2, np, pp, csh, snh, bet, col,
+        red, flag, total;
+};
+
+__host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc)
+{
+    CgLayout L;
+    const size_t npairs = (size_t)(nb + 1) / 2, rows = 3 * (size_t)bpc + 6 * (size_t)W;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o += (bytes + 15) / 16 * 16;
+        return at;
+    };
+    L.ipos = take(npairs * 3 * sizeof(float4));   // -x hi / lo of every source pair
+    L.iload = take(npairs * 2 * sizeof(float4));  // loads of every source pair
+    L.wl = take(rows * sizeof(double));
+    L.ql = take(rows * sizeof(double));
+    L.av = take((size_t)bpc * 6 * sizeof(double));
+    L.dl = take((size_t)bpc * 3 * sizeof(double));  // R refs of the CTA's blobs
+    L.kt = take(36 * (size_t)W * sizeof(double));
+    L.mb = take(36 * (size_t)W * sizeof(double));
+    L.mom1 = take(6 * (size_t)W * sizeof(double));
+    L.mom2 = take(6 * (size_t)W * sizeof(double));
+    L.sums = take(6 * (size_t)W * sizeof(double));
+    L.zb = take(6 * (size_t)W * sizeof(double));
+    L.hp1 = take(kCgMaxK * sizeof(double));
+    L.hp2 = take(kCgMaxK * sizeof(double));
+    L.h = take(kCgMaxK * sizeof(double));
+    L.h2 = take(kCgMaxK * sizeof(double));
+    L.np = take(2 * sizeof(double));
+    L.pp = take((size_t)kCgTpb * 3 * sizeof(double));
+    L.csh = take(kCgMaxK * sizeof(double));
+    L.snh = take(kCgMaxK * sizeof(double));
+    L.bet = take((kCgMaxK + 1) * sizeof(double));
+    L.col = take((kCgMaxK + 1) * sizeof(double));
+    L.red = take(kCgWarps * sizeof(double));
+    L.flag = take(4 * sizeof(int));
+    L.total = o;
+    return L;
+}
+
+// Deterministic block sum (fixed shuffle tree, then warps in order); the
+// result is returned to thread 0 only.
+__device__ __forceinline__ double cg_block_sum(double v, double *red)
+{
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < kCgWarps; ++i) t += red[i];
+    __syncthreads();
+    return t;
+}
+
+// out[e] = sum over the cluster's CTAs of arr[e] (e < count), for every
+// thread of the CTA: groups of G lanes (G a power of two, C <= G <= 32), lane
+// r of a group loads CTA r's element, an xor-shuffle tree adds them (every
+// lane ends with the same bits, in every CTA).
+__device__ __forceinline__ void cluster_reduce(cg::cluster_group &cl, double *arr, int count, double *out, int C,
+                                               int G)
+{
+    const int groups = kCgTpb / G, gid = threadIdx.x / G, r = threadIdx.x % G;
+    for (int base = 0; base < count; base += groups) {
+        const int e = base + gid;
+        double v = 0.0;
+        if (e < count && r < C) v = cl.map_shared_rank(arr, r)[e];
+        for (int o = G >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (e < count && r == 0) out[e] = v;
+    }
+}
+
+// mom[6 s + j] = sum over the CTA's blobs t of swimmer s of av[6 t + j], one
+// warp per (s, j): lanes stride over t, then a warp sum.
+__device__ __forceinline__ void swimmer_moments(const double *av, int W, int nblob, int b0, int bl, double *mom)
+{
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int task = wid; task < 6 * W; task += kCgWarps) {
+        const int sw = task / 6, j = task % 6;
+        const int t0 = max(0, sw * nblob - b0), t1 = min(bl, (sw + 1) * nblob - b0);
+        double v = 0.0;
+        for (int t = t0 + lane; t < t1; t += 32) v += av[6 * t + j];
+        v = warp_sum(v);
+        if (lane == 0) mom[task] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmresArgs a)
+{
+    cg::cluster_group cl = cg::this_cluster();
+    const int C = (int)cl.num_blocks(), c = (int)cl.block_rank(), tid = threadIdx.x;
+    const int G = C <= 8 ? 8 : (C <= 16 ? 16 : 32);
+    extern __shared__ __align__(16) unsigned char sm[];
+    const CgLayout L = cg_layout(a.nb, a.W, a.bpc);
+    float4 *ipos = reinterpret_cast<float4 *>(sm + L.ipos);
+    float4 *iload = reinterpret_cast<float4 *>(sm + L.iload);
+    double *wl = reinterpret_cast<double *>(sm + L.wl), *ql = reinterpret_cast<double *>(sm + L.ql);
+    double *av = reinterpret_cast<double *>(sm + L.av), *dl = reinterpret_cast<double *>(sm + L.dl);
+    double *kt = reinterpret_cast<double *>(sm + L.kt), *mb = reinterpret_cast<double *>(sm + L.mb);
+    double *mom1 = reinterpret_cast<double *>(sm + L.mom1), *mom2 = reinterpret_cast<double *>(sm + L.mom2);
+    double *sums = reinterpret_cast<double *>(sm + L.sums), *zb = reinterpret_cast<double *>(sm + L.zb);
+    double *hp1 = reinterpret_cast<double *>(sm + L.hp1), *hp2 = reinterpret_cast<double *>(sm + L.hp2);
+    double *h = reinterpret_cast<double *>(sm + L.h), *h2 = reinterpret_cast<double *>(sm + L.h2);
+    double *np = reinterpret_cast<double *>(sm + L.np), *pp = reinterpret_cast<double *>(sm + L.pp);
+    double *csh = reinterpret_cast<double *>(sm + L.csh), *snh = reinterpret_cast<double *>(sm + L.snh);
+    double *bet = reinterpret_cast<double *>(sm + L.bet), *col = reinterpret_cast<double *>(sm + L.col);
+    double *red = reinterpret_cast<double *>(sm + L.red);
+    int *flag = reinterpret_cast<int *>(sm + L.flag);
+
+    const int W = a.W, nb = a.nb, nblob = a.nblob, bpc = a.bpc;
+    const int npairs = (nb + 1) / 2;
+    const int b0 = c * bpc, bl = max(0, min(nb, b0 + bpc) - b0);
+    const int bl_last = max(0, nb - (C - 1) * bpc);           // blobs of the last CTA
+    const int nr = 3 * bl + (c == C - 1 ? 6 * W : 0);
+    const int nw6 = 6 * W;
+    const float load_scale = a.kbb.f8pm;
+    auto row_of = [&](int lr) { return lr < 3 * bl ? 3 * b0 + lr : 3 * nb + (lr - 3 * bl); };
+
+    // ---- setup: r0 rows, fixed geometry (positions, R refs, 6x6 blocks) ----
+    for (int lr = tid; lr < nr; lr += kCgTpb) wl[lr] = a.w0[row_of(lr)];
+    for (int t = tid; t < bl; t += kCgTpb) {
+        const int i = b0 + t;
+        rot_apply(a.R + 9 * (i / nblob), a.refs + 3 * (i % nblob), dl + 3 * t);
+    }
+    for (int e = tid; e < 36 * W; e += kCgTpb) {
+        kt[e] = a.ktk_rot[e];
+        mb[e] = a.mob_rot[e];
+    }
+    for (int p = tid; p < npairs; p += kCgTpb) {
+        float hp[2][3], lp[2][3];
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            const int j = 2 * p + l;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const double x = j < nb ? a.xb[3 * (size_t)j + d] : 0.0;
+                const float hi = (float)x;
+                hp[l][d] = -hi;
+                lp[l][d] = -(float)(x - (double)hi);
+            }
+        }
+        ipos[3 * p] = make_float4(hp[0][0], hp[1][0], hp[0][1], hp[1][1]);
+        ipos[3 * p + 1] = make_float4(hp[0][2], hp[1][2], lp[0][0], lp[1][0]);
+        ipos[3 * p + 2] = make_float4(lp[0][1], lp[1][1], lp[0][2], lp[1][2]);
+        iload[2 * p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        iload[2 * p + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (tid == 0) {
+        bet[0] = a.beta0;
+        flag[0] = 0;
+    }
+    double nrm = a.beta0;
+    // pair-phase thread map: bl target lanes x S source splits
+    const int S = bl > 0 ? kCgPairThreads / bl : 0;
+    const int pt = bl > 0 ? tid % bl : 0, ps = bl > 0 ? tid / bl : 0;
+    const int pc = S > 0 ? (npairs + S - 1) / S : 0;
+    float2 th[3], tlo[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double x = bl > 0 ? a.xb[3 * (size_t)(b0 + pt) + d] : 0.0;
+        const float hi = (float)x;
+        th[d] = bc2(hi);
+        tlo[d] = bc2((float)(x - (double)hi));
+    }
+    __syncthreads();
+
+    for (int k = 1; k <= a.max_iter + 1; ++k) {
+        double *qcol = a.Q + a.ld * (size_t)(k - 1);
+        // ---- A: q_{k-1}, body moments ------------------------------------
+        const double inrm = 1.0 / nrm;
+        for (int lr = tid; lr < nr; lr += kCgTpb) {
+            const double q = wl[lr] * inrm;
+            ql[lr] = q;
+            qcol[row_of(lr)] = q;
+        }
+        __syncthreads();
+        for (int t = tid; t < bl; t += kCgTpb) {
+            const double *d = dl + 3 * t, *f = ql + 3 * t;
+            double *o = av + 6 * t;
+            o[0] = f[0];
+            o[1] = f[1];
+            o[2] = f[2];
+            o[3] = d[1] * f[2] - d[2] * f[1];
+            o[4] = d[2] * f[0] - d[0] * f[2];
+            o[5] = d[0] * f[1] - d[1] * f[0];
+        }
+        __syncthreads();
+        swimmer_moments(av, W, nblob, b0, bl, mom1);
+        cl.sync();  // barrier 1
+        cluster_reduce(cl, mom1, nw6, sums, C, G);
+        {
+            const double *qb_remote = cl.map_shared_rank(ql, C - 1) + 3 * bl_last;
+            for (int e = tid; e < nw6; e += kCgTpb) col[e] = qb_remote[e];  // q body rows (col is free here)
+        }
+        __syncthreads();
+        for (int e = tid; e < nw6; e += kCgTpb) {
+            const int sw = e / 6, i = e % 6;
+            const double *Kt = kt + 36 * sw, *Mb = mb + 36 * sw;
+            double x = 0.0, y = 0.0;
+            for (int j = 0; j < 6; ++j) {
+                x += Kt[i + 6 * j] * (-sums[6 * sw + j]);
+                y += Mb[i + 6 * j] * col[6 * sw + j];
+            }
+            zb[e] = x - y;
+        }
+        __syncthreads();
+        // ---- B: blob preconditioner, loads, moments of z -------------------
+        for (int t = tid; t < bl; t += kCgTpb) {
+            const int i = b0 + t, sw = i / nblob;
+            const double *U = zb + 6 * sw, *d = dl + 3 * t;
+            double o[3] = {ql[3 * t] + U[0], ql[3 * t + 1] + U[1], ql[3 * t + 2] + U[2]};
+            o[0] += U[4] * d[2] - U[5] * d[1];
+            o[1] += U[5] * d[0] - U[3] * d[2];
+            o[2] += U[3] * d[1] - U[4] * d[0];
+            for (int q = sw; q < W; ++q) {
+                o[0] *= a.minv;
+                o[1] *= a.minv;
+                o[2] *= a.minv;
+            }
+            float *ld0 = reinterpret_cast<float *>(iload + 2 * (i >> 1)), *ld1 = ld0 + 4;
+            const int l = i & 1;
+            ld0[l] = (float)o[0] * load_scale;
+            ld0[2 + l] = (float)o[1] * load_scale;
+            ld1[l] = (float)o[2] * load_scale;
+            double *b = av + 6 * t;
+            b[0] = o[0];
+            b[1] = o[1];
+            b[2] = o[2];
+            b[3] = d[1] * o[2] - d[2] * o[1];
+            b[4] = d[2] * o[0] - d[0] * o[2];
+            b[5] = d[0] * o[1] - d[1] * o[0];
+        }
+        __syncthreads();
+        swimmer_moments(av, W, nblob, b0, bl, mom2);
+        cl.sync();  // barrier 2
+        // the other CTAs' loads (bpc is even: a source pair has one owner)
+        for (int e = tid; e < 2 * npairs; e += kCgTpb) {
+            const int owner = (2 * (e >> 1)) / bpc;
+            if (owner != c) iload[e] = cl.map_shared_rank(iload, owner)[e];
+        }
+        if (c == C - 1) {
+            cluster_reduce(cl, mom2, nw6, sums, C, G);
+            __syncthreads();
+            for (int e = tid; e < nw6; e += kCgTpb) wl[3 * bl + e] = -sums[e];  // w body rows = -K^T z
+        }
+        __syncthreads();
+        // ---- C: blob-blob sum (packed FP32); Givens step of iteration k-1 ---
+        if (tid < S * bl) {
+            float2 pacc[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+            double acc[3] = {0.0, 0.0, 0.0};
+            const int p0 = ps * pc, p1 = min(npairs, p0 + pc);
+            int cnt = 0;
+#pragma unroll 2
+            for (int p = p0; p < p1; ++p) {
+                const float4 q0 = ipos[3 * p], q1 = ipos[3 * p + 1], q2 = ipos[3 * p + 2];
+                const float4 f0 = iload[2 * p], f1 = iload[2 * p + 1];
+                const float2 dx = add2(add2(th[0], make_float2(q0.x, q0.y)), add2(tlo[0], make_float2(q1.z, q1.w)));
+                const float2 dy = add2(add2(th[1], make_float2(q0.z, q0.w)), add2(tlo[1], make_float2(q2.x, q2.y)));
+                const float2 dz = add2(add2(th[2], make_float2(q1.x, q1.y)), add2(tlo[2], make_float2(q2.z, q2.w)));
+                const float2 F[3] = {make_float2(f0.x, f0.y), make_float2(f0.z, f0.w), make_float2(f1.x, f1.y)};
+                pair2_bb(dx, dy, dz, F, a.kbb, pacc);
+                if (++cnt == kCgFold) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        acc[d] += (double)(pacc[d].x + pacc[d].y);
+                        pacc[d] = make_float2(0.f, 0.f);
+                    }
+                    cnt = 0;
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < 3; ++d) pp[3 * tid + d] = acc[d] + (double)(pacc[d].x + pacc[d].y);
+        } else if (tid == kCgPairThreads && k > 1) {
+            // Givens step of iteration k - 1: H column = h + h2 and ||w||
+            const int iter = k - 1;
+            for (int i = 0; i < iter; ++i) col[i] = h[i] + h2[i];
+            col[iter] = nrm;
+            for (int i = 1; i < iter; ++i) {
+                const double u = csh[i - 1] * col[i - 1] + snh[i - 1] * col[i];
+                col[i] = csh[i - 1] * col[i] - snh[i - 1] * col[i - 1];
+                col[i - 1] = u;
+            }
+            const double hk = col[iter], hd = col[iter - 1];
+            double cc, ss;
+            if (hk == 0.0) {
+                cc = 1.0;
+                ss = 0.0;
+            } else if (fabs(hk) > fabs(hd)) {
+                const double u = hd / hk;
+                ss = (2.0 * (double)(hk > 0) - 1.0) / sqrt(1.0 + u * u);
+                cc = u * ss;
+            } else {
+                const double u = hk / hd;
+                cc = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + u * u);
+                ss = u * cc;
+            }
+            csh[iter - 1] = cc;
+            snh[iter - 1] = ss;
+            col[iter - 1] = cc * hd + ss * hk;
+            col[iter] = 0.0;
+            bet[iter] = -ss * bet[iter - 1];
+            bet[iter - 1] = cc * bet[iter - 1];
+            const double resid = fabs(bet[iter]) / a.norm_ref;
+            const int done = !(resid > a.tol) || iter >= a.max_iter;
+            flag[0] = done;
+            if (c == 0) {
+                double *gcol = a.H + (size_t)a.ldh * (iter - 1);
+                for (int i = 0; i <= iter; ++i) gcol[i] = col[i];
+                a.cs[iter - 1] = cc;
+                a.sn[iter - 1] = ss;
+                a.beta[iter - 1] = bet[iter - 1];
+                a.beta[iter] = bet[iter];
+                if (done) {
+                    a.ctl->k = iter;
+                    a.ctl->resid = resid;
+                    a.ctl->done = 1;
+                    a.ctl->replays = iter;
+                }
+            }
+        }
+        __syncthreads();
+        if (flag[0]) break;  // the same in every CTA
+        for (int t = tid; t < bl; t += kCgTpb) {
+            double mbb[3] = {0.0, 0.0, 0.0};
+            for (int s = 0; s < S; ++s)
+                for (int d = 0; d < 3; ++d) mbb[d] += pp[3 * (s * bl + t) + d];
+            const double *U = zb + 6 * ((b0 + t) / nblob), *d = dl + 3 * t;
+            wl[3 * t] = -(U[0] - d[1] * U[5] + d[2] * U[4]) + mbb[0];
+            wl[3 * t + 1] = -(U[1] - d[2] * U[3] + d[0] * U[5]) + mbb[1];
+            wl[3 * t + 2] = -(U[2] - d[0] * U[4] + d[1] * U[3]) + mbb[2];
+        }
+        __syncthreads();
+        // ---- D..F: CGS2 and ||w|| ------------------------------------------
+        for (int pass = 0; pass < 2; ++pass) {
+            double *hp = pass == 0 ? hp1 : hp2, *hs = pass == 0 ? h : h2;
+            const int wid = tid >> 5, lane = tid & 31;
+            for (int i = wid; i < k; i += kCgWarps) {
+                const double *q = a.Q + a.ld * (size_t)i;
+                double s = 0.0;
+                for (int lr = lane; lr < nr; lr += 32) s += q[row_of(lr)] * wl[lr];
+                s = warp_sum(s);
+                if (lane == 0) hp[i] = s;
+            }
+            cl.sync();  // barriers 3 and 4
+            cluster_reduce(cl, hp, k, hs, C, G);
+            __syncthreads();
+            for (int lr = tid; lr < nr; lr += kCgTpb) {
+                const int row = row_of(lr);
+                double v = wl[lr];
+#pragma unroll 4
+                for (int i = 0; i < k; ++i) v -= hs[i] * a.Q[a.ld * (size_t)i + row];
+                wl[lr] = v;
+            }
+            __syncthreads();
+        }
+        double part = 0.0;
+        for (int lr = tid; lr < nr; lr += kCgTpb) part += wl[lr] * wl[lr];
+        part = cg_block_sum(part, red);
+        if (tid == 0) np[0] = part;
+        cl.sync();  // barrier 5
+        cluster_reduce(cl, np, 1, np + 1, C, G);
+        __syncthreads();
+        nrm = sqrt(np[1]);
+    }
+    // no CTA leaves while another may still read its shared memory
+    cl.sync();
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace {
+struct ClusterChoice {
+    int csize = 0;  // 0: not usable
+    int bpc = 0;
+    size_t smem = 0;
+};
+}  // namespace
+
+static ClusterChoice choose_cluster(gmi_solver *s)
+{
+    ClusterChoice ch;
+    const int nb = s->B, W = s->W;
+    if (nb <= 0 || nb > kCgMaxBlobs || W <= 0 || W > kCgMaxSwimmers || s->m + 1 > kCgMaxK) return ch;
+    const void *fn = reinterpret_cast<const void *>(&gmres_cluster_kernel);
+    for (int csize : {16, 8}) {
+        int bpc = (nb + csize - 1) / csize;
+        bpc += bpc & 1;  // even: a source pair never straddles two CTAs
+        const CgLayout L = cg_layout(nb, W, bpc);
+        if (L.total > 200 * 1024) continue;
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if (csize > 8 &&
+            cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg{};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = csize;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(csize);
+        cfg.blockDim = dim3(kCgTpb);
+        cfg.dynamicSmemBytes = L.total;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if (clusters < 1) continue;
+        ch.csize = csize;
+        ch.bpc = bpc;
+        ch.smem = L.total;
+        return ch;
+    }
+    return ch;
+}
+
+bool cluster_gmres_usable(gmi_solver *s)
+{
+    if (s->ctx->precision != GMI_FP32C) return false;
+    const char *env = std::getenv("GMI_GMRES_CLUSTER");
+    if (env && env[0] == '0') return false;
+    return choose_cluster(s).csize > 0;
+}
+
+gmi_status cluster_gmres_launch(gmi_solver *s, double beta0, double norm_ref, double tol, int max_iter)
+{
+    const ClusterChoice ch = choose_cluster(s);
+    if (ch.csize == 0) {
+        set_last_error_msg("the cluster GMRES solve does not fit this system");
+        return GMI_ERR_STATE;
+    }
+    ClusterGmresArgs a{};
+    a.W = s->W;
+    a.nblob = s->cfg.nblob;
+    a.nb = s->B;
+    a.n = s->n;
+    a.ldh = s->m + 1;
+    a.max_iter = max_iter;
+    a.bpc = ch.bpc;
+    a.ld = (size_t)s->n;
+    a.Q = s->Q;
+    a.H = s->H;
+    a.beta = s->beta;
+    a.cs = s->cs;
+    a.sn = s->sn;
+    a.w0 = s->w;
+    a.R = s->R;
+    a.refs = s->refs;
+    a.ktk_rot = s->ktk_rot;
+    a.mob_rot = s->mob_rot;
+    a.xb = s->x_blobs;
+    a.minv = 6.0 * kPi * s->cfg.mu * s->cfg.rblob;
+    a.beta0 = beta0;
+    a.tol = tol;
+    a.norm_ref = norm_ref;
+    a.ctl = s->ctl;
+    PairConsts k;
+    fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
+    a.kbb.four_a2 = (float)k.eq[0];
+    a.kbb.two_a2 = (float)k.eq[1];
+    a.kbb.f8pm = (float)k.eq[2];
+    a.kbb.f6pma = (float)k.eq[3];
+    a.kbb.q32 = (float)k.eq[4];
+    a.kbb.inv_a = (float)k.eq[5];
+    a.kbb.f8pma3 = (float)k.eq[6];
+    a.kbb.f16pma3 = (float)k.eq[7];
+    a.kbb.q8 = (float)k.eq[8];
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = ch.csize;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(ch.csize);
+    cfg.blockDim = dim3(kCgTpb);
+    cfg.dynamicSmemBytes = ch.smem;
+    cfg.stream = s->ctx->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GMI_CUDA_TRY(cudaLaunchKernelEx(&cfg, gmres_cluster_kernel, a));
+    s->ctx->launches++;
+    return GMI_OK;
+}
+
+}  // namespace gmi

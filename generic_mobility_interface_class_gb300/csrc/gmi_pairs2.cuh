@@ -53,7 +53,7 @@ __device__ __forceinline__ float2 dist2(float2 dx, float2 dy, float2 dz)
 struct SSCoeffs {
     float At, Bt, Ar, Br, c3;
 };
-__device__ __noinline__ SSCoeffs ss_near2(float r2, float ir, float dF, float dT, EqualK<float> k)
+static __device__ __noinline__ SSCoeffs ss_near2(float r2, float ir, float dF, float dT, EqualK<float> k)
 {
     SSCoeffs c;
     ss_near_coeffs<float>(r2, ir, dF, dT, k, c.At, c.Bt, c.Ar, c.Br, c.c3);
@@ -66,7 +66,7 @@ struct UnequalCoeffs {
     float A, Bd, Cd;
 };
 // The middle and overlapping branches of unequal_coeffs.
-__device__ __noinline__ UnequalCoeffs unequal_near2(float r2, float ir, float dF, UnequalK<float> k)
+static __device__ __noinline__ UnequalCoeffs unequal_near2(float r2, float ir, float dF, UnequalK<float> k)
 {
     UnequalCoeffs c;
     unequal_coeffs<float>(r2, ir, dF, k, c.A, c.Bd, c.Cd);

@@ -53,6 +53,8 @@ struct SimP {
     double *bx, *bq, *bf, *vb;  // solver arrays: body_x, body_q, body_f, v_bodies
     double *bxm1, *bxm2, *bu, *bum1, *bqm1, *bQ, *schur;
     double *mob_ref;
+    double *lk;    // per link (F x (NS-1)): hdl t_i x lam, hdl t_{i+1} x lam, R(q_mid) M_body
+    double *tang;  // per segment: tangent of q (filament update)
     int *flags;  // [0] error too large, [1] non-finite error, [2] singular Jacobian
 };
 
@@ -197,63 +199,80 @@ __device__ void body_frame_moment(const SimP &P, int fil, int link, double *M)
     M[2] = P.KB * (mq.z - st[2]);
 }
 
-// filament::internal_forces_and_torques (filament.cpp:1112-1220), instability cilia
+// filament::internal_forces_and_torques (filament.cpp:1112-1220), instability
+// cilia, in two passes so that the FP64 work spreads over one thread per link
+// and then one thread per segment (GB300's FP64 pipe makes a per-filament
+// loop in one thread the slowest part of the Broyden iteration).
+// Pass 1, thread per link i of a filament: the terms the reference's link
+// loop adds to segments i and i+1.
+__global__ void filament_link_terms_kernel(SimP P)
+{
+    const int nl = P.NS - 1;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nl <= 0 || g >= P.F * nl) return;
+    const int fil = g / nl, i = g % nl, s0 = fil * P.NS;
+    const double hdl = 0.5 * P.DL;
+    const double *lam = P.lam + 3 * (size_t)g;
+    double *o = P.lk + 9 * (size_t)g;
+    double t[3];
+    q_tangent(ldq(P.q + 4 * (s0 + i)), t);
+    o[0] = hdl * (t[1] * lam[2] - t[2] * lam[1]);
+    o[1] = hdl * (t[2] * lam[0] - t[0] * lam[2]);
+    o[2] = hdl * (t[0] * lam[1] - t[1] * lam[0]);
+    q_tangent(ldq(P.q + 4 * (s0 + i + 1)), t);
+    o[3] = hdl * (t[1] * lam[2] - t[2] * lam[1]);
+    o[4] = hdl * (t[2] * lam[0] - t[0] * lam[2]);
+    o[5] = hdl * (t[0] * lam[1] - t[1] * lam[0]);
+    const Q4 qmid = midpoint_quaternion(ldq(P.q + 4 * (s0 + i)), ldq(P.q + 4 * (s0 + i + 1)));
+    const M3 R = q_rot_mat(qmid);
+    double Mb[3];
+    body_frame_moment(P, fil, i, Mb);
+    m3_vec(R, Mb, o + 6);
+}
+
+// Pass 2, thread per segment: the link terms in the order the reference's
+// loop adds them (link i-1, then link i), then tether, end force, the
+// one-off perturbation and the clamp torque.
 __global__ void filament_forces_kernel(SimP P, int nt)
 {
-    const int fil = blockIdx.x * blockDim.x + threadIdx.x;
-    if (fil >= P.F) return;
-    const int s0 = fil * P.NS;
-    double *f = P.f + 6 * (size_t)s0;
-    for (int k = 0; k < 6 * P.NS; ++k) f[k] = 0.0;
-    const double hdl = 0.5 * P.DL;
-    for (int i = 0; i < P.NS - 1; ++i) {
-        const double *lam = P.lam + 3 * (P.NS - 1) * fil + 3 * i;
-        f[6 * i] -= lam[0];
-        f[6 * i + 1] -= lam[1];
-        f[6 * i + 2] -= lam[2];
-        f[6 * (i + 1)] += lam[0];
-        f[6 * (i + 1) + 1] += lam[1];
-        f[6 * (i + 1) + 2] += lam[2];
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.S) return;
+    const int NS = P.NS, fil = s / NS, i = s % NS, nl = NS - 1;
+    double f[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    if (i > 0) {
+        const size_t l = (size_t)fil * nl + (i - 1);
+        const double *lam = P.lam + 3 * l, *o = P.lk + 9 * l;
+        for (int c = 0; c < 3; ++c) f[c] += lam[c];
+        for (int c = 0; c < 3; ++c) f[3 + c] -= o[3 + c];
+        for (int c = 0; c < 3; ++c) f[3 + c] -= o[6 + c];
+    }
+    if (i < nl) {
+        const size_t l = (size_t)fil * nl + i;
+        const double *lam = P.lam + 3 * l, *o = P.lk + 9 * l;
+        for (int c = 0; c < 3; ++c) f[c] -= lam[c];
+        for (int c = 0; c < 3; ++c) f[3 + c] -= o[c];
+        for (int c = 0; c < 3; ++c) f[3 + c] += o[6 + c];
+    }
+    if (i == 0)
+        for (int c = 0; c < 3; ++c) f[c] += P.tl[3 * fil + c];
+    if (i == NS - 1) {
         double t[3];
-        q_tangent(ldq(P.q + 4 * (s0 + i)), t);
-        f[6 * i + 3] -= hdl * (t[1] * lam[2] - t[2] * lam[1]);
-        f[6 * i + 4] -= hdl * (t[2] * lam[0] - t[0] * lam[2]);
-        f[6 * i + 5] -= hdl * (t[0] * lam[1] - t[1] * lam[0]);
-        q_tangent(ldq(P.q + 4 * (s0 + i + 1)), t);
-        f[6 * (i + 1) + 3] -= hdl * (t[1] * lam[2] - t[2] * lam[1]);
-        f[6 * (i + 1) + 4] -= hdl * (t[2] * lam[0] - t[0] * lam[2]);
-        f[6 * (i + 1) + 5] -= hdl * (t[0] * lam[1] - t[1] * lam[0]);
-        const Q4 qmid = midpoint_quaternion(ldq(P.q + 4 * (s0 + i)), ldq(P.q + 4 * (s0 + i + 1)));
-        const M3 R = q_rot_mat(qmid);
-        double Mb[3], M[3];
-        body_frame_moment(P, fil, i, Mb);
-        m3_vec(R, Mb, M);
-        f[6 * i + 3] += M[0];
-        f[6 * i + 4] += M[1];
-        f[6 * i + 5] += M[2];
-        f[6 * (i + 1) + 3] -= M[0];
-        f[6 * (i + 1) + 4] -= M[1];
-        f[6 * (i + 1) + 5] -= M[2];
+        q_tangent(ldq(P.q + 4 * s), t);
+        for (int c = 0; c < 3; ++c) f[c] -= P.EFM * t[c];
     }
-    f[0] += P.tl[3 * fil];
-    f[1] += P.tl[3 * fil + 1];
-    f[2] += P.tl[3 * fil + 2];
-    double t[3];
-    q_tangent(ldq(P.q + 4 * (s0 + P.NS - 1)), t);
-    f[6 * (P.NS - 1)] -= P.EFM * t[0];
-    f[6 * (P.NS - 1) + 1] -= P.EFM * t[1];
-    f[6 * (P.NS - 1) + 2] -= P.EFM * t[2];
     if (nt == 0) {  // one-off perturbation of segments 4 and 12 (filament.cpp:1181-1196)
-        if (4 < P.NS)
-            for (int c = 0; c < 3; ++c) f[6 * 4 + c] += P.p1[3 * fil + c];
-        if (12 < P.NS)
-            for (int c = 0; c < 3; ++c) f[6 * 12 + c] += P.p2[3 * fil + c];
+        if (i == 4)
+            for (int c = 0; c < 3; ++c) f[c] += P.p1[3 * fil + c];
+        if (i == 12)
+            for (int c = 0; c < 3; ++c) f[c] += P.p2[3 * fil + c];
     }
-    double ct[3];
-    dexpinv_transpose(ct, P.u + 3 * s0, P.cl + 3 * fil);
-    f[3] += ct[0];
-    f[4] += ct[1];
-    f[5] += ct[2];
+    if (i == 0) {
+        double ct[3];
+        dexpinv_transpose(ct, P.u + 3 * s, P.cl + 3 * fil);
+        for (int c = 0; c < 3; ++c) f[3 + c] += ct[c];
+    }
+    double *fs = P.f + 6 * (size_t)s;
+    for (int c = 0; c < 6; ++c) fs[c] = f[c];
 }
 
 __device__ __forceinline__ double warp_sum_d(double v)
@@ -1016,22 +1035,47 @@ __global__ void body_update_kernel(SimP P, const double *upd)
 }
 
 // swimmer::update's per-filament part (swimmer.cpp:858-868) with
-// filament::update (filament.cpp:1541-1575).
-__global__ void filament_update_kernel(SimP P, const double *upd)
+// filament::update (filament.cpp:1541-1575), in two passes.  Pass 1, thread
+// per segment: segment 0 takes the body's state (accept_state_from_rigid_body,
+// filament.cpp:438-463: base position, u = body u); the others add their
+// update to u and the multiplier of the link before them; each segment's new
+// tangent goes to scratch.  (accept_state_from_rigid_body's own robot_arm is
+// left out: every position it writes is rewritten by the final robot_arm from
+// the same base.)
+__global__ void filament_update_segments_kernel(SimP P, const double *upd)
 {
-    const int fil = blockIdx.x * blockDim.x + threadIdx.x;
-    if (fil >= P.F) return;
-    const int n = fil / P.NF, i = fil % P.NF, NS = P.NS;
-    accept_state_from_body(P, fil);
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.S) return;
+    const int NS = P.NS, fil = s / NS, k = s % NS, n = fil / P.NF, i = fil % P.NF;
     const double *du = upd + (size_t)n * P.per_body + (size_t)6 * NS * i;
-    for (int c = 0; c < 3; ++c) P.tl[3 * fil + c] += du[c];
-    double *lam = P.lam + 3 * (NS - 1) * fil;
-    for (int k = 1; k < NS; ++k) {
+    if (k == 0) {
+        double base[3];
+        base_position(P, fil, base);
+        for (int c = 0; c < 3; ++c) P.x[3 * s + c] = base[c];
+        const double d0[3] = {P.bu[3 * n] - P.u[3 * s], P.bu[3 * n + 1] - P.u[3 * s + 1],
+                              P.bu[3 * n + 2] - P.u[3 * s + 2]};
+        segment_update(P, s, d0);
+        for (int c = 0; c < 3; ++c) P.tl[3 * fil + c] += du[c];
+        for (int c = 0; c < 3; ++c) P.cl[3 * fil + c] += du[3 * NS + c];
+    } else {
+        double *lam = P.lam + 3 * (NS - 1) * (size_t)fil;
         for (int c = 0; c < 3; ++c) lam[3 * (k - 1) + c] += du[3 * k + c];
-        segment_update(P, fil * NS + k, du + 3 * (NS + k));
+        segment_update(P, s, du + 3 * (NS + k));
     }
-    for (int c = 0; c < 3; ++c) P.cl[3 * fil + c] += du[3 * NS + c];
-    robot_arm(P, fil);
+    q_tangent(ldq(P.q + 4 * s), P.tang + 3 * (size_t)s);
+}
+
+// Pass 2, thread per (filament, coordinate): robot_arm (filament.cpp:416-436),
+// positions by midpoint-tangent chaining from the base.
+__global__ void filament_robot_arm_kernel(SimP P)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= 3 * P.F) return;
+    const int fil = g / 3, c = g % 3, s0 = fil * P.NS;
+    for (int i = 1; i < P.NS; ++i) {
+        const int s = s0 + i;
+        P.x[3 * s + c] = P.x[3 * (s - 1) + c] + 0.5 * P.DL * (P.tang[3 * (s - 1) + c] + P.tang[3 * s + c]);
+    }
 }
 
 // ---- Broyden vector kernels ----------------------------------------------
@@ -1145,7 +1189,9 @@ static gmi_status read_flags(gmi_sim *m)
 
 static gmi_status forces_and_torques(gmi_sim *m, int nt)
 {
-    filament_forces_kernel<<<gridN(m->P.F, 64), 64, 0, sst(m)>>>(m->P, nt);
+    if (m->P.NS > 1) filament_link_terms_kernel<<<gridN(m->P.F * (m->P.NS - 1), 64), 64, 0, sst(m)>>>(m->P);
+    filament_forces_kernel<<<gridN(m->P.S, 64), 64, 0, sst(m)>>>(m->P, nt);
+    GMI_TRY(sim_launched(m));
     // the host copy of the segment forces never receives the barrier forces
     // (mobility_solver.cpp:132-192); keep it for the writers
     GMI_CUDA_TRY(cudaMemcpyAsync(m->f_internal, m->P.f, 6 * (size_t)m->P.S * sizeof(double),
@@ -1262,7 +1308,9 @@ static gmi_status end_of_iter(gmi_sim *m, bool too_large)
 static gmi_status swimmer_update(gmi_sim *m)
 {
     if (!m->P.wall) body_update_kernel<<<gridN(m->P.W, 32), 32, 0, sst(m)>>>(m->P, m->upd);
-    filament_update_kernel<<<gridN(m->P.F, 64), 64, 0, sst(m)>>>(m->P, m->upd);
+    filament_update_segments_kernel<<<gridN(m->P.S, 64), 64, 0, sst(m)>>>(m->P, m->upd);
+    filament_robot_arm_kernel<<<gridN(3 * m->P.F, 64), 64, 0, sst(m)>>>(m->P);
+    GMI_TRY(sim_launched(m));
     return sim_launched(m, m->P.wall ? 1 : 2);
 }
 
@@ -1465,6 +1513,8 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
     SIM_ALLOC(m->jpart, 6 * F);
     SIM_ALLOC(m->spart, 45 * F);
     SIM_ALLOC(m->f_internal, 6 * S);
+    SIM_ALLOC(P.lk, 9 * F * (size_t)(P.NS > 1 ? P.NS - 1 : 1));
+    SIM_ALLOC(P.tang, 3 * (size_t)S);
     SIM_ALLOC(m->scal, 4);
     {
         double *fl = nullptr;

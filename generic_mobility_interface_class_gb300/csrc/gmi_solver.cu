@@ -23,6 +23,7 @@
 #include "gmi_pair_kernels.hpp"
 #include "gmi_solver_device.cuh"
 #include "gmi_solver_internal.hpp"
+#include "gmi_gmres_cluster.hpp"
 
 namespace gmi {
 
@@ -1103,8 +1104,26 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
     const int ldh = s->m + 1;
     const int pidx = s->ctx->precision == GMI_FP64 ? 0 : 1;
     size_t nodes = 0;
-    if (s->use_graphs && ensure_arnoldi_graph(s, pidx, &nodes) != GMI_OK) s->use_graphs = false;
-    if (s->use_graphs) {
+    const bool cluster = s->use_cluster && max_iter >= 1 && cluster_gmres_usable(s);
+    if (!cluster && s->use_graphs && ensure_arnoldi_graph(s, pidx, &nodes) != GMI_OK) s->use_graphs = false;
+    if (cluster) {
+        GmresCtl c{};
+        c.k = 1;
+        c.max_iter = max_iter;
+        c.tol = tol;
+        c.norm_ref = norm_ref;
+        *s->h_ctl = c;
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->ctl, s->h_ctl, sizeof c, cudaMemcpyHostToDevice, st));
+        GMI_TRY(cluster_gmres_launch(s, beta0, norm_ref, tol, max_iter));
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->ctl, sizeof c, cudaMemcpyDeviceToHost, st));
+        GMI_CUDA_TRY(cudaStreamSynchronize(st));
+        if (!s->h_ctl->done) {
+            set_last_error_msg("cluster GMRES solve ended without completion");
+            return GMI_ERR_STATE;
+        }
+    }
+    if (cluster || s->use_graphs) {
+      if (!cluster) {
         // the first step normalises w = r0 by beta0 into Q[:, 0]
         GMI_CUDA_TRY(cudaMemcpyAsync(s->st_scal + kNormOff, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
         GmresCtl c{};
@@ -1141,6 +1160,7 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
             }
             batch = batch * 2 < 32 ? batch * 2 : 32;
         }
+      }
         if (!std::isfinite(s->h_ctl->resid)) {
             set_last_error_msg("GMRES produced a non-finite residual");
             return GMI_ERR_NONFINITE;

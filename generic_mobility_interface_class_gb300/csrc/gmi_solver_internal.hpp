@@ -41,6 +41,7 @@ struct gmi_solver {
     size_t graph_nodes[2] = {0, 0};
     bool graph_loops[2] = {false, false};           // graph holds the whole device-side loop
     bool use_graphs = true;
+    bool use_cluster = true;  // FP32C solves of small systems in one thread-block cluster
     PrescribedWork *prescribed = nullptr;  // allocated by the first prescribed-cilia solve
 };
 

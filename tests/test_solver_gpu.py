@@ -135,6 +135,41 @@ def test_fp32c_solver_error(gmi_lib, oracle_built):
     s.close()
 
 
+@pytest.mark.parametrize("nswim", [1, 2, 3])
+def test_fp32c_cluster_solve_matches_multikernel(nswim, gmi_lib, oracle_built, monkeypatch):
+    """The FP32C solve inside one thread-block cluster against the
+    multi-kernel Arnoldi step (GMI_GMRES_CLUSTER=0) and the dense FP64
+    oracle.  162 blobs per swimmer: with 2 swimmers the last CTA of a
+    16-CTA cluster owns no blob, only the body rows; with 3, swimmers
+    straddle CTAs."""
+    from oracle import mobility_dense as md
+    nfil, nseg = 4, 10
+    refs, bx, bq, xs, fs, bf = swimmer_geometry(nswim, nfil, nseg)
+    want = md.compute_velocities(xs, fs, bx, bq, bf, refs, nseg, force_scale=1.5)
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("GMI_GMRES_CLUSTER", mode)
+        s = make_solver(refs, nswim, nfil, nseg, precision=1)
+        s.x_segs_host[:] = xs
+        s.f_segs_host[:] = fs
+        iters, _ = s.compute_velocities(bx, bq, bf)
+        iters2, _ = s.compute_velocities(bx, bq, bf)  # warm start
+        x = np.concatenate([s.f_blobs_host.ravel(), s.v_bodies().ravel()])
+        out[mode] = (iters, iters2, x.copy(), s.v_segs_host.copy())
+        s.close()
+    for mode in ("0", "1"):
+        iters, iters2, x, vs = out[mode]
+        assert iters > 0 and iters2 < iters
+        # FP32C refinement updates its residual with the FP32C operator, so
+        # the true FP64 residual stops near 1e-8 rather than at the 1e-10 target
+        resid = np.linalg.norm(want["A"] @ x - want["rhs"]) / np.linalg.norm(want["rhs"])
+        assert resid < 1e-7, (mode, resid)
+        assert rel_err(vs, want["v_segs"]) < 1e-5
+    # same refinement, same tolerance: the two paths agree far below the bound
+    assert rel_err(out["1"][2], out["0"][2]) < 1e-6
+    assert abs(out["1"][0] - out["0"][0]) <= max(3, out["0"][0] // 10)
+
+
 def test_backend_operations_match_oracle(gmi_lib, oracle_built):
     """The reference's per-backend calls, one by one, on the solver's pinned arrays."""
     from oracle import rpy
