@@ -283,24 +283,28 @@ __device__ __forceinline__ double warp_sum_d(double v)
 }
 
 // Free-swimming force/torque balance (swimmer.cpp:276-325): body f = -sum of
-// segment forces and torques about the body centre.  One CTA per swimmer.
-__global__ void __launch_bounds__(256) swimmer_force_sum_kernel(SimP P)
+// segment forces and torques about the body centre.  Two passes: kFsSegs
+// segments per CTA into part[(n gx + x) 6 + c], then one thread per (swimmer,
+// component) adds the CTA partials in order.
+constexpr int kFsSegs = 128;
+
+__global__ void __launch_bounds__(kFsSegs) swimmer_force_partial_kernel(SimP P, double *part)
 {
-    __shared__ double red[6][8];
-    const int n = blockIdx.x;
+    __shared__ double red[6][kFsSegs / 32];
+    const int n = blockIdx.y, k = blockIdx.x * kFsSegs + threadIdx.x;
     const int per = P.NF * P.NS;
     const double *X = P.bx + 3 * n;
     double a[6] = {0, 0, 0, 0, 0, 0};
-    for (int k = threadIdx.x; k < per; k += 256) {
+    if (k < per) {
         const int s = n * per + k;
         const double *fs = P.f + 6 * (size_t)s;
         const double dx = P.x[3 * s] - X[0], dy = P.x[3 * s + 1] - X[1], dz = P.x[3 * s + 2] - X[2];
-        a[0] += fs[0];
-        a[1] += fs[1];
-        a[2] += fs[2];
-        a[3] += fs[3] + dy * fs[2] - dz * fs[1];
-        a[4] += fs[4] + dz * fs[0] - dx * fs[2];
-        a[5] += fs[5] + dx * fs[1] - dy * fs[0];
+        a[0] = fs[0];
+        a[1] = fs[1];
+        a[2] = fs[2];
+        a[3] = fs[3] + dy * fs[2] - dz * fs[1];
+        a[4] = fs[4] + dz * fs[0] - dx * fs[2];
+        a[5] = fs[5] + dx * fs[1] - dy * fs[0];
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int c = 0; c < 6; ++c) {
@@ -309,10 +313,20 @@ __global__ void __launch_bounds__(256) swimmer_force_sum_kernel(SimP P)
     }
     __syncthreads();
     if (threadIdx.x < 6) {
-        double s = 0.0;
-        for (int w = 0; w < 8; ++w) s += red[threadIdx.x][w];
-        P.bf[6 * n + threadIdx.x] = -s;
+        double t = 0.0;
+        for (int w = 0; w < kFsSegs / 32; ++w) t += red[threadIdx.x][w];
+        part[((size_t)n * gridDim.x + blockIdx.x) * 6 + threadIdx.x] = t;
     }
+}
+
+__global__ void swimmer_force_finish_kernel(SimP P, int gx, const double *part)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 6 * P.W) return;
+    const int n = e / 6, c = e % 6;
+    double t = 0.0;
+    for (int x = 0; x < gx; ++x) t += part[((size_t)n * gx + x) * 6 + c];
+    P.bf[e] = -t;
 }
 
 // compute_errors (mobility_solver.cpp:1404-1689), GMRES branch.
@@ -439,21 +453,24 @@ __device__ M3 off_block(double tsf, const M3 &dOm, const M3 &Lie)
     return m3_scale(t, -tsf);
 }
 
-// filament::jacobian_lie_algebra_block (filament.cpp:1222-1404), written into
-// J at rows/cols [3NS, 6NS).
-__device__ void lie_algebra_block(const SimP &P, int fil, int nt, double *J, int ld)
+// filament::jacobian_lie_algebra_block (filament.cpp:1222-1404) for segment
+// k: the 3x3 blocks of rows [3NS + 3k, 3NS + 3k + 3) (diagonal, and the
+// neighbours' columns), written into J; the unit diagonal is added later.
+// Segments 0 and NS-1 are the reference's first and last cases (NS >= 2).
+__device__ void lie_segment_blocks(const SimP &P, int fil, int nt, int k, double *J, int ld)
 {
     const int NS = P.NS, s0 = fil * NS, o = 3 * NS;
     const double tsf = (nt < P.neuler) ? P.DT : 2.0 * P.DT / 3.0;
     const double Tfac = 1.0 / (8.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
     const double *lam = P.lam + 3 * (NS - 1) * fil;
     const double *f = P.f + 6 * (size_t)s0;
-    auto Q = [&](int k) { return ldq(P.q + 4 * (s0 + k)); };
-    auto Tn = [&](int k, double *t) { q_tangent(Q(k), t); };
+    auto Q = [&](int m) { return ldq(P.q + 4 * (s0 + m)); };
     double Kph[3], Kmh[3], t[3], om[3];
-    // first segment
-    {
-        Tn(0, t);
+    q_tangent(Q(k), t);
+    const M3 Lie = m3_scale(rcross(P.u + 3 * (s0 + k)), -1.0);
+    for (int c = 0; c < 3; ++c) om[c] = Tfac * f[6 * k + 3 + c];
+    const M3 Om = rcross(om);
+    if (k == 0) {
         const M3 Cp = m3_mul(m3_scale(rcross(lam), -0.5 * P.DL), rcross(t));
         const Q4 qph = midpoint_quaternion(Q(0), Q(1));
         body_frame_moment(P, fil, 0, Kph);
@@ -462,20 +479,14 @@ __device__ void lie_algebra_block(const SimP &P, int fil, int nt, double *J, int
         const M3 R = q_rot_mat(qph);
         El = m3_add(El, m3_mul(R, LD));
         M3 dOm = m3_scale(m3_add(El, Cp), Tfac);
-        const M3 Lie = m3_scale(rcross(P.u + 3 * s0), -1.0);
-        for (int c = 0; c < 3; ++c) om[c] = Tfac * f[3 + c];
-        const M3 Om = rcross(om);
         put_block(J, ld, o, o, diag_block(tsf, dOm, Lie, Om, P.u + 3 * s0));
         LD = bfm_lie_derivative(P, Q(0), Q(1), true);
         El = m3_scale(frame_cross(Kph[0], Kph[1], Kph[2], Q(1)), 0.5);
         El = m3_add(El, m3_mul(R, LD));
         dOm = m3_scale(El, Tfac);
         put_block(J, ld, o, o + 3, off_block(tsf, dOm, Lie));
-    }
-    // last segment
-    {
+    } else if (k == NS - 1) {
         const int e = NS - 1;
-        Tn(e, t);
         const M3 Cp = m3_mul(m3_scale(rcross(lam + 3 * (NS - 2)), -0.5 * P.DL), rcross(t));
         const Q4 qmh = midpoint_quaternion(Q(e - 1), Q(e));
         body_frame_moment(P, fil, NS - 2, Kmh);
@@ -484,21 +495,13 @@ __device__ void lie_algebra_block(const SimP &P, int fil, int nt, double *J, int
         const M3 R = q_rot_mat(qmh);
         El = m3_sub(El, m3_mul(R, LD));
         M3 dOm = m3_scale(m3_add(El, Cp), Tfac);
-        const M3 Lie = m3_scale(rcross(P.u + 3 * (s0 + e)), -1.0);
-        for (int c = 0; c < 3; ++c) om[c] = Tfac * f[6 * e + 3 + c];
-        const M3 Om = rcross(om);
         put_block(J, ld, o + 3 * e, o + 3 * e, diag_block(tsf, dOm, Lie, Om, P.u + 3 * (s0 + e)));
         LD = bfm_lie_derivative(P, Q(e - 1), Q(e), false);
         El = m3_scale(frame_cross(Kmh[0], Kmh[1], Kmh[2], Q(e - 1)), -0.5);
         El = m3_sub(El, m3_mul(R, LD));
         dOm = m3_scale(El, Tfac);
         put_block(J, ld, o + 3 * e, o + 3 * e - 3, off_block(tsf, dOm, Lie));
-    }
-    for (int k = 1; k < NS - 1; ++k) {
-        Tn(k, t);
-        const M3 Lie = m3_scale(rcross(P.u + 3 * (s0 + k)), -1.0);
-        for (int c = 0; c < 3; ++c) om[c] = Tfac * f[6 * k + 3 + c];
-        const M3 Om = rcross(om);
+    } else {
         body_frame_moment(P, fil, k, Kph);
         body_frame_moment(P, fil, k - 1, Kmh);
         const Q4 qph = midpoint_quaternion(Q(k), Q(k + 1));
@@ -527,72 +530,91 @@ __device__ void lie_algebra_block(const SimP &P, int fil, int nt, double *J, int
         dOm = m3_scale(El, Tfac);
         put_block(J, ld, o + 3 * k, o + 3 * k + 3, off_block(tsf, dOm, Lie));
     }
-    for (int k = 0; k < 3 * NS; ++k) J[(o + k) + (size_t)ld * (o + k)] += 1.0;
 }
 
 // filament::invert_approx_jacobian (filament.cpp:1406-1539) up to the
 // inversion: the approximate Jacobian in invJ, the two clamping blocks saved.
-__global__ void build_jacobian_kernel(SimP P, int nt)
+// One CTA per filament.  The reference's block writes fall into disjoint
+// regions (constraint diagonal; position couplings, rows < 3NS; Lie-algebra
+// rows >= 3NS, columns < 3NS; the Lie-algebra block, one row band per
+// segment), built in parallel, with the writes that depend on earlier ones
+// (end-force term, unit diagonal, clamping blocks) after a barrier.  Tasks
+// go to warps round-robin so the FP64 work spreads over the SM's schedulers.
+constexpr int kJacTpb = 128;
+
+__global__ void __launch_bounds__(kJacTpb) build_jacobian_kernel(SimP P, int nt)
 {
-    const int fil = blockIdx.x * blockDim.x + threadIdx.x;
-    if (fil >= P.F) return;
+    const int fil = blockIdx.x, tid = threadIdx.x;
     const int NS = P.NS, ld = P.n6, s0 = fil * NS;
     double *J = P.invJ + (size_t)fil * ld * ld;
-    for (size_t k = 0; k < (size_t)ld * ld; ++k) J[k] = 0.0;
+    for (size_t k = tid; k < (size_t)ld * ld; k += kJacTpb) J[k] = 0.0;
+    __syncthreads();
     const bool euler = nt < P.neuler;
-    double fac = euler ? -P.DT / (6.0 * kPi * P.MU * P.RSEG) : -P.DT / (9.0 * kPi * P.MU * P.RSEG);
-    for (int i = 0; i < 3 * NS; ++i) {
-        J[i + (size_t)ld * i] = fac;
-        if (i < 3 * NS - 3) J[i + (size_t)ld * (i + 3)] = -fac;
+    const double fac0 = euler ? -P.DT / (6.0 * kPi * P.MU * P.RSEG) : -P.DT / (9.0 * kPi * P.MU * P.RSEG);
+    const double fac1 = euler ? P.DL * P.DT / (16.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG)
+                              : P.DL * P.DT / (24.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
+    for (int i = tid; i < 3 * NS; i += kJacTpb) {
+        J[i + (size_t)ld * i] = fac0;
+        if (i < 3 * NS - 3) J[i + (size_t)ld * (i + 3)] = -fac0;
     }
-    double t[3];
-    for (int j = 1; j < NS; ++j) {
-        const int jpos = 3 * (NS + j);
-        q_tangent(ldq(P.q + 4 * (s0 + j)), t);
-        const M3 temp = m3_scale(rcross(t), P.DL);
-        put_block(J, ld, 3 * j, jpos, m3_scale(temp, 0.5));
-        for (int i = j + 1; i < NS; ++i) put_block(J, ld, 3 * i, jpos, temp);
+    // tasks: [0, NS-1) position columns j+1; [NS-1, 2NS-2) Lie-to-position
+    // rows for j+1; [2NS-2, 3NS-2) Lie-algebra segment k
+    const int ntask = 3 * NS - 2;
+    for (int task = 0; task < ntask; ++task) {
+        if (((task % 4) * 32 + task / 4) % kJacTpb != tid) continue;
+        double t[3];
+        if (task < NS - 1) {
+            const int j = task + 1, jpos = 3 * (NS + j);
+            q_tangent(ldq(P.q + 4 * (s0 + j)), t);
+            const M3 temp = m3_scale(rcross(t), P.DL);
+            put_block(J, ld, 3 * j, jpos, m3_scale(temp, 0.5));
+            for (int i = j + 1; i < NS; ++i) put_block(J, ld, 3 * i, jpos, temp);
+        } else if (task < 2 * NS - 2) {
+            const int j = task - (NS - 1) + 1, jpos = 3 * j;
+            int ipos = 3 * (NS + j - 1);
+            q_tangent(ldq(P.q + 4 * (s0 + j - 1)), t);
+            M3 um = rcross(P.u + 3 * (s0 + j - 1));
+            M3 tm = m3_scale(rcross(t), -1.0);
+            M3 blk =
+                m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
+            put_block(J, ld, ipos, jpos, m3_scale(blk, fac1));
+            ipos += 3;
+            q_tangent(ldq(P.q + 4 * (s0 + j)), t);
+            um = rcross(P.u + 3 * (s0 + j));
+            tm = m3_scale(rcross(t), -1.0);
+            blk = m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
+            put_block(J, ld, ipos, jpos, m3_scale(blk, fac1));
+        } else {
+            lie_segment_blocks(P, fil, nt, task - (2 * NS - 2), J, ld);
+        }
     }
-    q_tangent(ldq(P.q + 4 * (s0 + NS - 1)), t);
-    {
-        double et[3] = {t[0], t[1], t[2]};
-        const M3 sub = m3_scale(rcross(et), fac * P.EFM);
+    __syncthreads();
+    for (int k = tid; k < 3 * NS; k += kJacTpb) J[(3 * NS + k) + (size_t)ld * (3 * NS + k)] += 1.0;
+    if (tid == 0) {
+        double t[3];
+        q_tangent(ldq(P.q + 4 * (s0 + NS - 1)), t);
+        const M3 sub = m3_scale(rcross(t), fac0 * P.EFM);
         add_block(J, ld, 3 * (NS - 1), 3 * (2 * NS - 1), m3_scale(sub, -1.0));
     }
-    fac = euler ? P.DL * P.DT / (16.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG)
-                : P.DL * P.DT / (24.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
-    for (int j = 1; j < NS; ++j) {
-        const int jpos = 3 * j;
-        int ipos = 3 * (NS + j - 1);
-        q_tangent(ldq(P.q + 4 * (s0 + j - 1)), t);
-        M3 um = rcross(P.u + 3 * (s0 + j - 1));
-        M3 tm = m3_scale(rcross(t), -1.0);
-        M3 blk = m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
-        put_block(J, ld, ipos, jpos, m3_scale(blk, fac));
-        ipos += 3;
-        q_tangent(ldq(P.q + 4 * (s0 + j)), t);
-        um = rcross(P.u + 3 * (s0 + j));
-        tm = m3_scale(rcross(t), -1.0);
-        blk = m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
-        put_block(J, ld, ipos, jpos, m3_scale(blk, fac));
+    __syncthreads();
+    if (tid == 0) {
+        const double fac = euler ? -P.DT / (8.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG)
+                                 : -P.DT / (12.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
+        const M3 um = rcross(P.u + 3 * s0);
+        M3 blk = m3_add(m3_scale(um, 0.5), m3_scale(m3_mul(um, um), 1.0 / 12.0));
+        M3 blkT = m3_add(m3_scale(um, -0.5), m3_scale(m3_mul(um, um), 1.0 / 12.0));
+        for (int d = 0; d < 3; ++d) {
+            blk(d, d) += 1.0;
+            blkT(d, d) += 1.0;
+        }
+        const M3 e1 = get_block(J, ld, 3 * NS, 3 * NS), e2 = get_block(J, ld, 3 * NS + 3, 3 * NS);
+        for (int k = 0; k < 9; ++k) {
+            P.ecb1[9 * fil + k] = e1.a[k];
+            P.ecb2[9 * fil + k] = e2.a[k];
+        }
+        put_block(J, ld, 3 * NS, 3 * NS, m3_scale(m3_mul(blk, blkT), fac));
+        put_block(J, ld, 3 * NS + 3, 3 * NS, m3_zero());
     }
-    lie_algebra_block(P, fil, nt, J, ld);
-    fac = euler ? -P.DT / (8.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG)
-                : -P.DT / (12.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
-    const M3 um = rcross(P.u + 3 * s0);
-    M3 blk = m3_add(m3_scale(um, 0.5), m3_scale(m3_mul(um, um), 1.0 / 12.0));
-    M3 blkT = m3_add(m3_scale(um, -0.5), m3_scale(m3_mul(um, um), 1.0 / 12.0));
-    for (int d = 0; d < 3; ++d) {
-        blk(d, d) += 1.0;
-        blkT(d, d) += 1.0;
-    }
-    const M3 e1 = get_block(J, ld, 3 * NS, 3 * NS), e2 = get_block(J, ld, 3 * NS + 3, 3 * NS);
-    for (int k = 0; k < 9; ++k) {
-        P.ecb1[9 * fil + k] = e1.a[k];
-        P.ecb2[9 * fil + k] = e2.a[k];
-    }
-    put_block(J, ld, 3 * NS, 3 * NS, m3_scale(m3_mul(blk, blkT), fac));
-    put_block(J, ld, 3 * NS + 3, 3 * NS, m3_zero());
 }
 
 // In-place inverse of n x n column-major matrices, one CTA each, Gauss-Jordan
@@ -600,60 +622,52 @@ __global__ void build_jacobian_kernel(SimP P, int nt)
 // matrix lives in shared memory when it fits.  Stands in for the reference's
 // LAPACK dgetrf + dgetri (matrix.cpp:538-566); a zero pivot sets flags[2].
 constexpr int kGjTpb = 256;
+constexpr int kGjWarps = kGjTpb / 32;
 
 __global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, int use_smem, int *flags)
 {
     extern __shared__ double sh[];
     double *Mg = mats + (size_t)blockIdx.x * n * n;
-    double *col = sh;                      // n
-    double *redv = col + n;                // 32
+    double *col = sh;                      // n: pivot column before the step
+    double *redv = col + n;                // 32 (unused slots kept for the layout)
     int *redi = reinterpret_cast<int *>(redv + 32);  // 32
     int *perm = redi + 32;                 // n
     double *A = use_smem ? reinterpret_cast<double *>(perm + ((n + 1) & ~1)) : Mg;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     if (use_smem)
         for (int e = tid; e < n * n; e += kGjTpb) A[e] = Mg[e];
-    __syncthreads();
     __shared__ int singular;
     if (tid == 0) singular = 0;
     __syncthreads();
     for (int k = 0; k < n; ++k) {
-        double best = -1.0;
-        int bi = k;
-        for (int i = k + tid; i < n; i += kGjTpb) {
-            const double a = fabs(A[i + (size_t)n * k]);
-            if (a > best) {
-                best = a;
-                bi = i;
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            const double ob = __shfl_down_sync(0xffffffffu, best, o);
-            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-            if (ob > best || (ob == best && oi < bi)) {
-                best = ob;
-                bi = oi;
-            }
-        }
-        if (lane == 0) {
-            redv[wid] = best;
-            redi[wid] = bi;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            double b = redv[0];
-            int p = redi[0];
-            for (int w = 1; w < kGjTpb / 32; ++w)
-                if (redv[w] > b || (redv[w] == b && redi[w] < p)) {
-                    b = redv[w];
-                    p = redi[w];
+        // partial pivoting by warp 0: largest |A(i, k)|, i >= k, lowest i on ties
+        if (wid == 0) {
+            double best = -1.0;
+            int bi = k;
+            for (int i = k + lane; i < n; i += 32) {
+                const double a = fabs(A[i + (size_t)n * k]);
+                if (a > best) {
+                    best = a;
+                    bi = i;
                 }
-            perm[k] = p;
-            if (!(b > 0.0)) singular = 1;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_down_sync(0xffffffffu, best, o);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) {
+                    best = ob;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) {
+                perm[k] = bi;
+                if (!(best > 0.0)) singular = 1;
+            }
         }
         __syncthreads();
         if (singular) break;
         const int p = perm[k];
+        // row swap, then the pivot column saved
         if (p != k)
             for (int j = tid; j < n; j += kGjTpb) {
                 const double t = A[k + (size_t)n * j];
@@ -664,12 +678,19 @@ __global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, 
         const double pivinv = 1.0 / A[k + (size_t)n * k];
         for (int i = tid; i < n; i += kGjTpb) col[i] = A[i + (size_t)n * k];
         __syncthreads();
-        for (int j = tid; j < n; j += kGjTpb) A[k + (size_t)n * j] = (j == k) ? pivinv : A[k + (size_t)n * j] * pivinv;
-        __syncthreads();
-        for (int e = tid; e < n * n; e += kGjTpb) {
-            const int i = e % n, j = e / n;
-            if (i == k) continue;
-            A[e] = (j == k) ? -col[i] * pivinv : A[e] - A[k + (size_t)n * j] * col[i];
+        // column j (one warp per column, lanes over rows): scale the pivot
+        // row entry, eliminate every other row; column k becomes -col/pivot
+        for (int j = wid; j < n; j += kGjWarps) {
+            double *Aj = A + (size_t)n * j;
+            if (j == k) {
+                for (int i = lane; i < n; i += 32) Aj[i] = (i == k) ? pivinv : -col[i] * pivinv;
+            } else {
+                const double akj = Aj[k] * pivinv;
+                for (int i = lane; i < n; i += 32)
+                    if (i != k) Aj[i] = Aj[i] - akj * col[i];
+                __syncwarp();
+                if (lane == 0) Aj[k] = akj;
+            }
         }
         __syncthreads();
     }
@@ -982,13 +1003,14 @@ __global__ void __launch_bounds__(128) jim_partial_kernel(SimP P, const double *
 __global__ void __launch_bounds__(32) jim_body_kernel(SimP P, const double *in, const double *part, double *out)
 {
     __shared__ double b2[6];
-    const int n = blockIdx.x;
+    const int n = blockIdx.x, lane = threadIdx.x;
     const size_t b = (size_t)n * P.per_body + 6 * P.NF * P.NS;
-    if (threadIdx.x < 6) {
-        const int r = threadIdx.x;
-        double v = in[b + r];
-        for (int i = 0; i < P.NF; ++i) v -= part[6 * (n * P.NF + i) + r];
-        b2[r] = v;
+    // the filaments' parts, lanes strided over filaments, then a warp sum
+    for (int r = 0; r < 6; ++r) {
+        double v = 0.0;
+        for (int i = lane; i < P.NF; i += 32) v += part[6 * (n * P.NF + i) + r];
+        v = warp_sum_d(v);
+        if (lane == 0) b2[r] = in[b + r] - v;
     }
     __syncwarp();
     if (threadIdx.x < 6) {
@@ -1151,6 +1173,7 @@ struct gmi_sim {
     double *dots = nullptr, *part = nullptr, *jpart = nullptr, *scal = nullptr;
     double *spart = nullptr;  // per-filament parts of the Schur complement (45 each)
     double *f_internal = nullptr;  // segment forces before the barrier (the reference's f_segs_host)
+    double *fs_part = nullptr;     // per-CTA partials of the swimmer force/torque sums
     int *h_flags = nullptr;
     std::vector<void *> allocs;
     bool prepared = false;
@@ -1197,8 +1220,10 @@ static gmi_status forces_and_torques(gmi_sim *m, int nt)
     GMI_CUDA_TRY(cudaMemcpyAsync(m->f_internal, m->P.f, 6 * (size_t)m->P.S * sizeof(double),
                                  cudaMemcpyDeviceToDevice, sst(m)));
     if (m->P.wall) return sim_launched(m);
-    swimmer_force_sum_kernel<<<m->P.W, 256, 0, sst(m)>>>(m->P);
-    return sim_launched(m, 2);
+    const int gx = gridN(m->P.NF * m->P.NS, kFsSegs);
+    swimmer_force_partial_kernel<<<dim3(gx, m->P.W), kFsSegs, 0, sst(m)>>>(m->P, m->fs_part);
+    swimmer_force_finish_kernel<<<gridN(6 * m->P.W, 64), 64, 0, sst(m)>>>(m->P, gx, m->fs_part);
+    return sim_launched(m, 3);
 }
 
 // compute_velocities + compute_errors; sets *too_large, *nonfinite
@@ -1219,7 +1244,7 @@ static gmi_status velocities_and_errors(gmi_sim *m, int nt, double *err_out, boo
 static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
 {
     const SimP &P = m->P;
-    build_jacobian_kernel<<<gridN(P.F, 32), 32, 0, sst(m)>>>(P, nt);
+    build_jacobian_kernel<<<P.F, kJacTpb, 0, sst(m)>>>(P, nt);
     const size_t mat = (size_t)P.n6 * P.n6 * sizeof(double);
     const size_t base = (size_t)P.n6 * sizeof(double) + 32 * sizeof(double) + 32 * sizeof(int) +
                         (size_t)((P.n6 + 1) & ~1) * sizeof(int);
@@ -1515,6 +1540,7 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
     SIM_ALLOC(m->f_internal, 6 * S);
     SIM_ALLOC(P.lk, 9 * F * (size_t)(P.NS > 1 ? P.NS - 1 : 1));
     SIM_ALLOC(P.tang, 3 * (size_t)S);
+    SIM_ALLOC(m->fs_part, 6 * W * (size_t)gridN(P.NF * P.NS, kFsSegs));
     SIM_ALLOC(m->scal, 4);
     {
         double *fl = nullptr;

@@ -127,29 +127,43 @@ __global__ void blob_positions_kernel(int W, int nblob, const double *__restrict
 
 // Per swimmer: sums[6n..] = (sum_m f_m, sum_m (R ref_m) x f_m) over its blobs.
 // This is K^T f (mobility_solver.cpp:690-697, 921-940, 168-188).
-__global__ void __launch_bounds__(kRedTpb) kt_sums_kernel(int nblob, const double *__restrict__ R,
-                                                          const double *__restrict__ refs,
-                                                          const double *__restrict__ f, double *__restrict__ sums)
+// K^T f per swimmer (the 6-vector sum over its blobs of (f, (R ref) x f)),
+// in two passes: kKtBlobs blobs per CTA into part[(n gx + x) 6 + c], then
+// one thread per (swimmer, component) adds the CTA partials in order.
+constexpr int kKtBlobs = 128;
+
+__global__ void __launch_bounds__(kKtBlobs) kt_partial_kernel(int nblob, const double *__restrict__ R,
+                                                             const double *__restrict__ refs,
+                                                             const double *__restrict__ f, double *__restrict__ part)
 {
     __shared__ double red[32];
-    const int n = blockIdx.x;
-    const double *Rn = R + 9 * n;
+    const int n = blockIdx.y, m = blockIdx.x * kKtBlobs + threadIdx.x;
     double a[6] = {0, 0, 0, 0, 0, 0};
-    for (int m = threadIdx.x; m < nblob; m += kRedTpb) {
+    if (m < nblob) {
         const double *fm = f + 3 * ((size_t)n * nblob + m);
         double d[3];
-        rot_apply(Rn, refs + 3 * m, d);
-        a[0] += fm[0];
-        a[1] += fm[1];
-        a[2] += fm[2];
-        a[3] += d[1] * fm[2] - d[2] * fm[1];
-        a[4] += d[2] * fm[0] - d[0] * fm[2];
-        a[5] += d[0] * fm[1] - d[1] * fm[0];
+        rot_apply(R + 9 * n, refs + 3 * m, d);
+        a[0] = fm[0];
+        a[1] = fm[1];
+        a[2] = fm[2];
+        a[3] = d[1] * fm[2] - d[2] * fm[1];
+        a[4] = d[2] * fm[0] - d[0] * fm[2];
+        a[5] = d[0] * fm[1] - d[1] * fm[0];
     }
     for (int c = 0; c < 6; ++c) {
-        const double s = block_sum<kRedTpb>(a[c], red);
-        if (threadIdx.x == 0) sums[6 * n + c] = s;
+        const double t = block_sum<kKtBlobs>(a[c], red);
+        if (threadIdx.x == 0) part[((size_t)n * gridDim.x + blockIdx.x) * 6 + c] = t;
     }
+}
+
+__global__ void kt_finish_kernel(int W, int gx, const double *__restrict__ part, double *__restrict__ sums)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 6 * W) return;
+    const int n = e / 6, c = e % 6;
+    double t = 0.0;
+    for (int x = 0; x < gx; ++x) t += part[((size_t)n * gx + x) * 6 + c];
+    sums[e] = t;
 }
 
 // body_f += sums (the blob repulsion's force and torque on each body).
@@ -865,8 +879,10 @@ static gmi_status prepare_bodies(gmi_solver *s)
 // K^T of the blob block of `vec` into s->sums.
 static gmi_status kt_sums(gmi_solver *s, const double *vec)
 {
-    kt_sums_kernel<<<s->W, kRedTpb, 0, s->ctx->stream>>>(s->cfg.nblob, s->R, s->refs, vec, s->sums);
-    return launched(s);
+    const int gx = (s->cfg.nblob + kKtBlobs - 1) / kKtBlobs;
+    kt_partial_kernel<<<dim3(gx, s->W), kKtBlobs, 0, s->ctx->stream>>>(s->cfg.nblob, s->R, s->refs, vec, s->kt_part);
+    kt_finish_kernel<<<grid_for(6 * s->W, 64), 64, 0, s->ctx->stream>>>(s->W, gx, s->kt_part, s->sums);
+    return launched(s, 2);
 }
 
 // out = P^-1 in (apply_preconditioner, right preconditioning)
@@ -1222,11 +1238,15 @@ static gmi_status store_solution(gmi_solver *s)
 // FP32C context: mixed-precision iterative refinement.  The residual
 // b - A x is formed with the FP64 operator; each correction solves
 // A d = r by GMRES with the FP32C operator (FP64 Arnoldi, Givens and
-// vectors) to a relative tolerance kInnerTol; x += d.  This converges to
-// the FP64 solution at the requested tolerance, which GMRES on the FP32C
-// operator alone cannot (its answer is off by cond(A) times the operator's
-// rounding).  The iteration count returned is the sum of inner iterations.
-static constexpr double kInnerTol = 1e-4;
+// vectors) to the relative tolerance that would meet the target in one pass
+// (with a 0.3 margin for the FP32C operator's own error), but not below
+// kInnerTol, which stays above that error (~3e-7 of |A d|); x += d.  This
+// converges to the FP64 solution at the requested tolerance, which GMRES on
+// the FP32C operator alone cannot (its answer is off by cond(A) times the
+// operator's rounding).  The iteration count returned is the sum of inner
+// iterations.
+static constexpr double kInnerTol = 1e-6;
+static constexpr double kInnerMargin = 0.3;
 static constexpr int kMaxRefinements = 12;
 
 static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
@@ -1259,8 +1279,8 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         return store_solution(s);
     }
     // Mixed-precision refinement.  The residual of the warm start is formed
-    // with the FP64 operator; after each correction delta (solved to 1e-4,
-    // so |A delta| ~ |r|) it is updated as r -= A delta with the FP32C
+    // with the FP64 operator; after each correction delta (solved to at
+    // most 1e-6 relative, so |A delta| ~ |r|) it is updated as r -= A delta with the FP32C
     // operator, whose error (~3e-7 |A delta|) stays far below the tolerance.
     GMI_CUDA_TRY(cudaMemcpyAsync(s->b64, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
     int total = 0;
@@ -1293,7 +1313,8 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         }
         GMI_CUDA_TRY(cudaMemcpyAsync(s->xacc, s->soln, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
         GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
-        const double inner_tol = tol * norm_rhs / beta > kInnerTol ? tol * norm_rhs / beta : kInnerTol;
+        const double want = kInnerMargin * tol * norm_rhs / beta;
+        const double inner_tol = want > kInnerTol ? want : kInnerTol;
         int iters = 0;
         GMI_TRY(gmres_run(s, beta, beta, inner_tol, false, true, &iters));
         total += iters;
@@ -1567,6 +1588,7 @@ gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
     TRY_OR_DIE(dalloc(s, &s->mob_rot, 36 * W));
     TRY_OR_DIE(dalloc(s, &s->refs, 3 * (size_t)cfg->nblob));
     TRY_OR_DIE(dalloc(s, &s->sums, 6 * W));
+    TRY_OR_DIE(dalloc(s, &s->kt_part, 6 * W * (size_t)((cfg->nblob + kKtBlobs - 1) / kKtBlobs)));
     TRY_OR_DIE(dalloc(s, &s->scal, 8));
     if (n > 0) {
         TRY_OR_DIE(dalloc(s, &s->rhs, n));

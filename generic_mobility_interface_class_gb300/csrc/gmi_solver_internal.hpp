@@ -20,7 +20,7 @@ struct gmi_solver {
     double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
     double *body_x = nullptr, *body_q = nullptr, *body_f = nullptr, *v_bodies = nullptr;
     double *R = nullptr, *ktk_ref = nullptr, *mob_ref = nullptr, *ktk_rot = nullptr, *mob_rot = nullptr;
-    double *refs = nullptr, *sums = nullptr;
+    double *refs = nullptr, *sums = nullptr, *kt_part = nullptr;  // K^T sums and their per-CTA partials
     double *rhs = nullptr, *soln = nullptr, *Q = nullptr, *H = nullptr, *beta = nullptr, *cs = nullptr, *sn = nullptr;
     double *z = nullptr, *w = nullptr, *tmp = nullptr, *mbb = nullptr, *partial = nullptr, *yv = nullptr;
     double *b64 = nullptr, *xacc = nullptr;  // refinement: FP64 right-hand side, accumulated solution
