@@ -44,6 +44,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FLOP_PER_PAIR_SS = 87  # canonical algorithmic FLOPs per segment-segment pair (FMA = 2)
+# DRAM bytes (read + write) of one launch of the apply's pair kernel, from an
+# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of this
+# benchmark with the shape pinned: (n, precision, threads, targets, splits,
+# sources per step) -> bytes.  Beyond the records (48 B per particle read) and
+# V (48 B written), the traffic is the FP64 split partial sums.
+PAIR_KERNEL_TRAFFIC = {(131072, "fp32c", 256, 1, 8, 2): 7976192}
 METRIC = "RPY pair-interactions/sec"
 
 
@@ -59,6 +65,9 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the FP64 side measurement")
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU sample")
     p.add_argument("--no-autotune", action="store_true", help="use the default launch shape (profiling)")
+    p.add_argument("--shape", default=None,
+                   help="pin the apply's launch shape instead of autotuning: threads,targets,splits,sources_per_step "
+                        "(the traffic capture pins the shape the autotuner picks)")
     p.add_argument("--ts-workloads", default="config1,config3",
                    help="time-step workloads (comma separated; empty to skip)")
     p.add_argument("--ts-steps", default="config1:100,config3:10", help="timed steps per workload")
@@ -280,7 +289,10 @@ def run_gmi(args, world, rank, local):
     vd = torch.empty((n, 6), dtype=torch.float64, device="cuda")
     l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > 129 MB L2
 
-    if not args.no_autotune:
+    if args.shape:
+        tpb_, tt_, sp_, per_ = (int(v) for v in args.shape.split(","))
+        ctx.set_shape(0, n, n, tpb_, tt_, sp_, per_)
+    elif not args.no_autotune:
         ctx.autotune(0, n, n)
     tpb, tt, splits, tuned = ctx.tuned_shape(0, n, n)
     per_step = ctx.tuned_sources_per_step(0, n, n)
@@ -357,9 +369,13 @@ def run_gmi(args, world, rank, local):
 
     peak = ctx.fma_peak(prec)
     achieved = FLOP_PER_PAIR_SS * pairs / (ms_per_step / 1e3)
+    traffic = PAIR_KERNEL_TRAFFIC.get((n, args.precision, tpb, tt, splits, per_step))
     roofline = {"bound": "fp32" if prec == GMI_FP32C else "fp64",
                 "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None,
+                "traffic": traffic,
+                "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch of this shape"
+                                   if traffic is not None else "no capture of this launch shape"),
+                "algorithmic_bytes": int(n * 48 + n * 48),
                 "peak_source": "measured FMA-loop probe on this GPU (gmi_measure_fma_peak)",
                 "flops_per_pair": FLOP_PER_PAIR_SS}
     ctx.close()
@@ -386,7 +402,7 @@ def run_gmi(args, world, rank, local):
                        "n": n, "precision": args.precision, "parallelism": f"replicas x{world}",
                        "launch_shape": {"threads_per_cta": tpb, "targets_per_thread": tt,
                                         "source_splits": splits or "auto", "sources_per_step": per_step,
-                                        "autotuned": tuned},
+                                        "autotuned": bool(tuned and not args.shape), "pinned": bool(args.shape)},
                        "l2": "flushed (256 MB write) between timed steps"},
             "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(n * 9 * 8),
                     "d2h_bytes_per_step": int(n * 6 * 8), "path": "gmi_Mss_mult with pinned host X,F -> V"},

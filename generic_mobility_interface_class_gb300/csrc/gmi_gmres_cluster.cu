@@ -31,6 +31,7 @@
 // All arithmetic except the pair sum is FP64, as in the multi-kernel step.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 
@@ -51,12 +52,15 @@ constexpr int kCgPairThreads = kCgTpb - 32;  // the last warp runs the Givens st
 constexpr int kCgMaxK = 160;                 // H rows and Givens state (>= max_iter + 1)
 constexpr int kCgMaxBlobs = 2048;
 constexpr int kCgMaxSwimmers = 16;
-constexpr int kCgFold = 16;                  // source pairs summed in FP32 before an FP64 add
+constexpr int kCgFold = 64;                  // source pairs summed in FP32 before an FP64 add
 
 struct ClusterGmresArgs {
     int W, nblob, nb, n, ldh, max_iter, bpc;
     size_t ld;
     double *Q, *H, *beta, *cs, *sn;
+    double *Qr;                       // the basis again, row-major with ldr columns (projections)
+    int ldr;
+    int kq, kqs;                      // basis columns [0, kq) of the CTA's rows cached in shared memory, row stride kqs
     const double *w0;                 // r0, all n rows
     const double *R, *refs, *ktk_rot, *mob_rot, *xb;
     double minv, beta0, tol, norm_ref;
@@ -66,11 +70,11 @@ struct ClusterGmresArgs {
 
 // Shared-memory layout (offsets in bytes), fixed by nb, W and bpc.
 struct CgLayout {
-    size_t ipos, iload, wl, ql, av, dl, kt, mb, mom1, mom2, sums, zb, hp1, hp2, h, h2, np, pp, csh, snh, bet, col,
-        red, flag, total;
+    size_t ipos, iload, wl, ql, av, dl, kt, mb, mom1, mom2, sums, zb, hp1, hp2, h, h2, hw, np, pp, csh, snh, bet,
+        col, red, flag, qs, total;
 };
 
-__host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc)
+__host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc, int kqs = 0)
 {
     CgLayout L;
     const size_t npairs = (size_t)(nb + 1) / 2, rows = 3 * (size_t)bpc + 6 * (size_t)W;
@@ -96,6 +100,7 @@ __host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc)
     L.hp2 = take(kCgMaxK * sizeof(double));
     L.h = take(kCgMaxK * sizeof(double));
     L.h2 = take(kCgMaxK * sizeof(double));
+    L.hw = take((size_t)kCgWarps * kCgMaxK * sizeof(double));  // per-warp projection partials
     L.np = take(2 * sizeof(double));
     L.pp = take((size_t)kCgTpb * 3 * sizeof(double));
     L.csh = take(kCgMaxK * sizeof(double));
@@ -104,12 +109,26 @@ __host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc)
     L.col = take((kCgMaxK + 1) * sizeof(double));
     L.red = take(kCgWarps * sizeof(double));
     L.flag = take(4 * sizeof(int));
+    L.qs = take(rows * (size_t)kqs * sizeof(double));  // cached basis rows
     L.total = o;
     return L;
 }
 
-// Deterministic block sum (fixed shuffle tree, then warps in order); the
-// result is returned to thread 0 only.
+// Pairwise sum of kCgWarps values at stride `stride` (a fixed tree: FP64
+// additions on this GPU have long latency, so depth matters more than count).
+__device__ __forceinline__ double tree16(const double *v, int stride)
+{
+    static_assert(kCgWarps == 16, "tree16 adds 16 values");
+    double a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = v[(2 * i) * stride] + v[(2 * i + 1) * stride];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = a[2 * i] + a[2 * i + 1];
+    return (a[0] + a[1]) + (a[2] + a[3]);
+}
+
+// Deterministic block sum (fixed shuffle tree, then a tree over the warps);
+// the result is returned to thread 0 only.
 __device__ __forceinline__ double cg_block_sum(double v, double *red)
 {
     v = warp_sum(v);
@@ -117,8 +136,7 @@ __device__ __forceinline__ double cg_block_sum(double v, double *red)
     if (lane == 0) red[wid] = v;
     __syncthreads();
     double t = 0.0;
-    if (threadIdx.x == 0)
-        for (int i = 0; i < kCgWarps; ++i) t += red[i];
+    if (threadIdx.x == 0) t = tree16(red, 1);
     __syncthreads();
     return t;
 }
@@ -161,7 +179,7 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
     const int C = (int)cl.num_blocks(), c = (int)cl.block_rank(), tid = threadIdx.x;
     const int G = C <= 8 ? 8 : (C <= 16 ? 16 : 32);
     extern __shared__ __align__(16) unsigned char sm[];
-    const CgLayout L = cg_layout(a.nb, a.W, a.bpc);
+    const CgLayout L = cg_layout(a.nb, a.W, a.bpc, a.kqs);
     float4 *ipos = reinterpret_cast<float4 *>(sm + L.ipos);
     float4 *iload = reinterpret_cast<float4 *>(sm + L.iload);
     double *wl = reinterpret_cast<double *>(sm + L.wl), *ql = reinterpret_cast<double *>(sm + L.ql);
@@ -171,11 +189,14 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
     double *sums = reinterpret_cast<double *>(sm + L.sums), *zb = reinterpret_cast<double *>(sm + L.zb);
     double *hp1 = reinterpret_cast<double *>(sm + L.hp1), *hp2 = reinterpret_cast<double *>(sm + L.hp2);
     double *h = reinterpret_cast<double *>(sm + L.h), *h2 = reinterpret_cast<double *>(sm + L.h2);
+    double *hw = reinterpret_cast<double *>(sm + L.hw);
     double *np = reinterpret_cast<double *>(sm + L.np), *pp = reinterpret_cast<double *>(sm + L.pp);
     double *csh = reinterpret_cast<double *>(sm + L.csh), *snh = reinterpret_cast<double *>(sm + L.snh);
     double *bet = reinterpret_cast<double *>(sm + L.bet), *col = reinterpret_cast<double *>(sm + L.col);
     double *red = reinterpret_cast<double *>(sm + L.red);
     int *flag = reinterpret_cast<int *>(sm + L.flag);
+    double *qs = reinterpret_cast<double *>(sm + L.qs);
+    const int kq = a.kq, kqs = a.kqs;
 
     const int W = a.W, nb = a.nb, nblob = a.nblob, bpc = a.bpc;
     const int npairs = (nb + 1) / 2;
@@ -240,8 +261,13 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
         const double inrm = 1.0 / nrm;
         for (int lr = tid; lr < nr; lr += kCgTpb) {
             const double q = wl[lr] * inrm;
+            const int row = row_of(lr);
             ql[lr] = q;
-            qcol[row_of(lr)] = q;
+            qcol[row] = q;
+            if (k - 1 < kq)
+                qs[lr * kqs + (k - 1)] = q;
+            else
+                a.Qr[(size_t)row * a.ldr + (k - 1)] = q;
         }
         __syncthreads();
         for (int t = tid; t < bl; t += kCgTpb) {
@@ -343,14 +369,15 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
         } else if (tid == kCgPairThreads && k > 1) {
             // Givens step of iteration k - 1: H column = h + h2 and ||w||
             const int iter = k - 1;
-            for (int i = 0; i < iter; ++i) col[i] = h[i] + h2[i];
-            col[iter] = nrm;
+            // H column h + h2 through the previous rotations; the entry being
+            // rotated stays in a register
+            double prev = h[0] + h2[0];
             for (int i = 1; i < iter; ++i) {
-                const double u = csh[i - 1] * col[i - 1] + snh[i - 1] * col[i];
-                col[i] = csh[i - 1] * col[i] - snh[i - 1] * col[i - 1];
-                col[i - 1] = u;
+                const double cur = h[i] + h2[i], cc0 = csh[i - 1], ss0 = snh[i - 1];
+                col[i - 1] = cc0 * prev + ss0 * cur;
+                prev = cc0 * cur - ss0 * prev;
             }
-            const double hk = col[iter], hd = col[iter - 1];
+            const double hk = nrm, hd = prev;
             double cc, ss;
             if (hk == 0.0) {
                 cc = 1.0;
@@ -391,9 +418,18 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
         __syncthreads();
         if (flag[0]) break;  // the same in every CTA
         for (int t = tid; t < bl; t += kCgTpb) {
-            double mbb[3] = {0.0, 0.0, 0.0};
-            for (int s = 0; s < S; ++s)
-                for (int d = 0; d < 3; ++d) mbb[d] += pp[3 * (s * bl + t) + d];
+            // the S split partials, two interleaved sums each
+            double mbb[3], m2[3] = {0.0, 0.0, 0.0};
+            for (int d = 0; d < 3; ++d) mbb[d] = 0.0;
+            int sp = 0;
+            for (; sp + 1 < S; sp += 2)
+                for (int d = 0; d < 3; ++d) {
+                    mbb[d] += pp[3 * (sp * bl + t) + d];
+                    m2[d] += pp[3 * ((sp + 1) * bl + t) + d];
+                }
+            if (sp < S)
+                for (int d = 0; d < 3; ++d) mbb[d] += pp[3 * (sp * bl + t) + d];
+            for (int d = 0; d < 3; ++d) mbb[d] += m2[d];
             const double *U = zb + 6 * ((b0 + t) / nblob), *d = dl + 3 * t;
             wl[3 * t] = -(U[0] - d[1] * U[5] + d[2] * U[4]) + mbb[0];
             wl[3 * t + 1] = -(U[1] - d[2] * U[3] + d[0] * U[5]) + mbb[1];
@@ -404,22 +440,50 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
         for (int pass = 0; pass < 2; ++pass) {
             double *hp = pass == 0 ? hp1 : hp2, *hs = pass == 0 ? h : h2;
             const int wid = tid >> 5, lane = tid & 31;
-            for (int i = wid; i < k; i += kCgWarps) {
-                const double *q = a.Q + a.ld * (size_t)i;
-                double s = 0.0;
-                for (int lr = lane; lr < nr; lr += 32) s += q[row_of(lr)] * wl[lr];
-                s = warp_sum(s);
-                if (lane == 0) hp[i] = s;
+            // lane = column, warp = rows congruent to it mod kCgWarps; then
+            // the warps' partials added in warp order
+            for (int c0 = 0; c0 < k; c0 += 32) {
+                const int i = c0 + lane;
+                if (i < k) {
+                    double s0 = 0.0, s1 = 0.0;
+                    int lr = wid;
+                    if (i < kq) {
+                        for (; lr + kCgWarps < nr; lr += 2 * kCgWarps) {
+                            s0 += qs[lr * kqs + i] * wl[lr];
+                            s1 += qs[(lr + kCgWarps) * kqs + i] * wl[lr + kCgWarps];
+                        }
+                        if (lr < nr) s0 += qs[lr * kqs + i] * wl[lr];
+                    } else {
+                        for (; lr + kCgWarps < nr; lr += 2 * kCgWarps) {
+                            s0 += a.Qr[(size_t)row_of(lr) * a.ldr + i] * wl[lr];
+                            s1 += a.Qr[(size_t)row_of(lr + kCgWarps) * a.ldr + i] * wl[lr + kCgWarps];
+                        }
+                        if (lr < nr) s0 += a.Qr[(size_t)row_of(lr) * a.ldr + i] * wl[lr];
+                    }
+                    hw[wid * kCgMaxK + i] = s0 + s1;
+                }
             }
+            __syncthreads();
+            for (int i = tid; i < k; i += kCgTpb) hp[i] = tree16(hw + i, kCgMaxK);
             cl.sync();  // barriers 3 and 4
             cluster_reduce(cl, hp, k, hs, C, G);
             __syncthreads();
             for (int lr = tid; lr < nr; lr += kCgTpb) {
                 const int row = row_of(lr);
-                double v = wl[lr];
-#pragma unroll 4
-                for (int i = 0; i < k; ++i) v -= hs[i] * a.Q[a.ld * (size_t)i + row];
-                wl[lr] = v;
+                // (Q h)_row in four interleaved partial sums
+                double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+                const double *qr = qs + lr * kqs;
+                const int kc = min(k, kq);
+                int i = 0;
+                for (; i + 3 < kc; i += 4) {
+                    p0 += hs[i] * qr[i];
+                    p1 += hs[i + 1] * qr[i + 1];
+                    p2 += hs[i + 2] * qr[i + 2];
+                    p3 += hs[i + 3] * qr[i + 3];
+                }
+                for (; i < kc; ++i) p0 += hs[i] * qr[i];
+                for (; i < k; ++i) p0 += hs[i] * a.Q[a.ld * (size_t)i + row];
+                wl[lr] = wl[lr] - ((p0 + p1) + (p2 + p3));
             }
             __syncthreads();
         }
@@ -443,6 +507,7 @@ namespace {
 struct ClusterChoice {
     int csize = 0;  // 0: not usable
     int bpc = 0;
+    int kq = 0, kqs = 0;
     size_t smem = 0;
 };
 }  // namespace
@@ -456,8 +521,15 @@ static ClusterChoice choose_cluster(gmi_solver *s)
     for (int csize : {16, 8}) {
         int bpc = (nb + csize - 1) / csize;
         bpc += bpc & 1;  // even: a source pair never straddles two CTAs
-        const CgLayout L = cg_layout(nb, W, bpc);
-        if (L.total > 200 * 1024) continue;
+        // cache as many basis columns of the CTA's rows as fit next to the rest
+        const CgLayout L0 = cg_layout(nb, W, bpc, 0);
+        if (L0.total > 200 * 1024) continue;
+        const size_t rows = 3 * (size_t)bpc + 6 * (size_t)W;
+        int kq = (int)((200 * 1024 - L0.total) / (rows * sizeof(double))) - 1;
+        kq = std::min(kq, s->m + 1);
+        if (kq < 8) kq = 0;
+        const int kqs = kq > 0 ? (kq | 1) : 0;  // odd row stride: the per-row update loop avoids bank conflicts
+        const CgLayout L = cg_layout(nb, W, bpc, kqs);
         if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total) != cudaSuccess) {
             cudaGetLastError();
             continue;
@@ -486,6 +558,8 @@ static ClusterChoice choose_cluster(gmi_solver *s)
         if (clusters < 1) continue;
         ch.csize = csize;
         ch.bpc = bpc;
+        ch.kq = kq;
+        ch.kqs = kqs;
         ch.smem = L.total;
         return ch;
     }
@@ -507,6 +581,13 @@ gmi_status cluster_gmres_launch(gmi_solver *s, double beta0, double norm_ref, do
         set_last_error_msg("the cluster GMRES solve does not fit this system");
         return GMI_ERR_STATE;
     }
+    // row-major copy of the Krylov basis (n rows of ldr >= max_iter + 1 entries)
+    const int ldr = s->m + 1;
+    if (s->Qr == nullptr) {
+        GMI_CUDA_TRY(cudaMalloc(&s->Qr, (size_t)s->n * ldr * sizeof(double)));
+        s->allocs.push_back(s->Qr);
+    }
+    double *Qr = s->Qr;
     ClusterGmresArgs a{};
     a.W = s->W;
     a.nblob = s->cfg.nblob;
@@ -517,6 +598,10 @@ gmi_status cluster_gmres_launch(gmi_solver *s, double beta0, double norm_ref, do
     a.bpc = ch.bpc;
     a.ld = (size_t)s->n;
     a.Q = s->Q;
+    a.Qr = Qr;
+    a.ldr = ldr;
+    a.kq = ch.kq;
+    a.kqs = ch.kqs;
     a.H = s->H;
     a.beta = s->beta;
     a.cs = s->cs;

@@ -42,6 +42,7 @@ struct gmi_solver {
     bool graph_loops[2] = {false, false};           // graph holds the whole device-side loop
     bool use_graphs = true;
     bool use_cluster = true;  // FP32C solves of small systems in one thread-block cluster
+    double *Qr = nullptr;     // the cluster solve's row-major copy of Q (allocated by its first launch)
     PrescribedWork *prescribed = nullptr;  // allocated by the first prescribed-cilia solve
 };
 
