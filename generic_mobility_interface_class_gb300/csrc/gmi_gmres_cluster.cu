@@ -70,7 +70,7 @@ struct ClusterGmresArgs {
 
 // Shared-memory layout (offsets in bytes), fixed by nb, W and bpc.
 struct CgLayout {
-    size_t ipos, iload, wl, ql, av, dl, kt, mb, mom1, mom2, sums, zb, hp1, hp2, h, h2, hw, np, pp, csh, snh, bet,
+    size_t ipos, iload, wl, ql, av, dl, kt, mb, mom1, mom2, sums, zb, hp1, hp2, h, h2, np, pp, csh, snh, bet,
         col, red, flag, qs, total;
 };
 
@@ -100,8 +100,7 @@ __host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc, int kqs = 
     L.hp2 = take(kCgMaxK * sizeof(double));
     L.h = take(kCgMaxK * sizeof(double));
     L.h2 = take(kCgMaxK * sizeof(double));
-    L.hw = take((size_t)kCgWarps * kCgMaxK * sizeof(double));  // per-warp projection partials
-    L.np = take(2 * sizeof(double));
+    L.np = take(4 * sizeof(double));
     L.pp = take((size_t)kCgTpb * 3 * sizeof(double));
     L.csh = take(kCgMaxK * sizeof(double));
     L.snh = take(kCgMaxK * sizeof(double));
@@ -114,21 +113,9 @@ __host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc, int kqs = 
     return L;
 }
 
-// Pairwise sum of kCgWarps values at stride `stride` (a fixed tree: FP64
-// additions on this GPU have long latency, so depth matters more than count).
-__device__ __forceinline__ double tree16(const double *v, int stride)
-{
-    static_assert(kCgWarps == 16, "tree16 adds 16 values");
-    double a[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) a[i] = v[(2 * i) * stride] + v[(2 * i + 1) * stride];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) a[i] = a[2 * i] + a[2 * i + 1];
-    return (a[0] + a[1]) + (a[2] + a[3]);
-}
-
-// Deterministic block sum (fixed shuffle tree, then a tree over the warps);
-// the result is returned to thread 0 only.
+// Deterministic block sum (fixed shuffle tree in each warp, then one over
+// the 16 warp sums held by lanes of warp 0); the result is returned to thread
+// 0 only.
 __device__ __forceinline__ double cg_block_sum(double v, double *red)
 {
     v = warp_sum(v);
@@ -136,7 +123,10 @@ __device__ __forceinline__ double cg_block_sum(double v, double *red)
     if (lane == 0) red[wid] = v;
     __syncthreads();
     double t = 0.0;
-    if (threadIdx.x == 0) t = tree16(red, 1);
+    if (wid == 0) {
+        t = lane < kCgWarps ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    }
     __syncthreads();
     return t;
 }
@@ -150,6 +140,10 @@ __device__ __forceinline__ void cluster_reduce(cg::cluster_group &cl, double *ar
 {
     const int groups = kCgTpb / G, gid = threadIdx.x / G, r = threadIdx.x % G;
     for (int base = 0; base < count; base += groups) {
+        // only warps holding elements run the FP64 tree (a warp FP64
+        // instruction costs the same with any number of active lanes)
+        const int warps = (min(groups, count - base) * G + 31) / 32;
+        if ((int)(threadIdx.x >> 5) >= warps) continue;
         const int e = base + gid;
         double v = 0.0;
         if (e < count && r < C) v = cl.map_shared_rank(arr, r)[e];
@@ -189,8 +183,8 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
     double *sums = reinterpret_cast<double *>(sm + L.sums), *zb = reinterpret_cast<double *>(sm + L.zb);
     double *hp1 = reinterpret_cast<double *>(sm + L.hp1), *hp2 = reinterpret_cast<double *>(sm + L.hp2);
     double *h = reinterpret_cast<double *>(sm + L.h), *h2 = reinterpret_cast<double *>(sm + L.h2);
-    double *hw = reinterpret_cast<double *>(sm + L.hw);
-    double *np = reinterpret_cast<double *>(sm + L.np), *pp = reinterpret_cast<double *>(sm + L.pp);
+    double *np = reinterpret_cast<double *>(sm + L.np);
+    float *pp = reinterpret_cast<float *>(sm + L.pp);  // pair-sum partials, [split][target][3]
     double *csh = reinterpret_cast<double *>(sm + L.csh), *snh = reinterpret_cast<double *>(sm + L.snh);
     double *bet = reinterpret_cast<double *>(sm + L.bet), *col = reinterpret_cast<double *>(sm + L.col);
     double *red = reinterpret_cast<double *>(sm + L.red);
@@ -239,8 +233,9 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
     if (tid == 0) {
         bet[0] = a.beta0;
         flag[0] = 0;
+        np[2] = a.beta0;        // ||w||, computed once per CTA (np[1] holds ||w||^2)
+        np[3] = 1.0 / a.beta0;  // and its reciprocal
     }
-    double nrm = a.beta0;
     // pair-phase thread map: bl target lanes x S source splits
     const int S = bl > 0 ? kCgPairThreads / bl : 0;
     const int pt = bl > 0 ? tid % bl : 0, ps = bl > 0 ? tid / bl : 0;
@@ -258,7 +253,7 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
     for (int k = 1; k <= a.max_iter + 1; ++k) {
         double *qcol = a.Q + a.ld * (size_t)(k - 1);
         // ---- A: q_{k-1}, body moments ------------------------------------
-        const double inrm = 1.0 / nrm;
+        const double nrm = np[2], inrm = np[3];
         for (int lr = tid; lr < nr; lr += kCgTpb) {
             const double q = wl[lr] * inrm;
             const int row = row_of(lr);
@@ -365,19 +360,45 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
                 }
             }
 #pragma unroll
-            for (int d = 0; d < 3; ++d) pp[3 * tid + d] = acc[d] + (double)(pacc[d].x + pacc[d].y);
-        } else if (tid == kCgPairThreads && k > 1) {
-            // Givens step of iteration k - 1: H column = h + h2 and ||w||
-            const int iter = k - 1;
-            // H column h + h2 through the previous rotations; the entry being
-            // rotated stays in a register
-            double prev = h[0] + h2[0];
-            for (int i = 1; i < iter; ++i) {
-                const double cur = h[i] + h2[i], cc0 = csh[i - 1], ss0 = snh[i - 1];
-                col[i - 1] = cc0 * prev + ss0 * cur;
-                prev = cc0 * cur - ss0 * prev;
+            for (int d = 0; d < 3; ++d) pp[3 * tid + d] = (float)(acc[d] + (double)(pacc[d].x + pacc[d].y));
+        } else if (tid >= kCgPairThreads && k > 1) {
+            // Givens step of iteration k - 1 by the last warp: the H column
+            // h + h2 through the previous rotations.  Entry i after rotation
+            // i is x_i = -s_{i-1} x_{i-1} + c_{i-1} (h + h2)_i, a first-order
+            // linear recurrence, evaluated 32 entries at a time by a
+            // Kogge-Stone scan over (a, b) pairs (x -> a x + b); the rotated
+            // H entries are then c_{i-1} x_{i-1} + s_{i-1} (h + h2)_i.
+            const int iter = k - 1, lane = tid & 31;
+            double xin = 0.0;  // x just before the chunk
+            for (int base = 0; base < iter; base += 32) {
+                const int i = base + lane;
+                double aa = 1.0, bb = 0.0, cur = 0.0;
+                if (i < iter) {
+                    cur = h[i] + h2[i];
+                    if (i == 0) {
+                        aa = 0.0;
+                        bb = cur;
+                    } else {
+                        aa = -snh[i - 1];
+                        bb = csh[i - 1] * cur;
+                    }
+                }
+                for (int o = 1; o < 32; o <<= 1) {
+                    const double ap = __shfl_up_sync(0xffffffffu, aa, o), bp = __shfl_up_sync(0xffffffffu, bb, o);
+                    if (lane >= o) {
+                        bb = fma(aa, bp, bb);
+                        aa = aa * ap;
+                    }
+                }
+                const double xi = fma(aa, xin, bb);
+                double xm1 = __shfl_up_sync(0xffffffffu, xi, 1);
+                if (lane == 0) xm1 = xin;
+                if (i >= 1 && i < iter) col[i - 1] = csh[i - 1] * xm1 + snh[i - 1] * cur;
+                xin = __shfl_sync(0xffffffffu, xi, 31);  // lanes past the column repeat its last entry
             }
-            const double hk = nrm, hd = prev;
+            __syncwarp();
+          if (lane == 0) {
+            const double hk = nrm, hd = xin;
             double cc, ss;
             if (hk == 0.0) {
                 cc = 1.0;
@@ -401,8 +422,6 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
             const int done = !(resid > a.tol) || iter >= a.max_iter;
             flag[0] = done;
             if (c == 0) {
-                double *gcol = a.H + (size_t)a.ldh * (iter - 1);
-                for (int i = 0; i <= iter; ++i) gcol[i] = col[i];
                 a.cs[iter - 1] = cc;
                 a.sn[iter - 1] = ss;
                 a.beta[iter - 1] = bet[iter - 1];
@@ -414,57 +433,64 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
                     a.ctl->replays = iter;
                 }
             }
+          }
+            __syncwarp();
+            if (c == 0) {
+                double *gcol = a.H + (size_t)a.ldh * (iter - 1);
+                for (int i = lane; i <= iter; i += 32) gcol[i] = col[i];
+            }
         }
         __syncthreads();
         if (flag[0]) break;  // the same in every CTA
-        for (int t = tid; t < bl; t += kCgTpb) {
-            // the S split partials, two interleaved sums each
-            double mbb[3], m2[3] = {0.0, 0.0, 0.0};
-            for (int d = 0; d < 3; ++d) mbb[d] = 0.0;
+        for (int e = tid; e < 3 * bl; e += kCgTpb) {
+            // component d of blob t: the S split partials (FP32 sums of at
+            // most kCgFold source pairs each, added in FP32), then
+            // w = M_bb z - (K z_body) in FP64
+            const int t = e / 3, d = e % 3, i1 = (d + 1) % 3, i2 = (d + 2) % 3;
+            float m0 = 0.f, m1 = 0.f;
             int sp = 0;
-            for (; sp + 1 < S; sp += 2)
-                for (int d = 0; d < 3; ++d) {
-                    mbb[d] += pp[3 * (sp * bl + t) + d];
-                    m2[d] += pp[3 * ((sp + 1) * bl + t) + d];
-                }
-            if (sp < S)
-                for (int d = 0; d < 3; ++d) mbb[d] += pp[3 * (sp * bl + t) + d];
-            for (int d = 0; d < 3; ++d) mbb[d] += m2[d];
-            const double *U = zb + 6 * ((b0 + t) / nblob), *d = dl + 3 * t;
-            wl[3 * t] = -(U[0] - d[1] * U[5] + d[2] * U[4]) + mbb[0];
-            wl[3 * t + 1] = -(U[1] - d[2] * U[3] + d[0] * U[5]) + mbb[1];
-            wl[3 * t + 2] = -(U[2] - d[0] * U[4] + d[1] * U[3]) + mbb[2];
+            for (; sp + 1 < S; sp += 2) {
+                m0 += pp[3 * (sp * bl + t) + d];
+                m1 += pp[3 * ((sp + 1) * bl + t) + d];
+            }
+            if (sp < S) m0 += pp[3 * (sp * bl + t) + d];
+            const double *U = zb + 6 * ((b0 + t) / nblob), *dd = dl + 3 * t;
+            wl[e] = -(U[d] - dd[i1] * U[3 + i2] + dd[i2] * U[3 + i1]) + (double)(m0 + m1);
         }
         __syncthreads();
         // ---- D..F: CGS2 and ||w|| ------------------------------------------
+        double part = 0.0;  // ||w||^2 of the thread's rows after the second pass
         for (int pass = 0; pass < 2; ++pass) {
             double *hp = pass == 0 ? hp1 : hp2, *hs = pass == 0 ? h : h2;
-            const int wid = tid >> 5, lane = tid & 31;
-            // lane = column, warp = rows congruent to it mod kCgWarps; then
-            // the warps' partials added in warp order
-            for (int c0 = 0; c0 < k; c0 += 32) {
-                const int i = c0 + lane;
+            // items (column i, row group g), PG groups per column on adjacent
+            // lanes (PG a power of two, k PG <= the CTA's threads): every lane
+            // of a warp has FP64 work, and a segmented shuffle tree adds a
+            // column's groups
+            int PG = 16;
+            while (PG > 1 && k * PG > kCgTpb) PG >>= 1;
+            {
+                const int t = tid, i = t / PG, g = t % PG;
+                double s0 = 0.0, s1 = 0.0;
                 if (i < k) {
-                    double s0 = 0.0, s1 = 0.0;
-                    int lr = wid;
+                    int lr = g;
                     if (i < kq) {
-                        for (; lr + kCgWarps < nr; lr += 2 * kCgWarps) {
+                        for (; lr + PG < nr; lr += 2 * PG) {
                             s0 += qs[lr * kqs + i] * wl[lr];
-                            s1 += qs[(lr + kCgWarps) * kqs + i] * wl[lr + kCgWarps];
+                            s1 += qs[(lr + PG) * kqs + i] * wl[lr + PG];
                         }
                         if (lr < nr) s0 += qs[lr * kqs + i] * wl[lr];
                     } else {
-                        for (; lr + kCgWarps < nr; lr += 2 * kCgWarps) {
+                        for (; lr + PG < nr; lr += 2 * PG) {
                             s0 += a.Qr[(size_t)row_of(lr) * a.ldr + i] * wl[lr];
-                            s1 += a.Qr[(size_t)row_of(lr + kCgWarps) * a.ldr + i] * wl[lr + kCgWarps];
+                            s1 += a.Qr[(size_t)row_of(lr + PG) * a.ldr + i] * wl[lr + PG];
                         }
                         if (lr < nr) s0 += a.Qr[(size_t)row_of(lr) * a.ldr + i] * wl[lr];
                     }
-                    hw[wid * kCgMaxK + i] = s0 + s1;
                 }
+                double sg = s0 + s1;
+                for (int o = PG >> 1; o > 0; o >>= 1) sg += __shfl_xor_sync(0xffffffffu, sg, o);
+                if (i < k && g == 0) hp[i] = sg;
             }
-            __syncthreads();
-            for (int i = tid; i < k; i += kCgTpb) hp[i] = tree16(hw + i, kCgMaxK);
             cl.sync();  // barriers 3 and 4
             cluster_reduce(cl, hp, k, hs, C, G);
             __syncthreads();
@@ -483,18 +509,21 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
                 }
                 for (; i < kc; ++i) p0 += hs[i] * qr[i];
                 for (; i < k; ++i) p0 += hs[i] * a.Q[a.ld * (size_t)i + row];
-                wl[lr] = wl[lr] - ((p0 + p1) + (p2 + p3));
+                const double v = wl[lr] - ((p0 + p1) + (p2 + p3));
+                wl[lr] = v;
+                if (pass == 1) part += v * v;
             }
             __syncthreads();
         }
-        double part = 0.0;
-        for (int lr = tid; lr < nr; lr += kCgTpb) part += wl[lr] * wl[lr];
         part = cg_block_sum(part, red);
         if (tid == 0) np[0] = part;
         cl.sync();  // barrier 5
         cluster_reduce(cl, np, 1, np + 1, C, G);
+        if (tid == 0) {
+            np[2] = sqrt(np[1]);
+            np[3] = 1.0 / np[2];
+        }
         __syncthreads();
-        nrm = sqrt(np[1]);
     }
     // no CTA leaves while another may still read its shared memory
     cl.sync();
