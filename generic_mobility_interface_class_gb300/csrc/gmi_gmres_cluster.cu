@@ -113,13 +113,14 @@ __host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc, int kqs = 
     return L;
 }
 
-// Deterministic block sum (fixed shuffle tree in each warp, then one over
-// the 16 warp sums held by lanes of warp 0); the result is returned to thread
-// 0 only.
-__device__ __forceinline__ double cg_block_sum(double v, double *red)
+// Deterministic block sum of values held by threads [0, nthreads) (fixed
+// shuffle tree in each of their warps, then one over the warp sums held by
+// lanes of warp 0); the result is returned to thread 0 only.
+__device__ __forceinline__ double cg_block_sum(double v, double *red, int nthreads)
 {
-    v = warp_sum(v);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (wid * 32 < nthreads) v = warp_sum(v);  // warps without values skip the FP64 tree
+    else v = 0.0;
     if (lane == 0) red[wid] = v;
     __syncthreads();
     double t = 0.0;
@@ -132,22 +133,28 @@ __device__ __forceinline__ double cg_block_sum(double v, double *red)
 }
 
 // out[e] = sum over the cluster's CTAs of arr[e] (e < count), for every
-// thread of the CTA: groups of G lanes (G a power of two, C <= G <= 32), lane
-// r of a group loads CTA r's element, an xor-shuffle tree adds them (every
-// lane ends with the same bits, in every CTA).
+// thread of the CTA.  Each element has kCrLanes adjacent lanes; lane r adds
+// the elements of CTAs r, r + kCrLanes, ... in that order, then an
+// xor-shuffle tree adds the lanes (every lane ends with the same bits, in
+// every CTA).  Only warps holding elements run FP64 instructions (a warp
+// FP64 instruction costs the same with any number of active lanes).
+constexpr int kCrLanes = 4;
+
 __device__ __forceinline__ void cluster_reduce(cg::cluster_group &cl, double *arr, int count, double *out, int C,
-                                               int G)
+                                               int /*G*/)
 {
-    const int groups = kCgTpb / G, gid = threadIdx.x / G, r = threadIdx.x % G;
+    constexpr int groups = kCgTpb / kCrLanes;
+    const int gid = threadIdx.x / kCrLanes, r = threadIdx.x % kCrLanes;
     for (int base = 0; base < count; base += groups) {
-        // only warps holding elements run the FP64 tree (a warp FP64
-        // instruction costs the same with any number of active lanes)
-        const int warps = (min(groups, count - base) * G + 31) / 32;
+        const int warps = (min(groups, count - base) * kCrLanes + 31) / 32;
         if ((int)(threadIdx.x >> 5) >= warps) continue;
         const int e = base + gid;
         double v = 0.0;
-        if (e < count && r < C) v = cl.map_shared_rank(arr, r)[e];
-        for (int o = G >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (e < count) {
+#pragma unroll 4
+            for (int q = r; q < C; q += kCrLanes) v += cl.map_shared_rank(arr, q)[e];
+        }
+        for (int o = kCrLanes >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (e < count && r == 0) out[e] = v;
     }
 }
@@ -265,15 +272,12 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
                 a.Qr[(size_t)row * a.ldr + (k - 1)] = q;
         }
         __syncthreads();
-        for (int t = tid; t < bl; t += kCgTpb) {
+        // per (blob, component): q and (R ref) x q
+        for (int e = tid; e < 3 * bl; e += kCgTpb) {
+            const int t = e / 3, cc = e % 3, i1 = (cc + 1) % 3, i2 = (cc + 2) % 3;
             const double *d = dl + 3 * t, *f = ql + 3 * t;
-            double *o = av + 6 * t;
-            o[0] = f[0];
-            o[1] = f[1];
-            o[2] = f[2];
-            o[3] = d[1] * f[2] - d[2] * f[1];
-            o[4] = d[2] * f[0] - d[0] * f[2];
-            o[5] = d[0] * f[1] - d[1] * f[0];
+            av[6 * t + cc] = f[cc];
+            av[6 * t + 3 + cc] = d[i1] * f[i2] - d[i2] * f[i1];
         }
         __syncthreads();
         swimmer_moments(av, W, nblob, b0, bl, mom1);
@@ -296,30 +300,23 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
         }
         __syncthreads();
         // ---- B: blob preconditioner, loads, moments of z -------------------
-        for (int t = tid; t < bl; t += kCgTpb) {
+        // per (blob, component): z = the blob block applied to q + U + U_rot x (R ref)
+        for (int e = tid; e < 3 * bl; e += kCgTpb) {
+            const int t = e / 3, cc = e % 3, i1 = (cc + 1) % 3, i2 = (cc + 2) % 3;
             const int i = b0 + t, sw = i / nblob;
             const double *U = zb + 6 * sw, *d = dl + 3 * t;
-            double o[3] = {ql[3 * t] + U[0], ql[3 * t + 1] + U[1], ql[3 * t + 2] + U[2]};
-            o[0] += U[4] * d[2] - U[5] * d[1];
-            o[1] += U[5] * d[0] - U[3] * d[2];
-            o[2] += U[3] * d[1] - U[4] * d[0];
-            for (int q = sw; q < W; ++q) {
-                o[0] *= a.minv;
-                o[1] *= a.minv;
-                o[2] *= a.minv;
-            }
-            float *ld0 = reinterpret_cast<float *>(iload + 2 * (i >> 1)), *ld1 = ld0 + 4;
-            const int l = i & 1;
-            ld0[l] = (float)o[0] * load_scale;
-            ld0[2 + l] = (float)o[1] * load_scale;
-            ld1[l] = (float)o[2] * load_scale;
-            double *b = av + 6 * t;
-            b[0] = o[0];
-            b[1] = o[1];
-            b[2] = o[2];
-            b[3] = d[1] * o[2] - d[2] * o[1];
-            b[4] = d[2] * o[0] - d[0] * o[2];
-            b[5] = d[0] * o[1] - d[1] * o[0];
+            double o = ql[3 * t + cc] + U[cc];
+            o += U[3 + i1] * d[i2] - U[3 + i2] * d[i1];
+            for (int q = sw; q < W; ++q) o *= a.minv;
+            float *ld = reinterpret_cast<float *>(iload + 2 * (i >> 1));
+            ld[cc == 0 ? (i & 1) : (cc == 1 ? 2 + (i & 1) : 4 + (i & 1))] = (float)o * load_scale;
+            av[6 * t + cc] = o;
+        }
+        __syncthreads();
+        for (int e = tid; e < 3 * bl; e += kCgTpb) {  // (R ref) x z
+            const int t = e / 3, cc = e % 3, i1 = (cc + 1) % 3, i2 = (cc + 2) % 3;
+            const double *d = dl + 3 * t, *o = av + 6 * t;
+            av[6 * t + 3 + cc] = d[i1] * o[i2] - d[i2] * o[i1];
         }
         __syncthreads();
         swimmer_moments(av, W, nblob, b0, bl, mom2);
@@ -359,8 +356,13 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
                     cnt = 0;
                 }
             }
+            if (pc <= kCgFold) {  // no fold happened: the partial is an FP32 sum (no FP64 work)
 #pragma unroll
-            for (int d = 0; d < 3; ++d) pp[3 * tid + d] = (float)(acc[d] + (double)(pacc[d].x + pacc[d].y));
+                for (int d = 0; d < 3; ++d) pp[3 * tid + d] = pacc[d].x + pacc[d].y;
+            } else {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) pp[3 * tid + d] = (float)(acc[d] + (double)(pacc[d].x + pacc[d].y));
+            }
         } else if (tid >= kCgPairThreads && k > 1) {
             // Givens step of iteration k - 1 by the last warp: the H column
             // h + h2 through the previous rotations.  Entry i after rotation
@@ -515,13 +517,14 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
             }
             __syncthreads();
         }
-        part = cg_block_sum(part, red);
+        part = cg_block_sum(part, red, nr);
         if (tid == 0) np[0] = part;
         cl.sync();  // barrier 5
         cluster_reduce(cl, np, 1, np + 1, C, G);
         if (tid == 0) {
-            np[2] = sqrt(np[1]);
-            np[3] = 1.0 / np[2];
+            const double ir = rsqrt(np[1]);
+            np[2] = np[1] * ir;  // ||w||
+            np[3] = ir;          // 1 / ||w||
         }
         __syncthreads();
     }
