@@ -29,11 +29,13 @@
 //   with nbroy = W * (6*nfil*nseg + 6), the reference's unknown ordering
 //   (per swimmer: per filament [tether, lambdas, clamp, segment u's], then body).
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
 
 #include "gmi_context.hpp"
+#include "gmi_gj_cluster.hpp"
 #include "gmi_lie.cuh"
 #include "gmi_solver_internal.hpp"
 
@@ -1178,6 +1180,7 @@ struct gmi_sim {
     std::vector<void *> allocs;
     bool prepared = false;
     int broyden_iter = 0;
+    bool use_gj_cluster = true;  // GMI_GJ_CLUSTER=0: one CTA per Jacobian inversion always
 };
 
 namespace gmi {
@@ -1256,8 +1259,15 @@ static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
         use_smem = 1;
         smem = base + mat;
     }
-    GMI_CUDA_TRY(cudaFuncSetAttribute(gj_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    gj_invert_kernel<<<P.F, kGjTpb, smem, sst(m)>>>(P.invJ, P.n6, use_smem, P.flags);
+    // few filaments: each inversion spread over a cluster of CTAs (the FP64
+    // work of one 120 x 120 inversion is ~0.4 ms on one SM)
+    const int csize = gj_cluster_size(P.F, P.n6, m->solver->ctx->sm_count);
+    if (csize > 1 && m->use_gj_cluster) {
+        GMI_TRY(gj_invert_cluster(sst(m), P.invJ, P.F, P.n6, csize, P.flags));
+    } else {
+        GMI_CUDA_TRY(cudaFuncSetAttribute(gj_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        gj_invert_kernel<<<P.F, kGjTpb, smem, sst(m)>>>(P.invJ, P.n6, use_smem, P.flags);
+    }
     if (!P.wall) {  // the body coupling (swimmer.cpp:466-682); none on the wall
         filament_B_kernel<<<P.F, 128, 6 * P.n6 * sizeof(double), sst(m)>>>(P, nt);
         schur_filament_kernel<<<P.F, 32, 0, sst(m)>>>(P, m->spart);
@@ -1449,6 +1459,10 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
     }
     SIM_ARG_CHECK(cfg->dt > 0 && cfg->kb > 0 && cfg->kt > 0, "gmi_sim_create: dt, kb and kt must be positive");
     gmi_sim *m = new (std::nothrow) gmi_sim();
+    if (m != nullptr) {
+        const char *gj = std::getenv("GMI_GJ_CLUSTER");
+        m->use_gj_cluster = !(gj && gj[0] == '0');
+    }
     SIM_ARG_CHECK(m != nullptr, "gmi_sim_create: out of host memory");
     m->cfg = *cfg;
     gmi_status st = gmi_solver_create(&mc, &m->solver);
