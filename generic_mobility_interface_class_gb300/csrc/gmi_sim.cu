@@ -731,22 +731,46 @@ __device__ M3 mat6_block_mul(const double *bm6, int r0, int c0, const M3 &B)  //
 }
 
 // The B block of one filament (swimmer.cpp:553-670), then jacB = B * invJ
-// (swimmer.cpp:671).  One CTA per filament; thread 0 assembles B in shared
-// memory, all threads form the product.
+// (swimmer.cpp:671).  One CTA per filament, in phases that each spread the
+// FP64 work over threads (a warp FP64 instruction costs the same on one
+// lane as on 32): the fixed blocks; B = (rotated body mobility) B, one
+// column per thread; the sphere-correction matrices, one segment per thread;
+// their addition, one (column block, row half) per thread in the reference's
+// segment order; the D^-1 products, one column block per thread; the scale.
+// Needs NS >= 2 (as the Jacobian build does).
 __global__ void __launch_bounds__(128) filament_B_kernel(SimP P, int nt)
 {
-    extern __shared__ double Bs[];  // 6 x n6, column-major
-    const int fil = blockIdx.x;
+    extern __shared__ double Bs[];  // 6 x n6, column-major; then scratch
+    const int fil = blockIdx.x, tid = threadIdx.x, nthr = blockDim.x;
     const int n = fil / P.NF, NS = P.NS, n6 = P.n6, s0 = fil * NS;
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < 6 * n6; ++k) Bs[k] = 0.0;
-        const double dt_fac = (nt < P.neuler) ? -P.DT : -2.0 * P.DT / 3.0;
-        const double *u = P.bu + 3 * n, *x = P.bx + 3 * n;
-        const M3 Qi = ldm3(P.bQ + 9 * n);
+    double *seg = Bs + 6 * n6;    // per segment: add (rows 0-2, 3-5), sub (rows 0-2, 3-5), 3x3 each
+    double *spec = seg + 36 * NS;  // segment 0's columns 3NS.. terms, the last segment's end-force terms
+    double *Dm = spec + 36;        // Dinv, DinvT, Bend
+    double *bm = Dm + 27;          // rotated body mobility, 6 x 6 column-major
+    auto ld3 = [](const double *p) { M3 m; for (int k = 0; k < 9; ++k) m.a[k] = p[k]; return m; };
+    auto st3 = [](double *p, const M3 &m) { for (int k = 0; k < 9; ++k) p[k] = m.a[k]; };
+    const double dt_fac = (nt < P.neuler) ? -P.DT : -2.0 * P.DT / 3.0;
+    const double *u = P.bu + 3 * n, *x = P.bx + 3 * n;
+    const M3 Qi = ldm3(P.bQ + 9 * n);
+    for (int k = tid; k < 6 * n6; k += nthr) Bs[k] = 0.0;
+    if (tid == 0) {
         const M3 blc = m3_scale(rcross(u), -1.0);
         const M3 blc2 = m3_scale(m3_mul(blc, blc), 1.0 / 12.0);
-        M3 Dinv = m3_sub(m3_add(m3_eye(), blc2), m3_scale(blc, 0.5));
-        M3 DinvT = m3_add(m3_add(m3_eye(), blc2), m3_scale(blc, 0.5));
+        st3(Dm, m3_sub(m3_add(m3_eye(), blc2), m3_scale(blc, 0.5)));
+        st3(Dm + 9, m3_add(m3_add(m3_eye(), blc2), m3_scale(blc, 0.5)));
+        double t[3], te[3];
+        q_tangent(ldq(P.q + 4 * (s0 + NS - 1)), t);
+        for (int c = 0; c < 3; ++c) te[c] = P.EFM * t[c];
+        st3(Dm + 18, rcross(te));
+    }
+    if (tid >= 32 && tid < 36) {  // rotated_mobility: Q B Q^T, one 3x3 block per thread
+        const int bi = (tid - 32) / 2, bj = (tid - 32) % 2;
+        const M3 b = get_block(P.mob_ref, 6, 3 * bi, 3 * bj);
+        put_block(bm, 6, 3 * bi, 3 * bj, m3_mul(m3_mul(Qi, b), m3_T(Qi)));
+    }
+    __syncthreads();
+    const M3 Dinv = ld3(Dm), DinvT = ld3(Dm + 9), Bend = ld3(Dm + 18);
+    if (tid == 0) {
         double fbd[3];
         m3_vec(Qi, P.fref + 3 * fil, fbd);
         Bs[0 + 6 * 0] = -1.0;
@@ -754,78 +778,90 @@ __global__ void __launch_bounds__(128) filament_B_kernel(SimP P, int nt)
         Bs[2 + 6 * 2] = -1.0;
         put_block(Bs, 6, 3, 0, rcross(fbd));
         put_block(Bs, 6, 3, 3 * NS, m3_scale(DinvT, -1.0));
-        double t[3], te[3];
-        q_tangent(ldq(P.q + 4 * (s0 + NS - 1)), t);
-        for (int c = 0; c < 3; ++c) te[c] = P.EFM * t[c];
-        const M3 Bend = rcross(te);
         put_block(Bs, 6, 0, 6 * NS - 3, Bend);
-        double diff[3], w[3];
+        double t[3], diff[3], w[3];
+        q_tangent(ldq(P.q + 4 * (s0 + NS - 1)), t);
         for (int c = 0; c < 3; ++c) diff[c] = P.x[3 * (s0 + NS - 1) + c] - x[c];
         for (int c = 0; c < 3; ++c) w[c] = 0.5 * P.DL * t[c] - diff[c];
         put_block(Bs, 6, 3, 6 * NS - 3, m3_mul(rcross(w), Bend));
-        for (int m = 1; m < NS - 1; ++m) {
-            double tm[3], dtm[3];
-            q_tangent(ldq(P.q + 4 * (s0 + m)), tm);
-            for (int c = 0; c < 3; ++c) dtm[c] = P.DL * tm[c];
-            put_block(Bs, 6, 3, 3 * (NS + m), m3_mul(Bend, rcross(dtm)));
-        }
-        // B = body_mobility * B
-        double bm[36];
-        rotated_mobility(P, Qi, bm);
-        for (int c = 0; c < n6; ++c) {
-            double colv[6];
-            for (int r = 0; r < 6; ++r) {
-                double s = 0.0;
-                for (int k = 0; k < 6; ++k) s += bm[r + 6 * k] * Bs[k + 6 * c];
-                colv[r] = s;
-            }
-            for (int r = 0; r < 6; ++r) Bs[r + 6 * c] = colv[r];
-        }
-        // sphere corrections (swimmer.cpp:604-658)
-        const double R = P.Rbody;
-        const double R2 = R * R + P.RSEG * P.RSEG;
-        for (int k = 0; k < NS; ++k) {
-            double rh[3];
-            for (int c = 0; c < 3; ++c) rh[c] = P.x[3 * (s0 + k) + c] - x[c];
-            const double r = sqrt(rh[0] * rh[0] + rh[1] * rh[1] + rh[2] * rh[2]);
-            for (int c = 0; c < 3; ++c) rh[c] /= r;
-            M3 rr, I = m3_eye();
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) rr(i, j) = rh[i] * rh[j];
-            const M3 Mtt = m3_scale(m3_add(m3_scale(I, 1.0 + R2 / (3.0 * r * r)), m3_scale(rr, 1.0 - R2 / (r * r))),
-                                    1.0 / (8.0 * kPi * P.MU * r));
-            const M3 Mtr = m3_scale(rcross(rh), 1.0 / (8.0 * kPi * P.MU * r * r));
-            const M3 Mrr = m3_scale(m3_sub(m3_scale(rr, 3.0), I), 1.0 / (16.0 * kPi * P.MU * r * r * r));
-            double tk[3];
-            q_tangent(ldq(P.q + 4 * (s0 + k)), tk);
-            const M3 temp = rcross(tk);
-            const M3 Mtr_t = m3_mul(m3_scale(Mtr, 0.5 * P.DL), temp);
-            const M3 Mrr_t = m3_mul(m3_scale(Mrr, 0.5 * P.DL), temp);
-            if (k == 0) {
-                add_block(Bs, 6, 0, 0, Mtt);
-                add_block(Bs, 6, 3, 0, Mtr);
-                add_block(Bs, 6, 0, 3 * NS, m3_mul(Mtr, DinvT));
-                add_block(Bs, 6, 3, 3 * NS, m3_mul(Mrr, DinvT));
-                add_block(Bs, 6, 0, 3, m3_sub(Mtr_t, Mtt));
-                add_block(Bs, 6, 3, 3, m3_sub(Mrr_t, Mtr));
-            } else if (k == NS - 1) {
-                add_block(Bs, 6, 0, 6 * NS - 3, m3_mul(m3_scale(Mtt, -P.EFM), temp));
-                add_block(Bs, 6, 3, 6 * NS - 3, m3_mul(m3_scale(Mtr, -P.EFM), temp));
-                add_block(Bs, 6, 0, 3 * NS - 3, m3_add(Mtr_t, Mtt));
-                add_block(Bs, 6, 3, 3 * NS - 3, m3_add(Mrr_t, Mtr));
-            } else {
-                add_block(Bs, 6, 0, 3 * k, m3_add(Mtr_t, Mtt));
-                add_block(Bs, 6, 3, 3 * k, m3_add(Mrr_t, Mtr));
-                add_block(Bs, 6, 0, 3 * (k + 1), m3_sub(Mtr_t, Mtt));
-                add_block(Bs, 6, 3, 3 * (k + 1), m3_sub(Mrr_t, Mtr));
-            }
-        }
-        for (int k = 0; k < NS; ++k) {
-            put_block(Bs, 6, 3, 3 * k, m3_mul(Dinv, get_block(Bs, 6, 3, 3 * k)));
-            put_block(Bs, 6, 3, 3 * (k + NS), m3_mul(Dinv, get_block(Bs, 6, 3, 3 * (k + NS))));
-        }
-        for (int k = 0; k < 6 * n6; ++k) Bs[k] *= dt_fac;
     }
+    for (int m = 1 + tid; m < NS - 1; m += nthr) {
+        double tm[3], dtm[3];
+        q_tangent(ldq(P.q + 4 * (s0 + m)), tm);
+        for (int c = 0; c < 3; ++c) dtm[c] = P.DL * tm[c];
+        put_block(Bs, 6, 3, 3 * (NS + m), m3_mul(Bend, rcross(dtm)));
+    }
+    __syncthreads();
+    // B = body_mobility * B, one column per thread
+    for (int c = tid; c < n6; c += nthr) {
+        double colv[6];
+        for (int r = 0; r < 6; ++r) {
+            double acc = 0.0;
+            for (int k = 0; k < 6; ++k) acc += bm[r + 6 * k] * Bs[k + 6 * c];
+            colv[r] = acc;
+        }
+        for (int r = 0; r < 6; ++r) Bs[r + 6 * c] = colv[r];
+    }
+    // sphere corrections (swimmer.cpp:604-658), one segment per thread
+    const double R = P.Rbody;
+    const double R2 = R * R + P.RSEG * P.RSEG;
+    for (int k = tid; k < NS; k += nthr) {
+        double rh[3];
+        for (int c = 0; c < 3; ++c) rh[c] = P.x[3 * (s0 + k) + c] - x[c];
+        const double r = sqrt(rh[0] * rh[0] + rh[1] * rh[1] + rh[2] * rh[2]);
+        for (int c = 0; c < 3; ++c) rh[c] /= r;
+        M3 rr, I = m3_eye();
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) rr(i, j) = rh[i] * rh[j];
+        const M3 Mtt = m3_scale(m3_add(m3_scale(I, 1.0 + R2 / (3.0 * r * r)), m3_scale(rr, 1.0 - R2 / (r * r))),
+                                1.0 / (8.0 * kPi * P.MU * r));
+        const M3 Mtr = m3_scale(rcross(rh), 1.0 / (8.0 * kPi * P.MU * r * r));
+        const M3 Mrr = m3_scale(m3_sub(m3_scale(rr, 3.0), I), 1.0 / (16.0 * kPi * P.MU * r * r * r));
+        double tk[3];
+        q_tangent(ldq(P.q + 4 * (s0 + k)), tk);
+        const M3 temp = rcross(tk);
+        const M3 Mtr_t = m3_mul(m3_scale(Mtr, 0.5 * P.DL), temp);
+        const M3 Mrr_t = m3_mul(m3_scale(Mrr, 0.5 * P.DL), temp);
+        double *o = seg + 36 * k;
+        if (k == 0) {
+            st3(o, Mtt);
+            st3(o + 9, Mtr);
+            st3(spec, m3_mul(Mtr, DinvT));
+            st3(spec + 9, m3_mul(Mrr, DinvT));
+            st3(o + 18, m3_sub(Mtr_t, Mtt));
+            st3(o + 27, m3_sub(Mrr_t, Mtr));
+        } else if (k == NS - 1) {
+            st3(spec + 18, m3_mul(m3_scale(Mtt, -P.EFM), temp));
+            st3(spec + 27, m3_mul(m3_scale(Mtr, -P.EFM), temp));
+            st3(o, m3_add(Mtr_t, Mtt));
+            st3(o + 9, m3_add(Mrr_t, Mtr));
+        } else {
+            st3(o, m3_add(Mtr_t, Mtt));
+            st3(o + 9, m3_add(Mrr_t, Mtr));
+            st3(o + 18, m3_sub(Mtr_t, Mtt));
+            st3(o + 27, m3_sub(Mrr_t, Mtr));
+        }
+    }
+    __syncthreads();
+    // column block cb gets segment cb-1's second pair of terms, then segment
+    // cb's first (the order of the reference's segment loop)
+    for (int t = tid; t < 4 * NS; t += nthr) {
+        const int cb = t / 2, half = t % 2, r0 = 3 * half;
+        if (cb == 0) {
+            add_block(Bs, 6, r0, 0, ld3(seg + 9 * half));
+        } else if (cb < NS) {
+            add_block(Bs, 6, r0, 3 * cb, ld3(seg + 36 * (cb - 1) + 18 + 9 * half));
+            add_block(Bs, 6, r0, 3 * cb, ld3(seg + 36 * cb + 9 * half));
+        } else if (cb == NS) {
+            add_block(Bs, 6, r0, 3 * NS, ld3(spec + 9 * half));
+        } else if (cb == 2 * NS - 1) {
+            add_block(Bs, 6, r0, 6 * NS - 3, ld3(spec + 18 + 9 * half));
+        }
+    }
+    __syncthreads();
+    for (int cb = tid; cb < 2 * NS; cb += nthr) put_block(Bs, 6, 3, 3 * cb, m3_mul(Dinv, get_block(Bs, 6, 3, 3 * cb)));
+    __syncthreads();
+    for (int k = tid; k < 6 * n6; k += nthr) Bs[k] *= dt_fac;
     __syncthreads();
     const double *Jinv = P.invJ + (size_t)fil * n6 * n6;
     double *jB = P.jacB + (size_t)fil * 6 * n6;
@@ -1269,7 +1305,8 @@ static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
         gj_invert_kernel<<<P.F, kGjTpb, smem, sst(m)>>>(P.invJ, P.n6, use_smem, P.flags);
     }
     if (!P.wall) {  // the body coupling (swimmer.cpp:466-682); none on the wall
-        filament_B_kernel<<<P.F, 128, 6 * P.n6 * sizeof(double), sst(m)>>>(P, nt);
+        filament_B_kernel<<<P.F, 128, (6 * (size_t)P.n6 + 36 * (size_t)P.NS + 36 + 27 + 36) * sizeof(double),
+                            sst(m)>>>(P, nt);
         schur_filament_kernel<<<P.F, 32, 0, sst(m)>>>(P, m->spart);
         swimmer_schur_kernel<<<P.W, 64, 0, sst(m)>>>(P, nt, m->spart);
     }
