@@ -1220,6 +1220,7 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
                             int n_tgt, const void *src_rec, int n_src, const PairConsts &k, double *out,
                             int accumulate)
 {
+    if (env.splits_out) *env.splits_out = 1;
     if (n_tgt <= 0) return GMI_OK;
     const int nout = nout_of(kind);
     if (n_src <= 0) {
@@ -1277,6 +1278,10 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     if (st != GMI_OK) return st;
     void *params[] = {&map, &a};
     GMI_CUDA_TRY(cudaLaunchKernel(fn, dim3(n_tgt_ctas, splits), dim3(tpb), params, smem, env.stream));
+    if (env.splits_out) {
+        *env.splits_out = splits;
+        return GMI_OK;
+    }
     if (splits > 1) {
         const int count = n_tgt * nout;
         reduce_splits<<<(count + 255) / 256, 256, 0, env.stream>>>(a.partial, splits, count, out, accumulate,

@@ -79,6 +79,8 @@ struct ExplicitPairEnv {
     int tpb, tt;           // launch shape
     int scalar_only;       // non-zero: one source per thread step even where the packed kernel exists
     const int *skip;       // optional device flag: non-zero turns the launch into a no-op
+    int *splits_out;       // optional: the caller adds the per-split partials (partial[p * 3 n_tgt + e],
+                           // p < *splits_out) itself; 1 means the kernel wrote `out` directly
 };
 
 size_t record_bytes(bool f64);

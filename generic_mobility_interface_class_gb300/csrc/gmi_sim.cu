@@ -35,7 +35,7 @@
 #include <vector>
 
 #include "gmi_context.hpp"
-#include "gmi_gj_cluster.hpp"
+#include "gmi_gauss_jordan.hpp"
 #include "gmi_lie.cuh"
 #include "gmi_solver_internal.hpp"
 
@@ -619,102 +619,6 @@ __global__ void __launch_bounds__(kJacTpb) build_jacobian_kernel(SimP P, int nt)
     }
 }
 
-// In-place inverse of n x n column-major matrices, one CTA each, Gauss-Jordan
-// with partial (row) pivoting and the column swaps undone at the end; the
-// matrix lives in shared memory when it fits.  Stands in for the reference's
-// LAPACK dgetrf + dgetri (matrix.cpp:538-566); a zero pivot sets flags[2].
-constexpr int kGjTpb = 512;  // 16 warps: four per scheduler keep the FP64 unit busy
-constexpr int kGjWarps = kGjTpb / 32;
-
-__global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, int use_smem, int *flags)
-{
-    extern __shared__ double sh[];
-    double *Mg = mats + (size_t)blockIdx.x * n * n;
-    double *col = sh;                      // n: pivot column before the step
-    double *redv = col + n;                // 32 (unused slots kept for the layout)
-    int *redi = reinterpret_cast<int *>(redv + 32);  // 32
-    int *perm = redi + 32;                 // n
-    double *A = use_smem ? reinterpret_cast<double *>(perm + ((n + 1) & ~1)) : Mg;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (use_smem)
-        for (int e = tid; e < n * n; e += kGjTpb) A[e] = Mg[e];
-    __shared__ int singular;
-    if (tid == 0) singular = 0;
-    __syncthreads();
-    for (int k = 0; k < n; ++k) {
-        // partial pivoting by warp 0: largest |A(i, k)|, i >= k, lowest i on ties
-        if (wid == 0) {
-            double best = -1.0;
-            int bi = k;
-            for (int i = k + lane; i < n; i += 32) {
-                const double a = fabs(A[i + (size_t)n * k]);
-                if (a > best) {
-                    best = a;
-                    bi = i;
-                }
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_down_sync(0xffffffffu, best, o);
-                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-                if (ob > best || (ob == best && oi < bi)) {
-                    best = ob;
-                    bi = oi;
-                }
-            }
-            if (lane == 0) {
-                perm[k] = bi;
-                if (!(best > 0.0)) singular = 1;
-            }
-        }
-        __syncthreads();
-        if (singular) break;
-        const int p = perm[k];
-        // row swap, then the pivot column saved
-        if (p != k)
-            for (int j = tid; j < n; j += kGjTpb) {
-                const double t = A[k + (size_t)n * j];
-                A[k + (size_t)n * j] = A[p + (size_t)n * j];
-                A[p + (size_t)n * j] = t;
-            }
-        __syncthreads();
-        const double pivinv = 1.0 / A[k + (size_t)n * k];
-        for (int i = tid; i < n; i += kGjTpb) col[i] = A[i + (size_t)n * k];
-        __syncthreads();
-        // column j (one warp per column, lanes over rows): scale the pivot
-        // row entry, eliminate every other row; column k becomes -col/pivot
-        for (int j = wid; j < n; j += kGjWarps) {
-            double *Aj = A + (size_t)n * j;
-            if (j == k) {
-                for (int i = lane; i < n; i += 32) Aj[i] = (i == k) ? pivinv : -col[i] * pivinv;
-            } else {
-                const double akj = Aj[k] * pivinv;
-#pragma unroll 4
-                for (int i = lane; i < n; i += 32)
-                    if (i != k) Aj[i] = Aj[i] - akj * col[i];
-                __syncwarp();
-                if (lane == 0) Aj[k] = akj;
-            }
-        }
-        __syncthreads();
-    }
-    if (singular) {
-        if (tid == 0) atomicOr(flags + 2, 1);
-        return;
-    }
-    for (int k = n - 1; k >= 0; --k) {
-        const int p = perm[k];
-        if (p != k)
-            for (int i = tid; i < n; i += kGjTpb) {
-                const double t = A[i + (size_t)n * k];
-                A[i + (size_t)n * k] = A[i + (size_t)n * p];
-                A[i + (size_t)n * p] = t;
-            }
-        __syncthreads();
-    }
-    if (use_smem)
-        for (int e = tid; e < n * n; e += kGjTpb) Mg[e] = A[e];
-}
-
 // rotated body mobility: Q B Q^T blockwise (swimmer.cpp:522-527)
 __device__ void rotated_mobility(const SimP &P, const M3 &Q, double *bm /*36, column-major*/)
 {
@@ -1217,7 +1121,8 @@ struct gmi_sim {
     std::vector<void *> allocs;
     bool prepared = false;
     int broyden_iter = 0;
-    bool use_gj_cluster = true;  // GMI_GJ_CLUSTER=0: one CTA per Jacobian inversion always
+    bool use_gj_cluster = true;   // GMI_GJ_CLUSTER=0: one CTA per Jacobian inversion always
+    bool use_gj_registers = true;  // GMI_GJ_REGISTERS=0: the columns stepped through shared memory
 };
 
 namespace gmi {
@@ -1285,26 +1190,9 @@ static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
 {
     const SimP &P = m->P;
     build_jacobian_kernel<<<P.F, kJacTpb, 0, sst(m)>>>(P, nt);
-    const size_t mat = (size_t)P.n6 * P.n6 * sizeof(double);
-    const size_t base = (size_t)P.n6 * sizeof(double) + 32 * sizeof(double) + 32 * sizeof(int) +
-                        (size_t)((P.n6 + 1) & ~1) * sizeof(int);
-    int use_smem = 0;
-    size_t smem = base;
-    int dev_max = 0;
-    GMI_CUDA_TRY(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->solver->ctx->device));
-    if (base + mat + 256 <= (size_t)dev_max) {
-        use_smem = 1;
-        smem = base + mat;
-    }
-    // few filaments: each inversion spread over a cluster of CTAs (the FP64
-    // work of one 120 x 120 inversion is ~0.4 ms on one SM)
-    const int csize = gj_cluster_size(P.F, P.n6, m->solver->ctx->sm_count);
-    if (csize > 1 && m->use_gj_cluster) {
-        GMI_TRY(gj_invert_cluster(sst(m), P.invJ, P.F, P.n6, csize, P.flags));
-    } else {
-        GMI_CUDA_TRY(cudaFuncSetAttribute(gj_invert_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        gj_invert_kernel<<<P.F, kGjTpb, smem, sst(m)>>>(P.invJ, P.n6, use_smem, P.flags);
-    }
+    // few filaments: each inversion spread over a cluster of CTAs
+    const int csize = m->use_gj_cluster ? gj_cluster_size(P.F, P.n6, m->solver->ctx->sm_count) : 1;
+    GMI_TRY(gj_invert(sst(m), P.invJ, P.F, P.n6, csize, m->use_gj_registers, m->solver->ctx->device, P.flags));
     if (!P.wall) {  // the body coupling (swimmer.cpp:466-682); none on the wall
         filament_B_kernel<<<P.F, 128, (6 * (size_t)P.n6 + 36 * (size_t)P.NS + 36 + 27 + 36) * sizeof(double),
                             sst(m)>>>(P, nt);
@@ -1500,6 +1388,8 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
     if (m != nullptr) {
         const char *gj = std::getenv("GMI_GJ_CLUSTER");
         m->use_gj_cluster = !(gj && gj[0] == '0');
+        const char *gr = std::getenv("GMI_GJ_REGISTERS");
+        m->use_gj_registers = !(gr && gr[0] == '0');
     }
     SIM_ARG_CHECK(m != nullptr, "gmi_sim_create: out of host memory");
     m->cfg = *cfg;

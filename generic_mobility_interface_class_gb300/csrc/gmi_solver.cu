@@ -126,17 +126,32 @@ __global__ void blob_positions_kernel(int W, int nblob, const double *__restrict
 }
 
 // Per swimmer: sums[6n..] = (sum_m f_m, sum_m (R ref_m) x f_m) over its blobs.
-// This is K^T f (mobility_solver.cpp:690-697, 921-940, 168-188).
-// K^T f per swimmer (the 6-vector sum over its blobs of (f, (R ref) x f)),
-// in two passes: kKtBlobs blobs per CTA into part[(n gx + x) 6 + c], then
-// one thread per (swimmer, component) adds the CTA partials in order.
+// This is K^T f (mobility_solver.cpp:690-697, 921-940, 168-188), in two
+// passes: kKtBlobs blobs per CTA into part[(n gx + x) 6 + c], then the CTA
+// partials added per (swimmer, component) in a fixed order.
 constexpr int kKtBlobs = 128;
+
+// Block sum of six per-thread values, in a fixed order: threads 0..5 write
+// the totals to out[0..6).
+template <int TPB> __device__ __forceinline__ void block_sum6(const double *v, double *out)
+{
+    __shared__ double red[TPB / 32][6];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const double t = warp_sum6_scatter(v);
+    if ((lane & 3) == 0 && lane < 24) red[wid][lane >> 2] = t;
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < TPB / 32; ++w) s += red[w][threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+}
 
 __global__ void __launch_bounds__(kKtBlobs) kt_partial_kernel(int nblob, const double *__restrict__ R,
                                                              const double *__restrict__ refs,
                                                              const double *__restrict__ f, double *__restrict__ part)
 {
-    __shared__ double red[32];
     const int n = blockIdx.y, m = blockIdx.x * kKtBlobs + threadIdx.x;
     double a[6] = {0, 0, 0, 0, 0, 0};
     if (m < nblob) {
@@ -150,20 +165,21 @@ __global__ void __launch_bounds__(kKtBlobs) kt_partial_kernel(int nblob, const d
         a[4] = d[2] * fm[0] - d[0] * fm[2];
         a[5] = d[0] * fm[1] - d[1] * fm[0];
     }
-    for (int c = 0; c < 6; ++c) {
-        const double t = block_sum<kKtBlobs>(a[c], red);
-        if (threadIdx.x == 0) part[((size_t)n * gridDim.x + blockIdx.x) * 6 + c] = t;
-    }
+    block_sum6<kKtBlobs>(a, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
 }
 
+// One warp per swimmer: the lanes stride over the CTA partials, then one
+// six-value warp sum.
 __global__ void kt_finish_kernel(int W, int gx, const double *__restrict__ part, double *__restrict__ sums)
 {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= 6 * W) return;
-    const int n = e / 6, c = e % 6;
-    double t = 0.0;
-    for (int x = 0; x < gx; ++x) t += part[((size_t)n * gx + x) * 6 + c];
-    sums[e] = t;
+    const int lane = threadIdx.x & 31, n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (n >= W) return;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    for (int x = lane; x < gx; x += 32)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) a[c] += part[((size_t)n * gx + x) * 6 + c];
+    const double t = warp_sum6_scatter(a);
+    if ((lane & 3) == 0 && lane < 24) sums[6 * n + (lane >> 2)] = t;
 }
 
 // body_f += sums (the blob repulsion's force and torque on each body).
@@ -397,8 +413,9 @@ __global__ void scale_kernel(int n, const double *__restrict__ x, const double *
 //   S1 (CTA per 64 blobs)   q_{k-1} = w / ||w|| into Q; body moments;
 //                            last CTA: body rows of q and z_body = U
 //   S2 (CTA per 64 blobs)   z_blob; records of z; last CTA: w_body = -K^T z
-//   pair kernel (+ split reduction) on the records -> mbb
-//   S3 (CTA per kSRows rows) w_blob = M_bb z - K z_body; Q^T w; last: h, H col
+//   pair kernel on the records -> mbb, or per-split partials
+//   S3 (CTA per kSRows rows) w_blob = M_bb z - K z_body (adding the split
+//                            partials); Q^T w; last: h, H col
 //   S4 (CTA per kSRows rows) w -= Q h; Q^T w; last: h, H col +=
 //   S5 (CTA per kSRows rows) w -= Q h; ||w||^2; last: H(k, k-1), Givens, ctl
 // ---------------------------------------------------------------------------
@@ -415,47 +432,53 @@ constexpr int kStepScalars = kFMaxK + 8;
 // True in every thread of the CTA that arrives last (of `total`) at *ticket;
 // that CTA re-arms the ticket for the next launch.  Partials written before
 // the call are visible to the last CTA through L2 (__ldcg).
+// The block barrier orders the CTA's writes before thread 0's release fence
+// (a CTA barrier synchronises, and a release is cumulative over what
+// precedes it), so one thread fences for the whole CTA; the last CTA's
+// acquire fence, then its block barrier, make every partial visible to all
+// of its threads.
 __device__ __forceinline__ bool last_cta(int *ticket, int total)
 {
     __shared__ int is_last;
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
         const int t = atomicAdd(ticket, 1);
         is_last = (t == total - 1);
-        if (is_last) *ticket = 0;
+        if (is_last) {
+            *ticket = 0;
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        }
     }
     __syncthreads();
-    if (is_last) __threadfence();
     return is_last;
 }
 
-// Block sum of 6 per-thread values, in a fixed order; thread 0 writes them to out[0..6).
-template <int TPB> __device__ __forceinline__ void block_sum6(const double *v, double *out)
-{
-    __shared__ double red[6][TPB / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        const double t = warp_sum(v[c]);
-        if (lane == 0) red[c][wid] = t;
-    }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-        double t = 0.0;
-        for (int w = 0; w < TPB / 32; ++w) t += red[threadIdx.x][w];
-        out[threadIdx.x] = t;
-    }
-}
-
 // Sum over the gx per-CTA 6-vectors of each swimmer (part[(n*gx + x)*6 + c])
-// into sh[6n + c], in x order.  The CTA first copies the partials into
-// shared memory (stage, kStageMax doubles) with coalesced loads, so the
-// sequential sums read no global memory; one thread per (swimmer, component).
+// into sh[6n + c], in a fixed order, by whichever of two layouts issues
+// fewer FP64 warp instructions: few swimmers take one warp each (the lanes
+// stride over the partials, then a six-value warp sum); many swimmers take
+// one thread per (swimmer, component), after a coalesced copy of the
+// partials into shared memory (stage, kStageMax doubles) when they fit.
 constexpr int kStageMax = 4096;
 __device__ __forceinline__ void swimmer_sums(const double *part, int W, int gx, double *sh)
 {
     __shared__ double stage[kStageMax];
+    const int nw = blockDim.x >> 5, lane = threadIdx.x & 31;
+    const int per_warp = (W + nw - 1) / nw * (6 * ((gx + 31) / 32) + 9);
+    const int per_thread = (6 * W + blockDim.x - 1) / blockDim.x * gx;
+    if (per_warp < per_thread) {
+        for (int n = threadIdx.x >> 5; n < W; n += nw) {
+            double a[6] = {0, 0, 0, 0, 0, 0};
+            for (int x = lane; x < gx; x += 32)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) a[c] += __ldcg(part + ((size_t)n * gx + x) * 6 + c);
+            const double t = warp_sum6_scatter(a);
+            if ((lane & 3) == 0 && lane < 24) sh[6 * n + (lane >> 2)] = t;
+        }
+        __syncthreads();
+        return;
+    }
     const int total = 6 * W * gx;
     const bool staged = total <= kStageMax;
     if (staged)
@@ -520,22 +543,22 @@ __global__ void __launch_bounds__(kSBlobs) s1_normalise_moments_kernel(
     if (!last_cta(ticket, gridDim.x * gridDim.y)) return;
     extern __shared__ double sh[];  // 6 W
     swimmer_sums(part, W, gridDim.x, sh);
-    for (int s = threadIdx.x; s < W; s += kSBlobs) {
-        const double *sums = sh + 6 * s;
-        double qb[6];
-        for (int c = 0; c < 6; ++c) {
-            qb[c] = w[3 * nb + 6 * s + c] * inrm;
-            q[3 * nb + 6 * s + c] = qb[c];
+    // body rows of q, and z_body = KTKinv_rot (-sums) - mob_rot q_body: one
+    // thread per (swimmer, row), the products in two interleaved chains each
+    for (int e = threadIdx.x; e < 6 * W; e += kSBlobs) {
+        const int sw = e / 6, i = e % 6;
+        const double *sums = sh + 6 * sw, *wb = w + 3 * nb + 6 * sw;
+        q[3 * nb + e] = wb[i] * inrm;
+        const double *Kt = ktk_rot + 36 * sw + i, *Mb = mob_rot + 36 * sw + i;
+        double x0 = 0.0, x1 = 0.0, y0 = 0.0, y1 = 0.0;
+#pragma unroll
+        for (int j = 0; j < 6; j += 2) {
+            x0 += Kt[6 * j] * (-sums[j]);
+            x1 += Kt[6 * (j + 1)] * (-sums[j + 1]);
+            y0 += Mb[6 * j] * wb[j];
+            y1 += Mb[6 * (j + 1)] * wb[j + 1];
         }
-        const double *Kt = ktk_rot + 36 * s, *Mb = mob_rot + 36 * s;
-        for (int i = 0; i < 6; ++i) {
-            double x = 0.0, y = 0.0;
-            for (int j = 0; j < 6; ++j) {
-                x += Kt[i + 6 * j] * (-sums[j]);
-                y += Mb[i + 6 * j] * qb[j];
-            }
-            z[3 * nb + 6 * s + i] = x - y;
-        }
+        z[3 * nb + e] = (x0 + x1) - (y0 + y1) * inrm;
     }
 }
 
@@ -583,23 +606,61 @@ __global__ void __launch_bounds__(kSBlobs) s2_precond_blobs_kernel(
     for (int e = threadIdx.x; e < 6 * W; e += kSBlobs) w[3 * nb + e] = -sh[e];
 }
 
-// Projections of this CTA's rows (ws, kSRows of them) on Q[:, 0..k): one
-// column per thread, summed over the rows in order.  P[i*nblk + blk].
+// Column sums out[i * ostride] = sum over b < count of p[i * stride + b],
+// i < k.  A column's terms go to G adjacent lanes (G the largest power of
+// two, at most 32, with k G <= kSTpb), two interleaved chains per lane, and
+// meet by shuffles, so the FP64 adds spread over every warp of the CTA
+// whatever k is.  Fixed order: deterministic.
+template <bool kCg>
+__device__ __forceinline__ void sum_columns(const double *p, size_t stride, int count, int k, double *out,
+                                            size_t ostride)
+{
+    int G = 1;
+    while (G < 32 && k * (2 * G) <= kSTpb) G *= 2;
+    const int t = threadIdx.x, g = t & (G - 1), c0 = t / G, cstep = kSTpb / G;
+    for (int cb = 0; cb < k; cb += cstep) {
+        const int i = cb + c0;
+        double a0 = 0.0, a1 = 0.0;
+        if (i < k) {
+            const double *pi = p + (size_t)i * stride;
+            int b = g;
+            for (; b + G < count; b += 2 * G) {
+                a0 += kCg ? __ldcg(pi + b) : pi[b];
+                a1 += kCg ? __ldcg(pi + b + G) : pi[b + G];
+            }
+            if (b < count) a0 += kCg ? __ldcg(pi + b) : pi[b];
+        }
+        double sum = a0 + a1;
+        for (int o = 1; o < G; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (i < k && g == 0) out[(size_t)i * ostride] = sum;
+    }
+}
+
+// Projections of this CTA's rows (ws, kSRows of them) on Q[:, 0..k) into
+// P[i*nblk + blk]: each column's rows split into G groups on adjacent lanes
+// (the largest power of two with k G <= kSTpb), so every warp takes a share.
 __device__ __forceinline__ void cta_projections(const double *__restrict__ Q, size_t ld, int row0, int rows, int k,
                                                 const double *ws, double *__restrict__ P, int nblk)
 {
-    for (int i = threadIdx.x; i < k; i += kSTpb) {
-        const double *q = Q + ld * i + row0;
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-        int r = 0;
-        for (; r + 3 < rows; r += 4) {
-            a0 += q[r] * ws[r];
-            a1 += q[r + 1] * ws[r + 1];
-            a2 += q[r + 2] * ws[r + 2];
-            a3 += q[r + 3] * ws[r + 3];
+    int G = 1;
+    while (G < kSRows && k * (2 * G) <= kSTpb) G *= 2;
+    const int per = kSRows / G, t = threadIdx.x, g = t & (G - 1), c0 = t / G, cstep = kSTpb / G;
+    const int rb = g * per, re = min(rows, rb + per);
+    for (int cb = 0; cb < k; cb += cstep) {
+        const int i = cb + c0;
+        double a0 = 0.0, a1 = 0.0;
+        if (i < k) {
+            const double *q = Q + ld * i + row0;
+            int r = rb;
+            for (; r + 1 < re; r += 2) {
+                a0 += q[r] * ws[r];
+                a1 += q[r + 1] * ws[r + 1];
+            }
+            if (r < re) a0 += q[r] * ws[r];
         }
-        for (; r < rows; ++r) a0 += q[r] * ws[r];
-        P[(size_t)i * nblk + blockIdx.x] = (a0 + a1) + (a2 + a3);
+        double sum = a0 + a1;
+        for (int o = 1; o < G; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (i < k && g == 0) P[(size_t)i * nblk + blockIdx.x] = sum;
     }
 }
 
@@ -611,42 +672,43 @@ __device__ __forceinline__ bool finish_projections(const double *P, int k, int n
     const int ngroups = (nblk + kSGroup - 1) / kSGroup, g = blockIdx.x / kSGroup;
     const int first = g * kSGroup, gsize = min(kSGroup, nblk - first);
     if (!last_cta(tickets + 1 + g, gsize)) return false;
-    for (int i = threadIdx.x; i < k; i += kSTpb) {
-        const double *p = P + (size_t)i * nblk + first;
-        double t[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-        for (int b = 0; b < kSGroup; ++b)
-            if (b < gsize) t[b & 3] += __ldcg(p + b);
-        G[(size_t)i * ngroups + g] = (t[0] + t[1]) + (t[2] + t[3]);
-    }
+    sum_columns<true>(P + first, nblk, gsize, k, G + g, ngroups);
     if (!last_cta(tickets, ngroups)) return false;
-    for (int i = threadIdx.x; i < k; i += kSTpb) {
-        const double *p = G + (size_t)i * ngroups;
-        double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
-        int b = 0;
-        for (; b + 3 < ngroups; b += 4) {
-            t0 += __ldcg(p + b);
-            t1 += __ldcg(p + b + 1);
-            t2 += __ldcg(p + b + 2);
-            t3 += __ldcg(p + b + 3);
-        }
-        for (; b < ngroups; ++b) t0 += __ldcg(p + b);
-        h[i] = (t0 + t1) + (t2 + t3);
-    }
+    sum_columns<true>(G, ngroups, ngroups, k, h, 1);
+    __syncthreads();  // h[i] is written by column i's group lane, then read by thread i
     return true;
 }
 
-// S3: blob rows of w, first CGS pass.
+// S3: blob rows of w, first CGS pass.  With splits > 1 the blob-blob pair
+// sum left per-split partials (mpart[p * 3B + r]), which this kernel adds:
+// warp q takes the splits p = q mod 4 for the CTA's 32 rows (one per lane).
 __global__ void __launch_bounds__(kSTpb) s3_finish_project_kernel(
-    int W, int nblob, const double *__restrict__ mbb, const double *__restrict__ z, const double *__restrict__ R,
-    const double *__restrict__ refs, double *__restrict__ w, const double *__restrict__ Q, size_t ld, int n,
-    double *__restrict__ P, double *__restrict__ G, int *tickets, double *__restrict__ scal,
-    double *__restrict__ H, int ldh, const GmresCtl *ctl)
+    int W, int nblob, const double *__restrict__ mbb, const double *__restrict__ mpart, int splits,
+    const double *__restrict__ z, const double *__restrict__ R, const double *__restrict__ refs,
+    double *__restrict__ w, const double *__restrict__ Q, size_t ld, int n, double *__restrict__ P,
+    double *__restrict__ G, int *tickets, double *__restrict__ scal, double *__restrict__ H, int ldh,
+    const GmresCtl *ctl)
 {
+    static_assert(kSTpb == 4 * kSRows && kSRows == 32, "S3's split sum: four warps over 32 rows");
     if (ctl->done) return;
     __shared__ double ws[kSRows];
+    __shared__ double msum[4][kSRows];
     const int k = ctl->k, row0 = blockIdx.x * kSRows, nb3 = 3 * W * nblob;
     const int rows = min(kSRows, n - row0);
+    if (splits > 1) {
+        const int lr = threadIdx.x & 31, q = threadIdx.x >> 5, r = row0 + lr;
+        double a0 = 0.0, a1 = 0.0;
+        if (r < nb3) {
+            int p = q;
+            for (; p + 4 < splits; p += 8) {
+                a0 += mpart[(size_t)p * nb3 + r];
+                a1 += mpart[(size_t)(p + 4) * nb3 + r];
+            }
+            if (p < splits) a0 += mpart[(size_t)p * nb3 + r];
+        }
+        msum[q][lr] = a0 + a1;
+        __syncthreads();
+    }
     if (threadIdx.x < kSRows) {
         const int r = row0 + threadIdx.x;
         double v = 0.0;
@@ -659,7 +721,9 @@ __global__ void __launch_bounds__(kSTpb) s3_finish_project_kernel(
             if (c == 0) kz = U[0] - d[1] * U[5] + d[2] * U[4];
             else if (c == 1) kz = U[1] - d[2] * U[3] + d[0] * U[5];
             else kz = U[2] - d[0] * U[4] + d[1] * U[3];
-            v = -kz + mbb[r];
+            const int t = threadIdx.x;
+            const double mb = splits > 1 ? (msum[0][t] + msum[1][t]) + (msum[2][t] + msum[3][t]) : mbb[r];
+            v = -kz + mb;
             w[r] = v;
         } else if (r < n) {
             v = w[r];
@@ -674,27 +738,35 @@ __global__ void __launch_bounds__(kSTpb) s3_finish_project_kernel(
     for (int i = threadIdx.x; i < k; i += kSTpb) Hcol[i] = h[i];
 }
 
-// w -= Q h on this CTA's rows (rows go to ws).
+// w -= Q h on this CTA's rows (rows go to ws): warp q takes the columns
+// i = q mod 4 (lane = row, two interleaved chains), and the four partial
+// products meet in shared memory.
 __device__ __forceinline__ void cta_update(const double *__restrict__ Q, size_t ld, int row0, int rows, int k,
                                            const double *__restrict__ h, double *__restrict__ w, double *ws)
 {
+    static_assert(kSTpb == 4 * kSRows && kSRows == 32, "cta_update: four warps over 32 rows");
     __shared__ double hs[kFMaxK];
+    __shared__ double up[4][kSRows];
     for (int i = threadIdx.x; i < k; i += kSTpb) hs[i] = h[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double p0 = 0.0, p1 = 0.0;
+    if (lane < rows) {
+        const double *q = Q + row0 + lane;
+        int i = wid;
+        for (; i + 4 < k; i += 8) {
+            p0 += hs[i] * q[ld * i];
+            p1 += hs[i + 4] * q[ld * (i + 4)];
+        }
+        if (i < k) p0 += hs[i] * q[ld * i];
+    }
+    up[wid][lane] = p0 + p1;
     __syncthreads();
     if (threadIdx.x < kSRows) {
         double v = 0.0;
         if (threadIdx.x < rows) {
             const int r = row0 + threadIdx.x;
-            double p0 = 0.0, p1 = 0.0, p2 = 0.0, p3 = 0.0;
-            int i = 0;
-            for (; i + 3 < k; i += 4) {
-                p0 += hs[i] * Q[ld * i + r];
-                p1 += hs[i + 1] * Q[ld * (i + 1) + r];
-                p2 += hs[i + 2] * Q[ld * (i + 2) + r];
-                p3 += hs[i + 3] * Q[ld * (i + 3) + r];
-            }
-            for (; i < k; ++i) p0 += hs[i] * Q[ld * i + r];
-            v = w[r] - ((p0 + p1) + (p2 + p3));
+            v = w[r] - ((up[0][lane] + up[1][lane]) + (up[2][lane] + up[3][lane]));
             w[r] = v;
         }
         ws[threadIdx.x] = v;
@@ -842,35 +914,44 @@ __global__ void arnoldi_loop_guard_kernel(GmresCtl *ctl, cudaGraphConditionalHan
 // Back substitution y = H(0:iter, 0:iter)^-1 beta(0:iter)
 // (mobility_solver.cpp:1236-1250) by one warp: column by column, the lanes
 // update the remaining right-hand side, each row in the reference's order.
+// The diagonal's reciprocals are taken up front, all lanes at once, so a
+// column's step on the serial chain is one multiply and one FMA; the row
+// blocks below the column (nothing left to update) are skipped warp-wide.
 __global__ void backsolve_warp_kernel(const double *__restrict__ H, int ldh, const double *__restrict__ beta,
                                       int iter, double *__restrict__ y)
 {
     constexpr int kPer = (kFMaxK + 31) / 32;
-    __shared__ double b[kFMaxK];
-    for (int i = threadIdx.x; i < iter; i += 32) b[i] = beta[i];
+    __shared__ double b[kFMaxK], rd[kFMaxK];
+    const int lane = threadIdx.x;
+    for (int i = lane; i < iter; i += 32) {
+        b[i] = beta[i];
+        rd[i] = 1.0 / H[i + (size_t)ldh * i];
+    }
     __syncwarp();
     // column j of H in registers (row i = lane + 32 q), the next one in flight
     double cur[kPer], nxt[kPer];
     const int j0 = iter - 1;
 #pragma unroll
     for (int q = 0; q < kPer; ++q) {
-        const int i = threadIdx.x + 32 * q;
-        cur[q] = i <= j0 ? H[i + (size_t)ldh * j0] : 0.0;
+        const int i = lane + 32 * q;
+        cur[q] = i < j0 ? H[i + (size_t)ldh * j0] : 0.0;
     }
     for (int j = j0; j >= 0; --j) {
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
-            const int i = threadIdx.x + 32 * q;
-            nxt[q] = (j > 0 && i <= j - 1) ? H[i + (size_t)ldh * (j - 1)] : 0.0;
+            const int i = lane + 32 * q;
+            nxt[q] = (i < j - 1) ? H[i + (size_t)ldh * (j - 1)] : 0.0;
         }
-        const double diag = __shfl_sync(0xffffffffu, cur[j / 32], j % 32);
-        const double yj = b[j] / diag;
+        const double yj = b[j] * rd[j];
+        const int qmax = (j - 1) >> 5;  // row blocks holding rows < j (-1 when j == 0)
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
-            const int i = threadIdx.x + 32 * q;
-            if (i < j) b[i] -= cur[q] * yj;
+            if (q <= qmax) {
+                const int i = lane + 32 * q;
+                if (i < j) b[i] -= cur[q] * yj;
+            }
         }
-        if (threadIdx.x == 0) y[j] = yj;
+        if (lane == 0) y[j] = yj;
         __syncwarp();
 #pragma unroll
         for (int q = 0; q < kPer; ++q) cur[q] = nxt[q];
@@ -944,7 +1025,7 @@ static gmi_status kt_sums(gmi_solver *s, const double *vec)
 {
     const int gx = (s->cfg.nblob + kKtBlobs - 1) / kKtBlobs;
     kt_partial_kernel<<<dim3(gx, s->W), kKtBlobs, 0, s->ctx->stream>>>(s->cfg.nblob, s->R, s->refs, vec, s->kt_part);
-    kt_finish_kernel<<<grid_for(6 * s->W, 64), 64, 0, s->ctx->stream>>>(s->W, gx, s->kt_part, s->sums);
+    kt_finish_kernel<<<grid_for(32 * s->W, 128), 128, 0, s->ctx->stream>>>(s->W, gx, s->kt_part, s->sums);
     return launched(s, 2);
 }
 
@@ -1055,9 +1136,11 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     env.skip = &s->ctl->done;
     PairConsts k;
     fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
+    int splits = 1;
+    env.splits_out = &splits;  // S3 adds the split partials
     GMI_TRY(launch_pair_into(env, kBB, f64, s->gm_rec, 0, nb, s->gm_rec, nb, k, s->mbb, 0));
-    s3_finish_project_kernel<<<L.nblk, kSTpb, 0, st>>>(W, nblob, s->mbb, s->z, s->R, s->refs, s->w, s->Q, ld, n, P,
-                                                       G, tk3, s->st_scal, s->H, ldh, s->ctl);
+    s3_finish_project_kernel<<<L.nblk, kSTpb, 0, st>>>(W, nblob, s->mbb, s->gm_partial, splits, s->z, s->R, s->refs,
+                                                       s->w, s->Q, ld, n, P, G, tk3, s->st_scal, s->H, ldh, s->ctl);
     s4_update_project_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, G, tk4, s->st_scal, s->H, ldh, s->ctl);
     s5_update_norm_givens_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, tk5, s->st_scal, s->H, ldh,
                                                            s->beta, s->cs, s->sn, s->ctl);

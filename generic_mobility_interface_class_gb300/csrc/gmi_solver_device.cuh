@@ -13,6 +13,35 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
+// Warp sums of six values per lane by recursive halving: each level swaps
+// half of the remaining values with the partner lane and adds the other
+// half, so the six totals cost 9 FP64 adds per lane instead of the 30 of six
+// shuffle trees (a warp FP64 instruction costs the same on one lane as on
+// 32).  Lanes 4c .. 4c+3 return the total of value c (c < 6); lanes 24..31
+// return the zero padding's.
+__device__ __forceinline__ double warp_sum6_scatter(const double v[6])
+{
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool h16 = (lane & 16) != 0, h8 = (lane & 8) != 0, h4 = (lane & 4) != 0;
+    const double a[8] = {v[0], v[1], v[2], v[3], v[4], v[5], 0.0, 0.0};
+    double b[4], c[2];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const double keep = h16 ? a[j + 4] : a[j], send = h16 ? a[j] : a[j + 4];
+        b[j] = keep + __shfl_xor_sync(full, send, 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const double keep = h8 ? b[j + 2] : b[j], send = h8 ? b[j] : b[j + 2];
+        c[j] = keep + __shfl_xor_sync(full, send, 8);
+    }
+    double d = (h4 ? c[1] : c[0]) + __shfl_xor_sync(full, h4 ? c[0] : c[1], 4);
+    d += __shfl_xor_sync(full, d, 2);
+    d += __shfl_xor_sync(full, d, 1);
+    return d;
+}
+
 // o = R v, R row-major 3x3
 __device__ __forceinline__ void rot_apply(const double *R, const double *v, double *o)
 {

@@ -60,23 +60,27 @@ def run_against_golden(case, state_tol, vel_tol, precision=0, doubling_steps=Non
 
 
 def test_jacobian_inverse_paths_agree(gmi_lib, monkeypatch):
-    """The filament Jacobians inverted with one CTA each (GMI_GJ_CLUSTER=0)
-    and spread over thread-block clusters (the default for few filaments)
-    perform the same arithmetic: three steps of the 4-filament swimmer give
-    the same state."""
+    """The filament Jacobians inverted with one CTA each (GMI_GJ_CLUSTER=0),
+    spread over thread-block clusters (the default for few filaments), and
+    with the columns stepped through shared memory instead of registers
+    (GMI_GJ_REGISTERS=0) perform the same arithmetic: three steps of the
+    4-filament swimmer give the same state."""
     from generic_mobility_interface_class_gb300.sim import Simulation
     g = load_golden("small_swimmer", prefix="sim_")
     out = {}
-    for mode in ("0", "1"):
-        monkeypatch.setenv("GMI_GJ_CLUSTER", mode)
+    for mode, (cluster, registers) in {"one-cta": ("0", "1"), "cluster": ("1", "1"),
+                                       "one-cta-shared": ("0", "0"), "cluster-shared": ("1", "0")}.items():
+        monkeypatch.setenv("GMI_GJ_CLUSTER", cluster)
+        monkeypatch.setenv("GMI_GJ_REGISTERS", registers)
         sim = Simulation.from_golden(g, precision=0)
         sim.prepare()
         iters = [sim.step(nt)[0] for nt in range(3)]
         out[mode] = (iters, sim.state("seg_q").copy(), sim.state("seg_v").copy())
         sim.close()
-    assert out["0"][0] == out["1"][0]
-    assert rel_err(out["1"][1].ravel(), out["0"][1].ravel()) < 1e-13
-    assert rel_err(out["1"][2].ravel(), out["0"][2].ravel()) < 1e-9
+    for mode in ("cluster", "one-cta-shared", "cluster-shared"):
+        assert out[mode][0] == out["one-cta"][0], mode
+        assert rel_err(out[mode][1].ravel(), out["one-cta"][1].ravel()) < 1e-13, mode
+        assert rel_err(out[mode][2].ravel(), out["one-cta"][2].ravel()) < 1e-9, mode
 
 
 def test_trajectory_matches_reference(gmi_lib):

@@ -241,3 +241,25 @@ def test_solver_rejects_bad_config(gmi_lib):
     with pytest.raises(GmiError):
         s.compute_velocities()  # blob references never set
     s.close()
+
+
+def test_multikernel_fp32c_solve_is_deterministic(gmi_lib, monkeypatch):
+    """The multi-kernel Arnoldi step finishes every cross-CTA sum in a fixed
+    order, so the same solve run twice gives the same iteration counts and
+    bit-identical answers.  2562 blobs: 241 row blocks (16 two-level groups),
+    a split blob-blob sum, and Krylov bases long enough for every lane
+    layout of the projections."""
+    monkeypatch.setenv("GMI_GMRES_CLUSTER", "0")
+    nfil, nseg = 4, 10
+    refs, bx, bq, xs, fs, bf = swimmer_geometry(1, nfil, nseg, subdiv=4, R=30.0)
+    runs = []
+    for _ in range(2):
+        s = make_solver(refs, 1, nfil, nseg, precision=1)
+        s.x_segs_host[:] = xs
+        s.f_segs_host[:] = fs
+        iters = [s.compute_velocities(bx, bq, bf)[0] for _ in range(2)]
+        runs.append((iters, s.f_blobs_host.copy(), s.v_bodies().copy(), s.v_segs_host.copy()))
+        s.close()
+    assert runs[0][0] == runs[1][0]
+    for a, b in zip(runs[0][1:], runs[1][1:]):
+        assert np.array_equal(a, b)
