@@ -17,6 +17,7 @@ HEADER = os.path.join(ROOT, "include", "gmi.h")
 GMI_OK = 0
 GMI_FP64 = 0
 GMI_FP32C = 1
+GMI_DF64 = 2  # blob-blob sums only
 STATUS_NAMES = {0: "GMI_OK", 1: "GMI_ERR_ARG", 2: "GMI_ERR_CUDA", 3: "GMI_ERR_DEVICE_TIMEOUT",
                 4: "GMI_ERR_NONFINITE", 5: "GMI_ERR_NOT_CONVERGED", 6: "GMI_ERR_STATE"}
 

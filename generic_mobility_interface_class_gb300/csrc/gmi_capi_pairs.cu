@@ -87,7 +87,8 @@ gmi_status gmi_context_set_stream(gmi_context *ctx, void *cuda_stream)
 gmi_status gmi_context_set_precision(gmi_context *ctx, int precision)
 {
     GMI_ARG_CHECK(ctx != nullptr, "null context");
-    GMI_ARG_CHECK(precision == GMI_FP64 || precision == GMI_FP32C, "precision must be GMI_FP64 or GMI_FP32C");
+    GMI_ARG_CHECK(precision == GMI_FP64 || precision == GMI_FP32C || precision == GMI_DF64,
+                  "precision must be GMI_FP64, GMI_FP32C or GMI_DF64");
     ctx->precision = precision;
     return GMI_OK;
 }

@@ -23,6 +23,7 @@
 #include "gmi_context.hpp"
 #include "gmi_pairs.cuh"
 #include "gmi_pairs2.cuh"
+#include "gmi_df.cuh"
 #include "gmi_pair_kernels.hpp"
 
 namespace gmi {
@@ -57,6 +58,29 @@ __global__ void pack_records_f32(const double *__restrict__ x, const double *__r
     r[0] = make_float4(hx, hy, hz, f0);
     r[1] = make_float4(lx, ly, lz, f1);
     r[2] = make_float4(f2, t0, t1, t2);
+}
+
+// Double-float records (precision GMI_DF64, blob forces only):
+// [xh yh zh fxh][xl yl zl fyh][fzh fxl fyl fzl], every value an FP32
+// (hi, lo) pair.  Positions are taken relative to the first blob (in FP64),
+// so their 48 bits resolve the cloud, not its distance from the origin.
+__global__ void pack_records_df(const double *__restrict__ x, const double *__restrict__ f, int n,
+                                float4 *__restrict__ rec)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const df2 px = df_from_double(x[3 * i] - x[0]), py = df_from_double(x[3 * i + 1] - x[1]),
+              pz = df_from_double(x[3 * i + 2] - x[2]);
+    df2 f0 = df2{0.f, 0.f}, f1 = f0, f2 = f0;
+    if (f != nullptr) {
+        f0 = df_from_double(f[3 * i]);
+        f1 = df_from_double(f[3 * i + 1]);
+        f2 = df_from_double(f[3 * i + 2]);
+    }
+    float4 *r = rec + 3 * (size_t)i;
+    r[0] = make_float4(px.h, py.h, pz.h, f0.h);
+    r[1] = make_float4(px.l, py.l, pz.l, f1.h);
+    r[2] = make_float4(f2.h, f0.l, f1.l, f2.l);
 }
 
 __global__ void pack_records_f64(const double *__restrict__ x, const double *__restrict__ f, int nf, int n,
@@ -311,6 +335,137 @@ __global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ C
 #pragma unroll
             for (int c = 0; c < NOUT; ++c) o[c] = args.accumulate ? o[c] + acc[k].total(c) : acc[k].total(c);
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2''. double-float blob-blob sum (precision GMI_DF64): the FP64 operator's
+// accuracy (about 1e-13 per pair) on the FP32 pipe, for the residuals of the
+// mixed-precision refinement.  The scalar kernel's TMA ring on the records
+// of pack_records_df; per target three double-float accumulators; the pair
+// formulas of pair_bb (cuda_functions.cu:429-539) step by step in
+// double-float.
+// ---------------------------------------------------------------------------
+struct DfBBConsts {
+    df2 four_a2, two_a2, f8pm, f6pma, q32, third;
+};
+
+// a - b for double-float positions
+__device__ __forceinline__ df2 df_diff(df2 a, df2 b)
+{
+    const df2 s = df_two_sum(a.h, -b.h);
+    return df_fast_two_sum(s.h, __fadd_rn(s.l, __fsub_rn(a.l, b.l)));
+}
+
+__device__ __forceinline__ void pair_bb_df(const df2 *d, const df2 *F, const DfBBConsts &K, df2 *v)
+{
+    const df2 r2 = df_add(df_add(df_sqr(d[0]), df_sqr(d[1])), df_sqr(d[2]));
+    const df2 dF = df_add(df_add(df_mul(d[0], F[0]), df_mul(d[1], F[1])), df_mul(d[2], F[2]));
+    df2 At, Bt;
+    if (r2.h == 0.0f) {  // coincident blobs (the self term): the near-field limit r -> 0
+        At = K.f6pma;
+        Bt = df_make(0.0f);
+    } else {
+        const df2 ir = df_rsqrt(r2);
+        const df2 ir2 = df_sqr(ir);
+        if (r2.h > K.four_a2.h || (r2.h == K.four_a2.h && r2.l > K.four_a2.l)) {
+            const df2 s = df_mul(K.two_a2, ir2);
+            const df2 ik = df_mul(ir, K.f8pm);
+            At = df_mul(ik, df_add(df_make(1.0f), df_mul(s, K.third)));
+            const df2 c3dF = df_mul(df_mul(ik, ir2), dF);
+            Bt = df_sub(c3dF, df_mul(s, c3dF));
+        } else {
+            const df2 q = df_mul(df_mul(r2, ir), K.q32);
+            At = df_mul(df_sub(df_make(1.0f), df_mul_f(q, 3.0f)), K.f6pma);
+            Bt = df_mul(df_mul(df_mul(q, K.f6pma), ir2), dF);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] = df_add(v[c], df_add(df_mul(At, F[c]), df_mul(Bt, d[c])));
+}
+
+template <int TPB>
+__global__ void __launch_bounds__(TPB) rpy_bb_df_kernel(const __grid_constant__ CUtensorMap src_map,
+                                                        const PairLaunch args, const DfBBConsts K)
+{
+    constexpr int kStageScalars = kTile * kRecLen;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    float *ring = reinterpret_cast<float *>(smem_raw);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + kStages * kStageScalars * sizeof(float));
+
+    if (args.skip != nullptr && *args.skip != 0) return;
+    const int tid = threadIdx.x;
+    const int j_begin = blockIdx.y * args.chunk;
+    const int j_end = min(j_begin + args.chunk, args.n_src);
+    const int ntiles = j_end > j_begin ? (j_end - j_begin + kTile - 1) / kTile : 0;
+    constexpr unsigned kBoxBytes = kStageScalars * sizeof(float);
+
+    if (tid == 0) {
+        prefetch_tensormap(&src_map);
+#pragma unroll
+        for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    int issued = 0;  // tiles requested so far (meaningful on thread 0)
+    if (tid == 0) {
+        for (; issued < kStages && issued < ntiles; ++issued) {
+            mbar_arrive_expect_tx(&bars[issued], kBoxBytes);
+            tma_load_2d(ring + issued * kStageScalars, &src_map, 0, j_begin + issued * kTile, &bars[issued]);
+        }
+    }
+
+    const int ti = blockIdx.x * TPB + tid;
+    const float4 *tr = reinterpret_cast<const float4 *>(args.tgt_rec) +
+                       3 * (size_t)(args.tgt_start + min(ti, args.n_tgt - 1));
+    const float4 t0 = tr[0], t1 = tr[1];
+    const df2 xi[3] = {df2{t0.x, t1.x}, df2{t0.y, t1.y}, df2{t0.z, t1.z}};
+    df2 v[3] = {df2{0.f, 0.f}, df2{0.f, 0.f}, df2{0.f, 0.f}};
+
+    bool timed_out = false;
+    int t = 0;
+    for (; t < ntiles; ++t) {
+        const int s = t % kStages;
+        const bool ok = mbar_wait_bounded(&bars[s], (t / kStages) & 1);
+        if (__syncthreads_or(!ok)) {
+            timed_out = true;
+            break;
+        }
+        // Every thread has finished tile t-1: its stage can be refilled.
+        if (tid == 0 && t >= 1 && issued < ntiles) {
+            const int sp = (t - 1) % kStages;
+            mbar_arrive_expect_tx(&bars[sp], kBoxBytes);
+            tma_load_2d(ring + sp * kStageScalars, &src_map, 0, j_begin + issued * kTile, &bars[sp]);
+            ++issued;
+        }
+        const float4 *tile = reinterpret_cast<const float4 *>(ring + s * kStageScalars);
+        const int jn = min(kTile, j_end - (j_begin + t * kTile));
+#pragma unroll 2
+        for (int jj = 0; jj < jn; ++jj) {
+            const float4 b0 = tile[3 * jj], b1 = tile[3 * jj + 1], b2 = tile[3 * jj + 2];
+            const df2 d[3] = {df_diff(xi[0], df2{b0.x, b1.x}), df_diff(xi[1], df2{b0.y, b1.y}),
+                              df_diff(xi[2], df2{b0.z, b1.z})};
+            const df2 F[3] = {df2{b0.w, b2.y}, df2{b1.w, b2.z}, df2{b2.x, b2.w}};
+            pair_bb_df(d, F, K, v);
+        }
+    }
+
+    if (timed_out) {
+        if (tid == 0) {
+            atomicOr(args.err, kDevErrWaitTimeout);
+            for (int u = t; u < issued; ++u) (void)mbar_wait_bounded(&bars[u % kStages], (u / kStages) & 1);
+        }
+        return;
+    }
+    if (ti >= args.n_tgt) return;
+    if (args.partial != nullptr) {
+        double *p = args.partial + ((size_t)blockIdx.y * args.n_tgt + ti) * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) p[c] = df_to_double(v[c]);
+    } else {
+        double *o = args.out + (size_t)ti * 3;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[c] = args.accumulate ? o[c] + df_to_double(v[c]) : df_to_double(v[c]);
     }
 }
 
@@ -800,6 +955,19 @@ void fill_consts(PairConsts &c, double a_eq, double as, double ab, double mu)
 
 gmi_status pack_records(gmi_context *ctx, const double *x, const double *f, int nf, int n, DeviceBuffer &buf)
 {
+    if (ctx->precision == GMI_DF64) {
+        if (nf != 3) {
+            set_last_error_msg("double-float pair sums exist for the blob-blob sum only");
+            return GMI_ERR_ARG;
+        }
+        gmi_status st = buf.reserve(n > 0 ? (size_t)n * kRecLen * sizeof(float) : 16);
+        if (st != GMI_OK) return st;
+        if (n == 0) return GMI_OK;
+        pack_records_df<<<(n + 255) / 256, 256, 0, ctx->stream>>>(x, f, n, static_cast<float4 *>(buf.ptr));
+        ctx->launches++;
+        GMI_CUDA_TRY(cudaGetLastError());
+        return GMI_OK;
+    }
     const bool f64 = ctx->precision == GMI_FP64;
     const size_t bytes = (size_t)n * kRecLen * (f64 ? sizeof(double) : sizeof(float));
     gmi_status st = buf.reserve(bytes > 0 ? bytes : 16);
@@ -985,10 +1153,80 @@ static int choose_splits(const gmi_context *ctx, int n_tgt_ctas, int n_src, int 
     return s < max_splits ? s : max_splits;
 }
 
+// The double-float blob-blob sum: 128 targets per CTA, the sources split
+// over enough CTAs for two waves, the splits added in order.
+constexpr int kDfTpb = 128;
+static gmi_status launch_bb_df(gmi_context *ctx, const void *tgt_rec, int tgt_start, int n_tgt, const void *src_rec,
+                               int n_src, const PairConsts &k, double *out, int accumulate)
+{
+    void *fn = reinterpret_cast<void *>(&rpy_bb_df_kernel<kDfTpb>);
+    const size_t smem = ring_bytes(false, false);
+    GMI_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kDfTpb, smem));
+    const int n_tgt_ctas = (n_tgt + kDfTpb - 1) / kDfTpb;
+    const int slots = ctx->sm_count * (occ > 0 ? occ : 1);
+    int splits = 1;
+    if (n_tgt_ctas < 2 * slots) splits = (2 * slots + n_tgt_ctas - 1) / n_tgt_ctas;
+    const int max_by_src = (n_src + kTile - 1) / kTile;
+    if (splits > max_by_src) splits = max_by_src;
+    int chunk = (n_src + splits - 1) / splits;
+    chunk = (chunk + kTile - 1) / kTile * kTile;
+    splits = (n_src + chunk - 1) / chunk;
+    PairLaunch a{};
+    a.tgt_rec = tgt_rec;
+    a.tgt_start = tgt_start;
+    a.n_tgt = n_tgt;
+    a.n_src = n_src;
+    a.chunk = chunk;
+    a.k = k;
+    a.out = out;
+    a.accumulate = accumulate;
+    a.err = ctx->d_err;
+    a.partial = nullptr;
+    if (splits > 1) {
+        gmi_status st = ctx->partial.reserve((size_t)splits * n_tgt * 3 * sizeof(double));
+        if (st != GMI_OK) return st;
+        a.partial = static_cast<double *>(ctx->partial.ptr);
+    }
+    DfBBConsts K;
+    K.four_a2 = df_from_double(k.eq[0]);
+    K.two_a2 = df_from_double(k.eq[1]);
+    K.f8pm = df_from_double(k.eq[2]);
+    K.f6pma = df_from_double(k.eq[3]);
+    K.q32 = df_from_double(k.eq[4]);
+    K.third = df_from_double(1.0 / 3.0);
+    CUtensorMap map;
+    gmi_status st = make_record_map(ctx, &map, src_rec, n_src, false);
+    if (st != GMI_OK) return st;
+    void *params[] = {&map, &a, &K};
+    GMI_CUDA_TRY(cudaLaunchKernel(fn, dim3(n_tgt_ctas, splits), dim3(kDfTpb), params, smem, ctx->stream));
+    ctx->launches++;
+    if (splits > 1) {
+        const int count = n_tgt * 3;
+        reduce_splits<<<(count + 255) / 256, 256, 0, ctx->stream>>>(a.partial, splits, count, out, accumulate,
+                                                                    nullptr);
+        ctx->launches++;
+        GMI_CUDA_TRY(cudaGetLastError());
+    }
+    return GMI_OK;
+}
+
 gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_start, int n_tgt, const void *src_rec,
                        int n_src, const PairConsts &k, double *out, int accumulate, const PairShape *force_shape)
 {
     if (n_tgt <= 0) return GMI_OK;
+    if (ctx->precision == GMI_DF64) {
+        if (kind != kBB) {
+            set_last_error_msg("double-float pair sums exist for the blob-blob sum only");
+            return GMI_ERR_ARG;
+        }
+        if (n_src <= 0) {
+            if (!accumulate) GMI_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)n_tgt * 3 * sizeof(double), ctx->stream));
+            return GMI_OK;
+        }
+        return launch_bb_df(ctx, tgt_rec, tgt_start, n_tgt, src_rec, n_src, k, out, accumulate);
+    }
     const bool f64 = ctx->precision == GMI_FP64;
     const int nout = nout_of(kind);
     if (n_src <= 0) {

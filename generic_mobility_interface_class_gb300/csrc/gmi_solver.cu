@@ -1382,7 +1382,8 @@ static gmi_status store_solution(gmi_solver *s)
 //
 // FP64 context: the reference algorithm as is.
 // FP32C context: mixed-precision iterative refinement.  The residual
-// b - A x is formed with the FP64 operator; each correction solves
+// b - A x is formed with the FP64-grade operator (the blob-blob sum in
+// double-float arithmetic, the body terms in FP64); each correction solves
 // A d = r by GMRES with the FP32C operator (FP64 Arnoldi, Givens and
 // vectors) to the relative tolerance that would meet the target in one pass
 // (with a 0.3 margin for the FP32C operator's own error), but not below
@@ -1431,7 +1432,10 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
     GMI_CUDA_TRY(cudaMemcpyAsync(s->b64, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
     int total = 0;
     gmi_status status = GMI_OK;
-    s->ctx->precision = GMI_FP64;
+    // the blob-blob sum of this residual in double-float (FP64-grade, on the
+    // FP32 pipe); GMI_REFINE_DF=0 takes the FP64 kernel instead
+    const char *df_env = std::getenv("GMI_REFINE_DF");
+    s->ctx->precision = (df_env && df_env[0] == '0') ? GMI_FP64 : GMI_DF64;
     status = system_matrix_mult(s, s->soln, s->tmp);
     s->ctx->precision = prec;
     if (status != GMI_OK) return status;

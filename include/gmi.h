@@ -9,7 +9,9 @@
  *
  * Precision: GMI_FP64 evaluates the pair sums in FP64 like the reference;
  * GMI_FP32C evaluates them in FP32 with double-float source positions and
- * compensated (two-sum) accumulation, and returns FP64 results.
+ * compensated (two-sum) accumulation, and returns FP64 results; GMI_DF64
+ * (blob-blob only) carries every step of the pair formula as a double-float
+ * (hi, lo) FP32 pair, FP64-grade accuracy on the FP32 pipe.
  */
 #ifndef GMI_H
 #define GMI_H
@@ -36,7 +38,9 @@ typedef enum gmi_status {
 
 typedef enum gmi_precision {
     GMI_FP64 = 0,  /* reference arithmetic */
-    GMI_FP32C = 1  /* FP32 pair math, compensated accumulation, FP64 I/O */
+    GMI_FP32C = 1, /* FP32 pair math, compensated accumulation, FP64 I/O */
+    GMI_DF64 = 2   /* double-float (FP32 hi/lo pairs) pair math, ~1e-13, FP64 I/O;
+                      gmi_Mbb_mult only (other pair sums return GMI_ERR_ARG) */
 } gmi_precision;
 
 /* Message describing the last failure on the calling thread ("" if none). */

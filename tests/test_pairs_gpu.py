@@ -15,6 +15,7 @@ torch = pytest.importorskip("torch")
 
 FP64_TOL = 1e-10      # spec bound for the FP64 path
 FP32C_TOL = 2e-6      # max |v - v64| / max |v64| for the compensated FP32 path
+DF64_TOL = 1e-12      # the same for the double-float blob-blob sum
 FREE = [c for c in golden_cases() if not c.startswith("wall")]
 WALL = [c for c in golden_cases() if c.startswith("wall")]
 
@@ -223,3 +224,26 @@ def test_fp32c_is_translation_robust(gpu_ctx, oracle_built):
     got = N(gpu_ctx.mss(T(xs), T(g["fs"])))
     gpu_ctx.set_precision(0)
     assert rel_err(got, want) < FP32C_TOL
+
+
+@pytest.mark.parametrize("n", [3001, 5003])
+def test_double_float_blob_blob_against_oracle(own_ctx, oracle_built, n):
+    """GMI_DF64: the blob-blob sum in double-float arithmetic against the
+    FP64 oracle (near and far pairs, the self term, several tiles and source
+    splits), also with the cloud far from the origin, a target slice, and
+    accumulation; the other pair sums refuse the precision."""
+    from generic_mobility_interface_class_gb300 import GmiError, seeding
+    rpy = oracle_built
+    x = seeding.random_cube(n, seed=7)
+    f = np.random.default_rng(7).normal(size=(n, 3))
+    own_ctx.set_precision(2)
+    for shift in (np.zeros(3), np.array([1.0e3, -2.5e3, 3.3e2])):
+        xs = x + shift
+        want = rpy.mbb(xs, f)
+        assert rel_err(N(own_ctx.mbb(T(xs), T(f))), want) < DF64_TOL
+    want = rpy.mbb(x, f)
+    got = N(own_ctx.mbb(T(x), T(f), start=100, num=700))
+    assert rel_err(got, want[100:800]) < DF64_TOL
+    with pytest.raises(GmiError):
+        own_ctx.mss(T(x), T(np.zeros((n, 6))))
+    own_ctx.synchronize()
