@@ -13,7 +13,7 @@
 // and a fixed shuffle tree, so all CTAs hold bit-identical copies of h,
 // ||w|| and the Givens state and take the same stop decision.
 //
-// Per Arnoldi iteration k (phases of the multi-kernel step S1..S5):
+// Per Arnoldi iteration k (the phases of the multi-kernel step):
 //   A  q = w / ||w|| into Q[:, k-1]; body moments of q  -> barrier 1
 //      z_body from the summed moments (every CTA)
 //   B  blob block of the preconditioner; the CTA's blob loads (z, FP32,
@@ -26,8 +26,9 @@
 //      Q[:, k-1], a column past the solution)
 //      w_blob = M_bb z - K z_body
 //   D  first classical Gram-Schmidt projections  -> barrier 3, h
-//   E  w -= Q h; second projections  -> barrier 4, h2
-//   F  w -= Q h2; ||w||^2  -> barrier 5; ||w||
+//   E  w -= Q h; second projections and ||w||^2  -> barrier 4, h2
+//   F  w -= Q h2 on the CTA's rows; ||w - Q h2||^2 = ||w||^2 - ||h2||^2
+//      (no barrier)
 // All arithmetic except the pair sum is FP64, as in the multi-kernel step.
 #include <cooperative_groups.h>
 
@@ -96,10 +97,10 @@ __host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc, int kqs = 
     L.mom2 = take(6 * (size_t)W * sizeof(double));
     L.sums = take(6 * (size_t)W * sizeof(double));
     L.zb = take(6 * (size_t)W * sizeof(double));
-    L.hp1 = take(kCgMaxK * sizeof(double));
-    L.hp2 = take(kCgMaxK * sizeof(double));
-    L.h = take(kCgMaxK * sizeof(double));
-    L.h2 = take(kCgMaxK * sizeof(double));
+    L.hp1 = take((kCgMaxK + 1) * sizeof(double));
+    L.hp2 = take((kCgMaxK + 1) * sizeof(double));
+    L.h = take((kCgMaxK + 1) * sizeof(double));
+    L.h2 = take((kCgMaxK + 1) * sizeof(double));
     L.np = take(4 * sizeof(double));
     L.pp = take((size_t)kCgTpb * 3 * sizeof(double));
     L.csh = take(kCgMaxK * sizeof(double));
@@ -461,7 +462,6 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
         }
         __syncthreads();
         // ---- D..F: CGS2 and ||w|| ------------------------------------------
-        double part = 0.0;  // ||w||^2 of the thread's rows after the second pass
         for (int pass = 0; pass < 2; ++pass) {
             double *hp = pass == 0 ? hp1 : hp2, *hs = pass == 0 ? h : h2;
             // items (column i, row group g), PG groups per column on adjacent
@@ -493,8 +493,14 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
                 for (int o = PG >> 1; o > 0; o >>= 1) sg += __shfl_xor_sync(0xffffffffu, sg, o);
                 if (i < k && g == 0) hp[i] = sg;
             }
+            if (pass == 1) {  // ||w||^2 of the CTA's rows rides along as entry k
+                double v2 = 0.0;
+                for (int lr = tid; lr < nr; lr += kCgTpb) v2 += wl[lr] * wl[lr];
+                v2 = cg_block_sum(v2, red, nr);
+                if (tid == 0) hp2[k] = v2;
+            }
             cl.sync();  // barriers 3 and 4
-            cluster_reduce(cl, hp, k, hs, C, G);
+            cluster_reduce(cl, hp, pass == 0 ? k : k + 1, hs, C, G);
             __syncthreads();
             for (int lr = tid; lr < nr; lr += kCgTpb) {
                 const int row = row_of(lr);
@@ -511,20 +517,23 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
                 }
                 for (; i < kc; ++i) p0 += hs[i] * qr[i];
                 for (; i < k; ++i) p0 += hs[i] * a.Q[a.ld * (size_t)i + row];
-                const double v = wl[lr] - ((p0 + p1) + (p2 + p3));
-                wl[lr] = v;
-                if (pass == 1) part += v * v;
+                wl[lr] -= (p0 + p1) + (p2 + p3);
             }
             __syncthreads();
         }
-        part = cg_block_sum(part, red, nr);
-        if (tid == 0) np[0] = part;
-        cl.sync();  // barrier 5
-        cluster_reduce(cl, np, 1, np + 1, C, G);
-        if (tid == 0) {
-            const double ir = rsqrt(np[1]);
-            np[2] = np[1] * ir;  // ||w||
-            np[3] = ir;          // 1 / ||w||
+        // ||w - Q h2||^2 = ||w||^2 - ||h2||^2 (Q orthonormal; h2 is the second
+        // pass's small correction, so nothing cancels), from the same
+        // cluster sum as h2: every CTA computes the same bits
+        if (tid < 32) {
+            double t = 0.0;
+            for (int i = tid; i < k; i += 32) t += h2[i] * h2[i];
+            t = warp_sum(t);
+            if (tid == 0) {
+                np[1] = fmax(h2[k] - t, 0.0);
+                const double ir = rsqrt(np[1]);
+                np[2] = np[1] * ir;  // ||w||
+                np[3] = ir;          // 1 / ||w||
+            }
         }
         __syncthreads();
     }

@@ -410,18 +410,19 @@ __global__ void scale_kernel(int n, const double *__restrict__ x, const double *
 // (an atomic ticket; nobody waits), in a fixed order, so results are
 // deterministic.  Projections use two levels: the last CTA of each group of
 // kSGroup CTAs sums the group, the last group finisher sums the groups.
-//   S1 (CTA per 64 blobs)   q_{k-1} = w / ||w|| into Q; body moments;
+//   S1 (CTA per 32 blobs)   w -= Q h2 (the previous S4's second pass);
+//                            q_{k-1} = w / ||w|| into Q; body moments;
 //                            last CTA: body rows of q and z_body = U
 //   S2 (CTA per 64 blobs)   z_blob; records of z; last CTA: w_body = -K^T z
 //   pair kernel on the records -> mbb, or per-split partials
 //   S3 (CTA per kSRows rows) w_blob = M_bb z - K z_body (adding the split
-//                            partials); Q^T w; last: h, H col
-//   S4 (CTA per kSRows rows) w -= Q h; Q^T w; last: h, H col +=
-//   S5 (CTA per kSRows rows) w -= Q h; ||w||^2; last: H(k, k-1), Givens, ctl
+//                            partials); h1 = Q^T w; last: H col = h1
+//   S4 (CTA per kSRows rows) w -= Q h1; h2 = Q^T w and ||w||^2; last: H col
+//                            += h2, ||w - Q h2|| by Pythagoras, Givens, ctl
 // ---------------------------------------------------------------------------
-constexpr int kSBlobs = 64;   // blobs (threads) per CTA in S1, S2
-constexpr int kSRows = 32;    // rows per CTA in S3-S5
-constexpr int kSTpb = 128;    // threads per CTA in S3-S5
+constexpr int kSBlobs = 64;   // blobs (threads) per CTA in S2
+constexpr int kSRows = 32;    // rows per CTA in S3, S4
+constexpr int kSTpb = 128;    // threads per CTA in S3, S4
 constexpr int kSGroup = 16;   // CTAs per first-level group of the projection sums
 constexpr int kFMaxK = 160;   // >= max_iter + 1
 // layout of the step's scalar workspace (doubles)
@@ -511,24 +512,64 @@ __device__ __forceinline__ void swimmer_sums(const double *part, int W, int gx, 
     __syncthreads();
 }
 
-// S1: grid (ceil(nblob/kSBlobs), W).
-__global__ void __launch_bounds__(kSBlobs) s1_normalise_moments_kernel(
-    int W, int nblob, double *__restrict__ Q, size_t ld, const double *__restrict__ w,
+// S1: grid (ceil(nblob/kS1Blobs), W), kS1Tpb threads.  First the second
+// CGS pass's update that the previous S4 left pending, w -= Q[:, 0..k-1) h2
+// (h2 still in h): lane = blob, warp q takes the columns i = q mod 4, and
+// the CTAs with the lowest linear indices also update the body rows, 32
+// each.  Then q_{k-1} = w / ||w|| into Q and the body moments of q; the
+// last CTA adds the moments per swimmer and forms the body rows of q and
+// z_body.
+constexpr int kS1Blobs = 32;
+constexpr int kS1Tpb = 128;
+__global__ void __launch_bounds__(kS1Tpb) s1_update_normalise_moments_kernel(
+    int W, int nblob, double *__restrict__ Q, size_t ld, double *__restrict__ w,
     const double *__restrict__ R, const double *__restrict__ refs, const double *__restrict__ ktk_rot,
     const double *__restrict__ mob_rot, double *__restrict__ z, double *__restrict__ part,
     const double *__restrict__ scal, int *ticket, const GmresCtl *ctl)
 {
+    static_assert(kS1Tpb == 4 * 32 && kS1Blobs == 32, "S1: four warps over 32 blobs");
     if (ctl->done) return;
-    const int n = blockIdx.y, m = blockIdx.x * kSBlobs + threadIdx.x, nb = W * nblob;
-    double *q = Q + ld * (size_t)(ctl->k - 1);
+    __shared__ double hs[kFMaxK];
+    __shared__ double up[4][3 * kS1Blobs];
+    __shared__ double upb[4][32];
+    const int n = blockIdx.y, lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nb = W * nblob;
+    const int m = blockIdx.x * kS1Blobs + lane;
+    const int kq = ctl->k, cnt = kq - 1;  // the pending update spans Q[:, 0..cnt)
+    double *q = Q + ld * (size_t)(kq - 1);
     const double nrm = scal[kNormOff], inrm = 1.0 / nrm;
+    for (int i = threadIdx.x; i < cnt; i += kS1Tpb) hs[i] = scal[kHOff + i];
+    __syncthreads();
+    const size_t row = 3 * ((size_t)n * nblob + m);
+    double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+    if (m < nblob)
+        for (int i = wid; i < cnt; i += 4) {
+            const double *qi = Q + ld * i + row;
+            p0 += hs[i] * qi[0];
+            p1 += hs[i] * qi[1];
+            p2 += hs[i] * qi[2];
+        }
+    up[wid][3 * lane] = p0;
+    up[wid][3 * lane + 1] = p1;
+    up[wid][3 * lane + 2] = p2;
+    const int lin = blockIdx.y * gridDim.x + blockIdx.x, br = 32 * lin + lane;
+    const bool body_cta = 32 * lin < 6 * W;
+    if (body_cta) {
+        double pb = 0.0;
+        if (br < 6 * W)
+            for (int i = wid; i < cnt; i += 4) pb += hs[i] * Q[ld * i + 3 * (size_t)nb + br];
+        upb[wid][lane] = pb;
+    }
+    __syncthreads();
+    if (body_cta && wid == 0 && br < 6 * W)
+        w[3 * (size_t)nb + br] -= (upb[0][lane] + upb[1][lane]) + (upb[2][lane] + upb[3][lane]);
     double a[6] = {0, 0, 0, 0, 0, 0};
-    if (m < nblob) {
-        const size_t i = (size_t)n * nblob + m;
+    if (wid == 0 && m < nblob) {
         double f[3];
+#pragma unroll
         for (int c = 0; c < 3; ++c) {
-            f[c] = w[3 * i + c] * inrm;
-            q[3 * i + c] = f[c];
+            const int e = 3 * lane + c;
+            f[c] = (w[row + c] - ((up[0][e] + up[1][e]) + (up[2][e] + up[3][e]))) * inrm;
+            q[row + c] = f[c];
         }
         double d[3];
         rot_apply(R + 9 * n, refs + 3 * m, d);
@@ -539,24 +580,24 @@ __global__ void __launch_bounds__(kSBlobs) s1_normalise_moments_kernel(
         a[4] = d[2] * f[0] - d[0] * f[2];
         a[5] = d[0] * f[1] - d[1] * f[0];
     }
-    block_sum6<kSBlobs>(a, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
+    block_sum6<kS1Tpb>(a, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
     if (!last_cta(ticket, gridDim.x * gridDim.y)) return;
     extern __shared__ double sh[];  // 6 W
     swimmer_sums(part, W, gridDim.x, sh);
     // body rows of q, and z_body = KTKinv_rot (-sums) - mob_rot q_body: one
     // thread per (swimmer, row), the products in two interleaved chains each
-    for (int e = threadIdx.x; e < 6 * W; e += kSBlobs) {
+    for (int e = threadIdx.x; e < 6 * W; e += kS1Tpb) {
         const int sw = e / 6, i = e % 6;
-        const double *sums = sh + 6 * sw, *wb = w + 3 * nb + 6 * sw;
-        q[3 * nb + e] = wb[i] * inrm;
+        const double *sums = sh + 6 * sw, *wb = w + 3 * (size_t)nb + 6 * sw;
+        q[3 * nb + e] = __ldcg(wb + i) * inrm;
         const double *Kt = ktk_rot + 36 * sw + i, *Mb = mob_rot + 36 * sw + i;
         double x0 = 0.0, x1 = 0.0, y0 = 0.0, y1 = 0.0;
 #pragma unroll
         for (int j = 0; j < 6; j += 2) {
             x0 += Kt[6 * j] * (-sums[j]);
             x1 += Kt[6 * (j + 1)] * (-sums[j + 1]);
-            y0 += Mb[6 * j] * wb[j];
-            y1 += Mb[6 * (j + 1)] * wb[j + 1];
+            y0 += Mb[6 * j] * __ldcg(wb + j);
+            y1 += Mb[6 * (j + 1)] * __ldcg(wb + j + 1);
         }
         z[3 * nb + e] = (x0 + x1) - (y0 + y1) * inrm;
     }
@@ -774,51 +815,19 @@ __device__ __forceinline__ void cta_update(const double *__restrict__ Q, size_t 
     __syncthreads();
 }
 
-// S4: second CGS pass.
-__global__ void __launch_bounds__(kSTpb) s4_update_project_kernel(const double *__restrict__ Q, size_t ld, int n,
-                                                                  double *__restrict__ w, double *__restrict__ P,
-                                                                  double *__restrict__ G, int *tickets,
-                                                                  double *__restrict__ scal, double *__restrict__ H,
-                                                                  int ldh, const GmresCtl *ctl)
+// The Givens step of solve_linear_system (mobility_solver.cpp:1189-1231) on
+// H column iter-1, whose subdiagonal entry is nrm, run by the last CTA of
+// S4 (all of its threads enter; warp 0 does the work): the previous
+// rotations over the column, the new rotation, beta, the residual and the
+// iteration control.  The H column and the rotations go to shared memory
+// first, so the sequential parts read no global memory.
+__device__ __forceinline__ void givens_step(double *__restrict__ H, int ldh, int iter, double nrm,
+                                            double *__restrict__ beta, double *__restrict__ cs,
+                                            double *__restrict__ sn, double *__restrict__ scal, GmresCtl *ctl)
 {
-    if (ctl->done) return;
-    __shared__ double ws[kSRows];
-    const int k = ctl->k, row0 = blockIdx.x * kSRows, rows = min(kSRows, n - row0);
-    double *h = scal + kHOff;
-    cta_update(Q, ld, row0, rows, k, h, w, ws);
-    cta_projections(Q, ld, row0, rows, k, ws, P, gridDim.x);
-    // h is overwritten only after every CTA has read it (all arrived)
-    if (!finish_projections(P, k, gridDim.x, G, tickets, h)) return;
-    double *Hcol = H + (size_t)ldh * (k - 1);
-    for (int i = threadIdx.x; i < k; i += kSTpb) Hcol[i] += h[i];
-}
-
-// S5: w -= Q h; ||w||; H(k, k-1) = ||w||; Givens rotation; iteration control.
-__global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
-    const double *__restrict__ Q, size_t ld, int n, double *__restrict__ w, double *__restrict__ P, int *ticket,
-    double *__restrict__ scal, double *__restrict__ H, int ldh, double *__restrict__ beta, double *__restrict__ cs,
-    double *__restrict__ sn, GmresCtl *ctl)
-{
-    if (ctl->done) return;
-    __shared__ double ws[kSRows];
-    const int k = ctl->k, row0 = blockIdx.x * kSRows, rows = min(kSRows, n - row0);
-    cta_update(Q, ld, row0, rows, k, scal + kHOff, w, ws);
-    if (threadIdx.x < 32) {  // kSRows == 32: one row per lane, then a warp sum
-        const double v = threadIdx.x < rows ? ws[threadIdx.x] : 0.0;
-        const double a = warp_sum(v * v);
-        if (threadIdx.x == 0) P[blockIdx.x] = a;
-    }
-    if (!last_cta(ticket, gridDim.x)) return;
-    // ||w||^2 in a fixed two-level order; the H column and the rotations to
-    // shared memory, so the sequential Givens sweep reads no global memory
-    __shared__ double red[kSTpb];
     __shared__ double col[kFMaxK + 1], csh[kFMaxK], snh[kFMaxK];
-    double t = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += kSTpb) t += __ldcg(P + b);
-    red[threadIdx.x] = t;
-    const int iter = k;
     double *gcol = H + (size_t)ldh * (iter - 1);
-    for (int i = threadIdx.x; i < iter; i += kSTpb) {
+    for (int i = threadIdx.x; i < iter; i += blockDim.x) {
         col[i] = gcol[i];
         if (i < iter - 1) {
             csh[i] = cs[i];
@@ -828,9 +837,6 @@ __global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
     __syncthreads();
     if (threadIdx.x >= 32) return;
     const int lane = threadIdx.x;
-    double r = 0.0;
-    for (int b = lane; b < kSTpb; b += 32) r += red[b];
-    r = warp_sum(r);  // lane 0
     // The previous rotations over the new H column, as a warp scan: entry i
     // after rotation i is x_i = -s_{i-1} x_{i-1} + c_{i-1} col_i, a
     // first-order linear recurrence (x -> a x + b pairs, Kogge-Stone over 32
@@ -864,7 +870,6 @@ __global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
         xin = __shfl_sync(0xffffffffu, xi, 31);  // lanes past the column repeat its last entry
     }
     if (lane == 0) {
-        const double nrm = sqrt(r);
         scal[kNormOff] = nrm;
         const double hk = nrm, hd = xin;
         double c, s;
@@ -898,6 +903,44 @@ __global__ void __launch_bounds__(kSTpb) s5_update_norm_givens_kernel(
     }
     __syncwarp();
     for (int i = lane; i <= iter; i += 32) gcol[i] = col[i];
+}
+
+// S4: second CGS pass.  w -= Q h1 (S3's projections), then h2 = Q^T w and,
+// as one more projection column, ||w||^2.  The last CTA adds h2 to the H
+// column and takes the new basis vector's norm as
+// ||w - Q h2||^2 = ||w||^2 - ||h2||^2 (Q orthonormal; h2 is the second
+// pass's correction, small next to w, so the difference keeps its
+// precision), then runs the Givens step.  The update w -= Q h2 itself is
+// left to the next S1, which touches every row anyway.
+__global__ void __launch_bounds__(kSTpb) s4_project_norm_givens_kernel(
+    const double *__restrict__ Q, size_t ld, int n, double *__restrict__ w, double *__restrict__ P,
+    double *__restrict__ G, int *tickets, double *__restrict__ scal, double *__restrict__ H, int ldh,
+    double *__restrict__ beta, double *__restrict__ cs, double *__restrict__ sn, GmresCtl *ctl)
+{
+    if (ctl->done) return;
+    __shared__ double ws[kSRows];
+    __shared__ double nrm_s;
+    const int k = ctl->k, row0 = blockIdx.x * kSRows, rows = min(kSRows, n - row0);
+    double *h = scal + kHOff;
+    cta_update(Q, ld, row0, rows, k, h, w, ws);
+    cta_projections(Q, ld, row0, rows, k, ws, P, gridDim.x);
+    if (threadIdx.x < 32) {  // kSRows == 32: one row per lane (zero past the last row)
+        const double v = ws[threadIdx.x];
+        const double a = warp_sum(v * v);
+        if (threadIdx.x == 0) P[(size_t)k * gridDim.x + blockIdx.x] = a;
+    }
+    // h is overwritten only after every CTA has read it (all arrived)
+    if (!finish_projections(P, k + 1, gridDim.x, G, tickets, h)) return;
+    double *Hcol = H + (size_t)ldh * (k - 1);
+    for (int i = threadIdx.x; i < k; i += kSTpb) Hcol[i] += h[i];
+    if (threadIdx.x < 32) {
+        double t = 0.0;
+        for (int i = threadIdx.x; i < k; i += 32) t += h[i] * h[i];
+        t = warp_sum(t);
+        if (threadIdx.x == 0) nrm_s = sqrt(fmax(h[k] - t, 0.0));
+    }
+    __syncthreads();
+    givens_step(H, ldh, k, nrm_s, beta, cs, sn, scal, ctl);
 }
 
 // Last node of the device-side loop's body: one thread decides whether the
@@ -1083,7 +1126,7 @@ struct StepLayout {
 static StepLayout step_layout(int n, int nblob, int W)
 {
     StepLayout L;
-    L.gx = (nblob + kSBlobs - 1) / kSBlobs;
+    L.gx = (nblob + kS1Blobs - 1) / kS1Blobs;  // S1's CTAs per swimmer (S2 has fewer)
     L.nblk = (n + kSRows - 1) / kSRows;
     L.ngroups = (L.nblk + kSGroup - 1) / kSGroup;
     L.doubles = (size_t)kFMaxK * (L.nblk + L.ngroups) + (size_t)W * L.gx * 6;
@@ -1092,7 +1135,7 @@ static StepLayout step_layout(int n, int nblob, int W)
 }
 
 // One device-controlled Arnoldi step (S1, S2, the blob-blob pair apply, S3,
-// S4, S5) enqueued on the solver stream; captured once per precision into
+// S4) enqueued on the solver stream; captured once per precision into
 // s->graph[pidx].
 static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle loop, bool use_loop)
 {
@@ -1110,13 +1153,13 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     }
     double *P = s->partial, *G = P + (size_t)kFMaxK * L.nblk, *part = G + (size_t)kFMaxK * L.ngroups;
     int *tk = s->st_tickets;
-    int *tk3 = tk + 2, *tk4 = tk3 + 1 + L.ngroups, *tk5 = tk4 + 1 + L.ngroups;
-    const dim3 bgrid(L.gx, W);
+    int *tk3 = tk + 2, *tk4 = tk3 + 1 + L.ngroups;
     const size_t wsm = 6 * (size_t)W * sizeof(double);
-    s1_normalise_moments_kernel<<<bgrid, kSBlobs, wsm, st>>>(W, nblob, s->Q, ld, s->w, s->R, s->refs, s->ktk_rot,
-                                                          s->mob_rot, s->z, part, s->st_scal, tk, s->ctl);
-    s2_precond_blobs_kernel<<<bgrid, kSBlobs, wsm, st>>>(W, nblob, s->Q, ld, s->R, s->refs, minv, s->x_blobs, s->z,
-                                                      s->w, s->gm_rec, f64 ? 1 : 0, part, tk + 1, s->ctl);
+    s1_update_normalise_moments_kernel<<<dim3(L.gx, W), kS1Tpb, wsm, st>>>(
+        W, nblob, s->Q, ld, s->w, s->R, s->refs, s->ktk_rot, s->mob_rot, s->z, part, s->st_scal, tk, s->ctl);
+    s2_precond_blobs_kernel<<<dim3((nblob + kSBlobs - 1) / kSBlobs, W), kSBlobs, wsm, st>>>(
+        W, nblob, s->Q, ld, s->R, s->refs, minv, s->x_blobs, s->z, s->w, s->gm_rec, f64 ? 1 : 0, part, tk + 1,
+        s->ctl);
     GMI_CUDA_TRY(cudaGetLastError());
     ExplicitPairEnv env{};
     env.stream = st;
@@ -1141,9 +1184,8 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     GMI_TRY(launch_pair_into(env, kBB, f64, s->gm_rec, 0, nb, s->gm_rec, nb, k, s->mbb, 0));
     s3_finish_project_kernel<<<L.nblk, kSTpb, 0, st>>>(W, nblob, s->mbb, s->gm_partial, splits, s->z, s->R, s->refs,
                                                        s->w, s->Q, ld, n, P, G, tk3, s->st_scal, s->H, ldh, s->ctl);
-    s4_update_project_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, G, tk4, s->st_scal, s->H, ldh, s->ctl);
-    s5_update_norm_givens_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, tk5, s->st_scal, s->H, ldh,
-                                                           s->beta, s->cs, s->sn, s->ctl);
+    s4_project_norm_givens_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, G, tk4, s->st_scal, s->H, ldh,
+                                                            s->beta, s->cs, s->sn, s->ctl);
     if (use_loop) arnoldi_loop_guard_kernel<<<1, 32, 0, st>>>(s->ctl, loop);
     GMI_CUDA_TRY(cudaGetLastError());
     return GMI_OK;
