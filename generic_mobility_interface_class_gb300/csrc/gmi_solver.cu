@@ -1429,12 +1429,15 @@ static gmi_status store_solution(gmi_solver *s)
 // A d = r by GMRES with the FP32C operator (FP64 Arnoldi, Givens and
 // vectors) to the relative tolerance that would meet the target in one pass
 // (with a 0.3 margin for the FP32C operator's own error), but not below
-// kInnerTol, which stays above that error (~3e-7 of |A d|); x += d.  This
-// converges to the FP64 solution at the requested tolerance, which GMRES on
-// the FP32C operator alone cannot (its answer is off by cond(A) times the
-// operator's rounding).  The iteration count returned is the sum of inner
-// iterations.
-static constexpr double kInnerTol = 1e-6;
+// kInnerTol; x += d.  This converges to the FP64 solution at the requested
+// tolerance, which GMRES on the FP32C operator alone cannot (its answer is
+// off by cond(A) times the operator's rounding).  kInnerTol sits somewhat
+// below that rounding (~3e-7 of |A d|): GMRES's own residual estimate keeps
+// falling there, and the deeper inner solves save more refinement restarts
+// than they cost (the fewest total iterations on the 962- and 16,896-particle
+// swimmers among floors from 1e-6 to 2e-8; GMI_INNER_TOL overrides it).  The
+// iteration count returned is the sum of inner iterations.
+static constexpr double kInnerTol = 1e-7;
 static constexpr double kInnerMargin = 0.3;
 static constexpr int kMaxRefinements = 12;
 
@@ -1476,6 +1479,8 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
     gmi_status status = GMI_OK;
     // the blob-blob sum of this residual in double-float (FP64-grade, on the
     // FP32 pipe); GMI_REFINE_DF=0 takes the FP64 kernel instead
+    const char *floor_env = std::getenv("GMI_INNER_TOL");  // the floor of the inner tolerance
+    const double inner_floor = floor_env ? std::atof(floor_env) : kInnerTol;
     const char *df_env = std::getenv("GMI_REFINE_DF");
     s->ctx->precision = (df_env && df_env[0] == '0') ? GMI_FP64 : GMI_DF64;
     status = system_matrix_mult(s, s->soln, s->tmp);
@@ -1506,7 +1511,7 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         GMI_CUDA_TRY(cudaMemcpyAsync(s->xacc, s->soln, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
         GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
         const double want = kInnerMargin * tol * norm_rhs / beta;
-        const double inner_tol = want > kInnerTol ? want : kInnerTol;
+        const double inner_tol = want > inner_floor ? want : inner_floor;
         int iters = 0;
         GMI_TRY(gmres_run(s, beta, beta, inner_tol, false, true, &iters));
         total += iters;
