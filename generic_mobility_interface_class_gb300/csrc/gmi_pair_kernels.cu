@@ -734,6 +734,13 @@ __global__ void __launch_bounds__(kWarpCta) rpy_pair_warp_kernel(const PairLaunc
 // Targets: segments [0,S) then blobs [S, S+B) (of the requested ranges);
 // sources: all S segments then all B blobs.
 //
+// The screen positions are FP32 offsets from the first particle, one float4
+// each; a rounding margin from the largest offset (the pack kernel's
+// extent) keeps every pair that is inside the cutoff in FP64 inside the
+// screen.  Each lane screens its target against eight sources at a time
+// (independent arithmetic, one warp vote per eight), and only then looks at
+// the candidates one by one.
+//
 // The FP64 path (sqrt, divide) is slow on this GPU and rare per lane, so the
 // lanes of a warp do not each run it for their own candidates: every warp
 // queues its candidates (lane, j) in shared memory in screening order,
@@ -744,18 +751,25 @@ __global__ void __launch_bounds__(kWarpCta) rpy_pair_warp_kernel(const PairLaunc
 // ---------------------------------------------------------------------------
 constexpr int kBarrierTpb = 64;
 constexpr int kBarrierWarps = kBarrierTpb / 32;
-constexpr int kBarrierQ = 64;  // queue entries per warp (flushed at >= 32)
+constexpr int kBarrierQ = 64;     // queue entries per warp (flushed at >= 32)
+constexpr int kBarrierGroup = 8;  // sources per warp vote
 
+// out[i] = x_i - x_0 in FP32; *extent = max |coordinate| (FP32 bits, which
+// order like the values for non-negative floats; zeroed by the launcher)
 __global__ void pack_screen_positions(const double *__restrict__ xs, int S, const double *__restrict__ xb, int B,
-                                      float4 *__restrict__ out)
+                                      float4 *__restrict__ out, unsigned *__restrict__ extent)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= S + B) return;
-    const double *p = i < S ? xs + 3 * (size_t)i : xb + 3 * (size_t)(i - S);
-    const float hx = (float)p[0], hy = (float)p[1], hz = (float)p[2];
-    out[2 * (size_t)i] = make_float4(hx, hy, hz, 0.f);
-    out[2 * (size_t)i + 1] =
-        make_float4((float)(p[0] - (double)hx), (float)(p[1] - (double)hy), (float)(p[2] - (double)hz), 0.f);
+    const double *p0 = S > 0 ? xs : xb;
+    float m = 0.0f;
+    if (i < S + B) {
+        const double *p = i < S ? xs + 3 * (size_t)i : xb + 3 * (size_t)(i - S);
+        const float rx = (float)(p[0] - p0[0]), ry = (float)(p[1] - p0[1]), rz = (float)(p[2] - p0[2]);
+        out[i] = make_float4(rx, ry, rz, 0.f);
+        m = fmaxf(fabsf(rx), fmaxf(fabsf(ry), fabsf(rz)));
+    }
+    const unsigned mb = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
+    if ((threadIdx.x & 31) == 0 && mb != 0u) atomicMax(extent, mb);
 }
 
 struct BarrierQueue {
@@ -811,7 +825,7 @@ __device__ __forceinline__ void barrier_flush(const BarrierLaunch &a, BarrierQue
 
 __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
 {
-    __shared__ float4 tile[2 * kBarrierTpb];
+    __shared__ float4 tile[kBarrierTpb];
     __shared__ BarrierQueue queues[kBarrierWarps];
     BarrierQueue &q = queues[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -821,12 +835,11 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
     const bool valid = local < a.num_segs + (a.wall ? 0 : a.num_blobs);
     const int gi = is_seg_target ? a.start_seg + local : a.S + a.start_blob + (local - a.num_segs);
     double xi = 0, yi = 0, zi = 0;
-    float4 pf = make_float4(0.f, 0.f, 0.f, 0.f), pl = pf;
+    float4 pf = make_float4(0.f, 0.f, 0.f, 0.f);
     if (valid) {
         const double *p = is_seg_target ? a.xs + 3 * (size_t)gi : a.xb + 3 * (size_t)(gi - a.S);
         xi = p[0]; yi = p[1]; zi = p[2];
-        pf = a.screen[2 * (size_t)gi];
-        pl = a.screen[2 * (size_t)gi + 1];
+        pf = a.screen[gi];
     }
     const int fil_i = gi / a.nseg;
     double g0 = 0, g1 = 0, g2 = 0;
@@ -837,47 +850,56 @@ __global__ void __launch_bounds__(kBarrierTpb) barrier_kernel(BarrierLaunch a)
         g2 = a.scale * fz * fz * fz * fz;
     }
     const double a_tgt = is_seg_target ? a.rseg : a.rblob;
-    // squared FP32 screen cutoffs against segment and blob sources (host
-    // precomputed: no FP64 arithmetic in the loop)
-    const float c2_s = is_seg_target ? a.cut2_ss : a.cut2_sb;
-    const float c2_b = is_seg_target ? a.cut2_sb : a.cut2_bb;
+    // squared screen cutoffs against segment and blob sources: the FP32
+    // cutoff plus the rounding of the offsets (each within 2^-24 of the
+    // extent, their difference within 2^-23 of it) and of the separation
+    const float margin = 1.0e-6f * __uint_as_float(*a.extent);
+    const float cs = (is_seg_target ? a.cut_ss : a.cut_sb) + margin;
+    const float cb = (is_seg_target ? a.cut_sb : a.cut_bb) + margin;
+    const float c2_s = cs * cs, c2_b = cb * cb;
     int count = 0;  // warp-uniform
     for (int j0 = j_begin; j0 < j_end; j0 += kBarrierTpb) {
         const int jl = j0 + threadIdx.x;
-        if (jl < j_end) {
-            tile[2 * threadIdx.x] = a.screen[2 * (size_t)jl];
-            tile[2 * threadIdx.x + 1] = a.screen[2 * (size_t)jl + 1];
-        }
+        if (jl < j_end) tile[threadIdx.x] = a.screen[jl];
         __syncthreads();
         const int jn = min(kBarrierTpb, j_end - j0);
-        for (int jj = 0; jj < jn; ++jj) {
-            const int j = j0 + jj;
-            const float4 s = tile[2 * jj], sl = tile[2 * jj + 1];
-            const float dx = (pf.x - s.x) + (pl.x - sl.x);
-            const float dy = (pf.y - s.y) + (pl.y - sl.y);
-            const float dz = (pf.z - s.z) + (pl.z - sl.z);
-            const float d2 = dx * dx + dy * dy + dz * dz;
-            bool cand = valid && d2 < (j < a.S ? c2_s : c2_b);
-            if (cand) {
-                if (is_seg_target) {
-                    const int di = gi - j;
-                    cand = !((fil_i == j / a.nseg) && (di <= 1 && di >= -1));
-                } else {
-                    cand = (j != gi);
-                }
+        for (int u0 = 0; u0 < jn; u0 += kBarrierGroup) {
+            unsigned bits = 0u;
+#pragma unroll
+            for (int u = 0; u < kBarrierGroup; ++u) {
+                const int jj = u0 + u;
+                const float4 s = tile[jj < jn ? jj : jn - 1];
+                const float dx = pf.x - s.x, dy = pf.y - s.y, dz = pf.z - s.z;
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const bool in = jj < jn && d2 < ((j0 + jj) < a.S ? c2_s : c2_b);
+                bits |= in ? (1u << u) : 0u;
             }
-            const unsigned mask = __ballot_sync(0xffffffffu, cand);
-            if (mask) {
+            if (!valid) bits = 0u;
+            if (!__any_sync(0xffffffffu, bits != 0u)) continue;
+            for (int u = 0; u < kBarrierGroup; ++u) {
+                const int j = j0 + u0 + u;
+                bool cand = ((bits >> u) & 1u) != 0u;
                 if (cand) {
-                    const int pos = count + __popc(mask & ((1u << lane) - 1u));
-                    q.j[pos] = j;
-                    q.lane[pos] = lane;
+                    if (is_seg_target) {
+                        const int di = gi - j;
+                        cand = !((fil_i == j / a.nseg) && (di <= 1 && di >= -1));
+                    } else {
+                        cand = (j != gi);
+                    }
                 }
-                count += __popc(mask);
-                __syncwarp();
-                if (count >= 32) {
-                    barrier_flush(a, q, count, xi, yi, zi, a_tgt, g0, g1, g2);
-                    count = 0;
+                const unsigned mask = __ballot_sync(0xffffffffu, cand);
+                if (mask) {
+                    if (cand) {
+                        const int pos = count + __popc(mask & ((1u << lane) - 1u));
+                        q.j[pos] = j;
+                        q.lane[pos] = lane;
+                    }
+                    count += __popc(mask);
+                    __syncwarp();
+                    if (count >= 32) {
+                        barrier_flush(a, q, count, xi, yi, zi, a_tgt, g0, g1, g2);
+                        count = 0;
+                    }
                 }
             }
         }
@@ -1315,18 +1337,17 @@ gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &in)
     const int N = a.S + a.B;
     const int ntg = a.num_segs + (a.wall ? 0 : a.num_blobs);
     if (ntg <= 0) return GMI_OK;
-    gmi_status st = ctx->rec_tgt.reserve((size_t)(N > 0 ? N : 1) * 2 * sizeof(float4));
+    gmi_status st = ctx->rec_tgt.reserve((size_t)(N > 0 ? N : 1) * sizeof(float4) + sizeof(float4));
     if (st != GMI_OK) return st;
     a.screen = static_cast<float4 *>(ctx->rec_tgt.ptr);
-    // screen cutoffs 1.1 (a_i + a_j) with a relative margin of 1e-3 for the
-    // FP32 separation; pairs inside are re-evaluated in FP64
-    auto cut2 = [](double asum) {
-        const float c = (float)(1.1 * asum) * 1.001f;
-        return c * c;
-    };
-    a.cut2_ss = cut2(2.0 * a.rseg);
-    a.cut2_sb = cut2(a.rseg + a.rblob);
-    a.cut2_bb = cut2(2.0 * a.rblob);
+    a.extent = reinterpret_cast<unsigned *>(a.screen + (N > 0 ? N : 1));
+    // screen cutoffs 1.1 (a_i + a_j) with a relative margin of 1e-3 (FP32
+    // rounding of the separation and of the cutoff); the kernel adds the
+    // offsets' rounding; pairs inside are re-evaluated in FP64
+    auto cut = [](double asum) { return (float)(1.1 * asum) * 1.001f; };
+    a.cut_ss = cut(2.0 * a.rseg);
+    a.cut_sb = cut(a.rseg + a.rblob);
+    a.cut_bb = cut(2.0 * a.rblob);
     // source splits: enough CTAs for ~8 per SM, at least 64 sources each
     const int tgt_ctas = (ntg + kBarrierTpb - 1) / kBarrierTpb;
     int splits = (8 * ctx->sm_count + tgt_ctas - 1) / tgt_ctas;
@@ -1339,7 +1360,8 @@ gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &in)
         if (st != GMI_OK) return st;
         a.partial = static_cast<double *>(ctx->partial.ptr);
     }
-    pack_screen_positions<<<(N + 255) / 256, 256, 0, ctx->stream>>>(a.xs, a.S, a.xb, a.B, a.screen);
+    GMI_CUDA_TRY(cudaMemsetAsync(a.extent, 0, sizeof(unsigned), ctx->stream));
+    pack_screen_positions<<<(N + 255) / 256, 256, 0, ctx->stream>>>(a.xs, a.S, a.xb, a.B, a.screen, a.extent);
     barrier_kernel<<<dim3(tgt_ctas, splits), kBarrierTpb, 0, ctx->stream>>>(a);
     ctx->launches += 2;
     if (splits > 1) {

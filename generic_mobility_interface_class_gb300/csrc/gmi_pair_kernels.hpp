@@ -29,13 +29,14 @@ struct BarrierLaunch {
     double *f_blobs_rep;
     const double *xs;
     const double *xb;
-    float4 *screen;  // FP32 (hi, lo) positions of all S + B particles (filled by the launcher)
+    float4 *screen;   // FP32 positions of all S + B particles relative to the first (filled by the launcher)
+    unsigned *extent;  // largest |coordinate| of `screen`, as FP32 bits (filled by the launcher)
     int S, B;
     int start_seg, num_segs, start_blob, num_blobs;
     int nseg;
     double rseg, rblob, scale;
     int wall;
-    float cut2_ss, cut2_sb, cut2_bb;  // squared FP32 screen cutoffs (filled by the launcher)
+    float cut_ss, cut_sb, cut_bb;  // FP32 screen cutoffs before the rounding margin (filled by the launcher)
     int chunk;            // sources per split (filled by the launcher)
     double *partial;      // [splits][targets][3] when there are several splits (filled by the launcher)
 };
