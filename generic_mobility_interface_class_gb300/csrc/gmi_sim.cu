@@ -28,6 +28,7 @@
 //   Broyden: C, D [nbroy x max_iter] column-major, error/new_error/update [nbroy]
 //   with nbroy = W * (6*nfil*nseg + 6), the reference's unknown ordering
 //   (per swimmer: per filament [tether, lambdas, clamp, segment u's], then body).
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -536,34 +537,40 @@ __device__ void lie_segment_blocks(const SimP &P, int fil, int nt, int k, double
 
 // filament::invert_approx_jacobian (filament.cpp:1406-1539) up to the
 // inversion: the approximate Jacobian in invJ, the two clamping blocks saved.
-// One CTA per filament.  The reference's block writes fall into disjoint
-// regions (constraint diagonal; position couplings, rows < 3NS; Lie-algebra
-// rows >= 3NS, columns < 3NS; the Lie-algebra block, one row band per
-// segment), built in parallel, with the writes that depend on earlier ones
-// (end-force term, unit diagonal, clamping blocks) after a barrier.  Tasks
-// go to warps round-robin so the FP64 work spreads over the SM's schedulers.
+// The reference's block writes fall into disjoint regions (constraint
+// diagonal; position couplings, rows < 3NS; Lie-algebra rows >= 3NS, columns
+// < 3NS; the Lie-algebra block, one row band per segment), built in parallel
+// as tasks: grid (filament, split), the filament's 3NS-2 tasks dealt round-
+// robin to its gridDim.y CTAs and, within a CTA, to its warps, so the FP64
+// work spreads over the SM's schedulers and, with few filaments, over more
+// SMs.  The matrix is zeroed before the launch; the writes that depend on
+// earlier ones (end-force term, unit diagonal, clamping blocks) follow in
+// jacobian_finish_kernel.
 constexpr int kJacTpb = 128;
 
 __global__ void __launch_bounds__(kJacTpb) build_jacobian_kernel(SimP P, int nt)
 {
-    const int fil = blockIdx.x, tid = threadIdx.x;
+    const int fil = blockIdx.x, tid = threadIdx.x, nsplit = gridDim.y, split = blockIdx.y;
     const int NS = P.NS, ld = P.n6, s0 = fil * NS;
     double *J = P.invJ + (size_t)fil * ld * ld;
-    for (size_t k = tid; k < (size_t)ld * ld; k += kJacTpb) J[k] = 0.0;
-    __syncthreads();
     const bool euler = nt < P.neuler;
     const double fac0 = euler ? -P.DT / (6.0 * kPi * P.MU * P.RSEG) : -P.DT / (9.0 * kPi * P.MU * P.RSEG);
     const double fac1 = euler ? P.DL * P.DT / (16.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG)
                               : P.DL * P.DT / (24.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
-    for (int i = tid; i < 3 * NS; i += kJacTpb) {
-        J[i + (size_t)ld * i] = fac0;
-        if (i < 3 * NS - 3) J[i + (size_t)ld * (i + 3)] = -fac0;
-    }
+    if (split == 0)
+        for (int i = tid; i < 3 * NS; i += kJacTpb) {
+            J[i + (size_t)ld * i] = fac0;
+            if (i < 3 * NS - 3) J[i + (size_t)ld * (i + 3)] = -fac0;
+        }
     // tasks: [0, NS-1) position columns j+1; [NS-1, 2NS-2) Lie-to-position
     // rows for j+1; [2NS-2, 3NS-2) Lie-algebra segment k
     const int ntask = 3 * NS - 2;
-    for (int task = 0; task < ntask; ++task) {
-        if (((task % 4) * 32 + task / 4) % kJacTpb != tid) continue;
+    for (int task = split; task < ntask; task += nsplit) {
+        // the CTA's own tasks go to the warps round-robin: each task is a
+        // serial FP64 chain, so the chains of one CTA run on all four
+        // schedulers at once
+        const int lt = task / nsplit;
+        if (((lt % 4) * 32 + lt / 4) % kJacTpb != tid) continue;
         double t[3];
         if (task < NS - 1) {
             const int j = task + 1, jpos = 3 * (NS + j);
@@ -590,7 +597,18 @@ __global__ void __launch_bounds__(kJacTpb) build_jacobian_kernel(SimP P, int nt)
             lie_segment_blocks(P, fil, nt, task - (2 * NS - 2), J, ld);
         }
     }
-    __syncthreads();
+}
+
+// The writes of invert_approx_jacobian that depend on the task blocks: the
+// end-force term, the unit diagonal of the Lie-algebra block, and the two
+// clamping blocks (saved, then replaced).  One CTA per filament.
+__global__ void __launch_bounds__(kJacTpb) jacobian_finish_kernel(SimP P, int nt)
+{
+    const int fil = blockIdx.x, tid = threadIdx.x;
+    const int NS = P.NS, ld = P.n6, s0 = fil * NS;
+    double *J = P.invJ + (size_t)fil * ld * ld;
+    const bool euler = nt < P.neuler;
+    const double fac0 = euler ? -P.DT / (6.0 * kPi * P.MU * P.RSEG) : -P.DT / (9.0 * kPi * P.MU * P.RSEG);
     for (int k = tid; k < 3 * NS; k += kJacTpb) J[(3 * NS + k) + (size_t)ld * (3 * NS + k)] += 1.0;
     if (tid == 0) {
         double t[3];
@@ -1189,7 +1207,13 @@ static gmi_status velocities_and_errors(gmi_sim *m, int nt, double *err_out, boo
 static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
 {
     const SimP &P = m->P;
-    build_jacobian_kernel<<<P.F, kJacTpb, 0, sst(m)>>>(P, nt);
+    // the tasks of few filaments spread over several CTAs each (enough CTAs
+    // for about two per SM, at most 8 per filament)
+    const int sms = m->solver->ctx->sm_count;
+    const int nsplit = std::max(1, std::min(8, (2 * sms + P.F - 1) / std::max(P.F, 1)));
+    GMI_CUDA_TRY(cudaMemsetAsync(P.invJ, 0, (size_t)P.F * P.n6 * P.n6 * sizeof(double), sst(m)));
+    build_jacobian_kernel<<<dim3(P.F, nsplit), kJacTpb, 0, sst(m)>>>(P, nt);
+    jacobian_finish_kernel<<<P.F, kJacTpb, 0, sst(m)>>>(P, nt);
     // few filaments: each inversion spread over a cluster of CTAs
     const int csize = m->use_gj_cluster ? gj_cluster_size(P.F, P.n6, m->solver->ctx->sm_count) : 1;
     GMI_TRY(gj_invert(sst(m), P.invJ, P.F, P.n6, csize, m->use_gj_registers, m->solver->ctx->device, P.flags));
@@ -1199,7 +1223,7 @@ static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
         schur_filament_kernel<<<P.F, 32, 0, sst(m)>>>(P, m->spart);
         swimmer_schur_kernel<<<P.W, 64, 0, sst(m)>>>(P, nt, m->spart);
     }
-    GMI_TRY(sim_launched(m, P.wall ? 2 : 5));
+    GMI_TRY(sim_launched(m, P.wall ? 3 : 6));
     GMI_TRY(read_flags(m));
     if (m->h_flags[2]) {
         set_last_error_msg("the approximate Jacobian is singular (matrix.cpp:549-554 stops the reference here)");

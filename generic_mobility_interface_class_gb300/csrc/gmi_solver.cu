@@ -82,33 +82,28 @@ __device__ __forceinline__ void quat_rot(const double *q, double *R)
 // body kernels
 // ---------------------------------------------------------------------------
 // R per swimmer and the 6x6 reference matrices rotated block by block,
-// Q * block * Q^T (mobility_solver.cpp:660-677).
+// Q * block * Q^T (mobility_solver.cpp:660-677).  One thread per (swimmer,
+// matrix, entry): each forms R itself and its entry's row of R * block, then
+// the entry, with the operations of the whole-block product (a warp FP64
+// instruction costs the same on one lane as on 32, so the 72 entries of a
+// swimmer take about as long as one).
 __global__ void prepare_bodies_kernel(int W, const double *__restrict__ q, const double *__restrict__ ktk_ref,
                                       const double *__restrict__ mob_ref, double *__restrict__ R,
                                       double *__restrict__ ktk_rot, double *__restrict__ mob_rot)
 {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= W) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 72 * W) return;
+    const int n = e / 72, m = (e % 72) / 36, rc = e % 36, r = rc % 6, c = rc / 6;
     double Rn[9];
     quat_rot(q + 4 * n, Rn);
-    for (int k = 0; k < 9; ++k) R[9 * n + k] = Rn[k];
-    const double *src[2] = {ktk_ref, mob_ref};
-    double *dst[2] = {ktk_rot + 36 * n, mob_rot + 36 * n};
-    for (int m = 0; m < 2; ++m) {
-        for (int bi = 0; bi < 2; ++bi)
-            for (int bj = 0; bj < 2; ++bj) {
-                double A[9], T[9];
-                for (int i = 0; i < 3; ++i)
-                    for (int j = 0; j < 3; ++j) A[3 * i + j] = src[m][(3 * bi + i) + 6 * (3 * bj + j)];
-                for (int i = 0; i < 3; ++i)  // T = R A
-                    for (int j = 0; j < 3; ++j)
-                        T[3 * i + j] = Rn[3 * i] * A[j] + Rn[3 * i + 1] * A[3 + j] + Rn[3 * i + 2] * A[6 + j];
-                for (int i = 0; i < 3; ++i)  // T R^T
-                    for (int j = 0; j < 3; ++j)
-                        dst[m][(3 * bi + i) + 6 * (3 * bj + j)] =
-                            T[3 * i] * Rn[3 * j] + T[3 * i + 1] * Rn[3 * j + 1] + T[3 * i + 2] * Rn[3 * j + 2];
-            }
-    }
+    if (m == 0 && rc < 9) R[9 * n + rc] = Rn[rc];
+    const double *A = (m == 0 ? ktk_ref : mob_ref) + 3 * (r / 3) + 6 * (3 * (c / 3));  // the block, column-major
+    const int i = r % 3, j = c % 3;
+    double T[3];  // row i of R A
+#pragma unroll
+    for (int jj = 0; jj < 3; ++jj)
+        T[jj] = Rn[3 * i] * A[6 * jj] + Rn[3 * i + 1] * A[1 + 6 * jj] + Rn[3 * i + 2] * A[2 + 6 * jj];
+    (m == 0 ? ktk_rot : mob_rot)[36 * n + rc] = T[0] * Rn[3 * j] + T[1] * Rn[3 * j + 1] + T[2] * Rn[3 * j + 2];
 }
 
 // x_blob = X + R ref (rigid_body.cpp:334-352).
@@ -1058,7 +1053,7 @@ static gmi_status device_norm(gmi_solver *s, const double *x, int n)
 static gmi_status prepare_bodies(gmi_solver *s)
 {
     if (s->W == 0) return GMI_OK;
-    prepare_bodies_kernel<<<grid_for(s->W, 64), 64, 0, s->ctx->stream>>>(s->W, s->body_q, s->ktk_ref, s->mob_ref,
+    prepare_bodies_kernel<<<grid_for(72 * s->W, 128), 128, 0, s->ctx->stream>>>(s->W, s->body_q, s->ktk_ref, s->mob_ref,
                                                                           s->R, s->ktk_rot, s->mob_rot);
     return launched(s);
 }
