@@ -19,6 +19,23 @@ enum : unsigned {
     kDevErrNonFinite = 1u << 1,    // a reduction saw a NaN or Inf
 };
 
+// Programmatic dependent launch.  A kernel launched with the programmatic
+// stream-serialization attribute may start while the previous kernel on its
+// stream still runs.  griddepcontrol.wait blocks until that kernel has
+// completed and its memory is visible (a no-op after an ordinary launch);
+// launch_dependents then lets the next kernel start launching, so kernel
+// boundaries in a chain of short kernels overlap the launch latency.  The
+// kernels of the graph-replayed Arnoldi step call this first.  The pair
+// kernels only wait (pdl_wait): their many CTAs keep the SMs, and the next
+// kernel launches when they exit.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+__device__ __forceinline__ void pdl_wait_then_release()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Upper bound for any spin on an mbarrier: 2 s of %globaltimer.  A wait that
 // runs past it records kDevErrWaitTimeout and the kernel returns.
 constexpr unsigned long long kWaitDeadlineNs = 2000000000ull;

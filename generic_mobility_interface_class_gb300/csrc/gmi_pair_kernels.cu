@@ -247,6 +247,7 @@ __global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ C
     R *ring = reinterpret_cast<R *>(smem_raw);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + kStages * kStageScalars * sizeof(R));
 
+    pdl_wait();
     if (args.skip != nullptr && *args.skip != 0) return;
     const int tid = threadIdx.x;
     const int j_begin = blockIdx.y * args.chunk;
@@ -393,6 +394,7 @@ __global__ void __launch_bounds__(TPB) rpy_bb_df_kernel(const __grid_constant__ 
     float *ring = reinterpret_cast<float *>(smem_raw);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + kStages * kStageScalars * sizeof(float));
 
+    pdl_wait();
     if (args.skip != nullptr && *args.skip != 0) return;
     const int tid = threadIdx.x;
     const int j_begin = blockIdx.y * args.chunk;
@@ -508,6 +510,7 @@ __global__ void __launch_bounds__(TPB) rpy_pair2_kernel(const __grid_constant__ 
     float4 *ibuf = reinterpret_cast<float4 *>(smem_raw + kStagesP * kStageScalars * sizeof(float));
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + (kStagesP + 2) * kStageScalars * sizeof(float));
 
+    pdl_wait();
     if (args.skip != nullptr && *args.skip != 0) return;
     const int tid = threadIdx.x;
     const int j_begin = blockIdx.y * args.chunk;
@@ -685,6 +688,7 @@ template <int KIND, class R, int TPW>
 __global__ void __launch_bounds__(kWarpCta) rpy_pair_warp_kernel(const PairLaunch args, const R *__restrict__ src)
 {
     constexpr int NOUT = KindTraits<KIND>::nout;
+    pdl_wait();
     if (args.skip != nullptr && *args.skip != 0) return;
     const int lane = threadIdx.x & 31;
     const int t0 = ((blockIdx.x * kWarpCta + threadIdx.x) >> 5) * TPW;
@@ -1113,8 +1117,28 @@ static void *warp_kernel_ptr(int kind, bool f64, int tpw)
     }
 }
 
+// cudaLaunchKernel, or with pdl the same launch marked for programmatic
+// dependent launch (the kernel may start while the previous one on the
+// stream finishes; it waits in pdl_wait_then_release)
+static cudaError_t launch_fn(const void *fn, dim3 grid, dim3 block, void **params, size_t smem, cudaStream_t stream,
+                             bool pdl)
+{
+    if (!pdl) return cudaLaunchKernel(fn, grid, block, params, smem, stream);
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, params);
+}
+
 static gmi_status launch_warp(cudaStream_t stream, int kind, bool f64, int tpw, const PairLaunch &a,
-                              const void *src_rec)
+                              const void *src_rec, bool pdl = false)
 {
     tpw = tpw >= 2 ? 2 : 1;
     void *fn = warp_kernel_ptr(kind, f64, tpw);
@@ -1123,7 +1147,7 @@ static gmi_status launch_warp(cudaStream_t stream, int kind, bool f64, int tpw, 
     PairLaunch la = a;
     la.partial = nullptr;
     void *params[] = {&la, const_cast<void **>(&src_rec)};
-    GMI_CUDA_TRY(cudaLaunchKernel(fn, dim3(ctas), dim3(kWarpCta), params, 0, stream));
+    GMI_CUDA_TRY(launch_fn(fn, dim3(ctas), dim3(kWarpCta), params, 0, stream, pdl));
     return GMI_OK;
 }
 
@@ -1498,7 +1522,7 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
         a.accumulate = accumulate;
         a.err = env.err;
         a.skip = env.skip;
-        return launch_warp(env.stream, kind, f64, env.tt, a, src_rec);
+        return launch_warp(env.stream, kind, f64, env.tt, a, src_rec, env.pdl != 0);
     }
     const int sidx = shape_index(env.tpb, env.tt, env.scalar_only ? 0 : -1, kind, f64);
     const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;
@@ -1537,7 +1561,7 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     gmi_status st = encode_record_map(env.encode_tiled, &map, src_rec, n_src, f64);
     if (st != GMI_OK) return st;
     void *params[] = {&map, &a};
-    GMI_CUDA_TRY(cudaLaunchKernel(fn, dim3(n_tgt_ctas, splits), dim3(tpb), params, smem, env.stream));
+    GMI_CUDA_TRY(launch_fn(fn, dim3(n_tgt_ctas, splits), dim3(tpb), params, smem, env.stream, env.pdl != 0));
     if (env.splits_out) {
         *env.splits_out = splits;
         return GMI_OK;

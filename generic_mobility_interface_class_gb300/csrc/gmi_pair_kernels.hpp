@@ -82,6 +82,8 @@ struct ExplicitPairEnv {
     const int *skip;       // optional device flag: non-zero turns the launch into a no-op
     int *splits_out;       // optional: the caller adds the per-split partials (partial[p * 3 n_tgt + e],
                            // p < *splits_out) itself; 1 means the kernel wrote `out` directly
+    int pdl;               // non-zero: launch for programmatic dependent launch (the pair kernel
+                           // waits for the previous kernel in pdl_wait_then_release)
 };
 
 size_t record_bytes(bool f64);

@@ -522,6 +522,7 @@ __global__ void __launch_bounds__(kS1Tpb) s1_update_normalise_moments_kernel(
     const double *__restrict__ mob_rot, double *__restrict__ z, double *__restrict__ part,
     const double *__restrict__ scal, int *ticket, const GmresCtl *ctl)
 {
+    pdl_wait_then_release();
     static_assert(kS1Tpb == 4 * 32 && kS1Blobs == 32, "S1: four warps over 32 blobs");
     if (ctl->done) return;
     __shared__ double hs[kFMaxK];
@@ -606,6 +607,7 @@ __global__ void __launch_bounds__(kSBlobs) s2_precond_blobs_kernel(
     const double *__restrict__ refs, double minv, const double *__restrict__ xb, double *__restrict__ z,
     double *__restrict__ w, void *rec, int f64, double *__restrict__ part, int *ticket, const GmresCtl *ctl)
 {
+    pdl_wait_then_release();
     if (ctl->done) return;
     const int n = blockIdx.y, m = blockIdx.x * kSBlobs + threadIdx.x, nb = W * nblob;
     const double *in = Q + ld * (size_t)(ctl->k - 1);
@@ -725,6 +727,7 @@ __global__ void __launch_bounds__(kSTpb) s3_finish_project_kernel(
     double *__restrict__ G, int *tickets, double *__restrict__ scal, double *__restrict__ H, int ldh,
     const GmresCtl *ctl)
 {
+    pdl_wait_then_release();
     static_assert(kSTpb == 4 * kSRows && kSRows == 32, "S3's split sum: four warps over 32 rows");
     if (ctl->done) return;
     __shared__ double ws[kSRows];
@@ -912,6 +915,7 @@ __global__ void __launch_bounds__(kSTpb) s4_project_norm_givens_kernel(
     double *__restrict__ G, int *tickets, double *__restrict__ scal, double *__restrict__ H, int ldh,
     double *__restrict__ beta, double *__restrict__ cs, double *__restrict__ sn, GmresCtl *ctl)
 {
+    pdl_wait_then_release();
     if (ctl->done) return;
     __shared__ double ws[kSRows];
     __shared__ double nrm_s;
@@ -943,6 +947,7 @@ __global__ void __launch_bounds__(kSTpb) s4_project_norm_givens_kernel(
 // its own pass count ends the loop after max_iter + 1 passes in any case.
 __global__ void arnoldi_loop_guard_kernel(GmresCtl *ctl, cudaGraphConditionalHandle loop)
 {
+    pdl_wait_then_release();
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int passes = ++ctl->guard;
     const bool again = ctl->done == 0 && passes <= ctl->max_iter + 1;
@@ -1112,6 +1117,26 @@ static gmi_status orthonormalise(gmi_solver *s, double *w, int k, double *Hcol)
     return launched(s, 2);
 }
 
+// A kernel launch of the Arnoldi step; with pdl, marked for programmatic
+// dependent launch, so that it may start while the previous kernel finishes
+// (each step kernel waits first, in pdl_wait_then_release).
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_step(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                               cudaStream_t st, Args... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // Sizes of the Arnoldi step's workspace inside s->partial and s->st_tickets.
 struct StepLayout {
     int gx, nblk, ngroups;
@@ -1150,12 +1175,15 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     int *tk = s->st_tickets;
     int *tk3 = tk + 2, *tk4 = tk3 + 1 + L.ngroups;
     const size_t wsm = 6 * (size_t)W * sizeof(double);
-    s1_update_normalise_moments_kernel<<<dim3(L.gx, W), kS1Tpb, wsm, st>>>(
-        W, nblob, s->Q, ld, s->w, s->R, s->refs, s->ktk_rot, s->mob_rot, s->z, part, s->st_scal, tk, s->ctl);
-    s2_precond_blobs_kernel<<<dim3((nblob + kSBlobs - 1) / kSBlobs, W), kSBlobs, wsm, st>>>(
-        W, nblob, s->Q, ld, s->R, s->refs, minv, s->x_blobs, s->z, s->w, s->gm_rec, f64 ? 1 : 0, part, tk + 1,
-        s->ctl);
-    GMI_CUDA_TRY(cudaGetLastError());
+    const bool pdl = s->use_pdl;
+    GMI_CUDA_TRY(launch_step(pdl, s1_update_normalise_moments_kernel, dim3(L.gx, W), dim3(kS1Tpb), wsm, st, W, nblob,
+                             s->Q, ld, s->w, (const double *)s->R, (const double *)s->refs,
+                             (const double *)s->ktk_rot, (const double *)s->mob_rot, s->z, part,
+                             (const double *)s->st_scal, tk, (const GmresCtl *)s->ctl));
+    GMI_CUDA_TRY(launch_step(pdl, s2_precond_blobs_kernel, dim3((nblob + kSBlobs - 1) / kSBlobs, W), dim3(kSBlobs),
+                             wsm, st, W, nblob, (const double *)s->Q, ld, (const double *)s->R,
+                             (const double *)s->refs, minv, (const double *)s->x_blobs, s->z, s->w, s->gm_rec,
+                             f64 ? 1 : 0, part, tk + 1, (const GmresCtl *)s->ctl));
     ExplicitPairEnv env{};
     env.stream = st;
     env.partial = s->gm_partial;
@@ -1172,17 +1200,21 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
         env.tt = (small || !f64) ? 1 : 2;  // FP32: the packed kernel, one target per thread
     }
     env.skip = &s->ctl->done;
+    env.pdl = pdl ? 1 : 0;
     PairConsts k;
     fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);
     int splits = 1;
     env.splits_out = &splits;  // S3 adds the split partials
     GMI_TRY(launch_pair_into(env, kBB, f64, s->gm_rec, 0, nb, s->gm_rec, nb, k, s->mbb, 0));
-    s3_finish_project_kernel<<<L.nblk, kSTpb, 0, st>>>(W, nblob, s->mbb, s->gm_partial, splits, s->z, s->R, s->refs,
-                                                       s->w, s->Q, ld, n, P, G, tk3, s->st_scal, s->H, ldh, s->ctl);
-    s4_project_norm_givens_kernel<<<L.nblk, kSTpb, 0, st>>>(s->Q, ld, n, s->w, P, G, tk4, s->st_scal, s->H, ldh,
-                                                            s->beta, s->cs, s->sn, s->ctl);
-    if (use_loop) arnoldi_loop_guard_kernel<<<1, 32, 0, st>>>(s->ctl, loop);
-    GMI_CUDA_TRY(cudaGetLastError());
+    GMI_CUDA_TRY(launch_step(pdl, s3_finish_project_kernel, dim3(L.nblk), dim3(kSTpb), 0, st, W, nblob,
+                             (const double *)s->mbb, (const double *)s->gm_partial, splits, (const double *)s->z,
+                             (const double *)s->R, (const double *)s->refs, s->w, (const double *)s->Q, ld, n, P,
+                             G, tk3, s->st_scal, s->H, ldh, (const GmresCtl *)s->ctl));
+    GMI_CUDA_TRY(launch_step(pdl, s4_project_norm_givens_kernel, dim3(L.nblk), dim3(kSTpb), 0, st,
+                             (const double *)s->Q, ld, n, s->w, P, G, tk4, s->st_scal, s->H, ldh, s->beta, s->cs,
+                             s->sn, s->ctl));
+    if (use_loop)
+        GMI_CUDA_TRY(launch_step(pdl, arnoldi_loop_guard_kernel, dim3(1), dim3(32), 0, st, s->ctl, loop));
     return GMI_OK;
 }
 
@@ -1208,10 +1240,61 @@ static gmi_status capture_step(gmi_solver *s, cudaGraph_t body, cudaGraphConditi
     return GMI_OK;
 }
 
+// Capture the Arnoldi loop (a WHILE conditional node around one step, or the
+// step alone where conditional nodes are unavailable) and instantiate it.
+static gmi_status build_arnoldi_graph(gmi_solver *s, int pidx)
+{
+    cudaGraph_t g = nullptr;
+    bool loops = false;
+    size_t body_nodes = 0;
+    // GMI_GMRES_DEVICE_LOOP=0 selects the host-replayed step graph (whose
+    // kernels profilers can attribute one by one)
+    const char *env = std::getenv("GMI_GMRES_DEVICE_LOOP");
+    const bool want_loop = !(env && env[0] == '0');
+    if (want_loop && cudaGraphCreate(&g, 0) == cudaSuccess) {
+        cudaGraphConditionalHandle h{};
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cudaGraphNode_t node;
+        bool ok = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+        if (ok) {
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
+        }
+        if (ok) {
+            cudaGraph_t body = cp.conditional.phGraph_out[0], captured = nullptr;
+            const gmi_status cst = capture_step(s, body, h, true, &captured);
+            if (cst != GMI_OK) {
+                cudaGraphDestroy(g);
+                return cst;
+            }
+            cudaGraphGetNodes(body, nullptr, &body_nodes);
+            loops = true;
+        } else {
+            cudaGraphDestroy(g);
+            g = nullptr;
+            cudaGetLastError();
+        }
+    }
+    if (!loops) GMI_TRY(capture_step(s, nullptr, cudaGraphConditionalHandle{}, false, &g));
+    const cudaError_t ie = cudaGraphInstantiate(&s->graph[pidx], g, 0);
+    size_t cnt = body_nodes;  // launches per Arnoldi step
+    if (!loops) cudaGraphGetNodes(g, nullptr, &cnt);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) s->graph[pidx] = nullptr;
+    GMI_CUDA_TRY(ie);
+    s->graph_nodes[pidx] = cnt;
+    s->graph_loops[pidx] = loops;
+    return GMI_OK;
+}
+
 // The whole Arnoldi loop as one graph: a WHILE conditional node whose body is
 // one step; the norm kernel of the step clears the condition when the solve
 // is done.  Falls back to a graph of one step, replayed in batches from the
-// host, where conditional nodes are unavailable.
+// host, where conditional nodes are unavailable, and to launches without
+// programmatic dependencies where a graph with them fails to build.
 static gmi_status ensure_arnoldi_graph(gmi_solver *s, int pidx, size_t *nodes)
 {
     cudaStream_t st = s->ctx->stream;
@@ -1220,48 +1303,15 @@ static gmi_status ensure_arnoldi_graph(gmi_solver *s, int pidx, size_t *nodes)
         return GMI_ERR_STATE;
     }
     if (s->graph[pidx] == nullptr) {
-        cudaGraph_t g = nullptr;
-        bool loops = false;
-        size_t body_nodes = 0;
-        // GMI_GMRES_DEVICE_LOOP=0 selects the host-replayed step graph (whose
-        // kernels profilers can attribute one by one)
-        const char *env = std::getenv("GMI_GMRES_DEVICE_LOOP");
-        const bool want_loop = !(env && env[0] == '0');
-        if (want_loop && cudaGraphCreate(&g, 0) == cudaSuccess) {
-            cudaGraphConditionalHandle h{};
-            cudaGraphNodeParams cp{};
-            cp.type = cudaGraphNodeTypeConditional;
-            cudaGraphNode_t node;
-            bool ok = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
-            if (ok) {
-                cp.conditional.handle = h;
-                cp.conditional.type = cudaGraphCondTypeWhile;
-                cp.conditional.size = 1;
-                ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp) == cudaSuccess;
-            }
-            if (ok) {
-                cudaGraph_t body = cp.conditional.phGraph_out[0], captured = nullptr;
-                const gmi_status cst = capture_step(s, body, h, true, &captured);
-                if (cst != GMI_OK) {
-                    cudaGraphDestroy(g);
-                    return cst;
-                }
-                cudaGraphGetNodes(body, nullptr, &body_nodes);
-                loops = true;
-            } else {
-                cudaGraphDestroy(g);
-                g = nullptr;
-                cudaGetLastError();
-            }
+        const char *pdl_env = std::getenv("GMI_PDL");
+        if (pdl_env && pdl_env[0] == '0') s->use_pdl = false;
+        gmi_status gst = build_arnoldi_graph(s, pidx);
+        if (gst != GMI_OK && s->use_pdl) {
+            cudaGetLastError();
+            s->use_pdl = false;
+            gst = build_arnoldi_graph(s, pidx);
         }
-        if (!loops) GMI_TRY(capture_step(s, nullptr, cudaGraphConditionalHandle{}, false, &g));
-        const cudaError_t ie = cudaGraphInstantiate(&s->graph[pidx], g, 0);
-        size_t cnt = body_nodes;  // launches per Arnoldi step
-        if (!loops) cudaGraphGetNodes(g, nullptr, &cnt);
-        cudaGraphDestroy(g);
-        GMI_CUDA_TRY(ie);
-        s->graph_nodes[pidx] = cnt;
-        s->graph_loops[pidx] = loops;
+        if (gst != GMI_OK) return gst;
     }
     *nodes = s->graph_nodes[pidx];
     return GMI_OK;

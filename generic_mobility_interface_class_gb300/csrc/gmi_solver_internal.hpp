@@ -42,6 +42,8 @@ struct gmi_solver {
     bool graph_loops[2] = {false, false};           // graph holds the whole device-side loop
     bool use_graphs = true;
     bool use_cluster = true;  // FP32C solves of small systems in one thread-block cluster
+    bool use_pdl = true;      // Arnoldi-step kernels launched for programmatic dependent launch (GMI_PDL=0: off;
+                              // also off if a graph with programmatic edges fails to capture or instantiate)
     double *Qr = nullptr;     // the cluster solve's row-major copy of Q (allocated by its first launch)
     PrescribedWork *prescribed = nullptr;  // allocated by the first prescribed-cilia solve
 };
