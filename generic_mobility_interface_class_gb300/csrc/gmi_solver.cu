@@ -82,28 +82,33 @@ __device__ __forceinline__ void quat_rot(const double *q, double *R)
 // body kernels
 // ---------------------------------------------------------------------------
 // R per swimmer and the 6x6 reference matrices rotated block by block,
-// Q * block * Q^T (mobility_solver.cpp:660-677).  One thread per (swimmer,
-// matrix, entry): each forms R itself and its entry's row of R * block, then
-// the entry, with the operations of the whole-block product (a warp FP64
-// instruction costs the same on one lane as on 32, so the 72 entries of a
-// swimmer take about as long as one).
+// Q * block * Q^T (mobility_solver.cpp:660-677): (K^T K)^-1 and the body
+// mobility as the reference has them, and K^T K itself (for the Arnoldi
+// step's K^T z).  One thread per (swimmer, matrix, entry): each forms R
+// itself and its entry's row of R * block, then the entry, with the
+// operations of the whole-block product (a warp FP64 instruction costs the
+// same on one lane as on 32, so the 108 entries of a swimmer take about as
+// long as one).
 __global__ void prepare_bodies_kernel(int W, const double *__restrict__ q, const double *__restrict__ ktk_ref,
-                                      const double *__restrict__ mob_ref, double *__restrict__ R,
-                                      double *__restrict__ ktk_rot, double *__restrict__ mob_rot)
+                                      const double *__restrict__ mob_ref, const double *__restrict__ ktkf_ref,
+                                      double *__restrict__ R, double *__restrict__ ktk_rot,
+                                      double *__restrict__ mob_rot, double *__restrict__ ktkf_rot)
 {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= 72 * W) return;
-    const int n = e / 72, m = (e % 72) / 36, rc = e % 36, r = rc % 6, c = rc / 6;
+    if (e >= 108 * W) return;
+    const int n = e / 108, m = (e % 108) / 36, rc = e % 36, r = rc % 6, c = rc / 6;
     double Rn[9];
     quat_rot(q + 4 * n, Rn);
     if (m == 0 && rc < 9) R[9 * n + rc] = Rn[rc];
-    const double *A = (m == 0 ? ktk_ref : mob_ref) + 3 * (r / 3) + 6 * (3 * (c / 3));  // the block, column-major
+    const double *src = m == 0 ? ktk_ref : (m == 1 ? mob_ref : ktkf_ref);
+    double *dst = m == 0 ? ktk_rot : (m == 1 ? mob_rot : ktkf_rot);
+    const double *A = src + 3 * (r / 3) + 6 * (3 * (c / 3));  // the block, column-major
     const int i = r % 3, j = c % 3;
     double T[3];  // row i of R A
 #pragma unroll
     for (int jj = 0; jj < 3; ++jj)
         T[jj] = Rn[3 * i] * A[6 * jj] + Rn[3 * i + 1] * A[1 + 6 * jj] + Rn[3 * i + 2] * A[2 + 6 * jj];
-    (m == 0 ? ktk_rot : mob_rot)[36 * n + rc] = T[0] * Rn[3 * j] + T[1] * Rn[3 * j + 1] + T[2] * Rn[3 * j + 2];
+    dst[36 * n + rc] = T[0] * Rn[3 * j] + T[1] * Rn[3 * j + 1] + T[2] * Rn[3 * j + 2];
 }
 
 // x_blob = X + R ref (rigid_body.cpp:334-352).
@@ -408,7 +413,8 @@ __global__ void scale_kernel(int n, const double *__restrict__ x, const double *
 //   S1 (CTA per 32 blobs)   w -= Q h2 (the previous S4's second pass);
 //                            q_{k-1} = w / ||w|| into Q; body moments;
 //                            last CTA: body rows of q and z_body = U
-//   S2 (CTA per 64 blobs)   z_blob; records of z; last CTA: w_body = -K^T z
+//                            w_body = -K^T z of the coming z (linearity)
+//   S2 (CTA per 64 blobs)   z_blob; records of z
 //   pair kernel on the records -> mbb, or per-split partials
 //   S3 (CTA per kSRows rows) w_blob = M_bb z - K z_body (adding the split
 //                            partials); h1 = Q^T w; last: H col = h1
@@ -519,8 +525,8 @@ constexpr int kS1Tpb = 128;
 __global__ void __launch_bounds__(kS1Tpb) s1_update_normalise_moments_kernel(
     int W, int nblob, double *__restrict__ Q, size_t ld, double *__restrict__ w,
     const double *__restrict__ R, const double *__restrict__ refs, const double *__restrict__ ktk_rot,
-    const double *__restrict__ mob_rot, double *__restrict__ z, double *__restrict__ part,
-    const double *__restrict__ scal, int *ticket, const GmresCtl *ctl)
+    const double *__restrict__ mob_rot, const double *__restrict__ ktkf_rot, double minv, double *__restrict__ z,
+    double *__restrict__ part, const double *__restrict__ scal, int *ticket, const GmresCtl *ctl)
 {
     pdl_wait_then_release();
     static_assert(kS1Tpb == 4 * 32 && kS1Blobs == 32, "S1: four warps over 32 blobs");
@@ -578,7 +584,8 @@ __global__ void __launch_bounds__(kS1Tpb) s1_update_normalise_moments_kernel(
     }
     block_sum6<kS1Tpb>(a, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
     if (!last_cta(ticket, gridDim.x * gridDim.y)) return;
-    extern __shared__ double sh[];  // 6 W
+    extern __shared__ double sh[];  // 6 W moments of q, then 6 W of z_body
+    double *zsh = sh + 6 * W;
     swimmer_sums(part, W, gridDim.x, sh);
     // body rows of q, and z_body = KTKinv_rot (-sums) - mob_rot q_body: one
     // thread per (swimmer, row), the products in two interleaved chains each
@@ -595,53 +602,62 @@ __global__ void __launch_bounds__(kS1Tpb) s1_update_normalise_moments_kernel(
             y0 += Mb[6 * j] * __ldcg(wb + j);
             y1 += Mb[6 * (j + 1)] * __ldcg(wb + j + 1);
         }
-        z[3 * nb + e] = (x0 + x1) - (y0 + y1) * inrm;
+        const double zb = (x0 + x1) - (y0 + y1) * inrm;
+        z[3 * nb + e] = zb;
+        zsh[e] = zb;
+    }
+    __syncthreads();  // every body row of w is read; z_body is complete
+    // w_body = -K^T z for the blob block z = Minv^(W-n) (q + K z_body) that
+    // S2 is about to form: by linearity -Minv^(W-n) (K^T q + (K^T K) z_body),
+    // K^T q being the moments summed above (the reference sums K^T z over
+    // the blobs of z, mobility_solver.cpp:921-940)
+    for (int e = threadIdx.x; e < 6 * W; e += kS1Tpb) {
+        const int sw = e / 6, i = e % 6;
+        const double *Kf = ktkf_rot + 36 * sw + i, *zb = zsh + 6 * sw;
+        double x0 = 0.0, x1 = 0.0;
+#pragma unroll
+        for (int j = 0; j < 6; j += 2) {
+            x0 += Kf[6 * j] * zb[j];
+            x1 += Kf[6 * (j + 1)] * zb[j + 1];
+        }
+        double v = sh[e] + (x0 + x1);
+        for (int k = sw; k < W; ++k) v *= minv;
+        w[3 * (size_t)nb + e] = -v;
     }
 }
 
-// S2: grid (ceil(nblob/kSBlobs), W).  The blob block of the preconditioner
-// is applied W - n times for swimmer n, as the reference's loop does
-// (mobility_solver.cpp:651-721).
+// S2: grid (ceil(nblob/kSBlobs), W), one thread per blob: the blob block of
+// the preconditioner, z_blob = Minv^(W-n) (q + U + Omega x (R ref)), applied
+// W - n times for swimmer n as the reference's loop does
+// (mobility_solver.cpp:651-721), and the records of z for the pair kernel.
+// (w_body = -K^T z was formed by S1 from the moments of q.)
 __global__ void __launch_bounds__(kSBlobs) s2_precond_blobs_kernel(
     int W, int nblob, const double *__restrict__ Q, size_t ld, const double *__restrict__ R,
-    const double *__restrict__ refs, double minv, const double *__restrict__ xb, double *__restrict__ z,
-    double *__restrict__ w, void *rec, int f64, double *__restrict__ part, int *ticket, const GmresCtl *ctl)
+    const double *__restrict__ refs, double minv, const double *__restrict__ xb, double *__restrict__ z, void *rec,
+    int f64, const GmresCtl *ctl)
 {
     pdl_wait_then_release();
     if (ctl->done) return;
     const int n = blockIdx.y, m = blockIdx.x * kSBlobs + threadIdx.x, nb = W * nblob;
+    if (m >= nblob) return;
     const double *in = Q + ld * (size_t)(ctl->k - 1);
     const double *U = z + 3 * nb + 6 * n;
-    double b[6] = {0, 0, 0, 0, 0, 0};
-    if (m < nblob) {
-        const size_t i = (size_t)n * nblob + m;
-        double d[3];
-        rot_apply(R + 9 * n, refs + 3 * m, d);
-        double o[3] = {in[3 * i] + U[0], in[3 * i + 1] + U[1], in[3 * i + 2] + U[2]};
-        o[0] += U[4] * d[2] - U[5] * d[1];
-        o[1] += U[5] * d[0] - U[3] * d[2];
-        o[2] += U[3] * d[1] - U[4] * d[0];
-        for (int k = n; k < W; ++k) {
-            o[0] *= minv;
-            o[1] *= minv;
-            o[2] *= minv;
-        }
-        z[3 * i] = o[0];
-        z[3 * i + 1] = o[1];
-        z[3 * i + 2] = o[2];
-        pack_record(rec, (int)i, xb + 3 * i, o, f64);
-        b[0] = o[0];
-        b[1] = o[1];
-        b[2] = o[2];
-        b[3] = d[1] * o[2] - d[2] * o[1];
-        b[4] = d[2] * o[0] - d[0] * o[2];
-        b[5] = d[0] * o[1] - d[1] * o[0];
+    const size_t i = (size_t)n * nblob + m;
+    double d[3];
+    rot_apply(R + 9 * n, refs + 3 * m, d);
+    double o[3] = {in[3 * i] + U[0], in[3 * i + 1] + U[1], in[3 * i + 2] + U[2]};
+    o[0] += U[4] * d[2] - U[5] * d[1];
+    o[1] += U[5] * d[0] - U[3] * d[2];
+    o[2] += U[3] * d[1] - U[4] * d[0];
+    for (int k = n; k < W; ++k) {
+        o[0] *= minv;
+        o[1] *= minv;
+        o[2] *= minv;
     }
-    block_sum6<kSBlobs>(b, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
-    if (!last_cta(ticket, gridDim.x * gridDim.y)) return;
-    extern __shared__ double sh[];  // 6 W
-    swimmer_sums(part, W, gridDim.x, sh);
-    for (int e = threadIdx.x; e < 6 * W; e += kSBlobs) w[3 * nb + e] = -sh[e];
+    z[3 * i] = o[0];
+    z[3 * i + 1] = o[1];
+    z[3 * i + 2] = o[2];
+    pack_record(rec, (int)i, xb + 3 * i, o, f64);
 }
 
 // Column sums out[i * ostride] = sum over b < count of p[i * stride + b],
@@ -1058,8 +1074,8 @@ static gmi_status device_norm(gmi_solver *s, const double *x, int n)
 static gmi_status prepare_bodies(gmi_solver *s)
 {
     if (s->W == 0) return GMI_OK;
-    prepare_bodies_kernel<<<grid_for(72 * s->W, 128), 128, 0, s->ctx->stream>>>(s->W, s->body_q, s->ktk_ref, s->mob_ref,
-                                                                          s->R, s->ktk_rot, s->mob_rot);
+    prepare_bodies_kernel<<<grid_for(108 * s->W, 128), 128, 0, s->ctx->stream>>>(
+        s->W, s->body_q, s->ktk_ref, s->mob_ref, s->ktkf_ref, s->R, s->ktk_rot, s->mob_rot, s->ktkf_rot);
     return launched(s);
 }
 
@@ -1115,6 +1131,27 @@ static gmi_status orthonormalise(gmi_solver *s, double *w, int k, double *Hcol)
     dot_partials_kernel<<<dim3(nc, 1), kRedTpb, 0, s->ctx->stream>>>(w, ld, w, n, nc, s->partial);
     normalize_kernel<<<grid_for(n), 256, 0, s->ctx->stream>>>(w, n, s->partial, nc, s->Q + ld * k, Hcol + k);
     return launched(s, 2);
+}
+
+// K^T K of one swimmer's blob references, column-major 6x6
+// (mobility_solver.cpp:1697-1713): K maps (U, Omega) to U + Omega x r per blob.
+static void ktk_from_refs(const double *refs, int nblob, double *KTK)
+{
+    for (int e = 0; e < 36; ++e) KTK[e] = 0.0;
+    KTK[0] = KTK[7] = KTK[14] = (double)nblob;
+    for (int m = 0; m < nblob; ++m) {
+        const double *r = refs + 3 * m;
+        // the reference's rcross(r) (matrix.cpp:665-679), row-major: rcross(r) b = b x r
+        const double rc[9] = {0.0, r[2], -r[1], -r[2], 0.0, r[0], r[1], -r[0], 0.0};
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                KTK[i + 6 * (3 + j)] += rc[3 * i + j];
+                KTK[(3 + i) + 6 * j] -= rc[3 * i + j];
+                double rr = 0.0;
+                for (int k = 0; k < 3; ++k) rr += rc[3 * i + k] * rc[3 * k + j];
+                KTK[(3 + i) + 6 * (3 + j)] -= rr;
+            }
+    }
 }
 
 // A kernel launch of the Arnoldi step; with pdl, marked for programmatic
@@ -1176,14 +1213,14 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     int *tk3 = tk + 2, *tk4 = tk3 + 1 + L.ngroups;
     const size_t wsm = 6 * (size_t)W * sizeof(double);
     const bool pdl = s->use_pdl;
-    GMI_CUDA_TRY(launch_step(pdl, s1_update_normalise_moments_kernel, dim3(L.gx, W), dim3(kS1Tpb), wsm, st, W, nblob,
-                             s->Q, ld, s->w, (const double *)s->R, (const double *)s->refs,
-                             (const double *)s->ktk_rot, (const double *)s->mob_rot, s->z, part,
-                             (const double *)s->st_scal, tk, (const GmresCtl *)s->ctl));
+    GMI_CUDA_TRY(launch_step(pdl, s1_update_normalise_moments_kernel, dim3(L.gx, W), dim3(kS1Tpb), 2 * wsm, st, W,
+                             nblob, s->Q, ld, s->w, (const double *)s->R, (const double *)s->refs,
+                             (const double *)s->ktk_rot, (const double *)s->mob_rot, (const double *)s->ktkf_rot,
+                             minv, s->z, part, (const double *)s->st_scal, tk, (const GmresCtl *)s->ctl));
     GMI_CUDA_TRY(launch_step(pdl, s2_precond_blobs_kernel, dim3((nblob + kSBlobs - 1) / kSBlobs, W), dim3(kSBlobs),
-                             wsm, st, W, nblob, (const double *)s->Q, ld, (const double *)s->R,
-                             (const double *)s->refs, minv, (const double *)s->x_blobs, s->z, s->w, s->gm_rec,
-                             f64 ? 1 : 0, part, tk + 1, (const GmresCtl *)s->ctl));
+                             0, st, W, nblob, (const double *)s->Q, ld, (const double *)s->R,
+                             (const double *)s->refs, minv, (const double *)s->x_blobs, s->z, s->gm_rec,
+                             f64 ? 1 : 0, (const GmresCtl *)s->ctl));
     ExplicitPairEnv env{};
     env.stream = st;
     env.partial = s->gm_partial;
@@ -1828,6 +1865,8 @@ gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
     TRY_OR_DIE(dalloc(s, &s->mob_ref, 36));
     TRY_OR_DIE(dalloc(s, &s->ktk_rot, 36 * W));
     TRY_OR_DIE(dalloc(s, &s->mob_rot, 36 * W));
+    TRY_OR_DIE(dalloc(s, &s->ktkf_ref, 36));
+    TRY_OR_DIE(dalloc(s, &s->ktkf_rot, 36 * W));
     TRY_OR_DIE(dalloc(s, &s->refs, 3 * (size_t)cfg->nblob));
     TRY_OR_DIE(dalloc(s, &s->sums, 6 * W));
     TRY_OR_DIE(dalloc(s, &s->kt_part, 6 * W * (size_t)((cfg->nblob + kKtBlobs - 1) / kKtBlobs)));
@@ -1988,6 +2027,9 @@ gmi_status gmi_solver_set_blob_references(gmi_solver *s, const double *refs)
     if (nblob > 0) {
         GMI_CUDA_TRY(cudaMemcpy(s->refs, refs, 3 * (size_t)nblob * sizeof(double), cudaMemcpyHostToDevice));
     }
+    double KTK[36];
+    gmi::ktk_from_refs(refs, nblob, KTK);
+    GMI_CUDA_TRY(cudaMemcpy(s->ktkf_ref, KTK, sizeof KTK, cudaMemcpyHostToDevice));
     s->refs_set = true;
     return GMI_OK;
 }
@@ -2074,21 +2116,8 @@ gmi_status solver_make_body_reference_matrices_device(gmi_solver *s, double *ktk
     std::vector<double> refs(3 * (size_t)nblob);
     if (nblob > 0)
         GMI_CUDA_TRY(cudaMemcpy(refs.data(), s->refs, refs.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    double KTK[36] = {0};
-    KTK[0] = KTK[7] = KTK[14] = (double)nblob;
-    for (int m = 0; m < nblob; ++m) {
-        const double *r = &refs[3 * m];
-        // the reference's rcross(r) (matrix.cpp:665-679), row-major: rcross(r) b = b x r
-        const double rc[9] = {0.0, r[2], -r[1], -r[2], 0.0, r[0], r[1], -r[0], 0.0};
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) {
-                KTK[i + 6 * (3 + j)] += rc[3 * i + j];
-                KTK[(3 + i) + 6 * j] -= rc[3 * i + j];
-                double rr = 0.0;
-                for (int k = 0; k < 3; ++k) rr += rc[3 * i + k] * rc[3 * k + j];
-                KTK[(3 + i) + 6 * (3 + j)] -= rr;
-            }
-    }
+    double KTK[36];
+    ktk_from_refs(refs.data(), nblob, KTK);
     double KTKinv[36];
     if (!invert6(KTK, KTKinv)) {
         set_last_error_msg("K^T K is singular (are the blob references set?)");

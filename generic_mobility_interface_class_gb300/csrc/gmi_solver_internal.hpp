@@ -20,6 +20,7 @@ struct gmi_solver {
     double *x_blobs = nullptr, *f_blobs = nullptr, *v_blobs = nullptr, *f_rep = nullptr;
     double *body_x = nullptr, *body_q = nullptr, *body_f = nullptr, *v_bodies = nullptr;
     double *R = nullptr, *ktk_ref = nullptr, *mob_ref = nullptr, *ktk_rot = nullptr, *mob_rot = nullptr;
+    double *ktkf_ref = nullptr, *ktkf_rot = nullptr;  // K^T K itself (not inverted), reference and rotated
     double *refs = nullptr, *sums = nullptr, *kt_part = nullptr;  // K^T sums and their per-CTA partials
     double *rhs = nullptr, *soln = nullptr, *Q = nullptr, *H = nullptr, *beta = nullptr, *cs = nullptr, *sn = nullptr;
     double *z = nullptr, *w = nullptr, *tmp = nullptr, *mbb = nullptr, *partial = nullptr, *yv = nullptr;
