@@ -1232,9 +1232,12 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
         env.tpb = kPairWarpShapeTpb;  // warp per two target blobs
         env.tt = 2;
     } else {
+        // FP32: the packed kernel, 128 targets per CTA (at 4096 blobs, with
+        // 32 source splits of one tile each, 22 us against 24.5 us for 64);
+        // FP64: smaller CTAs for small target sets
         const bool small = (long long)nb * 2 < (long long)ctx->sm_count * 256;
-        env.tpb = small ? 64 : 128;
-        env.tt = (small || !f64) ? 1 : 2;  // FP32: the packed kernel, one target per thread
+        env.tpb = (small && f64) ? 64 : 128;
+        env.tt = (small || !f64) ? 1 : 2;
     }
     env.skip = &s->ctl->done;
     env.pdl = pdl ? 1 : 0;
