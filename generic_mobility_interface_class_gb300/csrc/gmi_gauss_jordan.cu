@@ -35,8 +35,10 @@ namespace cg = cooperative_groups;
 
 namespace gmi {
 
-constexpr int kGjTpb = 512;  // 16 warps: four per scheduler keep the FP64 unit busy
+constexpr int kGjTpb = 512;  // one CTA per matrix: 16 warps, four per scheduler keep the FP64 unit busy
 constexpr int kGjWarps = kGjTpb / 32;
+constexpr int kGcTpb = 256;  // cluster kernel: 8 warps per CTA (few columns each; a step is latency-bound)
+constexpr int kGcWarps = kGcTpb / 32;
 
 // Warp-wide pivot of column Ac (global column index c) among rows i >= c.
 // Writes the step's multiplier column ncol[i] = -A'(i, c) / pivot, A' the
@@ -134,18 +136,18 @@ static __device__ __forceinline__ void gj_cols(double *A, int n, int j0, const i
 }
 
 // Step k on the ncl columns at A (local column jl is global column j0 + jl),
-// warp wid taking columns wid, wid + 16, ...: the owner of column k + 1
+// warp wid taking columns wid, wid + NW, ...: the owner of column k + 1
 // eliminates it first and then searches it for the next pivot.  RPL > 0:
 // rows in registers (n <= 32 RPL), several columns at a time; RPL == 0: any
 // n, one column at a time through shared memory.
-template <int RPL>
+template <int RPL, int NW>
 static __device__ __forceinline__ void gj_step(double *A, int n, int ncl, int j0, int k, int p, double pivinv,
                                                const double *nc, double *next_ncol, double *next_pinv,
                                                int *next_piv, int wid, int lane)
 {
     const int la = k + 1 - j0;
-    const int T = (ncl > wid) ? (ncl - wid + kGjWarps - 1) / kGjWarps : 0;
-    const bool own_la = k + 1 < n && la >= 0 && la < ncl && la % kGjWarps == wid;
+    const int T = (ncl > wid) ? (ncl - wid + NW - 1) / NW : 0;
+    const bool own_la = k + 1 < n && la >= 0 && la < ncl && la % NW == wid;
     if constexpr (RPL > 0) {
         double ncr[RPL];
 #pragma unroll
@@ -170,7 +172,7 @@ static __device__ __forceinline__ void gj_step(double *A, int n, int ncl, int j0
             for (int c = 0; c < C; ++c) {
                 int jl = -1;
                 while (jl < 0 && t < T) {
-                    const int cand = wid + kGjWarps * t++;
+                    const int cand = wid + NW * t++;
                     if (!(own_la && cand == la)) jl = cand;
                 }
                 jj[c] = jl < 0 ? 0 : jl;
@@ -179,10 +181,10 @@ static __device__ __forceinline__ void gj_step(double *A, int n, int ncl, int j0
             if (cnt > 0) gj_cols<RPL>(A, n, j0, jj, cnt, k, p, pivinv, ncr, lane);
         }
     } else {
-        const int t0 = own_la ? la / kGjWarps : 0;
+        const int t0 = own_la ? la / NW : 0;
         for (int tt = 0; tt < T; ++tt) {
             const int t = (tt + t0 < T) ? tt + t0 : tt + t0 - T;
-            const int jl = wid + kGjWarps * t;
+            const int jl = wid + NW * t;
             double *Aj = A + (size_t)n * jl;
             if (j0 + jl == k) {
                 for (int i = lane; i < n; i += 32) Aj[i] = (i == k) ? pivinv : nc[i];
@@ -241,7 +243,7 @@ __global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, 
             if (tid == 0) atomicOr(flags + 2, 1);
             return;
         }
-        gj_step<RPL>(A, n, n, 0, k, p, pinv[par], ncol + par * (size_t)n, ncol + (par ^ 1) * (size_t)n,
+        gj_step<RPL, kGjWarps>(A, n, n, 0, k, p, pinv[par], ncol + par * (size_t)n, ncol + (par ^ 1) * (size_t)n,
                 pinv + (par ^ 1), perm + k + 1, wid, lane);
         __syncthreads();
     }
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, 
 // found them during the previous step) and runs the step on its columns.
 // The inverse is gathered at the end straight from the CTAs' shared memory.
 template <int RPL>
-__global__ void __launch_bounds__(kGjTpb) gj_cluster_kernel(double *mats, int n, int nc, int *flags)
+__global__ void __launch_bounds__(kGcTpb) gj_cluster_kernel(double *mats, int n, int nc, int *flags)
 {
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), r = (int)cl.block_rank(), tid = threadIdx.x;
@@ -287,7 +289,7 @@ __global__ void __launch_bounds__(kGjTpb) gj_cluster_kernel(double *mats, int n,
     int *piv = reinterpret_cast<int *>(pv + 2);       // [2], published
     int *pk = piv + 2;                                // [2]: this step's pivot row
     int *perm = pk + 2;                               // [n]
-    for (int e = tid; e < n * ncl; e += kGjTpb) A[e] = Mg[(size_t)n * j0 + e];
+    for (int e = tid; e < n * ncl; e += kGcTpb) A[e] = Mg[(size_t)n * j0 + e];
     __syncthreads();
     if (r == 0 && wid == 0) gj_pivot_warp(A, n, 0, ncol, pinv, piv, lane);
     bool singular = false;
@@ -295,7 +297,7 @@ __global__ void __launch_bounds__(kGjTpb) gj_cluster_kernel(double *mats, int n,
         const int owner = k / nc, par = k & 1;
         cl.sync();  // step k's pivot is published, and step k - 1 is done everywhere
         const double *src = cl.map_shared_rank(ncol, owner) + par * (size_t)n;
-        for (int i = tid; i < n; i += kGjTpb) cur[i] = src[i];
+        for (int i = tid; i < n; i += kGcTpb) cur[i] = src[i];
         if (tid == 0) {
             pk[0] = cl.map_shared_rank(piv, owner)[par];
             pv[0] = cl.map_shared_rank(pinv, owner)[par];
@@ -307,8 +309,8 @@ __global__ void __launch_bounds__(kGjTpb) gj_cluster_kernel(double *mats, int n,
             singular = true;
             break;
         }
-        gj_step<RPL>(A, n, ncl, j0, k, p, pv[0], cur, ncol + (par ^ 1) * (size_t)n, pinv + (par ^ 1), piv + (par ^ 1),
-                wid, lane);
+        gj_step<RPL, kGcWarps>(A, n, ncl, j0, k, p, pv[0], cur, ncol + (par ^ 1) * (size_t)n, pinv + (par ^ 1),
+                               piv + (par ^ 1), wid, lane);
     }
     if (singular) {
         if (r == 0 && tid == 0) atomicOr(flags + 2, 1);
@@ -318,7 +320,7 @@ __global__ void __launch_bounds__(kGjTpb) gj_cluster_kernel(double *mats, int n,
     int *where = reinterpret_cast<int *>(cur);
     if (tid == 0) gj_unpivot_map(perm, n, where);
     cl.sync();  // the last step is done in every CTA
-    for (int jl = wid; jl < ncl; jl += kGjWarps) {
+    for (int jl = wid; jl < ncl; jl += kGcWarps) {
         const int w = where[j0 + jl];
         const double *srcc = cl.map_shared_rank(A, w / nc) + (size_t)n * (w % nc);
         for (int i = lane; i < n; i += 32) Mg[(size_t)n * (j0 + jl) + i] = srcc[i];
@@ -356,7 +358,7 @@ static gmi_status gj_launch(cudaStream_t stream, double *mats, int nmat, int n, 
             attr[0].val.clusterDim.y = 1;
             attr[0].val.clusterDim.z = 1;
             cfg.gridDim = dim3(nmat * csize);
-            cfg.blockDim = dim3(kGjTpb);
+            cfg.blockDim = dim3(kGcTpb);
             cfg.dynamicSmemBytes = smem;
             cfg.stream = stream;
             cfg.attrs = attr;
