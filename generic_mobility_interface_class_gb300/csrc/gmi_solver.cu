@@ -373,11 +373,13 @@ __global__ void givens_kernel(double *__restrict__ H, int ldh, double *__restric
 }
 
 // out = sum_i y_i Q[:, i], in the reference's column order (mobility_solver.cpp:1252-1255).
+// (with ctl, k is the solve's iteration count on the device, ctl->k)
 __global__ void combine_kernel(const double *__restrict__ Q, size_t ld, const double *__restrict__ y, int k, int n,
-                               double *__restrict__ out)
+                               double *__restrict__ out, const GmresCtl *ctl)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
+    if (ctl != nullptr) k = ctl->k;
     double acc = 0.0;
     for (int i = 0; i < k; ++i) acc += y[i] * Q[ld * i + r];
     out[r] = acc;
@@ -977,11 +979,12 @@ __global__ void arnoldi_loop_guard_kernel(GmresCtl *ctl, cudaGraphConditionalHan
 // column's step on the serial chain is one multiply and one FMA; the row
 // blocks below the column (nothing left to update) are skipped warp-wide.
 __global__ void backsolve_warp_kernel(const double *__restrict__ H, int ldh, const double *__restrict__ beta,
-                                      int iter, double *__restrict__ y)
+                                      int iter, double *__restrict__ y, const GmresCtl *ctl)
 {
     constexpr int kPer = (kFMaxK + 31) / 32;
     __shared__ double b[kFMaxK], rd[kFMaxK];
     const int lane = threadIdx.x;
+    if (ctl != nullptr) iter = min(ctl->k, kFMaxK - 1);  // the solve's count, read on the device
     for (int i = lane; i < iter; i += 32) {
         b[i] = beta[i];
         rd[i] = 1.0 / H[i + (size_t)ldh * i];
@@ -1364,7 +1367,7 @@ static gmi_status ensure_arnoldi_graph(gmi_solver *s, int pidx, size_t *nodes)
 // ||b|| is replaced by zero (mobility_solver.cpp:1149-1156).  zero_start
 // skips the initial residual apply (x0 = 0, r0 = b, ||b|| = norm_b).
 static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, double tol, bool reject_warm_start,
-                            bool zero_start, int *iters_out)
+                            bool zero_start, int *iters_out, bool defer = false)
 {
     const int n = s->n;
     const size_t ld = (size_t)n;
@@ -1395,6 +1398,10 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
     size_t nodes = 0;
     const bool cluster = s->use_cluster && max_iter >= 1 && cluster_gmres_usable(s);
     if (!cluster && s->use_graphs && ensure_arnoldi_graph(s, pidx, &nodes) != GMI_OK) s->use_graphs = false;
+    // defer: the solve's control block is checked at the caller's next
+    // synchronisation (gmres_finish_pending) instead of here, and the
+    // epilogue reads the iteration count on the device
+    bool deferred = false;
     if (cluster) {
         GmresCtl c{};
         c.k = 1;
@@ -1404,11 +1411,16 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
         *s->h_ctl = c;
         GMI_CUDA_TRY(cudaMemcpyAsync(s->ctl, s->h_ctl, sizeof c, cudaMemcpyHostToDevice, st));
         GMI_TRY(cluster_gmres_launch(s, beta0, norm_ref, tol, max_iter));
-        GMI_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->ctl, sizeof c, cudaMemcpyDeviceToHost, st));
-        GMI_CUDA_TRY(cudaStreamSynchronize(st));
-        if (!s->h_ctl->done) {
-            set_last_error_msg("cluster GMRES solve ended without completion");
-            return GMI_ERR_STATE;
+        if (defer) {
+            deferred = true;
+            s->ctl_pending_nodes = 0;
+        } else {
+            GMI_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->ctl, sizeof c, cudaMemcpyDeviceToHost, st));
+            GMI_CUDA_TRY(cudaStreamSynchronize(st));
+            if (!s->h_ctl->done) {
+                set_last_error_msg("cluster GMRES solve ended without completion");
+                return GMI_ERR_STATE;
+            }
         }
     }
     if (cluster || s->use_graphs) {
@@ -1428,12 +1440,17 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
         int batch = 4, replayed = 0;
         if (s->graph_loops[pidx]) {
             GMI_CUDA_TRY(cudaGraphLaunch(s->graph[pidx], st));
-            GMI_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->ctl, sizeof c, cudaMemcpyDeviceToHost, st));
-            GMI_CUDA_TRY(cudaStreamSynchronize(st));
-            s->ctx->launches += (long long)s->h_ctl->guard * (long long)nodes;
-            if (!s->h_ctl->done) {
-                set_last_error_msg("GMRES loop ended without completion");
-                return GMI_ERR_STATE;
+            if (defer) {
+                deferred = true;
+                s->ctl_pending_nodes = (long long)nodes;
+            } else {
+                GMI_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->ctl, sizeof c, cudaMemcpyDeviceToHost, st));
+                GMI_CUDA_TRY(cudaStreamSynchronize(st));
+                s->ctx->launches += (long long)s->h_ctl->guard * (long long)nodes;
+                if (!s->h_ctl->done) {
+                    set_last_error_msg("GMRES loop ended without completion");
+                    return GMI_ERR_STATE;
+                }
             }
         }
         for (; !s->graph_loops[pidx];) {
@@ -1450,18 +1467,27 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
             batch = batch * 2 < 32 ? batch * 2 : 32;
         }
       }
-        if (!std::isfinite(s->h_ctl->resid)) {
-            set_last_error_msg("GMRES produced a non-finite residual");
-            return GMI_ERR_NONFINITE;
+        if (deferred) {
+            backsolve_warp_kernel<<<1, 32, 0, st>>>(s->H, ldh, s->beta, 0, s->yv, s->ctl);
+            combine_kernel<<<grid_for(n, 64), 64, 0, st>>>(s->Q, ld, s->yv, 0, n, s->tmp, s->ctl);
+        } else {
+            if (!std::isfinite(s->h_ctl->resid)) {
+                set_last_error_msg("GMRES produced a non-finite residual");
+                return GMI_ERR_NONFINITE;
+            }
+            const int iter = s->h_ctl->k;
+            backsolve_warp_kernel<<<1, 32, 0, st>>>(s->H, ldh, s->beta, iter, s->yv, nullptr);
+            combine_kernel<<<grid_for(n, 64), 64, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp, nullptr);
+            *iters_out = iter;
         }
-        const int iter = s->h_ctl->k;
-        backsolve_warp_kernel<<<1, 32, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
-        combine_kernel<<<grid_for(n, 64), 64, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
         GMI_TRY(launched(s, 2));
         GMI_TRY(apply_preconditioner(s, s->tmp, s->z));
         axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->soln, 1.0, s->z, s->soln);
         GMI_TRY(launched(s));
-        *iters_out = iter;
+        if (deferred) {
+            GMI_CUDA_TRY(cudaMemcpyAsync(s->h_ctl, s->ctl, sizeof(GmresCtl), cudaMemcpyDeviceToHost, st));
+            s->ctl_pending = true;
+        }
         return GMI_OK;
     }
     GMI_CUDA_TRY(cudaMemcpyAsync(s->scal, s->h_stage, sizeof(double), cudaMemcpyHostToDevice, st));
@@ -1481,8 +1507,8 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
             return GMI_ERR_NONFINITE;
         }
         if (resid <= tol || iter == max_iter) {
-            backsolve_warp_kernel<<<1, 32, 0, st>>>(s->H, ldh, s->beta, iter, s->yv);
-            combine_kernel<<<grid_for(n, 64), 64, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp);
+            backsolve_warp_kernel<<<1, 32, 0, st>>>(s->H, ldh, s->beta, iter, s->yv, nullptr);
+            combine_kernel<<<grid_for(n, 64), 64, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp, nullptr);
             GMI_TRY(launched(s, 2));
             GMI_TRY(apply_preconditioner(s, s->tmp, s->z));
             axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->soln, 1.0, s->z, s->soln);
@@ -1491,6 +1517,26 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
             return GMI_OK;
         }
     }
+    return GMI_OK;
+}
+
+// The checks of a deferred GMRES solve (gmres_run with defer), once the
+// stream has been synchronised: completion, a finite residual, and its
+// iteration count added to *iters.
+static gmi_status gmres_finish_pending(gmi_solver *s, int *iters)
+{
+    if (!s->ctl_pending) return GMI_OK;
+    s->ctl_pending = false;
+    s->ctx->launches += (long long)s->h_ctl->guard * s->ctl_pending_nodes;
+    if (!s->h_ctl->done) {
+        set_last_error_msg("GMRES solve ended without completion");
+        return GMI_ERR_STATE;
+    }
+    if (!std::isfinite(s->h_ctl->resid)) {
+        set_last_error_msg("GMRES produced a non-finite residual");
+        return GMI_ERR_NONFINITE;
+    }
+    *iters += s->h_ctl->k;
     return GMI_OK;
 }
 
@@ -1533,22 +1579,32 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
     const double tol = s->cfg.linear_tol;
     cudaStream_t st = s->ctx->stream;
     *iters_out = 0;
-    GMI_TRY(device_norm(s, s->rhs, n));
-    double norm_rhs;
-    GMI_TRY(read_scalar(s, s->scal, &norm_rhs));
-    if (!std::isfinite(norm_rhs)) {
-        set_last_error_msg("non-finite right-hand side in the linear solve");
-        return GMI_ERR_NONFINITE;
-    }
-    if (norm_rhs == 0.0) {
-        GMI_CUDA_TRY(cudaMemsetAsync(s->f_blobs, 0, 3 * (size_t)nb * sizeof(double), st));
-        GMI_CUDA_TRY(cudaMemsetAsync(s->v_bodies, 0, 6 * (size_t)s->W * sizeof(double), st));
+    const int prec = s->ctx->precision;
+    auto check_rhs = [&](double norm) -> gmi_status {
+        if (!std::isfinite(norm)) {
+            set_last_error_msg("non-finite right-hand side in the linear solve");
+            return GMI_ERR_NONFINITE;
+        }
         return GMI_OK;
+    };
+    GMI_TRY(device_norm(s, s->rhs, n));
+    double norm_rhs = 0.0;
+    if (prec == GMI_FP64) {
+        GMI_TRY(read_scalar(s, s->scal, &norm_rhs));
+        GMI_TRY(check_rhs(norm_rhs));
+        if (norm_rhs == 0.0) {
+            GMI_CUDA_TRY(cudaMemsetAsync(s->f_blobs, 0, 3 * (size_t)nb * sizeof(double), st));
+            GMI_CUDA_TRY(cudaMemsetAsync(s->v_bodies, 0, 6 * (size_t)s->W * sizeof(double), st));
+            return GMI_OK;
+        }
+    } else {
+        // the mixed path reads ||b|| together with its first residual norm
+        // (one host round trip for both), from scal[2]
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->scal + 2, s->scal, sizeof(double), cudaMemcpyDeviceToDevice, st));
     }
     GMI_CUDA_TRY(cudaMemcpyAsync(s->soln, s->f_blobs, 3 * (size_t)nb * sizeof(double), cudaMemcpyDeviceToDevice, st));
     GMI_CUDA_TRY(cudaMemcpyAsync(s->soln + 3 * nb, s->v_bodies, 6 * (size_t)s->W * sizeof(double),
                                  cudaMemcpyDeviceToDevice, st));
-    const int prec = s->ctx->precision;
     if (prec == GMI_FP64) {
         int iters = 0;
         GMI_TRY(gmres_run(s, norm_rhs, norm_rhs, tol, true, false, &iters));
@@ -1582,7 +1638,22 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         }
         GMI_TRY(device_norm(s, s->rhs, n));
         double beta;
-        GMI_TRY(read_scalar(s, s->scal, &beta));
+        if (outer == 0) {  // ||r|| and ||b|| in one read
+            GMI_CUDA_TRY(cudaMemcpyAsync(s->h_stage, s->scal, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            GMI_CUDA_TRY(cudaStreamSynchronize(st));
+            beta = s->h_stage[0];
+            norm_rhs = s->h_stage[2];
+            GMI_TRY(check_rhs(norm_rhs));
+            if (norm_rhs == 0.0) {
+                GMI_CUDA_TRY(cudaMemcpyAsync(s->rhs, s->b64, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
+                GMI_CUDA_TRY(cudaMemsetAsync(s->f_blobs, 0, 3 * (size_t)nb * sizeof(double), st));
+                GMI_CUDA_TRY(cudaMemsetAsync(s->v_bodies, 0, 6 * (size_t)s->W * sizeof(double), st));
+                return GMI_OK;
+            }
+        } else {
+            GMI_TRY(read_scalar(s, s->scal, &beta));
+        }
+        GMI_TRY(gmres_finish_pending(s, &total));  // the previous correction's solve
         if (!std::isfinite(beta)) {
             set_last_error_msg("non-finite residual in the refinement loop");
             return GMI_ERR_NONFINITE;
@@ -1598,12 +1669,16 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         const double want = kInnerMargin * tol * norm_rhs / beta;
         const double inner_tol = want > inner_floor ? want : inner_floor;
         int iters = 0;
-        GMI_TRY(gmres_run(s, beta, beta, inner_tol, false, true, &iters));
-        total += iters;
+        GMI_TRY(gmres_run(s, beta, beta, inner_tol, false, true, &iters, true));
+        total += iters;  // zero when the solve is deferred (counted at the next synchronisation)
         // keep the correction for the residual update, then accumulate it
         GMI_CUDA_TRY(cudaMemcpyAsync(s->z, s->soln, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
         axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->xacc, 1.0, s->soln, s->soln);
         GMI_TRY(launched(s));
+    }
+    if (s->ctl_pending) {  // the refinement cap ended the loop after a solve
+        GMI_CUDA_TRY(cudaStreamSynchronize(st));
+        GMI_TRY(gmres_finish_pending(s, &total));
     }
     GMI_CUDA_TRY(cudaMemcpyAsync(s->rhs, s->b64, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
     *iters_out = total;

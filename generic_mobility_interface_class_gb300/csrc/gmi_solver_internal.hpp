@@ -31,6 +31,8 @@ struct gmi_solver {
     // device-controlled Arnoldi iterations replayed from a CUDA graph
     struct GmresCtl *ctl = nullptr;   // device control block
     struct GmresCtl *h_ctl = nullptr; // pinned mirror
+    bool ctl_pending = false;          // a GMRES solve's control block is on its way to h_ctl, unchecked
+    long long ctl_pending_nodes = 0;   // launches per pass of that solve's device loop (0: cluster kernel)
     void *gm_rec = nullptr;           // blob records of the GMRES operator (own buffer: fixed address)
     size_t partial_count = 0;         // doubles in partial
     double *st_scal = nullptr;        // Arnoldi step scalars: projections h, ||w||
