@@ -17,8 +17,9 @@
 //   A  q = w / ||w|| into Q[:, k-1]; body moments of q  -> barrier 1
 //      z_body from the summed moments (every CTA)
 //   B  blob block of the preconditioner; the CTA's blob loads (z, FP32,
-//      pair-interleaved) into its shared memory; moments of z  -> barrier 2
-//      copy the other CTAs' loads; w_body = -K^T z (last CTA)
+//      pair-interleaved) into its shared memory  -> barrier 2
+//      copy the other CTAs' loads; w_body = -K^T z by linearity from the
+//      moments of q and K^T K (last CTA)
 //   C  blob-blob RPY sum over all blobs, packed FP32 (gmi_pairs2.cuh), from
 //      shared memory; meanwhile one reserved warp finishes the Givens step
 //      of iteration k-1, whose stop flag is read right after this phase
@@ -63,7 +64,7 @@ struct ClusterGmresArgs {
     int ldr;
     int kq, kqs;                      // basis columns [0, kq) of the CTA's rows cached in shared memory, row stride kqs
     const double *w0;                 // r0, all n rows
-    const double *R, *refs, *ktk_rot, *mob_rot, *xb;
+    const double *R, *refs, *ktk_rot, *mob_rot, *ktkf_rot, *xb;
     double minv, beta0, tol, norm_ref;
     GmresCtl *ctl;
     EqualK<float> kbb;
@@ -71,7 +72,7 @@ struct ClusterGmresArgs {
 
 // Shared-memory layout (offsets in bytes), fixed by nb, W and bpc.
 struct CgLayout {
-    size_t ipos, iload, wl, ql, av, dl, kt, mb, mom1, mom2, sums, zb, hp1, hp2, h, h2, np, pp, csh, snh, bet,
+    size_t ipos, iload, wl, ql, av, dl, kt, mb, kf, mom1, sums, zb, hp1, hp2, h, h2, np, pp, csh, snh, bet,
         col, red, flag, qs, total;
 };
 
@@ -93,8 +94,8 @@ __host__ __device__ inline CgLayout cg_layout(int nb, int W, int bpc, int kqs = 
     L.dl = take((size_t)bpc * 3 * sizeof(double));  // R refs of the CTA's blobs
     L.kt = take(36 * (size_t)W * sizeof(double));
     L.mb = take(36 * (size_t)W * sizeof(double));
+    L.kf = take(36 * (size_t)W * sizeof(double));  // K^T K itself, rotated
     L.mom1 = take(6 * (size_t)W * sizeof(double));
-    L.mom2 = take(6 * (size_t)W * sizeof(double));
     L.sums = take(6 * (size_t)W * sizeof(double));
     L.zb = take(6 * (size_t)W * sizeof(double));
     L.hp1 = take((kCgMaxK + 1) * sizeof(double));
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
     double *wl = reinterpret_cast<double *>(sm + L.wl), *ql = reinterpret_cast<double *>(sm + L.ql);
     double *av = reinterpret_cast<double *>(sm + L.av), *dl = reinterpret_cast<double *>(sm + L.dl);
     double *kt = reinterpret_cast<double *>(sm + L.kt), *mb = reinterpret_cast<double *>(sm + L.mb);
-    double *mom1 = reinterpret_cast<double *>(sm + L.mom1), *mom2 = reinterpret_cast<double *>(sm + L.mom2);
+    double *mom1 = reinterpret_cast<double *>(sm + L.mom1), *kf = reinterpret_cast<double *>(sm + L.kf);
     double *sums = reinterpret_cast<double *>(sm + L.sums), *zb = reinterpret_cast<double *>(sm + L.zb);
     double *hp1 = reinterpret_cast<double *>(sm + L.hp1), *hp2 = reinterpret_cast<double *>(sm + L.hp2);
     double *h = reinterpret_cast<double *>(sm + L.h), *h2 = reinterpret_cast<double *>(sm + L.h2);
@@ -218,6 +219,7 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
     for (int e = tid; e < 36 * W; e += kCgTpb) {
         kt[e] = a.ktk_rot[e];
         mb[e] = a.mob_rot[e];
+        kf[e] = a.ktkf_rot[e];
     }
     for (int p = tid; p < npairs; p += kCgTpb) {
         float hp[2][3], lp[2][3];
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
             zb[e] = x - y;
         }
         __syncthreads();
-        // ---- B: blob preconditioner, loads, moments of z -------------------
+        // ---- B: blob preconditioner, loads, w_body -------------------------
         // per (blob, component): z = the blob block applied to q + U + U_rot x (R ref)
         for (int e = tid; e < 3 * bl; e += kCgTpb) {
             const int t = e / 3, cc = e % 3, i1 = (cc + 1) % 3, i2 = (cc + 2) % 3;
@@ -311,16 +313,7 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
             for (int q = sw; q < W; ++q) o *= a.minv;
             float *ld = reinterpret_cast<float *>(iload + 2 * (i >> 1));
             ld[cc == 0 ? (i & 1) : (cc == 1 ? 2 + (i & 1) : 4 + (i & 1))] = (float)o * load_scale;
-            av[6 * t + cc] = o;
         }
-        __syncthreads();
-        for (int e = tid; e < 3 * bl; e += kCgTpb) {  // (R ref) x z
-            const int t = e / 3, cc = e % 3, i1 = (cc + 1) % 3, i2 = (cc + 2) % 3;
-            const double *d = dl + 3 * t, *o = av + 6 * t;
-            av[6 * t + 3 + cc] = d[i1] * o[i2] - d[i2] * o[i1];
-        }
-        __syncthreads();
-        swimmer_moments(av, W, nblob, b0, bl, mom2);
         cl.sync();  // barrier 2
         // the other CTAs' loads (bpc is even: a source pair has one owner)
         for (int e = tid; e < 2 * npairs; e += kCgTpb) {
@@ -328,9 +321,22 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
             if (owner != c) iload[e] = cl.map_shared_rank(iload, owner)[e];
         }
         if (c == C - 1) {
-            cluster_reduce(cl, mom2, nw6, sums, C, G);
-            __syncthreads();
-            for (int e = tid; e < nw6; e += kCgTpb) wl[3 * bl + e] = -sums[e];  // w body rows = -K^T z
+            // w body rows = -K^T z for z = Minv^(W-n) (q + K z_body): by
+            // linearity -Minv^(W-n) (K^T q + (K^T K) z_body), K^T q being
+            // phase A's summed moments (still in sums)
+            for (int e = tid; e < nw6; e += kCgTpb) {
+                const int sw = e / 6, i = e % 6;
+                const double *Kf = kf + 36 * sw + i, *zz = zb + 6 * sw;
+                double x0 = 0.0, x1 = 0.0;
+#pragma unroll
+                for (int j = 0; j < 6; j += 2) {
+                    x0 += Kf[6 * j] * zz[j];
+                    x1 += Kf[6 * (j + 1)] * zz[j + 1];
+                }
+                double v = sums[e] + (x0 + x1);
+                for (int q = sw; q < W; ++q) v *= a.minv;
+                wl[3 * bl + e] = -v;
+            }
         }
         __syncthreads();
         // ---- C: blob-blob sum (packed FP32); Givens step of iteration k-1 ---
@@ -652,6 +658,7 @@ gmi_status cluster_gmres_launch(gmi_solver *s, double beta0, double norm_ref, do
     a.refs = s->refs;
     a.ktk_rot = s->ktk_rot;
     a.mob_rot = s->mob_rot;
+    a.ktkf_rot = s->ktkf_rot;
     a.xb = s->x_blobs;
     a.minv = 6.0 * kPi * s->cfg.mu * s->cfg.rblob;
     a.beta0 = beta0;
