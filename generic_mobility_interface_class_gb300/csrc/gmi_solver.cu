@@ -127,8 +127,8 @@ __global__ void blob_positions_kernel(int W, int nblob, const double *__restrict
 
 // Per swimmer: sums[6n..] = (sum_m f_m, sum_m (R ref_m) x f_m) over its blobs.
 // This is K^T f (mobility_solver.cpp:690-697, 921-940, 168-188), in two
-// passes: kKtBlobs blobs per CTA into part[(n gx + x) 6 + c], then the CTA
-// partials added per (swimmer, component) in a fixed order.
+// passes of kt_kernel: kKtBlobs blobs per CTA into part[(n gx + x) 6 + c],
+// then the CTA partials added per (swimmer, component) in a fixed order.
 constexpr int kKtBlobs = 128;
 
 // Block sum of six per-thread values, in a fixed order: threads 0..5 write
@@ -146,40 +146,6 @@ template <int TPB> __device__ __forceinline__ void block_sum6(const double *v, d
         for (int w = 0; w < TPB / 32; ++w) s += red[w][threadIdx.x];
         out[threadIdx.x] = s;
     }
-}
-
-__global__ void __launch_bounds__(kKtBlobs) kt_partial_kernel(int nblob, const double *__restrict__ R,
-                                                             const double *__restrict__ refs,
-                                                             const double *__restrict__ f, double *__restrict__ part)
-{
-    const int n = blockIdx.y, m = blockIdx.x * kKtBlobs + threadIdx.x;
-    double a[6] = {0, 0, 0, 0, 0, 0};
-    if (m < nblob) {
-        const double *fm = f + 3 * ((size_t)n * nblob + m);
-        double d[3];
-        rot_apply(R + 9 * n, refs + 3 * m, d);
-        a[0] = fm[0];
-        a[1] = fm[1];
-        a[2] = fm[2];
-        a[3] = d[1] * fm[2] - d[2] * fm[1];
-        a[4] = d[2] * fm[0] - d[0] * fm[2];
-        a[5] = d[0] * fm[1] - d[1] * fm[0];
-    }
-    block_sum6<kKtBlobs>(a, part + ((size_t)n * gridDim.x + blockIdx.x) * 6);
-}
-
-// One warp per swimmer: the lanes stride over the CTA partials, then one
-// six-value warp sum.
-__global__ void kt_finish_kernel(int W, int gx, const double *__restrict__ part, double *__restrict__ sums)
-{
-    const int lane = threadIdx.x & 31, n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (n >= W) return;
-    double a[6] = {0, 0, 0, 0, 0, 0};
-    for (int x = lane; x < gx; x += 32)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) a[c] += part[((size_t)n * gx + x) * 6 + c];
-    const double t = warp_sum6_scatter(a);
-    if ((lane & 3) == 0 && lane < 24) sums[6 * n + (lane >> 2)] = t;
 }
 
 // body_f += sums (the blob repulsion's force and torque on each body).
@@ -329,14 +295,6 @@ __global__ void normalize_kernel(const double *__restrict__ w, int n, const doub
     if (r < n) q_out[r] = nrm > 0.0 ? w[r] / nrm : 0.0;
 }
 
-// sqrt of the summed partials into out[0] (norms of single vectors).
-__global__ void finish_norm_kernel(const double *__restrict__ partial, int nchunks, double *__restrict__ out)
-{
-    double s = 0.0;
-    for (int c = 0; c < nchunks; ++c) s += partial[c];
-    out[0] = sqrt(s);
-}
-
 // One Givens step of solve_linear_system (mobility_solver.cpp:1189-1231) on
 // column iter-1; writes |beta(iter)| / norm_rhs to *resid.
 __global__ void givens_kernel(double *__restrict__ H, int ldh, double *__restrict__ beta, double *__restrict__ cs,
@@ -456,6 +414,62 @@ __device__ __forceinline__ bool last_cta(int *ticket, int total)
     }
     __syncthreads();
     return is_last;
+}
+
+// ||x|| into *out in one launch: CTA c sums the squares of rows
+// [c kChunkRows, (c + 1) kChunkRows) into partial[c] (as dot_partials_kernel
+// would), and the last CTA to arrive adds the partials in chunk order.
+__global__ void __launch_bounds__(kRedTpb) norm_kernel(const double *__restrict__ x, int n,
+                                                       double *__restrict__ partial, double *__restrict__ out,
+                                                       int *ticket)
+{
+    __shared__ double red[32];
+    const int c = blockIdx.x;
+    double a = 0.0;
+    const int r0 = c * kChunkRows, r1 = min(n, r0 + kChunkRows);
+    for (int r = r0 + threadIdx.x; r < r1; r += kRedTpb) a += x[r] * x[r];
+    const double sum = block_sum<kRedTpb>(a, red);
+    if (threadIdx.x == 0) partial[c] = sum;
+    if (!last_cta(ticket, gridDim.x)) return;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(partial + b);
+        *out = sqrt(t);
+    }
+}
+
+// K^T f per swimmer in one launch: each CTA's partial over its kKtBlobs
+// blobs; then, in the last CTA to arrive, the partials added per swimmer
+// (one warp per swimmer, lanes over the partials, a six-value warp sum).
+__global__ void __launch_bounds__(kKtBlobs) kt_kernel(int W, int nblob, const double *__restrict__ R,
+                                                      const double *__restrict__ refs,
+                                                      const double *__restrict__ f, double *__restrict__ part,
+                                                      double *__restrict__ sums, int *ticket)
+{
+    const int n = blockIdx.y, m = blockIdx.x * kKtBlobs + threadIdx.x, gx = gridDim.x;
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    if (m < nblob) {
+        const double *fm = f + 3 * ((size_t)n * nblob + m);
+        double d[3];
+        rot_apply(R + 9 * n, refs + 3 * m, d);
+        a[0] = fm[0];
+        a[1] = fm[1];
+        a[2] = fm[2];
+        a[3] = d[1] * fm[2] - d[2] * fm[1];
+        a[4] = d[2] * fm[0] - d[0] * fm[2];
+        a[5] = d[0] * fm[1] - d[1] * fm[0];
+    }
+    block_sum6<kKtBlobs>(a, part + ((size_t)n * gx + blockIdx.x) * 6);
+    if (!last_cta(ticket, gx * gridDim.y)) return;
+    const int lane = threadIdx.x & 31;
+    for (int sw = threadIdx.x >> 5; sw < W; sw += kKtBlobs / 32) {
+        double b[6] = {0, 0, 0, 0, 0, 0};
+        for (int x = lane; x < gx; x += 32)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) b[c] += __ldcg(part + ((size_t)sw * gx + x) * 6 + c);
+        const double t = warp_sum6_scatter(b);
+        if ((lane & 3) == 0 && lane < 24) sums[6 * sw + (lane >> 2)] = t;
+    }
 }
 
 // Sum over the gx per-CTA 6-vectors of each swimmer (part[(n*gx + x)*6 + c])
@@ -1069,9 +1083,8 @@ static int nchunks_of(int n) { return (n + kChunkRows - 1) / kChunkRows; }
 static gmi_status device_norm(gmi_solver *s, const double *x, int n)
 {
     const int nc = nchunks_of(n);
-    dot_partials_kernel<<<dim3(nc, 1), kRedTpb, 0, s->ctx->stream>>>(x, (size_t)n, x, n, nc, s->partial);
-    finish_norm_kernel<<<1, 1, 0, s->ctx->stream>>>(s->partial, nc, s->scal);
-    return launched(s, 2);
+    norm_kernel<<<nc, kRedTpb, 0, s->ctx->stream>>>(x, n, s->partial, s->scal, s->aux_tickets);
+    return launched(s);
 }
 
 static gmi_status prepare_bodies(gmi_solver *s)
@@ -1086,9 +1099,9 @@ static gmi_status prepare_bodies(gmi_solver *s)
 static gmi_status kt_sums(gmi_solver *s, const double *vec)
 {
     const int gx = (s->cfg.nblob + kKtBlobs - 1) / kKtBlobs;
-    kt_partial_kernel<<<dim3(gx, s->W), kKtBlobs, 0, s->ctx->stream>>>(s->cfg.nblob, s->R, s->refs, vec, s->kt_part);
-    kt_finish_kernel<<<grid_for(32 * s->W, 128), 128, 0, s->ctx->stream>>>(s->W, gx, s->kt_part, s->sums);
-    return launched(s, 2);
+    kt_kernel<<<dim3(gx, s->W), kKtBlobs, 0, s->ctx->stream>>>(s->W, s->cfg.nblob, s->R, s->refs, vec, s->kt_part,
+                                                              s->sums, s->aux_tickets + 1);
+    return launched(s);
 }
 
 // out = P^-1 in (apply_preconditioner, right preconditioning)
@@ -1949,6 +1962,9 @@ gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
     TRY_OR_DIE(dalloc(s, &s->sums, 6 * W));
     TRY_OR_DIE(dalloc(s, &s->kt_part, 6 * W * (size_t)((cfg->nblob + kKtBlobs - 1) / kKtBlobs)));
     TRY_OR_DIE(dalloc(s, &s->scal, 8));
+    double *aux_mem = nullptr;
+    TRY_OR_DIE(dalloc(s, &aux_mem, 4));  // zeroed: tickets of norm_kernel and kt_kernel
+    s->aux_tickets = reinterpret_cast<int *>(aux_mem);
     if (n > 0) {
         TRY_OR_DIE(dalloc(s, &s->rhs, n));
         TRY_OR_DIE(dalloc(s, &s->soln, n));

@@ -37,6 +37,7 @@ struct gmi_solver {
     size_t partial_count = 0;         // doubles in partial
     double *st_scal = nullptr;        // Arnoldi step scalars: projections h, ||w||
     int *st_tickets = nullptr;        // Arnoldi step arrival tickets (zero between launches)
+    int *aux_tickets = nullptr;       // the same for norm_kernel [0] and kt_kernel [1]
     size_t st_ticket_count = 0;
     double *gm_partial = nullptr;     // split partial sums of the GMRES operator
     size_t gm_partial_bytes = 0;
