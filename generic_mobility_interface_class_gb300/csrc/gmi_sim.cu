@@ -38,6 +38,7 @@
 #include "gmi_context.hpp"
 #include "gmi_gauss_jordan.hpp"
 #include "gmi_lie.cuh"
+#include "gmi_solver_device.cuh"
 #include "gmi_solver_internal.hpp"
 
 namespace gmi {
@@ -286,15 +287,15 @@ __device__ __forceinline__ double warp_sum_d(double v)
 }
 
 // Free-swimming force/torque balance (swimmer.cpp:276-325): body f = -sum of
-// segment forces and torques about the body centre.  Two passes: kFsSegs
-// segments per CTA into part[(n gx + x) 6 + c], then one thread per (swimmer,
-// component) adds the CTA partials in order.
+// segment forces and torques about the body centre, in one launch: kFsSegs
+// segments per CTA into part[(n gx + x) 6 + c]; the last CTA to arrive adds
+// the CTA partials in order, one thread per (swimmer, component).
 constexpr int kFsSegs = 128;
 
-__global__ void __launch_bounds__(kFsSegs) swimmer_force_partial_kernel(SimP P, double *part)
+__global__ void __launch_bounds__(kFsSegs) swimmer_force_kernel(SimP P, double *part, int *ticket)
 {
     __shared__ double red[6][kFsSegs / 32];
-    const int n = blockIdx.y, k = blockIdx.x * kFsSegs + threadIdx.x;
+    const int n = blockIdx.y, k = blockIdx.x * kFsSegs + threadIdx.x, gx = gridDim.x;
     const int per = P.NF * P.NS;
     const double *X = P.bx + 3 * n;
     double a[6] = {0, 0, 0, 0, 0, 0};
@@ -318,18 +319,15 @@ __global__ void __launch_bounds__(kFsSegs) swimmer_force_partial_kernel(SimP P, 
     if (threadIdx.x < 6) {
         double t = 0.0;
         for (int w = 0; w < kFsSegs / 32; ++w) t += red[threadIdx.x][w];
-        part[((size_t)n * gridDim.x + blockIdx.x) * 6 + threadIdx.x] = t;
+        part[((size_t)n * gx + blockIdx.x) * 6 + threadIdx.x] = t;
     }
-}
-
-__global__ void swimmer_force_finish_kernel(SimP P, int gx, const double *part)
-{
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= 6 * P.W) return;
-    const int n = e / 6, c = e % 6;
-    double t = 0.0;
-    for (int x = 0; x < gx; ++x) t += part[((size_t)n * gx + x) * 6 + c];
-    P.bf[e] = -t;
+    if (!last_cta(ticket, gx * gridDim.y)) return;
+    for (int e = threadIdx.x; e < 6 * P.W; e += kFsSegs) {
+        const int sw = e / 6, c = e % 6;
+        double t = 0.0;
+        for (int x = 0; x < gx; ++x) t += __ldcg(part + ((size_t)sw * gx + x) * 6 + c);
+        P.bf[e] = -t;
+    }
 }
 
 // compute_errors (mobility_solver.cpp:1404-1689), GMRES branch.
@@ -938,11 +936,16 @@ __global__ void __launch_bounds__(64) swimmer_schur_kernel(SimP P, int nt, const
     for (int k = 0; k < 36; ++k) P.schur[36 * n + k] = S6[k];
 }
 
-// jacobian_inv_mult (swimmer.cpp:793-837), three stages.
-// (1) per filament: part[6 fil..] = jacB_f * in_f
-__global__ void __launch_bounds__(128) jim_partial_kernel(SimP P, const double *in, double *part)
+// jacobian_inv_mult (swimmer.cpp:793-837), in two launches.
+// (1)+(2) per filament: part[6 fil..] = jacB_f * in_f; then, in the last CTA
+// to arrive, per swimmer (one warp each): out_body = schur_inv *
+// (in_body - sum_f part_f), the filaments' parts added by lanes strided over
+// the filaments and a warp sum.
+__global__ void __launch_bounds__(128) jim_partial_body_kernel(SimP P, const double *in, double *part, double *out,
+                                                               int *ticket)
 {
     __shared__ double red[6][4];
+    __shared__ double b2[4][6];
     const int fil = blockIdx.x, n = fil / P.NF, i = fil % P.NF;
     const double *x = in + (size_t)n * P.per_body + (size_t)6 * P.NS * i;
     const double *jB = P.jacB + (size_t)fil * 6 * P.n6;
@@ -957,29 +960,23 @@ __global__ void __launch_bounds__(128) jim_partial_kernel(SimP P, const double *
     __syncthreads();
     if (threadIdx.x < 6) part[6 * fil + threadIdx.x] = red[threadIdx.x][0] + red[threadIdx.x][1] +
                                                        red[threadIdx.x][2] + red[threadIdx.x][3];
-}
-
-// (2) per swimmer: out_body = schur_inv * (in_body - sum_f part_f); one CTA
-// per swimmer, thread r subtracts the filaments' parts of row r in order.
-__global__ void __launch_bounds__(32) jim_body_kernel(SimP P, const double *in, const double *part, double *out)
-{
-    __shared__ double b2[6];
-    const int n = blockIdx.x, lane = threadIdx.x;
-    const size_t b = (size_t)n * P.per_body + 6 * P.NF * P.NS;
-    // the filaments' parts, lanes strided over filaments, then a warp sum
-    for (int r = 0; r < 6; ++r) {
-        double v = 0.0;
-        for (int i = lane; i < P.NF; i += 32) v += part[6 * (n * P.NF + i) + r];
-        v = warp_sum_d(v);
-        if (lane == 0) b2[r] = in[b + r] - v;
-    }
-    __syncwarp();
-    if (threadIdx.x < 6) {
-        const int r = threadIdx.x;
-        const double *Si = P.schur + 36 * n;
-        double s = 0.0;
-        for (int k = 0; k < 6; ++k) s += Si[r + 6 * k] * b2[k];
-        out[b + r] = s;
+    if (!last_cta(ticket, gridDim.x)) return;
+    for (int sw = wid; sw < P.W; sw += 4) {
+        const size_t b = (size_t)sw * P.per_body + 6 * P.NF * P.NS;
+        for (int r = 0; r < 6; ++r) {
+            double v = 0.0;
+            for (int f = lane; f < P.NF; f += 32) v += __ldcg(part + 6 * (sw * P.NF + f) + r);
+            v = warp_sum_d(v);
+            if (lane == 0) b2[wid][r] = in[b + r] - v;
+        }
+        __syncwarp();
+        if (lane < 6) {
+            const double *Si = P.schur + 36 * sw;
+            double s = 0.0;
+            for (int k = 0; k < 6; ++k) s += Si[lane + 6 * k] * b2[wid][k];
+            out[b + lane] = s;
+        }
+        __syncwarp();
     }
 }
 
@@ -1065,9 +1062,10 @@ __global__ void filament_robot_arm_kernel(SimP P)
 constexpr int kVecTpb = 256;
 constexpr int kVecChunk = 2048;
 
-// part[i * nch + c] = sum over chunk c of M[:, i] . v   (i < k)
-__global__ void __launch_bounds__(kVecTpb) coldot_partial_kernel(const double *M, size_t ld, int k, const double *v,
-                                                                  int n, int nch, double *part)
+// dots[i] = M[:, i] . v (i < k) in one launch: part[i * nch + c] = the sum
+// over chunk c; the last CTA to arrive adds each column's chunks in order.
+__global__ void __launch_bounds__(kVecTpb) coldot_kernel(const double *M, size_t ld, int k, const double *v, int n,
+                                                          int nch, double *part, double *dots, int *ticket)
 {
     __shared__ double red[8];
     const int c = blockIdx.x, i = blockIdx.y;
@@ -1082,15 +1080,12 @@ __global__ void __launch_bounds__(kVecTpb) coldot_partial_kernel(const double *M
         for (int w = 0; w < kVecTpb / 32; ++w) s += red[w];
         part[(size_t)i * nch + c] = s;
     }
-}
-
-__global__ void coldot_finish_kernel(const double *part, int k, int nch, double *dots)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= k) return;
-    double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += part[(size_t)i * nch + c];
-    dots[i] = s;
+    if (!last_cta(ticket, gridDim.x * gridDim.y)) return;
+    for (int j = threadIdx.x; j < k; j += kVecTpb) {
+        double s = 0.0;
+        for (int cc = 0; cc < nch; ++cc) s += __ldcg(part + (size_t)j * nch + cc);
+        dots[j] = s;
+    }
 }
 
 // out[r] = a * x[r] - sum_{i<k} dots[i] C[r, i]   (in order of i)
@@ -1135,6 +1130,7 @@ struct gmi_sim {
     double *spart = nullptr;  // per-filament parts of the Schur complement (45 each)
     double *f_internal = nullptr;  // segment forces before the barrier (the reference's f_segs_host)
     double *fs_part = nullptr;     // per-CTA partials of the swimmer force/torque sums
+    int *tickets = nullptr;        // swimmer_force_kernel [0], jim_partial_body_kernel [1], coldot_kernel [2]
     int *h_flags = nullptr;
     std::vector<void *> allocs;
     bool prepared = false;
@@ -1177,16 +1173,15 @@ static gmi_status forces_and_torques(gmi_sim *m, int nt)
 {
     if (m->P.NS > 1) filament_link_terms_kernel<<<gridN(m->P.F * (m->P.NS - 1), 64), 64, 0, sst(m)>>>(m->P);
     filament_forces_kernel<<<gridN(m->P.S, 64), 64, 0, sst(m)>>>(m->P, nt);
-    GMI_TRY(sim_launched(m));
+    GMI_TRY(sim_launched(m, m->P.NS > 1 ? 2 : 1));
     // the host copy of the segment forces never receives the barrier forces
     // (mobility_solver.cpp:132-192); keep it for the writers
     GMI_CUDA_TRY(cudaMemcpyAsync(m->f_internal, m->P.f, 6 * (size_t)m->P.S * sizeof(double),
                                  cudaMemcpyDeviceToDevice, sst(m)));
-    if (m->P.wall) return sim_launched(m);
+    if (m->P.wall) return GMI_OK;
     const int gx = gridN(m->P.NF * m->P.NS, kFsSegs);
-    swimmer_force_partial_kernel<<<dim3(gx, m->P.W), kFsSegs, 0, sst(m)>>>(m->P, m->fs_part);
-    swimmer_force_finish_kernel<<<gridN(6 * m->P.W, 64), 64, 0, sst(m)>>>(m->P, gx, m->fs_part);
-    return sim_launched(m, 3);
+    swimmer_force_kernel<<<dim3(gx, m->P.W), kFsSegs, 0, sst(m)>>>(m->P, m->fs_part, m->tickets);
+    return sim_launched(m);
 }
 
 // compute_velocities + compute_errors; sets *too_large, *nonfinite
@@ -1239,10 +1234,9 @@ static gmi_status jacobian_inv_mult(gmi_sim *m, const double *in, double *out)
         jim_fil_kernel<<<P.F, 128, P.n6 * sizeof(double), sst(m)>>>(P, in, out);
         return sim_launched(m);
     }
-    jim_partial_kernel<<<P.F, 128, 0, sst(m)>>>(P, in, m->jpart);
-    jim_body_kernel<<<P.W, 32, 0, sst(m)>>>(P, in, m->jpart, out);
+    jim_partial_body_kernel<<<P.F, 128, 0, sst(m)>>>(P, in, m->jpart, out, m->tickets + 1);
     jim_fil_kernel<<<P.F, 128, P.n6 * sizeof(double), sst(m)>>>(P, in, out);
-    return sim_launched(m, 3);
+    return sim_launched(m, 2);
 }
 
 // dots[i] = v . D[:, i], i < k
@@ -1250,9 +1244,9 @@ static gmi_status dots_with_D(gmi_sim *m, const double *v, int k)
 {
     if (k == 0) return GMI_OK;
     const int n = m->P.nbroy, nch = (n + kVecChunk - 1) / kVecChunk;
-    coldot_partial_kernel<<<dim3(nch, k), kVecTpb, 0, sst(m)>>>(m->D, (size_t)n, k, v, n, nch, m->part);
-    coldot_finish_kernel<<<gridN(k, 64), 64, 0, sst(m)>>>(m->part, k, nch, m->dots);
-    return sim_launched(m, 2);
+    coldot_kernel<<<dim3(nch, k), kVecTpb, 0, sst(m)>>>(m->D, (size_t)n, k, v, n, nch, m->part, m->dots,
+                                                         m->tickets + 2);
+    return sim_launched(m);
 }
 
 // broyden_solver::find_update (broyden_solver.cpp:26-68)
@@ -1279,10 +1273,10 @@ static gmi_status end_of_iter(gmi_sim *m, bool too_large)
         vec_sub_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, m->nerr, m->err, Dcol);
         GMI_TRY(sim_launched(m, 2));
         const int nch = (n + kVecChunk - 1) / kVecChunk;
-        coldot_partial_kernel<<<dim3(nch, 1), kVecTpb, 0, sst(m)>>>(Dcol, (size_t)n, 1, Dcol, n, nch, m->part);
-        coldot_finish_kernel<<<1, 64, 0, sst(m)>>>(m->part, 1, nch, m->scal);
+        coldot_kernel<<<dim3(nch, 1), kVecTpb, 0, sst(m)>>>(Dcol, (size_t)n, 1, Dcol, n, nch, m->part, m->scal,
+                                                            m->tickets + 2);
         vec_div2_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, Ccol, Dcol, m->scal);
-        GMI_TRY(sim_launched(m, 3));
+        GMI_TRY(sim_launched(m, 2));
         std::swap(m->err, m->nerr);
     }
     m->broyden_iter++;
@@ -1512,6 +1506,9 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
         double *fl = nullptr;
         SIM_ALLOC(fl, 4);
         P.flags = reinterpret_cast<int *>(fl);
+        double *tk = nullptr;
+        SIM_ALLOC(tk, 4);  // zeroed arrival tickets of the one-launch reductions
+        m->tickets = reinterpret_cast<int *>(tk);
     }
 #undef SIM_ALLOC
     if (cudaMallocHost(&m->h_flags, 4 * sizeof(int)) != cudaSuccess) {

@@ -391,31 +391,6 @@ constexpr int kHOff = 0;             // h[kFMaxK]: the last projections
 constexpr int kNormOff = kFMaxK;     // ||w|| of the last step (or beta0 before the first)
 constexpr int kStepScalars = kFMaxK + 8;
 
-// True in every thread of the CTA that arrives last (of `total`) at *ticket;
-// that CTA re-arms the ticket for the next launch.  Partials written before
-// the call are visible to the last CTA through L2 (__ldcg).
-// The block barrier orders the CTA's writes before thread 0's release fence
-// (a CTA barrier synchronises, and a release is cumulative over what
-// precedes it), so one thread fences for the whole CTA; the last CTA's
-// acquire fence, then its block barrier, make every partial visible to all
-// of its threads.
-__device__ __forceinline__ bool last_cta(int *ticket, int total)
-{
-    __shared__ int is_last;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        asm volatile("fence.acq_rel.gpu;" ::: "memory");
-        const int t = atomicAdd(ticket, 1);
-        is_last = (t == total - 1);
-        if (is_last) {
-            *ticket = 0;
-            asm volatile("fence.acq_rel.gpu;" ::: "memory");
-        }
-    }
-    __syncthreads();
-    return is_last;
-}
-
 // ||x|| into *out in one launch: CTA c sums the squares of rows
 // [c kChunkRows, (c + 1) kChunkRows) into partial[c] (as dot_partials_kernel
 // would), and the last CTA to arrive adds the partials in chunk order.

@@ -42,6 +42,31 @@ __device__ __forceinline__ double warp_sum6_scatter(const double v[6])
     return d;
 }
 
+// True in every thread of the CTA that arrives last (of `total`) at *ticket;
+// that CTA re-arms the ticket for the next launch.  Partials written before
+// the call are visible to the last CTA through L2 (__ldcg).
+// The block barrier orders the CTA's writes before thread 0's release fence
+// (a CTA barrier synchronises, and a release is cumulative over what
+// precedes it), so one thread fences for the whole CTA; the last CTA's
+// acquire fence, then its block barrier, make every partial visible to all
+// of its threads.
+__device__ __forceinline__ bool last_cta(int *ticket, int total)
+{
+    __shared__ int is_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        const int t = atomicAdd(ticket, 1);
+        is_last = (t == total - 1);
+        if (is_last) {
+            *ticket = 0;
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        }
+    }
+    __syncthreads();
+    return is_last;
+}
+
 // o = R v, R row-major 3x3
 __device__ __forceinline__ void rot_apply(const double *R, const double *v, double *o)
 {
