@@ -263,3 +263,50 @@ def test_multikernel_fp32c_solve_is_deterministic(gmi_lib, monkeypatch):
     assert runs[0][0] == runs[1][0]
     for a, b in zip(runs[0][1:], runs[1][1:]):
         assert np.array_equal(a, b)
+
+
+def test_refinement_residual_double_float_matches_fp64(gmi_lib, oracle_built, monkeypatch):
+    """The mixed-precision refinement forms its residual with the double-float
+    blob-blob sum by default and with the FP64 kernel under GMI_REFINE_DF=0:
+    both meet the tolerance in the dense FP64 system and agree with each
+    other far below it, with the same iteration counts up to rounding."""
+    from oracle import mobility_dense as md
+    nfil, nseg = 4, 10
+    refs, bx, bq, xs, fs, bf = swimmer_geometry(1, nfil, nseg)
+    want = md.compute_velocities(xs, fs, bx, bq, bf, refs, nseg, force_scale=1.5)
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("GMI_REFINE_DF", mode)
+        s = make_solver(refs, 1, nfil, nseg, precision=1)
+        s.x_segs_host[:] = xs
+        s.f_segs_host[:] = fs
+        iters, _ = s.compute_velocities(bx, bq, bf)
+        out[mode] = (iters, np.concatenate([s.f_blobs_host.ravel(), s.v_bodies().ravel()]))
+        s.close()
+    for mode, (iters, x) in out.items():
+        assert iters > 0
+        resid = np.linalg.norm(want["A"] @ x - want["rhs"]) / np.linalg.norm(want["rhs"])
+        assert resid < 1e-7, (mode, resid)
+    assert rel_err(out["1"][1], out["0"][1]) < 1e-6
+    assert abs(out["1"][0] - out["0"][0]) <= max(3, out["0"][0] // 10)
+
+
+def test_programmatic_dependent_launch_changes_nothing(gmi_lib, monkeypatch):
+    """The Arnoldi-step kernels launched with programmatic dependencies (the
+    default) and without (GMI_PDL=0) do the same arithmetic in the same
+    order: bit-identical answers and iteration counts."""
+    monkeypatch.setenv("GMI_GMRES_CLUSTER", "0")
+    nfil, nseg = 4, 10
+    refs, bx, bq, xs, fs, bf = swimmer_geometry(1, nfil, nseg, subdiv=4, R=30.0)
+    runs = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("GMI_PDL", mode)
+        s = make_solver(refs, 1, nfil, nseg, precision=1)
+        s.x_segs_host[:] = xs
+        s.f_segs_host[:] = fs
+        iters = [s.compute_velocities(bx, bq, bf)[0] for _ in range(2)]
+        runs[mode] = (iters, s.f_blobs_host.copy(), s.v_bodies().copy())
+        s.close()
+    assert runs["1"][0] == runs["0"][0]
+    for a, b in zip(runs["1"][1:], runs["0"][1:]):
+        assert np.array_equal(a, b)
