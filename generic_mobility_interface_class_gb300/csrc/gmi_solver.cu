@@ -1600,9 +1600,10 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         return store_solution(s);
     }
     // Mixed-precision refinement.  The residual of the warm start is formed
-    // with the FP64 operator; after each correction delta (solved to at
-    // most 1e-6 relative, so |A delta| ~ |r|) it is updated as r -= A delta with the FP32C
-    // operator, whose error (~3e-7 |A delta|) stays far below the tolerance.
+    // with the FP64-grade operator; after each correction delta (A delta ~ r,
+    // so |A delta| ~ |r|) it is updated as r -= A delta with the FP32C
+    // operator, whose error (~3e-7 |A delta|, i.e. ~3e-7 of a residual that is
+    // already small against |b|) stays far below the tolerance.
     GMI_CUDA_TRY(cudaMemcpyAsync(s->b64, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
     int total = 0;
     gmi_status status = GMI_OK;
