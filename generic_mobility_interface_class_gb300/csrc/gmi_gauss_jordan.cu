@@ -21,7 +21,11 @@
 //     its own column as it reads them);
 //   * the search for step k + 1 runs inside step k, in the warp that owns
 //     column k + 1, right after it has eliminated that column first, so a step
-//     needs one barrier.
+//     needs one barrier;
+//   * for n <= 256 a warp holds several of its columns in registers at once
+//     (rows lane + 32 t) and takes the pivot-row entries by shuffle, so their
+//     FMAs are all in flight together; larger n steps one column at a time
+//     through shared memory (the same arithmetic).
 // Two kernels share that step: one CTA per matrix (many filaments), and one
 // thread-block cluster per matrix with the columns sliced over the CTAs and
 // the published pivot column read through distributed shared memory (few
