@@ -65,7 +65,7 @@ struct ClusterGmresArgs {
     int kq, kqs;                      // basis columns [0, kq) of the CTA's rows cached in shared memory, row stride kqs
     const double *w0;                 // r0, all n rows
     const double *R, *refs, *ktk_rot, *mob_rot, *ktkf_rot, *xb;
-    double minv, beta0, tol, norm_ref;
+    double minv, beta0, tol, norm_ref, inv_norm_ref;
     GmresCtl *ctl;
     EqualK<float> kbb;
 };
@@ -412,13 +412,13 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
             if (hk == 0.0) {
                 cc = 1.0;
                 ss = 0.0;
-            } else if (fabs(hk) > fabs(hd)) {
+            } else if (fabs(hk) > fabs(hd)) {  // the reference's scaled form; rsqrt saves a division
                 const double u = hd / hk;
-                ss = (2.0 * (double)(hk > 0) - 1.0) / sqrt(1.0 + u * u);
+                ss = (2.0 * (double)(hk > 0) - 1.0) * rsqrt(1.0 + u * u);
                 cc = u * ss;
             } else {
                 const double u = hk / hd;
-                cc = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + u * u);
+                cc = (2.0 * (double)(hd > 0) - 1.0) * rsqrt(1.0 + u * u);
                 ss = u * cc;
             }
             csh[iter - 1] = cc;
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
             col[iter] = 0.0;
             bet[iter] = -ss * bet[iter - 1];
             bet[iter - 1] = cc * bet[iter - 1];
-            const double resid = fabs(bet[iter]) / a.norm_ref;
+            const double resid = fabs(bet[iter]) * a.inv_norm_ref;
             const int done = !(resid > a.tol) || iter >= a.max_iter;
             flag[0] = done;
             if (c == 0) {
@@ -664,6 +664,7 @@ gmi_status cluster_gmres_launch(gmi_solver *s, double beta0, double norm_ref, do
     a.beta0 = beta0;
     a.tol = tol;
     a.norm_ref = norm_ref;
+    a.inv_norm_ref = 1.0 / norm_ref;
     a.ctl = s->ctl;
     PairConsts k;
     fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);

@@ -881,13 +881,13 @@ __device__ __forceinline__ void givens_step(double *__restrict__ H, int ldh, int
         if (hk == 0.0) {
             c = 1.0;
             s = 0.0;
-        } else if (fabs(hk) > fabs(hd)) {
+        } else if (fabs(hk) > fabs(hd)) {  // the reference's scaled form; rsqrt saves a division
             const double u = hd / hk;
-            s = (2.0 * (double)(hk > 0) - 1.0) / sqrt(1.0 + u * u);
+            s = (2.0 * (double)(hk > 0) - 1.0) * rsqrt(1.0 + u * u);
             c = u * s;
         } else {
             const double u = hk / hd;
-            c = (2.0 * (double)(hd > 0) - 1.0) / sqrt(1.0 + u * u);
+            c = (2.0 * (double)(hd > 0) - 1.0) * rsqrt(1.0 + u * u);
             s = u * c;
         }
         cs[iter - 1] = c;
@@ -896,7 +896,7 @@ __device__ __forceinline__ void givens_step(double *__restrict__ H, int ldh, int
         col[iter] = 0.0;
         beta[iter] = -s * beta[iter - 1];
         beta[iter - 1] = c * beta[iter - 1];
-        const double resid = fabs(beta[iter]) / ctl->norm_ref;
+        const double resid = fabs(beta[iter]) * ctl->inv_norm_ref;
         ctl->resid = resid;
         const int replays = ++ctl->replays;
         // converged, at the cap, or NaN; the replay count bounds the loop even if k stalled
@@ -1396,6 +1396,7 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
         c.max_iter = max_iter;
         c.tol = tol;
         c.norm_ref = norm_ref;
+        c.inv_norm_ref = 1.0 / norm_ref;
         *s->h_ctl = c;
         GMI_CUDA_TRY(cudaMemcpyAsync(s->ctl, s->h_ctl, sizeof c, cudaMemcpyHostToDevice, st));
         GMI_TRY(cluster_gmres_launch(s, beta0, norm_ref, tol, max_iter));
@@ -1423,6 +1424,7 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
         c.guard = 0;
         c.tol = tol;
         c.norm_ref = norm_ref;
+        c.inv_norm_ref = 1.0 / norm_ref;
         *s->h_ctl = c;
         GMI_CUDA_TRY(cudaMemcpyAsync(s->ctl, s->h_ctl, sizeof c, cudaMemcpyHostToDevice, st));
         int batch = 4, replayed = 0;

@@ -64,7 +64,9 @@ struct GmresCtl {
     double tol;    // relative residual target
     double norm_ref;
     double resid;  // |beta(k)| / norm_ref after the last Givens step
+    double inv_norm_ref;  // 1 / norm_ref (the Givens step multiplies: no division on its serial path)
 };
+static_assert(sizeof(GmresCtl) <= 64, "GmresCtl lives in an 8-double device block");
 
 namespace gmi {
 
