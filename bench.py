@@ -21,7 +21,9 @@ self pair included.  One step = one full apply.  Default N = 131072.
              Broyden, GMRES, every pair sum) on seeded free swimmers
              (1 sphere of 642 blobs with 16 x 20 segments; 1 sphere of 4096
              blobs with 640 x 20 segments), plain FP64 against FP32C pair
-             sums with FP64 solves, with the velocity error between the two
+             sums with FP64 solves, with the velocity error between the two;
+             with --ts-workloads config4, the aggregate rate of 64
+             independent swimmers of uneven size and the per-swimmer error
 
 Runs one replica per GPU under torchrun (the apply does not shard here:
 "replicas only"), max-over-ranks time, rank 0 prints one JSON line.
@@ -72,6 +74,7 @@ def parse():
                    help="time-step workloads (comma separated; empty to skip)")
     p.add_argument("--ts-steps", default="config1:100,config3:10", help="timed steps per workload")
     p.add_argument("--ts-warmup", type=int, default=5, help="untimed steps before the timed ones")
+    p.add_argument("--ts-swimmers", type=int, default=64, help="swimmers of a batch time-step workload (config4)")
     return p.parse_args()
 
 
@@ -229,6 +232,9 @@ def run_time_steps(args, dev):
     steps_for = dict(kv.split(":") for kv in args.ts_steps.split(",") if kv)
     out = {}
     for name in [w for w in args.ts_workloads.split(",") if w]:
+        if name in workloads.BATCH_WORKLOADS:
+            out[name] = run_batch_time_steps(args, dev, name, int(steps_for.get(name, 3)))
+            continue
         desc, make = workloads.WORKLOADS[name]
         kw = make()
         nsteps = int(steps_for.get(name, 10))
@@ -267,6 +273,59 @@ def run_time_steps(args, dev):
                                                        "segment_quaternion_rel": rel("seg_q"),
                                                        "body_position_rel": rel("body_x")}}
     return out
+
+
+def run_batch_time_steps(args, dev, name, nsteps):
+    """Aggregate time-steps/sec of independent swimmers of uneven size
+    (batch.SwimmerBatch: one stream and one host thread per swimmer), plain
+    FP64 against FP32C pair sums with FP64 solves, and the per-swimmer error
+    between the two after the run."""
+    import torch
+    from generic_mobility_interface_class_gb300 import workloads
+    from generic_mobility_interface_class_gb300.batch import SwimmerBatch
+    from generic_mobility_interface_class_gb300._lib import GMI_FP32C, GMI_FP64
+    desc, make = workloads.BATCH_WORKLOADS[name]
+    swimmers = make(nswim=args.ts_swimmers)
+    runs, final = {}, {}
+    for label, prec in (("fp64", GMI_FP64), ("fp32c", GMI_FP32C)):
+        batch = SwimmerBatch(swimmers, precision=prec, device=dev)
+        batch.prepare()
+        for nt in range(args.ts_warmup):
+            batch.step(nt)
+        torch.cuda.synchronize()
+        l0 = batch.launches
+        broyden, gmres = [], []
+        with ClockSampler(dev) as clocks:
+            t0 = time.perf_counter()
+            for nt in range(args.ts_warmup, args.ts_warmup + nsteps):
+                it = batch.step(nt)
+                broyden.append(sum(b for b, _ in it))
+                gmres.append(sum(g for _, g in it))
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        n = len(batch)
+        runs[label] = {"swimmer_steps_per_s": n * nsteps / wall, "batch_steps_per_s": nsteps / wall,
+                       "ms_per_batch_step": 1e3 * wall / nsteps,
+                       "broyden_iters_per_swimmer_step": sum(broyden) / (n * nsteps),
+                       "gmres_iters_per_swimmer_step": sum(gmres) / (n * nsteps),
+                       "gpu_launches": batch.launches - l0, "clocks": clocks.summary()}
+        final[label] = {f: [a.ravel() for a in batch.state(f)] for f in ("body_v", "seg_v")}
+        batch.close()
+
+    def rel(f):
+        errs = []
+        for a, b in zip(final["fp64"][f], final["fp32c"][f]):
+            errs.append(float(np.linalg.norm(b - a) / max(np.linalg.norm(a), 1e-300)))
+        return {"max": max(errs), "median": float(np.median(errs))}
+
+    sizes = [(kw["nblob"], kw["nfil"] * kw["nseg"]) for kw in swimmers]
+    return {"workload": desc, "swimmers": len(swimmers), "blobs": sum(b for b, _ in sizes),
+            "segments": sum(s for _, s in sizes), "host_threads": len(swimmers), "timed_steps": nsteps,
+            "warmup_steps": args.ts_warmup, "broyden_tol": swimmers[0]["tol"], "gmres_tol": swimmers[0]["linear_tol"],
+            **runs,
+            "speedup_fp32c_vs_fp64": runs["fp32c"]["swimmer_steps_per_s"] / runs["fp64"]["swimmer_steps_per_s"],
+            "error_fp32c_vs_fp64_after_run": {"per_swimmer_velocity_rel": rel("body_v"),
+                                              "per_swimmer_segment_velocity_rel": rel("seg_v")}}
 
 
 def run_gmi(args, world, rank, local):

@@ -8,6 +8,7 @@ from __future__ import annotations
 import ctypes
 import os
 import re
+import threading
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
@@ -115,6 +116,7 @@ class HostArrays(ctypes.Structure):
                  "f_blobs_repulsion_host")]
 
 _lib = None
+_load_lock = threading.Lock()
 
 
 def header_symbols() -> list[str]:
@@ -127,16 +129,19 @@ def load() -> ctypes.CDLL:
     global _lib
     if _lib is not None:
         return _lib
-    if not os.path.exists(LIB_PATH):
-        raise GmiLibraryMissing(
-            f"{LIB_PATH} is not built; run generic_mobility_interface_class_gb300.build.build() first")
-    lib = ctypes.CDLL(LIB_PATH)
-    for name, (args, res) in SIGNATURES.items():
-        fn = getattr(lib, name)
-        fn.argtypes = args
-        fn.restype = res
-    _lib = lib
-    return lib
+    with _load_lock:  # the swimmers of a batch are built on several threads
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise GmiLibraryMissing(
+                f"{LIB_PATH} is not built; run generic_mobility_interface_class_gb300.build.build() first")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = lib
+        return lib
 
 
 def check(status: int) -> None:

@@ -57,8 +57,8 @@ gmi_status gmi_context_destroy(gmi_context *ctx)
     ctx->rec_src.release();
     ctx->rec_tgt.release();
     ctx->partial.release();
-    if (ctx->d_err) cudaFree(ctx->d_err);
-    if (ctx->h_err) cudaFreeHost(ctx->h_err);
+    if (ctx->d_err) gmi::dev_free(ctx->d_err);
+    if (ctx->h_err) gmi::host_free(ctx->h_err);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return GMI_OK;
@@ -289,7 +289,7 @@ gmi_status gmi_autotune(gmi_context *ctx, int kind, int num_targets, int num_sou
     {
         const size_t nbytes_max = (size_t)(num_targets > num_sources ? num_targets : num_sources) * 6;
         double *h = nullptr;
-        GMI_CUDA_TRY(cudaMallocHost(&h, nbytes_max * sizeof(double)));
+        GMI_CUDA_TRY(gmi::host_alloc(&h, nbytes_max * sizeof(double)));
         auto fill_pos = [&](int n, double *dst) -> gmi_status {
             const int side = (int)std::ceil(std::cbrt((double)n));
             for (int i = 0; i < n; ++i) {
@@ -308,7 +308,7 @@ gmi_status gmi_autotune(gmi_context *ctx, int kind, int num_targets, int num_sou
             cudaError_t e = cudaMemcpy(fsrc.ptr, h, (size_t)num_sources * nf * sizeof(double), cudaMemcpyHostToDevice);
             if (e != cudaSuccess) st = GMI_ERR_CUDA;
         }
-        cudaFreeHost(h);
+        gmi::host_free(h);
         if (st != GMI_OK) return st;
     }
     st = pack_records(ctx, static_cast<double *>(xt.ptr), nullptr, 0, num_targets, rt);

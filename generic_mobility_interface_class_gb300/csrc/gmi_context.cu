@@ -1,7 +1,10 @@
 // gmi_context.cu -- context lifetime, scratch buffers, error reporting.
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
 
 #include "gmi_context.hpp"
 
@@ -20,11 +23,56 @@ void set_last_error_msg(const char *msg) { g_last_error = msg; }
 
 const char *last_error() { return g_last_error.c_str(); }
 
+std::recursive_mutex &device_sync_mutex()
+{
+    static std::recursive_mutex mu;
+    return mu;
+}
+
+cudaError_t dev_malloc_bytes(void **p, size_t bytes)
+{
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t dev_free(void *p)
+{
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
+    return cudaFree(p);
+}
+
+cudaError_t host_alloc_bytes(void **p, size_t bytes, unsigned flags)
+{
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
+    return cudaHostAlloc(p, bytes, flags);
+}
+
+cudaError_t host_free(void *p)
+{
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
+    return cudaFreeHost(p);
+}
+
+cudaError_t raise_dynamic_smem_limit(const void *fn, size_t bytes)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> limits;  // (device, function) -> limit set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &have = limits[{dev, fn}];
+    if (bytes <= have) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) have = bytes;
+    return e;
+}
+
 gmi_status DeviceBuffer::reserve(size_t need)
 {
     if (need <= bytes) return GMI_OK;
     if (ptr) {
-        cudaError_t e = cudaFree(ptr);
+        cudaError_t e = dev_free(ptr);
         ptr = nullptr;
         bytes = 0;
         if (e != cudaSuccess) {
@@ -35,7 +83,7 @@ gmi_status DeviceBuffer::reserve(size_t need)
     // round up to 2 MiB so that small growth steps do not reallocate
     const size_t grain = size_t(2) << 20;
     const size_t alloc = (need + grain - 1) / grain * grain;
-    cudaError_t e = cudaMalloc(&ptr, alloc);
+    cudaError_t e = dev_malloc(&ptr, alloc);
     if (e != cudaSuccess) {
         ptr = nullptr;
         set_last_error(cudaGetErrorString(e), "cudaMalloc", __FILE__, __LINE__);
@@ -47,7 +95,7 @@ gmi_status DeviceBuffer::reserve(size_t need)
 
 void DeviceBuffer::release()
 {
-    if (ptr) cudaFree(ptr);
+    if (ptr) dev_free(ptr);
     ptr = nullptr;
     bytes = 0;
 }
@@ -65,9 +113,9 @@ gmi_status context_init(gmi_context *ctx, int device)
     GMI_CUDA_TRY(cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device));
     GMI_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     ctx->own_stream = true;
-    GMI_CUDA_TRY(cudaMalloc(&ctx->d_err, sizeof(unsigned)));
+    GMI_CUDA_TRY(dev_malloc(&ctx->d_err, sizeof(unsigned)));
     GMI_CUDA_TRY(cudaMemset(ctx->d_err, 0, sizeof(unsigned)));
-    GMI_CUDA_TRY(cudaMallocHost(&ctx->h_err, sizeof(unsigned)));
+    GMI_CUDA_TRY(host_alloc(&ctx->h_err, sizeof(unsigned)));
     *ctx->h_err = 0;
     cudaDriverEntryPointQueryResult q;
     void *fn = nullptr;

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <mutex>
 #include <tuple>
 
 #include "gmi_common.cuh"
@@ -53,4 +54,35 @@ struct gmi_context {
 namespace gmi {
 gmi_status context_init(gmi_context *ctx, int device);
 gmi_status context_check_device_errors(gmi_context *ctx);
+
+// Make fn's dynamic shared-memory limit on the current device at least
+// bytes.  The limit belongs to the function, not to a context or a stream,
+// so solvers of different sizes driven from different host threads share
+// it: it is only ever raised, under a lock, and a launch sized for one
+// solver never finds it lowered by another.
+cudaError_t raise_dynamic_smem_limit(const void *fn, size_t bytes);
+
+// One process-wide lock over every stream capture and every call that
+// synchronises the whole device (cudaFree, cudaFreeHost, and cudaMalloc,
+// which may).  A device-wide synchronisation on one host thread invalidates
+// a capture in progress on another, so solvers stepped from several threads
+// (independent swimmers) allocate, free and capture one at a time; their
+// kernels still overlap.  Recursive: a capture may allocate.
+std::recursive_mutex &device_sync_mutex();
+cudaError_t dev_malloc_bytes(void **p, size_t bytes);
+cudaError_t dev_free(void *p);
+cudaError_t host_alloc_bytes(void **p, size_t bytes, unsigned flags);
+cudaError_t host_free(void *p);
+
+template <class T>
+cudaError_t dev_malloc(T **p, size_t bytes)
+{
+    return dev_malloc_bytes(reinterpret_cast<void **>(p), bytes);
+}
+
+template <class T>
+cudaError_t host_alloc(T **p, size_t bytes, unsigned flags = cudaHostAllocDefault)
+{
+    return host_alloc_bytes(reinterpret_cast<void **>(p), bytes, flags);
+}
 }  // namespace gmi

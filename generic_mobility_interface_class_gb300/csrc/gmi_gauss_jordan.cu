@@ -354,7 +354,7 @@ static gmi_status gj_launch(cudaStream_t stream, double *mats, int nmat, int n, 
         const size_t smem = ((size_t)n * nc + 3 * (size_t)n + 4) * sizeof(double) + (6 + (size_t)n) * sizeof(int);
         if (smem <= (size_t)dev_max) {
             const void *fn = reinterpret_cast<const void *>(&gj_cluster_kernel<RPL>);
-            GMI_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            GMI_CUDA_TRY(raise_dynamic_smem_limit(fn, smem));
             cudaLaunchConfig_t cfg{};
             cudaLaunchAttribute attr[1];
             attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -375,7 +375,7 @@ static gmi_status gj_launch(cudaStream_t stream, double *mats, int nmat, int n, 
     const size_t mat = (size_t)n * n * sizeof(double);
     const int use_smem = (base + mat <= (size_t)dev_max) ? 1 : 0;
     const size_t smem = use_smem ? base + mat : base;
-    GMI_CUDA_TRY(cudaFuncSetAttribute(gj_invert_kernel<RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GMI_CUDA_TRY(raise_dynamic_smem_limit(reinterpret_cast<const void *>(&gj_invert_kernel<RPL>), smem));
     gj_invert_kernel<RPL><<<nmat, kGjTpb, smem, stream>>>(mats, n, use_smem, flags);
     GMI_CUDA_TRY(cudaGetLastError());
     return GMI_OK;

@@ -140,7 +140,7 @@ __global__ void kaxpby(int n, double a, const double *__restrict__ x, double b, 
 
 gmi_status dev_alloc(double **p, size_t count, cudaStream_t st)
 {
-    GMI_CUDA_TRY(cudaMalloc(p, (count ? count : 1) * sizeof(double)));
+    GMI_CUDA_TRY(dev_malloc(p, (count ? count : 1) * sizeof(double)));
     GMI_CUDA_TRY(cudaMemsetAsync(*p, 0, (count ? count : 1) * sizeof(double), st));
     return GMI_OK;
 }
@@ -178,7 +178,7 @@ gmi_status krylov_alloc(KrylovSpace &K, int n, int m, cudaStream_t st)
         krylov_free(K);
         return e;
     }
-    if (cudaMallocHost(&K.h_scal, 4 * sizeof(double)) != cudaSuccess) {
+    if (host_alloc(&K.h_scal, 4 * sizeof(double)) != cudaSuccess) {
         K.h_scal = nullptr;
         krylov_free(K);
         set_last_error_msg("krylov_alloc: pinned allocation failed");
@@ -190,10 +190,10 @@ gmi_status krylov_alloc(KrylovSpace &K, int n, int m, cudaStream_t st)
 void krylov_free(KrylovSpace &K)
 {
     for (double **p : {&K.Q, &K.H, &K.beta, &K.cs, &K.sn, &K.yv, &K.w, &K.z, &K.tmp, &K.partial, &K.scal}) {
-        if (*p) cudaFree(*p);
+        if (*p) dev_free(*p);
         *p = nullptr;
     }
-    if (K.h_scal) cudaFreeHost(K.h_scal);
+    if (K.h_scal) host_free(K.h_scal);
     K.h_scal = nullptr;
     K.n = K.m = 0;
 }

@@ -577,7 +577,7 @@ static ClusterChoice choose_cluster(gmi_solver *s)
         if (kq < 8) kq = 0;
         const int kqs = kq > 0 ? (kq | 1) : 0;  // odd row stride: the per-row update loop avoids bank conflicts
         const CgLayout L = cg_layout(nb, W, bpc, kqs);
-        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total) != cudaSuccess) {
+        if (raise_dynamic_smem_limit(fn, L.total) != cudaSuccess) {
             cudaGetLastError();
             continue;
         }
@@ -631,7 +631,7 @@ gmi_status cluster_gmres_launch(gmi_solver *s, double beta0, double norm_ref, do
     // row-major copy of the Krylov basis (n rows of ldr >= max_iter + 1 entries)
     const int ldr = s->m + 1;
     if (s->Qr == nullptr) {
-        GMI_CUDA_TRY(cudaMalloc(&s->Qr, (size_t)s->n * ldr * sizeof(double)));
+        GMI_CUDA_TRY(dev_malloc(&s->Qr, (size_t)s->n * ldr * sizeof(double)));
         s->allocs.push_back(s->Qr);
     }
     double *Qr = s->Qr;

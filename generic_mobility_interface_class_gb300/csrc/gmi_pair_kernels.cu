@@ -1207,7 +1207,7 @@ static gmi_status launch_bb_df(gmi_context *ctx, const void *tgt_rec, int tgt_st
 {
     void *fn = reinterpret_cast<void *>(&rpy_bb_df_kernel<kDfTpb>);
     const size_t smem = ring_bytes(false, false);
-    GMI_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GMI_CUDA_TRY(raise_dynamic_smem_limit(fn, smem));
     int occ = 0;
     GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kDfTpb, smem));
     const int n_tgt_ctas = (n_tgt + kDfTpb - 1) / kDfTpb;
@@ -1312,7 +1312,7 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
     const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;
     void *fn = kernel_ptr(kind, f64, sidx);
     const size_t smem = ring_bytes(f64, kShapes[sidx].packed != 0);
-    GMI_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GMI_CUDA_TRY(raise_dynamic_smem_limit(fn, smem));
     int occ = 0;
     GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, tpb, smem));
     const int n_tgt_ctas = (n_tgt + tpb * tt - 1) / (tpb * tt);
@@ -1528,7 +1528,7 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     const int tpb = kShapes[sidx].tpb, tt = kShapes[sidx].tt;
     void *fn = kernel_ptr(kind, f64, sidx);
     const size_t smem = ring_bytes(f64, kShapes[sidx].packed != 0);
-    GMI_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GMI_CUDA_TRY(raise_dynamic_smem_limit(fn, smem));
     int occ = 0;
     GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, tpb, smem));
     const int n_tgt_ctas = (n_tgt + tpb * tt - 1) / (tpb * tt);

@@ -271,7 +271,7 @@ inline int blocks(int n) { return (n + kTpb - 1) / kTpb; }
 
 gmi_status dalloc0(double **p, size_t n, cudaStream_t st)
 {
-    GMI_CUDA_TRY(cudaMalloc(p, (n ? n : 1) * sizeof(double)));
+    GMI_CUDA_TRY(dev_malloc(p, (n ? n : 1) * sizeof(double)));
     GMI_CUDA_TRY(cudaMemsetAsync(*p, 0, (n ? n : 1) * sizeof(double), st));
     return GMI_OK;
 }
@@ -309,8 +309,8 @@ void prescribed_release(gmi_solver *s)
     if (!pw) return;
     krylov_free(pw->K);
     for (double *p : {pw->vel_dir, pw->phase, pw->P6, pw->rhs, pw->soln, pw->f6})
-        if (p) cudaFree(p);
-    if (pw->flag) cudaFree(pw->flag);
+        if (p) dev_free(p);
+    if (pw->flag) dev_free(pw->flag);
     delete pw;
     s->prescribed = nullptr;
 }

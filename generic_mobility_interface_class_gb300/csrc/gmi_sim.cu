@@ -1147,7 +1147,7 @@ static inline int gridN(int n, int tpb = 128) { return (n + tpb - 1) / tpb; }
 static gmi_status sim_alloc(gmi_sim *m, double **p, size_t count)
 {
     if (count == 0) count = 1;
-    GMI_CUDA_TRY(cudaMalloc(p, count * sizeof(double)));
+    GMI_CUDA_TRY(dev_malloc(p, count * sizeof(double)));
     m->allocs.push_back(*p);
     GMI_CUDA_TRY(cudaMemset(*p, 0, count * sizeof(double)));
     return GMI_OK;
@@ -1376,8 +1376,8 @@ gmi_status gmi_sim_destroy(gmi_sim *m)
         cudaSetDevice(m->solver->ctx->device);
         cudaStreamSynchronize(m->solver->ctx->stream);
     }
-    for (void *p : m->allocs) cudaFree(p);
-    if (m->h_flags) cudaFreeHost(m->h_flags);
+    for (void *p : m->allocs) dev_free(p);
+    if (m->h_flags) host_free(m->h_flags);
     if (m->solver) gmi_solver_destroy(m->solver);
     delete m;
     return GMI_OK;
@@ -1511,7 +1511,7 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
         m->tickets = reinterpret_cast<int *>(tk);
     }
 #undef SIM_ALLOC
-    if (cudaMallocHost(&m->h_flags, 4 * sizeof(int)) != cudaSuccess) {
+    if (host_alloc(&m->h_flags, 4 * sizeof(int)) != cudaSuccess) {
         set_last_error_msg("gmi_sim_create: pinned allocation failed");
         gmi_sim_destroy(m);
         return GMI_ERR_CUDA;

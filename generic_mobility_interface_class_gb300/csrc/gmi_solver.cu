@@ -1018,7 +1018,7 @@ static inline int grid_for(int n, int tpb = 256) { return (n + tpb - 1) / tpb; }
 static gmi_status dalloc(gmi_solver *s, double **p, size_t count)
 {
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc(p, count * sizeof(double));
+    cudaError_t e = dev_malloc(p, count * sizeof(double));
     if (e != cudaSuccess) {
         set_last_error(cudaGetErrorString(e), "cudaMalloc", __FILE__, __LINE__);
         return GMI_ERR_CUDA;
@@ -1031,7 +1031,7 @@ static gmi_status dalloc(gmi_solver *s, double **p, size_t count)
 static gmi_status halloc(double **p, size_t count)
 {
     if (count == 0) count = 1;
-    GMI_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void **>(p), count * sizeof(double), cudaHostAllocPortable));
+    GMI_CUDA_TRY(host_alloc(p, count * sizeof(double), cudaHostAllocPortable));
     std::memset(*p, 0, count * sizeof(double));
     return GMI_OK;
 }
@@ -1255,6 +1255,8 @@ static gmi_status capture_step(gmi_solver *s, cudaGraph_t body, cudaGraphConditi
                                cudaGraph_t *out)
 {
     cudaStream_t st = s->ctx->stream;
+    // no thread synchronises the device while this capture is open
+    std::lock_guard<std::recursive_mutex> lock(device_sync_mutex());
     if (body)
         GMI_CUDA_TRY(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
     else
@@ -1857,12 +1859,12 @@ gmi_status gmi_solver_destroy(gmi_solver *s)
     for (int g = 0; g < 2; ++g)
         if (s->graph[g]) cudaGraphExecDestroy(s->graph[g]);
     prescribed_release(s);
-    if (s->h_ctl) cudaFreeHost(s->h_ctl);
-    for (void *p : s->allocs) cudaFree(p);
+    if (s->h_ctl) host_free(s->h_ctl);
+    for (void *p : s->allocs) dev_free(p);
     double *hp[] = {s->h.v_segs_host, s->h.v_blobs_host, s->h.x_segs_host, s->h.x_blobs_host, s->h.f_segs_host,
                     s->h.f_blobs_host, s->h.f_blobs_repulsion_host, s->h_stage};
     for (double *p : hp)
-        if (p) cudaFreeHost(p);
+        if (p) host_free(p);
     if (s->ctx) gmi_context_destroy(s->ctx);
     delete s;
     return GMI_OK;
@@ -1977,7 +1979,7 @@ gmi_status gmi_solver_create(const gmi_solver_config *cfg, gmi_solver **out)
         TRY_OR_DIE(dalloc(s, &part_mem, max_splits * 3 * B));
         s->gm_partial = part_mem;
         s->gm_partial_bytes = max_splits * 3 * B * sizeof(double);
-        if (cudaMallocHost(&s->h_ctl, sizeof(GmresCtl)) != cudaSuccess) {
+        if (host_alloc(&s->h_ctl, sizeof(GmresCtl)) != cudaSuccess) {
             s->h_ctl = nullptr;
             set_last_error_msg("gmi_solver_create: pinned allocation failed");
             gmi_solver_destroy(s);

@@ -22,6 +22,9 @@ with DL = 2.2 RSEG (config.hpp:204).
 * ``config3``: R = 40a, 4096 Fibonacci-lattice blobs, 640 filaments of 20
   segments at seeded random surface points (rejection below an angular
   separation that keeps neighbouring bases 2 DL apart).
+* ``config4``: 64 independent swimmers of uneven size (radius 10a-40a,
+  642-4096 blobs, 16-512 filaments, fewer where the surface holds fewer),
+  a list of keyword sets for ``batch.SwimmerBatch``.
 
 The prescribed preferred-curvature beat and metachronal phase lag of the
 benchmark's description are not reference features; the filaments here beat
@@ -98,9 +101,48 @@ def config3(seed: int = 2026) -> dict:
     return free_swimmer(seeding.fibonacci_sphere(4096), fils, radius=radius, nseg=nseg, seed=seed)
 
 
+def max_filaments(radius: float, rseg: float = 1.0, rblob: float = 1.0, fill: float = 0.6) -> int:
+    """How many filament bases random sequential addition places on a body
+    of this radius with neighbouring bases 2 DL apart, as a fraction fill of
+    the jamming count (0.547 of the sphere covered by disks of radius DL)."""
+    dl = 2.2 * rseg
+    base = radius + 1.05 * (0.5 * dl + rblob)
+    return int(fill * 0.547 * 4.0 * np.pi * base * base / (np.pi * dl * dl))
+
+
+def config4(seed: int = 2026, nswim: int = 64, radius=(10.0, 40.0), blobs=(642, 4096), filaments=(16, 512),
+            nseg: int = 20) -> list[dict]:
+    """Independent swimmers of uneven size, one ``Simulation`` keyword set
+    each.  Per swimmer, from the seed: the radius uniform in ``radius``;
+    Fibonacci-lattice blobs, their count growing linearly with the radius
+    across ``blobs``; a filament count log-uniform in ``filaments``, capped by
+    ``max_filaments`` so that the bases keep 2 DL apart (a 10a sphere holds
+    40 of them); bases at random surface points."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(radius[0], radius[1], size=nswim)
+    f = np.exp(rng.uniform(np.log(filaments[0]), np.log(filaments[1]), size=nswim))
+    span = max(radius[1] - radius[0], 1e-300)
+    out = []
+    for i in range(nswim):
+        nblob = int(round(blobs[0] + (blobs[1] - blobs[0]) * (r[i] - radius[0]) / span))
+        nfil = max(1, min(int(round(f[i])), max_filaments(r[i])))
+        base = r[i] + 1.05 * (0.5 * 2.2 + 1.0)
+        fils = random_surface_points(nfil, 2.0 * 2.2 / base, seed + 1000 * (i + 1))
+        out.append(free_swimmer(seeding.fibonacci_sphere(nblob), fils, radius=float(r[i]), nseg=nseg,
+                                seed=seed + 1000 * (i + 1)))
+    return out
+
+
 WORKLOADS = {
     "config1": ("1 swimmer, R=10a, 642 icosphere blobs, 16 x 20 segments (962 particles)", config1),
     "config3": ("1 swimmer, R=40a, 4096 Fibonacci blobs, 640 x 20 segments (16,896 particles)", config3),
+}
+
+# Workloads of independent swimmers (a list of Simulation keyword sets), run
+# by batch.SwimmerBatch.
+BATCH_WORKLOADS = {
+    "config4": ("64 independent swimmers, R ~ U[10a, 40a], 642-4096 Fibonacci blobs, 16-512 (log-uniform, "
+                "capped by the surface) x 20 segments", config4),
 }
 
 
@@ -109,31 +151,47 @@ def main(argv=None) -> None:
     step, the Broyden and GMRES iteration counts and the wall time:
 
         python -m generic_mobility_interface_class_gb300.workloads config3 --precision fp32c --steps 3
+        python -m generic_mobility_interface_class_gb300.workloads config4 --swimmers 64 --steps 3
     """
     import argparse
     import time
 
     from . import build
     from ._lib import GMI_FP32C, GMI_FP64
+    from .batch import SwimmerBatch
     from .sim import Simulation
 
     p = argparse.ArgumentParser(prog="python -m generic_mobility_interface_class_gb300.workloads")
-    p.add_argument("workload", choices=sorted(WORKLOADS))
+    p.add_argument("workload", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
     p.add_argument("--precision", choices=["fp64", "fp32c"], default="fp32c")
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--device", type=int, default=0)
+    p.add_argument("--swimmers", type=int, default=64, help="swimmers of a batch workload")
+    p.add_argument("--threads", type=int, default=None, help="host threads of a batch workload (default: one each)")
     args = p.parse_args(argv)
     build.build()
-    desc, make = WORKLOADS[args.workload]
-    sim = Simulation(**make(), precision=GMI_FP32C if args.precision == "fp32c" else GMI_FP64, device=args.device)
-    t0 = time.perf_counter()
-    sim.prepare()
+    prec = GMI_FP32C if args.precision == "fp32c" else GMI_FP64
+    if args.workload in BATCH_WORKLOADS:
+        desc, make = BATCH_WORKLOADS[args.workload]
+        t0 = time.perf_counter()
+        sim = SwimmerBatch(make(nswim=args.swimmers), precision=prec, device=args.device, threads=args.threads)
+        sim.prepare()
+    else:
+        desc, make = WORKLOADS[args.workload]
+        t0 = time.perf_counter()
+        sim = Simulation(**make(), precision=prec, device=args.device)
+        sim.prepare()
     print(f"{args.workload} ({desc}), {args.precision}: prepare {1e3 * (time.perf_counter() - t0):.1f} ms", flush=True)
     for nt in range(args.steps):
         t0 = time.perf_counter()
-        b, g = sim.step(nt)
-        print(f"step {nt}: {b} Broyden iterations, {g} GMRES iterations, {1e3 * (time.perf_counter() - t0):.1f} ms",
-              flush=True)
+        it = sim.step(nt)
+        ms = 1e3 * (time.perf_counter() - t0)
+        if isinstance(it, list):
+            b, g = sum(x[0] for x in it), sum(x[1] for x in it)
+            print(f"step {nt}: {len(it)} swimmers, {b} Broyden and {g} GMRES iterations in all, {ms:.1f} ms",
+                  flush=True)
+        else:
+            print(f"step {nt}: {it[0]} Broyden iterations, {it[1]} GMRES iterations, {ms:.1f} ms", flush=True)
     sim.close()
 
 
