@@ -22,8 +22,9 @@ self pair included.  One step = one full apply.  Default N = 131072.
              (1 sphere of 642 blobs with 16 x 20 segments; 1 sphere of 4096
              blobs with 640 x 20 segments), plain FP64 against FP32C pair
              sums with FP64 solves, with the velocity error between the two;
-             with --ts-workloads config4, the aggregate rate of 64
-             independent swimmers of uneven size and the per-swimmer error
+             and (config4) the aggregate rate of 64 independent swimmers of
+             uneven size, one stream and host thread each, with the
+             per-swimmer error
 
 Runs one replica per GPU under torchrun (the apply does not shard here:
 "replicas only"), max-over-ranks time, rank 0 prints one JSON line.
@@ -70,10 +71,12 @@ def parse():
     p.add_argument("--shape", default=None,
                    help="pin the apply's launch shape instead of autotuning: threads,targets,splits,sources_per_step "
                         "(the traffic capture pins the shape the autotuner picks)")
-    p.add_argument("--ts-workloads", default="config1,config3",
+    p.add_argument("--ts-workloads", default="config1,config3,config4",
                    help="time-step workloads (comma separated; empty to skip)")
-    p.add_argument("--ts-steps", default="config1:100,config3:10", help="timed steps per workload")
+    p.add_argument("--ts-steps", default="config1:100,config3:10,config4:2", help="timed steps per workload")
     p.add_argument("--ts-warmup", type=int, default=5, help="untimed steps before the timed ones")
+    p.add_argument("--ts-warmups", default="config4:1",
+                   help="untimed steps per workload where they differ from --ts-warmup")
     p.add_argument("--ts-swimmers", type=int, default=64, help="swimmers of a batch time-step workload (config4)")
     return p.parse_args()
 
@@ -230,10 +233,15 @@ def run_time_steps(args, dev):
     from generic_mobility_interface_class_gb300.sim import Simulation
     from generic_mobility_interface_class_gb300._lib import GMI_FP32C, GMI_FP64
     steps_for = dict(kv.split(":") for kv in args.ts_steps.split(",") if kv)
+    warm_for = dict(kv.split(":") for kv in getattr(args, "ts_warmups", "").split(",") if kv)
     out = {}
     for name in [w for w in args.ts_workloads.split(",") if w]:
         if name in workloads.BATCH_WORKLOADS:
-            out[name] = run_batch_time_steps(args, dev, name, int(steps_for.get(name, 3)))
+            warm = int(warm_for.get(name, args.ts_warmup))
+            try:
+                out[name] = run_batch_time_steps(args, dev, name, int(steps_for.get(name, 3)), warm)
+            except Exception as e:  # keep the rest of the line
+                out[name] = {"error": f"{type(e).__name__}: {e}"}
             continue
         desc, make = workloads.WORKLOADS[name]
         kw = make()
@@ -275,7 +283,7 @@ def run_time_steps(args, dev):
     return out
 
 
-def run_batch_time_steps(args, dev, name, nsteps):
+def run_batch_time_steps(args, dev, name, nsteps, warmup):
     """Aggregate time-steps/sec of independent swimmers of uneven size
     (batch.SwimmerBatch: one stream and one host thread per swimmer), plain
     FP64 against FP32C pair sums with FP64 solves, and the per-swimmer error
@@ -290,14 +298,14 @@ def run_batch_time_steps(args, dev, name, nsteps):
     for label, prec in (("fp64", GMI_FP64), ("fp32c", GMI_FP32C)):
         batch = SwimmerBatch(swimmers, precision=prec, device=dev)
         batch.prepare()
-        for nt in range(args.ts_warmup):
+        for nt in range(warmup):
             batch.step(nt)
         torch.cuda.synchronize()
         l0 = batch.launches
         broyden, gmres = [], []
         with ClockSampler(dev) as clocks:
             t0 = time.perf_counter()
-            for nt in range(args.ts_warmup, args.ts_warmup + nsteps):
+            for nt in range(warmup, warmup + nsteps):
                 it = batch.step(nt)
                 broyden.append(sum(b for b, _ in it))
                 gmres.append(sum(g for _, g in it))
@@ -319,9 +327,11 @@ def run_batch_time_steps(args, dev, name, nsteps):
         return {"max": max(errs), "median": float(np.median(errs))}
 
     sizes = [(kw["nblob"], kw["nfil"] * kw["nseg"]) for kw in swimmers]
+    if len(swimmers) != 64:
+        desc = desc.replace("64 independent", f"{len(swimmers)} independent", 1)
     return {"workload": desc, "swimmers": len(swimmers), "blobs": sum(b for b, _ in sizes),
             "segments": sum(s for _, s in sizes), "host_threads": len(swimmers), "timed_steps": nsteps,
-            "warmup_steps": args.ts_warmup, "broyden_tol": swimmers[0]["tol"], "gmres_tol": swimmers[0]["linear_tol"],
+            "warmup_steps": warmup, "broyden_tol": swimmers[0]["tol"], "gmres_tol": swimmers[0]["linear_tol"],
             **runs,
             "speedup_fp32c_vs_fp64": runs["fp32c"]["swimmer_steps_per_s"] / runs["fp64"]["swimmer_steps_per_s"],
             "error_fp32c_vs_fp64_after_run": {"per_swimmer_velocity_rel": rel("body_v"),
