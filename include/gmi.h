@@ -53,6 +53,12 @@ GMI_API int gmi_version(void);
  * the launch-shape cache of the autotuner, and a device error word.
  * (The reference keeps the equivalent state in rpy_mobility_solver's
  * members, rpy_mobility_solver.hpp:45-58.)
+ *
+ * Threads: separate contexts (and the solvers and simulations built on
+ * them) may be driven from separate host threads at once; the library
+ * serialises graph captures with device-wide synchronising allocations and
+ * only ever raises a kernel's shared-memory limit.  One handle must not be
+ * used from two threads at once.
  * ---------------------------------------------------------------------- */
 typedef struct gmi_context gmi_context;
 
