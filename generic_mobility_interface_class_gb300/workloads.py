@@ -168,6 +168,8 @@ def main(argv=None) -> None:
     p.add_argument("--device", type=int, default=0)
     p.add_argument("--swimmers", type=int, default=64, help="swimmers of a batch workload")
     p.add_argument("--threads", type=int, default=None, help="host threads of a batch workload (default: one each)")
+    p.add_argument("--per-swimmer", action="store_true",
+                   help="batch workloads: also print each swimmer's Broyden and GMRES iterations per step")
     args = p.parse_args(argv)
     build.build()
     prec = GMI_FP32C if args.precision == "fp32c" else GMI_FP64
@@ -190,6 +192,8 @@ def main(argv=None) -> None:
             b, g = sum(x[0] for x in it), sum(x[1] for x in it)
             print(f"step {nt}: {len(it)} swimmers, {b} Broyden and {g} GMRES iterations in all, {ms:.1f} ms",
                   flush=True)
+            if args.per_swimmer:
+                print("  per swimmer (Broyden, GMRES): " + " ".join(f"{x[0]},{x[1]}" for x in it), flush=True)
         else:
             print(f"step {nt}: {it[0]} Broyden iterations, {it[1]} GMRES iterations, {ms:.1f} ms", flush=True)
     sim.close()
