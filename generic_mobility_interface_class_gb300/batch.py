@@ -96,6 +96,23 @@ class SwimmerBatch:
         self.nt = nt + 1
         return out
 
+    def run(self, steps, nt=None):
+        """steps time steps of every swimmer, each swimmer's thread going on
+        to its next step without waiting for the others (no batch-wide
+        barrier between steps, so the GPU keeps the large swimmers' work
+        and the small swimmers' next steps in flight together).  Returns,
+        per swimmer, its list of (Broyden iterations, GMRES iterations).
+        A swimmer that fails stops there; the others finish their steps and
+        the first failure (in swimmer order) is raised."""
+        nt = self.nt if nt is None else nt
+
+        def advance(s):
+            return [s.step(nt + i) for i in range(steps)]
+
+        out = self._map(advance, self.sims)
+        self.nt = nt + steps
+        return out
+
     def state(self, name):
         """The state field ``name`` of every swimmer (see ``Simulation.state``)."""
         return [s.state(name) for s in self.sims]

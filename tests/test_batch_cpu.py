@@ -135,3 +135,35 @@ def test_batch_creation_failure_closes_the_batch():
     assert len(made) == 4 and all(s.closed for s in made)
     with pytest.raises(ValueError):
         SwimmerBatch([], sim_factory=FakeSim)
+
+
+def test_batch_run_needs_no_batch_wide_barrier():
+    """run(steps): a swimmer goes on to its next step while another is still
+    in its first, which a per-step barrier would forbid."""
+    first_done = threading.Event()
+
+    class Slow(FakeSim):
+        def step(self, nt):
+            if self.name == 0 and nt == 0:
+                # swimmer 0 finishes its first step only once swimmer 1 has
+                # taken its second
+                assert first_done.wait(timeout=10)
+            if self.name == 1 and nt == 1:
+                first_done.set()
+            return super().step(nt)
+
+    batch = SwimmerBatch([dict(name=i) for i in range(2)], sim_factory=Slow)
+    out = batch.run(3)
+    assert out == [[(i, 0), (i, 10), (i, 20)] for i in range(2)]
+    assert batch.nt == 3 and all(s.nt_seen == [0, 1, 2] for s in batch.sims)
+    assert batch.step() == [(0, 30), (1, 30)]
+    batch.close()
+
+
+def test_batch_run_stops_a_failing_swimmer_only():
+    batch = SwimmerBatch([dict(name=i, fail_at=(1 if i == 0 else None)) for i in range(3)], sim_factory=FakeSim)
+    with pytest.raises(RuntimeError, match="swimmer 0 failed at step 1"):
+        batch.run(3)
+    assert batch.sims[0].nt_seen == [0, 1]
+    assert batch.sims[1].nt_seen == [0, 1, 2] and batch.sims[2].nt_seen == [0, 1, 2]
+    batch.close()
