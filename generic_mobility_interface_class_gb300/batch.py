@@ -71,9 +71,10 @@ class SwimmerBatch:
             for it in items:
                 try:
                     results.append(fn(it))
-                except BaseException as e:  # keep stepping the others, as the pool does
+                except Exception as e:  # keep stepping the others, as the pool does
                     results.append(None)
-                    first = first or e
+                    if first is None:
+                        first = e
             if first is not None:
                 raise first
             return results
