@@ -175,8 +175,10 @@ def make_inputs(n: int, seed: int = 2026):
     return x, f
 
 
-def cpu_sample(x, f, seconds: float):
-    """FP64 CPU oracle on a target slice sized for ~`seconds` of work."""
+def cpu_sample(x, f, seconds: float, keep: bool = False):
+    """FP64 CPU oracle on the target slice [0, nt) sized for ~`seconds` of
+    work.  Returns (nt, seconds taken, cores, the slice's velocities when
+    keep is set)."""
     from oracle import rpy
     n = x.shape[0]
     probe = min(n, 256)
@@ -185,10 +187,21 @@ def cpu_sample(x, f, seconds: float):
     dt = max(time.perf_counter() - t0, 1e-6)
     nt = int(min(n, max(probe, probe * seconds / dt)))
     t0 = time.perf_counter()
-    rpy.mss(x, f, targets=(0, nt))
+    v = rpy.mss(x, f, targets=(0, nt))
     dt = time.perf_counter() - t0
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return nt, dt, cores
+    return nt, dt, cores, (v if keep else None)
+
+
+def per_target_error(got, want):
+    """Max and RMS over targets of |got_i - want_i| / |want_i|, for the
+    velocity and the angular velocity of each target separately, and the
+    max-normalised error max|got - want| / max|want|."""
+    g = np.asarray(got, dtype=np.float64).reshape(-1, 3)
+    w = np.asarray(want, dtype=np.float64).reshape(-1, 3)
+    r = np.linalg.norm(g - w, axis=1) / np.maximum(np.linalg.norm(w, axis=1), 1e-300)
+    return {"max_rel_per_target": float(r.max()), "rms_rel_per_target": float(np.sqrt(np.mean(r * r))),
+            "max_normalised": float(np.abs(g - w).max() / np.abs(w).max())}
 
 
 def run_reference(args, world, rank):
@@ -201,7 +214,7 @@ def run_reference(args, world, rank):
     rpy.build(with_reference=False)
     x, f = make_inputs(args.n)
     n = x.shape[0]
-    nt, dt, cores = cpu_sample(x, f, max(1.0, min(args.cpu_seconds, 60.0) / max(args.steps, 1)))
+    nt, dt, cores, _ = cpu_sample(x, f, max(1.0, min(args.cpu_seconds, 60.0) / max(args.steps, 1)))
     for _ in range(args.warmup):
         rpy.mss(x, f, targets=(0, min(nt, 64)))
     times = []
@@ -417,6 +430,8 @@ def run_gmi(args, world, rank, local):
     # ---- accuracy of this precision against the FP64 path ------------------
     extra = {}
     v_main = vd.clone()
+    v_main_h = v_main.cpu().numpy()
+    v64_h = None
     if not args.no_fp64:
         ctx.set_precision(GMI_FP64)
         ctx.mss(xd, fd, out=vd)  # warm
@@ -427,6 +442,7 @@ def run_gmi(args, world, rank, local):
         torch.cuda.synchronize()
         t64 = a.elapsed_time(b) / 1e3
         v64 = vd.clone()
+        v64_h = v64.cpu().numpy()
         ctx.set_precision(prec)
         d = (v_main - v64)
         per_t = torch.linalg.norm(d, dim=1) / torch.linalg.norm(v64, dim=1)
@@ -456,9 +472,15 @@ def run_gmi(args, world, rank, local):
         try:
             from oracle import rpy
             rpy.build(with_reference=False)
-            nt, dt, cores = cpu_sample(x, f, args.cpu_seconds)
+            nt, dt, cores, v_cpu = cpu_sample(x, f, args.cpu_seconds, keep=True)
             cpu = {"value": nt * n / dt, "unit": "pairs/s", "cores": cores, "kind": "port",
                    "sample": f"FP64 oracle, {nt} targets x {n} sources ({dt:.1f} s), OpenMP over targets"}
+            # the GPU results on the same targets against the oracle's FP64 sums
+            err = {"targets": f"[0, {nt}) of {n}",
+                   args.precision: per_target_error(v_main_h[:nt], v_cpu)}
+            if v64_h is not None and args.precision != "fp64":
+                err["fp64"] = per_target_error(v64_h[:nt], v_cpu)
+            extra["error_vs_oracle"] = err
         except Exception as e:  # the baseline is reported, never the measured path
             cpu = {"value": None, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}

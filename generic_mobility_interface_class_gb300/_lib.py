@@ -48,6 +48,8 @@ SIGNATURES = {
     "gmi_context_precision": ([_P], _I),
     "gmi_context_synchronize": ([_P], _I),
     "gmi_context_launch_count": ([_P], ctypes.c_longlong),
+    "gmi_context_set_wait_deadline": ([_P, ctypes.c_longlong], _I),
+    "gmi_context_check_bounded_wait": ([_P, _I], _I),
     "gmi_Mss_mult": ([_P, _P, _P, _P, _I, _I, _I, _D, _D], _I),
     "gmi_Mss_mult_wall": ([_P, _P, _P, _P, _I, _I, _I], _I),
     "gmi_Mss_mult_noalloc": ([_P, _P, _P, _I, _I, _I, _D, _D, _I, _P], _I),
@@ -82,6 +84,8 @@ SIGNATURES = {
     "gmi_solver_set_body_reference_matrices": ([_P, _P, _P], _I),
     "gmi_solver_compute_velocities": ([_P, _P, _P, _P, ctypes.POINTER(_I)], _I),
     "gmi_solver_compute_velocities_prescribed": ([_P, _P, _P, _P, _P, ctypes.POINTER(_I)], _I),
+    "gmi_solver_last_linear_solve": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_D)], _I),
+    "gmi_solver_set_strict_convergence": ([_P, _I], _I),
     "gmi_solver_get_v_bodies": ([_P, _P], _I),
     "gmi_solver_set_v_bodies": ([_P, _P], _I),
     "gmi_sim_create": ([_P, _P, _P, _P, _P, _P, ctypes.POINTER(_P)], _I),
@@ -93,6 +97,27 @@ SIGNATURES = {
     "gmi_sim_backup_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),
     "gmi_sim_export_backup": ([_P, _P], _I),
     "gmi_sim_import_backup": ([_P, _P], _I),
+    "gmi_mlp_create": ([_I, _I, _I, _I, ctypes.c_ulonglong, ctypes.POINTER(_P)], _I),
+    "gmi_mlp_destroy": ([_P], _I),
+    "gmi_mlp_param_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "gmi_mlp_param_offsets": ([_P, _P], _I),
+    "gmi_mlp_get_params": ([_P, _P, ctypes.c_longlong], _I),
+    "gmi_mlp_set_params": ([_P, _P, ctypes.c_longlong], _I),
+    "gmi_mlp_forward": ([_P, _P, _I, _P], _I),
+    "gmi_mlp_backward": ([_P, _P, _I, _P], _I),
+    "gmi_mlp_secant_loss": ([_P, _P, ctypes.c_longlong, _I, _I, _P, ctypes.POINTER(_D), _P], _I),
+    "gmi_mlp_train_secant": ([_P, _P, ctypes.c_longlong, _I, _I, _I, _I, ctypes.c_float, ctypes.c_ulonglong, _P],
+                             _I),
+    "gmi_mlp_launch_count": ([_P], ctypes.c_longlong),
+    "gmi_learned_policy_init": ([_P], None),
+    "gmi_learned_policy_use_learned": ([_P], _I),
+    "gmi_learned_policy_iteration_cap": ([_P, _I], _I),
+    "gmi_learned_policy_record": ([_P, _I, _I, _I], None),
+    "gmi_sim_set_beat": ([_P, _D, _D, _P, _D], _I),
+    "gmi_sim_set_secant_buffer": ([_P, _P, ctypes.c_longlong], _I),
+    "gmi_sim_secant_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "gmi_sim_set_learned_jacobian": ([_P, _P, _I, _P], _I),
+    "gmi_sim_learned_policy": ([_P, _P], _I),
 }
 
 
@@ -107,6 +132,13 @@ class SimConfig(ctypes.Structure):
     """gmi_sim_config (include/gmi.h)."""
     _fields_ = [("mobility", SolverConfig), ("kb", _D), ("kt", _D), ("dt", _D), ("num_euler_steps", _I),
                 ("max_broyden_iter", _I), ("tol", _D), ("jacobian_confidence", _D), ("body_radius", _D)]
+
+
+class LearnedPolicy(ctypes.Structure):
+    """gmi_learned_policy (include/gmi.h)."""
+    _fields_ = [("calibration_steps", _I), ("window", _I), ("max_regressions", _I), ("margin", _D),
+                ("cap_factor", _D), ("mode", _I), ("steps_plain", _I), ("steps_learned", _I), ("regressions", _I),
+                ("plain_iters_sum", _D), ("recent", _I * 64), ("recent_count", _I)]
 
 
 class HostArrays(ctypes.Structure):

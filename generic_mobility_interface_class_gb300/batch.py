@@ -57,7 +57,19 @@ class SwimmerBatch:
             self.sims = made  # close whatever was built
             self.close()
             raise
-        self.nt = 0
+        # the next time step of each swimmer: advanced per swimmer as each of
+        # its steps completes, so after a failure every swimmer's count is
+        # the steps it really took
+        self.next_nt = [0] * len(self.sims)
+
+    @property
+    def nt(self):
+        """The next time step of the batch: every swimmer's, when they agree;
+        after a failure that left them apart, a ValueError names them
+        (``next_nt`` holds each swimmer's)."""
+        if len(set(self.next_nt)) != 1:
+            raise ValueError(f"swimmers are at different time steps: {self.next_nt}")
+        return self.next_nt[0]
 
     def __len__(self):
         return len(self.sims)
@@ -90,12 +102,18 @@ class SwimmerBatch:
         return self._map(lambda s: s.prepare(), self.sims)
 
     def step(self, nt=None):
-        """One implicit time step of every swimmer; returns the per-swimmer
-        (Broyden iterations, GMRES iterations)."""
-        nt = self.nt if nt is None else nt
-        out = self._map(lambda s: s.step(nt), self.sims)
-        self.nt = nt + 1
-        return out
+        """One implicit time step of every swimmer (time step nt, or each
+        swimmer's own next step); returns the per-swimmer (Broyden
+        iterations, GMRES iterations).  A swimmer that fails keeps its step
+        count; the others advance, and the first failure is raised."""
+
+        def one(i):
+            t = self.next_nt[i] if nt is None else nt
+            r = self.sims[i].step(t)
+            self.next_nt[i] = t + 1
+            return r
+
+        return self._map(one, range(len(self.sims)))
 
     def run(self, steps, nt=None):
         """steps time steps of every swimmer, each swimmer's thread going on
@@ -103,16 +121,19 @@ class SwimmerBatch:
         barrier between steps, so the GPU keeps the large swimmers' work
         and the small swimmers' next steps in flight together).  Returns,
         per swimmer, its list of (Broyden iterations, GMRES iterations).
-        A swimmer that fails stops there; the others finish their steps and
-        the first failure (in swimmer order) is raised."""
-        nt = self.nt if nt is None else nt
+        A swimmer that fails stops there, with ``next_nt`` at the step that
+        failed; the others finish their steps and the first failure (in
+        swimmer order) is raised."""
 
-        def advance(s):
-            return [s.step(nt + i) for i in range(steps)]
+        def advance(i):
+            t0 = self.next_nt[i] if nt is None else nt
+            out = []
+            for k in range(steps):
+                out.append(self.sims[i].step(t0 + k))
+                self.next_nt[i] = t0 + k + 1
+            return out
 
-        out = self._map(advance, self.sims)
-        self.nt = nt + steps
-        return out
+        return self._map(advance, range(len(self.sims)))
 
     def state(self, name):
         """The state field ``name`` of every swimmer (see ``Simulation.state``)."""

@@ -13,10 +13,12 @@ namespace gmi {
 
 constexpr double kPi = 3.14159265358979323846264338327950288;
 
-// Device-side error bits, OR-ed into the solver's device error word.
+// Device-side error bits, OR-ed into the context's device error word.
+// (Non-finite values are not flagged here: the host checks every residual it
+// reads -- GMRES's, the refinement's, Broyden's -- and a NaN residual also
+// ends the device-side Arnoldi loop, whose convergence test fails for it.)
 enum : unsigned {
     kDevErrWaitTimeout = 1u << 0,  // an mbarrier wait ran past its deadline
-    kDevErrNonFinite = 1u << 1,    // a reduction saw a NaN or Inf
 };
 
 // Programmatic dependent launch.  A kernel launched with the programmatic
@@ -36,8 +38,10 @@ __device__ __forceinline__ void pdl_wait_then_release()
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
-// Upper bound for any spin on an mbarrier: 2 s of %globaltimer.  A wait that
-// runs past it records kDevErrWaitTimeout and the kernel returns.
+// Upper bound for any spin on an mbarrier: by default 2 s of %globaltimer
+// (a context can set its own, gmi_context_set_wait_deadline; a launch passes
+// it by value, 0 meaning the default).  A wait that runs past it records
+// kDevErrWaitTimeout and the kernel returns.
 constexpr unsigned long long kWaitDeadlineNs = 2000000000ull;
 
 #define GMI_CUDA_TRY(expr)                                        \
@@ -88,6 +92,11 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned by
                  : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
 {
     unsigned ok;
@@ -109,14 +118,16 @@ __device__ __forceinline__ unsigned long long global_ns()
 }
 
 // Wait for the mbarrier phase with the given parity to complete, giving up
-// after kWaitDeadlineNs.  Returns false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity)
+// after deadline_ns (kWaitDeadlineNs when 0).  Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity,
+                                                  unsigned long long deadline_ns = 0)
 {
     if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long limit = deadline_ns ? deadline_ns : kWaitDeadlineNs;
     const unsigned long long t0 = global_ns();
     for (unsigned it = 0;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255u) == 255u && global_ns() - t0 > kWaitDeadlineNs) return false;
+        if ((it & 255u) == 255u && global_ns() - t0 > limit) return false;
     }
 }
 

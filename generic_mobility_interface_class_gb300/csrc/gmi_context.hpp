@@ -49,6 +49,7 @@ struct gmi_context {
     std::map<gmi::TuneKey, gmi::PairShape> tuned;
     int last_splits = 1;  // source splits of the last tiled pair launch (the autotuner reads it)
     void *encode_tiled = nullptr;    // cuTensorMapEncodeTiled from the driver
+    unsigned long long wait_ns = 0;  // deadline of the pair kernels' bounded waits (0: kWaitDeadlineNs)
 };
 
 namespace gmi {

@@ -16,6 +16,7 @@
 // bounds the problem to kMaxSegs segments.  All calls share it and it keeps
 // the contents of the last call, so two calls that overlap on the GPU
 // (different streams, or different host threads on one device) race on it.
+#include <map>
 #include <mutex>
 
 #include "gmi_context.hpp"
@@ -26,14 +27,17 @@ namespace {
 constexpr size_t kScratchBytes = size_t(16) << 20;
 constexpr int kMaxSegs = 32768;
 constexpr size_t kErrBytes = 256;  // the device error word, then records, then partial sums
-constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Per-device set-up, done on the first call on that device with the device
-// current: the device address of g_noalloc_scratch (in host code the name
-// g_noalloc_scratch is only a host-side stand-in, not a device address), the
-// SM count, and the driver's tensor-map encoder.
+// Per-context set-up, done on the first call in a CUDA context with that
+// context current: the device address of g_noalloc_scratch (in host code the
+// name g_noalloc_scratch is only a host-side stand-in, not a device
+// address), the SM count, and the driver's tensor-map encoder.  The address
+// belongs to the context the module was loaded into, so the table is keyed
+// by the current driver context (the device's primary context for runtime
+// API callers; a context of the caller's own made current with
+// cuCtxSetCurrent gets its own entry).
 struct DeviceSetup {
     unsigned char *scratch = nullptr;
     int sm_count = 0;
@@ -41,26 +45,62 @@ struct DeviceSetup {
     bool ready = false;
 };
 
-DeviceSetup g_setup[kMaxDevices];
+std::map<CUcontext, DeviceSetup> g_setup;
 std::mutex g_setup_mutex;
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+
+gmi_status current_driver_context(CUcontext *ctx)
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    if (get_current == nullptr) {
+        cudaDriverEntryPointQueryResult q;
+        void *fn = nullptr;
+        GMI_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q));
+        if (q != cudaDriverEntryPointSuccess || fn == nullptr) {
+            gmi::set_last_error_msg("driver does not provide cuCtxGetCurrent");
+            return GMI_ERR_CUDA;
+        }
+        get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+    }
+    *ctx = nullptr;
+    if (get_current(ctx) != CUDA_SUCCESS || *ctx == nullptr) {
+        gmi::set_last_error_msg("gmi_Mss_mult_noalloc: no current CUDA context");
+        return GMI_ERR_CUDA;
+    }
+    return GMI_OK;
+}
+
+gmi_status scratch_address(void **p)
+{
+    *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(p, g_noalloc_scratch);
+    if (e != cudaSuccess || *p == nullptr) {
+        gmi::set_last_error(cudaGetErrorString(e), "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+        return GMI_ERR_CUDA;
+    }
+    return GMI_OK;
+}
 
 gmi_status setup_current_device(DeviceSetup **out)
 {
     int dev = 0;
     GMI_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) {
-        gmi::set_last_error_msg("gmi_Mss_mult_noalloc: device index beyond the set-up table");
-        return GMI_ERR_ARG;
-    }
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    DeviceSetup &d = g_setup[dev];
+    CUcontext cu = nullptr;
+    void *p = nullptr;
+    if (current_driver_context(&cu) != GMI_OK) {
+        // no context is current on this thread yet: the symbol lookup makes
+        // the runtime bind the device's primary context, which is then current
+        gmi_status ps = scratch_address(&p);
+        if (ps != GMI_OK) return ps;
+        ps = current_driver_context(&cu);
+        if (ps != GMI_OK) return ps;
+    }
+    DeviceSetup &d = g_setup[cu];
     if (!d.ready) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            gmi::set_last_error(cudaGetErrorString(e), "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__,
-                                __LINE__);
-            return GMI_ERR_CUDA;
+        if (p == nullptr) {
+            gmi_status ps = scratch_address(&p);
+            if (ps != GMI_OK) return ps;
         }
         int sms = 0;
         GMI_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -92,7 +132,7 @@ extern "C" gmi_status gmi_Mss_mult_noalloc(double *V_d, const double *F_d, const
         set_last_error_msg("gmi_Mss_mult_noalloc: null argument");
         return GMI_ERR_ARG;
     }
-    if (!(start_seg >= 0 && num_segs >= 0 && start_seg + num_segs <= total_segs)) {
+    if (!(start_seg >= 0 && num_segs >= 0 && (long long)start_seg + num_segs <= (long long)total_segs)) {
         set_last_error_msg("gmi_Mss_mult_noalloc: target range outside [0, total_segs)");
         return GMI_ERR_ARG;
     }

@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(TPB) rpy_pair_kernel(const __grid_constant__ C
     int t = 0;
     for (; t < ntiles; ++t) {
         const int s = t % kStages;
-        const bool ok = mbar_wait_bounded(&bars[s], (t / kStages) & 1);
+        const bool ok = mbar_wait_bounded(&bars[s], (t / kStages) & 1, args.wait_ns);
         if (__syncthreads_or(!ok)) {
             timed_out = true;
             break;
@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(TPB) rpy_bb_df_kernel(const __grid_constant__ 
     int t = 0;
     for (; t < ntiles; ++t) {
         const int s = t % kStages;
-        const bool ok = mbar_wait_bounded(&bars[s], (t / kStages) & 1);
+        const bool ok = mbar_wait_bounded(&bars[s], (t / kStages) & 1, args.wait_ns);
         if (__syncthreads_or(!ok)) {
             timed_out = true;
             break;
@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(TPB) rpy_pair2_kernel(const __grid_constant__ 
     int t = 0;
     for (; t < ntiles; ++t) {
         const int s = t % kStagesP;
-        const bool ok = mbar_wait_bounded(&bars[s], (t / kStagesP) & 1);
+        const bool ok = mbar_wait_bounded(&bars[s], (t / kStagesP) & 1, args.wait_ns);
         const int j0 = j_begin + t * kTile;
         const int jn = min(kTile, j_end - j0);
         const int npair = (jn + 1) >> 1;
@@ -1229,6 +1229,7 @@ static gmi_status launch_bb_df(gmi_context *ctx, const void *tgt_rec, int tgt_st
     a.out = out;
     a.accumulate = accumulate;
     a.err = ctx->d_err;
+    a.wait_ns = ctx->wait_ns;
     a.partial = nullptr;
     if (splits > 1) {
         gmi_status st = ctx->partial.reserve((size_t)splits * n_tgt * 3 * sizeof(double));
@@ -1304,6 +1305,7 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
         a.out = out;
         a.accumulate = accumulate;
         a.err = ctx->d_err;
+        a.wait_ns = ctx->wait_ns;
         const gmi_status ws = launch_warp(ctx->stream, kind, f64, shape.tt, a, src_rec);
         if (ws == GMI_OK) ctx->launches++;
         return ws;
@@ -1332,6 +1334,7 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
     a.out = out;
     a.accumulate = accumulate;
     a.err = ctx->d_err;
+    a.wait_ns = ctx->wait_ns;
     a.partial = nullptr;
     if (splits > 1) {
         gmi_status st = ctx->partial.reserve((size_t)splits * n_tgt * nout * sizeof(double));
@@ -1521,6 +1524,7 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
         a.out = out;
         a.accumulate = accumulate;
         a.err = env.err;
+        a.wait_ns = env.wait_ns;
         a.skip = env.skip;
         return launch_warp(env.stream, kind, f64, env.tt, a, src_rec, env.pdl != 0);
     }
@@ -1555,6 +1559,7 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     a.out = out;
     a.accumulate = accumulate;
     a.err = env.err;
+    a.wait_ns = env.wait_ns;
     a.partial = splits > 1 ? env.partial : nullptr;
     a.skip = env.skip;
     CUtensorMap map;

@@ -22,6 +22,7 @@ struct PairLaunch {
     int accumulate;
     unsigned *err;
     const int *skip;      // if non-null and *skip != 0 the launch does nothing (converged GMRES)
+    unsigned long long wait_ns;  // deadline of the source-tile waits (0: kWaitDeadlineNs)
 };
 
 struct BarrierLaunch {
@@ -84,6 +85,7 @@ struct ExplicitPairEnv {
                            // p < *splits_out) itself; 1 means the kernel wrote `out` directly
     int pdl;               // non-zero: launch for programmatic dependent launch (the pair kernel
                            // waits for the previous kernel in pdl_wait_then_release)
+    unsigned long long wait_ns;  // deadline of the source-tile waits (0: kWaitDeadlineNs)
 };
 
 size_t record_bytes(bool f64);

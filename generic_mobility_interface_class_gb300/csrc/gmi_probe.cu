@@ -1,7 +1,8 @@
-// gmi_probe.cu -- FMA-pipe throughput probe.  The pair kernels are bound by
-// the FP32 (or FP64) FMA pipe, not by HBM or the tensor cores, so their
-// roofline denominator is measured on the running GPU with this kernel:
-// eight independent FMA chains per thread, enough CTAs to fill every SM.
+// gmi_probe.cu -- FMA-pipe throughput probe, and the check of the bounded
+// mbarrier wait.  The pair kernels are bound by the FP32 (or FP64) FMA pipe,
+// not by HBM or the tensor cores, so their roofline denominator is measured
+// on the running GPU with fma_probe_kernel: eight independent FMA chains per
+// thread, enough CTAs to fill every SM.
 #include "gmi_context.hpp"
 
 namespace gmi {
@@ -23,9 +24,53 @@ __global__ void __launch_bounds__(256) fma_probe_kernel(R seed, int iters, R *si
     if (s == R(-12345.0)) sink[0] = s;  // never true; keeps the chains live
 }
 
+// One CTA waits on an mbarrier that expects two arrivals, through the same
+// bounded wait (mbar_wait_bounded) as the pair kernels' source-tile waits.
+// With withhold == 0 both arrivals come and the wait completes; with
+// withhold == 1 the second never comes (a flag nothing sets), the wait gives
+// up after deadline_ns and records kDevErrWaitTimeout, and the kernel
+// returns.  No asynchronous copy is involved.
+__global__ void bounded_wait_check_kernel(int withhold, unsigned long long deadline_ns, unsigned *err)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 2);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_arrive(&bar);
+    if (threadIdx.x == 1 && withhold == 0) mbar_arrive(&bar);
+    if (threadIdx.x == 0 && !mbar_wait_bounded(&bar, 0, deadline_ns)) atomicOr(err, kDevErrWaitTimeout);
+}
+
 }  // namespace gmi
 
 using namespace gmi;
+
+extern "C" gmi_status gmi_context_set_wait_deadline(gmi_context *ctx, long long nanoseconds)
+{
+    if (ctx == nullptr || nanoseconds < 0 || (nanoseconds != 0 && nanoseconds < 1000) ||
+        nanoseconds > 60000000000ll) {
+        set_last_error_msg("gmi_context_set_wait_deadline: null context, or a deadline outside [1 us, 60 s] "
+                           "(0 restores the default of 2 s)");
+        return GMI_ERR_ARG;
+    }
+    ctx->wait_ns = (unsigned long long)nanoseconds;
+    return GMI_OK;
+}
+
+extern "C" gmi_status gmi_context_check_bounded_wait(gmi_context *ctx, int withhold_arrival)
+{
+    if (ctx == nullptr || (withhold_arrival != 0 && withhold_arrival != 1)) {
+        set_last_error_msg("gmi_context_check_bounded_wait: null context or withhold_arrival not 0/1");
+        return GMI_ERR_ARG;
+    }
+    GMI_CUDA_TRY(cudaSetDevice(ctx->device));
+    bounded_wait_check_kernel<<<1, 32, 0, ctx->stream>>>(withhold_arrival, ctx->wait_ns, ctx->d_err);
+    GMI_CUDA_TRY(cudaGetLastError());
+    ctx->launches++;
+    return context_check_device_errors(ctx);
+}
 
 extern "C" gmi_status gmi_measure_fma_peak(gmi_context *ctx, int precision, double *flops_per_s)
 {

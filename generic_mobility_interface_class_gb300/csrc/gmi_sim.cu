@@ -38,6 +38,7 @@
 #include "gmi_context.hpp"
 #include "gmi_gauss_jordan.hpp"
 #include "gmi_lie.cuh"
+#include "gmi_mlp.hpp"
 #include "gmi_solver_device.cuh"
 #include "gmi_solver_internal.hpp"
 
@@ -1115,6 +1116,160 @@ __global__ void vec_div2_kernel(int n, double *a, double *b, const double *nrm2)
     }
 }
 
+// ---- prescribed preferred-curvature beat ----------------------------------
+// filament::body_frame_moment's strain_twist (filament.cpp:1104-1106) as a
+// time-dependent preferred bending curvature: for time step nt (solving for
+// t = (nt + 1) dt), strain_twist = (0, A sin(2 pi t / T + phase_f), 0).
+__global__ void beat_strain_kernel(SimP P, const double *phase, double amplitude, double omega, double t)
+{
+    const int fil = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fil >= P.F) return;
+    P.st[3 * fil] = 0.0;
+    P.st[3 * fil + 1] = amplitude * sin(omega * t + phase[fil]);
+    P.st[3 * fil + 2] = 0.0;
+}
+
+// ---- learned initial inverse Jacobian ------------------------------------
+// Each filament's local frame: e3 along its base direction (R_body fref; +z
+// on the wall), e1 the body's x axis (its y axis near the poles) made
+// orthogonal to e3, e2 = e3 x e1.  frames[9 fil + 3 c + j] = (e_c)_j.
+__device__ void filament_frame(const SimP &P, int fil, double E[9])
+{
+    double e1[3], e3[3];
+    if (P.wall) {
+        e3[0] = 0.0; e3[1] = 0.0; e3[2] = 1.0;
+        e1[0] = 1.0; e1[1] = 0.0; e1[2] = 0.0;
+    } else {
+        const int n = fil / P.NF;
+        const M3 R = q_rot_mat(ldq(P.bq + 4 * n));
+        double a[3];
+        m3_vec(R, P.fref + 3 * fil, a);
+        const double na = sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        for (int c = 0; c < 3; ++c) e3[c] = a[c] / na;
+        double x[3] = {R(0, 0), R(1, 0), R(2, 0)};
+        if (fabs(x[0] * e3[0] + x[1] * e3[1] + x[2] * e3[2]) > 0.9) {
+            x[0] = R(0, 1); x[1] = R(1, 1); x[2] = R(2, 1);
+        }
+        const double d = x[0] * e3[0] + x[1] * e3[1] + x[2] * e3[2];
+        for (int c = 0; c < 3; ++c) e1[c] = x[c] - d * e3[c];
+        const double n1 = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+        for (int c = 0; c < 3; ++c) e1[c] /= n1;
+    }
+    const double e2[3] = {e3[1] * e1[2] - e3[2] * e1[1], e3[2] * e1[0] - e3[0] * e1[2], e3[0] * e1[1] - e3[1] * e1[0]};
+    for (int c = 0; c < 3; ++c) {
+        E[c] = e1[c];
+        E[3 + c] = e2[c];
+        E[6 + c] = e3[c];
+    }
+}
+
+// Thread per filament: its frame and its features phi (per segment, the
+// position relative to the base over the filament length, then the
+// tangent, both in the local frame), FP32 and bf16.
+__global__ void filament_features_kernel(SimP P, double *frames, float *phi, __nv_bfloat16 *phi16)
+{
+    const int fil = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fil >= P.F) return;
+    double E[9];
+    filament_frame(P, fil, E);
+    for (int k = 0; k < 9; ++k) frames[9 * (size_t)fil + k] = E[k];
+    const int s0 = fil * P.NS, n6 = P.n6;
+    const double inv_len = 1.0 / (P.NS * P.DL);
+    for (int i = 0; i < P.NS; ++i) {
+        const int sg = s0 + i;
+        double d[3], t[3];
+        for (int c = 0; c < 3; ++c) d[c] = P.x[3 * sg + c] - P.x[3 * s0 + c];
+        q_tangent(ldq(P.q + 4 * sg), t);
+        for (int c = 0; c < 3; ++c) {
+            const double pv = (E[3 * c] * d[0] + E[3 * c + 1] * d[1] + E[3 * c + 2] * d[2]) * inv_len;
+            const double tv = E[3 * c] * t[0] + E[3 * c + 1] * t[1] + E[3 * c + 2] * t[2];
+            const size_t o = (size_t)fil * n6 + 6 * i;
+            phi[o + c] = (float)pv;
+            phi[o + 3 + c] = (float)tv;
+            phi16[o + c] = __float2bfloat16_rn((float)pv);
+            phi16[o + 3 + c] = __float2bfloat16_rn((float)tv);
+        }
+    }
+}
+
+// tmp_f <- sigma (.) tmp_f + (1/conf) E^T U V^T E in_f for every filament f
+// (tmp holds Jinv in from jacobian_inv_mult; the caller's combine step
+// multiplies by -conf), one CTA per filament; the body rows are left as
+// they are.  O: the network's output rows [F x n_out] (see gmi_mlp.cu).
+template <int R>
+__global__ void __launch_bounds__(128) learned_apply_kernel(SimP P, const float *__restrict__ O, int n_out,
+                                                            const double *__restrict__ frames,
+                                                            const double *__restrict__ in, double *__restrict__ tmp,
+                                                            double inv_conf)
+{
+    extern __shared__ double dl[];  // n6: in_f in the local frame
+    __shared__ double red[4][R], y[R];
+    const int fil = blockIdx.x, n = fil / P.NF, i = fil % P.NF, NS = P.NS, n6 = P.n6, nblk = 2 * NS;
+    const size_t base = (size_t)n * P.per_body + (size_t)6 * NS * i;
+    const double *E = frames + 9 * (size_t)fil;
+    const float *o = O + (size_t)fil * n_out, *U = o + nblk, *V = U + (size_t)n6 * R;
+    for (int k = threadIdx.x; k < nblk; k += 128) {
+        const double *v = in + base + 3 * k;
+        for (int c = 0; c < 3; ++c) dl[3 * k + c] = E[3 * c] * v[0] + E[3 * c + 1] * v[1] + E[3 * c + 2] * v[2];
+    }
+    __syncthreads();
+    double yp[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) yp[j] = 0.0;
+    for (int r = threadIdx.x; r < n6; r += 128)
+#pragma unroll
+        for (int j = 0; j < R; ++j) yp[j] += (double)V[r * R + j] * dl[r];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+        const double v = warp_sum_d(yp[j]);
+        if (lane == 0) red[w][j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < R) y[threadIdx.x] = red[0][threadIdx.x] + red[1][threadIdx.x] + red[2][threadIdx.x] +
+                                          red[3][threadIdx.x];
+    __syncthreads();
+    for (int k = threadIdx.x; k < nblk; k += 128) {
+        double cl[3];
+        for (int c = 0; c < 3; ++c) {
+            double a = 0.0;
+#pragma unroll
+            for (int j = 0; j < R; ++j) a += (double)U[(3 * k + c) * R + j] * y[j];
+            cl[c] = a;
+        }
+        const double sg = exp((double)fminf(fmaxf(o[k], -3.f), 3.f));
+        double *t = tmp + base + 3 * k;
+        for (int c = 0; c < 3; ++c) {
+            const double lab = E[c] * cl[0] + E[3 + c] * cl[1] + E[6 + c] * cl[2];
+            t[c] = sg * t[c] + inv_conf * lab;
+        }
+    }
+}
+
+// One secant-pair record per filament (layout in gmi_mlp.cu): phi, then
+// d = dv_f, b = conf jv_f, t = upd_f rotated into the local frame; record
+// index first + fil, skipped past capacity.
+__global__ void secant_record_kernel(SimP P, const double *__restrict__ frames, const float *__restrict__ phi,
+                                     const double *__restrict__ dv, const double *__restrict__ jv,
+                                     const double *__restrict__ upd, double conf, float *__restrict__ rec,
+                                     long long first, long long cap)
+{
+    const int fil = blockIdx.x, n = fil / P.NF, i = fil % P.NF, n6 = P.n6, nblk = 2 * P.NS;
+    const long long r = first + fil;
+    if (r >= cap) return;
+    float *out = rec + r * (long long)(4 * n6);
+    const size_t base = (size_t)n * P.per_body + (size_t)6 * P.NS * i;
+    const double *E = frames + 9 * (size_t)fil;
+    for (int c = threadIdx.x; c < n6; c += blockDim.x) out[c] = phi[(size_t)fil * n6 + c];
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) {
+        const double *src[3] = {dv + base + 3 * k, jv + base + 3 * k, upd + base + 3 * k};
+        const double sc[3] = {1.0, conf, 1.0};
+        for (int q = 0; q < 3; ++q)
+            for (int c = 0; c < 3; ++c)
+                out[(q + 1) * n6 + 3 * k + c] =
+                    (float)(sc[q] * (E[3 * c] * src[q][0] + E[3 * c + 1] * src[q][1] + E[3 * c + 2] * src[q][2]));
+    }
+}
 }  // namespace gmi
 
 // ---------------------------------------------------------------------------
@@ -1137,6 +1292,31 @@ struct gmi_sim {
     int broyden_iter = 0;
     bool use_gj_cluster = true;   // GMI_GJ_CLUSTER=0: one CTA per Jacobian inversion always
     bool use_gj_registers = true;  // GMI_GJ_REGISTERS=0: the columns stepped through shared memory
+    // learned initial inverse Jacobian (gmi_sim_set_learned_jacobian)
+    const gmi_mlp *mlp = nullptr;
+    int rank = 0;
+    gmi_learned_policy policy{};
+    bool learned_now = false;       // this Broyden solve applies the network's H0
+    double *frames = nullptr;       // [F x 9] local frames
+    float *phi = nullptr;           // [F x n6] features
+    __nv_bfloat16 *phi16 = nullptr, *H1 = nullptr, *H2 = nullptr;
+    float *O = nullptr;             // [F x n_out] network outputs of this step
+    bool features_ready = false;
+    // secant-pair collection (gmi_sim_set_secant_buffer)
+    float *sec = nullptr;
+    long long sec_cap = 0, sec_count = 0;
+    double *dv = nullptr, *jv = nullptr;  // d = change of the error, Jinv d
+    // prescribed preferred-curvature beat (gmi_sim_set_beat)
+    double *beat_phase = nullptr;
+    double beat_amplitude = 0.0, beat_period = 1.0;
+    bool beat = false;
+    // the state after the initial guess, for a learned step that is restarted plain
+    struct Field {
+        double *p;
+        size_t n;
+    };
+    std::vector<Field> snap_fields;
+    double *snap = nullptr;
 };
 
 namespace gmi {
@@ -1150,6 +1330,15 @@ static gmi_status sim_alloc(gmi_sim *m, double **p, size_t count)
     GMI_CUDA_TRY(dev_malloc(p, count * sizeof(double)));
     m->allocs.push_back(*p);
     GMI_CUDA_TRY(cudaMemset(*p, 0, count * sizeof(double)));
+    return GMI_OK;
+}
+
+static gmi_status sim_alloc_bytes(gmi_sim *m, void **p, size_t bytes)
+{
+    if (bytes < 16) bytes = 16;
+    GMI_CUDA_TRY(dev_malloc(p, bytes));
+    m->allocs.push_back(*p);
+    GMI_CUDA_TRY(cudaMemset(*p, 0, bytes));
     return GMI_OK;
 }
 
@@ -1249,11 +1438,60 @@ static gmi_status dots_with_D(gmi_sim *m, const double *v, int k)
     return sim_launched(m);
 }
 
+// The network's H0 on top of jacobian_inv_mult's result (learned steps only).
+static gmi_status learned_apply(gmi_sim *m, const double *in, double *tmp)
+{
+    const SimP &P = m->P;
+    const size_t smem = (size_t)P.n6 * sizeof(double);
+    const int no = m->mlp->n_out;
+    const double ic = 1.0 / P.conf;
+    switch (m->rank) {
+    case 2: learned_apply_kernel<2><<<P.F, 128, smem, sst(m)>>>(P, m->O, no, m->frames, in, tmp, ic); break;
+    case 4: learned_apply_kernel<4><<<P.F, 128, smem, sst(m)>>>(P, m->O, no, m->frames, in, tmp, ic); break;
+    default: learned_apply_kernel<8><<<P.F, 128, smem, sst(m)>>>(P, m->O, no, m->frames, in, tmp, ic); break;
+    }
+    return sim_launched(m);
+}
+
+// features and frames of this step's state (after the initial guess), and
+// the network's output when the step is a learned one
+static gmi_status learned_prepare(gmi_sim *m)
+{
+    const SimP &P = m->P;
+    m->features_ready = false;
+    if (!(m->learned_now || m->sec)) return GMI_OK;
+    filament_features_kernel<<<gridN(P.F, 64), 64, 0, sst(m)>>>(P, m->frames, m->phi, m->phi16);
+    GMI_TRY(sim_launched(m));
+    if (m->learned_now) {
+        GMI_TRY(mlp_forward_ws(m->mlp, sst(m), m->phi16, P.F, m->H1, m->H2, m->O));
+        GMI_TRY(sim_launched(m, 3));
+    }
+    m->features_ready = true;
+    return GMI_OK;
+}
+
+// one secant-pair record per filament for this iteration (plain steps only)
+static gmi_status record_secant_pairs(gmi_sim *m)
+{
+    const SimP &P = m->P;
+    if (!m->sec || m->learned_now || !m->features_ready || m->sec_count >= m->sec_cap) return GMI_OK;
+    const int n = P.nbroy;
+    vec_sub_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, m->nerr, m->err, m->dv);
+    GMI_TRY(sim_launched(m));
+    GMI_TRY(jacobian_inv_mult(m, m->dv, m->jv));
+    secant_record_kernel<<<P.F, 64, 0, sst(m)>>>(P, m->frames, m->phi, m->dv, m->jv, m->upd, P.conf, m->sec,
+                                                  m->sec_count, m->sec_cap);
+    GMI_TRY(sim_launched(m));
+    m->sec_count = std::min(m->sec_cap, m->sec_count + P.F);
+    return GMI_OK;
+}
+
 // broyden_solver::find_update (broyden_solver.cpp:26-68)
 static gmi_status find_update(gmi_sim *m)
 {
     const int n = m->P.nbroy, it = m->broyden_iter;
     GMI_TRY(jacobian_inv_mult(m, m->err, m->tmp));
+    if (m->learned_now) GMI_TRY(learned_apply(m, m->err, m->tmp));
     GMI_TRY(dots_with_D(m, m->err, it));
     broyden_combine_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, -m->P.conf, m->tmp, m->C, (size_t)n, m->dots, it,
                                                               m->upd);
@@ -1264,9 +1502,11 @@ static gmi_status find_update(gmi_sim *m)
 static gmi_status end_of_iter(gmi_sim *m, bool too_large)
 {
     const int n = m->P.nbroy, it = m->broyden_iter;
+    GMI_TRY(record_secant_pairs(m));
     if (too_large && it < m->maxb - 1) {
         double *Ccol = m->C + (size_t)n * it, *Dcol = m->D + (size_t)n * it;
         GMI_TRY(jacobian_inv_mult(m, m->nerr, m->tmp));
+        if (m->learned_now) GMI_TRY(learned_apply(m, m->nerr, m->tmp));
         GMI_TRY(dots_with_D(m, m->nerr, it));
         broyden_combine_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, -m->P.conf, m->tmp, m->C, (size_t)n, m->dots,
                                                                   it, Ccol);
@@ -1594,7 +1834,69 @@ gmi_status gmi_sim_prepare(gmi_sim *m, double *body_mobility_out)
     return GMI_OK;
 }
 
-// One time step, cilia_sim_main.cpp:207-343 (GMRES branch).
+}  // extern "C"
+
+namespace gmi {
+
+// Copy the state a Broyden solve changes to the snapshot (restore = false)
+// or back (restore = true): segment x, q, u, the filament multipliers, the
+// body x, u, q and the linear solver's warm start.
+static gmi_status snapshot_state(gmi_sim *m, bool restore)
+{
+    size_t off = 0;
+    for (const auto &f : m->snap_fields) {
+        double *a = m->snap + off;
+        GMI_CUDA_TRY(cudaMemcpyAsync(restore ? f.p : a, restore ? a : f.p, f.n * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, sst(m)));
+        off += f.n;
+    }
+    return GMI_OK;
+}
+
+// Broyden's method from the initial guess (cilia_sim_main.cpp:266-314), at
+// most cap iterations.  *too_large: the error still above tolerance at the
+// end; *diverged: a non-finite error.
+static gmi_status broyden_solve(gmi_sim *m, int nt, int cap, int *iters, int *gtot, bool *too_large,
+                                bool *diverged)
+{
+    int gi = 0;
+    bool nonfinite = false;
+    *too_large = false;
+    *diverged = false;
+    GMI_TRY(forces_and_torques(m, nt));
+    GMI_TRY(velocities_and_errors(m, nt, m->err, too_large, &nonfinite, &gi));
+    *gtot += gi;
+    if (*too_large) {
+        GMI_TRY(prepare_jacobian_inv(m, nt));
+        GMI_TRY(learned_prepare(m));
+    }
+    m->broyden_iter = 0;
+    while (*too_large && m->broyden_iter < cap) {
+        GMI_TRY(find_update(m));
+        GMI_TRY(swimmer_update(m));
+        GMI_TRY(forces_and_torques(m, nt));
+        GMI_TRY(velocities_and_errors(m, nt, m->nerr, too_large, &nonfinite, &gi));
+        *gtot += gi;
+        if (nonfinite) {
+            *diverged = true;
+            break;
+        }
+        GMI_TRY(end_of_iter(m, *too_large));
+    }
+    *iters = m->broyden_iter;
+    return GMI_OK;
+}
+
+}  // namespace gmi
+
+extern "C" {
+
+// One time step, cilia_sim_main.cpp:207-343 (GMRES branch).  With a learned
+// initial inverse Jacobian the policy decides whether this step tries it; a
+// learned attempt that misses the policy's iteration cap or diverges is
+// restarted from the step's initial guess with the plain H0, so the step's
+// outcome never depends on the network.  broyden_iters counts every
+// iteration done, the abandoned attempt's included.
 gmi_status gmi_sim_step(gmi_sim *m, int nt, int *broyden_iters, int *gmres_iters_total)
 {
     SIM_ARG_CHECK(m != nullptr && nt >= 0, "gmi_sim_step: bad argument");
@@ -1604,32 +1906,149 @@ gmi_status gmi_sim_step(gmi_sim *m, int nt, int *broyden_iters, int *gmres_iters
     if (!P.wall) body_initial_guess_kernel<<<gridN(P.W, 32), 32, 0, sst(m)>>>(P, nt);
     filament_initial_guess_kernel<<<gridN(P.F, 64), 64, 0, sst(m)>>>(P, nt);
     GMI_TRY(sim_launched(m, P.wall ? 1 : 2));
-    GMI_TRY(forces_and_torques(m, nt));
-    int gi = 0, gtot = 0;
-    bool too_large = false, nonfinite = false;
-    GMI_TRY(velocities_and_errors(m, nt, m->err, &too_large, &nonfinite, &gi));
-    gtot += gi;
-    if (too_large) GMI_TRY(prepare_jacobian_inv(m, nt));
-    m->broyden_iter = 0;
-    while (too_large && m->broyden_iter < m->maxb) {
-        GMI_TRY(find_update(m));
-        GMI_TRY(swimmer_update(m));
-        GMI_TRY(forces_and_torques(m, nt));
-        GMI_TRY(velocities_and_errors(m, nt, m->nerr, &too_large, &nonfinite, &gi));
-        gtot += gi;
-        if (nonfinite) {
-            set_last_error_msg("Broyden's method diverged (non-finite residual)");
-            return GMI_ERR_NONFINITE;
-        }
-        GMI_TRY(end_of_iter(m, too_large));
+    if (m->beat) {
+        beat_strain_kernel<<<gridN(P.F, 64), 64, 0, sst(m)>>>(P, m->beat_phase, m->beat_amplitude,
+                                                              2.0 * kPi / m->beat_period, (nt + 1) * P.DT);
+        GMI_TRY(sim_launched(m));
     }
-    if (broyden_iters) *broyden_iters = m->broyden_iter;
+    const bool policy_on = m->mlp != nullptr;
+    m->learned_now = policy_on && gmi_learned_policy_use_learned(&m->policy);
+    if (m->learned_now) GMI_TRY(snapshot_state(m, false));
+    const int cap = m->learned_now ? gmi_learned_policy_iteration_cap(&m->policy, m->maxb) : m->maxb;
+    int iters = 0, gtot = 0;
+    bool too_large = false, diverged = false;
+    gmi_status st = broyden_solve(m, nt, cap, &iters, &gtot, &too_large, &diverged);
+    int total = iters;
+    if (st == GMI_OK && m->learned_now) {
+        const bool ok = !too_large && !diverged;
+        gmi_learned_policy_record(&m->policy, 1, ok ? 1 : 0, iters);
+        if (!ok) {  // restart from the initial guess with the plain H0
+            m->learned_now = false;
+            st = snapshot_state(m, true);
+            int it2 = 0;
+            if (st == GMI_OK) st = broyden_solve(m, nt, m->maxb, &it2, &gtot, &too_large, &diverged);
+            if (st == GMI_OK) gmi_learned_policy_record(&m->policy, 0, (!too_large && !diverged) ? 1 : 0, it2);
+            total += it2;
+        }
+    } else if (st == GMI_OK && policy_on) {
+        gmi_learned_policy_record(&m->policy, 0, (!too_large && !diverged) ? 1 : 0, iters);
+    }
+    m->learned_now = false;
+    GMI_TRY(st);
+    if (broyden_iters) *broyden_iters = total;
     if (gmres_iters_total) *gmres_iters_total = gtot;
     GMI_TRY(context_check_device_errors(m->solver->ctx));
+    if (diverged) {
+        set_last_error_msg("Broyden's method diverged (non-finite residual)");
+        return GMI_ERR_NONFINITE;
+    }
     if (too_large) {
         set_last_error_msg("Broyden's method did not converge within max_broyden_iter iterations");
         return GMI_ERR_NOT_CONVERGED;
     }
+    return GMI_OK;
+}
+
+gmi_status gmi_sim_set_beat(gmi_sim *m, double amplitude, double period, const double *phases_h,
+                            double end_force_scale)
+{
+    SIM_ARG_CHECK(m != nullptr && phases_h != nullptr && period > 0 && std::isfinite(amplitude) &&
+                      end_force_scale >= 0,
+                  "gmi_sim_set_beat: bad argument");
+    GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
+    if (!m->beat_phase) GMI_TRY(sim_alloc(m, &m->beat_phase, m->P.F));
+    GMI_CUDA_TRY(cudaMemcpy(m->beat_phase, phases_h, (size_t)m->P.F * sizeof(double), cudaMemcpyHostToDevice));
+    m->beat_amplitude = amplitude;
+    m->beat_period = period;
+    m->beat = true;
+    m->P.EFM = m->cfg.mobility.end_force_magnitude * end_force_scale;
+    return GMI_OK;
+}
+
+gmi_status gmi_sim_set_secant_buffer(gmi_sim *m, float *records_d, long long capacity)
+{
+    SIM_ARG_CHECK(m != nullptr && capacity >= 0, "gmi_sim_set_secant_buffer: bad argument");
+    GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
+    GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
+    m->sec_count = 0;
+    if (records_d == nullptr || capacity == 0) {
+        m->sec = nullptr;
+        m->sec_cap = 0;
+        return GMI_OK;
+    }
+    const SimP &P = m->P;
+    const size_t F = P.F, n6 = P.n6;
+    if (!m->dv) {
+        GMI_TRY(sim_alloc(m, &m->dv, P.nbroy));
+        GMI_TRY(sim_alloc(m, &m->jv, P.nbroy));
+    }
+    if (!m->frames) {
+        GMI_TRY(sim_alloc(m, &m->frames, 9 * F));
+        GMI_TRY(sim_alloc_bytes(m, (void **)&m->phi, F * n6 * sizeof(float)));
+        GMI_TRY(sim_alloc_bytes(m, (void **)&m->phi16, F * n6 * sizeof(__nv_bfloat16)));
+    }
+    m->sec = records_d;
+    m->sec_cap = capacity;
+    return GMI_OK;
+}
+
+gmi_status gmi_sim_secant_count(const gmi_sim *m, long long *count)
+{
+    SIM_ARG_CHECK(m != nullptr && count != nullptr, "gmi_sim_secant_count: null argument");
+    *count = m->sec_count;
+    return GMI_OK;
+}
+
+gmi_status gmi_sim_set_learned_jacobian(gmi_sim *m, const gmi_mlp *mlp, int rank, const gmi_learned_policy *policy)
+{
+    SIM_ARG_CHECK(m != nullptr, "gmi_sim_set_learned_jacobian: null simulation");
+    GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
+    GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
+    if (mlp == nullptr) {
+        m->mlp = nullptr;
+        return GMI_OK;
+    }
+    const SimP &P = m->P;
+    SIM_ARG_CHECK(rank == 2 || rank == 4 || rank == 8, "gmi_sim_set_learned_jacobian: rank must be 2, 4 or 8");
+    SIM_ARG_CHECK(mlp->n_in == P.n6 && 2 * P.NS + 2 * P.n6 * rank <= mlp->n_out,
+                  "gmi_sim_set_learned_jacobian: the network's widths do not fit 6 nseg inputs and this rank");
+    SIM_ARG_CHECK(mlp->device == m->solver->ctx->device,
+                  "gmi_sim_set_learned_jacobian: the network lives on another device");
+    const size_t F = P.F, n6 = P.n6;
+    if (!m->frames) {
+        GMI_TRY(sim_alloc(m, &m->frames, 9 * F));
+        GMI_TRY(sim_alloc_bytes(m, (void **)&m->phi, F * n6 * sizeof(float)));
+        GMI_TRY(sim_alloc_bytes(m, (void **)&m->phi16, F * n6 * sizeof(__nv_bfloat16)));
+    }
+    if (!m->mlp || m->mlp->n_hidden != mlp->n_hidden || m->mlp->n_out != mlp->n_out || !m->O) {
+        GMI_TRY(sim_alloc_bytes(m, (void **)&m->H1, F * mlp->n_hidden * sizeof(__nv_bfloat16)));
+        GMI_TRY(sim_alloc_bytes(m, (void **)&m->H2, F * mlp->n_hidden * sizeof(__nv_bfloat16)));
+        GMI_TRY(sim_alloc_bytes(m, (void **)&m->O, F * mlp->n_out * sizeof(float)));
+    }
+    if (!m->snap) {
+        const size_t S = P.S, W = P.W;
+        gmi_solver *s = m->solver;
+        m->snap_fields = {{P.x, 3 * S},   {P.q, 4 * S},  {P.u, 3 * S},  {P.lam, 3 * (P.NS - 1) * F},
+                          {P.tl, 3 * F},  {P.cl, 3 * F}, {P.bx, 3 * W}, {P.bu, 3 * W},
+                          {P.bq, 4 * W},  {P.vb, 6 * W}};
+        if (s->B > 0) m->snap_fields.push_back({s->f_blobs, 3 * (size_t)s->B});
+        size_t total = 0;
+        for (const auto &f : m->snap_fields) total += f.n;
+        GMI_TRY(sim_alloc(m, &m->snap, total));
+    }
+    m->mlp = mlp;
+    m->rank = rank;
+    if (policy)
+        m->policy = *policy;
+    else
+        gmi_learned_policy_init(&m->policy);
+    return GMI_OK;
+}
+
+gmi_status gmi_sim_learned_policy(const gmi_sim *m, gmi_learned_policy *out)
+{
+    SIM_ARG_CHECK(m != nullptr && out != nullptr, "gmi_sim_learned_policy: null argument");
+    *out = m->policy;
     return GMI_OK;
 }
 

@@ -1217,6 +1217,7 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     env.partial = s->gm_partial;
     env.partial_bytes = s->gm_partial_bytes;
     env.err = ctx->d_err;
+    env.wait_ns = ctx->wait_ns;
     env.encode_tiled = ctx->encode_tiled;
     env.sm_count = ctx->sm_count;
     if (nb <= kPairWarpMaxSources) {
@@ -1373,7 +1374,10 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
         GMI_TRY(launched(s));
         GMI_TRY(device_norm(s, s->w, n));
         GMI_TRY(read_scalar(s, s->scal, &beta0));
-        if (fabs(beta0) <= tol * norm_ref) return GMI_OK;  // the initial guess is good enough
+        if (fabs(beta0) <= tol * norm_ref) {  // the initial guess is good enough
+            s->gm_resid = fabs(beta0) / norm_ref;
+            return GMI_OK;
+        }
         if (reject_warm_start && fabs(beta0) > norm_b) {
             GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
             GMI_CUDA_TRY(cudaMemcpyAsync(s->w, s->rhs, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -1467,6 +1471,7 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
                 set_last_error_msg("GMRES produced a non-finite residual");
                 return GMI_ERR_NONFINITE;
             }
+            s->gm_resid = s->h_ctl->resid;
             const int iter = s->h_ctl->k;
             backsolve_warp_kernel<<<1, 32, 0, st>>>(s->H, ldh, s->beta, iter, s->yv, nullptr);
             combine_kernel<<<grid_for(n, 64), 64, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp, nullptr);
@@ -1499,6 +1504,7 @@ static gmi_status gmres_run(gmi_solver *s, double norm_b, double norm_ref, doubl
             return GMI_ERR_NONFINITE;
         }
         if (resid <= tol || iter == max_iter) {
+            s->gm_resid = resid;
             backsolve_warp_kernel<<<1, 32, 0, st>>>(s->H, ldh, s->beta, iter, s->yv, nullptr);
             combine_kernel<<<grid_for(n, 64), 64, 0, st>>>(s->Q, ld, s->yv, iter, n, s->tmp, nullptr);
             GMI_TRY(launched(s, 2));
@@ -1528,6 +1534,7 @@ static gmi_status gmres_finish_pending(gmi_solver *s, int *iters)
         set_last_error_msg("GMRES produced a non-finite residual");
         return GMI_ERR_NONFINITE;
     }
+    s->gm_resid = s->h_ctl->resid;
     *iters += s->h_ctl->k;
     return GMI_OK;
 }
@@ -1571,6 +1578,8 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
     const double tol = s->cfg.linear_tol;
     cudaStream_t st = s->ctx->stream;
     *iters_out = 0;
+    s->last_rel_resid = 0.0;  // a zero right-hand side is solved exactly
+    s->last_iters = 0;
     const int prec = s->ctx->precision;
     auto check_rhs = [&](double norm) -> gmi_status {
         if (!std::isfinite(norm)) {
@@ -1601,6 +1610,8 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         int iters = 0;
         GMI_TRY(gmres_run(s, norm_rhs, norm_rhs, tol, true, false, &iters));
         *iters_out = iters;
+        s->last_rel_resid = s->gm_resid;
+        s->last_iters = iters;
         return store_solution(s);
     }
     // Mixed-precision refinement.  The residual of the warm start is formed
@@ -1651,6 +1662,7 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
             set_last_error_msg("non-finite residual in the refinement loop");
             return GMI_ERR_NONFINITE;
         }
+        s->last_rel_resid = beta / norm_rhs;
         if (beta <= tol * norm_rhs) break;
         if (outer == 0 && beta > norm_rhs) {  // reject a poor warm start, as the reference does
             GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
@@ -1672,9 +1684,19 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
     if (s->ctl_pending) {  // the refinement cap ended the loop after a solve
         GMI_CUDA_TRY(cudaStreamSynchronize(st));
         GMI_TRY(gmres_finish_pending(s, &total));
+        // the residual after that last correction (the loop had no turn left
+        // to check it): r -= A delta, as at the top of the loop
+        GMI_TRY(system_matrix_mult(s, s->z, s->tmp));
+        axpby_kernel<<<grid_for(n), 256, 0, st>>>(n, 1.0, s->rhs, -1.0, s->tmp, s->rhs);
+        GMI_TRY(launched(s));
+        GMI_TRY(device_norm(s, s->rhs, n));
+        double beta = 0.0;
+        GMI_TRY(read_scalar(s, s->scal, &beta));
+        s->last_rel_resid = beta / norm_rhs;
     }
     GMI_CUDA_TRY(cudaMemcpyAsync(s->rhs, s->b64, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
     *iters_out = total;
+    s->last_iters = total;
     return store_solution(s);
 }
 
@@ -2163,6 +2185,26 @@ gmi_status gmi_solver_compute_velocities(gmi_solver *s, const double *body_x, co
     GMI_TRY(context_check_device_errors(s->ctx));
     if (!s->cfg.wall) std::memcpy(body_f, s->h_stage + 8, 6 * W * sizeof(double));
     if (num_gmres_iterations) *num_gmres_iterations = iters;
+    if (s->strict && !s->cfg.wall && !(s->last_rel_resid <= s->cfg.linear_tol)) {
+        set_last_error_msg("gmi_solver_compute_velocities: the linear solve stopped at its iteration cap above "
+                           "the tolerance (results were written back; gmi_solver_last_linear_solve has the residual)");
+        return GMI_ERR_NOT_CONVERGED;
+    }
+    return GMI_OK;
+}
+
+gmi_status gmi_solver_set_strict_convergence(gmi_solver *s, int strict)
+{
+    GMI_ARG_CHECK(s != nullptr, "gmi_solver_set_strict_convergence: null solver");
+    s->strict = strict != 0;
+    return GMI_OK;
+}
+
+gmi_status gmi_solver_last_linear_solve(const gmi_solver *s, int *iterations, double *relative_residual)
+{
+    GMI_ARG_CHECK(s != nullptr, "gmi_solver_last_linear_solve: null solver");
+    if (iterations) *iterations = s->last_iters;
+    if (relative_residual) *relative_residual = s->last_rel_resid;
     return GMI_OK;
 }
 

@@ -27,6 +27,13 @@ struct gmi_solver {
     double *b64 = nullptr, *xacc = nullptr;  // refinement: FP64 right-hand side, accumulated solution
     double *scal = nullptr;  // device scalars: [0] norm, [1] resid
     bool refs_set = false;
+    // the last linear solve: its relative residual (GMRES's estimate |beta|/||b||
+    // in FP64; the FP64-grade refinement residual in FP32C) and whether it met
+    // the tolerance; strict makes compute_velocities report a solve that did not
+    double last_rel_resid = 0.0;
+    int last_iters = 0;
+    bool strict = false;
+    double gm_resid = 0.0;  // relative residual estimate at the end of the last gmres_run
     std::vector<void *> allocs;
     // device-controlled Arnoldi iterations replayed from a CUDA graph
     struct GmresCtl *ctl = nullptr;   // device control block

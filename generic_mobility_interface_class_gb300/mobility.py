@@ -51,6 +51,15 @@ class Context:
     def launches(self) -> int:
         return int(self.lib.gmi_context_launch_count(self.handle))
 
+    def set_wait_deadline(self, nanoseconds: int) -> None:
+        """Deadline of the pair kernels' bounded waits (0: the 2 s default)."""
+        check(self.lib.gmi_context_set_wait_deadline(self.handle, int(nanoseconds)))
+
+    def check_bounded_wait(self, withhold_arrival: bool) -> None:
+        """Run the bounded-wait check kernel; raises GmiError
+        (GMI_ERR_DEVICE_TIMEOUT) when an arrival is withheld."""
+        check(self.lib.gmi_context_check_bounded_wait(self.handle, int(withhold_arrival)))
+
     def close(self) -> None:
         if getattr(self, "handle", None):
             self.lib.gmi_context_destroy(self.handle)

@@ -24,7 +24,7 @@ class Simulation:
                  perturbation2=None, mu=1.0, rseg=1.0, rblob=1.0, kb, kt, dt, end_force_magnitude,
                  repulsive_force_factor=2.0, body_radius, tol=1e-4, max_broyden_iter=100, jacobian_confidence=0.1,
                  num_euler_steps=1, linear_tol=1e-10, max_linear_iter=150, precision=GMI_FP64, device=0,
-                 wall=False):
+                 wall=False, beat=None):
         self.lib = _lib.load()
         mob = SolverConfig(nswim, nfil, nseg, nblob, mu, rseg, rblob, repulsive_force_factor, end_force_magnitude,
                            int(wall), max_linear_iter, linear_tol, precision, device)
@@ -47,6 +47,8 @@ class Simulation:
         check(self.lib.gmi_sim_create(ctypes.byref(cfg), *[p for _, p in arrays], ctypes.byref(h)))
         self.handle = h
         self.nt = 0
+        if beat is not None:  # dict(amplitude, period, phases, end_force_scale)
+            self.set_beat(**beat)
 
     def prepare(self):
         mob = np.zeros(36)
@@ -104,6 +106,53 @@ class Simulation:
                                 self.state("seg_v"), self.state("seg_f_internal"),
                                 None if self.wall else self.state("body_v"),
                                 None if self.wall else self.state("blob_f"), digits)
+
+    def set_beat(self, amplitude, period, phases, end_force_scale=0.0):
+        """Prescribed preferred-curvature beat (gmi_sim_set_beat): the
+        filaments' preferred bending curvature is amplitude sin(2 pi t /
+        period + phase), phases one per filament; end_force_scale 0 turns
+        the end force off."""
+        ph, p = _c(np.asarray(phases, dtype=np.float64).reshape(-1))
+        if ph.size != self.F:
+            raise ValueError(f"need {self.F} phases, got {ph.size}")
+        check(self.lib.gmi_sim_set_beat(self.handle, float(amplitude), float(period), p, float(end_force_scale)))
+
+    # -- learned initial inverse Jacobian ------------------------------------
+    def set_secant_buffer(self, records, capacity=None):
+        """Collect one secant-pair record per filament and plain Broyden
+        iteration into ``records`` (a float32 CUDA tensor of shape
+        (capacity, 24 nseg)); None stops collecting."""
+        if records is None:
+            check(self.lib.gmi_sim_set_secant_buffer(self.handle, None, 0))
+            self._secant = None
+            return
+        cap = records.shape[0] if capacity is None else capacity
+        if records.dtype.itemsize != 4 or records.shape[1] != 24 * self.nseg or not records.is_contiguous():
+            raise ValueError("records must be a contiguous float32 tensor of shape (capacity, 24 nseg)")
+        self._secant = records
+        check(self.lib.gmi_sim_set_secant_buffer(self.handle, ctypes.c_void_p(records.data_ptr()), cap))
+
+    def secant_count(self) -> int:
+        n = ctypes.c_longlong()
+        check(self.lib.gmi_sim_secant_count(self.handle, ctypes.byref(n)))
+        return n.value
+
+    def set_learned_jacobian(self, net, policy=None):
+        """Start Broyden from the network's initial inverse Jacobian
+        (``learned.LearnedJacobian``; None: the plain method) under
+        ``policy`` (a ``_lib.LearnedPolicy``; None: defaults)."""
+        if net is None:
+            check(self.lib.gmi_sim_set_learned_jacobian(self.handle, None, 0, None))
+            self._net = None
+            return
+        self._net = net  # keep the network alive while the simulation uses it
+        check(self.lib.gmi_sim_set_learned_jacobian(self.handle, net.handle, net.rank,
+                                                    ctypes.byref(policy) if policy is not None else None))
+
+    def learned_policy(self):
+        out = _lib.LearnedPolicy()
+        check(self.lib.gmi_sim_learned_policy(self.handle, ctypes.byref(out)))
+        return out
 
     @property
     def launches(self):

@@ -135,6 +135,17 @@ class MobilitySolver:
                                                                 ctypes.byref(it)))
         return it.value
 
+    def last_linear_solve(self):
+        """(GMRES iterations, relative residual) of the last linear solve."""
+        it, res = ctypes.c_int(), ctypes.c_double()
+        check(self.lib.gmi_solver_last_linear_solve(self.handle, ctypes.byref(it), ctypes.byref(res)))
+        return it.value, res.value
+
+    def set_strict_convergence(self, strict: bool) -> None:
+        """Report a linear solve that stops at its cap above tolerance as
+        GMI_ERR_NOT_CONVERGED (the reference accepts it silently)."""
+        check(self.lib.gmi_solver_set_strict_convergence(self.handle, int(strict)))
+
     def v_bodies(self):
         out = np.zeros((self.W, 6))
         check(self.lib.gmi_solver_get_v_bodies(self.handle, _cptr(out)))

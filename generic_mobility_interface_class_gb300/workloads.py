@@ -25,10 +25,16 @@ with DL = 2.2 RSEG (config.hpp:204).
 * ``config4``: 64 independent swimmers of uneven size (radius 10a-40a,
   642-4096 blobs, 16-512 filaments, fewer where the surface holds fewer),
   a list of keyword sets for ``batch.SwimmerBatch``.
+* ``config5``: R = 100a, 10,242 icosphere blobs (5 subdivisions), 8000
+  filaments of 20 segments on a Fibonacci lattice (170,242 particles).
 
-The prescribed preferred-curvature beat and metachronal phase lag of the
-benchmark's description are not reference features; the filaments here beat
-through the reference's own end-force instability.
+``config1_beat`` and ``config3_beat`` drive the same geometries the way the
+benchmark describes them instead: a prescribed sinusoidal preferred-curvature
+beat (period 1, a random phase per filament for config 1, the metachronal
+lag 2 pi (azimuth / 2 pi) 4 for config 3), KB = KT = 1, dt = 1/300, no end
+force.  The beat is not a reference feature; it enters through the
+reference's own preferred-curvature hook (strain_twist,
+filament.cpp:1104-1106; gmi_sim_set_beat).
 """
 from __future__ import annotations
 
@@ -55,12 +61,13 @@ def _perturbations(rng, nfil: int, magnitude: float):
 
 
 def free_swimmer(blob_seeds, fil_seeds, radius: float, nseg: int, seed: int, rseg: float = 1.0, rblob: float = 1.0,
-                 tol: float = 1e-4, linear_tol: float = 1e-8, max_linear_iter: int = 150) -> dict:
+                 tol: float = 1e-4, linear_tol: float = 1e-8, max_linear_iter: int = 150, kb: float = 1800.0,
+                 kt: float = 1800.0) -> dict:
     blob_seeds = np.asarray(blob_seeds, dtype=np.float64)
     fil_seeds = np.asarray(fil_seeds, dtype=np.float64)
     nfil = fil_seeds.shape[0]
     dl = 2.2 * rseg
-    phys = instability_parameters(nseg, rseg)
+    phys = instability_parameters(nseg, rseg, kb, kt)
     p1, p2 = _perturbations(np.random.default_rng(seed + 17), nfil, 0.01 * phys["end_force_magnitude"])
     return dict(nfil=nfil, nseg=nseg, nblob=blob_seeds.shape[0], blob_refs=radius * blob_seeds,
                 fil_refs=fil_seeds * (radius + 1.05 * (0.5 * dl + rblob)), perturbation1=p1, perturbation2=p2,
@@ -133,9 +140,59 @@ def config4(seed: int = 2026, nswim: int = 64, radius=(10.0, 40.0), blobs=(642, 
     return out
 
 
+def config5(seed: int = 2026) -> dict:
+    """R = 100a, 10,242 icosphere blobs (5 subdivisions), 8000 filaments of
+    20 segments (170,242 particles), driven by the instability end force.
+    8000 bases do not fit at 2 DL apart on this sphere (about 2,800 do), so
+    they sit on a Fibonacci lattice, about 4a (1.8 DL) apart."""
+    return free_swimmer(seeding.icosphere(5), seeding.fibonacci_sphere(8000), radius=100.0, nseg=20, seed=seed)
+
+
+# ---- the prescribed preferred-curvature beat ---------------------------------
+# KB = KT = 1, dt = 1/300, period 1; the preferred bending curvature
+# amplitude sin(2 pi t + phase), with amplitude pi / (2 L) (a quarter turn
+# over the filament length L = NSEG DL); no end force (the barrier keeps the
+# instability workloads' scale for KB = 1).  An extension of the reference
+# through its strain_twist hook (filament.cpp:1104-1106).
+BEAT_PERIOD = 1.0
+
+
+def beat_swimmer(blob_seeds, fil_seeds, radius: float, nseg: int, seed: int, phases) -> dict:
+    kw = free_swimmer(blob_seeds, fil_seeds, radius, nseg, seed, kb=1.0, kt=1.0)
+    kw["dt"] = BEAT_PERIOD / STEPS_PER_PERIOD
+    length = nseg * 2.2 * kw["rseg"]
+    kw["beat"] = dict(amplitude=np.pi / (2.0 * length), period=BEAT_PERIOD,
+                      phases=np.asarray(phases, dtype=np.float64), end_force_scale=0.0)
+    return kw
+
+
+def config1_beat(seed: int = 2026) -> dict:
+    """config1's geometry driven by the beat, a random phase per filament."""
+    verts = seeding.icosphere(3)
+    rng = np.random.default_rng(seed)
+    fils = verts[rng.choice(len(verts), 16, replace=False)]
+    phases = np.random.default_rng(seed + 5).uniform(0.0, 2.0 * np.pi, size=16)
+    return beat_swimmer(verts, fils, radius=10.0, nseg=20, seed=seed, phases=phases)
+
+
+def config3_beat(seed: int = 2026) -> dict:
+    """config3's geometry driven by the beat with the metachronal phase lag
+    2 pi (azimuth / 2 pi) 4, the azimuth of each filament's base."""
+    radius, nseg = 40.0, 20
+    base = radius + 1.05 * (0.5 * 2.2 + 1.0)
+    fils = random_surface_points(640, 2.0 * 2.2 / base, seed)
+    azimuth = np.mod(np.arctan2(fils[:, 1], fils[:, 0]), 2.0 * np.pi)
+    phases = 2.0 * np.pi * (azimuth / (2.0 * np.pi)) * 4.0
+    return beat_swimmer(seeding.fibonacci_sphere(4096), fils, radius=radius, nseg=nseg, seed=seed, phases=phases)
+
+
 WORKLOADS = {
     "config1": ("1 swimmer, R=10a, 642 icosphere blobs, 16 x 20 segments (962 particles)", config1),
     "config3": ("1 swimmer, R=40a, 4096 Fibonacci blobs, 640 x 20 segments (16,896 particles)", config3),
+    "config5": ("1 swimmer, R=100a, 10,242 icosphere blobs, 8000 x 20 segments (170,242 particles)", config5),
+    "config1_beat": ("config1 geometry, preferred-curvature beat (random phases), KB=KT=1, dt=1/300", config1_beat),
+    "config3_beat": ("config3 geometry, preferred-curvature beat (metachronal lag 4 x azimuth), KB=KT=1, dt=1/300",
+                     config3_beat),
 }
 
 # Workloads of independent swimmers (a list of Simulation keyword sets), run

@@ -77,6 +77,20 @@ GMI_API int gmi_context_precision(const gmi_context *ctx);
 GMI_API gmi_status gmi_context_synchronize(gmi_context *ctx);
 /* Number of library kernels launched on this context so far. */
 GMI_API long long gmi_context_launch_count(const gmi_context *ctx);
+/* Deadline of the pair kernels' bounded waits on their source tiles, in
+ * nanoseconds of the GPU's global timer: a wait that runs past it makes the
+ * kernel record a timeout and return, and the next synchronising call
+ * reports GMI_ERR_DEVICE_TIMEOUT.  0 restores the default (2 s); otherwise
+ * 1 us .. 60 s.  A launch captured in a CUDA graph keeps the deadline it was
+ * captured with.  The reference's kernels have no waits to bound. */
+GMI_API gmi_status gmi_context_set_wait_deadline(gmi_context *ctx, long long nanoseconds);
+/* Check of the bounded-wait machinery: one CTA waits, through the pair
+ * kernels' bounded wait and the context's deadline, on an mbarrier that
+ * expects two arrivals.  withhold_arrival 0: both arrive, GMI_OK.
+ * withhold_arrival 1: one never arrives, the wait gives up at the deadline
+ * and the call returns GMI_ERR_DEVICE_TIMEOUT; the context stays usable.
+ * Synchronises the context stream.  No counterpart in the reference. */
+GMI_API gmi_status gmi_context_check_bounded_wait(gmi_context *ctx, int withhold_arrival);
 
 /* ------------------------------------------------------------------------
  * Pair sums on device arrays, in the reference's layouts (FP64, AoS):
@@ -123,8 +137,9 @@ GMI_API gmi_status gmi_Mbs_mult(gmi_context *ctx, double *V_d, const double *F_s
  * GPU that loads the library holds until process exit.  Limit:
  * total_segs <= 32768 (larger problems return GMI_ERR_ARG).  precision is a
  * gmi_precision; cuda_stream a cudaStream_t (NULL = legacy default stream).
- * The first call on a device (that device current) looks up the array's
- * device address; make it before any stream capture.  All calls share the
+ * The first call in each CUDA context (the device's primary context, or a
+ * context the caller made current) looks up the array's device address in
+ * that context; make it before any stream capture.  All calls share the
  * array, so calls that overlap on the GPU race.  Returns when V is complete.
  * No counterpart in the reference. */
 GMI_API gmi_status gmi_Mss_mult_noalloc(double *V_d, const double *F_d, const double *X_d, int start_seg,
@@ -272,6 +287,18 @@ GMI_API gmi_status gmi_solver_compute_velocities_prescribed(gmi_solver *s, const
                                                             const double *body_q_h, const double *vel_dir_h,
                                                             const double *phase_speed_h, int *gmres_iters);
 
+/* The last linear solve (GMRES, or in FP32C the mixed-precision refinement):
+ * its GMRES iterations and its relative residual |b - A x| / |b| (GMRES's
+ * estimate in FP64; the FP64-grade refinement residual in FP32C).  Either
+ * pointer may be NULL.  No counterpart in the reference. */
+GMI_API gmi_status gmi_solver_last_linear_solve(const gmi_solver *s, int *iterations, double *relative_residual);
+/* strict != 0: gmi_solver_compute_velocities returns GMI_ERR_NOT_CONVERGED
+ * when the linear solve stopped at max_linear_iter (or, in FP32C, at the
+ * refinement cap) with its residual above linear_tol; the results are still
+ * written back.  0 (the default) keeps the reference's behaviour, which
+ * accepts the capped solve silently (mobility_solver.cpp:1234). */
+GMI_API gmi_status gmi_solver_set_strict_convergence(gmi_solver *s, int strict);
+
 /* v_bodies after the last solve: 6*nswim values (U, Omega per swimmer). */
 GMI_API gmi_status gmi_solver_get_v_bodies(gmi_solver *s, double *v_bodies_h);
 GMI_API gmi_status gmi_solver_set_v_bodies(gmi_solver *s, const double *v_bodies_h);
@@ -338,6 +365,17 @@ GMI_API gmi_status gmi_sim_prepare(gmi_sim *sim, double *body_mobility_out);
 /* Time step nt (0-based): Broyden until the residual meets tol.  Returns
  * GMI_ERR_NOT_CONVERGED / GMI_ERR_NONFINITE where the reference stops. */
 GMI_API gmi_status gmi_sim_step(gmi_sim *sim, int nt, int *broyden_iters, int *gmres_iters_total);
+/* Drive the filaments by a prescribed preferred-curvature beat through the
+ * reference's strain_twist hook (filament::body_frame_moment,
+ * filament.cpp:1104-1106, which the reference leaves at zero,
+ * swimmer.cpp:92, 210): time step nt solves with
+ *     strain_twist_f = (0, amplitude sin(2 pi (nt + 1) dt / period + phase_f), 0)
+ * (phases_h: one per filament).  end_force_scale multiplies the end force
+ * (0: the beat alone drives the filaments); the barrier keeps its scale
+ * (repulsive_force_factor * end_force_magnitude).  An extension: the
+ * reference has no time-dependent preferred curvature. */
+GMI_API gmi_status gmi_sim_set_beat(gmi_sim *sim, double amplitude, double period, const double *phases_h,
+                                    double end_force_scale);
 GMI_API gmi_status gmi_sim_get_state(gmi_sim *sim, int field, double *out_h);
 
 /* Checkpoints in the reference's .backup layout (replaces the state part of
@@ -352,6 +390,103 @@ GMI_API gmi_status gmi_sim_get_state(gmi_sim *sim, int field, double *out_h);
 GMI_API gmi_status gmi_sim_backup_count(const gmi_sim *sim, long long *count);
 GMI_API gmi_status gmi_sim_export_backup(gmi_sim *sim, double *out_h);
 GMI_API gmi_status gmi_sim_import_backup(gmi_sim *sim, const double *in_h);
+
+/* ------------------------------------------------------------------------
+ * Learned initial inverse Jacobian (no counterpart in the reference, which
+ * starts every time step's Broyden solve from JACOBIAN_CONFIDENCE_FACTOR
+ * times the approximate inverse of swimmer::jacobian_inv_mult,
+ * broyden_solver.cpp:26-68, swimmer.cpp:690-845).
+ *
+ * A 3-layer MLP (n_in -> n_hidden -> n_hidden -> n_out, ReLU, bf16 weights
+ * and activations, FP32 accumulation on the tensor cores) maps a filament's
+ * shape in its local frame (phi: per segment, the position relative to the
+ * base over the filament length and the tangent, 6 nseg values) to a
+ * per-filament initial inverse Jacobian
+ *     H0 d = sigma (.) (conf Jinv d) + U (V^T d)
+ * (sigma: one scale per 3-vector, U, V: 6 nseg x rank), fitted to the secant
+ * pairs (change of the Broyden error, update) of plain Broyden runs.
+ * ---------------------------------------------------------------------- */
+typedef struct gmi_mlp gmi_mlp;
+
+/* Widths are positive multiples of 8; weights Kaiming-uniform from seed, the
+ * last layer scaled down so that the untrained network is close to the plain
+ * method (sigma = 1, U V^T = 0). */
+GMI_API gmi_status gmi_mlp_create(int device, int n_in, int n_hidden, int n_out, unsigned long long seed,
+                                  gmi_mlp **out);
+GMI_API gmi_status gmi_mlp_destroy(gmi_mlp *m);
+/* FP32 master parameters, flat: W1 [n_hidden x n_in] b1 W2 b2 W3 [n_out x
+ * n_hidden] b3, each segment starting at offsets6[l] (row-major W). */
+GMI_API gmi_status gmi_mlp_param_count(const gmi_mlp *m, long long *count);
+GMI_API gmi_status gmi_mlp_param_offsets(const gmi_mlp *m, long long *offsets6);
+GMI_API gmi_status gmi_mlp_get_params(gmi_mlp *m, float *params_h, long long count);
+GMI_API gmi_status gmi_mlp_set_params(gmi_mlp *m, const float *params_h, long long count);
+/* O [batch x n_out] (FP32, device) of X [batch x n_in] (FP32, device;
+ * rounded to bf16 on input).  Synchronous. */
+GMI_API gmi_status gmi_mlp_forward(gmi_mlp *m, const float *X_d, int batch, float *O_d);
+/* Gradients of the last gmi_mlp_forward's batch for upstream dO [batch x
+ * n_out] (FP32, device), in the flat parameter layout (grad_h may be NULL).
+ * Synchronous. */
+GMI_API gmi_status gmi_mlp_backward(gmi_mlp *m, const float *dO_d, int batch, float *grad_h);
+/* Mean secant-pair loss of records [nrec x (n_in + 18 nseg)] (FP32, device;
+ * layout phi | d | b | t, see gmi_sim_set_secant_buffer) for a head of the
+ * given rank (2, 4 or 8; n_in = 6 nseg, n_out >= 2 nseg + 12 nseg rank).
+ * O_scratch_d holds min(nrec, 4096) x n_out floats; dO_d (nrec x n_out, or
+ * NULL) receives the gradient of the mean over each chunk of 4096. */
+GMI_API gmi_status gmi_mlp_secant_loss(gmi_mlp *m, const float *records_d, long long nrec, int nseg, int rank,
+                                       float *O_scratch_d, double *mean_loss, float *dO_d);
+/* Adam on the secant-pair loss: steps minibatches of batch records drawn
+ * with replacement (a counter-based hash of seed and the step).  loss_h
+ * (steps floats, or NULL) receives each step's minibatch loss. */
+GMI_API gmi_status gmi_mlp_train_secant(gmi_mlp *m, const float *records_d, long long nrec, int nseg, int rank,
+                                        int steps, int batch, float lr, unsigned long long seed, float *loss_h);
+GMI_API long long gmi_mlp_launch_count(const gmi_mlp *m);
+
+/* When a time step uses the learned H0 and when it falls back to the plain
+ * one.  Plain host logic (no GPU), the same the time step runs.
+ * Modes: 0 calibrating (the first calibration_steps steps are plain, their
+ * mean Broyden count is the yardstick), 1 learned, 2 fell back (plain from
+ * then on).  A learned step gets at most
+ *     cap = ceil(cap_factor * plain mean) + 2
+ * Broyden iterations; one that does not converge within it (or diverges) is
+ * a regression: the step is restarted from its initial guess with the plain
+ * H0.  max_regressions regressions, or a mean learned count above
+ * (1 + margin) * plain mean over the last window learned steps, end the
+ * learned mode. */
+typedef struct gmi_learned_policy {
+    int calibration_steps;  /* default 3 */
+    int window;             /* default 8 */
+    int max_regressions;    /* default 2 */
+    double margin;          /* default 0.05 */
+    double cap_factor;      /* default 2 */
+    /* state, written by gmi_learned_policy_record */
+    int mode;
+    int steps_plain, steps_learned, regressions;
+    double plain_iters_sum;
+    int recent[64];         /* Broyden counts of the last learned steps (ring) */
+    int recent_count;
+} gmi_learned_policy;
+
+GMI_API void gmi_learned_policy_init(gmi_learned_policy *p);
+GMI_API int gmi_learned_policy_use_learned(const gmi_learned_policy *p);
+GMI_API int gmi_learned_policy_iteration_cap(const gmi_learned_policy *p, int max_broyden_iter);
+GMI_API void gmi_learned_policy_record(gmi_learned_policy *p, int used_learned, int converged, int broyden_iters);
+
+/* Collect secant pairs: every Broyden iteration of a plain step appends one
+ * record per filament, [phi (6 nseg) | d | b | t (6 nseg each)] in FP32, to
+ * records_d (device, capacity records; NULL stops collecting), while room
+ * is left.  d: the change of the filament's Broyden error over the
+ * iteration; b: conf Jinv d (the plain initial inverse Jacobian applied to
+ * it); t: the filament's update of that iteration; all in the filament's
+ * local frame (e3 along the filament's base direction). */
+GMI_API gmi_status gmi_sim_set_secant_buffer(gmi_sim *sim, float *records_d, long long capacity);
+GMI_API gmi_status gmi_sim_secant_count(const gmi_sim *sim, long long *count);
+/* Use the network's H0 (mlp NULL: the plain method) under policy (NULL:
+ * defaults).  The network is read, not modified; several simulations may
+ * share one.  rank is the head's rank (2, 4 or 8); n_in must be 6 nseg. */
+GMI_API gmi_status gmi_sim_set_learned_jacobian(gmi_sim *sim, const gmi_mlp *mlp, int rank,
+                                                const gmi_learned_policy *policy);
+/* The policy's state after the steps so far. */
+GMI_API gmi_status gmi_sim_learned_policy(const gmi_sim *sim, gmi_learned_policy *out);
 
 /* Measured FMA-pipe throughput (FLOP/s, FMA = 2) of this GPU for
  * precision GMI_FP32C (FP32 pipe) or GMI_FP64 (FP64 pipe): the roofline

@@ -27,8 +27,20 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 ROOT = os.path.dirname(ORACLE)
-REF = os.environ.get("GMI_REFERENCE_DIR", "/root/reference")
-SCIPY_LIBS = "/usr/local/lib/python3.12/dist-packages/scipy.libs"
+sys.path.insert(0, ROOT)
+from oracle import reference_dir  # noqa: E402
+
+REF = reference_dir()
+
+
+def _scipy_libs() -> str:
+    """The directory of the OpenBLAS that scipy's wheel bundles (the LAPACK
+    behind lapack_shim.c): ``scipy.libs`` beside the installed package."""
+    import scipy
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(scipy.__file__))), "scipy.libs")
+
+
+SCIPY_LIBS = _scipy_libs()
 
 REF_CPP = ["cilia_sim_main.cpp", "matrix.cpp", "quaternion.cpp", "segment.cpp", "filament.cpp", "broyden_solver.cpp",
            "rigid_body.cpp", "swimmer.cpp", "mobility_solver.cpp"]

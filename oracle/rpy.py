@@ -28,7 +28,8 @@ def build(with_reference: bool | None = None) -> None:
     """Compile the restatement (always) and, when the reference tree is
     present, the reference's own kernels for the CPU."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref_root = os.environ.get("GMI_REFERENCE_DIR", "/root/reference")
+    from oracle import reference_dir
+    ref_root = reference_dir()
     if with_reference is None:
         with_reference = os.path.isfile(os.path.join(ref_root, "cuda_functions.cu"))
     if with_reference:

@@ -26,10 +26,28 @@ def load_golden(name, prefix="pairs_"):
 
 
 def rel_err(got, want):
+    """max |got - want| / max |want|: the error normalised by the largest
+    value of the whole output."""
     got = np.asarray(got)
     want = np.asarray(want)
     scale = np.max(np.abs(want))
     return float(np.max(np.abs(got - want)) / (scale if scale > 0 else 1.0))
+
+
+def per_target_rel(got, want):
+    """Per-target relative error of velocity outputs: for every target and
+    every 3-vector block of its row (v, and omega for 6-column rows),
+    |got - want| / |want|.  Returns (max, rms) over all blocks.  Unlike
+    rel_err, a target with a small velocity is held to its own magnitude."""
+    got = np.asarray(got, dtype=np.float64)
+    want = np.asarray(want, dtype=np.float64)
+    assert got.shape == want.shape and got.shape[-1] % 3 == 0
+    g = got.reshape(-1, 3)
+    w = want.reshape(-1, 3)
+    den = np.linalg.norm(w, axis=1)
+    assert np.all(den > 0), "per-target error needs non-zero reference rows"
+    r = np.linalg.norm(g - w, axis=1) / den
+    return float(r.max()), float(np.sqrt(np.mean(r * r)))
 
 
 @pytest.fixture(scope="session")

@@ -3,7 +3,8 @@
 Runs cuda_functions.cu (Mss_mult free and wall, Mbb_mult, Msb_mult,
 Mbs_mult, barrier_forces), compiled for the CPU by `make -C oracle ref`, on
 small seeded inputs and stores inputs and outputs in pairs_<case>.npz.
-Needs the reference tree (default /root/reference, or GMI_REFERENCE_DIR);
+Needs the reference tree (GMI_REFERENCE_DIR, or a ``reference`` directory
+beside the repository);
 the fixtures it writes are committed, so the tests never need the tree.
 
     python tests/golden/make_golden.py

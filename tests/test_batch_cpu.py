@@ -166,4 +166,22 @@ def test_batch_run_stops_a_failing_swimmer_only():
         batch.run(3)
     assert batch.sims[0].nt_seen == [0, 1]
     assert batch.sims[1].nt_seen == [0, 1, 2] and batch.sims[2].nt_seen == [0, 1, 2]
+    # each swimmer's count is the steps it really took: the failed one is
+    # still at step 1, and the batch no longer claims one step number
+    assert batch.next_nt == [1, 3, 3]
+    with pytest.raises(ValueError, match="different time steps"):
+        batch.nt
+    # stepping on continues each swimmer from its own step
+    batch.sims[0].fail_at = None
+    batch.step()
+    assert batch.sims[0].nt_seen == [0, 1, 1] and batch.sims[1].nt_seen == [0, 1, 2, 3]
+    assert batch.next_nt == [2, 4, 4]
+    batch.close()
+
+
+def test_batch_step_failure_keeps_per_swimmer_counts():
+    batch = SwimmerBatch([dict(name=i, fail_at=(0 if i == 1 else None)) for i in range(3)], sim_factory=FakeSim)
+    with pytest.raises(RuntimeError, match="swimmer 1 failed at step 0"):
+        batch.step()
+    assert batch.next_nt == [1, 0, 1]
     batch.close()

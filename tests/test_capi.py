@@ -64,7 +64,8 @@ def test_reference_side_adapter_compiles(gmi_lib):
     """The reference-side binding (adapter/gb300_mobility_solver.cpp) compiles
     against the reference's own headers (config.hpp, mobility_solver.hpp,
     swimmer.hpp); skipped where the reference tree is absent."""
-    ref = os.environ.get("GMI_REFERENCE_DIR", "/root/reference")
+    from oracle import reference_dir
+    ref = reference_dir()
     if not os.path.isfile(os.path.join(ref, "mobility_solver.hpp")):
         pytest.skip("reference tree not present")
     from generic_mobility_interface_class_gb300 import _lib
