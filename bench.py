@@ -71,12 +71,18 @@ def parse():
     p.add_argument("--shape", default=None,
                    help="pin the apply's launch shape instead of autotuning: threads,targets,splits,sources_per_step "
                         "(the traffic capture pins the shape the autotuner picks)")
-    p.add_argument("--ts-workloads", default="config1,config3,config4",
+    p.add_argument("--ts-workloads", default="config1,config3,config4,config1_beat,config3_beat,config5",
                    help="time-step workloads (comma separated; empty to skip)")
-    p.add_argument("--ts-steps", default="config1:100,config3:10,config4:2", help="timed steps per workload")
+    p.add_argument("--ts-steps", default="config1:100,config3:10,config4:2,config1_beat:100,config3_beat:100,"
+                                         "config5:1", help="timed steps per workload")
     p.add_argument("--ts-warmup", type=int, default=5, help="untimed steps before the timed ones")
-    p.add_argument("--ts-warmups", default="config4:1",
+    p.add_argument("--ts-warmups", default="config4:1,config5:1",
                    help="untimed steps per workload where they differ from --ts-warmup")
+    p.add_argument("--learned", default="config3",
+                   help="workloads of the learned initial inverse Jacobian A/B (comma separated; empty to skip)")
+    p.add_argument("--learned-data-steps", type=int, default=15,
+                   help="plain time steps of the training geometry whose secant pairs train the network")
+    p.add_argument("--learned-train-steps", type=int, default=2000, help="Adam steps of the network")
     p.add_argument("--ts-swimmers", type=int, default=64, help="swimmers of a batch time-step workload (config4)")
     return p.parse_args()
 
@@ -206,8 +212,10 @@ def per_target_error(got, want):
 
 def run_reference(args, world, rank):
     """Reference arm: the reference algorithm on the host cores (the oracle
-    port of cuda_functions.cu's Mss_mult; the reference's own build cannot
-    run on this host), bounded target slice per step."""
+    port of cuda_functions.cu's Mss_mult; the reference's own host build
+    cannot run on this host), bounded target slice per step.  Beside it
+    (``cuda_on_gb300``), the reference's own CUDA kernel built for sm_103a,
+    timed on the GPU, where its build is present."""
     if rank != 0:
         return
     from oracle import rpy
@@ -224,6 +232,7 @@ def run_reference(args, world, rank):
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = nt * n * args.steps / total
+    cuda = reference_cuda_timing(x, f, nt)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
@@ -234,7 +243,124 @@ def run_reference(args, world, rank):
                          "sample": f"{nt} targets x {n} sources per step"},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if cuda is not None:
+        line["cuda_on_gb300"] = cuda
     print(json.dumps(line), flush=True)
+
+
+def reference_cuda_timing(x, f, nt, launches: int = 2):
+    """The reference's own Mss_mult (cuda_functions.cu:246-425) built for
+    sm_103a with this N compiled in (oracle/ref_gpu.py), launched as its
+    solver launches it (64 threads per block), timed with CUDA events on
+    device-resident inputs; its result on targets [0, nt) against the FP64
+    CPU oracle.  None without a GPU or without the build."""
+    try:
+        import torch
+        from oracle import ref_gpu, rpy
+        n = x.shape[0]
+        if not (torch.cuda.is_available() and ref_gpu.available(n)):
+            return None
+        k = ref_gpu.RefKernels(n)
+        X = torch.as_tensor(x, device="cuda")
+        F = torch.as_tensor(f, device="cuda")
+        V = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+        k.mss(V, F, X)  # warm-up
+        torch.cuda.synchronize()
+        stream = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(launches):
+            k.mss(V, F, X)
+        b.record(stream)
+        torch.cuda.synchronize()
+        sec = a.elapsed_time(b) / 1e3 / launches
+        got = V[:nt].cpu().numpy()
+        k.close()
+        want = rpy.mss(x, f, targets=(0, nt))
+        return {"value": float(n) * n / sec, "unit": "pairs/s", "ms_per_launch": 1e3 * sec, "launches": launches,
+                "dtype": "f64", "build": "reference cuda_functions.cu, nvcc -gencode arch=compute_103a,code=sm_103a "
+                                         "-O3, sizes compiled in, 64 threads per block",
+                "error_vs_cpu_oracle": per_target_error(got, want)}
+    except Exception as e:  # the CPU arm stands without it
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
+final_fp64 = {}  # the FP64 runs' final state per workload: the yardstick of the learned A/B
+
+
+def run_learned_ab(args, dev):
+    """The learned initial inverse Jacobian against the plain start, FP32C
+    pair sums with FP64 solves, on the time-step workloads: the network is
+    trained on the secant pairs of a plain run of the same workload built
+    from another seed (another geometry), then both starts run the
+    benchmark geometry from the same initial state (the policy's
+    calibration steps fall in the warm-up).  Reports Broyden and GMRES
+    counts, time-steps/sec, the policy's final state, and each run's
+    swimmer-velocity error against the FP64 run of the same steps."""
+    import torch
+    from generic_mobility_interface_class_gb300 import learned, workloads
+    from generic_mobility_interface_class_gb300.sim import Simulation
+    from generic_mobility_interface_class_gb300._lib import GMI_FP32C
+    warm_for = dict(kv.split(":") for kv in getattr(args, "ts_warmups", "").split(",") if kv)
+    steps_for = dict(kv.split(":") for kv in args.ts_steps.split(",") if kv)
+    out = {}
+    for name in [w for w in args.learned.split(",") if w]:
+        desc, make = workloads.WORKLOADS[name]
+        t0 = time.perf_counter()
+        records = learned.collect_secant_pairs(make(seed=2027), steps=args.learned_data_steps, capacity=50000,
+                                               device=dev)
+        collect_s = time.perf_counter() - t0
+        net = learned.LearnedJacobian(nseg=20, device=dev)
+        loss0 = net.loss(records)
+        t0 = time.perf_counter()
+        losses = net.train(records, steps=args.learned_train_steps, batch=512, lr=1e-3)
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t0
+        loss1 = net.loss(records)
+        kw = make()
+        warm = int(warm_for.get(name, args.ts_warmup))
+        nsteps = int(steps_for.get(name, 10))
+        runs = {}
+        for label in ("plain", "learned"):
+            sim = Simulation(**kw, precision=GMI_FP32C, device=dev)
+            sim.prepare()
+            if label == "learned":
+                sim.set_learned_jacobian(net, learned.default_policy())
+            for nt in range(warm):
+                sim.step(nt)
+            torch.cuda.synchronize()
+            broyden, gmres = [], []
+            t0 = time.perf_counter()
+            for nt in range(warm, warm + nsteps):
+                b, g = sim.step(nt)
+                broyden.append(b)
+                gmres.append(g)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+            pol = sim.learned_policy()
+            r = {"steps_per_s": nsteps / wall, "broyden_iters_per_step": sum(broyden) / nsteps,
+                 "gmres_iters_per_step": sum(gmres) / nsteps, "broyden_iters": broyden}
+            if label == "learned":
+                r["policy"] = {"mode": ["calibrating", "learned", "fell back"][pol.mode],
+                               "steps_learned": pol.steps_learned, "steps_plain": pol.steps_plain,
+                               "regressions": pol.regressions}
+            ref = final_fp64.get(name)
+            if ref is not None:
+                v = sim.state("body_v").ravel()
+                r["swimmer_velocity_error_vs_fp64"] = float(np.linalg.norm(v - ref["body_v"]) /
+                                                            np.linalg.norm(ref["body_v"]))
+            runs[label] = r
+            sim.close()
+        out[name] = {"workload": desc, "training_geometry": "same workload, seed 2027",
+                     "records": int(records.shape[0]), "collect_s": collect_s,
+                     "network": "3 layers, 120 -> 256 -> 256 -> 1000, bf16 weights, FP32 accumulate, rank 4",
+                     "train_steps": args.learned_train_steps, "train_s": train_s, "loss_before": loss0,
+                     "loss_after": loss1, "loss_last_minibatch": float(losses[-1]) if len(losses) else None,
+                     "warmup_steps": warm, "timed_steps": nsteps, **runs,
+                     "speedup_learned_vs_plain": runs["learned"]["steps_per_s"] / runs["plain"]["steps_per_s"],
+                     "mlp_launches": net.launches}
+        net.close()
+    return out
 
 
 def run_time_steps(args, dev):
@@ -259,18 +385,19 @@ def run_time_steps(args, dev):
         desc, make = workloads.WORKLOADS[name]
         kw = make()
         nsteps = int(steps_for.get(name, 10))
+        warm = int(warm_for.get(name, args.ts_warmup))
         runs, final = {}, {}
         for label, prec in (("fp64", GMI_FP64), ("fp32c", GMI_FP32C)):
             sim = Simulation(**kw, precision=prec, device=dev)
             sim.prepare()
-            for nt in range(args.ts_warmup):
+            for nt in range(warm):
                 sim.step(nt)
             torch.cuda.synchronize()
             l0 = sim.launches
             broyden, gmres = [], []
             with ClockSampler(dev) as clocks:
                 t0 = time.perf_counter()
-                for nt in range(args.ts_warmup, args.ts_warmup + nsteps):
+                for nt in range(warm, warm + nsteps):
                     b, g = sim.step(nt)
                     broyden.append(b)
                     gmres.append(g)
@@ -286,7 +413,9 @@ def run_time_steps(args, dev):
             a, b = final["fp64"][f], final["fp32c"][f]
             return float(np.linalg.norm(b - a) / max(np.linalg.norm(a), 1e-300))
 
-        out[name] = {"workload": desc, "timed_steps": nsteps, "warmup_steps": args.ts_warmup,
+        if name in ("config3", "config5"):
+            final_fp64[name] = final["fp64"]
+        out[name] = {"workload": desc, "timed_steps": nsteps, "warmup_steps": warm,
                      "broyden_tol": kw["tol"], "gmres_tol": kw["linear_tol"], **runs,
                      "speedup_fp32c_vs_fp64": runs["fp32c"]["steps_per_s"] / runs["fp64"]["steps_per_s"],
                      "error_fp32c_vs_fp64_after_run": {"swimmer_velocity_rel": rel("body_v"),
@@ -465,6 +594,12 @@ def run_gmi(args, world, rank, local):
                 "flops_per_pair": FLOP_PER_PAIR_SS}
     ctx.close()
     time_steps = run_time_steps(args, dev) if args.ts_workloads else {}
+    learned_ab = {}
+    if args.learned:
+        try:
+            learned_ab = run_learned_ab(args, dev)
+        except Exception as e:  # keep the rest of the line
+            learned_ab = {"error": f"{type(e).__name__}: {e}"}
 
     line = None
     if rank == 0:
@@ -503,6 +638,7 @@ def run_gmi(args, world, rank, local):
             "gpu_launches": gpu_launches,
             "wall_s_timed_region": wall,
             "time_steps": time_steps,
+            "learned_initial_inverse_jacobian": learned_ab,
         }
         line.update(extra)
         print(json.dumps(line), flush=True)

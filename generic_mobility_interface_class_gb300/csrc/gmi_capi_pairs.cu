@@ -298,14 +298,17 @@ gmi_status gmi_autotune(gmi_context *ctx, int kind, int num_targets, int num_sou
                 h[3 * i + 1] = 2.5 * b + 0.1 * std::sin(2.0 + i);
                 h[3 * i + 2] = 2.5 * c + 1.5 + 0.1 * std::sin(3.0 + i);
             }
-            GMI_CUDA_TRY(cudaMemcpy(dst, h, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice));
+            GMI_CUDA_TRY(cudaMemcpyAsync(dst, h, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+            GMI_CUDA_TRY(cudaStreamSynchronize(ctx->stream));  // h is refilled next
             return GMI_OK;
         };
         st = fill_pos(num_targets, static_cast<double *>(xt.ptr));
         if (st == GMI_OK) st = fill_pos(num_sources, static_cast<double *>(xsrc.ptr));
         if (st == GMI_OK) {
             for (size_t i = 0; i < (size_t)num_sources * nf; ++i) h[i] = std::cos(0.7 * (double)i);
-            cudaError_t e = cudaMemcpy(fsrc.ptr, h, (size_t)num_sources * nf * sizeof(double), cudaMemcpyHostToDevice);
+            cudaError_t e = cudaMemcpyAsync(fsrc.ptr, h, (size_t)num_sources * nf * sizeof(double),
+                                            cudaMemcpyHostToDevice, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // before h is freed
             if (e != cudaSuccess) st = GMI_ERR_CUDA;
         }
         gmi::host_free(h);

@@ -114,7 +114,9 @@ gmi_status context_init(gmi_context *ctx, int device)
     GMI_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     ctx->own_stream = true;
     GMI_CUDA_TRY(dev_malloc(&ctx->d_err, sizeof(unsigned)));
-    GMI_CUDA_TRY(cudaMemset(ctx->d_err, 0, sizeof(unsigned)));
+    // stream-ordered and complete before the caller can launch anything
+    GMI_CUDA_TRY(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
+    GMI_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     GMI_CUDA_TRY(host_alloc(&ctx->h_err, sizeof(unsigned)));
     *ctx->h_err = 0;
     cudaDriverEntryPointQueryResult q;

@@ -1329,7 +1329,7 @@ static gmi_status sim_alloc(gmi_sim *m, double **p, size_t count)
     if (count == 0) count = 1;
     GMI_CUDA_TRY(dev_malloc(p, count * sizeof(double)));
     m->allocs.push_back(*p);
-    GMI_CUDA_TRY(cudaMemset(*p, 0, count * sizeof(double)));
+    GMI_CUDA_TRY(cudaMemsetAsync(*p, 0, count * sizeof(double), m->solver->ctx->stream));
     return GMI_OK;
 }
 
@@ -1338,7 +1338,7 @@ static gmi_status sim_alloc_bytes(gmi_sim *m, void **p, size_t bytes)
     if (bytes < 16) bytes = 16;
     GMI_CUDA_TRY(dev_malloc(p, bytes));
     m->allocs.push_back(*p);
-    GMI_CUDA_TRY(cudaMemset(*p, 0, bytes));
+    GMI_CUDA_TRY(cudaMemsetAsync(*p, 0, bytes, m->solver->ctx->stream));
     return GMI_OK;
 }
 
@@ -1791,7 +1791,7 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
         }
     }
     auto up = [&](double *d, const std::vector<double> &h) -> gmi_status {
-        GMI_CUDA_TRY(cudaMemcpy(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        GMI_CUDA_TRY(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, sst(m)));
         return GMI_OK;
     };
     if ((st = up(P.x, hx)) != GMI_OK || (st = up(P.xm1, hx)) != GMI_OK || (st = up(P.xm2, hx)) != GMI_OK ||
@@ -1808,6 +1808,11 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
             gmi_sim_destroy(m);
             return st;
         }
+    }
+    if (cudaStreamSynchronize(sst(m)) != cudaSuccess) {
+        set_last_error_msg("gmi_sim_create: the initial state did not reach the device");
+        gmi_sim_destroy(m);
+        return GMI_ERR_CUDA;
     }
     *out = m;
     return GMI_OK;
@@ -1828,7 +1833,8 @@ gmi_status gmi_sim_prepare(gmi_sim *m, double *body_mobility_out)
         return GMI_OK;
     }
     GMI_TRY(solver_make_body_reference_matrices_device(m->solver, nullptr, mob));
-    GMI_CUDA_TRY(cudaMemcpy(m->P.mob_ref, mob, sizeof mob, cudaMemcpyHostToDevice));
+    GMI_CUDA_TRY(cudaMemcpyAsync(m->P.mob_ref, mob, sizeof mob, cudaMemcpyHostToDevice, sst(m)));
+    GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
     if (body_mobility_out) std::memcpy(body_mobility_out, mob, sizeof mob);
     m->prepared = true;
     return GMI_OK;
@@ -1957,7 +1963,9 @@ gmi_status gmi_sim_set_beat(gmi_sim *m, double amplitude, double period, const d
                   "gmi_sim_set_beat: bad argument");
     GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
     if (!m->beat_phase) GMI_TRY(sim_alloc(m, &m->beat_phase, m->P.F));
-    GMI_CUDA_TRY(cudaMemcpy(m->beat_phase, phases_h, (size_t)m->P.F * sizeof(double), cudaMemcpyHostToDevice));
+    GMI_CUDA_TRY(cudaMemcpyAsync(m->beat_phase, phases_h, (size_t)m->P.F * sizeof(double), cudaMemcpyHostToDevice,
+                                 sst(m)));
+    GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
     m->beat_amplitude = amplitude;
     m->beat_period = period;
     m->beat = true;
@@ -2103,11 +2111,13 @@ gmi_status gmi_sim_export_backup(gmi_sim *m, double *out_h)
     GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
     GMI_CUDA_TRY(cudaStreamSynchronize(sst(m)));
     BackupHost h;
-    GMI_TRY(for_each_field(m->P, h, [](double *d, std::vector<double> &v, size_t n) -> gmi_status {
+    cudaStream_t st = sst(m);
+    GMI_TRY(for_each_field(m->P, h, [st](double *d, std::vector<double> &v, size_t n) -> gmi_status {
         v.resize(n);
-        GMI_CUDA_TRY(cudaMemcpy(v.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost));
+        GMI_CUDA_TRY(cudaMemcpyAsync(v.data(), d, n * sizeof(double), cudaMemcpyDeviceToHost, st));
         return GMI_OK;
     }));
+    GMI_CUDA_TRY(cudaStreamSynchronize(st));
     size_t p = 0;
     walk_backup(m->P, h, [&](double &v) { out_h[p++] = v; });
     return GMI_OK;
@@ -2125,17 +2135,20 @@ gmi_status gmi_sim_import_backup(gmi_sim *m, const double *in_h)
     }));
     size_t p = 0;
     walk_backup(m->P, h, [&](double &v) { v = in_h[p++]; });
-    GMI_TRY(for_each_field(m->P, h, [](double *d, std::vector<double> &v, size_t n) -> gmi_status {
-        GMI_CUDA_TRY(cudaMemcpy(d, v.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    cudaStream_t st = sst(m);
+    GMI_TRY(for_each_field(m->P, h, [st](double *d, std::vector<double> &v, size_t n) -> gmi_status {
+        GMI_CUDA_TRY(cudaMemcpyAsync(d, v.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
         return GMI_OK;
     }));
     // q^{n-1} = q for segments and bodies (filament.cpp initial_setup and
     // rigid_body.cpp:71-100 read the backup this way); a fresh linear solver
     // starts from zero blob forces and body velocities
-    GMI_CUDA_TRY(cudaMemcpy(m->P.qm1, m->P.q, 4 * (size_t)m->P.S * sizeof(double), cudaMemcpyDeviceToDevice));
-    GMI_CUDA_TRY(cudaMemcpy(m->P.bqm1, m->P.bq, 4 * (size_t)m->P.W * sizeof(double), cudaMemcpyDeviceToDevice));
-    GMI_CUDA_TRY(cudaMemset(m->solver->f_blobs, 0, 3 * (size_t)m->solver->B * sizeof(double)));
-    GMI_CUDA_TRY(cudaMemset(m->solver->v_bodies, 0, 6 * (size_t)m->P.W * sizeof(double)));
+    GMI_CUDA_TRY(cudaMemcpyAsync(m->P.qm1, m->P.q, 4 * (size_t)m->P.S * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    GMI_CUDA_TRY(cudaMemcpyAsync(m->P.bqm1, m->P.bq, 4 * (size_t)m->P.W * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 st));
+    GMI_CUDA_TRY(cudaMemsetAsync(m->solver->f_blobs, 0, 3 * (size_t)m->solver->B * sizeof(double), st));
+    GMI_CUDA_TRY(cudaMemsetAsync(m->solver->v_bodies, 0, 6 * (size_t)m->P.W * sizeof(double), st));
+    GMI_CUDA_TRY(cudaStreamSynchronize(st));
     m->prepared = false;  // the body reference matrices follow the restored state
     return GMI_OK;
 }

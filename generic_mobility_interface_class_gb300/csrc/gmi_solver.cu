@@ -2121,11 +2121,13 @@ gmi_status gmi_solver_set_blob_references(gmi_solver *s, const double *refs)
     const int nblob = s->cfg.nblob;
     GMI_ARG_CHECK(nblob == 0 || refs != nullptr, "gmi_solver_set_blob_references: null references");
     if (nblob > 0) {
-        GMI_CUDA_TRY(cudaMemcpy(s->refs, refs, 3 * (size_t)nblob * sizeof(double), cudaMemcpyHostToDevice));
+        GMI_CUDA_TRY(cudaMemcpyAsync(s->refs, refs, 3 * (size_t)nblob * sizeof(double), cudaMemcpyHostToDevice,
+                                     s->ctx->stream));
     }
     double KTK[36];
     gmi::ktk_from_refs(refs, nblob, KTK);
-    GMI_CUDA_TRY(cudaMemcpy(s->ktkf_ref, KTK, sizeof KTK, cudaMemcpyHostToDevice));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->ktkf_ref, KTK, sizeof KTK, cudaMemcpyHostToDevice, s->ctx->stream));
+    GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));  // KTK is a local
     s->refs_set = true;
     return GMI_OK;
 }
@@ -2134,8 +2136,12 @@ gmi_status gmi_solver_set_body_reference_matrices(gmi_solver *s, const double *k
 {
     SOLVER_ENTRY(s);
     GMI_ARG_CHECK(ktkinv && mob, "gmi_solver_set_body_reference_matrices: null argument");
-    GMI_CUDA_TRY(cudaMemcpy(s->ktk_ref, ktkinv, 36 * sizeof(double), cudaMemcpyHostToDevice));
-    GMI_CUDA_TRY(cudaMemcpy(s->mob_ref, mob, 36 * sizeof(double), cudaMemcpyHostToDevice));
+    // ordered on the solver stream: the kernels that rotate these matrices
+    // (prepare_bodies) run on it; the legacy default stream would not be
+    // ordered with a non-blocking solver stream
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->ktk_ref, ktkinv, 36 * sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->mob_ref, mob, 36 * sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream));
+    GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));  // the caller's arrays may go away
     return GMI_OK;
 }
 
@@ -2231,7 +2237,9 @@ gmi_status solver_make_body_reference_matrices_device(gmi_solver *s, double *ktk
     // (K^T K) from the references (mobility_solver.cpp:1697-1713), inverted on the host
     std::vector<double> refs(3 * (size_t)nblob);
     if (nblob > 0)
-        GMI_CUDA_TRY(cudaMemcpy(refs.data(), s->refs, refs.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        GMI_CUDA_TRY(cudaMemcpyAsync(refs.data(), s->refs, refs.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                     s->ctx->stream));
+    GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
     double KTK[36];
     ktk_from_refs(refs.data(), nblob, KTK);
     double KTKinv[36];
@@ -2244,12 +2252,15 @@ gmi_status solver_make_body_reference_matrices_device(gmi_solver *s, double *ktk
     GMI_TRY(gmi_solver_set_body_reference_matrices(s, KTKinv, mob));
     // all swimmers but the last moved far away (mobility_solver.cpp:1721-1731), restored after
     std::vector<double> bx0(3 * (size_t)W), bx;
-    GMI_CUDA_TRY(cudaMemcpy(bx0.data(), s->body_x, bx0.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    GMI_CUDA_TRY(cudaMemcpyAsync(bx0.data(), s->body_x, bx0.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                 s->ctx->stream));
+    GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
     bx = bx0;
     const double shift = 1e10 * 2.2 * s->cfg.rseg * s->cfg.nseg;
     for (int n = 0; n < W - 1; ++n)
         for (int c = 0; c < 3; ++c) bx[3 * n + c] += shift;
-    GMI_CUDA_TRY(cudaMemcpy(s->body_x, bx.data(), bx.size() * sizeof(double), cudaMemcpyHostToDevice));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->body_x, bx.data(), bx.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                 s->ctx->stream));
     GMI_TRY(positions_and_barrier(s));
     for (int col = 0; col < 6; ++col) {
         GMI_CUDA_TRY(cudaMemsetAsync(s->rhs, 0, (size_t)s->n * sizeof(double), s->ctx->stream));
@@ -2267,7 +2278,9 @@ gmi_status solver_make_body_reference_matrices_device(gmi_solver *s, double *ktk
         GMI_TRY(gmi_solver_set_body_reference_matrices(s, KTKinv, mob));
         GMI_TRY(prepare_bodies(s));
     }
-    GMI_CUDA_TRY(cudaMemcpy(s->body_x, bx0.data(), bx0.size() * sizeof(double), cudaMemcpyHostToDevice));
+    GMI_CUDA_TRY(cudaMemcpyAsync(s->body_x, bx0.data(), bx0.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                 s->ctx->stream));
+    GMI_CUDA_TRY(cudaStreamSynchronize(s->ctx->stream));
     if (ktkinv_out) std::memcpy(ktkinv_out, KTKinv, sizeof KTKinv);
     if (mob_out) std::memcpy(mob_out, mob, sizeof mob);
     return context_check_device_errors(s->ctx);

@@ -33,7 +33,7 @@ def build(with_reference: bool | None = None) -> None:
     if with_reference is None:
         with_reference = os.path.isfile(os.path.join(ref_root, "cuda_functions.cu"))
     if with_reference:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+        subprocess.run(["make", "-s", "-j4", "-C", HERE, "ref", "ref-gpu", f"REF={ref_root}"], check=True)
 
 
 def _ptr(a: np.ndarray):

@@ -2,8 +2,9 @@
 one stream and one host thread per swimmer) on the GPU.
 
 * Stepping the swimmers concurrently changes no bit of any swimmer's state
-  against stepping them one after another: the kernels reduce in a fixed
-  order and the swimmers share no device memory.
+  against stepping them one after another, on small swimmers and on
+  full-size ones: the kernels reduce in a fixed order, the swimmers share no
+  device memory, and every copy is ordered on the swimmer's own stream.
 * Per swimmer, the FP32C pair sums with FP64 solves follow the plain FP64
   method.  Both stop Broyden at a residual of 1e-4, so their states may
   differ at that level: these small swimmers (205-314 blobs, 6-10
@@ -49,6 +50,27 @@ def test_concurrent_batch_is_bitwise_the_sequential_one(gmi_lib):
     for f in seq:
         for i, (a, b) in enumerate(zip(seq[f], par[f])):
             assert np.array_equal(a, b), f"swimmer {i}: {f} differs"
+
+
+def test_full_size_concurrent_batches_are_bitwise_the_sequential_one(gmi_lib):
+    """Twelve swimmers of the uneven-batch workload at full size (642-4096
+    blobs, so some take the one-cluster GMRES solve and some the
+    multi-kernel one): two concurrent runs and one in turn agree bit for
+    bit, Broyden and GMRES counts included.  Every host-device copy of the
+    library is ordered on its context's own (non-blocking) stream; a copy on
+    the legacy default stream would not be ordered with the kernels and, on
+    a GPU busy with the other swimmers, could land after them."""
+    from generic_mobility_interface_class_gb300 import workloads
+    from generic_mobility_interface_class_gb300._lib import GMI_FP32C
+    sw = workloads.config4(nswim=12)
+    assert min(s["nblob"] for s in sw) <= 2048 < max(s["nblob"] for s in sw)
+    it_a, a = run(sw, GMI_FP32C, threads=None, steps=2)
+    it_b, b = run(sw, GMI_FP32C, threads=None, steps=2)
+    it_s, s = run(sw, GMI_FP32C, threads=1, steps=2)
+    assert it_a == it_s and it_b == it_s
+    for f in s:
+        for i in range(len(sw)):
+            assert np.array_equal(a[f][i], s[f][i]) and np.array_equal(b[f][i], s[f][i]), f"swimmer {i}: {f}"
 
 
 def test_fp32c_batch_against_fp64_per_swimmer(gmi_lib):
