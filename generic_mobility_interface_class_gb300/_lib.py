@@ -113,6 +113,7 @@ SIGNATURES = {
     "gmi_learned_policy_use_learned": ([_P], _I),
     "gmi_learned_policy_iteration_cap": ([_P, _I], _I),
     "gmi_learned_policy_record": ([_P, _I, _I, _I], None),
+    "gmi_seed_sphere_repulsive": ([_I, _I, _I, _P, ctypes.POINTER(_I)], _I),
     "gmi_sim_set_beat": ([_P, _D, _D, _P, _D], _I),
     "gmi_sim_set_secant_buffer": ([_P, _P, ctypes.c_longlong], _I),
     "gmi_sim_secant_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),

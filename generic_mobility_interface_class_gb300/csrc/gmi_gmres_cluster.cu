@@ -66,6 +66,7 @@ struct ClusterGmresArgs {
     const double *w0;                 // r0, all n rows
     const double *R, *refs, *ktk_rot, *mob_rot, *ktkf_rot, *xb;
     double minv, beta0, tol, norm_ref, inv_norm_ref;
+    double eta2;                      // conditional re-orthogonalisation threshold (0: two passes always)
     GmresCtl *ctl;
     EqualK<float> kbb;
 };
@@ -468,6 +469,11 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
         }
         __syncthreads();
         // ---- D..F: CGS2 and ||w|| ------------------------------------------
+        // With eta2 > 0 the first pass also sums ||w||^2 (entry k), and the
+        // second pass is skipped when ||w - Q h||^2 = ||w||^2 - ||h||^2 keeps
+        // at least eta2 of ||w||^2 (Daniel, Gragg, Kaufman and Stewart): every
+        // CTA holds the same h, so every CTA takes the same branch.
+        const bool dgks = a.eta2 > 0.0;
         for (int pass = 0; pass < 2; ++pass) {
             double *hp = pass == 0 ? hp1 : hp2, *hs = pass == 0 ? h : h2;
             // items (column i, row group g), PG groups per column on adjacent
@@ -499,14 +505,14 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
                 for (int o = PG >> 1; o > 0; o >>= 1) sg += __shfl_xor_sync(0xffffffffu, sg, o);
                 if (i < k && g == 0) hp[i] = sg;
             }
-            if (pass == 1) {  // ||w||^2 of the CTA's rows rides along as entry k
+            if (pass == 1 || dgks) {  // ||w||^2 of the CTA's rows rides along as entry k
                 double v2 = 0.0;
                 for (int lr = tid; lr < nr; lr += kCgTpb) v2 += wl[lr] * wl[lr];
                 v2 = cg_block_sum(v2, red, nr);
-                if (tid == 0) hp2[k] = v2;
+                if (tid == 0) hp[k] = v2;
             }
             cl.sync();  // barriers 3 and 4
-            cluster_reduce(cl, hp, pass == 0 ? k : k + 1, hs, C, G);
+            cluster_reduce(cl, hp, (pass == 0 && !dgks) ? k : k + 1, hs, C, G);
             __syncthreads();
             for (int lr = tid; lr < nr; lr += kCgTpb) {
                 const int row = row_of(lr);
@@ -526,6 +532,26 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
                 wl[lr] -= (p0 + p1) + (p2 + p3);
             }
             __syncthreads();
+            if (pass == 0 && dgks) {
+                // ||h||^2 by one warp (fixed tree: the same bits in every CTA)
+                if (tid < 32) {
+                    double t = 0.0;
+                    for (int i = tid; i < k; i += 32) t += h[i] * h[i];
+                    t = warp_sum(t);
+                    if (tid == 0) {
+                        const double w2 = h[k], after = w2 - t;
+                        const int skip = (w2 > 0.0 && after >= a.eta2 * w2 && after < INFINITY) ? 1 : 0;
+                        flag[1] = skip;
+                        if (skip) h2[k] = after;  // the norm below: ||w||^2 - ||h2||^2 with h2 = 0
+                    }
+                }
+                __syncthreads();
+                if (flag[1]) {
+                    for (int i = tid; i < k; i += kCgTpb) h2[i] = 0.0;
+                    __syncthreads();
+                    break;
+                }
+            }
         }
         // ||w - Q h2||^2 = ||w||^2 - ||h2||^2 (Q orthonormal; h2 is the second
         // pass's small correction, so nothing cancels), from the same
@@ -665,6 +691,7 @@ gmi_status cluster_gmres_launch(gmi_solver *s, double beta0, double norm_ref, do
     a.tol = tol;
     a.norm_ref = norm_ref;
     a.inv_norm_ref = 1.0 / norm_ref;
+    a.eta2 = reorth_eta2();
     a.ctl = s->ctl;
     PairConsts k;
     fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);

@@ -724,6 +724,10 @@ __device__ __forceinline__ bool finish_projections(const double *P, int k, int n
     return true;
 }
 
+__device__ __forceinline__ void givens_step(double *__restrict__ H, int ldh, int iter, double nrm,
+                                            double *__restrict__ beta, double *__restrict__ cs,
+                                            double *__restrict__ sn, double *__restrict__ scal, GmresCtl *ctl);
+
 // S3: blob rows of w, first CGS pass.  With splits > 1 the blob-blob pair
 // sum left per-split partials (mpart[p * 3B + r]), which this kernel adds:
 // warp q takes the splits p = q mod 4 for the CTA's 32 rows (one per lane).
@@ -732,7 +736,7 @@ __global__ void __launch_bounds__(kSTpb) s3_finish_project_kernel(
     const double *__restrict__ z, const double *__restrict__ R, const double *__restrict__ refs,
     double *__restrict__ w, const double *__restrict__ Q, size_t ld, int n, double *__restrict__ P,
     double *__restrict__ G, int *tickets, double *__restrict__ scal, double *__restrict__ H, int ldh,
-    const GmresCtl *ctl)
+    double *__restrict__ beta, double *__restrict__ cs, double *__restrict__ sn, GmresCtl *ctl, double eta2)
 {
     pdl_wait_then_release();
     static_assert(kSTpb == 4 * kSRows && kSRows == 32, "S3's split sum: four warps over 32 rows");
@@ -778,10 +782,44 @@ __global__ void __launch_bounds__(kSTpb) s3_finish_project_kernel(
     }
     __syncthreads();
     cta_projections(Q, ld, row0, rows, k, ws, P, gridDim.x);
+    const bool dgks = eta2 > 0.0;
+    if (dgks && threadIdx.x < 32) {  // ||w||^2 of the CTA's rows rides along as column k
+        const double v = ws[threadIdx.x];
+        const double a = warp_sum(v * v);
+        if (threadIdx.x == 0) P[(size_t)k * gridDim.x + blockIdx.x] = a;
+    }
     double *h = scal + kHOff;
-    if (!finish_projections(P, k, gridDim.x, G, tickets, h)) return;
+    if (!finish_projections(P, dgks ? k + 1 : k, gridDim.x, G, tickets, h)) return;
     double *Hcol = H + (size_t)ldh * (k - 1);
     for (int i = threadIdx.x; i < k; i += kSTpb) Hcol[i] = h[i];
+    // Conditional re-orthogonalisation (Daniel, Gragg, Kaufman and Stewart):
+    // after one classical pass ||w - Q h||^2 = ||w||^2 - ||h||^2; when that
+    // keeps at least eta^2 of ||w||^2 (eta = 1/sqrt 2: "twice is enough"),
+    // w - Q h is orthogonal to Q to working precision and the difference
+    // has not cancelled, so the second pass (S4) is skipped: its norm is
+    // taken here and the Givens step runs in this CTA.  S1 then applies the
+    // pending update w -= Q h with these first-pass coefficients.
+    __shared__ double nrm_s;
+    __shared__ int skip_s;
+    if (threadIdx.x < 32) {
+        int skip = 0;
+        double nrm = 0.0;
+        if (dgks) {
+            double t = 0.0;
+            for (int i = threadIdx.x; i < k; i += 32) t += h[i] * h[i];
+            t = warp_sum(t);
+            const double w2 = h[k], after = w2 - t;
+            skip = (w2 > 0.0 && after >= eta2 * w2 && after < INFINITY) ? 1 : 0;
+            nrm = skip ? sqrt(after) : 0.0;
+        }
+        if (threadIdx.x == 0) {
+            nrm_s = nrm;
+            skip_s = skip;
+            ctl->pass2 = skip ? 0 : 1;
+        }
+    }
+    __syncthreads();  // the H column is written; the decision is shared
+    if (skip_s) givens_step(H, ldh, k, nrm_s, beta, cs, sn, scal, ctl);
 }
 
 // w -= Q h on this CTA's rows (rows go to ws): warp q takes the columns
@@ -923,7 +961,7 @@ __global__ void __launch_bounds__(kSTpb) s4_project_norm_givens_kernel(
     double *__restrict__ beta, double *__restrict__ cs, double *__restrict__ sn, GmresCtl *ctl)
 {
     pdl_wait_then_release();
-    if (ctl->done) return;
+    if (ctl->done || ctl->pass2 == 0) return;  // converged, or S3 skipped the second pass
     __shared__ double ws[kSRows];
     __shared__ double nrm_s;
     const int k = ctl->k, row0 = blockIdx.x * kSRows, rows = min(kSRows, n - row0);
@@ -1165,6 +1203,17 @@ static cudaError_t launch_step(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3
     return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
 }
 
+// eta^2 of the conditional re-orthogonalisation in the device Arnoldi
+// steps: the second Gram-Schmidt pass runs only when one pass kept less
+// than eta^2 of ||w||^2.  eta = 1/sqrt(2) by default; GMI_REORTH_ETA sets
+// it, and 0 runs the second pass always.
+double reorth_eta2()
+{
+    const char *env = std::getenv("GMI_REORTH_ETA");
+    const double eta = env ? std::atof(env) : 0.70710678118654752440;
+    return eta > 0.0 ? eta * eta : 0.0;
+}
+
 // Sizes of the Arnoldi step's workspace inside s->partial and s->st_tickets.
 struct StepLayout {
     int gx, nblk, ngroups;
@@ -1241,7 +1290,7 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     GMI_CUDA_TRY(launch_step(pdl, s3_finish_project_kernel, dim3(L.nblk), dim3(kSTpb), 0, st, W, nblob,
                              (const double *)s->mbb, (const double *)s->gm_partial, splits, (const double *)s->z,
                              (const double *)s->R, (const double *)s->refs, s->w, (const double *)s->Q, ld, n, P,
-                             G, tk3, s->st_scal, s->H, ldh, (const GmresCtl *)s->ctl));
+                             G, tk3, s->st_scal, s->H, ldh, s->beta, s->cs, s->sn, s->ctl, reorth_eta2()));
     GMI_CUDA_TRY(launch_step(pdl, s4_project_norm_givens_kernel, dim3(L.nblk), dim3(kSTpb), 0, st,
                              (const double *)s->Q, ld, n, s->w, P, G, tk4, s->st_scal, s->H, ldh, s->beta, s->cs,
                              s->sn, s->ctl));

@@ -67,7 +67,7 @@ struct GmresCtl {
     int max_iter;
     int replays;   // Arnoldi steps completed by the norm kernel in this solve
     int guard;     // passes of the device-side loop (counted by its guard kernel)
-    int pad;
+    int pass2;     // set by S3: 1 = this step runs the second Gram-Schmidt pass (S4), 0 = skipped
     double tol;    // relative residual target
     double norm_ref;
     double resid;  // |beta(k)| / norm_ref after the last Givens step
@@ -86,6 +86,10 @@ gmi_status solver_compute_velocities_device(gmi_solver *s, int *iters);
 // Body state from the host (x[3W], q[4W]), rotation matrices and blob
 // positions on the device.
 gmi_status solver_place_blobs(gmi_solver *s, const double *body_x, const double *body_q);
+
+// eta^2 of the conditional re-orthogonalisation of the device Arnoldi steps
+// (GMI_REORTH_ETA; 0: the second Gram-Schmidt pass always runs).
+double reorth_eta2();
 
 // Frees the prescribed-cilia workspace (gmi_solver_destroy).
 void prescribed_release(gmi_solver *s);

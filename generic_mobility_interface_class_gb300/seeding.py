@@ -88,3 +88,17 @@ def radial_filaments(base_dirs: np.ndarray, base_radius: float, nseg: int, dl: f
     d = base_dirs / np.linalg.norm(base_dirs, axis=1, keepdims=True)
     s = base_radius + dl * np.arange(nseg, dtype=np.float64)
     return (d[:, None, :] * s[None, :, None]).reshape(-1, 3)
+
+
+def repulsive_sphere(n: int, device: int = 0, max_steps: int = 100000) -> np.ndarray:
+    """The reference's repulsive seeding of n points on the unit sphere
+    (seeding.cu:13-160), run on the GPU by gmi_seed_sphere_repulsive; the
+    (n, 3) unit vectors the reference caches as sphere<n>.seed."""
+    import ctypes
+
+    from . import _lib
+    out = np.zeros((n, 3))
+    steps = ctypes.c_int()
+    _lib.check(_lib.load().gmi_seed_sphere_repulsive(device, n, max_steps, out.ctypes.data_as(ctypes.c_void_p),
+                                                       ctypes.byref(steps)))
+    return out

@@ -488,6 +488,18 @@ GMI_API gmi_status gmi_sim_set_learned_jacobian(gmi_sim *sim, const gmi_mlp *mlp
 /* The policy's state after the steps so far. */
 GMI_API gmi_status gmi_sim_learned_policy(const gmi_sim *sim, gmi_learned_policy *out);
 
+/* Repulsive seeding of n points on the unit sphere, the reference's blob
+ * seeding and uniform filament seeding (repulsive_blob_seeding,
+ * seeding.cu:13-160, and seeding.cu:233-389 with UNIFORM_SEEDING; force
+ * kernel seeding_repulsion_step, cuda_functions.cu:1159-1250): a spiral
+ * start, then steps that move every point by the sum of 5 (2 - d) times
+ * the unit separation from every other point and put it back on the
+ * sphere, until no coordinate moves by more than 1e-4.  refs_out_h
+ * receives 3 n coordinates (the reference writes them to sphere<n>.seed);
+ * steps_out (may be NULL) the steps taken.  GMI_ERR_NOT_CONVERGED after
+ * max_steps steps, GMI_ERR_NONFINITE for coincident points. */
+GMI_API gmi_status gmi_seed_sphere_repulsive(int device, int n, int max_steps, double *refs_out_h, int *steps_out);
+
 /* Measured FMA-pipe throughput (FLOP/s, FMA = 2) of this GPU for
  * precision GMI_FP32C (FP32 pipe) or GMI_FP64 (FP64 pipe): the roofline
  * denominator of the pair kernels, which are bound by that pipe.  No

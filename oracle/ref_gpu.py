@@ -25,6 +25,7 @@ THREADS_PER_BLOCK = 64
 # C++ names of the reference's kernels (cuda_functions.hpp:9-10)
 MSS = b"_Z8Mss_multPdPKdS1_ii"
 MBB = b"_Z8Mbb_multPdPKdS1_ii"
+SEED = b"_Z22seeding_repulsion_stepPdPKdi"
 
 
 def cubin_path(n: int) -> str:
@@ -74,7 +75,7 @@ class RefKernels:
         self.mod = ctypes.c_void_p()
         _check(cu.cuModuleLoad(ctypes.byref(self.mod), cubin_path(n).encode()), "cuModuleLoad")
         self.fn = {}
-        for key, name in (("mss", MSS), ("mbb", MBB)):
+        for key, name in (("mss", MSS), ("mbb", MBB), ("seed", SEED)):
             f = ctypes.c_void_p()
             _check(cu.cuModuleGetFunction(ctypes.byref(f), self.mod, name), f"cuModuleGetFunction {name!r}")
             self.fn[key] = f
@@ -100,6 +101,48 @@ class RefKernels:
         num = self.n - start if num is None else num
         s = torch.cuda.current_stream().cuda_stream if stream is None else stream
         self._launch("mbb", V, F, X, start, num, s)
+
+    def seed_sphere(self, n, max_steps=100000):
+        """The reference's repulsive seeding of n points (seeding.cu:13-160,
+        its GPU path): the spiral start on the host, then per step the
+        reference's seeding_repulsion_step kernel for the forces and the
+        host update of seeding.cu:113-136 (numpy, elementwise in the written
+        order).  Returns (points (n, 3), steps)."""
+        import math
+
+        import numpy as np
+        import torch
+        x = np.zeros((n, 3))
+        phi = 0.0
+        for m in range(n):
+            z = -1.0 if n == 1 else 2.0 * m / float(n - 1) - 1.0
+            r = math.sqrt(1.0 - z * z)
+            if m == 0 or m == n - 1:
+                phi = 0.0
+            else:
+                phi += 3.6 / (r * math.sqrt(n))
+            x[m] = (r * math.cos(phi), r * math.sin(phi), z)
+        X = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        F = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        stream = torch.cuda.current_stream().cuda_stream
+        blocks = (n + THREADS_PER_BLOCK - 1) // THREADS_PER_BLOCK
+        steps = 0
+        while steps < max_steps:
+            X.copy_(torch.as_tensor(x))
+            args = [ctypes.c_void_p(F.data_ptr()), ctypes.c_void_p(X.data_ptr()), ctypes.c_int(n)]
+            params = (ctypes.c_void_p * 3)(*[ctypes.cast(ctypes.pointer(a), ctypes.c_void_p) for a in args])
+            _check(_driver().cuLaunchKernel(self.fn["seed"], blocks, 1, 1, THREADS_PER_BLOCK, 1, 1, 0,
+                                            ctypes.c_void_p(stream), params, None), "cuLaunchKernel seed")
+            f = F.cpu().numpy()
+            p = x + f
+            nrm = np.sqrt(p[:, 0] * p[:, 0] + p[:, 1] * p[:, 1] + p[:, 2] * p[:, 2])
+            p = p / nrm[:, None]
+            move = float(np.abs(p - x).max())
+            x = p
+            steps += 1
+            if move <= 1e-4:
+                break
+        return x, steps
 
     def close(self):
         if getattr(self, "mod", None):
