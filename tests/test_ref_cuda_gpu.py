@@ -62,7 +62,8 @@ def test_reference_cuda_mbb_against_this_library(ref_kernels):
     x, f = cube(7)
     X = torch.as_tensor(x, device="cuda")
     F = torch.as_tensor(np.ascontiguousarray(f[:, :3]), device="cuda")
-    V = torch.empty((N, 3), dtype=torch.float64, device="cuda")
+    # the reference writes the targets of [start, start + num) from V's first row
+    V = torch.empty((5000, 3), dtype=torch.float64, device="cuda")
     ref_kernels.mbb(V, F, X, start=100, num=5000)
     torch.cuda.synchronize()
     with Context(0) as ctx:
