@@ -117,6 +117,7 @@ SIGNATURES = {
     "gmi_sim_set_beat": ([_P, _D, _D, _P, _D], _I),
     "gmi_sim_set_secant_buffer": ([_P, _P, ctypes.c_longlong], _I),
     "gmi_sim_secant_count": ([_P, ctypes.POINTER(ctypes.c_longlong)], _I),
+    "gmi_sim_set_jacobian_probes": ([_P, _I, ctypes.c_ulonglong, _I], _I),
     "gmi_sim_set_learned_jacobian": ([_P, _P, _I, _P], _I),
     "gmi_sim_learned_policy": ([_P, _P], _I),
 }

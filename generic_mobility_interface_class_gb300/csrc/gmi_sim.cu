@@ -1270,6 +1270,49 @@ __global__ void secant_record_kernel(SimP P, const double *__restrict__ frames, 
                     (float)(sc[q] * (E[3 * c] * src[q][0] + E[3 * c + 1] * src[q][1] + E[3 * c + 2] * src[q][2]));
     }
 }
+// Random probe directions for the Jacobian, one CTA per filament: on the
+// filament's 6 NS rows r_i = g_i (|e_i| + e_f / 4), g_i standard normal
+// (splitmix64 counter hash, Box-Muller), e = the Broyden error of the step's
+// initial guess and e_f its RMS over the filament's rows, so that a probe
+// carries every component of the error in its own units; body rows are
+// zero.  The probe update is then -conf Jinv r: a first Broyden step from a
+// random error of the current one's size.
+__device__ __forceinline__ unsigned long long probe_hash(unsigned long long z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(128) probe_direction_kernel(SimP P, const double *__restrict__ err,
+                                                              unsigned long long seed, double *__restrict__ r)
+{
+    const int fil = blockIdx.x, n = fil / P.NF, i = fil % P.NF, n6 = P.n6;
+    const size_t base = (size_t)n * P.per_body + (size_t)6 * P.NS * i;
+    __shared__ double red[4];
+    double s = 0.0;
+    for (int k = threadIdx.x; k < n6; k += 128) s += err[base + k] * err[base + k];
+    s = warp_sum_d(s);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    const double ef = sqrt((red[0] + red[1] + red[2] + red[3]) / n6);
+    for (int k = threadIdx.x; k < n6; k += 128) {
+        const unsigned long long h = probe_hash(seed ^ probe_hash(base + k));
+        const double u1 = ((double)(h >> 11) + 1.0) * 0x1.0p-53;  // (0, 1]
+        const double u2 = (double)(probe_hash(h) >> 11) * 0x1.0p-53;
+        const double g = sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+        r[base + k] = g * (fabs(err[base + k]) + 0.25 * ef);
+    }
+    if (i == 0 && !P.wall)  // the swimmer's body rows (6, after its filaments)
+        for (int k = threadIdx.x; k < 6; k += 128) r[(size_t)n * P.per_body + (size_t)6 * P.NS * P.NF + k] = 0.0;
+}
+
+__global__ void vec_scale_kernel(int n, double a, const double *__restrict__ x, double *__restrict__ y)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) y[r] = a * x[r];
+}
 }  // namespace gmi
 
 // ---------------------------------------------------------------------------
@@ -1306,6 +1349,11 @@ struct gmi_sim {
     float *sec = nullptr;
     long long sec_cap = 0, sec_count = 0;
     double *dv = nullptr, *jv = nullptr;  // d = change of the error, Jinv d
+    // Jacobian probes recorded with the secant pairs (gmi_sim_set_jacobian_probes)
+    int probes = 0;
+    bool secant_pairs = true;
+    unsigned long long probe_seed = 0, probe_serial = 0;
+    double *probe_r = nullptr;
     // prescribed preferred-curvature beat (gmi_sim_set_beat)
     double *beat_phase = nullptr;
     double beat_amplitude = 0.0, beat_period = 1.0;
@@ -1474,7 +1522,8 @@ static gmi_status learned_prepare(gmi_sim *m)
 static gmi_status record_secant_pairs(gmi_sim *m)
 {
     const SimP &P = m->P;
-    if (!m->sec || m->learned_now || !m->features_ready || m->sec_count >= m->sec_cap) return GMI_OK;
+    if (!m->sec || !m->secant_pairs || m->learned_now || !m->features_ready || m->sec_count >= m->sec_cap)
+        return GMI_OK;
     const int n = P.nbroy;
     vec_sub_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, m->nerr, m->err, m->dv);
     GMI_TRY(sim_launched(m));
@@ -1844,6 +1893,23 @@ gmi_status gmi_sim_prepare(gmi_sim *m, double *body_mobility_out)
 
 namespace gmi {
 
+// The snapshot of the state a Broyden solve changes (snapshot_state),
+// allocated on first use.
+static gmi_status ensure_snapshot(gmi_sim *m)
+{
+    if (m->snap) return GMI_OK;
+    const SimP &P = m->P;
+    const size_t S = P.S, W = P.W, F = P.F;
+    gmi_solver *s = m->solver;
+    m->snap_fields = {{P.x, 3 * S},  {P.q, 4 * S},  {P.u, 3 * S},  {P.lam, 3 * (P.NS - 1) * F},
+                      {P.tl, 3 * F}, {P.cl, 3 * F}, {P.bx, 3 * W}, {P.bu, 3 * W},
+                      {P.bq, 4 * W}, {P.vb, 6 * W}};
+    if (s->B > 0) m->snap_fields.push_back({s->f_blobs, 3 * (size_t)s->B});
+    size_t total = 0;
+    for (const auto &f : m->snap_fields) total += f.n;
+    return sim_alloc(m, &m->snap, total);
+}
+
 // Copy the state a Broyden solve changes to the snapshot (restore = false)
 // or back (restore = true): segment x, q, u, the filament multipliers, the
 // body x, u, q and the linear solver's warm start.
@@ -1855,6 +1921,49 @@ static gmi_status snapshot_state(gmi_sim *m, bool restore)
         GMI_CUDA_TRY(cudaMemcpyAsync(restore ? f.p : a, restore ? a : f.p, f.n * sizeof(double),
                                      cudaMemcpyDeviceToDevice, sst(m)));
         off += f.n;
+    }
+    return GMI_OK;
+}
+
+// Jacobian probes (collection runs only): from the step's initial guess,
+// m->probes times a random update v = -conf Jinv r (probe_direction_kernel)
+// is applied, the error is evaluated there and one record per filament,
+// [phi | d = e(x + v) - e(x) | conf Jinv d | v], is appended beside the
+// secant pairs; the state is restored after each probe.  Unlike the secant
+// pairs of plain Broyden runs, whose updates stay in the directions the
+// damped plain start explores, the probes sample every direction of the
+// plain start's range, the stiff ones included.
+static gmi_status record_jacobian_probes(gmi_sim *m, int nt, int *gtot)
+{
+    const SimP &P = m->P;
+    if (!m->sec || m->probes <= 0 || m->learned_now || !m->features_ready) return GMI_OK;
+    const int n = P.nbroy;
+    if (!m->probe_r) GMI_TRY(sim_alloc(m, &m->probe_r, n));
+    GMI_TRY(ensure_snapshot(m));
+    for (int p = 0; p < m->probes && m->sec_count < m->sec_cap; ++p) {
+        const unsigned long long seed = m->probe_seed ^ (0x5851F42D4C957F2Dull * (++m->probe_serial));
+        probe_direction_kernel<<<P.F, 128, 0, sst(m)>>>(P, m->err, seed, m->probe_r);
+        GMI_TRY(sim_launched(m));
+        GMI_TRY(jacobian_inv_mult(m, m->probe_r, m->tmp));
+        vec_scale_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, -P.conf, m->tmp, m->upd);
+        GMI_TRY(sim_launched(m));
+        GMI_TRY(snapshot_state(m, false));
+        GMI_TRY(swimmer_update(m));
+        GMI_TRY(forces_and_torques(m, nt));
+        bool too_large = false, nonfinite = false;
+        int gi = 0;
+        GMI_TRY(velocities_and_errors(m, nt, m->nerr, &too_large, &nonfinite, &gi));
+        *gtot += gi;
+        if (!nonfinite) {
+            vec_sub_kernel<<<gridN(n, 256), 256, 0, sst(m)>>>(n, m->nerr, m->err, m->dv);
+            GMI_TRY(sim_launched(m));
+            GMI_TRY(jacobian_inv_mult(m, m->dv, m->jv));
+            secant_record_kernel<<<P.F, 64, 0, sst(m)>>>(P, m->frames, m->phi, m->dv, m->jv, m->upd, P.conf, m->sec,
+                                                          m->sec_count, m->sec_cap);
+            GMI_TRY(sim_launched(m));
+            m->sec_count = std::min(m->sec_cap, m->sec_count + P.F);
+        }
+        GMI_TRY(snapshot_state(m, true));
     }
     return GMI_OK;
 }
@@ -1875,6 +1984,7 @@ static gmi_status broyden_solve(gmi_sim *m, int nt, int cap, int *iters, int *gt
     if (*too_large) {
         GMI_TRY(prepare_jacobian_inv(m, nt));
         GMI_TRY(learned_prepare(m));
+        GMI_TRY(record_jacobian_probes(m, nt, gtot));
     }
     m->broyden_iter = 0;
     while (*too_large && m->broyden_iter < cap) {
@@ -1924,6 +2034,14 @@ gmi_status gmi_sim_step(gmi_sim *m, int nt, int *broyden_iters, int *gmres_iters
     int iters = 0, gtot = 0;
     bool too_large = false, diverged = false;
     gmi_status st = broyden_solve(m, nt, cap, &iters, &gtot, &too_large, &diverged);
+    if (st == GMI_ERR_NONFINITE && m->learned_now) {
+        // the learned H0 drove the state non-finite (a linear solve met a
+        // non-finite right-hand side): a divergence like any other, the
+        // step is restarted plain below
+        diverged = true;
+        iters = m->broyden_iter;
+        st = GMI_OK;
+    }
     int total = iters;
     if (st == GMI_OK && m->learned_now) {
         const bool ok = !too_large && !diverged;
@@ -2000,6 +2118,17 @@ gmi_status gmi_sim_set_secant_buffer(gmi_sim *m, float *records_d, long long cap
     return GMI_OK;
 }
 
+gmi_status gmi_sim_set_jacobian_probes(gmi_sim *m, int probes_per_step, unsigned long long seed, int secant_pairs)
+{
+    SIM_ARG_CHECK(m != nullptr && probes_per_step >= 0 && probes_per_step <= 64,
+                  "gmi_sim_set_jacobian_probes: probes_per_step must be 0..64");
+    m->probes = probes_per_step;
+    m->probe_seed = seed;
+    m->probe_serial = 0;
+    m->secant_pairs = secant_pairs != 0;
+    return GMI_OK;
+}
+
 gmi_status gmi_sim_secant_count(const gmi_sim *m, long long *count)
 {
     SIM_ARG_CHECK(m != nullptr && count != nullptr, "gmi_sim_secant_count: null argument");
@@ -2033,17 +2162,7 @@ gmi_status gmi_sim_set_learned_jacobian(gmi_sim *m, const gmi_mlp *mlp, int rank
         GMI_TRY(sim_alloc_bytes(m, (void **)&m->H2, F * mlp->n_hidden * sizeof(__nv_bfloat16)));
         GMI_TRY(sim_alloc_bytes(m, (void **)&m->O, F * mlp->n_out * sizeof(float)));
     }
-    if (!m->snap) {
-        const size_t S = P.S, W = P.W;
-        gmi_solver *s = m->solver;
-        m->snap_fields = {{P.x, 3 * S},   {P.q, 4 * S},  {P.u, 3 * S},  {P.lam, 3 * (P.NS - 1) * F},
-                          {P.tl, 3 * F},  {P.cl, 3 * F}, {P.bx, 3 * W}, {P.bu, 3 * W},
-                          {P.bq, 4 * W},  {P.vb, 6 * W}};
-        if (s->B > 0) m->snap_fields.push_back({s->f_blobs, 3 * (size_t)s->B});
-        size_t total = 0;
-        for (const auto &f : m->snap_fields) total += f.n;
-        GMI_TRY(sim_alloc(m, &m->snap, total));
-    }
+    GMI_TRY(ensure_snapshot(m));
     m->mlp = mlp;
     m->rank = rank;
     if (policy)

@@ -156,9 +156,11 @@ class LearnedJacobian:
 
 
 def collect_secant_pairs(sim_kwargs: dict, steps: int, capacity: int, precision: int = GMI_FP32C, device: int = 0,
-                         first_step: int = 0):
+                         first_step: int = 0, probes: int = 0, secant_pairs: bool = True, seed: int = 0):
     """Run the plain method for ``steps`` time steps and return the secant-pair
-    records it produced (a float32 CUDA tensor, at most ``capacity`` rows)."""
+    records it produced (a float32 CUDA tensor, at most ``capacity`` rows):
+    the Broyden iterations' own pairs (``secant_pairs``) and ``probes``
+    random-direction Jacobian probes per iterating step."""
     import torch
 
     from .sim import Simulation
@@ -168,6 +170,8 @@ def collect_secant_pairs(sim_kwargs: dict, steps: int, capacity: int, precision:
     try:
         sim.prepare()
         sim.set_secant_buffer(rec)
+        if probes or not secant_pairs:
+            sim.set_jacobian_probes(probes, seed, secant_pairs)
         for nt in range(first_step, first_step + steps):
             sim.step(nt)
             if sim.secant_count() >= capacity:

@@ -137,6 +137,12 @@ class Simulation:
         check(self.lib.gmi_sim_secant_count(self.handle, ctypes.byref(n)))
         return n.value
 
+    def set_jacobian_probes(self, probes_per_step: int, seed: int = 0, secant_pairs: bool = True):
+        """Record ``probes_per_step`` random-direction Jacobian probes per
+        iterating step beside (or, with ``secant_pairs=False``, instead of)
+        the Broyden iterations' secant pairs (gmi_sim_set_jacobian_probes)."""
+        check(self.lib.gmi_sim_set_jacobian_probes(self.handle, probes_per_step, seed, 1 if secant_pairs else 0))
+
     def set_learned_jacobian(self, net, policy=None):
         """Start Broyden from the network's initial inverse Jacobian
         (``learned.LearnedJacobian``; None: the plain method) under

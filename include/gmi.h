@@ -480,6 +480,15 @@ GMI_API void gmi_learned_policy_record(gmi_learned_policy *p, int used_learned, 
  * local frame (e3 along the filament's base direction). */
 GMI_API gmi_status gmi_sim_set_secant_buffer(gmi_sim *sim, float *records_d, long long capacity);
 GMI_API gmi_status gmi_sim_secant_count(const gmi_sim *sim, long long *count);
+/* Jacobian probes for the records of gmi_sim_set_secant_buffer: every step
+ * whose Broyden solve iterates first applies probes_per_step (0..64) random
+ * updates v = -conf Jinv r from its initial guess (r: normal samples scaled
+ * per row by the size of the step's error), evaluates the error there and
+ * appends one record per filament, [phi | d = e(x + v) - e(x) | conf Jinv d
+ * | v], restoring the state after each probe.  secant_pairs = 0 leaves the
+ * Broyden iterations' own records out.  No counterpart in the reference. */
+GMI_API gmi_status gmi_sim_set_jacobian_probes(gmi_sim *sim, int probes_per_step, unsigned long long seed,
+                                               int secant_pairs);
 /* Use the network's H0 (mlp NULL: the plain method) under policy (NULL:
  * defaults).  The network is read, not modified; several simulations may
  * share one.  rank is the head's rank (2, 4 or 8); n_in must be 6 nseg. */

@@ -164,6 +164,60 @@ def test_bad_network_falls_back_to_the_plain_trajectory(net):
         np.testing.assert_array_equal(s1[f], s0[f])
 
 
+def test_nonfinite_network_falls_back_to_the_plain_trajectory(net):
+    """A network whose U outputs are NaN makes the first learned update
+    non-finite, so the state goes non-finite and the step's next linear solve
+    meets a non-finite right-hand side.  That is a divergence of the learned
+    attempt: the step is restarted plain from its initial guess, and after
+    two such regressions the policy stops trying.  The trajectory is the
+    plain method's, bit for bit."""
+    from generic_mobility_interface_class_gb300.learned import default_policy
+    kw = small_swimmer()
+    plain, s0, _, _ = run(kw, 5)
+    zero_net(net)
+    p = net.params()
+    b3 = net.offsets[5]
+    p[b3 + 2 * net.nseg:b3 + 2 * net.nseg + 6 * net.nseg * net.rank] = np.nan  # U
+    net.set_params(p)
+    learned, s1, pol, _ = run(kw, 5, net, default_policy(calibration_steps=0))
+    assert pol.mode == 2 and pol.regressions == 2 and pol.steps_learned == 2
+    assert [c[1] > 0 for c in learned] == [True] * 5
+    for f in s0:
+        np.testing.assert_array_equal(s1[f], s0[f])
+
+
+def test_jacobian_probes_leave_the_trajectory_unchanged(gmi_lib):
+    """Probe records (gmi_sim_set_jacobian_probes): each iterating step
+    appends probes x filaments records of finite, non-zero d, b and t, and
+    the state is restored after every probe, so the trajectory is the one
+    without probes, bit for bit."""
+    from generic_mobility_interface_class_gb300.learned import record_length
+    from generic_mobility_interface_class_gb300.sim import Simulation
+    kw = small_swimmer()
+    plain, s0, _, _ = run(kw, 3)
+    rec = torch.zeros((2000, record_length(20)), dtype=torch.float32, device="cuda")
+    sim = Simulation(**kw, precision=1)
+    sim.prepare()
+    sim.set_secant_buffer(rec)
+    sim.set_jacobian_probes(3, seed=5, secant_pairs=False)
+    counts = [sim.step(nt) for nt in range(3)]
+    s1 = {f: sim.state(f) for f in s0}
+    nrec = sim.secant_count()
+    sim.close()
+    assert [c[0] for c in counts] == [c[0] for c in plain]
+    for f in s0:
+        np.testing.assert_array_equal(s1[f], s0[f])
+    iterating = sum(1 for c in plain if c[0] > 0)
+    assert nrec == 3 * 6 * iterating
+    r = rec[:nrec].cpu().numpy()
+    assert np.all(np.isfinite(r))
+    n6 = 120
+    for k in (1, 2, 3):
+        assert np.all(np.linalg.norm(r[:, k * n6:(k + 1) * n6], axis=1) > 0)
+    # the probes of one step differ from one another
+    assert not np.array_equal(r[0, 3 * n6:], r[6, 3 * n6:])
+
+
 def test_secant_pairs_are_collected(gmi_lib):
     from generic_mobility_interface_class_gb300.learned import record_length
     kw = small_swimmer()
