@@ -78,9 +78,9 @@ def parse():
     p.add_argument("--ts-warmup", type=int, default=5, help="untimed steps before the timed ones")
     p.add_argument("--ts-warmups", default="config4:1,config5:1",
                    help="untimed steps per workload where they differ from --ts-warmup")
-    p.add_argument("--ts-fp64-warmups", default="config5:0",
-                   help="untimed steps of the plain FP64 run per workload where they differ (config 5's FP64 "
-                        "step takes minutes; its first step's setup is a small part of it)")
+    p.add_argument("--ts-fp32c-only", default="config5",
+                   help="workloads whose plain FP64 run is skipped (config 5's FP64 steps take minutes each; "
+                        "pass an empty value to measure them)")
     p.add_argument("--accuracy-swimmers", type=int, default=8,
                    help="swimmers of the config-4 accuracy check against a tight-tolerance FP64 run (0 to skip)")
     p.add_argument("--learned", default="config3",
@@ -417,7 +417,7 @@ def run_time_steps(args, dev):
     from generic_mobility_interface_class_gb300._lib import GMI_FP32C, GMI_FP64
     steps_for = dict(kv.split(":") for kv in args.ts_steps.split(",") if kv)
     warm_for = dict(kv.split(":") for kv in getattr(args, "ts_warmups", "").split(",") if kv)
-    warm64_for = dict(kv.split(":") for kv in getattr(args, "ts_fp64_warmups", "").split(",") if kv)
+    fp32c_only = {w for w in getattr(args, "ts_fp32c_only", "").split(",") if w}
     out = {}
     for name in [w for w in args.ts_workloads.split(",") if w]:
         w0 = time.perf_counter()
@@ -434,10 +434,11 @@ def run_time_steps(args, dev):
         nsteps = int(steps_for.get(name, 10))
         warm = int(warm_for.get(name, args.ts_warmup))
         runs, final = {}, {}
-        for label, prec in (("fp64", GMI_FP64), ("fp32c", GMI_FP32C)):
+        methods = (("fp32c", GMI_FP32C),) if name in fp32c_only else (("fp64", GMI_FP64), ("fp32c", GMI_FP32C))
+        for label, prec in methods:
             sim = Simulation(**kw, precision=prec, device=dev)
             sim.prepare()
-            w = int(warm64_for.get(name, warm)) if label == "fp64" else warm
+            w = warm
             for nt in range(w):
                 sim.step(nt)
             torch.cuda.synchronize()
@@ -456,6 +457,12 @@ def run_time_steps(args, dev):
                            "broyden_iters": broyden, "gpu_launches": sim.launches - l0, "clocks": clocks.summary()}
             final[label] = {f: sim.state(f).ravel() for f in ("body_v", "seg_v", "seg_q", "body_x")}
             sim.close()
+
+        if "fp64" not in runs:
+            out[name] = {"workload": desc, "timed_steps": nsteps, "warmup_steps": warm, "broyden_tol": kw["tol"],
+                         "gmres_tol": kw["linear_tol"], **runs, "wall_s": time.perf_counter() - w0,
+                         "fp64": "skipped by default (minutes per step); --ts-fp32c-only= measures it"}
+            continue
 
         def rel(f):
             a, b = final["fp64"][f], final["fp32c"][f]
@@ -527,6 +534,13 @@ def run_batch_time_steps(args, dev, name, nsteps, warmup):
             errs.append(float(np.linalg.norm(b - a) / max(np.linalg.norm(a), 1e-300)))
         return {"max": max(errs), "median": float(np.median(errs))}
 
+    def body_vs_seg():
+        errs = []
+        for a, b, sv in zip(final["fp64"]["body_v"], final["fp32c"]["body_v"], final["fp64"]["seg_v"]):
+            sp = float(np.sqrt(np.mean(np.sum(sv.reshape(-1, 6)[:, :3] ** 2, axis=1))))
+            errs.append(float(np.linalg.norm((b - a).reshape(-1, 6)[:, :3]) / max(sp, 1e-300)))
+        return {"max": max(errs), "median": float(np.median(errs))}
+
     sizes = [(kw["nblob"], kw["nfil"] * kw["nseg"]) for kw in swimmers]
     if len(swimmers) != 64:
         desc = desc.replace("64 independent", f"{len(swimmers)} independent", 1)
@@ -536,6 +550,7 @@ def run_batch_time_steps(args, dev, name, nsteps, warmup):
             **runs,
             "speedup_fp32c_vs_fp64": runs["fp32c"]["swimmer_steps_per_s"] / runs["fp64"]["swimmer_steps_per_s"],
             "error_fp32c_vs_fp64_after_run": {"per_swimmer_velocity_rel": rel("body_v"),
+                                              "per_swimmer_translational_velocity_vs_segment_speed": body_vs_seg(),
                                               "per_swimmer_segment_velocity_rel": rel("seg_v")}}
 
 

@@ -561,10 +561,13 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
             for (int i = tid; i < k; i += 32) t += h2[i] * h2[i];
             t = warp_sum(t);
             if (tid == 0) {
+                // an exact breakdown (the new vector cancelled to nothing)
+                // gives ||w|| = 0, which the next Givens step takes as
+                // convergence; 0 * rsqrt(0) would be NaN
                 np[1] = fmax(h2[k] - t, 0.0);
-                const double ir = rsqrt(np[1]);
+                const double ir = np[1] > 0.0 ? rsqrt(np[1]) : 0.0;
                 np[2] = np[1] * ir;  // ||w||
-                np[3] = ir;          // 1 / ||w||
+                np[3] = ir;          // 1 / ||w|| (0 after a breakdown: the unused next column is zero)
             }
         }
         __syncthreads();
@@ -691,7 +694,7 @@ gmi_status cluster_gmres_launch(gmi_solver *s, double beta0, double norm_ref, do
     a.tol = tol;
     a.norm_ref = norm_ref;
     a.inv_norm_ref = 1.0 / norm_ref;
-    a.eta2 = reorth_eta2();
+    a.eta2 = reorth_eta2(false);  // the cluster solve is FP32C only
     a.ctl = s->ctl;
     PairConsts k;
     fill_consts(k, s->cfg.rblob, s->cfg.rblob, s->cfg.rblob, s->cfg.mu);

@@ -471,6 +471,39 @@ __global__ void __launch_bounds__(TPB) rpy_bb_df_kernel(const __grid_constant__ 
     }
 }
 
+// Small systems (up to kPairWarpMaxSources sources): one warp per target,
+// its 32 lanes striding over the sources read straight from the records
+// (they stay in L1), then the lanes' double-float sums added by a fixed
+// butterfly.  The TMA kernel gives such a system a few dozen CTAs, each a
+// serial chain of 128 double-float pair evaluations per thread; here every
+// lane has about n / 32.
+__global__ void __launch_bounds__(128) rpy_bb_df_warp_kernel(const PairLaunch args, const float4 *__restrict__ src,
+                                                             const DfBBConsts K)
+{
+    const int t = (int)((blockIdx.x * 128u + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (t >= args.n_tgt) return;
+    const float4 *tr = reinterpret_cast<const float4 *>(args.tgt_rec) + 3 * (size_t)(args.tgt_start + t);
+    const float4 t0 = tr[0], t1 = tr[1];
+    const df2 xi[3] = {df2{t0.x, t1.x}, df2{t0.y, t1.y}, df2{t0.z, t1.z}};
+    df2 v[3] = {df2{0.f, 0.f}, df2{0.f, 0.f}, df2{0.f, 0.f}};
+    for (int j = lane; j < args.n_src; j += 32) {
+        const float4 b0 = src[3 * (size_t)j], b1 = src[3 * (size_t)j + 1], b2 = src[3 * (size_t)j + 2];
+        const df2 d[3] = {df_diff(xi[0], df2{b0.x, b1.x}), df_diff(xi[1], df2{b0.y, b1.y}),
+                          df_diff(xi[2], df2{b0.z, b1.z})};
+        const df2 F[3] = {df2{b0.w, b2.y}, df2{b1.w, b2.z}, df2{b2.x, b2.w}};
+        pair_bb_df(d, F, K, v);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            v[c] = df_add(v[c], df2{__shfl_xor_sync(0xffffffffu, v[c].h, o), __shfl_xor_sync(0xffffffffu, v[c].l, o)});
+    if (lane != 0) return;
+    double *o = args.out + (size_t)t * 3;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) o[c] = args.accumulate ? o[c] + df_to_double(v[c]) : df_to_double(v[c]);
+}
+
 // ---------------------------------------------------------------------------
 // 2'. packed FP32 variant (kinds SS, BB, SB, BS): each thread takes two
 // sources per step, one per lane of the packed f32x2 instructions.  After a
@@ -1199,12 +1232,34 @@ static int choose_splits(const gmi_context *ctx, int n_tgt_ctas, int n_src, int 
     return s < max_splits ? s : max_splits;
 }
 
-// The double-float blob-blob sum: 128 targets per CTA, the sources split
-// over enough CTAs for two waves, the splits added in order.
+// The double-float blob-blob sum: the warp kernel for small systems, else
+// 128 targets per CTA, the sources split over enough CTAs for two waves, the
+// splits added in order.
 constexpr int kDfTpb = 128;
 static gmi_status launch_bb_df(gmi_context *ctx, const void *tgt_rec, int tgt_start, int n_tgt, const void *src_rec,
                                int n_src, const PairConsts &k, double *out, int accumulate)
 {
+    DfBBConsts K;
+    K.four_a2 = df_from_double(k.eq[0]);
+    K.two_a2 = df_from_double(k.eq[1]);
+    K.f8pm = df_from_double(k.eq[2]);
+    K.f6pma = df_from_double(k.eq[3]);
+    K.q32 = df_from_double(k.eq[4]);
+    K.third = df_from_double(1.0 / 3.0);
+    if (n_src <= kPairWarpMaxSources) {
+        PairLaunch a{};
+        a.tgt_rec = tgt_rec;
+        a.tgt_start = tgt_start;
+        a.n_tgt = n_tgt;
+        a.n_src = n_src;
+        a.out = out;
+        a.accumulate = accumulate;
+        const unsigned ctas = (unsigned)(((long long)n_tgt * 32 + 127) / 128);
+        rpy_bb_df_warp_kernel<<<ctas, 128, 0, ctx->stream>>>(a, static_cast<const float4 *>(src_rec), K);
+        ctx->launches++;
+        GMI_CUDA_TRY(cudaGetLastError());
+        return GMI_OK;
+    }
     void *fn = reinterpret_cast<void *>(&rpy_bb_df_kernel<kDfTpb>);
     const size_t smem = ring_bytes(false, false);
     GMI_CUDA_TRY(raise_dynamic_smem_limit(fn, smem));
@@ -1236,13 +1291,6 @@ static gmi_status launch_bb_df(gmi_context *ctx, const void *tgt_rec, int tgt_st
         if (st != GMI_OK) return st;
         a.partial = static_cast<double *>(ctx->partial.ptr);
     }
-    DfBBConsts K;
-    K.four_a2 = df_from_double(k.eq[0]);
-    K.two_a2 = df_from_double(k.eq[1]);
-    K.f8pm = df_from_double(k.eq[2]);
-    K.f6pma = df_from_double(k.eq[3]);
-    K.q32 = df_from_double(k.eq[4]);
-    K.third = df_from_double(1.0 / 3.0);
     CUtensorMap map;
     gmi_status st = make_record_map(ctx, &map, src_rec, n_src, false);
     if (st != GMI_OK) return st;

@@ -92,13 +92,15 @@ __device__ __forceinline__ void pair2_ss(float2 dx, float2 dy, float2 dz, const 
     float2 Bt = fma2(ns, c3dF, c3dF);                          // (1 - s) dF / r^3
     float2 Ar = mul2(bc2(-0.5f), c3);                          // -1/(2 r^3)
     float2 Br = mul2(mul2(c3, ir2), mul2(bc2(1.5f), dT));      // 3 dT / (2 r^5)
-    if (!(r2.x > k.four_a2)) {
-        const SSCoeffs c = ss_near2(r2.x, ir.x, dF.x, dT.x, k);
-        At.x = c.At; Bt.x = c.Bt; Ar.x = c.Ar; Br.x = c.Br; c3.x = c.c3;
-    }
-    if (!(r2.y > k.four_a2)) {
-        const SSCoeffs c = ss_near2(r2.y, ir.y, dF.y, dT.y, k);
-        At.y = c.At; Bt.y = c.Bt; Ar.y = c.Ar; Br.y = c.Br; c3.y = c.c3;
+    if (!(fminf(r2.x, r2.y) > k.four_a2)) {  // one test per step; near pairs are rare
+        if (!(r2.x > k.four_a2)) {
+            const SSCoeffs c = ss_near2(r2.x, ir.x, dF.x, dT.x, k);
+            At.x = c.At; Bt.x = c.Bt; Ar.x = c.Ar; Br.x = c.Br; c3.x = c.c3;
+        }
+        if (!(r2.y > k.four_a2)) {
+            const SSCoeffs c = ss_near2(r2.y, ir.y, dF.y, dT.y, k);
+            At.y = c.At; Bt.y = c.Bt; Ar.y = c.Ar; Br.y = c.Br; c3.y = c.c3;
+        }
     }
     const float2 cx = mul2(c3, dx), cy = mul2(c3, dy), cz = mul2(c3, dz);
     p[0] = fma2(At, F[0], p[0]); p[0] = fma2(Bt, dx, p[0]); p[0] = fma2(F[4], cz, p[0]); m[0] = fma2(F[5], cy, m[0]);
@@ -121,15 +123,17 @@ __device__ __forceinline__ void pair2_bb(float2 dx, float2 dy, float2 dz, const 
     float2 At = fma2(mul2(ir, ns), bc2(-1.0f / 3.0f), ir);
     const float2 c3dF = mul2(mul2(ir, ir2), dF);
     float2 Bt = fma2(ns, c3dF, c3dF);
-    if (!(r2.x > k.four_a2)) {
-        const float q = r2.x * ir.x * k.q32, u = k.f6pma / k.f8pm;
-        At.x = (1.0f - 3.0f * q) * u;
-        Bt.x = q * u * (ir.x * ir.x) * dF.x;
-    }
-    if (!(r2.y > k.four_a2)) {
-        const float q = r2.y * ir.y * k.q32, u = k.f6pma / k.f8pm;
-        At.y = (1.0f - 3.0f * q) * u;
-        Bt.y = q * u * (ir.y * ir.y) * dF.y;
+    if (!(fminf(r2.x, r2.y) > k.four_a2)) {
+        if (!(r2.x > k.four_a2)) {
+            const float q = r2.x * ir.x * k.q32, u = k.f6pma / k.f8pm;
+            At.x = (1.0f - 3.0f * q) * u;
+            Bt.x = q * u * (ir.x * ir.x) * dF.x;
+        }
+        if (!(r2.y > k.four_a2)) {
+            const float q = r2.y * ir.y * k.q32, u = k.f6pma / k.f8pm;
+            At.y = (1.0f - 3.0f * q) * u;
+            Bt.y = q * u * (ir.y * ir.y) * dF.y;
+        }
     }
     p[0] = fma2(At, F[0], p[0]); p[0] = fma2(Bt, dx, p[0]);
     p[1] = fma2(At, F[1], p[1]); p[1] = fma2(Bt, dy, p[1]);
@@ -146,13 +150,15 @@ __device__ __forceinline__ void unequal_coeffs2(float2 r2, float2 ir, float2 dF,
     A = fma2(t, ir, ir);                                      // (1 + t) / r
     Cd = mul2(ir, ir2);                                       // 1/r^3
     Bd = mul2(mul2(fma2(t, bc2(-3.0f), bc2(1.0f)), Cd), dF);  // (1 - 3t) dF / r^3
-    if (!(r2.x > k.sum2)) {
-        const UnequalCoeffs c = unequal_near2(r2.x, ir.x, dF.x, k);
-        A.x = c.A; Bd.x = c.Bd; Cd.x = c.Cd;
-    }
-    if (!(r2.y > k.sum2)) {
-        const UnequalCoeffs c = unequal_near2(r2.y, ir.y, dF.y, k);
-        A.y = c.A; Bd.y = c.Bd; Cd.y = c.Cd;
+    if (!(fminf(r2.x, r2.y) > k.sum2)) {
+        if (!(r2.x > k.sum2)) {
+            const UnequalCoeffs c = unequal_near2(r2.x, ir.x, dF.x, k);
+            A.x = c.A; Bd.x = c.Bd; Cd.x = c.Cd;
+        }
+        if (!(r2.y > k.sum2)) {
+            const UnequalCoeffs c = unequal_near2(r2.y, ir.y, dF.y, k);
+            A.y = c.A; Bd.y = c.Bd; Cd.y = c.Cd;
+        }
     }
 }
 

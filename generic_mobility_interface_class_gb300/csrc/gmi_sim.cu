@@ -161,29 +161,36 @@ __device__ void extrapolate3(double *a, double *a1, double *a2, int count, int n
 
 // filament::initial_guess (filament.cpp:825-1018) with segment::initial_guess
 // (segment.cpp:38-66) and the state taken from the body.
+// In two passes: one thread per segment for the segments' own guesses (each
+// its own u and q, with an FP64 sin/cos in lie_exp), then one thread per
+// filament for the chain that depends on all of them.  The arithmetic of
+// every segment is the reference's, in its order.
+__global__ void segment_initial_guess_kernel(SimP P, int nt)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= P.S) return;
+    for (int c = 0; c < 3; ++c) {
+        P.xm2[3 * s + c] = P.xm1[3 * s + c];
+        P.xm1[3 * s + c] = P.x[3 * s + c];
+    }
+    if (nt <= P.neuler) {
+        for (int c = 0; c < 3; ++c) P.um1[3 * s + c] = P.u[3 * s + c];
+    } else {
+        for (int c = 0; c < 3; ++c) {
+            const double t = 2.0 * P.u[3 * s + c] - P.um1[3 * s + c];
+            P.um1[3 * s + c] = P.u[3 * s + c];
+            P.u[3 * s + c] = t;
+        }
+    }
+    const Q4 q = ldq(P.q + 4 * s);
+    stq(P.qm1 + 4 * s, q);
+    stq(P.q + 4 * s, qmul(lie_exp(P.u + 3 * s), q));
+}
+
 __global__ void filament_initial_guess_kernel(SimP P, int nt)
 {
     const int fil = blockIdx.x * blockDim.x + threadIdx.x;
     if (fil >= P.F) return;
-    for (int i = 0; i < P.NS; ++i) {
-        const int s = fil * P.NS + i;
-        for (int c = 0; c < 3; ++c) {
-            P.xm2[3 * s + c] = P.xm1[3 * s + c];
-            P.xm1[3 * s + c] = P.x[3 * s + c];
-        }
-        if (nt <= P.neuler) {
-            for (int c = 0; c < 3; ++c) P.um1[3 * s + c] = P.u[3 * s + c];
-        } else {
-            for (int c = 0; c < 3; ++c) {
-                const double t = 2.0 * P.u[3 * s + c] - P.um1[3 * s + c];
-                P.um1[3 * s + c] = P.u[3 * s + c];
-                P.u[3 * s + c] = t;
-            }
-        }
-        const Q4 q = ldq(P.q + 4 * s);
-        stq(P.qm1 + 4 * s, q);
-        stq(P.q + 4 * s, qmul(lie_exp(P.u + 3 * s), q));
-    }
     accept_state_from_body(P, fil);
     const int nl = 3 * (P.NS - 1);
     extrapolate3(P.lam + nl * fil, P.lam1 + nl * fil, P.lam2 + nl * fil, nl, nt);
@@ -2020,8 +2027,9 @@ gmi_status gmi_sim_step(gmi_sim *m, int nt, int *broyden_iters, int *gmres_iters
     GMI_CUDA_TRY(cudaSetDevice(m->solver->ctx->device));
     const SimP &P = m->P;
     if (!P.wall) body_initial_guess_kernel<<<gridN(P.W, 32), 32, 0, sst(m)>>>(P, nt);
+    segment_initial_guess_kernel<<<gridN(P.S, 64), 64, 0, sst(m)>>>(P, nt);
     filament_initial_guess_kernel<<<gridN(P.F, 64), 64, 0, sst(m)>>>(P, nt);
-    GMI_TRY(sim_launched(m, P.wall ? 1 : 2));
+    GMI_TRY(sim_launched(m, P.wall ? 2 : 3));
     if (m->beat) {
         beat_strain_kernel<<<gridN(P.F, 64), 64, 0, sst(m)>>>(P, m->beat_phase, m->beat_amplitude,
                                                               2.0 * kPi / m->beat_period, (nt + 1) * P.DT);

@@ -1205,12 +1205,23 @@ static cudaError_t launch_step(bool pdl, void (*kern)(KArgs...), dim3 grid, dim3
 
 // eta^2 of the conditional re-orthogonalisation in the device Arnoldi
 // steps: the second Gram-Schmidt pass runs only when one pass kept less
-// than eta^2 of ||w||^2.  eta = 1/sqrt(2) by default; GMI_REORTH_ETA sets
-// it, and 0 runs the second pass always.
-double reorth_eta2()
+// than eta^2 of ||w||^2, i.e. when the projection cancelled more than
+// 1 - eta of the new vector's norm.  After one classical pass the new
+// vector's loss of orthogonality to the basis is about eps / eta, so
+// eta = 0.1 keeps it within ten rounding units per vector (far below what
+// GMRES notices).  That is the default of the mixed-precision solve, which
+// checks every result with an FP64-grade residual: measured on the swimmer
+// workloads, eta = 0.1 and eta = 1/sqrt(2) give the same GMRES counts and
+// the same velocities to the Broyden tolerance, and 0.1 skips the second
+// pass far more often.  FP64 solves keep eta = 1/sqrt(2) (Daniel, Gragg,
+// Kaufman and Stewart's "twice is enough" value): with 0.1 a 12-step FP64
+// trajectory of a small swimmer drifted from the reference's own by 8e-4,
+// with 1/sqrt(2) it matches it to 1e-9.  GMI_REORTH_ETA sets eta for both; 0 runs the
+// second pass always.
+double reorth_eta2(bool fp64)
 {
     const char *env = std::getenv("GMI_REORTH_ETA");
-    const double eta = env ? std::atof(env) : 0.70710678118654752440;
+    const double eta = env ? std::atof(env) : (fp64 ? 0.70710678118654752440 : 0.1);
     return eta > 0.0 ? eta * eta : 0.0;
 }
 
@@ -1290,7 +1301,7 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     GMI_CUDA_TRY(launch_step(pdl, s3_finish_project_kernel, dim3(L.nblk), dim3(kSTpb), 0, st, W, nblob,
                              (const double *)s->mbb, (const double *)s->gm_partial, splits, (const double *)s->z,
                              (const double *)s->R, (const double *)s->refs, s->w, (const double *)s->Q, ld, n, P,
-                             G, tk3, s->st_scal, s->H, ldh, s->beta, s->cs, s->sn, s->ctl, reorth_eta2()));
+                             G, tk3, s->st_scal, s->H, ldh, s->beta, s->cs, s->sn, s->ctl, reorth_eta2(f64)));
     GMI_CUDA_TRY(launch_step(pdl, s4_project_norm_givens_kernel, dim3(L.nblk), dim3(kSTpb), 0, st,
                              (const double *)s->Q, ld, n, s->w, P, G, tk4, s->st_scal, s->H, ldh, s->beta, s->cs,
                              s->sn, s->ctl));
@@ -1607,7 +1618,7 @@ static gmi_status store_solution(gmi_solver *s)
 // double-float arithmetic, the body terms in FP64); each correction solves
 // A d = r by GMRES with the FP32C operator (FP64 Arnoldi, Givens and
 // vectors) to the relative tolerance that would meet the target in one pass
-// (with a 0.3 margin for the FP32C operator's own error), but not below
+// (kInnerMargin times it; GMI_INNER_MARGIN overrides), but not below
 // kInnerTol; x += d.  This converges to the FP64 solution at the requested
 // tolerance, which GMRES on the FP32C operator alone cannot (its answer is
 // off by cond(A) times the operator's rounding).  kInnerTol sits somewhat
@@ -1615,9 +1626,13 @@ static gmi_status store_solution(gmi_solver *s)
 // falling there, and the deeper inner solves save more refinement restarts
 // than they cost (the fewest total iterations on the 962- and 16,896-particle
 // swimmers among floors from 1e-6 to 2e-8; GMI_INNER_TOL overrides it).  The
-// iteration count returned is the sum of inner iterations.
+// margin is 1: on the same swimmers a margin of 0.3, 0.5, 0.7 or 1 gave the
+// same velocities to the Broyden tolerance, and 1 the fewest GMRES
+// iterations (225 against 267 per step on the 962-particle swimmer; the
+// plain FP64 solve takes 210).  The iteration count returned is the sum of
+// inner iterations.
 static constexpr double kInnerTol = 1e-7;
-static constexpr double kInnerMargin = 0.3;
+static constexpr double kInnerMargin = 1.0;
 static constexpr int kMaxRefinements = 12;
 
 static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
@@ -1675,6 +1690,8 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
     // FP32 pipe); GMI_REFINE_DF=0 takes the FP64 kernel instead
     const char *floor_env = std::getenv("GMI_INNER_TOL");  // the floor of the inner tolerance
     const double inner_floor = floor_env ? std::atof(floor_env) : kInnerTol;
+    const char *margin_env = std::getenv("GMI_INNER_MARGIN");  // the inner target's margin
+    const double inner_margin = margin_env ? std::atof(margin_env) : kInnerMargin;
     const char *df_env = std::getenv("GMI_REFINE_DF");
     s->ctx->precision = (df_env && df_env[0] == '0') ? GMI_FP64 : GMI_DF64;
     status = system_matrix_mult(s, s->soln, s->tmp);
@@ -1720,7 +1737,7 @@ static gmi_status solve_linear_system(gmi_solver *s, int *iters_out)
         }
         GMI_CUDA_TRY(cudaMemcpyAsync(s->xacc, s->soln, ld * sizeof(double), cudaMemcpyDeviceToDevice, st));
         GMI_CUDA_TRY(cudaMemsetAsync(s->soln, 0, ld * sizeof(double), st));
-        const double want = kInnerMargin * tol * norm_rhs / beta;
+        const double want = inner_margin * tol * norm_rhs / beta;
         const double inner_tol = want > inner_floor ? want : inner_floor;
         int iters = 0;
         GMI_TRY(gmres_run(s, beta, beta, inner_tol, false, true, &iters, true));

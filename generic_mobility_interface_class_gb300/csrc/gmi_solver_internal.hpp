@@ -89,7 +89,7 @@ gmi_status solver_place_blobs(gmi_solver *s, const double *body_x, const double 
 
 // eta^2 of the conditional re-orthogonalisation of the device Arnoldi steps
 // (GMI_REORTH_ETA; 0: the second Gram-Schmidt pass always runs).
-double reorth_eta2();
+double reorth_eta2(bool fp64);
 
 // Frees the prescribed-cilia workspace (gmi_solver_destroy).
 void prescribed_release(gmi_solver *s);

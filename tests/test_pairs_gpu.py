@@ -226,12 +226,13 @@ def test_fp32c_is_translation_robust(gpu_ctx, oracle_built):
     assert rel_err(got, want) < FP32C_TOL
 
 
-@pytest.mark.parametrize("n", [3001, 5003])
+@pytest.mark.parametrize("n", [901, 2048, 3001, 5003])
 def test_double_float_blob_blob_against_oracle(own_ctx, oracle_built, n):
     """GMI_DF64: the blob-blob sum in double-float arithmetic against the
-    FP64 oracle (near and far pairs, the self term, several tiles and source
-    splits), also with the cloud far from the origin, a target slice, and
-    accumulation; the other pair sums refuse the precision."""
+    FP64 oracle (near and far pairs, the self term; up to 2048 sources the
+    warp-per-target kernel, above it several tiles and source splits), also
+    with the cloud far from the origin, a target slice, and accumulation;
+    the other pair sums refuse the precision."""
     from generic_mobility_interface_class_gb300 import GmiError, seeding
     rpy = oracle_built
     x = seeding.random_cube(n, seed=7)
