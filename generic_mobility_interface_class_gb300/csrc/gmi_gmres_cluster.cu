@@ -342,27 +342,41 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
         __syncthreads();
         // ---- C: blob-blob sum (packed FP32); Givens step of iteration k-1 ---
         if (tid < S * bl) {
+            // two accumulator sets, one per source pair of an unrolled step,
+            // so that their chains overlap: a thread has only a few dozen
+            // steps and a few warps share each scheduler
             float2 pacc[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+            float2 pacc2[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
             double acc[3] = {0.0, 0.0, 0.0};
             const int p0 = ps * pc, p1 = min(npairs, p0 + pc);
             int cnt = 0;
-#pragma unroll 2
-            for (int p = p0; p < p1; ++p) {
+            auto step = [&](int p, float2 *acc2) {
                 const float4 q0 = ipos[3 * p], q1 = ipos[3 * p + 1], q2 = ipos[3 * p + 2];
                 const float4 f0 = iload[2 * p], f1 = iload[2 * p + 1];
                 const float2 dx = add2(add2(th[0], make_float2(q0.x, q0.y)), add2(tlo[0], make_float2(q1.z, q1.w)));
                 const float2 dy = add2(add2(th[1], make_float2(q0.z, q0.w)), add2(tlo[1], make_float2(q2.x, q2.y)));
                 const float2 dz = add2(add2(th[2], make_float2(q1.x, q1.y)), add2(tlo[2], make_float2(q2.z, q2.w)));
                 const float2 F[3] = {make_float2(f0.x, f0.y), make_float2(f0.z, f0.w), make_float2(f1.x, f1.y)};
-                pair2_bb(dx, dy, dz, F, a.kbb, pacc);
-                if (++cnt == kCgFold) {
+                pair2_bb(dx, dy, dz, F, a.kbb, acc2);
+            };
+            int p = p0;
+            for (; p + 1 < p1; p += 2) {
+                step(p, pacc);
+                step(p + 1, pacc2);
+                if ((cnt += 2) >= kCgFold) {
 #pragma unroll
                     for (int d = 0; d < 3; ++d) {
-                        acc[d] += (double)(pacc[d].x + pacc[d].y);
-                        pacc[d] = make_float2(0.f, 0.f);
+                        acc[d] += (double)((pacc[d].x + pacc[d].y) + (pacc2[d].x + pacc2[d].y));
+                        pacc[d] = pacc2[d] = make_float2(0.f, 0.f);
                     }
                     cnt = 0;
                 }
+            }
+            if (p < p1) step(p, pacc);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                pacc[d].x += pacc2[d].x;
+                pacc[d].y += pacc2[d].y;
             }
             if (pc <= kCgFold) {  // no fold happened: the partial is an FP32 sum (no FP64 work)
 #pragma unroll
@@ -558,8 +572,10 @@ __global__ void __launch_bounds__(kCgTpb) gmres_cluster_kernel(const ClusterGmre
         // cluster sum as h2: every CTA computes the same bits
         if (tid < 32) {
             double t = 0.0;
-            for (int i = tid; i < k; i += 32) t += h2[i] * h2[i];
-            t = warp_sum(t);
+            if (!(dgks && flag[1])) {  // a skipped second pass left h2 = 0
+                for (int i = tid; i < k; i += 32) t += h2[i] * h2[i];
+                t = warp_sum(t);
+            }
             if (tid == 0) {
                 // an exact breakdown (the new vector cancelled to nothing)
                 // gives ||w|| = 0, which the next Givens step takes as
