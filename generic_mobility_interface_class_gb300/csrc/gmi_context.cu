@@ -2,6 +2,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -65,6 +66,25 @@ cudaError_t raise_dynamic_smem_limit(const void *fn, size_t bytes)
     if (bytes <= have) return cudaSuccess;
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
     if (e == cudaSuccess) have = bytes;
+    return e;
+}
+
+cudaError_t max_active_blocks(int *blocks, const void *fn, int threads, size_t smem)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<int, const void *, int, size_t>, int> known;  // (device, function, threads, smem)
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_tuple(dev, fn, threads, smem);
+    const auto it = known.find(key);
+    if (it != known.end()) {
+        *blocks = it->second;
+        return cudaSuccess;
+    }
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks, fn, threads, smem);
+    if (e == cudaSuccess) known[key] = *blocks;
     return e;
 }
 

@@ -62,6 +62,10 @@ gmi_status context_check_device_errors(gmi_context *ctx);
 // it: it is only ever raised, under a lock, and a launch sized for one
 // solver never finds it lowered by another.
 cudaError_t raise_dynamic_smem_limit(const void *fn, size_t bytes);
+// cudaOccupancyMaxActiveBlocksPerMultiprocessor for this device, function,
+// block size and dynamic shared memory, asked once and remembered (a pair
+// launch sizes its grid by it on every call).
+cudaError_t max_active_blocks(int *blocks, const void *fn, int threads, size_t smem);
 
 // One process-wide lock over every stream capture and every call that
 // synchronises the whole device (cudaFree, cudaFreeHost, and cudaMalloc,

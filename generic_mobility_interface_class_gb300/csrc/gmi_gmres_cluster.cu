@@ -604,7 +604,36 @@ struct ClusterChoice {
 };
 }  // namespace
 
+static ClusterChoice choose_cluster_uncached(gmi_solver *s);
+
+// The launch shape of this solver's cluster solve: chosen on its first solve
+// and kept (the shared-memory limit, the cluster-size attribute and the
+// occupancy query are driver calls that would otherwise sit between the
+// kernels of every linear solve).
 static ClusterChoice choose_cluster(gmi_solver *s)
+{
+    ClusterChoice ch;
+    if (s->cluster_state == 0) {
+        ch = choose_cluster_uncached(s);
+        s->cluster_state = ch.csize > 0 ? 1 : -1;
+        s->cluster_csize = ch.csize;
+        s->cluster_bpc = ch.bpc;
+        s->cluster_kq = ch.kq;
+        s->cluster_kqs = ch.kqs;
+        s->cluster_smem = ch.smem;
+        return ch;
+    }
+    if (s->cluster_state > 0) {
+        ch.csize = s->cluster_csize;
+        ch.bpc = s->cluster_bpc;
+        ch.kq = s->cluster_kq;
+        ch.kqs = s->cluster_kqs;
+        ch.smem = s->cluster_smem;
+    }
+    return ch;
+}
+
+static ClusterChoice choose_cluster_uncached(gmi_solver *s)
 {
     ClusterChoice ch;
     const int nb = s->B, W = s->W;

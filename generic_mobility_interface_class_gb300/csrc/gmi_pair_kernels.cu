@@ -1264,7 +1264,7 @@ static gmi_status launch_bb_df(gmi_context *ctx, const void *tgt_rec, int tgt_st
     const size_t smem = ring_bytes(false, false);
     GMI_CUDA_TRY(raise_dynamic_smem_limit(fn, smem));
     int occ = 0;
-    GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kDfTpb, smem));
+    GMI_CUDA_TRY(max_active_blocks(&occ, fn, kDfTpb, smem));
     const int n_tgt_ctas = (n_tgt + kDfTpb - 1) / kDfTpb;
     const int slots = ctx->sm_count * (occ > 0 ? occ : 1);
     int splits = 1;
@@ -1364,7 +1364,7 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
     const size_t smem = ring_bytes(f64, kShapes[sidx].packed != 0);
     GMI_CUDA_TRY(raise_dynamic_smem_limit(fn, smem));
     int occ = 0;
-    GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, tpb, smem));
+    GMI_CUDA_TRY(max_active_blocks(&occ, fn, tpb, smem));
     const int n_tgt_ctas = (n_tgt + tpb * tt - 1) / (tpb * tt);
     int splits = shape.splits > 0 ? shape.splits : choose_splits(ctx, n_tgt_ctas, n_src, occ);
     int chunk = (n_src + splits - 1) / splits;
@@ -1582,7 +1582,7 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     const size_t smem = ring_bytes(f64, kShapes[sidx].packed != 0);
     GMI_CUDA_TRY(raise_dynamic_smem_limit(fn, smem));
     int occ = 0;
-    GMI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, tpb, smem));
+    GMI_CUDA_TRY(max_active_blocks(&occ, fn, tpb, smem));
     const int n_tgt_ctas = (n_tgt + tpb * tt - 1) / (tpb * tt);
     const int slots = env.sm_count * (occ > 0 ? occ : 1);
     int splits = 1;

@@ -56,6 +56,11 @@ struct gmi_solver {
     bool use_pdl = true;      // Arnoldi-step kernels launched for programmatic dependent launch (GMI_PDL=0: off;
                               // also off if a graph with programmatic edges fails to capture or instantiate)
     double *Qr = nullptr;     // the cluster solve's row-major copy of Q (allocated by its first launch)
+    // the cluster solve's launch shape, chosen once (it depends only on the
+    // sizes): 0 not chosen yet, 1 chosen (cluster_* below), -1 unusable
+    int cluster_state = 0;
+    int cluster_csize = 0, cluster_bpc = 0, cluster_kq = 0, cluster_kqs = 0;
+    size_t cluster_smem = 0;
     PrescribedWork *prescribed = nullptr;  // allocated by the first prescribed-cilia solve
 };
 
