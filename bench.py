@@ -438,21 +438,20 @@ def run_time_steps(args, dev):
         for label, prec in methods:
             sim = Simulation(**kw, precision=prec, device=dev)
             sim.prepare()
-            w = warm
-            for nt in range(w):
+            for nt in range(warm):
                 sim.step(nt)
             torch.cuda.synchronize()
             l0 = sim.launches
             broyden, gmres = [], []
             with ClockSampler(dev) as clocks:
                 t0 = time.perf_counter()
-                for nt in range(w, w + nsteps):
+                for nt in range(warm, warm + nsteps):
                     b, g = sim.step(nt)
                     broyden.append(b)
                     gmres.append(g)
                 torch.cuda.synchronize()
                 wall = time.perf_counter() - t0
-            runs[label] = {"warmup_steps": w, "steps_per_s": nsteps / wall, "ms_per_step": 1e3 * wall / nsteps,
+            runs[label] = {"warmup_steps": warm, "steps_per_s": nsteps / wall, "ms_per_step": 1e3 * wall / nsteps,
                            "broyden_iters_per_step": sum(broyden) / nsteps, "gmres_iters_per_step": sum(gmres) / nsteps,
                            "broyden_iters": broyden, "gpu_launches": sim.launches - l0, "clocks": clocks.summary()}
             final[label] = {f: sim.state(f).ravel() for f in ("body_v", "seg_v", "seg_q", "body_x")}

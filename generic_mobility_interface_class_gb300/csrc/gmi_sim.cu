@@ -1277,6 +1277,7 @@ __global__ void secant_record_kernel(SimP P, const double *__restrict__ frames, 
                     (float)(sc[q] * (E[3 * c] * src[q][0] + E[3 * c + 1] * src[q][1] + E[3 * c + 2] * src[q][2]));
     }
 }
+
 // Random probe directions for the Jacobian, one CTA per filament: on the
 // filament's 6 NS rows r_i = g_i (|e_i| + e_f / 4), g_i standard normal
 // (splitmix64 counter hash, Box-Muller), e = the Broyden error of the step's

@@ -228,6 +228,9 @@ def main(argv=None) -> None:
     p.add_argument("--threads", type=int, default=None, help="host threads of a batch workload (default: one each)")
     p.add_argument("--per-swimmer", action="store_true",
                    help="batch workloads: also print each swimmer's Broyden and GMRES iterations per step")
+    p.add_argument("--profile-from", type=int, default=None,
+                   help="bracket steps from this one to the last with cudaProfilerStart/Stop, so that a profiler "
+                        "started with --profile-from-start off captures only those steps")
     p.add_argument("--no-barrier", action="store_true",
                    help="batch workloads: after step 0, run the remaining steps with SwimmerBatch.run (no "
                         "batch-wide barrier between steps) and print their total time")
@@ -246,7 +249,13 @@ def main(argv=None) -> None:
         sim.prepare()
     print(f"{args.workload} ({desc}), {args.precision}: prepare {1e3 * (time.perf_counter() - t0):.1f} ms", flush=True)
     batch = isinstance(sim, SwimmerBatch)
+    profiling = False
     for nt in range(args.steps):
+        if args.profile_from is not None and nt == args.profile_from:
+            import torch
+            torch.cuda.synchronize()
+            torch.cuda.profiler.start()
+            profiling = True
         if batch and args.no_barrier and nt == 1:
             t0 = time.perf_counter()
             runs = sim.run(args.steps - 1, nt)
@@ -268,6 +277,10 @@ def main(argv=None) -> None:
                 print("  per swimmer (Broyden, GMRES): " + " ".join(f"{x[0]},{x[1]}" for x in it), flush=True)
         else:
             print(f"step {nt}: {it[0]} Broyden iterations, {it[1]} GMRES iterations, {ms:.1f} ms", flush=True)
+    if profiling:
+        import torch
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     sim.close()
 
 

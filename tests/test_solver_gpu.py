@@ -291,6 +291,44 @@ def test_refinement_residual_double_float_matches_fp64(gmi_lib, oracle_built, mo
     assert abs(out["1"][0] - out["0"][0]) <= max(3, out["0"][0] // 10)
 
 
+@pytest.mark.parametrize("cluster,precision", [("1", 1), ("0", 1), ("0", 0)])
+def test_conditional_reorthogonalisation_and_inner_target(cluster, precision, gmi_lib, monkeypatch):
+    """The conditional second Gram-Schmidt pass (the default eta: 0.1 in
+    FP32C solves, 1/sqrt 2 in FP64) against a second pass on every iteration
+    (GMI_REORTH_ETA=0), and in FP32C the one-pass inner target against a
+    0.3 margin (GMI_INNER_MARGIN): on the cluster solve and on the
+    multi-kernel Arnoldi step, every setting meets the tolerance in the
+    dense FP64 system and they agree far below it."""
+    from oracle import mobility_dense as md
+    monkeypatch.setenv("GMI_GMRES_CLUSTER", cluster)
+    nfil, nseg = 4, 10
+    refs, bx, bq, xs, fs, bf = swimmer_geometry(1, nfil, nseg)
+    want = md.compute_velocities(xs, fs, bx, bq, bf, refs, nseg, force_scale=1.5)
+    settings = [("default", None, None), ("always two passes", "0", None)]
+    if precision == 1:
+        settings.append(("inner margin 0.3", None, "0.3"))
+    out = {}
+    for label, eta, margin in settings:
+        for var, val in (("GMI_REORTH_ETA", eta), ("GMI_INNER_MARGIN", margin)):
+            if val is None:
+                monkeypatch.delenv(var, raising=False)
+            else:
+                monkeypatch.setenv(var, val)
+        s = make_solver(refs, 1, nfil, nseg, precision=precision)
+        s.x_segs_host[:] = xs
+        s.f_segs_host[:] = fs
+        iters = [s.compute_velocities(bx, bq, bf)[0] for _ in range(2)]
+        out[label] = (iters, np.concatenate([s.f_blobs_host.ravel(), s.v_bodies().ravel()]))
+        s.close()
+    bound = 1e-7 if precision == 1 else 1e-8
+    for label, (iters, x) in out.items():
+        assert iters[0] > 0
+        resid = np.linalg.norm(want["A"] @ x - want["rhs"]) / np.linalg.norm(want["rhs"])
+        assert resid < bound, (label, resid)
+        assert rel_err(x, out["default"][1]) < 1e-6, label
+        assert abs(iters[0] - out["default"][0][0]) <= max(3, out["default"][0][0] // 5), (label, iters)
+
+
 def test_programmatic_dependent_launch_changes_nothing(gmi_lib, monkeypatch):
     """The Arnoldi-step kernels launched with programmatic dependencies (the
     default) and without (GMI_PDL=0) do the same arithmetic in the same
