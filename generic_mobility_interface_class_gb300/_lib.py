@@ -84,6 +84,8 @@ SIGNATURES = {
     "gmi_solver_set_body_reference_matrices": ([_P, _P, _P], _I),
     "gmi_solver_compute_velocities": ([_P, _P, _P, _P, ctypes.POINTER(_I)], _I),
     "gmi_solver_compute_velocities_prescribed": ([_P, _P, _P, _P, _P, ctypes.POINTER(_I)], _I),
+    "gmi_solver_set_generalised_force_refs": ([_P, _P, _I], _I),
+    "gmi_solver_compute_velocities_prescribed_dynamic": ([_P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(_I)], _I),
     "gmi_solver_last_linear_solve": ([_P, ctypes.POINTER(_I), ctypes.POINTER(_D)], _I),
     "gmi_solver_set_strict_convergence": ([_P, _I], _I),
     "gmi_solver_get_v_bodies": ([_P, _P], _I),

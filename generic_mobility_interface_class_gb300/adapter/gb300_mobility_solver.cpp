@@ -36,8 +36,15 @@ void gb300_mobility_solver::allocate_host_memory()
     cfg.mu = MU;
     cfg.rseg = RSEG;
     cfg.rblob = RBLOB;
+#if defined(REPULSIVE_FORCE_FACTOR) && defined(END_FORCE_MAGNITUDE)
     cfg.repulsive_force_factor = REPULSIVE_FORCE_FACTOR;
     cfg.end_force_magnitude = END_FORCE_MAGNITUDE;
+#else
+    // prescribed-shape cilia define no barrier (mobility_solver.cpp:152-163
+    // skips it); the solver's defaults stand in, unused
+    cfg.repulsive_force_factor = 2.0;
+    cfg.end_force_magnitude = 1.0;
+#endif
     cfg.wall = INFINITE_PLANE_WALL;
 #if USE_GMRES_FOR_LINEAR_SYSTEM
     cfg.max_linear_iter = MAX_LINEAR_SYSTEM_ITER;
@@ -152,6 +159,10 @@ void gb300_mobility_solver::compute_velocities_on_device(std::vector<swimmer> &s
                                                          const int nt)
 {
     (void)nt;
+#if PRESCRIBED_CILIA
+    compute_velocities_prescribed_on_device(swimmers, num_gmres_iterations);
+    return;
+#endif
     ensure_blob_references(swimmers);
     std::vector<double> x, q, f;
     gather_bodies(swimmers, x, q, f);
@@ -164,6 +175,53 @@ void gb300_mobility_solver::compute_velocities_on_device(std::vector<swimmer> &s
         check(gmi_solver_get_v_bodies(solver, &v_bodies.data[0]), "gmi_solver_get_v_bodies");
 #endif
 }
+
+#if PRESCRIBED_CILIA
+// mobility_solver::compute_velocities for prescribed-shape cilia
+// (mobility_solver.cpp:1362-1369): the filaments' shape-velocity directions
+// and phase speeds go to the device solve; the segment forces land in
+// f_segs_host, the blob forces in f_blobs_host, the body velocities in
+// v_bodies.  With DYNAMIC_PHASE_EVOLUTION the phase speeds are unknowns: the
+// generalised-force table the base class read (mobility_solver.cpp:37-65) is
+// handed over once, and the solved speeds are written back to the filaments
+// (mobility_solver.cpp:1306-1320).
+void gb300_mobility_solver::compute_velocities_prescribed_on_device(std::vector<swimmer> &swimmers,
+                                                                    int &num_gmres_iterations)
+{
+    ensure_blob_references(swimmers);
+    std::vector<double> x, q, f;
+    gather_bodies(swimmers, x, q, f);
+    const size_t F = swimmers.size() * NFIL;
+    std::vector<double> vel_dir(3 * NSEG * F), speed(F), phase(F), omega0(F);
+    for (size_t n = 0; n < swimmers.size(); ++n)
+        for (int i = 0; i < NFIL; ++i) {
+            const filament &fil = swimmers[n].filaments[i];
+            const size_t k = n * NFIL + i;
+            for (int m = 0; m < 3 * NSEG; ++m) vel_dir[3 * NSEG * k + m] = fil.vel_dir[m];
+            speed[k] = fil.phase_speed;
+            phase[k] = fil.phase;
+            omega0[k] = fil.omega0;
+        }
+#if DYNAMIC_PHASE_EVOLUTION
+    if (!gen_force_refs_set) {
+        check(gmi_solver_set_generalised_force_refs(solver, gen_force_refs.data(), (int)gen_force_refs.size()),
+              "gmi_solver_set_generalised_force_refs");
+        gen_force_refs_set = true;
+    }
+    check(gmi_solver_compute_velocities_prescribed_dynamic(solver, x.data(), q.data(), vel_dir.data(), phase.data(),
+                                                           omega0.data(), speed.data(), &num_gmres_iterations),
+          "gmi_solver_compute_velocities_prescribed_dynamic");
+    for (size_t n = 0; n < swimmers.size(); ++n)
+        for (int i = 0; i < NFIL; ++i) swimmers[n].filaments[i].phase_speed = speed[n * NFIL + i];
+#else
+    check(gmi_solver_compute_velocities_prescribed(solver, x.data(), q.data(), vel_dir.data(), speed.data(),
+                                                   &num_gmres_iterations),
+          "gmi_solver_compute_velocities_prescribed");
+#endif
+    if (v_bodies.num_rows == 6 * NSWIM)
+        check(gmi_solver_get_v_bodies(solver, &v_bodies.data[0]), "gmi_solver_get_v_bodies");
+}
+#endif
 
 // mobility_solver::make_body_reference_matrices (mobility_solver.cpp:1693-1771)
 // on the device; the matrices land in the base class's members.

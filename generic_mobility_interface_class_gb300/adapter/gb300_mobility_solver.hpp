@@ -63,6 +63,10 @@ public:
 
 private:
     bool blob_refs_set = false;
+    bool gen_force_refs_set = false;
+#if PRESCRIBED_CILIA
+    void compute_velocities_prescribed_on_device(std::vector<swimmer> &swimmers, int &num_gmres_iterations);
+#endif
     void check(gmi_status st, const char *what) const;
     void ensure_blob_references(const std::vector<swimmer> &swimmers);
 };

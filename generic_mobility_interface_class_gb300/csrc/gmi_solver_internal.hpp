@@ -62,6 +62,10 @@ struct gmi_solver {
     int cluster_csize = 0, cluster_bpc = 0, cluster_kq = 0, cluster_kqs = 0;
     size_t cluster_smem = 0;
     PrescribedWork *prescribed = nullptr;  // allocated by the first prescribed-cilia solve
+    // generalised forces of the prescribed beat over one period, for solves
+    // with the phase speeds as unknowns; serial counts the setter's calls
+    std::vector<double> gen_force_refs;
+    unsigned gen_force_serial = 0;
 };
 
 

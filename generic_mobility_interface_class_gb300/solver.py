@@ -135,6 +135,34 @@ class MobilitySolver:
                                                                 ctypes.byref(it)))
         return it.value
 
+    def set_generalised_force_refs(self, refs) -> None:
+        """The beat's generalised-force table over one period (count >= 2
+        samples; empty clears it), as the reference reads it from its
+        reference file (mobility_solver.cpp:37-65)."""
+        r = np.ascontiguousarray(refs, dtype=np.float64).ravel()
+        check(self.lib.gmi_solver_set_generalised_force_refs(self.handle, _cptr(r) if r.size else None, int(r.size)))
+
+    def compute_velocities_prescribed_dynamic(self, vel_dir, phase, omega0, phase_speed=None, body_x=None,
+                                              body_q=None):
+        """Prescribed-shape cilia with the phase speeds solved for
+        (DYNAMIC_PHASE_EVOLUTION).  phase, omega0: (W*nfil,) phases and
+        natural frequencies; phase_speed: the initial guess (default omega0,
+        as the reference).  Returns (GMRES iterations, phase speeds); the
+        forces and body velocities land as in compute_velocities_prescribed."""
+        W = self.W
+        bx = np.ascontiguousarray(np.zeros((W, 3)) if body_x is None else body_x, dtype=np.float64)
+        bq = np.ascontiguousarray(np.tile([1.0, 0, 0, 0], (W, 1)) if body_q is None else body_q, dtype=np.float64)
+        vd = np.ascontiguousarray(vel_dir, dtype=np.float64)
+        ph = np.ascontiguousarray(phase, dtype=np.float64)
+        om = np.ascontiguousarray(omega0, dtype=np.float64)
+        sp = np.array(om if phase_speed is None else phase_speed, dtype=np.float64).ravel()
+        if vd.size != 3 * self.S or ph.size != sp.size or om.size != sp.size or sp.size != W * self.cfg.nfil:
+            raise ValueError("vel_dir must hold 3 values per segment; phase, omega0, phase_speed one per filament")
+        it = ctypes.c_int()
+        check(self.lib.gmi_solver_compute_velocities_prescribed_dynamic(
+            self.handle, _cptr(bx), _cptr(bq), _cptr(vd), _cptr(ph), _cptr(om), _cptr(sp), ctypes.byref(it)))
+        return it.value, sp
+
     def last_linear_solve(self):
         """(GMRES iterations, relative residual) of the last linear solve."""
         it, res = ctypes.c_int(), ctypes.c_double()

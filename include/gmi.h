@@ -287,6 +287,29 @@ GMI_API gmi_status gmi_solver_compute_velocities_prescribed(gmi_solver *s, const
                                                             const double *body_q_h, const double *vel_dir_h,
                                                             const double *phase_speed_h, int *gmres_iters);
 
+/* The generalised-force table of the prescribed beat, which the reference's
+ * mobility_solver constructor reads from its reference file
+ * (mobility_solver.cpp:37-65; written by a WRITE_GENERALISED_FORCES run,
+ * cilia_sim_main.cpp:184-246): count samples of sum_k vel_dir_k . f_k of one
+ * cilium over one beat period, sample j at phase 2 pi j / count.  count >= 2;
+ * count 0 clears the table.  The solver keeps its own copy. */
+GMI_API gmi_status gmi_solver_set_generalised_force_refs(gmi_solver *s, const double *refs_h, int count);
+
+/* gmi_solver_compute_velocities_prescribed with the phase speeds among the
+ * unknowns (DYNAMIC_PHASE_EVOLUTION; mobility_solver.cpp:219-296, :518-634,
+ * :831-866, :1031-1113, :1306-1320; swimmer.cpp:974-1023): each filament's
+ * segments move at phase_speed times its vel_dir, and its generalised force
+ * sum_k vel_dir_k . f_k equals the table's value at phase[f] (cubic Hermite
+ * interpolation) times omega0[f] / (2 pi).  phase_speed_h[F]: on entry the
+ * initial guess (the reference uses omega0, filament.cpp:841), on return the
+ * solved speeds.  Needs gmi_solver_set_generalised_force_refs first.  The
+ * other results are those of gmi_solver_compute_velocities_prescribed; a
+ * solve of the other kind than the last one starts cold. */
+GMI_API gmi_status gmi_solver_compute_velocities_prescribed_dynamic(gmi_solver *s, const double *body_x_h,
+                                                                    const double *body_q_h, const double *vel_dir_h,
+                                                                    const double *phase_h, const double *omega0_h,
+                                                                    double *phase_speed_h, int *gmres_iters);
+
 /* The last linear solve (GMRES, or in FP32C the mixed-precision refinement):
  * its GMRES iterations and its relative residual |b - A x| / |b| (GMRES's
  * estimate in FP64; the FP64-grade refinement residual in FP32C).  Either

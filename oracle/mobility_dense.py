@@ -117,3 +117,79 @@ def body_mobility_reference(xb_last, refs, body_q_last, a_blob, mu):
         _, vb = saddle_solve(xb_last, np.asarray(body_q_last).reshape(1, 4), refs, rhs, a_blob, mu)
         N[:, 5 - col] = vb[0]
     return N
+
+
+def generalised_force(table, phase):
+    """The generalised force of the prescribed beat at each phase: the
+    reference's cubic Hermite interpolation of its table over one period,
+    with its one-sided difference at sample 0 (mobility_solver.cpp:219-280)."""
+    t = np.asarray(table, dtype=np.float64)
+    n = len(t)
+    out = []
+    for phi in np.atleast_1d(np.asarray(phase, dtype=np.float64)):
+        x = 0.5 * phi / np.pi
+        x -= np.floor(x)
+        x *= n
+        lo = int(x)
+        if lo == n:
+            out.append(t[0])
+            continue
+        hi = 0 if lo == n - 1 else lo + 1
+        dlo = t[1] - t[0] if lo == 0 else 0.5 * (t[hi] - t[lo - 1])
+        dhi = t[0] - t[n - 1] if hi == 0 else 0.5 * (t[0 if hi == n - 1 else hi + 1] - t[lo])
+        s = x - lo
+        out.append(t[lo] * (2 * s ** 3 - 3 * s ** 2 + 1) + dlo * (s ** 3 - 2 * s ** 2 + s) +
+                   t[hi] * (3 * s ** 2 - 2 * s ** 3) + dhi * (s ** 3 - s ** 2))
+    return np.array(out)
+
+
+def prescribed_system(x, xs, body_x, body_q, refs, vel_dir, nfil, nseg, rseg=1.0, rblob=1.0, mu=1.0,
+                      phase_speed=None, table=None, phase=None, omega0=None):
+    """(A x, b) of the prescribed-shape cilia system (CILIA_TYPE 3):
+    system_matrix_mult (mobility_solver.cpp:733-905) and assemble_rhs
+    (:211-310) for free bodies.  x = [f_seg (S,3) | f_blob (B,3) | (U, Omega)
+    (W,6) | phase speeds (F,) when table is given].  With phase_speed given
+    (the speeds prescribed) the segment rows of b are phase_speed * vel_dir;
+    with table, phase and omega0 given (DYNAMIC_PHASE_EVOLUTION) the phase
+    speeds are unknowns: their rows of A x are -sum_k K_k . f_k, the segment
+    rows take -phase_speed K, and b's phase rows are -q omega0 / (2 pi)."""
+    body_x = np.asarray(body_x, dtype=np.float64).reshape(-1, 3)
+    body_q = np.asarray(body_q, dtype=np.float64).reshape(-1, 4)
+    refs = np.asarray(refs, dtype=np.float64).reshape(-1, 3)
+    xs = np.asarray(xs, dtype=np.float64).reshape(-1, 3)
+    K = np.asarray(vel_dir, dtype=np.float64).reshape(-1, 3)
+    W, S, nblob = len(body_x), len(xs), len(refs)
+    dynamic = table is not None
+    F = W * nfil if dynamic else 0
+    B = W * nblob
+    x = np.asarray(x, dtype=np.float64)
+    fs = x[:3 * S].reshape(S, 3)
+    fb = x[3 * S:3 * (S + B)].reshape(B, 3)
+    U = x[3 * (S + B):3 * (S + B) + 6 * W].reshape(W, 6)
+    ps = x[3 * (S + B) + 6 * W:]
+    xb = blob_positions(body_x, body_q, refs)
+    fs6 = np.concatenate([fs, np.zeros_like(fs)], axis=1)
+    v_segs = rpy.msb(xs, xb, fb, rseg, rblob, mu, v_in=rpy.mss(xs, fs6, rseg, mu))[:, :3]
+    v_blobs = rpy.mbs(xb, xs, fs6, rseg, rblob, mu) + rpy.mbb(xb, fb, rblob, mu)
+    sw_seg = np.arange(S) // (nfil * nseg)
+    sw_blob = np.arange(B) // nblob
+    d_seg = xs - body_x[sw_seg]
+    d_blob = xb - body_x[sw_blob]
+    rows_seg = v_segs - U[sw_seg, :3] - np.cross(U[sw_seg, 3:], d_seg)
+    rows_blob = v_blobs - U[sw_blob, :3] - np.cross(U[sw_blob, 3:], d_blob)
+    body = np.zeros((W, 6))
+    for n in range(W):
+        body[n, :3] = -fs[sw_seg == n].sum(0) - fb[sw_blob == n].sum(0)
+        body[n, 3:] = -np.cross(d_seg[sw_seg == n], fs[sw_seg == n]).sum(0) - \
+            np.cross(d_blob[sw_blob == n], fb[sw_blob == n]).sum(0)
+    b = np.zeros(3 * (S + B) + 6 * W + F)
+    fil = np.arange(S) // nseg
+    if dynamic:
+        rows_seg = rows_seg - ps[fil][:, None] * K
+        phase_rows = -np.einsum("fkc,fkc->f", K.reshape(F, nseg, 3), fs.reshape(F, nseg, 3))
+        b[3 * (S + B) + 6 * W:] = -generalised_force(table, phase) * (0.5 * np.asarray(omega0) / np.pi)
+    else:
+        phase_rows = np.zeros(0)
+        b[:3 * S] = (np.asarray(phase_speed, dtype=np.float64)[fil][:, None] * K).ravel()
+    Ax = np.concatenate([rows_seg.ravel(), rows_blob.ravel(), body.ravel(), phase_rows])
+    return Ax, b

@@ -66,6 +66,19 @@ CASES = {
     # advancing at constant speed): the solver's prescribed-motion system
     "prescribed": dict(CILIA_TYPE="3", NFIL="4", NSEG="20", NBLOB="162", R_OVER_L="0.25", RBLOB="1.0",
                        TOTAL_TIME_STEPS="3", DYNAMIC_PHASE_EVOLUTION="false", nblob_subdiv=2, fil_subdiv=1, seed=5),
+    # the reference's generalised-force table for that beat: its own main
+    # built with WRITE_GENERALISED_FORCES (config.hpp:259-266 makes that one
+    # swimmer with one cilium over one period, phase 0, omega0 = 2 pi), which
+    # writes sum_k vel_dir_k . f_k of the cilium after every step
+    # (cilia_sim_main.cpp:184-246)
+    "prescribed_table": dict(CILIA_TYPE="3", NFIL="1", NSEG="20", NBLOB="162", R_OVER_L="0.25", RBLOB="1.0",
+                             TOTAL_TIME_STEPS="STEPS_PER_PERIOD", DYNAMIC_PHASE_EVOLUTION="false",
+                             WRITE_GENERALISED_FORCES="true", nblob_subdiv=2, fil_subdiv=1, seed=5),
+    # phase speeds solved with the forces (DYNAMIC_PHASE_EVOLUTION): the
+    # "prescribed" swimmer driven by that table
+    "prescribed_dynamic": dict(CILIA_TYPE="3", NFIL="4", NSEG="20", NBLOB="162", R_OVER_L="0.25", RBLOB="1.0",
+                               TOTAL_TIME_STEPS="4", DYNAMIC_PHASE_EVOLUTION="true", nblob_subdiv=2, fil_subdiv=1,
+                               seed=5),
     "wall_filaments": dict(BODY_OR_SURFACE_TYPE="0", NFIL="9", NSEG="20", NBLOB="0", R_OVER_L="0.25",
                            RBLOB="1.0", TOTAL_TIME_STEPS="10", seed=3),
     # BASELINE config 1 geometry: sphere of radius 10a, 642 blobs (icosphere 3),
@@ -190,14 +203,30 @@ def run_case(case: str, exe: str | None = None) -> str:
     return rundir
 
 
+GEN_FORCE_FILE = "coral_larvae_reference_generalised_forces.dat"  # filament.cpp:1666-1674, SHAPE_SEQUENCE 2
+
+
+def generalised_force_table() -> str:
+    """Run the "prescribed_table" case (the reference's own main) and return
+    the path of the generalised-force file it wrote."""
+    rundir = run_case("prescribed_table")
+    return os.path.join(rundir, GEN_FORCE_FILE)
+
+
 def run_prescribed_dump(case: str) -> str:
     """Build the case with prescribed_dump.cpp as its driver, run it, and
-    return the path of its dump (see prescribed_dump.cpp)."""
+    return the path of its dump (see prescribed_dump.cpp).  A case with
+    DYNAMIC_PHASE_EVOLUTION reads the generalised-force table, which the
+    "prescribed_table" case writes first."""
+    import shutil
+    table = generalised_force_table() if CASES[case].get("DYNAMIC_PHASE_EVOLUTION") == "true" else None
     exe = build(case, tag="_dump", driver="prescribed_dump.cpp")
     rundir = os.path.join(os.path.dirname(exe), "run")
     os.makedirs(rundir, exist_ok=True)
     for f in os.listdir(rundir):
         os.remove(os.path.join(rundir, f))
+    if table:
+        shutil.copy(table, rundir)
     blobs, fils = seeds(case)
     spec = CASES[case]
     import numpy as np

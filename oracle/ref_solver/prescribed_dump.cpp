@@ -8,8 +8,10 @@
 // what the mobility solver receives and returns:
 //   step, GMRES iterations, then per swimmer the body x and q; per segment
 //   its position and shape-velocity direction (filament vel_dir); per
-//   filament its phase speed; after the solve the segment forces, blob
-//   forces and body velocities.
+//   filament its phase, natural frequency omega0 and phase speed (with
+//   DYNAMIC_PHASE_EVOLUTION the solver's initial guess); after the solve
+//   the segment forces, blob forces, body velocities and, per filament, the
+//   phase speed the solve left (phase_speed_out).
 // One line per item, "<name> <values...>", in prescribed_dump.txt.
 #include <cstdio>
 #include <fstream>
@@ -53,6 +55,8 @@ int main()
             for (int i = 0; i < NFIL; i++) {
                 put(out, "vel_dir", sw.filaments[i].vel_dir.data(), 3 * NSEG);
                 put(out, "phase_speed", &sw.filaments[i].phase_speed, 1);
+                put(out, "phase", &sw.filaments[i].phase, 1);
+                put(out, "omega0", &sw.filaments[i].omega0, 1);
             }
         }
         put(out, "x_segs", mobility.x_segs_host, 3 * NSWIM * NFIL * NSEG);
@@ -63,6 +67,8 @@ int main()
         put(out, "f_segs", mobility.f_segs_host, 6 * NSWIM * NFIL * NSEG);
         put(out, "f_blobs", mobility.f_blobs_host, 3 * NSWIM * NBLOB);
         put(out, "v_bodies", &mobility.v_bodies.data[0], 6 * NSWIM);
+        for (int n = 0; n < NSWIM; n++)
+            for (int i = 0; i < NFIL; i++) put(out, "phase_speed_out", &swimmers[n].filaments[i].phase_speed, 1);
         for (int n = 0; n < NSWIM; n++) {  // explicit body update, as cilia_sim_main.cpp:218-232
             swimmer &sw = swimmers[n];
             for (int c = 0; c < 3; c++) {

@@ -74,3 +74,28 @@ def test_reference_side_adapter_compiles(gmi_lib):
                         "-I" + adapter, os.path.join(adapter, "gb300_mobility_solver.cpp")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_reference_side_adapter_compiles_for_prescribed_cilia(gmi_lib, tmp_path):
+    """The adapter's prescribed-cilia branch (CILIA_TYPE 3, with and without
+    DYNAMIC_PHASE_EVOLUTION) compiles against the reference's headers, with the
+    reference's config.hpp set for it; skipped where the reference tree is
+    absent."""
+    from oracle import reference_dir
+    ref = reference_dir()
+    if not os.path.isfile(os.path.join(ref, "mobility_solver.hpp")):
+        pytest.skip("reference tree not present")
+    from generic_mobility_interface_class_gb300 import _lib
+    from oracle.ref_solver import build_ref_solver as brs
+    adapter = os.path.join(_lib.PKG, "adapter")
+    for dyn in ("true", "false"):
+        spec = dict(brs.COMMON)
+        spec.update(CILIA_TYPE="3", DYNAMIC_PHASE_EVOLUTION=dyn)
+        cfg = tmp_path / dyn
+        cfg.mkdir()
+        (cfg / "config.hpp").write_text(brs.config_text(spec))
+        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I" + str(cfg), "-I" + ref,
+                            "-I" + os.path.join(_lib.ROOT, "include"), "-I" + adapter, "-include",
+                            str(cfg / "config.hpp"), os.path.join(adapter, "gb300_mobility_solver.cpp")],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, (dyn, r.stderr[-3000:])

@@ -114,3 +114,50 @@ def test_mobility_symmetry(oracle_built):
             M[:, c] = rpy.mss(x, f).ravel()
         np.testing.assert_allclose(M, M.T, atol=1e-15)
         assert np.all(np.linalg.eigvalsh(M) > 0)
+
+
+@pytest.mark.parametrize("case", ["prescribed", "prescribed_dynamic"])
+def test_prescribed_system_restatement_against_reference_solutions(case, oracle_built):
+    """The dense restatement of the prescribed-cilia system
+    (oracle/mobility_dense.py prescribed_system) holds the reference's own
+    solutions: |A x - b| / |b| at the GMRES tolerance (1e-10) for every step of
+    both golden cases, with the phase speeds given and with them solved for
+    (whose b is the interpolated generalised-force table alone)."""
+    from oracle import mobility_dense as md
+    g = load_golden(case, prefix="")
+    nfil, nseg = int(g["nfil"]), int(g["nseg"])
+    S = nfil * nseg
+    for k in range(len(g["gmres_iters"])):
+        x = [g["f_segs"][k].reshape(S, 6)[:, :3].ravel(), g["f_blobs"][k], g["v_bodies"][k]]
+        if case == "prescribed_dynamic":
+            x.append(g["phase_speed_out"][k])
+            kw = dict(table=g["gen_force_refs"], phase=g["phase"][k], omega0=g["omega0"][k])
+        else:
+            kw = dict(phase_speed=g["phase_speed"][k])
+        Ax, b = md.prescribed_system(np.concatenate(x), g["x_segs"][k], g["body_x"][k], g["body_q"][k],
+                                     g["blob_refs"], g["vel_dir"][k], nfil, nseg, float(g["rseg"]),
+                                     float(g["rblob"]), float(g["mu"]), **kw)
+        assert np.linalg.norm(Ax - b) / np.linalg.norm(b) < 2e-10, (case, k)
+
+
+def test_generalised_force_interpolation_edges():
+    """The table interpolation hits the samples at phases 2 pi j / n, wraps
+    over the period (phase + 2 pi, negative phases) and runs from sample
+    n - 1 back to sample 0 near 2 pi; with samples of a smooth periodic
+    function it is close to that function between the samples."""
+    from oracle.mobility_dense import generalised_force
+    n = 300
+    ph = 2 * np.pi * np.arange(n) / n
+    table = 3.0 + np.cos(ph) + 0.5 * np.sin(2 * ph)
+    assert np.allclose(generalised_force(table, ph), table, rtol=0, atol=1e-12)
+    assert np.allclose(generalised_force(table, ph + 2 * np.pi), table, rtol=0, atol=1e-12)
+    assert np.allclose(generalised_force(table, ph - 4 * np.pi), table, rtol=0, atol=1e-12)
+    mid = 2 * np.pi * (np.arange(n) + 0.37) / n
+    exact = 3.0 + np.cos(mid) + 0.5 * np.sin(2 * mid)
+    got = generalised_force(table, mid)
+    assert np.max(np.abs(got[1:-1] - exact[1:-1])) < 1e-6
+    # the first and last intervals take one-sided differences at sample 0
+    assert abs(got[0] - exact[0]) < 1e-4 and abs(got[-1] - exact[-1]) < 1e-4
+    # the last interval runs back to sample 0
+    assert min(table[-1], table[0]) - 1e-3 <= generalised_force(table, [2 * np.pi - 1e-9])[0] <= \
+        max(table[-1], table[0]) + 1e-3

@@ -47,6 +47,70 @@ def test_prescribed_solves_match_reference(gmi_lib, precision):
     s.close()
 
 
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32c"])
+def test_prescribed_dynamic_solves_match_reference(gmi_lib, precision):
+    """Phase speeds among the unknowns (DYNAMIC_PHASE_EVOLUTION):
+    tests/golden/prescribed_dynamic.npz holds the reference's generalised-force
+    table (its own WRITE_GENERALISED_FORCES run over one beat period) and four
+    solves of the same swimmer driven by it.  Each solve here gets that
+    table, the step's phases, natural frequencies, shapes and body state, and
+    omega0 as the phase speeds' initial guess (as the reference); it must
+    return the same forces, body velocities and phase speeds.  A static solve
+    after the dynamic ones starts cold and still matches its own golden."""
+    from generic_mobility_interface_class_gb300.solver import MobilitySolver
+    g = load_golden("prescribed_dynamic", prefix="")
+    nfil, nseg, nblob = int(g["nfil"]), int(g["nseg"]), int(g["nblob"])
+    s = MobilitySolver(nswim=1, nfil=nfil, nseg=nseg, nblob=nblob, mu=float(g["mu"]), rseg=float(g["rseg"]),
+                       rblob=float(g["rblob"]), linear_tol=float(g["linear_tol"]),
+                       max_linear_iter=int(g["max_linear_iter"]), precision=precision)
+    s.set_blob_references(g["blob_refs"])
+    s.set_generalised_force_refs(g["gen_force_refs"])
+    S = nfil * nseg
+    tol = SOLVE_TOL if precision == 0 else 1e-4
+    for k in range(len(g["gmres_iters"])):
+        s.x_segs_host[:] = g["x_segs"][k].reshape(S, 3)
+        it, speeds = s.compute_velocities_prescribed_dynamic(
+            g["vel_dir"][k].reshape(S, 3), g["phase"][k], g["omega0"][k], phase_speed=g["phase_speed"][k],
+            body_x=g["body_x"][k].reshape(1, 3), body_q=g["body_q"][k].reshape(1, 4))
+        assert rel_err(speeds, g["phase_speed_out"][k]) < tol, (k, speeds, g["phase_speed_out"][k])
+        want_fs = g["f_segs"][k].reshape(S, 6)[:, :3]
+        assert rel_err(np.array(s.f_segs_host[:, :3]), want_fs) < tol, k
+        assert np.all(np.array(s.f_segs_host[:, 3:]) == 0.0)
+        assert rel_err(np.array(s.f_blobs_host), g["f_blobs"][k].reshape(nblob, 3)) < tol, k
+        assert rel_err(s.v_bodies().ravel(), g["v_bodies"][k]) < tol, k
+        if precision == 0:
+            assert abs(it - int(g["gmres_iters"][k])) <= 3, (k, it, int(g["gmres_iters"][k]))
+    st = load_golden("prescribed", prefix="")
+    s.x_segs_host[:] = st["x_segs"][0].reshape(S, 3)
+    s.compute_velocities_prescribed(st["vel_dir"][0].reshape(S, 3), st["phase_speed"][0],
+                                    st["body_x"][0].reshape(1, 3), st["body_q"][0].reshape(1, 4))
+    assert rel_err(s.v_bodies().ravel(), st["v_bodies"][0]) < tol
+    s.close()
+
+
+def test_prescribed_dynamic_needs_a_table(gmi_lib):
+    from generic_mobility_interface_class_gb300._lib import GmiError
+    from generic_mobility_interface_class_gb300.solver import MobilitySolver
+    g = load_golden("prescribed_dynamic", prefix="")
+    nfil, nseg, nblob = int(g["nfil"]), int(g["nseg"]), int(g["nblob"])
+    s = MobilitySolver(nswim=1, nfil=nfil, nseg=nseg, nblob=nblob)
+    s.set_blob_references(g["blob_refs"])
+    S = nfil * nseg
+    s.x_segs_host[:] = g["x_segs"][0].reshape(S, 3)
+    args = (g["vel_dir"][0].reshape(S, 3), g["phase"][0], g["omega0"][0])
+    with pytest.raises(GmiError):
+        s.compute_velocities_prescribed_dynamic(*args)
+    with pytest.raises(GmiError):
+        s.set_generalised_force_refs([1.0])
+    with pytest.raises(GmiError):
+        s.set_generalised_force_refs([1.0, np.nan])
+    s.set_generalised_force_refs(g["gen_force_refs"])
+    s.set_generalised_force_refs([])
+    with pytest.raises(GmiError):
+        s.compute_velocities_prescribed_dynamic(*args)
+    s.close()
+
+
 def test_prescribed_rejects_the_wall(gmi_lib):
     from generic_mobility_interface_class_gb300._lib import GmiError
     from generic_mobility_interface_class_gb300.solver import MobilitySolver
