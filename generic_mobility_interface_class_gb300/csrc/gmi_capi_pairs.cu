@@ -57,6 +57,7 @@ gmi_status gmi_context_destroy(gmi_context *ctx)
     ctx->rec_src.release();
     ctx->rec_tgt.release();
     ctx->partial.release();
+    ctx->cells.release();
     if (ctx->d_err) gmi::dev_free(ctx->d_err);
     if (ctx->h_err) gmi::host_free(ctx->h_err);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);

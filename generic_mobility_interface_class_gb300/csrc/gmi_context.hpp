@@ -46,6 +46,7 @@ struct gmi_context {
     unsigned *h_err = nullptr;       // pinned mirror for the synchronising read
     long long launches = 0;          // kernels this context has launched
     gmi::DeviceBuffer rec_src, rec_tgt, partial;
+    gmi::DeviceBuffer cells;  // the barrier's cell list
     std::map<gmi::TuneKey, gmi::PairShape> tuned;
     int last_splits = 1;  // source splits of the last tiled pair launch (the autotuner reads it)
     void *encode_tiled = nullptr;    // cuTensorMapEncodeTiled from the driver

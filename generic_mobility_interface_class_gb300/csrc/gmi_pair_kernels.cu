@@ -17,6 +17,7 @@
 //      and a reduce kernel adds them in split order into the output (= or +=).
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <type_traits>
 #include <vector>
 
@@ -982,6 +983,325 @@ __global__ void barrier_reduce(BarrierLaunch a, int splits)
 }
 
 // ---------------------------------------------------------------------------
+// Barrier forces through a hashed cell list.
+//
+// The barrier force is short-ranged: a pair contributes only inside
+// 1.1 (a_i + a_j) (cuda_functions.cu:1031-1046, 1121-1135).  With cells at
+// least as wide as the widest screen cutoff, a target's candidates lie in
+// the 27 cells around its own.  Cell (cx, cy, cz) of a particle's FP32 screen
+// position hashes to one of T = 2^k buckets, and a counting sort (count,
+// bucket offsets, scatter) lists each bucket's particles.  Each target
+// screens the particles of its 27 buckets exactly as barrier_kernel does
+// (the same FP32 test and exclusions), keeps its candidates in shared
+// memory, sorts them by index, drops repeats (two of its cells can share a
+// bucket), and adds their FP64 forces in ascending j in one accumulator: the
+// reference's per-target order, so each force is the reference's bit for
+// bit.  A target with more than kCellCand candidates goes to an overflow
+// list, which a warp-per-target all-pairs kernel finishes in the same order.
+// ---------------------------------------------------------------------------
+constexpr int kCellTpb = 128;
+constexpr int kCellCand = 40;          // candidates per target kept in shared memory
+constexpr int kCellScanTpb = 1024;
+constexpr int kCellScanTile = 4 * kCellScanTpb;  // buckets per CTA of the offset scan
+constexpr int kCellMinParticles = 8192;          // fewer particles: the all-pairs kernel
+
+struct CellList {
+    int T;              // buckets (a power of two, a multiple of kCellScanTile)
+    float cut_max;      // widest FP32 screen cutoff before the rounding margin
+    const unsigned *extent;
+    int *count;         // [T] particles per bucket (counted down again by the scatter)
+    int *local;         // [T] exclusive scan of count within its scan tile
+    int *tile_prefix;   // [T / kCellScanTile] particles before each scan tile
+    int *order;         // [N] particles by bucket
+    int *key;           // [N] each particle's bucket
+    int *overflow;      // [1 + targets]: count, then the overflowed targets (launch-local indices)
+    int *ticket;        // [1] the scan's last-CTA ticket (zero between launches)
+};
+
+// cell width: the widest screen cutoff plus the rounding margin of the
+// screen (as barrier_kernel) with 1 % to spare, so that any pair the screen
+// can accept lies in adjacent cells whatever the rounding of x / h
+__device__ __forceinline__ float cell_inv_width(const CellList &c)
+{
+    const float margin = 1.0e-6f * __uint_as_float(*c.extent);
+    return 1.0f / ((c.cut_max + margin) * 1.01f);
+}
+__device__ __forceinline__ int cell_coord(float x, float inv_h) { return (int)floorf(x * inv_h); }
+__device__ __forceinline__ int cell_bucket(int cx, int cy, int cz, int T)
+{
+    const unsigned h = ((unsigned)cx * 73856093u) ^ ((unsigned)cy * 19349663u) ^ ((unsigned)cz * 83492791u);
+    return (int)(h & (unsigned)(T - 1));
+}
+__device__ __forceinline__ int cell_offset(const CellList &c, int b)
+{
+    return __ldcg(c.local + b) + __ldcg(c.tile_prefix + b / kCellScanTile);
+}
+
+__global__ void cell_keys_kernel(CellList c, const float4 *__restrict__ screen, int N)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const float inv_h = cell_inv_width(c);
+    const float4 p = screen[i];
+    const int b = cell_bucket(cell_coord(p.x, inv_h), cell_coord(p.y, inv_h), cell_coord(p.z, inv_h), c.T);
+    c.key[i] = b;
+    atomicAdd(c.count + b, 1);
+}
+
+// Exclusive scan of the bucket counts: each CTA scans one tile of
+// kCellScanTile buckets (four per thread) into local[] and writes its total;
+// the last CTA to finish scans the totals into tile_prefix[].
+__global__ void __launch_bounds__(kCellScanTpb) cell_scan_kernel(CellList c)
+{
+    __shared__ int warp_tot[kCellScanTpb / 32];
+    __shared__ int is_last;
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    const int base = blockIdx.x * kCellScanTile + 4 * t;
+    const int4 v = *reinterpret_cast<const int4 *>(c.count + base);
+    const int own = v.x + v.y + v.z + v.w;
+    int incl = own;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        int w = warp_tot[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        warp_tot[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const int before = incl - own + (wid > 0 ? warp_tot[wid - 1] : 0);
+    int4 e;
+    e.x = before;
+    e.y = before + v.x;
+    e.z = e.y + v.y;
+    e.w = e.z + v.z;
+    *reinterpret_cast<int4 *>(c.local + base) = e;
+    if (t == kCellScanTpb - 1) {
+        c.tile_prefix[blockIdx.x] = before + own;  // the tile's total, scanned below
+        __threadfence();
+        is_last = atomicAdd(c.ticket, 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    // the last CTA: exclusive scan of the gridDim.x (<= kCellScanTpb) tile totals
+    const int n = gridDim.x;
+    const int tot = t < n ? __ldcg(c.tile_prefix + t) : 0;
+    int x = tot;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) warp_tot[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int w = warp_tot[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        warp_tot[lane] = w;
+    }
+    __syncthreads();
+    if (t < n) c.tile_prefix[t] = x - tot + (wid > 0 ? warp_tot[wid - 1] : 0);
+    if (t == 0) *c.ticket = 0;
+}
+
+__global__ void cell_scatter_kernel(CellList c, int N)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int b = c.key[i];
+    const int slot = atomicSub(c.count + b, 1) - 1;
+    c.order[cell_offset(c, b) + slot] = i;
+}
+
+// The FP64 force of one accepted pair, as barrier_flush: zero outside the
+// exact cutoff.
+__device__ __forceinline__ void barrier_pair(const BarrierLaunch &a, int j, double xi, double yi, double zi,
+                                             double a_tgt, double &g0, double &g1, double &g2)
+{
+    const bool src_seg = j < a.S;
+    const double asum = a_tgt + (src_seg ? a.rseg : a.rblob);
+    const double *pj = src_seg ? a.xs + 3 * (size_t)j : a.xb + 3 * (size_t)(j - a.S);
+    const double ddx = xi - pj[0], ddy = yi - pj[1], ddz = zi - pj[2];
+    const double dist = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+    if (dist < 1.1 * asum) {
+        double cc = fmin(1.0, 1.0 - (10.0 / asum) * (dist - asum));
+        cc = a.scale * cc * cc * cc * cc;
+        const double idist = 1.0 / dist;
+        g0 += cc * ddx * idist;
+        g1 += cc * ddy * idist;
+        g2 += cc * ddz * idist;
+    }
+}
+
+// a target's launch-local index -> its global particle index, position and
+// the store of its force (segment targets add, blob targets overwrite)
+struct BarrierTarget {
+    int gi;
+    bool seg;
+    double x, y, z;
+};
+__device__ __forceinline__ BarrierTarget barrier_target(const BarrierLaunch &a, int local)
+{
+    BarrierTarget t;
+    t.seg = local < a.num_segs;
+    t.gi = t.seg ? a.start_seg + local : a.S + a.start_blob + (local - a.num_segs);
+    const double *p = t.seg ? a.xs + 3 * (size_t)t.gi : a.xb + 3 * (size_t)(t.gi - a.S);
+    t.x = p[0];
+    t.y = p[1];
+    t.z = p[2];
+    return t;
+}
+__device__ __forceinline__ double barrier_wall_z(const BarrierLaunch &a, const BarrierTarget &t)
+{
+    const double DL = 2.2 * a.rseg;
+    if (!(t.seg && a.wall && t.z < 0.5 * DL)) return 0.0;
+    const double fz = fmin(1.0, 1.0 - (t.z - a.rseg) / (0.5 * DL - a.rseg));
+    return a.scale * fz * fz * fz * fz;
+}
+__device__ __forceinline__ void barrier_store(const BarrierLaunch &a, const BarrierTarget &t, int local, double g0,
+                                              double g1, double g2)
+{
+    if (t.seg) {
+        double *f = a.f_segs + 6 * (size_t)t.gi;
+        f[0] += g0;
+        f[1] += g1;
+        f[2] += g2;
+    } else {
+        double *f = a.f_blobs_rep + 3 * (size_t)(local - a.num_segs);
+        f[0] = g0;
+        f[1] = g1;
+        f[2] = g2;
+    }
+}
+// the screen and exclusions of barrier_kernel for target t (screen position
+// pf, squared cutoffs c2_s / c2_b against segment / blob sources) and source j
+__device__ __forceinline__ bool barrier_candidate(const BarrierLaunch &a, const BarrierTarget &t, float4 pf,
+                                                  float c2_s, float c2_b, int j, float4 s)
+{
+    const float dx = pf.x - s.x, dy = pf.y - s.y, dz = pf.z - s.z;
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (!(d2 < (j < a.S ? c2_s : c2_b))) return false;
+    if (t.seg) {
+        const int di = t.gi - j;
+        return !((t.gi / a.nseg == j / a.nseg) && (di <= 1 && di >= -1));
+    }
+    return j != t.gi;
+}
+__device__ __forceinline__ void barrier_cutoffs(const BarrierLaunch &a, bool seg, float &c2_s, float &c2_b)
+{
+    const float margin = 1.0e-6f * __uint_as_float(*a.extent);
+    const float cs = (seg ? a.cut_ss : a.cut_sb) + margin;
+    const float cb = (seg ? a.cut_sb : a.cut_bb) + margin;
+    c2_s = cs * cs;
+    c2_b = cb * cb;
+}
+
+__global__ void __launch_bounds__(kCellTpb) barrier_cell_kernel(BarrierLaunch a, CellList c)
+{
+    __shared__ int cand[kCellCand * kCellTpb];  // candidate e of thread t at [e * kCellTpb + t]
+    const int ntg = a.num_segs + (a.wall ? 0 : a.num_blobs);
+    const int local = blockIdx.x * blockDim.x + threadIdx.x;
+    if (local >= ntg) return;
+    const int N = a.S + a.B;
+    const BarrierTarget t = barrier_target(a, local);
+    const float4 pf = a.screen[t.gi];
+    float c2_s, c2_b;
+    barrier_cutoffs(a, t.seg, c2_s, c2_b);
+    const float inv_h = cell_inv_width(c);
+    const int cx = cell_coord(pf.x, inv_h), cy = cell_coord(pf.y, inv_h), cz = cell_coord(pf.z, inv_h);
+    int n = 0;
+    bool over = false;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int b = cell_bucket(cx + dx, cy + dy, cz + dz, c.T);
+                const int beg = cell_offset(c, b), end = b + 1 < c.T ? cell_offset(c, b + 1) : N;
+                for (int p = beg; p < end; ++p) {
+                    const int j = __ldcg(c.order + p);
+                    if (!barrier_candidate(a, t, pf, c2_s, c2_b, j, a.screen[j])) continue;
+                    if (n < kCellCand)
+                        cand[n * kCellTpb + threadIdx.x] = j;
+                    else
+                        over = true;
+                    ++n;
+                }
+            }
+    if (over) {
+        const int pos = atomicAdd(c.overflow, 1);
+        c.overflow[1 + pos] = local;
+        return;
+    }
+    // ascending j (insertion sort of a handful), repeats dropped below
+    for (int e = 1; e < n; ++e) {
+        const int v = cand[e * kCellTpb + threadIdx.x];
+        int f = e - 1;
+        while (f >= 0 && cand[f * kCellTpb + threadIdx.x] > v) {
+            cand[(f + 1) * kCellTpb + threadIdx.x] = cand[f * kCellTpb + threadIdx.x];
+            --f;
+        }
+        cand[(f + 1) * kCellTpb + threadIdx.x] = v;
+    }
+    const double a_tgt = t.seg ? a.rseg : a.rblob;
+    double g0 = 0.0, g1 = 0.0, g2 = barrier_wall_z(a, t);
+    int prev = -1;
+    for (int e = 0; e < n; ++e) {
+        const int j = cand[e * kCellTpb + threadIdx.x];
+        if (j == prev) continue;
+        prev = j;
+        barrier_pair(a, j, t.x, t.y, t.z, a_tgt, g0, g1, g2);
+    }
+    barrier_store(a, t, local, g0, g1, g2);
+}
+
+// Targets with more candidates than the cell kernel keeps: one warp each,
+// all sources screened 32 at a time and the accepted ones added in
+// ascending j by lane 0 (the lanes evaluate their own source's force).
+__global__ void __launch_bounds__(128) barrier_overflow_kernel(BarrierLaunch a, CellList c)
+{
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (blockDim.x >> 5);
+    const int N = a.S + a.B;
+    const int todo = __ldcg(c.overflow);
+    for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < todo; w += warps) {
+        const int local = __ldcg(c.overflow + 1 + w);
+        const BarrierTarget t = barrier_target(a, local);
+        const float4 pf = a.screen[t.gi];
+        float c2_s, c2_b;
+        barrier_cutoffs(a, t.seg, c2_s, c2_b);
+        const double a_tgt = t.seg ? a.rseg : a.rblob;
+        double g0 = 0.0, g1 = 0.0, g2 = barrier_wall_z(a, t);
+        for (int j0 = 0; j0 < N; j0 += 32) {
+            const int j = j0 + lane;
+            const bool cand = j < N && barrier_candidate(a, t, pf, c2_s, c2_b, j, a.screen[j]);
+            unsigned mask = __ballot_sync(0xffffffffu, cand);
+            double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+            if (cand) barrier_pair(a, j, t.x, t.y, t.z, a_tgt, v0, v1, v2);
+            while (mask) {
+                const int src = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const double u0 = __shfl_sync(0xffffffffu, v0, src);
+                const double u1 = __shfl_sync(0xffffffffu, v1, src);
+                const double u2 = __shfl_sync(0xffffffffu, v2, src);
+                g0 += u0;
+                g1 += u1;
+                g2 += u2;
+            }
+        }
+        if (lane == 0) barrier_store(a, t, local, g0, g1, g2);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 void fill_consts(PairConsts &c, double a_eq, double as, double ab, double mu)
@@ -1437,8 +1757,44 @@ gmi_status launch_barrier(gmi_context *ctx, const BarrierLaunch &in)
     }
     GMI_CUDA_TRY(cudaMemsetAsync(a.extent, 0, sizeof(unsigned), ctx->stream));
     pack_screen_positions<<<(N + 255) / 256, 256, 0, ctx->stream>>>(a.xs, a.S, a.xb, a.B, a.screen, a.extent);
+    ctx->launches++;
+    // the cell list from kCellMinParticles particles (GMI_BARRIER_CELLS=0
+    // never, =1 always), up to the scan's 4 M buckets
+    const char *cells_env = std::getenv("GMI_BARRIER_CELLS");
+    const bool cells = cells_env ? cells_env[0] != '0' : N >= kCellMinParticles;
+    int T = kCellScanTile;
+    while (T < 2 * N) T *= 2;
+    if (cells && T / kCellScanTile <= kCellScanTpb) {
+        a.partial = nullptr;
+        const size_t tiles = (size_t)T / kCellScanTile;
+        const size_t ints = 4 + 2 * (size_t)T + ((tiles + 3) & ~(size_t)3) + 2 * (size_t)N + 1 + (size_t)ntg;
+        st = ctx->cells.reserve(ints * sizeof(int));
+        if (st != GMI_OK) return st;
+        CellList c{};
+        int *base = static_cast<int *>(ctx->cells.ptr);
+        c.T = T;
+        c.cut_max = std::max(a.cut_ss, std::max(a.cut_sb, a.cut_bb));
+        c.extent = a.extent;
+        c.ticket = base;
+        c.count = base + 4;
+        c.local = c.count + T;
+        c.tile_prefix = c.local + T;
+        c.key = c.tile_prefix + ((tiles + 3) & ~(size_t)3);
+        c.order = c.key + N;
+        c.overflow = c.order + N;
+        GMI_CUDA_TRY(cudaMemsetAsync(base, 0, (4 + (size_t)T) * sizeof(int), ctx->stream));
+        GMI_CUDA_TRY(cudaMemsetAsync(c.overflow, 0, sizeof(int), ctx->stream));
+        cell_keys_kernel<<<(N + 255) / 256, 256, 0, ctx->stream>>>(c, a.screen, N);
+        cell_scan_kernel<<<(unsigned)tiles, kCellScanTpb, 0, ctx->stream>>>(c);
+        cell_scatter_kernel<<<(N + 255) / 256, 256, 0, ctx->stream>>>(c, N);
+        barrier_cell_kernel<<<(ntg + kCellTpb - 1) / kCellTpb, kCellTpb, 0, ctx->stream>>>(a, c);
+        barrier_overflow_kernel<<<ctx->sm_count, 128, 0, ctx->stream>>>(a, c);
+        ctx->launches += 5;
+        GMI_CUDA_TRY(cudaGetLastError());
+        return GMI_OK;
+    }
     barrier_kernel<<<dim3(tgt_ctas, splits), kBarrierTpb, 0, ctx->stream>>>(a);
-    ctx->launches += 2;
+    ctx->launches++;
     if (splits > 1) {
         barrier_reduce<<<(3 * ntg + 255) / 256, 256, 0, ctx->stream>>>(a, splits);
         ctx->launches++;

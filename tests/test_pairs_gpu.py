@@ -73,6 +73,84 @@ def test_wall_matches_golden(case, prec_ctx):
     assert rel_err(N(fs), g["fs_barrier"]) < 1e-14
 
 
+def _swimmer_cloud(nblob, nfil, nseg, R, seed):
+    """Blobs on a Fibonacci sphere of radius R and nfil filaments of nseg
+    segments (spacing 2.2) standing out of it in random directions, jittered
+    so that segments of nearby filaments and base segments and blobs come
+    within the barrier's reach."""
+    rng = np.random.default_rng(seed)
+    k = np.arange(nblob) + 0.5
+    polar, az = np.arccos(1 - 2 * k / nblob), np.pi * (1 + 5 ** 0.5) * k
+    xb = R * np.stack([np.cos(az) * np.sin(polar), np.sin(az) * np.sin(polar), np.cos(polar)], 1)
+    d = rng.normal(size=(nfil, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = R + 1.1 + 2.2 * np.arange(nseg)
+    xs = (d[:, None, :] * r[None, :, None] + 0.3 * rng.normal(size=(nfil, nseg, 3))).reshape(-1, 3)
+    return xs, xb
+
+
+@pytest.mark.parametrize("cells", ["1", "0"], ids=["cell_list", "all_pairs"])
+def test_barrier_swimmer_against_oracle(gpu_ctx, oracle_built, monkeypatch, cells):
+    """The barrier at the config-3 shape (4096 blobs, 640 x 20 segments), by
+    the cell list and by the all-pairs kernel, against the oracle (which adds
+    each target's pairs in ascending source order, as the reference)."""
+    rpy = oracle_built
+    monkeypatch.setenv("GMI_BARRIER_CELLS", cells)
+    xs, xb = _swimmer_cloud(4096, 640, 20, 40.0, seed=3)
+    fs = np.random.default_rng(4).normal(size=(len(xs), 6))
+    want_s, want_b = rpy.barrier(xs, xb, fs, 20, 1.0, 1.0, 2.5)
+    assert np.count_nonzero(np.abs(want_s - fs).sum(1)) > 100 and np.count_nonzero(want_b.any(1)) > 100
+    got = T(fs)
+    fb = gpu_ctx.barrier(T(xs), T(xb), got, 20, 1.0, 1.0, 2.5)
+    gpu_ctx.synchronize()
+    assert rel_err(N(got), want_s) < 1e-14
+    assert rel_err(N(fb), want_b) < 1e-14
+
+
+def test_barrier_cell_overflow_against_oracle(gpu_ctx, oracle_built, monkeypatch):
+    """A cluster of 64 blobs inside a unit ball: each of them has more
+    candidates than the cell kernel keeps, so the overflow kernel finishes
+    them; the rest take the cell list."""
+    rpy = oracle_built
+    monkeypatch.setenv("GMI_BARRIER_CELLS", "1")
+    rng = np.random.default_rng(9)
+    xs, xb = _swimmer_cloud(2048, 100, 20, 25.0, seed=8)
+    ball = rng.normal(size=(64, 3))
+    ball *= (rng.uniform(size=(64, 1)) ** (1 / 3)) / np.linalg.norm(ball, axis=1, keepdims=True)
+    xb = np.concatenate([xb, ball + np.array([0.0, 0.0, 60.0])])
+    fs = rng.normal(size=(len(xs), 6))
+    want_s, want_b = rpy.barrier(xs, xb, fs, 20, 1.0, 1.0, 1.5)
+    got = T(fs)
+    fb = gpu_ctx.barrier(T(xs), T(xb), got, 20, 1.0, 1.0, 1.5)
+    gpu_ctx.synchronize()
+    assert rel_err(N(got), want_s) < 1e-14
+    assert rel_err(N(fb), want_b) < 1e-14
+    assert np.abs(want_b[-64:]).max() > 0
+
+
+@pytest.mark.parametrize("case", WALL)
+def test_wall_barrier_cell_list(case, gpu_ctx, monkeypatch):
+    monkeypatch.setenv("GMI_BARRIER_CELLS", "1")
+    g = load_golden(case)
+    fs = T(g["fs"])
+    gpu_ctx.barrier(T(g["xs"]), torch.zeros((0, 3), dtype=torch.float64, device="cuda"), fs, int(g["nseg"]),
+                    1.0, 1.0, float(g["force_scale"]), wall=True)
+    gpu_ctx.synchronize()
+    assert rel_err(N(fs), g["fs_barrier"]) < 1e-14
+
+
+@pytest.mark.parametrize("case", FREE)
+def test_barrier_cell_list_matches_golden(case, gpu_ctx, monkeypatch):
+    monkeypatch.setenv("GMI_BARRIER_CELLS", "1")
+    g = load_golden(case)
+    fs = T(g["fs"])
+    fb = gpu_ctx.barrier(T(g["xs"]), T(g["xb"]), fs, int(g["nseg"]), float(g["rseg"]), float(g["rblob"]),
+                         float(g["force_scale"]))
+    gpu_ctx.synchronize()
+    assert rel_err(N(fs), g["fs_barrier"]) < 1e-14
+    assert rel_err(N(fb), g["fb_repulsion"]) < 1e-14
+
+
 def test_larger_against_oracle(prec_ctx, oracle_built):
     """Thousands of particles (the warp-per-target kernel, at most 4096
     sources); random cube with rejection (config-2 shape)."""
