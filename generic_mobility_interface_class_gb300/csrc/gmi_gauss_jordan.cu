@@ -29,7 +29,11 @@
 // Two kernels share that step: one CTA per matrix (many filaments), and one
 // thread-block cluster per matrix with the columns sliced over the CTAs and
 // the published pivot column read through distributed shared memory (few
-// filaments, where one CTA per matrix would leave most SMs idle).
+// filaments, where one CTA per matrix would leave most SMs idle).  Both are
+// templates on the element type: FP64 for the reference's arithmetic, FP32
+// for the mixed-precision time step, whose approximate inverse only starts
+// the Broyden iteration (on the FMA pipe a step is latency-bound, not
+// FP64-bound).
 #include <cooperative_groups.h>
 
 #include "gmi_context.hpp"
@@ -48,13 +52,22 @@ constexpr int kGcWarps = kGcTpb / 32;
 // Writes the step's multiplier column ncol[i] = -A'(i, c) / pivot, A' the
 // column with rows c and p swapped, 1/pivot to *pinv and p to *piv (-1 when
 // the column is zero there).
-static __device__ void gj_pivot_warp(const double *Ac, int n, int c, double *ncol, double *pinv, int *piv,
-                                     int lane)
+// |x| as an unsigned integer that orders finite values like fabs does
+__device__ __forceinline__ unsigned long long gj_mag(double x)
+{
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ unsigned long long gj_mag(float x) { return __float_as_uint(x) & 0x7fffffffu; }
+__device__ __forceinline__ double gj_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float gj_fma(float a, float b, float c) { return fmaf(a, b, c); }
+
+template <typename T>
+static __device__ void gj_pivot_warp(const T *Ac, int n, int c, T *ncol, T *pinv, int *piv, int lane)
 {
     unsigned long long best = 0ull;
     int bi = c;
     for (int i = c + lane; i < n; i += 32) {
-        const unsigned long long m = (unsigned long long)__double_as_longlong(Ac[i]) & 0x7fffffffffffffffull;
+        const unsigned long long m = gj_mag(Ac[i]);
         if (m > best) {
             best = m;
             bi = i;
@@ -72,7 +85,7 @@ static __device__ void gj_pivot_warp(const double *Ac, int n, int c, double *nco
         if (lane == 0) *piv = -1;
         return;
     }
-    const double pivinv = 1.0 / Ac[bi];
+    const T pivinv = T(1) / Ac[bi];
     for (int i = lane; i < n; i += 32) {
         const int src = (i == c) ? bi : ((i == bi) ? c : i);
         ncol[i] = -(Ac[src] * pivinv);
@@ -91,17 +104,17 @@ template <int RPL> struct GjColsPerPass {
     static constexpr int value = RPL >= 8 ? 2 : 4;
 };
 
-template <int RPL, int C = GjColsPerPass<RPL>::value>
-static __device__ __forceinline__ void gj_cols(double *A, int n, int j0, const int (&jl)[C], int cnt, int k, int p,
-                                               double pivinv, const double (&ncr)[RPL], int lane)
+template <typename T, int RPL, int C = GjColsPerPass<RPL>::value>
+static __device__ __forceinline__ void gj_cols(T *A, int n, int j0, const int (&jl)[C], int cnt, int k, int p,
+                                               T pivinv, const T (&ncr)[RPL], int lane)
 {
-    double v[C][RPL];
+    T v[C][RPL];
 #pragma unroll
     for (int c = 0; c < C; ++c)
 #pragma unroll
         for (int t = 0; t < RPL; ++t) {
             const int i = lane + 32 * t;
-            v[c][t] = (c < cnt && i < n) ? A[(size_t)n * jl[c] + i] : 0.0;
+            v[c][t] = (c < cnt && i < n) ? A[(size_t)n * jl[c] + i] : T(0);
         }
     const int pq = p >> 5, pl = p & 31, kq = k >> 5, kl = k & 31;
 #pragma unroll
@@ -115,19 +128,19 @@ static __device__ __forceinline__ void gj_cols(double *A, int n, int j0, const i
             }
             continue;
         }
-        double sp = v[c][0], sk = v[c][0];
+        T sp = v[c][0], sk = v[c][0];
 #pragma unroll
         for (int t = 1; t < RPL; ++t) {
             if (pq == t) sp = v[c][t];
             if (kq == t) sk = v[c][t];
         }
-        const double akj = __shfl_sync(0xffffffffu, sp, pl);  // row p, swapped into row k
-        const double apj = __shfl_sync(0xffffffffu, sk, kl);  // row k, swapped into row p
+        const T akj = __shfl_sync(0xffffffffu, sp, pl);  // row p, swapped into row k
+        const T apj = __shfl_sync(0xffffffffu, sk, kl);  // row k, swapped into row p
 #pragma unroll
         for (int t = 0; t < RPL; ++t) {
             const int i = lane + 32 * t;
-            const double a = (i == k) ? 0.0 : ((i == p) ? apj : v[c][t]);
-            v[c][t] = fma(akj, (i == k) ? pivinv : ncr[t], a);
+            const T a = (i == k) ? T(0) : ((i == p) ? apj : v[c][t]);
+            v[c][t] = gj_fma(akj, (i == k) ? pivinv : ncr[t], a);
         }
     }
 #pragma unroll
@@ -144,61 +157,60 @@ static __device__ __forceinline__ void gj_cols(double *A, int n, int j0, const i
 // eliminates it first and then searches it for the next pivot.  RPL > 0:
 // rows in registers (n <= 32 RPL), several columns at a time; RPL == 0: any
 // n, one column at a time through shared memory.
-template <int RPL, int NW>
-static __device__ __forceinline__ void gj_step(double *A, int n, int ncl, int j0, int k, int p, double pivinv,
-                                               const double *nc, double *next_ncol, double *next_pinv,
-                                               int *next_piv, int wid, int lane)
+template <typename T, int RPL, int NW>
+static __device__ __forceinline__ void gj_step(T *A, int n, int ncl, int j0, int k, int p, T pivinv, const T *nc,
+                                               T *next_ncol, T *next_pinv, int *next_piv, int wid, int lane)
 {
     const int la = k + 1 - j0;
-    const int T = (ncl > wid) ? (ncl - wid + NW - 1) / NW : 0;
+    const int nt = (ncl > wid) ? (ncl - wid + NW - 1) / NW : 0;
     const bool own_la = k + 1 < n && la >= 0 && la < ncl && la % NW == wid;
     if constexpr (RPL > 0) {
-        double ncr[RPL];
+        T ncr[RPL];
 #pragma unroll
         for (int t = 0; t < RPL; ++t) {
             const int i = lane + 32 * t;
-            ncr[t] = i < n ? nc[i] : 0.0;
+            ncr[t] = i < n ? nc[i] : T(0);
         }
         constexpr int C = GjColsPerPass<RPL>::value;
         int jj[C] = {};
         if (own_la) {
             jj[0] = la;
-            gj_cols<RPL>(A, n, j0, jj, 1, k, p, pivinv, ncr, lane);
+            gj_cols<T, RPL>(A, n, j0, jj, 1, k, p, pivinv, ncr, lane);
             __syncwarp();
             gj_pivot_warp(A + (size_t)n * la, n, k + 1, next_ncol, next_pinv, next_piv, lane);
         }
         int t = 0;
-        while (t < T) {
+        while (t < nt) {
             // the next columns in slots 0 .. cnt-1 (a slot is empty only
             // once the warp's columns have run out)
             int cnt = 0;
 #pragma unroll
             for (int c = 0; c < C; ++c) {
                 int jl = -1;
-                while (jl < 0 && t < T) {
+                while (jl < 0 && t < nt) {
                     const int cand = wid + NW * t++;
                     if (!(own_la && cand == la)) jl = cand;
                 }
                 jj[c] = jl < 0 ? 0 : jl;
                 cnt += jl >= 0 ? 1 : 0;
             }
-            if (cnt > 0) gj_cols<RPL>(A, n, j0, jj, cnt, k, p, pivinv, ncr, lane);
+            if (cnt > 0) gj_cols<T, RPL>(A, n, j0, jj, cnt, k, p, pivinv, ncr, lane);
         }
     } else {
         const int t0 = own_la ? la / NW : 0;
-        for (int tt = 0; tt < T; ++tt) {
-            const int t = (tt + t0 < T) ? tt + t0 : tt + t0 - T;
+        for (int tt = 0; tt < nt; ++tt) {
+            const int t = (tt + t0 < nt) ? tt + t0 : tt + t0 - nt;
             const int jl = wid + NW * t;
-            double *Aj = A + (size_t)n * jl;
+            T *Aj = A + (size_t)n * jl;
             if (j0 + jl == k) {
                 for (int i = lane; i < n; i += 32) Aj[i] = (i == k) ? pivinv : nc[i];
             } else {
-                const double akj = Aj[p], apj = Aj[k];  // rows p and k, swapped
+                const T akj = Aj[p], apj = Aj[k];  // rows p and k, swapped
                 __syncwarp();
 #pragma unroll 4
                 for (int i = lane; i < n; i += 32) {
-                    const double a = (i == k) ? 0.0 : ((i == p) ? apj : Aj[i]);
-                    Aj[i] = fma(akj, (i == k) ? pivinv : nc[i], a);
+                    const T a = (i == k) ? T(0) : ((i == p) ? apj : Aj[i]);
+                    Aj[i] = gj_fma(akj, (i == k) ? pivinv : nc[i], a);
                 }
             }
             if (jl == la && own_la) {
@@ -226,15 +238,15 @@ static __device__ void gj_unpivot_map(const int *perm, int n, int *where)
 
 // one CTA per matrix; the matrix in shared memory when use_smem, else
 // worked on in place in global memory
-template <int RPL>
-__global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, int use_smem, int *flags)
+template <typename T, int RPL>
+__global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(T *mats, int n, int use_smem, int *flags)
 {
     extern __shared__ __align__(16) double sh[];
-    double *Mg = mats + (size_t)blockIdx.x * n * n;
-    double *ncol = sh;                                // [2][n], by step parity
-    double *pinv = ncol + 2 * (size_t)n;              // [2]
+    T *Mg = mats + (size_t)blockIdx.x * n * n;
+    T *ncol = reinterpret_cast<T *>(sh);              // [2][n], by step parity
+    T *pinv = ncol + 2 * (size_t)n;                   // [2]
     int *perm = reinterpret_cast<int *>(pinv + 2);    // [n]
-    double *A = use_smem ? reinterpret_cast<double *>(perm + ((n + 1) & ~1)) : Mg;
+    T *A = use_smem ? reinterpret_cast<T *>(perm + ((n + 1) & ~1)) : Mg;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     if (use_smem)
         for (int e = tid; e < n * n; e += kGjTpb) A[e] = Mg[e];
@@ -247,8 +259,8 @@ __global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, 
             if (tid == 0) atomicOr(flags + 2, 1);
             return;
         }
-        gj_step<RPL, kGjWarps>(A, n, n, 0, k, p, pinv[par], ncol + par * (size_t)n, ncol + (par ^ 1) * (size_t)n,
-                pinv + (par ^ 1), perm + k + 1, wid, lane);
+        gj_step<T, RPL, kGjWarps>(A, n, n, 0, k, p, pinv[par], ncol + par * (size_t)n,
+                                  ncol + (par ^ 1) * (size_t)n, pinv + (par ^ 1), perm + k + 1, wid, lane);
         __syncthreads();
     }
     if (use_smem) {
@@ -262,7 +274,7 @@ __global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, 
             const int q = perm[k];
             if (q != k)
                 for (int i = tid; i < n; i += kGjTpb) {
-                    const double t = A[i + (size_t)n * k];
+                    const T t = A[i + (size_t)n * k];
                     A[i + (size_t)n * k] = A[i + (size_t)n * q];
                     A[i + (size_t)n * q] = t;
                 }
@@ -276,20 +288,20 @@ __global__ void __launch_bounds__(kGjTpb) gj_invert_kernel(double *mats, int n, 
 // multiplier column, pivot row and 1/pivot from the owner of column k (who
 // found them during the previous step) and runs the step on its columns.
 // The inverse is gathered at the end straight from the CTAs' shared memory.
-template <int RPL>
-__global__ void __launch_bounds__(kGcTpb) gj_cluster_kernel(double *mats, int n, int nc, int *flags)
+template <typename T, int RPL>
+__global__ void __launch_bounds__(kGcTpb) gj_cluster_kernel(T *mats, int n, int nc, int *flags)
 {
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), r = (int)cl.block_rank(), tid = threadIdx.x;
     const int lane = tid & 31, wid = tid >> 5;
-    double *Mg = mats + (size_t)(blockIdx.x / C) * n * n;
+    T *Mg = mats + (size_t)(blockIdx.x / C) * n * n;
     const int j0 = r * nc, ncl = max(0, min(n, j0 + nc) - j0);
     extern __shared__ __align__(16) double sh[];
-    double *A = sh;                                   // [nc][n]
-    double *ncol = A + (size_t)n * nc;                // [2][n]: published by the pivot column's owner
-    double *cur = ncol + 2 * (size_t)n;               // [n]: this step's copy
-    double *pinv = cur + n;                           // [2], published
-    double *pv = pinv + 2;                            // [2]: this step's copy of 1/pivot
+    T *A = reinterpret_cast<T *>(sh);                 // [nc][n]
+    T *ncol = A + (size_t)n * nc;                     // [2][n]: published by the pivot column's owner
+    T *cur = ncol + 2 * (size_t)n;                    // [n]: this step's copy
+    T *pinv = cur + n;                                // [2], published
+    T *pv = pinv + 2;                                 // [2]: this step's copy of 1/pivot
     int *piv = reinterpret_cast<int *>(pv + 2);       // [2], published
     int *pk = piv + 2;                                // [2]: this step's pivot row
     int *perm = pk + 2;                               // [n]
@@ -300,7 +312,7 @@ __global__ void __launch_bounds__(kGcTpb) gj_cluster_kernel(double *mats, int n,
     for (int k = 0; k < n; ++k) {
         const int owner = k / nc, par = k & 1;
         cl.sync();  // step k's pivot is published, and step k - 1 is done everywhere
-        const double *src = cl.map_shared_rank(ncol, owner) + par * (size_t)n;
+        const T *src = cl.map_shared_rank(ncol, owner) + par * (size_t)n;
         for (int i = tid; i < n; i += kGcTpb) cur[i] = src[i];
         if (tid == 0) {
             pk[0] = cl.map_shared_rank(piv, owner)[par];
@@ -313,8 +325,8 @@ __global__ void __launch_bounds__(kGcTpb) gj_cluster_kernel(double *mats, int n,
             singular = true;
             break;
         }
-        gj_step<RPL, kGcWarps>(A, n, ncl, j0, k, p, pv[0], cur, ncol + (par ^ 1) * (size_t)n, pinv + (par ^ 1),
-                               piv + (par ^ 1), wid, lane);
+        gj_step<T, RPL, kGcWarps>(A, n, ncl, j0, k, p, pv[0], cur, ncol + (par ^ 1) * (size_t)n, pinv + (par ^ 1),
+                                  piv + (par ^ 1), wid, lane);
     }
     if (singular) {
         if (r == 0 && tid == 0) atomicOr(flags + 2, 1);
@@ -326,7 +338,7 @@ __global__ void __launch_bounds__(kGcTpb) gj_cluster_kernel(double *mats, int n,
     cl.sync();  // the last step is done in every CTA
     for (int jl = wid; jl < ncl; jl += kGcWarps) {
         const int w = where[j0 + jl];
-        const double *srcc = cl.map_shared_rank(A, w / nc) + (size_t)n * (w % nc);
+        const T *srcc = cl.map_shared_rank(A, w / nc) + (size_t)n * (w % nc);
         for (int i = lane; i < n; i += 32) Mg[(size_t)n * (j0 + jl) + i] = srcc[i];
     }
     cl.sync();  // every CTA has read the columns it needs
@@ -346,14 +358,14 @@ static int gj_rows_per_lane(int n)
     return n <= 32 ? 1 : n <= 64 ? 2 : n <= 128 ? 4 : n <= 256 ? 8 : 0;
 }
 
-template <int RPL>
-static gmi_status gj_launch(cudaStream_t stream, double *mats, int nmat, int n, int csize, int dev_max, int *flags)
+template <typename T, int RPL>
+static gmi_status gj_launch(cudaStream_t stream, T *mats, int nmat, int n, int csize, int dev_max, int *flags)
 {
     if (csize > 1) {
         const int nc = (n + csize - 1) / csize;
-        const size_t smem = ((size_t)n * nc + 3 * (size_t)n + 4) * sizeof(double) + (6 + (size_t)n) * sizeof(int);
+        const size_t smem = ((size_t)n * nc + 3 * (size_t)n + 4) * sizeof(T) + (6 + (size_t)n) * sizeof(int);
         if (smem <= (size_t)dev_max) {
-            const void *fn = reinterpret_cast<const void *>(&gj_cluster_kernel<RPL>);
+            const void *fn = reinterpret_cast<const void *>(&gj_cluster_kernel<T, RPL>);
             GMI_CUDA_TRY(raise_dynamic_smem_limit(fn, smem));
             cudaLaunchConfig_t cfg{};
             cudaLaunchAttribute attr[1];
@@ -367,33 +379,46 @@ static gmi_status gj_launch(cudaStream_t stream, double *mats, int nmat, int n, 
             cfg.stream = stream;
             cfg.attrs = attr;
             cfg.numAttrs = 1;
-            GMI_CUDA_TRY(cudaLaunchKernelEx(&cfg, gj_cluster_kernel<RPL>, mats, n, nc, flags));
+            GMI_CUDA_TRY(cudaLaunchKernelEx(&cfg, gj_cluster_kernel<T, RPL>, mats, n, nc, flags));
             return GMI_OK;
         }
     }
-    const size_t base = (2 * (size_t)n + 2) * sizeof(double) + (size_t)((n + 1) & ~1) * sizeof(int);
-    const size_t mat = (size_t)n * n * sizeof(double);
+    const size_t base = (2 * (size_t)n + 2) * sizeof(T) + (size_t)((n + 1) & ~1) * sizeof(int);
+    const size_t mat = (size_t)n * n * sizeof(T);
     const int use_smem = (base + mat <= (size_t)dev_max) ? 1 : 0;
     const size_t smem = use_smem ? base + mat : base;
-    GMI_CUDA_TRY(raise_dynamic_smem_limit(reinterpret_cast<const void *>(&gj_invert_kernel<RPL>), smem));
-    gj_invert_kernel<RPL><<<nmat, kGjTpb, smem, stream>>>(mats, n, use_smem, flags);
+    GMI_CUDA_TRY(raise_dynamic_smem_limit(reinterpret_cast<const void *>(&gj_invert_kernel<T, RPL>), smem));
+    gj_invert_kernel<T, RPL><<<nmat, kGjTpb, smem, stream>>>(mats, n, use_smem, flags);
     GMI_CUDA_TRY(cudaGetLastError());
     return GMI_OK;
 }
 
-gmi_status gj_invert(cudaStream_t stream, double *mats, int nmat, int n, int csize, bool registers, int device,
-                     int *flags)
+template <typename T>
+static gmi_status gj_invert_t(cudaStream_t stream, T *mats, int nmat, int n, int csize, bool registers, int device,
+                              int *flags)
 {
     if (nmat <= 0) return GMI_OK;
     int dev_max = 0;
     GMI_CUDA_TRY(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
     switch (registers ? gj_rows_per_lane(n) : 0) {
-    case 1: return gj_launch<1>(stream, mats, nmat, n, csize, dev_max, flags);
-    case 2: return gj_launch<2>(stream, mats, nmat, n, csize, dev_max, flags);
-    case 4: return gj_launch<4>(stream, mats, nmat, n, csize, dev_max, flags);
-    case 8: return gj_launch<8>(stream, mats, nmat, n, csize, dev_max, flags);
-    default: return gj_launch<0>(stream, mats, nmat, n, csize, dev_max, flags);
+    case 1: return gj_launch<T, 1>(stream, mats, nmat, n, csize, dev_max, flags);
+    case 2: return gj_launch<T, 2>(stream, mats, nmat, n, csize, dev_max, flags);
+    case 4: return gj_launch<T, 4>(stream, mats, nmat, n, csize, dev_max, flags);
+    case 8: return gj_launch<T, 8>(stream, mats, nmat, n, csize, dev_max, flags);
+    default: return gj_launch<T, 0>(stream, mats, nmat, n, csize, dev_max, flags);
     }
+}
+
+gmi_status gj_invert(cudaStream_t stream, double *mats, int nmat, int n, int csize, bool registers, int device,
+                     int *flags)
+{
+    return gj_invert_t(stream, mats, nmat, n, csize, registers, device, flags);
+}
+
+gmi_status gj_invert(cudaStream_t stream, float *mats, int nmat, int n, int csize, bool registers, int device,
+                     int *flags)
+{
+    return gj_invert_t(stream, mats, nmat, n, csize, registers, device, flags);
 }
 
 }  // namespace gmi

@@ -17,5 +17,8 @@ int gj_cluster_size(int nmat, int n, int sm_count);
 // arithmetic).  A zero pivot sets flags[2].
 gmi_status gj_invert(cudaStream_t stream, double *mats, int nmat, int n, int csize, bool registers, int device,
                      int *flags);
+// The same in FP32 (the mixed-precision time step's approximate inverse).
+gmi_status gj_invert(cudaStream_t stream, float *mats, int nmat, int n, int csize, bool registers, int device,
+                     int *flags);
 
 }  // namespace gmi

@@ -546,61 +546,58 @@ __device__ void lie_segment_blocks(const SimP &P, int fil, int nt, int k, double
 // The reference's block writes fall into disjoint regions (constraint
 // diagonal; position couplings, rows < 3NS; Lie-algebra rows >= 3NS, columns
 // < 3NS; the Lie-algebra block, one row band per segment), built in parallel
-// as tasks: grid (filament, split), the filament's 3NS-2 tasks dealt round-
-// robin to its gridDim.y CTAs and, within a CTA, to its warps, so the FP64
-// work spreads over the SM's schedulers and, with few filaments, over more
-// SMs.  The matrix is zeroed before the launch; the writes that depend on
-// earlier ones (end-force term, unit diagonal, clamping blocks) follow in
+// as 3NS - 1 tasks per filament: grid (filament blocks, task), one thread per
+// (filament, task), so the 32 lanes of a warp run the same task for 32
+// filaments.  Each task is a serial FP64 chain, and a warp FP64 instruction
+// costs the same on one lane as on 32: lanes of one task for many filaments
+// keep every lane busy and the warp on one code path (the reference's
+// boundary cases, segments 0 and NS-1, are whole tasks).  The matrix is
+// zeroed before the launch; the writes that depend on earlier ones
+// (end-force term, unit diagonal, clamping blocks) follow in
 // jacobian_finish_kernel.
 constexpr int kJacTpb = 128;
 
 __global__ void __launch_bounds__(kJacTpb) build_jacobian_kernel(SimP P, int nt)
 {
-    const int fil = blockIdx.x, tid = threadIdx.x, nsplit = gridDim.y, split = blockIdx.y;
+    const int fil = blockIdx.x * kJacTpb + threadIdx.x, task = blockIdx.y;
+    if (fil >= P.F) return;
     const int NS = P.NS, ld = P.n6, s0 = fil * NS;
     double *J = P.invJ + (size_t)fil * ld * ld;
     const bool euler = nt < P.neuler;
     const double fac0 = euler ? -P.DT / (6.0 * kPi * P.MU * P.RSEG) : -P.DT / (9.0 * kPi * P.MU * P.RSEG);
     const double fac1 = euler ? P.DL * P.DT / (16.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG)
                               : P.DL * P.DT / (24.0 * kPi * P.MU * P.RSEG * P.RSEG * P.RSEG);
-    if (split == 0)
-        for (int i = tid; i < 3 * NS; i += kJacTpb) {
+    // tasks: [0, NS-1) position columns j+1; [NS-1, 2NS-2) Lie-to-position
+    // rows for j+1; [2NS-2, 3NS-2) Lie-algebra segment k; 3NS-2 the
+    // constraint diagonal
+    double t[3];
+    if (task < NS - 1) {
+        const int j = task + 1, jpos = 3 * (NS + j);
+        q_tangent(ldq(P.q + 4 * (s0 + j)), t);
+        const M3 temp = m3_scale(rcross(t), P.DL);
+        put_block(J, ld, 3 * j, jpos, m3_scale(temp, 0.5));
+        for (int i = j + 1; i < NS; ++i) put_block(J, ld, 3 * i, jpos, temp);
+    } else if (task < 2 * NS - 2) {
+        const int j = task - (NS - 1) + 1, jpos = 3 * j;
+        int ipos = 3 * (NS + j - 1);
+        q_tangent(ldq(P.q + 4 * (s0 + j - 1)), t);
+        M3 um = rcross(P.u + 3 * (s0 + j - 1));
+        M3 tm = m3_scale(rcross(t), -1.0);
+        M3 blk =
+            m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
+        put_block(J, ld, ipos, jpos, m3_scale(blk, fac1));
+        ipos += 3;
+        q_tangent(ldq(P.q + 4 * (s0 + j)), t);
+        um = rcross(P.u + 3 * (s0 + j));
+        tm = m3_scale(rcross(t), -1.0);
+        blk = m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
+        put_block(J, ld, ipos, jpos, m3_scale(blk, fac1));
+    } else if (task < 3 * NS - 2) {
+        lie_segment_blocks(P, fil, nt, task - (2 * NS - 2), J, ld);
+    } else {
+        for (int i = 0; i < 3 * NS; ++i) {
             J[i + (size_t)ld * i] = fac0;
             if (i < 3 * NS - 3) J[i + (size_t)ld * (i + 3)] = -fac0;
-        }
-    // tasks: [0, NS-1) position columns j+1; [NS-1, 2NS-2) Lie-to-position
-    // rows for j+1; [2NS-2, 3NS-2) Lie-algebra segment k
-    const int ntask = 3 * NS - 2;
-    for (int task = split; task < ntask; task += nsplit) {
-        // the CTA's own tasks go to the warps round-robin: each task is a
-        // serial FP64 chain, so the chains of one CTA run on all four
-        // schedulers at once
-        const int lt = task / nsplit;
-        if (((lt % 4) * 32 + lt / 4) % kJacTpb != tid) continue;
-        double t[3];
-        if (task < NS - 1) {
-            const int j = task + 1, jpos = 3 * (NS + j);
-            q_tangent(ldq(P.q + 4 * (s0 + j)), t);
-            const M3 temp = m3_scale(rcross(t), P.DL);
-            put_block(J, ld, 3 * j, jpos, m3_scale(temp, 0.5));
-            for (int i = j + 1; i < NS; ++i) put_block(J, ld, 3 * i, jpos, temp);
-        } else if (task < 2 * NS - 2) {
-            const int j = task - (NS - 1) + 1, jpos = 3 * j;
-            int ipos = 3 * (NS + j - 1);
-            q_tangent(ldq(P.q + 4 * (s0 + j - 1)), t);
-            M3 um = rcross(P.u + 3 * (s0 + j - 1));
-            M3 tm = m3_scale(rcross(t), -1.0);
-            M3 blk =
-                m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
-            put_block(J, ld, ipos, jpos, m3_scale(blk, fac1));
-            ipos += 3;
-            q_tangent(ldq(P.q + 4 * (s0 + j)), t);
-            um = rcross(P.u + 3 * (s0 + j));
-            tm = m3_scale(rcross(t), -1.0);
-            blk = m3_add(m3_add(tm, m3_scale(m3_mul(um, tm), 0.5)), m3_scale(m3_mul(m3_mul(um, um), tm), 1.0 / 12.0));
-            put_block(J, ld, ipos, jpos, m3_scale(blk, fac1));
-        } else {
-            lie_segment_blocks(P, fil, nt, task - (2 * NS - 2), J, ld);
         }
     }
 }
@@ -1343,6 +1340,8 @@ struct gmi_sim {
     int broyden_iter = 0;
     bool use_gj_cluster = true;   // GMI_GJ_CLUSTER=0: one CTA per Jacobian inversion always
     bool use_gj_registers = true;  // GMI_GJ_REGISTERS=0: the columns stepped through shared memory
+    bool gj_fp32 = false;          // FP32C steps: the approximate Jacobians inverted in FP32 (GMI_GJ_FP32=0: FP64)
+    float *invJ32 = nullptr;       // their FP32 copy
     // learned initial inverse Jacobian (gmi_sim_set_learned_jacobian)
     const gmi_mlp *mlp = nullptr;
     int rank = 0;
@@ -1444,19 +1443,42 @@ static gmi_status velocities_and_errors(gmi_sim *m, int nt, double *err_out, boo
     return GMI_OK;
 }
 
+// FP64 <-> FP32 copies of the Jacobians (grid-stride)
+__global__ void narrow_kernel(size_t n, const double *__restrict__ in, float *__restrict__ out)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+__global__ void widen_kernel(size_t n, const float *__restrict__ in, double *__restrict__ out)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+
 static gmi_status prepare_jacobian_inv(gmi_sim *m, int nt)
 {
     const SimP &P = m->P;
-    // the tasks of few filaments spread over several CTAs each (enough CTAs
-    // for about two per SM, at most 8 per filament)
-    const int sms = m->solver->ctx->sm_count;
-    const int nsplit = std::max(1, std::min(8, (2 * sms + P.F - 1) / std::max(P.F, 1)));
     GMI_CUDA_TRY(cudaMemsetAsync(P.invJ, 0, (size_t)P.F * P.n6 * P.n6 * sizeof(double), sst(m)));
-    build_jacobian_kernel<<<dim3(P.F, nsplit), kJacTpb, 0, sst(m)>>>(P, nt);
+    build_jacobian_kernel<<<dim3((P.F + kJacTpb - 1) / kJacTpb, 3 * P.NS - 1), kJacTpb, 0, sst(m)>>>(P, nt);
     jacobian_finish_kernel<<<P.F, kJacTpb, 0, sst(m)>>>(P, nt);
     // few filaments: each inversion spread over a cluster of CTAs
     const int csize = m->use_gj_cluster ? gj_cluster_size(P.F, P.n6, m->solver->ctx->sm_count) : 1;
-    GMI_TRY(gj_invert(sst(m), P.invJ, P.F, P.n6, csize, m->use_gj_registers, m->solver->ctx->device, P.flags));
+    const size_t jn = (size_t)P.F * P.n6 * P.n6;
+    if (m->gj_fp32) {
+        // the mixed-precision step: the approximate inverse in FP32, widened
+        if (!m->invJ32) {
+            GMI_CUDA_TRY(dev_malloc(reinterpret_cast<void **>(&m->invJ32), jn * sizeof(float)));
+            m->allocs.push_back(m->invJ32);
+        }
+        const unsigned g = (unsigned)std::min<size_t>((jn + 255) / 256, 65535u * 8u);
+        narrow_kernel<<<g, 256, 0, sst(m)>>>(jn, P.invJ, m->invJ32);
+        GMI_TRY(gj_invert(sst(m), m->invJ32, P.F, P.n6, csize, m->use_gj_registers, m->solver->ctx->device,
+                          P.flags));
+        widen_kernel<<<g, 256, 0, sst(m)>>>(jn, m->invJ32, P.invJ);
+        GMI_TRY(sim_launched(m, 2));
+    } else {
+        GMI_TRY(gj_invert(sst(m), P.invJ, P.F, P.n6, csize, m->use_gj_registers, m->solver->ctx->device, P.flags));
+    }
     if (!P.wall) {  // the body coupling (swimmer.cpp:466-682); none on the wall
         filament_B_kernel<<<P.F, 128, (6 * (size_t)P.n6 + 36 * (size_t)P.NS + 36 + 27 + 36) * sizeof(double),
                             sst(m)>>>(P, nt);
@@ -1705,6 +1727,8 @@ gmi_status gmi_sim_create(const gmi_sim_config *cfg, const double *blob_refs, co
         m->use_gj_cluster = !(gj && gj[0] == '0');
         const char *gr = std::getenv("GMI_GJ_REGISTERS");
         m->use_gj_registers = !(gr && gr[0] == '0');
+        const char *gf = std::getenv("GMI_GJ_FP32");
+        m->gj_fp32 = cfg->mobility.precision == GMI_FP32C && !(gf && gf[0] == '0');
     }
     SIM_ARG_CHECK(m != nullptr, "gmi_sim_create: out of host memory");
     m->cfg = *cfg;

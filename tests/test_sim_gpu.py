@@ -83,6 +83,31 @@ def test_jacobian_inverse_paths_agree(gmi_lib, monkeypatch):
         assert rel_err(out[mode][2].ravel(), out["one-cta"][2].ravel()) < 1e-9, mode
 
 
+def test_fp32_jacobian_inverse_in_mixed_precision(gmi_lib, monkeypatch):
+    """Mixed-precision (FP32C) steps invert the approximate Jacobians in FP32
+    by default (GMI_GJ_FP32=0: FP64).  The inverse only starts each Broyden
+    iteration, so both take the same Broyden iterations (to one per step) and
+    end at the same state to the Broyden tolerance; with one CTA per matrix
+    and with clusters."""
+    from generic_mobility_interface_class_gb300.sim import Simulation
+    g = load_golden("small_swimmer", prefix="sim_")
+    out = {}
+    for gj in ("0", "1"):
+        for cluster in ("0", "1"):
+            monkeypatch.setenv("GMI_GJ_FP32", gj)
+            monkeypatch.setenv("GMI_GJ_CLUSTER", cluster)
+            sim = Simulation.from_golden(g, precision=1)
+            sim.prepare()
+            iters = [sim.step(nt)[0] for nt in range(6)]
+            out[gj, cluster] = (iters, sim.state("seg_q").copy(), sim.state("seg_v").copy())
+            sim.close()
+    ref = out["0", "0"]
+    for key, (iters, q, v) in out.items():
+        assert all(abs(a - b) <= 1 for a, b in zip(iters, ref[0])), (key, iters, ref[0])
+        assert rel_err(q.ravel(), ref[1].ravel()) < 1e-6, key
+        assert rel_err(v.ravel(), ref[2].ravel()) < 1e-4, key
+
+
 def test_trajectory_matches_reference(gmi_lib):
     """12 steps of a 4-filament swimmer, every step compared."""
     run_against_golden("small_swimmer", TRAJ_TOL, VEL_TOL)
