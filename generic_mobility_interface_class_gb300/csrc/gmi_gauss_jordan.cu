@@ -136,11 +136,34 @@ static __device__ __forceinline__ void gj_cols(T *A, int n, int j0, const int (&
         }
         const T akj = __shfl_sync(0xffffffffu, sp, pl);  // row p, swapped into row k
         const T apj = __shfl_sync(0xffffffffu, sk, kl);  // row k, swapped into row p
+        if constexpr (sizeof(T) == 8) {
+            // FP64: the FP64 pipe bounds the step, so rows k and p are
+            // selected inside the one FMA per row (the selects are free)
 #pragma unroll
-        for (int t = 0; t < RPL; ++t) {
-            const int i = lane + 32 * t;
-            const T a = (i == k) ? T(0) : ((i == p) ? apj : v[c][t]);
-            v[c][t] = gj_fma(akj, (i == k) ? pivinv : ncr[t], a);
+            for (int t = 0; t < RPL; ++t) {
+                const int i = lane + 32 * t;
+                const T a = (i == k) ? T(0) : ((i == p) ? apj : v[c][t]);
+                v[c][t] = gj_fma(akj, (i == k) ? pivinv : ncr[t], a);
+            }
+        } else {
+            // FP32: the per-row selects, not the FMAs, bound the step (ALU
+            // pipe 86 % busy, FMA pipe 7 %), so every row takes one FMA as if
+            // it were neither k nor p, and the lanes that hold rows p and k
+            // redo theirs: row p from the old row k, row k as akj / pivot (a
+            // zero addend; when p == k the second fix wins, as in the
+            // swap-free case).  1.77 -> 1.57 ms for config 3's 640 matrices.
+#pragma unroll
+            for (int t = 0; t < RPL; ++t) v[c][t] = gj_fma(akj, ncr[t], v[c][t]);
+            if (lane == pl) {
+#pragma unroll
+                for (int t = 0; t < RPL; ++t)
+                    if (t == pq) v[c][t] = gj_fma(akj, ncr[t], apj);
+            }
+            if (lane == kl) {
+#pragma unroll
+                for (int t = 0; t < RPL; ++t)
+                    if (t == kq) v[c][t] = gj_fma(akj, pivinv, T(0));
+            }
         }
     }
 #pragma unroll

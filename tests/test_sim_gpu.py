@@ -87,8 +87,9 @@ def test_fp32_jacobian_inverse_in_mixed_precision(gmi_lib, monkeypatch):
     """Mixed-precision (FP32C) steps invert the approximate Jacobians in FP32
     by default (GMI_GJ_FP32=0: FP64).  The inverse only starts each Broyden
     iteration, so both take the same Broyden iterations (to one per step) and
-    end at the same state to the Broyden tolerance; with one CTA per matrix
-    and with clusters."""
+    end at the same state to the Broyden tolerance: two runs that each stop
+    at a residual of 1e-4 differ in the velocities by up to a few times that
+    (3e-4 here, max-normalised); with one CTA per matrix and with clusters."""
     from generic_mobility_interface_class_gb300.sim import Simulation
     g = load_golden("small_swimmer", prefix="sim_")
     out = {}
@@ -105,7 +106,7 @@ def test_fp32_jacobian_inverse_in_mixed_precision(gmi_lib, monkeypatch):
     for key, (iters, q, v) in out.items():
         assert all(abs(a - b) <= 1 for a, b in zip(iters, ref[0])), (key, iters, ref[0])
         assert rel_err(q.ravel(), ref[1].ravel()) < 1e-6, key
-        assert rel_err(v.ravel(), ref[2].ravel()) < 1e-4, key
+        assert rel_err(v.ravel(), ref[2].ravel()) < 3e-4, key
 
 
 def test_trajectory_matches_reference(gmi_lib):
