@@ -1219,28 +1219,23 @@ __global__ void __launch_bounds__(kCellTpb) barrier_cell_kernel(BarrierLaunch a,
     barrier_cutoffs(a, t.seg, c2_s, c2_b);
     const float inv_h = cell_inv_width(c);
     const int cx = cell_coord(pf.x, inv_h), cy = cell_coord(pf.y, inv_h), cz = cell_coord(pf.z, inv_h);
-    // the 27 buckets' ranges first, all loads in flight at once (a chain of
-    // 27 dependent L2 round trips otherwise)
-    int beg[27], end[27];
-#pragma unroll
-    for (int q = 0; q < 27; ++q) {
-        const int b = cell_bucket(cx + q % 3 - 1, cy + (q / 3) % 3 - 1, cz + q / 9 - 1, c.T);
-        beg[q] = cell_offset(c, b);
-        end[q] = b + 1 < c.T ? cell_offset(c, b + 1) : N;
-    }
     int n = 0;
     bool over = false;
-#pragma unroll
-    for (int q = 0; q < 27; ++q)
-        for (int p = beg[q]; p < end[q]; ++p) {
-            const int j = __ldcg(c.order + p);
-            if (!barrier_candidate(a, t, pf, c2_s, c2_b, j, a.screen[j])) continue;
-            if (n < kCellCand)
-                cand[n * kCellTpb + threadIdx.x] = j;
-            else
-                over = true;
-            ++n;
-        }
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int b = cell_bucket(cx + dx, cy + dy, cz + dz, c.T);
+                const int beg = cell_offset(c, b), end = b + 1 < c.T ? cell_offset(c, b + 1) : N;
+                for (int p = beg; p < end; ++p) {
+                    const int j = __ldcg(c.order + p);
+                    if (!barrier_candidate(a, t, pf, c2_s, c2_b, j, a.screen[j])) continue;
+                    if (n < kCellCand)
+                        cand[n * kCellTpb + threadIdx.x] = j;
+                    else
+                        over = true;
+                    ++n;
+                }
+            }
     if (over) {
         const int pos = atomicAdd(c.overflow, 1);
         c.overflow[1 + pos] = local;
@@ -1953,6 +1948,7 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     const size_t per_split = (size_t)n_tgt * nout * sizeof(double);
     const int max_by_scratch = env.partial_bytes / per_split > 0 ? (int)(env.partial_bytes / per_split) : 1;
     if (splits > max_by_scratch) splits = max_by_scratch;
+    if (env.max_splits > 0 && splits > env.max_splits) splits = env.max_splits;
     if (splits < 1) splits = 1;
     int chunk = (n_src + splits - 1) / splits;
     chunk = (chunk + kTile - 1) / kTile * kTile;

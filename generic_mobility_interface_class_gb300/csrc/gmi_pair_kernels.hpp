@@ -23,6 +23,7 @@ struct PairLaunch {
     unsigned *err;
     const int *skip;      // if non-null and *skip != 0 the launch does nothing (converged GMRES)
     unsigned long long wait_ns;  // deadline of the source-tile waits (0: kWaitDeadlineNs)
+    int max_splits;              // cap on the source splits (0: none beyond the automatic choice)
 };
 
 struct BarrierLaunch {
@@ -86,6 +87,7 @@ struct ExplicitPairEnv {
     int pdl;               // non-zero: launch for programmatic dependent launch (the pair kernel
                            // waits for the previous kernel in pdl_wait_then_release)
     unsigned long long wait_ns;  // deadline of the source-tile waits (0: kWaitDeadlineNs)
+    int max_splits;              // cap on the source splits (0: none beyond the automatic choice)
 };
 
 size_t record_bytes(bool f64);

@@ -14,6 +14,7 @@
 // S = nswim*nfil*nseg segments, B = nswim*nblob blobs, W = nswim.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -1284,12 +1285,23 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
         env.tpb = kPairWarpShapeTpb;  // warp per two target blobs
         env.tt = 2;
     } else {
-        // FP32: the packed kernel, 128 targets per CTA (at 4096 blobs, with
-        // 32 source splits of one tile each, 22 us against 24.5 us for 64);
-        // FP64: smaller CTAs for small target sets
+        // FP32: the packed kernel, 64 targets per CTA with one source tile
+        // per split (at 4096 blobs, in the time step: config 3 steps 0.6-1.1
+        // ms faster than with 128, every step; 128 had been faster with the
+        // kernels timed one at a time under a profiler); FP64: smaller CTAs
+        // for small target sets
         const bool small = (long long)nb * 2 < (long long)ctx->sm_count * 256;
-        env.tpb = (small && f64) ? 64 : 128;
+        env.tpb = (small || !f64) ? 64 : 128;
         env.tt = (small || !f64) ? 1 : 2;
+    }
+    // GMI_GM_PAIR="tpb,tt,splits" overrides the shape (0 keeps a field's choice)
+    if (const char *gs = std::getenv("GMI_GM_PAIR")) {
+        int a = 0, b = 0, c = 0;
+        if (std::sscanf(gs, "%d,%d,%d", &a, &b, &c) == 3) {
+            if (a > 0) env.tpb = a;
+            if (b > 0) env.tt = b;
+            env.max_splits = c > 0 ? c : 0;
+        }
     }
     env.skip = &s->ctl->done;
     env.pdl = pdl ? 1 : 0;
