@@ -540,9 +540,14 @@ __global__ void __launch_bounds__(TPB) rpy_pair2_kernel(const __grid_constant__ 
     constexpr int NOUT = KindTraits<KIND>::nout;
     constexpr int kStageScalars = kTile * kRecLen;
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    // a launch whose splits are one tile each (chunk <= kTile) uses ring
+    // stage 0 and interleave buffer 0 only, and the launcher allocates just
+    // those (half the shared memory: twice the CTAs per SM)
+    const bool single = args.chunk <= kTile;
     float *ring = reinterpret_cast<float *>(smem_raw);
-    float4 *ibuf = reinterpret_cast<float4 *>(smem_raw + kStagesP * kStageScalars * sizeof(float));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + (kStagesP + 2) * kStageScalars * sizeof(float));
+    float4 *ibuf = reinterpret_cast<float4 *>(smem_raw + (single ? 1 : kStagesP) * kStageScalars * sizeof(float));
+    uint64_t *bars =
+        reinterpret_cast<uint64_t *>(smem_raw + (single ? 2 : kStagesP + 2) * kStageScalars * sizeof(float));
 
     pdl_wait();
     if (args.skip != nullptr && *args.skip != 0) return;
@@ -1539,6 +1544,10 @@ static size_t ring_bytes(bool f64, bool packed)
     return (size_t)kStages * kTile * kRecLen * (f64 ? 8 : 4) + kStages * 8;
 }
 
+// the packed kernel's shared memory when every split is one tile: ring
+// stage 0, interleave buffer 0 and the barriers (rpy_pair2_kernel)
+static size_t ring_bytes_single_tile() { return (size_t)2 * kTile * kRecLen * sizeof(float) + kStagesP * 8; }
+
 static int nout_of(int kind) { return (kind == kBB || kind == kBS) ? 3 : 6; }
 
 // Source splits: enough CTAs for ~2 full waves when the target tiles alone
@@ -1714,7 +1723,8 @@ gmi_status launch_pair(gmi_context *ctx, int kind, const void *tgt_rec, int tgt_
     if (st != GMI_OK) return st;
     void *params[] = {&map, &a};
     dim3 grid(n_tgt_ctas, splits);
-    GMI_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(tpb), params, smem, ctx->stream));
+    const size_t smem_run = (kShapes[sidx].packed != 0 && chunk <= kTile) ? ring_bytes_single_tile() : smem;
+    GMI_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(tpb), params, smem_run, ctx->stream));
     ctx->launches++;
     if (splits > 1) {
         const int count = n_tgt * nout;
@@ -1971,7 +1981,8 @@ gmi_status launch_pair_into(const ExplicitPairEnv &env, int kind, bool f64, cons
     gmi_status st = encode_record_map(env.encode_tiled, &map, src_rec, n_src, f64);
     if (st != GMI_OK) return st;
     void *params[] = {&map, &a};
-    GMI_CUDA_TRY(launch_fn(fn, dim3(n_tgt_ctas, splits), dim3(tpb), params, smem, env.stream, env.pdl != 0));
+    const size_t smem_run = (kShapes[sidx].packed != 0 && chunk <= kTile) ? ring_bytes_single_tile() : smem;
+    GMI_CUDA_TRY(launch_fn(fn, dim3(n_tgt_ctas, splits), dim3(tpb), params, smem_run, env.stream, env.pdl != 0));
     if (env.splits_out) {
         *env.splits_out = splits;
         return GMI_OK;

@@ -206,13 +206,14 @@ def own_ctx(gmi_lib):
     ctx.close()
 
 
-@pytest.mark.parametrize("splits", [0, 3])
+@pytest.mark.parametrize("splits", [0, 3, 9])
 @pytest.mark.parametrize("per_step,tpb,tt", [(1, *s) for s in TILED_SHAPES] + [(2, *s) for s in PACKED_SHAPES])
 def test_every_tiled_shape_against_oracle(own_ctx, oracle_built, per_step, tpb, tt, splits):
     """Every entry of the tiled-kernel table, scalar (one source per thread
     step) and packed (two sources per f32x2 step), pinned with set_shape, on
     an odd source count (a ragged last tile whose last source has no
-    partner) and with forced source splits: all four free-space kinds
+    partner) and with forced source splits (9: one tile per split, where the
+    packed kernel runs in half its shared memory): all four free-space kinds
     against the FP64 oracle at the FP32C bound."""
     from generic_mobility_interface_class_gb300 import seeding
     rpy = oracle_built
