@@ -88,6 +88,64 @@ def test_prescribed_dynamic_solves_match_reference(gmi_lib, precision):
     s.close()
 
 
+def _two_swimmers(g, k, phase_shift=0.7):
+    """The golden swimmer of step k and a copy 3 (R + L) further along x (the
+    reference's spacing of swimmers, rigid_body.cpp), its phases shifted."""
+    nfil, nseg = int(g["nfil"]), int(g["nseg"])
+    L = 2.2 * float(g["rseg"]) * nseg
+    R = np.linalg.norm(g["blob_refs"], axis=1).max()
+    shift = np.array([3.0 * (R + L), 0.0, 0.0])
+    xs0 = g["x_segs"][k].reshape(-1, 3)
+    return dict(xs=np.concatenate([xs0, xs0 + shift]),
+                bx=np.stack([g["body_x"][k], g["body_x"][k] + shift]),
+                bq=np.stack([g["body_q"][k], g["body_q"][k]]),
+                vd=np.concatenate([g["vel_dir"][k], g["vel_dir"][k]]).reshape(-1, 3),
+                phase=np.concatenate([g["phase"][k], g["phase"][k] + phase_shift]),
+                omega0=np.concatenate([g["omega0"][k], g["omega0"][k]]), nfil=nfil, nseg=nseg)
+
+
+def test_prescribed_dynamic_two_swimmers_against_oracle(gmi_lib, oracle_built):
+    """Two swimmers with the phase speeds solved for: the golden geometry and
+    a copy 3 (R + L) away with its phases shifted.  The solution satisfies
+    the restated system (oracle/mobility_dense.py prescribed_system, pinned
+    to the reference's own solutions) to the GMRES tolerance, and matches
+    its dense solve.  With several swimmers the reference's preconditioner
+    treats the phase rows differently (its block operations over all
+    swimmers' phase rows sit inside the loop over swimmers); the system and
+    its solution are the same."""
+    from generic_mobility_interface_class_gb300.solver import MobilitySolver
+    from oracle import mobility_dense as md
+    g = load_golden("prescribed_dynamic", prefix="")
+    t = _two_swimmers(g, 0)
+    nfil, nseg, nblob = t["nfil"], t["nseg"], int(g["nblob"])
+    rseg, rblob, mu = float(g["rseg"]), float(g["rblob"]), float(g["mu"])
+    s = MobilitySolver(nswim=2, nfil=nfil, nseg=nseg, nblob=nblob, mu=mu, rseg=rseg, rblob=rblob,
+                       linear_tol=1e-10, max_linear_iter=150)
+    s.set_blob_references(g["blob_refs"])
+    s.set_generalised_force_refs(g["gen_force_refs"])
+    s.x_segs_host[:] = t["xs"]
+    it, speeds = s.compute_velocities_prescribed_dynamic(t["vd"], t["phase"], t["omega0"], body_x=t["bx"],
+                                                         body_q=t["bq"])
+    x = np.concatenate([np.array(s.f_segs_host[:, :3]).ravel(), np.array(s.f_blobs_host).ravel(),
+                        s.v_bodies().ravel(), speeds])
+    s.close()
+    args = (t["xs"], t["bx"], t["bq"], g["blob_refs"], t["vd"], nfil, nseg, rseg, rblob, mu)
+    kw = dict(table=g["gen_force_refs"], phase=t["phase"], omega0=t["omega0"])
+    Ax, b = md.prescribed_system(x, *args, **kw)
+    assert np.linalg.norm(Ax - b) / np.linalg.norm(b) < 1e-9, it
+    n = len(x)
+    A = np.zeros((n, n))
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        A[:, j] = md.prescribed_system(e, *args, **kw)[0]
+    xd = np.linalg.solve(A, b)
+    assert rel_err(x, xd) < 1e-6
+    assert rel_err(speeds, xd[-2 * nfil:]) < 1e-7
+    # the two swimmers' phase speeds differ (their phases do)
+    assert np.abs(speeds[:nfil] - speeds[nfil:]).max() > 1e-3
+
+
 def test_prescribed_dynamic_needs_a_table(gmi_lib):
     from generic_mobility_interface_class_gb300._lib import GmiError
     from generic_mobility_interface_class_gb300.solver import MobilitySolver
