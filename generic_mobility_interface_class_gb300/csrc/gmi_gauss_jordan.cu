@@ -151,7 +151,7 @@ static __device__ __forceinline__ void gj_cols(T *A, int n, int j0, const int (&
             // it were neither k nor p, and the lanes that hold rows p and k
             // redo theirs: row p from the old row k, row k as akj / pivot (a
             // zero addend; when p == k the second fix wins, as in the
-            // swap-free case).  1.77 -> 1.57 ms for config 3's 640 matrices.
+            // swap-free case).  1.77 -> 1.57 ms for 640 matrices of 120 x 120.
 #pragma unroll
             for (int t = 0; t < RPL; ++t) v[c][t] = gj_fma(akj, ncr[t], v[c][t]);
             if (lane == pl) {

@@ -1286,10 +1286,10 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
         env.tt = 2;
     } else {
         // FP32: the packed kernel, 64 targets per CTA with one source tile
-        // per split (at 4096 blobs, in the time step: config 3 steps 0.6-1.1
-        // ms faster than with 128, every step; 128 had been faster with the
-        // kernels timed one at a time under a profiler); FP64: smaller CTAs
-        // for small target sets
+        // per split (at 4096 blobs, in the time step of a 16,896-particle
+        // swimmer: steps 0.6-1.1 ms faster than with 128, every step; 128 had
+        // been faster with the kernels timed one at a time under a profiler);
+        // FP64: smaller CTAs for small target sets
         const bool small = (long long)nb * 2 < (long long)ctx->sm_count * 256;
         env.tpb = (small || !f64) ? 64 : 128;
         env.tt = (small || !f64) ? 1 : 2;
@@ -1322,9 +1322,9 @@ static gmi_status enqueue_arnoldi_step(gmi_solver *s, cudaGraphConditionalHandle
     return GMI_OK;
 }
 
-// Arnoldi steps per pass of the device-side loop: 4 by default (config 3
-// FP32C 30.5 -> 30.0 ms and config 1 FP64 27.9 -> 27.0 ms per step against
-// one), GMI_GMRES_UNROLL (1..8) overrides.
+// Arnoldi steps per pass of the device-side loop: 4 by default (against
+// one: FP32C steps of a 16,896-particle swimmer 30.5 -> 30.0 ms, FP64 steps
+// of a 962-particle one 27.9 -> 27.0 ms), GMI_GMRES_UNROLL (1..8) overrides.
 static int gmres_loop_unroll()
 {
     const char *e = std::getenv("GMI_GMRES_UNROLL");
