@@ -52,7 +52,8 @@ FLOP_PER_PAIR_SS = 87  # canonical algorithmic FLOPs per segment-segment pair (F
 # benchmark with the shape pinned: (n, precision, threads, targets, splits,
 # sources per step) -> bytes.  Beyond the records (48 B per particle read) and
 # V (48 B written), the traffic is the FP64 split partial sums.
-PAIR_KERNEL_TRAFFIC = {(131072, "fp32c", 256, 1, 8, 2): 7976192, (131072, "fp32c", 64, 1, 4, 2): 7011584}
+PAIR_KERNEL_TRAFFIC = {(131072, "fp32c", 256, 1, 8, 2): 7976192, (131072, "fp32c", 64, 1, 4, 2): 7011584,
+                       (131072, "fp32c", 64, 1, 8, 2): 8071168}
 METRIC = "RPY pair-interactions/sec"
 
 
