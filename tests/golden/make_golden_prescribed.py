@@ -32,7 +32,8 @@ from oracle.ref_solver import build_ref_solver as brs  # noqa: E402
 PER_FILAMENT = ("vel_dir", "phase_speed", "phase", "omega0", "phase_speed_out")
 
 
-def main(case: str = "prescribed"):
+def collect(case: str = "prescribed") -> dict:
+    """Run the case and return the fixture's arrays (main saves them)."""
     path = brs.run_prescribed_dump(case)
     spec = dict(brs.COMMON)
     spec.update({k: v for k, v in brs.CASES[case].items() if k.isupper()})
@@ -72,6 +73,11 @@ def main(case: str = "prescribed"):
                     phase=np.stack([np.concatenate(s["phase"]) for s in steps]),
                     omega0=np.stack([np.concatenate(s["omega0"]) for s in steps]),
                     phase_speed_out=np.stack([np.concatenate(s["phase_speed_out"]) for s in steps]))
+    return data
+
+
+def main(case: str = "prescribed"):
+    data = collect(case)
     np.savez_compressed(os.path.join(HERE, f"{case}.npz"), **data)
     print({k: np.shape(v) for k, v in data.items() if np.ndim(v)})
 

@@ -4,10 +4,13 @@ Two pins: the committed golden fixtures (made by tests/golden/make_golden.py
 from cuda_functions.cu compiled for the CPU), and, where the reference tree
 is present, fresh random inputs run through the reference kernels directly.
 """
+import os
+import sys
+
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden, rel_err
+from conftest import ROOT, golden_cases, load_golden, rel_err
 
 FREE = [c for c in golden_cases() if not c.startswith("wall")]
 WALL = [c for c in golden_cases() if c.startswith("wall")]
@@ -161,3 +164,23 @@ def test_generalised_force_interpolation_edges():
     # the last interval runs back to sample 0
     assert min(table[-1], table[0]) - 1e-3 <= generalised_force(table, [2 * np.pi - 1e-9])[0] <= \
         max(table[-1], table[0]) + 1e-3
+
+
+@pytest.mark.parametrize("case", ["prescribed", "prescribed_dynamic"])
+def test_prescribed_fixtures_regenerate_from_the_reference(case):
+    """tests/golden/<case>.npz is what the reference's own builds produce:
+    its CILIA_TYPE 3 simulator driven by oracle/ref_solver/prescribed_dump.cpp
+    (and, for the solved phase speeds, the generalised-force table its own
+    WRITE_GENERALISED_FORCES run writes), rebuilt and rerun here; every array
+    matches the committed fixture exactly.  Skipped without the reference
+    tree."""
+    from oracle import reference_dir
+    if not os.path.isfile(os.path.join(reference_dir(), "mobility_solver.cpp")):
+        pytest.skip("reference tree not present")
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_golden_prescribed as mg
+    fresh = mg.collect(case)
+    want = load_golden(case, prefix="")
+    assert sorted(fresh) == sorted(want)
+    for k in want:
+        assert np.array_equal(np.asarray(fresh[k]), want[k]), k
