@@ -35,7 +35,9 @@ def parse_dat(path, skip_cols=1):
     return np.stack(rows)
 
 
-def main(case, restart_steps=0):
+def collect(case, restart_steps=0):
+    """Run the case (and the restart) and return (fixture name, arrays); main
+    saves them."""
     if restart_steps:
         first, rundir = brs.run_restart(case, restart_steps)
     else:
@@ -125,6 +127,11 @@ def main(case, restart_steps=0):
         data["backup_in"] = np.array(tok[1:], dtype=np.float64)
         data["steps"] = keep + int(tok[0])
         name += "_restart"
+    return name, data
+
+
+def main(case, restart_steps=0):
+    name, data = collect(case, restart_steps)
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **data)
     print(case, {k: np.shape(v) for k, v in data.items() if np.ndim(v)})
 

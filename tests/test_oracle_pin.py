@@ -184,3 +184,22 @@ def test_prescribed_fixtures_regenerate_from_the_reference(case):
     assert sorted(fresh) == sorted(want)
     for k in want:
         assert np.array_equal(np.asarray(fresh[k]), want[k]), k
+
+
+@pytest.mark.parametrize("case", ["small_swimmer", "two_swimmers", "wall_filaments"])
+def test_trajectory_fixtures_regenerate_from_the_reference(case):
+    """tests/golden/sim_<case>.npz is the reference's own simulator,
+    rebuilt from its unmodified sources and rerun here
+    (tests/golden/make_golden_sim.py): every committed array matches the
+    fresh run exactly.  (The generator has since added a few scalar keys the
+    older fixtures do not carry.)  Skipped without the reference tree."""
+    from oracle import reference_dir
+    if not os.path.isfile(os.path.join(reference_dir(), "mobility_solver.cpp")):
+        pytest.skip("reference tree not present")
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import make_golden_sim as mg
+    name, fresh = mg.collect(case)
+    want = load_golden(name, prefix="")
+    assert set(want) <= set(fresh)
+    for k in want:
+        assert np.array_equal(np.asarray(fresh[k]), want[k]), k
